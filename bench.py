@@ -1,0 +1,349 @@
+"""Benchmark: PD-IPC cloth steps/s on GB300 (512x512 cloth onto an icosphere).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision fp32|fp64|mixed] [--config c1|c0]
+
+One step = PdIpcSimulator::run(frame) on the 512x512 workload: prediction,
+outer CCD iterations (each 20 local-global iterations of 15 Chebyshev-Jacobi
+R2 sweeps, CCD, contact), velocity update.  `value` is device time from CUDA
+events recorded on the library's own stream around every step (L2 flushed
+between steps); `e2e` is wall time of BaseSimulator::animate (step + postRun
+copy of all positions to host memory) through the C ABI.  With torchrun
+(N > 1) every rank steps an independent replica on its own GPU (the path does
+not shard: "replicas only"); the value is all replicas' steps over the slowest
+rank's time.
+
+--impl reference times the CPU restatement of the reference algorithm (the
+reference has no CPU path and cannot be built here) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "pd-ipc-armadillodemo_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "512x512 cloth PD-IPC steps/sec: mixed/batched vs plain GPU vs CPU at <=1e-4 m err"
+UNIT = "steps/s"
+
+
+def workload(name: str):
+    from pdipc import scenes
+    if name == "c1":
+        return scenes.config1(seed=0)
+    if name == "c0":
+        return scenes.config0(seed=0)
+    raise ValueError(name)
+
+
+def workload_desc(sc, prec: str) -> str:
+    c = sc.cloths[0]
+    s = sc.statics[0]
+    n = int(round(c.X.shape[0] ** 0.5))
+    return (f"{n}x{n} cloth ({c.X.shape[0]} v / {c.F.shape[0]} f, 1 m, alternating diagonals, +/-1e-4 m jitter, "
+            f"seed 0, 2 corners pinned) onto a fixed icosphere ({s.X.shape[0]} v / {s.F.shape[0]} f, r 0.3 m, "
+            f"0.5 m below); dt 1/240 s, {sc.lg_iterations} PD iterations x 15 Chebyshev-Jacobi R2 sweeps, "
+            f"dhat {sc.dhat:g} m, kappa {sc.kappa:g}; {prec}")
+
+
+# ---------------------------------------------------------------------------- distributed
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws: int, backend: str):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(dist, value: float, device=None) -> float:
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist, device=None):
+    if dist is None:
+        return
+    if device is not None:
+        dist.barrier(device_ids=[device.index])
+    else:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------- helpers
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(prec: str):
+    """DRAM bytes per sweep launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", f"sweep_c1_{prec}.md")
+    try:
+        for ln in open(p):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_reference_sample(scene, prec: str, outer_sample: int, outer_per_step: float, threads: int):
+    """Oracle (the reference's R2 algorithm restated on the CPU) on a bounded
+    sample: one step limited to `outer_sample` outer iterations, scaled to the
+    outer iterations a full step runs."""
+    from oracle.oracle import FORM_R2, Oracle
+    t0 = time.perf_counter()
+    orc = Oracle(scene, prec, FORM_R2, threads=threads, fixed_outer=outer_sample)
+    t_init = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    orc.step(1)
+    t_step = time.perf_counter() - t0
+    st = orc.stats()
+    per_outer = t_step / outer_sample
+    sec_per_step = per_outer * outer_per_step
+    return {"value": 1.0 / sec_per_step, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"step 0 of the same workload with {outer_sample} outer iterations "
+                       f"({t_step:.1f} s, residual after them {st['last_residual']:.2e} > tol), scaled to "
+                       f"{outer_per_step:.1f} outer iterations per step as run by the GPU; "
+                       f"reference R2-operator form, {prec}, {threads} threads; init {t_init:.1f} s untimed"),
+            "seconds_per_outer_iteration": per_outer}
+
+
+# ---------------------------------------------------------------------------- arms
+def run_ours(args):
+    import torch
+    import pdipc
+
+    ws, rank, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dist = init_dist(ws, "nccl")
+    sc = workload(args.config)
+    sim = pdipc.Simulator(sc, args.precision, device=local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    sim.step(args.warmup)                    # captures the graph, grows candidate buffers
+    sim.reset()
+    torch.cuda.synchronize()
+    barrier(dist, dev)
+    dev_ms, launches, outers, wall = 0.0, 0, [], 0.0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()                    # L2 flush between timed steps (256 MB write)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sim.step(1)
+            wall += time.perf_counter() - t0
+            st = sim.stats()
+            dev_ms += st["device_ms"]
+            launches += st["kernel_launches"]
+            outers.append(st["last_outer_iters"])
+        torch.cuda.synchronize()
+    barrier(dist, dev)
+    dev_ms_max = max_over_ranks(dist, dev_ms, dev)
+    st_end = sim.stats()
+
+    # e2e through the public API: animate = run + postRun (positions to host)
+    sim.reset()
+    out = np.empty((sim.n_total, 3), np.float64)
+    barrier(dist, dev)
+    e2e_wall = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.animate(out)
+        e2e_wall += time.perf_counter() - t0
+    barrier(dist, dev)
+    e2e_max = max_over_ranks(dist, e2e_wall, dev)
+
+    # roofline of the dominant kernel (the J sweep), timed alone on this stream
+    sweep_ms, sweep_bytes = sim.sweep_timing(400)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = sweep_bytes / (sweep_ms * 1e-3) / 1e9
+
+    value = ws * args.steps / (dev_ms_max * 1e-3)
+    e2e = ws * args.steps / e2e_max
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    mean_outer = float(np.mean(outers))
+    res = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": {"fp32": "f32", "fp64": "f64", "mixed": "f32+f64"}[
+            args.precision], "data": "synthetic (seeded generator; no public dataset for this path)",
+        "config": {"workload": workload_desc(sc, args.precision), "steps_timed": f"0..{args.steps - 1}",
+                   "parallelism": "replicas only" if ws > 1 else "single GPU",
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "outer_iterations_per_step": {"mean": mean_outer, "min": int(min(outers)),
+                                                 "max": int(max(outers))},
+                   "vertices_sim": sim.n_sim, "vertices_total": sim.n_total,
+                   "patch_pairs": st_end["patch_pairs"], "pt_candidates": st_end["pt_candidates"],
+                   "ee_candidates": st_end["ee_candidates"], "device_bytes": st_end["device_bytes"]},
+        "element_updates_per_s": round(sim.n_sim * sc.lg_iterations * float(np.sum(outers)) / (dev_ms / 1e3), 1),
+        "wall_ms_per_step": round(1e3 * wall / args.steps, 4),
+        "gpu_launches": int(launches),
+        "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(sim.n_total * 16 + 8 * round(mean_outer) + 32),
+                "note": "animate(): step + copy of every position to host; the step takes no host input "
+                        "(state stays on the device, as in the reference)"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.precision),
+                     "kernel": "k_sweep (weighted-Jacobi sweep, SELL-32)",
+                     "bytes_per_launch": int(sweep_bytes), "ms_per_launch": round(sweep_ms, 6),
+                     "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_reference_sample(sc, args.precision, args.cpu_outer_sample, mean_outer,
+                                                   os.cpu_count() or 1)
+    print(json.dumps(res), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from oracle.oracle import FORM_R2, Oracle
+    sc = workload(args.config)
+    threads = os.cpu_count() or 1
+    sample_outer = args.cpu_outer_sample
+    orc = Oracle(sc, args.precision, FORM_R2, threads=threads, fixed_outer=sample_outer)
+    for _ in range(min(args.warmup, 1)):
+        orc.step(1)
+    orc.set_state(np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics]),
+                  np.zeros((sc.n_sim, 3)))
+    budget, t_used, n = args.ref_budget_s, 0.0, 0
+    while n < args.steps and t_used < budget:
+        t0 = time.perf_counter()
+        orc.step(1)
+        t_used += time.perf_counter() - t0
+        n += 1
+    per_outer = t_used / (n * sample_outer)
+    outer_per_step = args.ref_outer_per_step
+    value = 1.0 / (per_outer * outer_per_step)
+    sample = (f"{n} steps from step 0, each with {sample_outer} outer iterations, scaled to {outer_per_step} "
+              f"outer iterations per step (the reference stopping rule never fires at this size in FP32); "
+              f"reference R2-operator form restated on the CPU, {threads} threads")
+    res = {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": ws,
+           "steps": n, "warmup": args.warmup, "ms_per_step": round(1e3 / value, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else args.precision,
+           "data": "synthetic", "config": {"workload": workload_desc(sc, args.precision)},
+           "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(res), flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "mixed"])
+    ap.add_argument("--config", default="c1", choices=["c1", "c0"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-outer-sample", type=int, default=2)
+    ap.add_argument("--ref-outer-per-step", type=float, default=30.0)
+    ap.add_argument("--ref-budget-s", type=float, default=60.0)
+    args = ap.parse_args(argv)
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,240 @@
+/*
+ * pdipc.h — C ABI of the GB300 PD-IPC cloth time step (libpdipc.so).
+ *
+ * The reference exposes this path as a C++ virtual class, not as an FFI:
+ *   BaseSimulator / PD_IPC::PdIpcSimulator   (Simulator/BaseSimulator.h:32-136,
+ *                                             Simulator/PD-IPC/PdIpcSimulator.h:441-642)
+ * created through the factory createSimulator("pd_ipc_simulator", ...)
+ * (Simulator/SimulatorFactor.h:13-57).  Each entry point below replaces one
+ * member of that class; the citation on each names it.  A header-only C++
+ * class with the reference's member names sits on top of this ABI in
+ * include/pdipc_simulator.hpp.
+ *
+ * Conventions
+ *   - plain pointers and sizes; no C++ or torch types cross the boundary;
+ *   - every call returns a pdipc_status, no exceptions escape;
+ *   - a context owns one CUDA stream and all of its device memory; contexts
+ *     are independent, calls on one context are not re-entrant;
+ *   - positions cross the boundary as float64 xyz triplets whatever the
+ *     precision mode; vertex order is every cloth (sim) model in the order
+ *     added, then every static model in the order added — the reference's
+ *     devPoints layout (PdIpcSimulator.cpp:34-200);
+ *   - there is no CPU fallback: without a usable GB300 (sm_103) pdipc_create
+ *     fails with PDIPC_ERR_CUDA.
+ */
+#ifndef PDIPC_H
+#define PDIPC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PDIPC_ABI_VERSION 1
+
+typedef struct pdipc_ctx pdipc_ctx;
+
+typedef enum {
+    PDIPC_OK = 0,
+    PDIPC_ERR_ARG = 1,           /* bad argument (null, size, index out of range) */
+    PDIPC_ERR_CUDA = 2,          /* CUDA runtime error or no suitable device */
+    PDIPC_ERR_OVERFLOW = 3,      /* a bounded device buffer or loop overflowed */
+    PDIPC_ERR_NONFINITE = 4,     /* NaN/Inf appeared in the state */
+    PDIPC_ERR_NOT_CONVERGED = 5, /* reserved: outer loop hit its cap in strict mode */
+    PDIPC_ERR_STATE = 6,         /* call out of order (e.g. step before initialize) */
+    PDIPC_ERR_ALLOC = 7,         /* host or device allocation failed */
+    PDIPC_ERR_IO = 8             /* checkpoint file could not be read or written */
+} pdipc_status;
+
+typedef enum {
+    PDIPC_PREC_FP32 = 0,  /* every kernel in float: the reference's own arithmetic (DataCore.h:8,19) */
+    PDIPC_PREC_FP64 = 1,  /* every kernel in double: the plain FP64 GPU form */
+    PDIPC_PREC_MIXED = 2  /* float state / local step / sweeps / barrier, double CCD and contact distance */
+} pdipc_precision;
+
+/* Solver parameters.  Defaults (pdipc_default_params) are the reference's
+ * constants; each field names where the reference fixes it. */
+typedef struct {
+    double time_step;        /* _timeStep, BaseSimulator.h:37 (config <timeStep>) */
+    double gravity;          /* _gravity along y, BaseSimulator.h:38 (-9.8) */
+    double dhat;             /* dHat, PdIpcSimulator.h:444 (1e-3) */
+    double kappa;            /* barrier stiffness, PdIpcSimulator.h:445 (1e4) */
+    double inflation_radius; /* patch AABB inflation; <0 means 0.5*dhat (PdIpcSimulator.cpp:1154) */
+    int lg_iterations;       /* local-global iterations per outer iteration, cpp:1592 (10) */
+    int cheby_iterations;    /* R2 sweeps per global step, cpp:1597 (15) */
+    double cheby_rho;        /* spectral radius estimate, PdIpcGpuFunc.cu:1318 (0.9992) */
+    double jacobi_relax;     /* weighted-Jacobi w, PdIpcGpuFunc.cu:949,1051 (2/3) */
+    int max_outer;           /* outer CCD iterations cap, cpp:1685 (30) */
+    double outer_tol;        /* stop when ||dx||^2 < tol (after the first), cpp:1776 (1e-5) */
+    double ccd_slack;        /* per-pair swept-AABB slack, PdIpcGpuFunc.cu:2656,2676 (5e-3) */
+    double toi_scale;        /* applied to toi < 1, PdIpcGpuFunc.cu:2698-2699 (0.98) */
+    int ccd_max_iter;        /* additive-CCD iterations, PdIpcGpuFunc.cu:2493 (10) */
+    double ccd_eta;          /* additive-CCD gap fraction, PdIpcGpuFunc.cu:2488 (0.1) */
+    double static_mass;      /* collision mass of static vertices, cpp:1494 (1e4) */
+    int precision;           /* pdipc_precision (FP32) */
+    int fixed_outer;         /* 0: reference stopping rule; >0: run exactly this many outer iterations */
+    int use_graphs;          /* 1: replay each outer iteration's PD solve as a CUDA graph */
+    int device;              /* CUDA device ordinal */
+    int rebuild_bvh;         /* 0: build the patch BVH once at initialize and refit per step
+                                (reference behaviour, cpp:1296-1320); 1: rebuild every step */
+    int reserved[7];
+} pdipc_params;
+
+/* Per-context statistics of the most recent pdipc_step call. */
+typedef struct {
+    int64_t steps_done;          /* steps since initialize (or reset) */
+    int32_t last_outer_iters;    /* outer iterations in the last step */
+    int32_t max_outer_iters;     /* max over the steps of the last pdipc_step call */
+    int64_t total_outer_iters;   /* sum over the steps of the last pdipc_step call */
+    int64_t patch_pairs;         /* overlapping patch pairs found by the last broad phase */
+    int64_t pt_candidates;       /* point-triangle candidates of the last broad phase */
+    int64_t ee_candidates;       /* edge-edge candidates of the last broad phase */
+    int64_t active_contacts;     /* pairs with d < dhat in the last contact pass */
+    double last_toi;             /* clamped step fraction of the last outer iteration */
+    double last_residual;        /* ||dx||^2 of the last outer iteration */
+    int32_t n_sim;               /* simulated (cloth) vertices */
+    int32_t n_total;             /* all vertices including static ones */
+    int32_t n_patches;           /* collision patches (all models) */
+    int32_t precision;           /* pdipc_precision in use */
+    int64_t device_bytes;        /* device memory held by the context */
+    int64_t kernel_launches;     /* kernels launched by the last pdipc_step call (graph nodes included) */
+    double device_ms;            /* device time of the last pdipc_step call: CUDA events recorded on the
+                                    context's stream around every step, summed */
+} pdipc_stats;
+
+/* Fill *p with the reference defaults listed beside each field. */
+void pdipc_default_params(pdipc_params* p);
+
+/* Create a context: BaseSimulator(simName, RunPlatform::CUDA) ctor plus the
+ * PdIpcSimulator constructor (BaseSimulator.h:35-45, PdIpcSimulator.h:441-449).
+ * Selects p->device, checks it is sm_103, creates the context's stream. */
+pdipc_status pdipc_create(const pdipc_params* p, pdipc_ctx** out);
+
+/* Add a simulated cloth model: PdIpcSimulator::addModelFromConfigFile with
+ * <type> 0 k_stretch k_bend k_pin, <density>, <patchDim>
+ * (PdIpcSimulator.h:462-534) plus readFixedInfo (PdIpcModel.h:56-77).
+ * X: 3*nv float64, F: 3*nf int32 (0-based), pins: npins local vertex ids. */
+pdipc_status pdipc_add_cloth(pdipc_ctx* ctx, const double* X, int nv, const int* F, int nf,
+                             double density, double k_stretch, double k_bend,
+                             const int* pins, int npins, double k_pin, int patch_dim);
+
+/* Add a static (kinematically fixed) triangle mesh:
+ * PdIpcSimulator::addStaticModelFromConfigFile (PdIpcSimulator.h:536-600). */
+pdipc_status pdipc_add_static(pdipc_ctx* ctx, const double* X, int nv, const int* F, int nf,
+                              int patch_dim);
+
+/* PdIpcSimulator::initialization (PdIpcSimulator.cpp:34-268): per-model
+ * precompute, system assembly (setupHessMat cpp:270-414), device upload
+ * (gpuGeneralInit/gpuSolverInit cpp:416-1149) and collision set-up including
+ * the patch BVH build (gpuCollisionInit cpp:1151-1504). */
+pdipc_status pdipc_initialize(pdipc_ctx* ctx);
+
+/* nsteps x PdIpcSimulator::run(frame) (cpp:18-21 -> doTime cpp:1538 -> advance cpp:1683-1796).
+ * The state stays on the device. */
+pdipc_status pdipc_step(pdipc_ctx* ctx, int nsteps);
+
+/* BaseSimulator::animate(frame) = run(frame); postRun() (BaseSimulator.h:73-76):
+ * one step, then copy every vertex position to out (3*n_total float64) —
+ * the reference's postRun D2H of devPoints (cpp:23-32) into a headless buffer. */
+pdipc_status pdipc_animate(pdipc_ctx* ctx, double* out);
+
+/* postRun's device-to-host copy alone: out receives 3*n_total float64. */
+pdipc_status pdipc_get_positions(pdipc_ctx* ctx, double* out);
+
+/* Velocities of the simulated vertices: out receives 3*n_sim float64. */
+pdipc_status pdipc_get_velocities(pdipc_ctx* ctx, double* out);
+
+/* Overwrite positions (3*n_total) and optionally velocities (3*n_sim; NULL keeps them). */
+pdipc_status pdipc_set_state(pdipc_ctx* ctx, const double* X, const double* V);
+
+/* PdIpcSimulator::reset (BaseSimulator.h:79, empty in the reference): restore the
+ * positions given at add time and zero velocities. */
+pdipc_status pdipc_reset(pdipc_ctx* ctx);
+
+pdipc_status pdipc_get_stats(pdipc_ctx* ctx, pdipc_stats* out);
+
+/* PdIpcSimulator::saveSimulator(frame) (PdIpcSimulator.h:879-916): writes the
+ * EigenMatrixIO::write_binary layout (int64 rows=3, int64 cols=n_total, float32
+ * column-major xyz; Commom/EigenMatrixIO.h:11-27) followed by a second block of
+ * the same layout holding the n_sim velocities.  pdipc_load reads it back. */
+pdipc_status pdipc_save(pdipc_ctx* ctx, const char* path);
+pdipc_status pdipc_load(pdipc_ctx* ctx, const char* path);
+
+/* Destroy the context and free everything it holds (the reference frees nothing). */
+void pdipc_destroy(pdipc_ctx* ctx);
+
+const char* pdipc_status_string(pdipc_status s);
+/* Message of the last failing call on ctx (never NULL; "" if none). */
+const char* pdipc_last_error(const pdipc_ctx* ctx);
+int pdipc_abi_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Stage entry points.  Each runs one stage of the step on the context's
+ * device tables with caller-supplied host inputs, so a stage can be checked
+ * on its own against the oracle.  They need pdipc_initialize first and leave
+ * the simulation state untouched.
+ * ------------------------------------------------------------------------- */
+
+/* The patch broad phase of gpuCcdCulling (PdIpcSimulator.cpp:1799-1869):
+ * swept patch AABBs from x_old (3*n_total) and dir (3*n_total), BVH refit,
+ * overlapping patch pairs (a<b), expansion to point-triangle records
+ * (v, f0, f1, f2) and edge-edge records (a0, a1, b0, b1).
+ * Arrays of capacity cap_* receive up to that many records; *n_* receive the
+ * full counts (PDIPC_ERR_OVERFLOW if a count exceeds its capacity). */
+pdipc_status pdipc_stage_broadphase(pdipc_ctx* ctx, const double* x_old, const double* dir,
+                                    int* pairs, int64_t cap_pairs, int64_t* n_pairs,
+                                    int* pt, int64_t cap_pt, int64_t* n_pt,
+                                    int* ee, int64_t cap_ee, int64_t* n_ee);
+
+/* Morton codes (63-bit, 21 bits per axis) of the patch AABB centres computed
+ * at initialize, and the stable sort order of the patches by code
+ * (AipcBvhs::init, Simulator/Bvhs/AipcBvhs.cpp:134-213). */
+pdipc_status pdipc_stage_morton(pdipc_ctx* ctx, uint64_t* codes, int* order, int cap);
+
+/* getImpactOfTimeHost (PdIpcGpuFunc.cu:2706-2742) over the candidate set of the
+ * last broad phase: per-candidate toi (1 where skipped) and the clamped global
+ * toi (0.98*min if min<1).  x0, x1: 3*n_total. toi_pt/toi_ee may be NULL. */
+pdipc_status pdipc_stage_toi(pdipc_ctx* ctx, const double* x0, const double* x1,
+                             double* toi_pt, double* toi_ee, double* toi_global);
+
+/* setCollisionConstraintsHost (PdIpcGpuFunc.cu:2894-2930) over the candidate set
+ * of the last broad phase at positions x (3*n_total): collision diagonal
+ * (n_total) and right-hand side (3*n_total); *n_active gets the pair count. */
+pdipc_status pdipc_stage_contact(pdipc_ctx* ctx, const double* x,
+                                 double* coll_diag, double* coll_rhs, int64_t* n_active);
+
+/* predictiveKernel (PdIpcGpuFunc.cu:88-147) from the state (X: 3*n_total,
+ * V: 3*n_sim) followed by one outer iteration's projective-dynamics solve:
+ * lg_iterations x (doLocalProjection cpp:1624-1681 + Chebyshev-accelerated
+ * Jacobi cu:1245-1346) with no contact terms.  out_X receives 3*n_total
+ * positions.  The context's state is restored afterwards. */
+pdipc_status pdipc_stage_pd(pdipc_ctx* ctx, const double* X, const double* V, double* out_X);
+
+/* Times the dominant kernel of the step, one plain weighted-Jacobi sweep over
+ * the system matrix (the R2 sweep of chebyshevJacobiR2IterationKernel,
+ * PdIpcGpuFunc.cu:1076-1129, here applied as one of two J sweeps), on the
+ * current state: `launches` back-to-back launches on the context's stream
+ * between two CUDA events.  *avg_ms = mean duration of one launch;
+ * *bytes = algorithmic bytes one launch must move (8 per stored matrix entry
+ * + 40 per row: x, rhs and output xyz, inverse diagonal). */
+pdipc_status pdipc_stage_sweep_timing(pdipc_ctx* ctx, int launches, double* avg_ms, double* bytes);
+
+/* Topology precompute of one mesh, on the host (no device needed):
+ * sorted unique edges (Model/TriangleMesh/BaseSurfaceMesh.cpp:219-275), the grid
+ * collision patches (PdIpcClothModel::setCollisionPatches, PdIpcClothModel.h:45-140)
+ * and the one-owner-face assignment of points and edges
+ * (PdIpcModel::postProcessBoundaryInfo, PdIpcModel.h:84-172).
+ * edges: 2*cap_edges ints; patch_off: npatch+1 ints (cap_patches+1), patch_faces:
+ * cap_faces ints; owner_of_point: nv ints; owner_of_edge: cap_edges ints.
+ * The counts are returned even when a capacity is too small (PDIPC_ERR_OVERFLOW). */
+pdipc_status pdipc_mesh_topology(const double* X, int nv, const int* F, int nf, int patch_dim,
+                                 int* edges, int cap_edges, int* n_edges,
+                                 int* patch_off, int cap_patches, int* patch_faces, int cap_faces,
+                                 int* n_patches, int* owner_of_point, int* owner_of_edge);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PDIPC_H */

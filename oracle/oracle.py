@@ -1,0 +1,209 @@
+"""ctypes wrapper of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module; the shipped library never loads it.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "pd-ipc-armadillodemo_gb300"))
+
+from pdipc.abi import Params, Stats, STATUS_NAMES, params_for_scene  # noqa: E402
+
+from . import build as _build  # noqa: E402
+
+_lib = None
+
+FORM_R2 = 0   # the reference's R2 operator with path tables
+FORM_JJ = 1   # R2 applied as two weighted-Jacobi sweeps (the library's form)
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_i64p = C.POINTER(C.c_longlong)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        L.orc_create.restype = C.c_void_p
+        L.orc_create.argtypes = [C.POINTER(Params), C.c_int, C.c_int]
+        L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_add_cloth.argtypes = [C.c_void_p, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double,
+                                    C.c_double, _ip, C.c_int, C.c_double, C.c_int]
+        L.orc_add_static.argtypes = [C.c_void_p, _dp, C.c_int, _ip, C.c_int, C.c_int]
+        L.orc_initialize.argtypes = [C.c_void_p]
+        L.orc_step.argtypes = [C.c_void_p, C.c_int]
+        L.orc_get_positions.argtypes = [C.c_void_p, _dp]
+        L.orc_get_velocities.argtypes = [C.c_void_p, _dp]
+        L.orc_set_state.argtypes = [C.c_void_p, _dp, _dp]
+        L.orc_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+        L.orc_broadphase.argtypes = [C.c_void_p, _dp, _dp, _ip, C.c_longlong, _i64p, _ip, C.c_longlong,
+                                     _i64p, _ip, C.c_longlong, _i64p]
+        L.orc_morton.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), _ip, C.c_int]
+        L.orc_toi.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
+        L.orc_contact.argtypes = [C.c_void_p, _dp, _dp, _dp, _i64p]
+        L.orc_stage_pd.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.orc_mesh_topology.argtypes = [_dp, C.c_int, _ip, C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, C.c_int,
+                                        _ip, C.c_int, _ip, _ip, _ip, _ip, _ip]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise OracleError(f"{what}: {STATUS_NAMES.get(rc, rc)}")
+
+
+class Oracle:
+    """CPU restatement of PdIpcSimulator for one scene."""
+
+    def __init__(self, scene, precision="fp64", form=FORM_JJ, threads=None, **overrides):
+        L = lib()
+        self.params = params_for_scene(scene, precision, **overrides)
+        if threads is None:
+            threads = os.cpu_count() or 1
+        self.threads = threads
+        self.h = L.orc_create(C.byref(self.params), form, threads)
+        if not self.h:
+            raise OracleError("orc_create failed")
+        self._keep = []
+        for c in scene.cloths:
+            X = np.ascontiguousarray(c.X, dtype=np.float64)
+            F = np.ascontiguousarray(c.F, dtype=np.int32)
+            P = np.ascontiguousarray(c.pins, dtype=np.int32)
+            _check(L.orc_add_cloth(self.h, _d(X), X.shape[0], _i(F), F.shape[0], c.density, c.k_stretch,
+                                   c.k_bend, _i(P), P.shape[0], c.k_pin, c.patch_dim), "add_cloth")
+        for s in scene.statics:
+            X = np.ascontiguousarray(s.X, dtype=np.float64)
+            F = np.ascontiguousarray(s.F, dtype=np.int32)
+            _check(L.orc_add_static(self.h, _d(X), X.shape[0], _i(F), F.shape[0], s.patch_dim), "add_static")
+        _check(L.orc_initialize(self.h), "initialize")
+        self.n_sim = scene.n_sim
+        self.n_total = scene.n_total
+
+    def close(self):
+        if self.h:
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, n=1):
+        _check(lib().orc_step(self.h, n), "step")
+
+    def positions(self):
+        out = np.empty((self.n_total, 3), dtype=np.float64)
+        _check(lib().orc_get_positions(self.h, _d(out)), "get_positions")
+        return out
+
+    def velocities(self):
+        out = np.empty((self.n_sim, 3), dtype=np.float64)
+        _check(lib().orc_get_velocities(self.h, _d(out)), "get_velocities")
+        return out
+
+    def set_state(self, X, V=None):
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        Vp = None
+        if V is not None:
+            V = np.ascontiguousarray(V, dtype=np.float64)
+            Vp = _d(V)
+        _check(lib().orc_set_state(self.h, _d(X), Vp), "set_state")
+
+    def stats(self):
+        s = Stats()
+        _check(lib().orc_get_stats(self.h, C.byref(s)), "get_stats")
+        return s.as_dict()
+
+    def broadphase(self, x_old, dx, cap=None):
+        x_old = np.ascontiguousarray(x_old, dtype=np.float64)
+        dx = np.ascontiguousarray(dx, dtype=np.float64)
+        npair, npt, nee = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        cap = cap or 1 << 16
+        while True:
+            pairs = np.empty((cap, 2), np.int32)
+            pt = np.empty((cap, 4), np.int32)
+            ee = np.empty((cap, 4), np.int32)
+            rc = lib().orc_broadphase(self.h, _d(x_old), _d(dx), _i(pairs), cap, C.byref(npair), _i(pt), cap,
+                                      C.byref(npt), _i(ee), cap, C.byref(nee))
+            if rc == 3:
+                cap = max(npair.value, npt.value, nee.value)
+                continue
+            _check(rc, "broadphase")
+            return pairs[:npair.value].copy(), pt[:npt.value].copy(), ee[:nee.value].copy()
+
+    def morton(self, npatch):
+        codes = np.empty(npatch, np.uint64)
+        order = np.empty(npatch, np.int32)
+        _check(lib().orc_morton(self.h, codes.ctypes.data_as(C.POINTER(C.c_ulonglong)), _i(order), npatch),
+               "morton")
+        return codes, order
+
+    def toi(self, x0, x1, npt, nee):
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        x1 = np.ascontiguousarray(x1, dtype=np.float64)
+        tp = np.empty(max(npt, 1), np.float64)
+        te = np.empty(max(nee, 1), np.float64)
+        g = C.c_double()
+        _check(lib().orc_toi(self.h, _d(x0), _d(x1), _d(tp), _d(te), C.byref(g)), "toi")
+        return tp[:npt], te[:nee], g.value
+
+    def stage_pd(self, X, V):
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        out = np.empty((self.n_total, 3), np.float64)
+        _check(lib().orc_stage_pd(self.h, _d(X), _d(V), _d(out)), "stage_pd")
+        return out
+
+    def contact(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        diag = np.empty(self.n_total, np.float64)
+        rhs = np.empty((self.n_total, 3), np.float64)
+        na = C.c_longlong()
+        _check(lib().orc_contact(self.h, _d(x), _d(diag), _d(rhs), C.byref(na)), "contact")
+        return diag, rhs, na.value
+
+
+def mesh_topology(X, F, patch_dim):
+    """Edges, grid patches and face ownership lists of one standalone mesh."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    F = np.ascontiguousarray(F, dtype=np.int32)
+    nv, nf = X.shape[0], F.shape[0]
+    cap_e = 3 * nf
+    edges = np.empty((cap_e, 2), np.int32)
+    ne, npch = C.c_int(), C.c_int()
+    poff = np.empty(nf + 1, np.int32)
+    pf = np.empty(nf, np.int32)
+    opo = np.empty(nf + 1, np.int32)
+    op = np.empty(nv, np.int32)
+    oeo = np.empty(nf + 1, np.int32)
+    oe = np.empty(cap_e, np.int32)
+    _check(lib().orc_mesh_topology(_d(X), nv, _i(F), nf, patch_dim, _i(edges), cap_e, C.byref(ne), _i(poff), nf,
+                                   _i(pf), nf, C.byref(npch), _i(opo), _i(op), _i(oeo), _i(oe)), "mesh_topology")
+    n_e, n_p = ne.value, npch.value
+    patches = [pf[poff[p]:poff[p + 1]].copy() for p in range(n_p)]
+    owned_points = [op[opo[f]:opo[f + 1]].copy() for f in range(nf)]
+    owned_edges = [oe[oeo[f]:oeo[f + 1]].copy() for f in range(nf)]
+    return edges[:n_e].copy(), patches, owned_points, owned_edges

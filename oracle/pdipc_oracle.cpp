@@ -1,0 +1,1465 @@
+// pdipc_oracle.cpp — CPU restatement of the reference PD-IPC cloth time step.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the correctness oracle for the GB300
+// library and the timed CPU baseline; nothing in the shipped library links,
+// loads or calls it.  It restates, in plain C++17 (no Eigen, no CUDA), what the
+// reference does on its GPU path — the reference has no CPU implementation of
+// PD-IPC (RunPlatform is stored but never consulted, Simulator/BaseSimulator.h:13-18).
+//
+// Parity status: unpinned by reference outputs.  The reference ships no tests,
+// no golden trajectories and cannot be compiled here (MSVC project, Eigen/Qt/TBB
+// absent).  The only known answers are the example scene's topology caches
+// (example/ClothArmadillo/cloth1/{boundary.dat,patchInfo.dat}); tests pin the
+// edge enumeration and patch partition of this oracle against them.
+//
+// Precision: templated on the state scalar T and the CCD/contact scalar TC.
+// <float,float> reproduces the reference arithmetic (qeal = float,
+// DataCore.h:8,19); <double,double> is the FP64 oracle; <float,double> mirrors
+// the library's mixed mode.  Compiled with -ffp-contract=off so results do not
+// depend on whether the host CPU fuses multiply-adds.
+//
+// Summation order: the reference accumulates the right-hand side and the
+// collision diagonal with float atomics (PdIpcGpuFunc.cu:713-725, 2826-2888),
+// so its order is unspecified.  Here every sum is a gather in ascending
+// source order: rhs_i = ((rhs0_i + own_i + sum_{k in N(i)} bend_k(i) aq_k)
+// + contact_i) + pin_i, and contact contributions in candidate-list order.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <set>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "pdipc.h"
+
+namespace orc {
+
+using i64 = long long;
+
+// ---------------------------------------------------------------------------
+// Mesh topology (Model/TriangleMesh/BaseSurfaceMesh.cpp:219-275 and
+// Simulator/PD-IPC/PdIpcModel.h:84-172).
+// ---------------------------------------------------------------------------
+struct Topology {
+    int nv = 0, nf = 0;
+    std::vector<std::array<int, 3>> faces;
+    std::vector<std::array<int, 2>> edges;           // sorted unique (min,max)
+    std::vector<std::vector<int>> point_edges;       // edge ids, ascending
+    std::vector<std::vector<int>> edge_faces;        // face ids, ascending
+    std::vector<std::vector<int>> face_owned_edges;  // boundaryFacesSharedEdges
+    std::vector<std::vector<int>> face_owned_points; // boundaryFacesSharedPoints
+    std::vector<std::vector<int>> patches;           // face ids per patch
+};
+
+static std::array<int, 2> sorted_pair(int a, int b) {
+    return a < b ? std::array<int, 2>{a, b} : std::array<int, 2>{b, a};
+}
+
+// Edge list: every face contributes (f[k], f[k+1]) sorted; sort
+// lexicographically; unique (BaseSurfaceMesh.cpp:221-234).  Edge ids therefore
+// follow (min,max) order, and each vertex's edge list is ascending in the
+// neighbouring vertex id.
+static void build_edges(Topology& t) {
+    std::vector<std::array<int, 2>> el;
+    el.reserve(3 * (size_t)t.nf);
+    for (auto& f : t.faces)
+        for (int k = 0; k < 3; ++k) el.push_back(sorted_pair(f[k], f[(k + 1) % 3]));
+    std::sort(el.begin(), el.end());
+    el.erase(std::unique(el.begin(), el.end()), el.end());
+    t.edges = el;
+    t.point_edges.assign(t.nv, {});
+    for (int e = 0; e < (int)el.size(); ++e) {
+        t.point_edges[el[e][0]].push_back(e);
+        t.point_edges[el[e][1]].push_back(e);
+    }
+    t.edge_faces.assign(el.size(), {});
+    for (int f = 0; f < t.nf; ++f)
+        for (int k = 0; k < 3; ++k) {
+            auto key = sorted_pair(t.faces[f][k], t.faces[f][(k + 1) % 3]);
+            int e = (int)(std::lower_bound(el.begin(), el.end(), key) - el.begin());
+            t.edge_faces[e].push_back(f);
+        }
+}
+
+// Ownership: every edge and every point is handed to exactly one incident face,
+// the first one (in incidence order) whose owned list is currently smallest
+// (PdIpcModel.h:136-171).  Patch-pair expansion then never repeats a primitive.
+static bool build_ownership(Topology& t) {
+    std::vector<std::vector<int>> point_faces(t.nv);
+    for (int f = 0; f < t.nf; ++f)
+        for (int k = 0; k < 3; ++k) point_faces[t.faces[f][k]].push_back(f);
+    // edges shared faces, in the order faces push their (01,12,20) edges
+    std::vector<std::vector<int>> esf(t.edges.size());
+    for (int f = 0; f < t.nf; ++f) {
+        const auto& F = t.faces[f];
+        int ks[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+        for (auto& kk : ks) {
+            auto key = sorted_pair(F[kk[0]], F[kk[1]]);
+            int e = (int)(std::lower_bound(t.edges.begin(), t.edges.end(), key) - t.edges.begin());
+            esf[e].push_back(f);
+        }
+    }
+    t.face_owned_edges.assign(t.nf, {});
+    for (int e = 0; e < (int)t.edges.size(); ++e) {
+        int best = esf[e][0];
+        size_t bs = t.face_owned_edges[best].size();
+        for (size_t k = 1; k < esf[e].size(); ++k) {
+            int f = esf[e][k];
+            if (t.face_owned_edges[f].size() < bs) { best = f; bs = t.face_owned_edges[f].size(); }
+        }
+        t.face_owned_edges[best].push_back(e);
+    }
+    t.face_owned_points.assign(t.nf, {});
+    for (int p = 0; p < t.nv; ++p) {
+        if (point_faces[p].empty()) return false;  // isolated vertex: the reference reads past the list
+        int best = point_faces[p][0];
+        size_t bs = t.face_owned_points[best].size();
+        for (size_t k = 1; k < point_faces[p].size(); ++k) {
+            int f = point_faces[p][k];
+            if (t.face_owned_points[f].size() < bs) { best = f; bs = t.face_owned_points[f].size(); }
+        }
+        t.face_owned_points[best].push_back(p);
+    }
+    return true;
+}
+
+// Grid collision patches (PdIpcClothModel.h:45-140), in float as the reference
+// (qeal = float).  Cells form a len x len grid over the bounding box in the two
+// axes other than the thinnest one; a face goes to the first cell (row-major)
+// whose closed box holds its centroid; empty cells are dropped.  When no axis
+// is strictly thinnest the reference leaves the axis pair uninitialised; here
+// the last axis achieving the minimum extent is taken as the normal.
+static void build_patches(Topology& t, const std::vector<double>& X, int patch_dim) {
+    const float FMAX = std::numeric_limits<float>::infinity();
+    float mn[3] = {FMAX, FMAX, FMAX}, mx[3] = {-FMAX, -FMAX, -FMAX};
+    for (int i = 0; i < t.nv; ++i)
+        for (int k = 0; k < 3; ++k) {
+            float p = (float)X[3 * i + k];
+            mn[k] = std::min(mn[k], p);
+            mx[k] = std::max(mx[k], p);
+        }
+    int len = (int)(std::sqrt((float)t.nv) < (float)patch_dim ? std::sqrt((float)t.nv) : (float)patch_dim);
+    if (len < 1) len = 1;
+    float size[3];
+    for (int k = 0; k < 3; ++k) size[k] = mx[k] - mn[k];
+    int nrm = -1;
+    if (size[0] < size[1] && size[0] < size[2]) nrm = 0;
+    if (size[1] < size[0] && size[1] < size[2]) nrm = 1;
+    if (size[2] < size[0] && size[2] < size[1]) nrm = 2;
+    if (nrm < 0) {
+        float m = std::min(size[0], std::min(size[1], size[2]));
+        for (int k = 0; k < 3; ++k)
+            if (size[k] == m) nrm = k;
+    }
+    int u = nrm == 0 ? 1 : 0;
+    int v = nrm == 2 ? 1 : 2;
+    const float su = size[u] / (float)len, sv = size[v] / (float)len;
+    std::vector<std::vector<int>> pocket((size_t)len * len);
+    for (int f = 0; f < t.nf; ++f) {
+        float c[3] = {0.f, 0.f, 0.f};
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) c[a] += (float)X[3 * t.faces[f][k] + a];
+        for (int a = 0; a < 3; ++a) c[a] /= 3.f;
+        for (int r = 0; r < len; ++r) {
+            float bu0 = mn[u] + (float)r * su, bu1 = bu0 + su;
+            if (!(c[u] >= bu0 && c[u] <= bu1)) continue;
+            bool done = false;
+            for (int cc = 0; cc < len; ++cc) {
+                float bv0 = mn[v] + (float)cc * sv, bv1 = bv0 + sv;
+                if (c[v] >= bv0 && c[v] <= bv1) {
+                    pocket[(size_t)r * len + cc].push_back(f);
+                    done = true;
+                    break;
+                }
+            }
+            if (done) break;
+        }
+    }
+    t.patches.clear();
+    for (auto& p : pocket)
+        if (!p.empty()) t.patches.push_back(p);
+}
+
+struct ModelIn {
+    std::vector<double> X;
+    std::vector<int> F;
+    int nv = 0, nf = 0;
+    bool is_static = false;
+    double density = 0, k_stretch = 0, k_bend = 0, k_pin = 0;
+    std::vector<int> pins;
+    int patch_dim = 10;
+};
+
+// Morton code of a quantised, centred patch centre.  The reference calls the
+// un-vendored Resorting::MortonCode64(int,int,int) (AipcBvhs.cpp:181); this is
+// the 63-bit interleave used by the library: each coordinate offset by 2^20,
+// clamped to 21 bits, bit b of x/y/z at positions 3b/3b+1/3b+2.
+static uint64_t spread21(uint64_t v) {
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+static uint64_t morton63(int x, int y, int z) {
+    auto q = [](int a) -> uint64_t {
+        long long s = (long long)a + (1ll << 20);
+        if (s < 0) s = 0;
+        if (s > (1ll << 21) - 1) s = (1ll << 21) - 1;
+        return (uint64_t)s;
+    };
+    return spread21(q(x)) | (spread21(q(y)) << 1) | (spread21(q(z)) << 2);
+}
+
+template <typename T>
+static T omega_first(T rho2) {  // PdIpcGpuFunc.cu:1321 — 2.0/(2-rho) in double, stored as qeal
+    T d = T(2) - rho2;
+    return (T)(2.0 / (double)d);
+}
+template <typename T>
+static T omega_next(T rho2, T omega) {  // PdIpcGpuFunc.cu:1341
+    T d = T(4) - rho2 * omega;
+    return (T)(4.0 / (double)d);
+}
+
+// ---------------------------------------------------------------------------
+// The simulator.
+// ---------------------------------------------------------------------------
+template <typename T, typename TC>
+struct Sim {
+    pdipc_params prm;
+    int global_form = 0;  // 0: reference R2 operator with path tables; 1: two J sweeps
+    std::vector<ModelIn> models;
+    bool initialized = false;
+
+    int nsim = 0, ntot = 0;
+    // state (AoS xyz, the reference layout)
+    std::vector<T> X, X0, Xold, dir, V, Xrest_all, rhs0, rhs, Dinert, Delastic, D, collDiag, collRhs;
+    std::vector<T> grav, invMass;
+    std::vector<int> pinFlag;
+    std::vector<T> pinStiff;
+    std::vector<TC> collMass;
+    // local step tables (flattened per vertex: [self, neighbours ascending])
+    std::vector<int> lOff, lNum, lNbr;
+    std::vector<T> lStrain, lRest, lLbo, lBend, lBendT, curvNorm;
+    // system off-diagonals N_ij = -A_ij (CSR, ascending columns)
+    std::vector<int> nPtr, nCol;
+    std::vector<T> nVal;
+    // reference R2 form
+    std::vector<int> r2Ptr, r2Col, r2Const, r2First, pathPtr, pathK;
+    std::vector<T> pathA, r2Val, r1Op, firstTerm;
+    // collision topology (global ids)
+    std::vector<std::array<int, 3>> faces;
+    std::vector<std::array<int, 2>> edges;
+    std::vector<std::vector<int>> pFaces, pPoints, pEdges, pAll;
+    std::vector<char> pStatic;
+    int npatch = 0;
+    // patch tree (heap-indexed median split, AipcBvhs)
+    std::vector<int> nodeElem;                   // -2 null, -1 internal, >=0 patch id
+    std::vector<std::array<T, 6>> nodeBox;
+    std::vector<int> patchNode;
+    std::vector<uint64_t> morton;
+    std::vector<int> order;
+    // candidates
+    std::vector<std::array<int, 2>> pairs;
+    std::vector<std::array<int, 4>> pt, ee;
+    // stats
+    pdipc_stats st{};
+    std::vector<T> xsweepA, xsweepB, xsweepY;
+    int threads = 1;
+
+    explicit Sim(const pdipc_params& p, int form, int nthreads) : prm(p), global_form(form) {
+        threads = nthreads > 0 ? nthreads : 1;
+    }
+
+    T tp(double v) const { return (T)v; }
+
+    // ---------------- initialisation ----------------
+    int initialize() {
+        nsim = 0;
+        ntot = 0;
+        for (auto& m : models) if (!m.is_static) nsim += m.nv;
+        ntot = nsim;
+        for (auto& m : models) if (m.is_static) ntot += m.nv;
+        if (nsim == 0) return PDIPC_ERR_STATE;
+        X.assign(3 * (size_t)ntot, T(0));
+        std::vector<Topology> topo;
+        // order: sim models first then static, each in add order
+        std::vector<int> morder;
+        for (int i = 0; i < (int)models.size(); ++i) if (!models[i].is_static) morder.push_back(i);
+        for (int i = 0; i < (int)models.size(); ++i) if (models[i].is_static) morder.push_back(i);
+        std::vector<int> voff(models.size()), foff(models.size()), eoff(models.size());
+        int vo = 0, fo = 0, eo = 0;
+        topo.resize(models.size());
+        for (int mi : morder) {
+            auto& m = models[mi];
+            Topology& t = topo[mi];
+            t.nv = m.nv;
+            t.nf = m.nf;
+            t.faces.resize(m.nf);
+            for (int f = 0; f < m.nf; ++f) t.faces[f] = {m.F[3 * f], m.F[3 * f + 1], m.F[3 * f + 2]};
+            build_edges(t);
+            if (!build_ownership(t)) return PDIPC_ERR_ARG;
+            build_patches(t, m.X, m.patch_dim);
+            voff[mi] = vo; foff[mi] = fo; eoff[mi] = eo;
+            for (int i = 0; i < m.nv; ++i)
+                for (int k = 0; k < 3; ++k) X[3 * (size_t)(vo + i) + k] = (T)m.X[3 * i + k];
+            vo += m.nv; fo += m.nf; eo += (int)t.edges.size();
+        }
+        // --- per-vertex cloth tables (PdIpcClothModel.h:177-328) ---
+        invMass.assign(nsim, T(0));
+        std::vector<double> massD(nsim, 0.0);
+        grav.assign(3 * (size_t)nsim, T(0));
+        pinFlag.assign(nsim, -1);
+        pinStiff.clear();
+        lOff.assign(nsim, 0); lNum.assign(nsim, 0);
+        lNbr.clear(); lStrain.clear(); lRest.clear(); lLbo.clear(); lBend.clear(); curvNorm.assign(nsim, T(0));
+        std::vector<double> bendArea(nsim, 0.0);       // A_i * b
+        std::vector<std::vector<double>> lboD(nsim);
+        std::vector<double> strainD(nsim, 0.0);
+        for (int mi : morder) {
+            auto& m = models[mi];
+            if (m.is_static) continue;
+            Topology& t = topo[mi];
+            int o = voff[mi];
+            std::vector<double> area(m.nv, 0.0);
+            auto P = [&](int i, int k) { return m.X[3 * i + k]; };
+            for (int f = 0; f < m.nf; ++f) {
+                const auto& F = t.faces[f];
+                double a[3], b[3];
+                for (int k = 0; k < 3; ++k) { a[k] = P(F[1], k) - P(F[0], k); b[k] = P(F[2], k) - P(F[0], k); }
+                double c[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+                double ar = 0.5 * std::fabs(std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
+                for (int k = 0; k < 3; ++k) area[F[k]] += ar / 3.0;
+            }
+            std::vector<double> restLen(t.edges.size()), cotw(t.edges.size(), 0.0);
+            for (size_t e = 0; e < t.edges.size(); ++e) {
+                int a = t.edges[e][0], b = t.edges[e][1];
+                double d[3] = {P(a, 0) - P(b, 0), P(a, 1) - P(b, 1), P(a, 2) - P(b, 2)};
+                restLen[e] = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                for (int f : t.edge_faces[e]) {
+                    int opp = -1;
+                    for (int k = 0; k < 3; ++k) {
+                        int vk = t.faces[f][k];
+                        if (vk != a && vk != b) opp = vk;
+                        if (opp != -1) break;
+                    }
+                    double x10[3], x20[3];
+                    for (int k = 0; k < 3; ++k) { x10[k] = P(a, k) - P(opp, k); x20[k] = P(b, k) - P(opp, k); }
+                    double l10 = std::sqrt(x10[0] * x10[0] + x10[1] * x10[1] + x10[2] * x10[2]);
+                    double l20 = std::sqrt(x20[0] * x20[0] + x20[1] * x20[1] + x20[2] * x20[2]);
+                    double th = std::acos((x10[0] * x20[0] + x10[1] * x20[1] + x10[2] * x20[2]) / (l10 * l20));
+                    cotw[e] += -0.5 * (1.0 / std::tan(th));
+                }
+            }
+            for (int i = 0; i < m.nv; ++i) {
+                int g = o + i;
+                massD[g] = area[i] * m.density;
+                invMass[g] = (T)(1.0 / massD[g]);
+                bendArea[g] = area[i] * m.k_bend;
+                strainD[g] = m.k_stretch;
+            }
+            for (int i = 0; i < m.nv; ++i) {
+                int g = o + i;
+                int deg = (int)t.point_edges[i].size();
+                lOff[g] = (int)lNbr.size();
+                lNum[g] = deg + 1;
+                std::vector<double> lbo(deg + 1, 0.0);
+                std::vector<int> nb(deg + 1);
+                std::vector<double> rl(deg + 1, 0.0);
+                nb[0] = g;
+                double sum = 0.0;
+                std::vector<std::array<double, 3>> qq(deg + 1);
+                qq[0] = {P(i, 0), P(i, 1), P(i, 2)};
+                for (int k = 0; k < deg; ++k) {
+                    int e = t.point_edges[i][k];
+                    int ve = (t.edges[e][0] == i) ? t.edges[e][1] : t.edges[e][0];
+                    nb[k + 1] = ve + o;
+                    double d[3] = {P(i, 0) - P(ve, 0), P(i, 1) - P(ve, 1), P(i, 2) - P(ve, 2)};
+                    rl[k + 1] = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                    double ew = cotw[e] / area[i];
+                    sum += ew;
+                    lbo[k + 1] = ew;
+                    qq[k + 1] = {P(ve, 0), P(ve, 1), P(ve, 2)};
+                }
+                lbo[0] = -sum;
+                double cv[3] = {0, 0, 0};
+                for (int k = 0; k < deg + 1; ++k)
+                    for (int a = 0; a < 3; ++a) cv[a] += lbo[k] * qq[k][a];
+                curvNorm[g] = (T)std::sqrt(cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2]);
+                for (int k = 0; k < deg + 1; ++k) {
+                    lNbr.push_back(nb[k]);
+                    lStrain.push_back((T)m.k_stretch);
+                    lRest.push_back((T)rl[k]);
+                    lLbo.push_back((T)lbo[k]);
+                    lBend.push_back((T)(lbo[k] * m.k_bend * area[i]));
+                }
+                lboD[g] = lbo;
+            }
+            for (int p : m.pins) {
+                if (p < 0 || p >= m.nv) return PDIPC_ERR_ARG;
+                if (pinFlag[o + p] == -1) {
+                    pinFlag[o + p] = (int)pinStiff.size();
+                    pinStiff.push_back((T)m.k_pin);
+                }
+            }
+        }
+        // transposed bending coefficient: bendT(i, s) = bend_{k}(slot of i in k's list), k = N(i)[s]
+        lBendT.assign(lNbr.size(), T(0));
+        for (int i = 0; i < nsim; ++i) {
+            for (int s = 0; s < lNum[i]; ++s) {
+                int k = lNbr[lOff[i] + s];
+                int pos = -1;
+                for (int r = 0; r < lNum[k]; ++r)
+                    if (lNbr[lOff[k] + r] == i) { pos = r; break; }
+                if (pos < 0) return PDIPC_ERR_ARG;
+                lBendT[lOff[i] + s] = lBend[lOff[k] + pos];
+            }
+        }
+        for (int i = 0; i < nsim; ++i)
+            grav[3 * (size_t)i + 1] = (T)prm.gravity * (T)massD[i];
+        // --- system matrix (setupHessMat, PdIpcSimulator.cpp:270-414) ---
+        std::vector<std::map<int, double>> rows(nsim);
+        std::vector<double> diagE(nsim, 0.0);
+        for (int i = 0; i < nsim; ++i)
+            if (pinFlag[i] >= 0) diagE[i] += (double)pinStiff[pinFlag[i]];
+        for (int i = 0; i < nsim; ++i) {
+            double k = strainD[i];
+            for (int s = 1; s < lNum[i]; ++s) {
+                int j = lNbr[lOff[i] + s];
+                diagE[i] += k;
+                rows[i][j] -= k;
+            }
+        }
+        for (int i = 0; i < nsim; ++i) {
+            int n = lNum[i];
+            for (int r = 0; r < n; ++r)
+                for (int c = 0; c < n; ++c) {
+                    int a = lNbr[lOff[i] + r], b = lNbr[lOff[i] + c];
+                    double v = bendArea[i] * lboD[i][r] * lboD[i][c];
+                    if (a == b) diagE[a] += v;
+                    else rows[a][b] += v;
+                }
+        }
+        Delastic.assign(nsim, T(0));
+        for (int i = 0; i < nsim; ++i) Delastic[i] = (T)diagE[i];
+        nPtr.assign(nsim + 1, 0);
+        nCol.clear(); nVal.clear();
+        for (int i = 0; i < nsim; ++i) {
+            for (auto& kv : rows[i]) {
+                if (std::fabs(kv.second) < 1e-12) continue;  // IG drop, cpp:640-669
+                nCol.push_back(kv.first);
+                nVal.push_back((T)(-kv.second));
+            }
+            nPtr[i + 1] = (int)nCol.size();
+        }
+        if (global_form == 0) build_r2_tables();
+        // --- state ---
+        X0.assign(3 * (size_t)nsim, T(0));
+        V.assign(3 * (size_t)nsim, T(0));
+        Xold = X;
+        Xrest_all = X;
+        dir.assign(3 * (size_t)ntot, T(0));
+        rhs0.assign(3 * (size_t)nsim, T(0));
+        rhs.assign(3 * (size_t)nsim, T(0));
+        Dinert.assign(nsim, T(0));
+        D.assign(nsim, T(0));
+        collDiag.assign(ntot, T(0));
+        collRhs.assign(3 * (size_t)ntot, T(0));
+        collMass.assign(ntot, (TC)prm.static_mass);
+        for (int i = 0; i < nsim; ++i) collMass[i] = (TC)(T)massD[i];
+        // --- collision topology (gpuCollisionInit cpp:1151-1504) ---
+        faces.clear(); edges.clear();
+        pFaces.clear(); pPoints.clear(); pEdges.clear(); pAll.clear(); pStatic.clear();
+        for (int mi : morder) {
+            Topology& t = topo[mi];
+            int o = voff[mi], fo2 = foff[mi], eo2 = eoff[mi];
+            for (auto& f : t.faces) faces.push_back({f[0] + o, f[1] + o, f[2] + o});
+            for (auto& e : t.edges) edges.push_back({e[0] + o, e[1] + o});
+            for (auto& p : t.patches) {
+                std::set<int> es, ps, xs;
+                std::vector<int> fl;
+                for (int f : p) {
+                    fl.push_back(f + fo2);
+                    for (int e : t.face_owned_edges[f]) es.insert(e + eo2);
+                    for (int q : t.face_owned_points[f]) ps.insert(q + o);
+                    for (int k = 0; k < 3; ++k) xs.insert(t.faces[f][k] + o);
+                }
+                pFaces.push_back(fl);
+                pEdges.emplace_back(es.begin(), es.end());
+                pPoints.emplace_back(ps.begin(), ps.end());
+                pAll.emplace_back(xs.begin(), xs.end());
+                pStatic.push_back(models[mi].is_static ? 1 : 0);
+            }
+        }
+        npatch = (int)pFaces.size();
+        build_tree();
+        st = pdipc_stats{};
+        st.n_sim = nsim;
+        st.n_total = ntot;
+        st.n_patches = npatch;
+        initialized = true;
+        return PDIPC_OK;
+    }
+
+    // R1/R2 tables of the reference (gpuSolverInit cpp:640-882): R2 = R1*R1
+    // sparsity, entries |v|<1e-12 dropped, per entry the list of path terms
+    // N_ik*N_jk (|.|<1e-12 dropped), const-order flag (j==i) and first-order
+    // link (j in R1 row i).
+    void build_r2_tables() {
+        std::vector<std::map<int, int>> rowpos(nsim);
+        for (int i = 0; i < nsim; ++i)
+            for (int e = nPtr[i]; e < nPtr[i + 1]; ++e) rowpos[i][nCol[e]] = e;
+        r2Ptr.assign(nsim + 1, 0);
+        r2Col.clear(); r2Const.clear(); r2First.clear(); pathPtr.clear(); pathK.clear(); pathA.clear();
+        pathPtr.push_back(0);
+        for (int i = 0; i < nsim; ++i) {
+            std::map<int, double> acc;
+            for (int e = nPtr[i]; e < nPtr[i + 1]; ++e) {
+                int k = nCol[e];
+                double nik = (double)nVal[e];
+                for (int f = nPtr[k]; f < nPtr[k + 1]; ++f) acc[nCol[f]] += nik * (double)nVal[f];
+            }
+            for (auto& kv : acc) {
+                if (std::fabs(kv.second) < 1e-12) continue;
+                int j = kv.first;
+                // paths k ascending: k in R1 row i and in R1 row j
+                std::vector<std::pair<int, double>> paths;
+                for (int e = nPtr[i]; e < nPtr[i + 1]; ++e) {
+                    int k = nCol[e];
+                    auto it = rowpos[j].find(k);
+                    if (it == rowpos[j].end()) continue;
+                    double a = (double)nVal[e] * (double)nVal[it->second];
+                    if (std::fabs(a) < 1e-12) continue;
+                    paths.push_back({k, a});
+                }
+                if (paths.empty()) continue;
+                r2Col.push_back(j);
+                r2Const.push_back(j == i ? 1 : 0);
+                auto itf = rowpos[i].find(j);
+                r2First.push_back(itf == rowpos[i].end() ? -1 : itf->second);
+                for (auto& pk : paths) { pathK.push_back(pk.first); pathA.push_back((T)pk.second); }
+                pathPtr.push_back((int)pathK.size());
+            }
+            r2Ptr[i + 1] = (int)r2Col.size();
+        }
+        r2Val.assign(r2Col.size(), T(0));
+        r1Op.assign(nCol.size(), T(0));
+        firstTerm.assign(3 * (size_t)nsim, T(0));
+    }
+
+    // Patch tree of AipcBvhs::init (AipcBvhs.cpp:134-213): centres of the
+    // initial (unswept, inflated) patch boxes, centred, scaled if wider than
+    // 100, times 1000, truncated, Morton-coded, stably sorted; heap-indexed
+    // median split with children 2n, 2n+1.
+    void build_tree() {
+        T infl = (T)(prm.inflation_radius < 0 ? 0.5 * prm.dhat : prm.inflation_radius);
+        std::vector<std::array<T, 6>> box(npatch);
+        for (int p = 0; p < npatch; ++p) {
+            std::array<T, 6> b;
+            for (int k = 0; k < 3; ++k) { b[k] = std::numeric_limits<T>::infinity(); b[k + 3] = -b[k]; }
+            for (int v : pAll[p])
+                for (int k = 0; k < 3; ++k) {
+                    b[k] = std::min(b[k], (T)(X[3 * (size_t)v + k] - infl));
+                    b[k + 3] = std::max(b[k + 3], (T)(X[3 * (size_t)v + k] + infl));
+                }
+            box[p] = b;
+        }
+        morton.assign(npatch, 0);
+        order.resize(npatch);
+        if (npatch == 0) { nodeElem.clear(); nodeBox.clear(); patchNode.clear(); return; }
+        std::vector<std::array<T, 3>> c(npatch);
+        T vmin[3], vmax[3];
+        for (int k = 0; k < 3; ++k) { vmin[k] = std::numeric_limits<T>::infinity(); vmax[k] = -vmin[k]; }
+        for (int p = 0; p < npatch; ++p)
+            for (int k = 0; k < 3; ++k) {
+                c[p][k] = (box[p][k] + box[p][k + 3]) / T(2);
+                vmin[k] = std::min(vmin[k], c[p][k]);
+                vmax[k] = std::max(vmax[k], c[p][k]);
+            }
+        T ctr[3];
+        for (int k = 0; k < 3; ++k) ctr[k] = (vmin[k] + vmax[k]) / T(2);
+        T scale = T(0);
+        for (int k = 0; k < 3; ++k) scale = std::max(scale, (T)std::fabs(vmax[k] - ctr[k]));
+        for (int p = 0; p < npatch; ++p) {
+            int q[3];
+            for (int k = 0; k < 3; ++k) {
+                T v = c[p][k] - ctr[k];
+                if (scale > T(100)) v = v / scale;
+                q[k] = (int)(v * T(1000));
+            }
+            morton[p] = morton63(q[0], q[1], q[2]);
+        }
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return morton[a] < morton[b]; });
+        int maxn = max_node(1, 0, npatch);
+        nodeElem.assign(maxn + 1, -2);
+        nodeBox.assign(maxn + 1, std::array<T, 6>{});
+        patchNode.assign(npatch, -1);
+        init_rec(1, 0, npatch);
+    }
+    int max_node(int n, int b, int e) {
+        if (b + 1 == e) return n;
+        int m = b + (e - b) / 2;
+        return std::max(max_node(2 * n, b, m), max_node(2 * n + 1, m, e));
+    }
+    void init_rec(int n, int b, int e) {
+        if (b + 1 == e) {
+            nodeElem[n] = order[b];
+            patchNode[order[b]] = n;
+            return;
+        }
+        int m = b + (e - b) / 2;
+        init_rec(2 * n, b, m);
+        init_rec(2 * n + 1, m, e);
+        nodeElem[n] = -1;
+    }
+
+    // ---------------- broad phase (gpuCcdCulling cpp:1799-1869) ----------------
+    void patch_boxes(const std::vector<T>& xo, const std::vector<T>& dx, std::vector<std::array<T, 6>>& pb) {
+        T infl = (T)(prm.inflation_radius < 0 ? 0.5 * prm.dhat : prm.inflation_radius);
+        pb.resize(npatch);
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (int p = 0; p < npatch; ++p) {
+            std::array<T, 6> b;
+            for (int k = 0; k < 3; ++k) { b[k] = std::numeric_limits<T>::max(); b[k + 3] = -std::numeric_limits<T>::max(); }
+            for (int f : pFaces[p]) {
+                // getFaceBbox with displacement (PdIpcGpuFunc.cu:1350-1375)
+                for (int k = 0; k < 3; ++k) {
+                    T a0 = xo[3 * (size_t)faces[f][0] + k], a1 = xo[3 * (size_t)faces[f][1] + k], a2 = xo[3 * (size_t)faces[f][2] + k];
+                    T b0 = a0 + dx[3 * (size_t)faces[f][0] + k], b1 = a1 + dx[3 * (size_t)faces[f][1] + k], b2 = a2 + dx[3 * (size_t)faces[f][2] + k];
+                    T mn = std::min(std::min(std::min(a0, a1), a2), std::min(std::min(b0, b1), b2)) - infl;
+                    T mx = std::max(std::max(std::max(a0, a1), a2), std::max(std::max(b0, b1), b2)) + infl;
+                    b[k] = std::min(b[k], mn);
+                    b[k + 3] = std::max(b[k + 3], mx);
+                }
+            }
+            pb[p] = b;
+        }
+    }
+    static bool overlap(const std::array<T, 6>& a, const std::array<T, 6>& b) {
+        if (a[3] < b[0] || b[3] < a[0]) return false;
+        if (a[4] < b[1] || b[4] < a[1]) return false;
+        if (a[5] < b[2] || b[5] < a[2]) return false;
+        return true;
+    }
+    void refit(const std::vector<std::array<T, 6>>& pb) {
+        for (int n = (int)nodeElem.size() - 1; n >= 1; --n) {
+            if (nodeElem[n] >= 0) nodeBox[n] = pb[nodeElem[n]];
+            else if (nodeElem[n] == -1) {
+                for (int k = 0; k < 3; ++k) {
+                    nodeBox[n][k] = std::min(nodeBox[2 * n][k], nodeBox[2 * n + 1][k]);
+                    nodeBox[n][k + 3] = std::max(nodeBox[2 * n][k + 3], nodeBox[2 * n + 1][k + 3]);
+                }
+            }
+        }
+    }
+    // traverseIterative (PdIpcGpuFunc.cu:1628-1697): reports (q, p) with q < p.
+    void traverse(int q, std::vector<std::array<int, 2>>& out) {
+        const auto& qb = nodeBox[patchNode[q]];
+        int stack[128];
+        int sp = 0;
+        stack[sp++] = 0;
+        int node = 1;
+        int nn = (int)nodeElem.size();
+        if (nn <= 1) return;
+        if (nodeElem[1] >= 0) return;  // single patch
+        do {
+            int cl = 2 * node, cr = cl + 1;
+            bool ol = cl < nn && nodeElem[cl] != -2 && overlap(qb, nodeBox[cl]);
+            bool orr = cr < nn && nodeElem[cr] != -2 && overlap(qb, nodeBox[cr]);
+            if (ol && nodeElem[cl] >= 0 && q < nodeElem[cl]) out.push_back({q, nodeElem[cl]});
+            if (orr && nodeElem[cr] >= 0 && q < nodeElem[cr]) out.push_back({q, nodeElem[cr]});
+            bool tl = ol && nodeElem[cl] == -1, tr = orr && nodeElem[cr] == -1;
+            if (!tl && !tr) node = stack[--sp];
+            else {
+                node = tl ? cl : cr;
+                if (tl && tr) stack[sp++] = cr;
+            }
+        } while (node != 0);
+    }
+    void broadphase(const std::vector<T>& xo, const std::vector<T>& dx) {
+        std::vector<std::array<T, 6>> pb;
+        patch_boxes(xo, dx, pb);
+        refit(pb);
+        std::vector<std::vector<std::array<int, 2>>> per(npatch);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads)
+        for (int q = 0; q < npatch; ++q) traverse(q, per[q]);
+        pairs.clear();
+        for (int q = 0; q < npatch; ++q) {
+            std::sort(per[q].begin(), per[q].end());
+            for (auto& pr : per[q])
+                if (!(pStatic[pr[0]] && pStatic[pr[1]])) pairs.push_back(pr);
+        }
+        // expansion (getCcdPotentialICPairsListKernel, PdIpcGpuFunc.cu:1838-1948)
+        pt.clear();
+        ee.clear();
+        for (auto& pr : pairs) {
+            int A = pr[0], B = pr[1];
+            for (int v : pPoints[A])
+                for (int f : pFaces[B]) pt.push_back({v, faces[f][0], faces[f][1], faces[f][2]});
+            for (int v : pPoints[B])
+                for (int f : pFaces[A]) pt.push_back({v, faces[f][0], faces[f][1], faces[f][2]});
+            for (int a : pEdges[A])
+                for (int b : pEdges[B]) ee.push_back({edges[a][0], edges[a][1], edges[b][0], edges[b][1]});
+        }
+        st.patch_pairs = (i64)pairs.size();
+        st.pt_candidates = (i64)pt.size();
+        st.ee_candidates = (i64)ee.size();
+    }
+
+    // ---------------- geometry (PdIpcGpuFunc.cu:2152-2292) ----------------
+    static TC dot3(const TC* a, const TC* b) { TC s = 0; for (int k = 0; k < 3; ++k) s += a[k] * b[k]; return s; }
+    static void sub3(const TC* a, const TC* b, TC* r) { for (int k = 0; k < 3; ++k) r[k] = a[k] - b[k]; }
+    static void cross3(const TC* a, const TC* b, TC* r) {
+        r[0] = a[1] * b[2] - b[1] * a[2];
+        r[1] = a[2] * b[0] - b[2] * a[0];
+        r[2] = a[0] * b[1] - b[0] * a[1];
+    }
+    static TC vtx_edge_sq(const TC* v, const TC* ea, const TC* eb, TC* r, TC* d) {
+        TC va[3], ba[3];
+        sub3(v, ea, va); sub3(eb, ea, ba);
+        TC vb = dot3(va, ba), bb = dot3(ba, ba);
+        if (vb < 0) *r = 0; else if (vb > bb) *r = 1; else *r = vb / bb;
+        for (int k = 0; k < 3; ++k) d[k] = v[k] - (ea[k] * ((TC)1.0 - *r) + eb[k] * *r);
+        return dot3(d, d);
+    }
+    static TC edge_edge_sq(const TC* xi, const TC* xj, const TC* xa, const TC* xb, TC* r, TC* s, TC* d) {
+        TC xba[3], xji[3], xai[3], tmp[3];
+        sub3(xb, xa, xba); sub3(xj, xi, xji); sub3(xa, xi, xai);
+        cross3(xji, xba, d);
+        TC nn = dot3(d, d);
+        cross3(xai, xji, tmp);
+        TC w_aiji = dot3(d, tmp);
+        cross3(xai, xba, tmp);
+        TC w_aiba = dot3(d, tmp);
+        if (nn > (TC)1e-24f && w_aiji >= 0 && w_aiji <= nn && w_aiba >= 0 && w_aiba <= nn) {
+            *r = w_aiba / nn;
+            *s = w_aiji / nn;
+        } else {
+            TC best = (TC)999999999, dd, v, nd[3];
+            if (w_aiba < 0 && ((dd = vtx_edge_sq(xi, xa, xb, &v, nd)) < best)) { best = dd; *r = 0; *s = v; }
+            if (w_aiba > nn && ((dd = vtx_edge_sq(xj, xa, xb, &v, nd)) < best)) { best = dd; *r = 1; *s = v; }
+            if (w_aiji < 0 && ((dd = vtx_edge_sq(xa, xi, xj, &v, nd)) < best)) { best = dd; *r = v; *s = 0; }
+            if (w_aiji > nn && ((dd = vtx_edge_sq(xb, xi, xj, &v, nd)) < best)) { best = dd; *r = v; *s = 1; }
+        }
+        for (int k = 0; k < 3; ++k)
+            d[k] = xi[k] * (1 - *r) + xj[k] * *r - xa[k] * ((TC)1.0 - *s) - xb[k] * *s;
+        return dot3(d, d);
+    }
+    static TC vtx_tri(const TC* xi, const TC* xa, const TC* xb, const TC* xc, TC* ba, TC* bb, TC* bc, TC* d) {
+        TC xba[3], xca[3], xia[3], tmp[3];
+        sub3(xb, xa, xba); sub3(xc, xa, xca); sub3(xi, xa, xia);
+        cross3(xba, xca, d);
+        TC nn = dot3(d, d);
+        cross3(xia, xca, tmp);
+        TC w_iaca = dot3(d, tmp);
+        cross3(xba, xia, tmp);
+        TC w_baia = dot3(d, tmp);
+        if (nn > (TC)1e-24f && w_iaca >= 0 && w_baia >= 0 && nn - w_iaca - w_baia >= 0) {
+            *bb = w_iaca / nn;
+            *bc = w_baia / nn;
+            *ba = 1 - *bb - *bc;
+        } else {
+            TC best = (TC)999999999, r, dd, N[3];
+            if (nn - w_iaca - w_baia < 0 && ((dd = vtx_edge_sq(xi, xb, xc, &r, N)) < best)) { best = dd; *bb = 1 - r; *bc = r; *ba = 0; }
+            if (w_iaca < 0 && ((dd = vtx_edge_sq(xi, xa, xc, &r, N)) < best)) { best = dd; *bb = 0; *bc = r; *ba = 1 - *bb - *bc; }
+            if (w_baia < 0 && ((dd = vtx_edge_sq(xi, xa, xb, &r, N)) < best)) { best = dd; *bb = r; *bc = 0; *ba = 1 - *bb - *bc; }
+        }
+        for (int k = 0; k < 3; ++k) d[k] = xi[k] - xa[k] * *ba - xb[k] * *bb - xc[k] * *bc;
+        return dot3(d, d);
+    }
+    static TC mn3(TC a, TC b, TC c) { return std::min(std::min(a, b), c); }
+    static TC mx3(TC a, TC b, TC c) { return std::max(std::max(a, b), c); }
+    static bool pt_ccd_broad(const TC* p, const TC* t0, const TC* t1, const TC* t2, const TC* dp, const TC* d0,
+                             const TC* d1, const TC* d2, TC dist) {
+        for (int k = 0; k < 3; ++k) {
+            TC tmin = mn3(t0[k], t1[k], t2[k]);
+            tmin = mn3(tmin, t0[k] + d0[k], t1[k] + d1[k]);
+            tmin = std::min(tmin, t2[k] + d2[k]);
+            TC tmax = mx3(t0[k], t1[k], t2[k]);
+            tmax = mx3(tmax, t0[k] + d0[k], t1[k] + d1[k]);
+            tmax = std::max(tmax, t2[k] + d2[k]);
+            TC pmin = std::min(p[k], p[k] + dp[k]), pmax = std::max(p[k], p[k] + dp[k]);
+            if ((pmin - tmax) > dist || (tmin - pmax) > dist) return false;
+        }
+        return true;
+    }
+    static bool ee_ccd_broad(const TC* a0, const TC* a1, const TC* b0, const TC* b1, const TC* da0, const TC* da1,
+                             const TC* db0, const TC* db1, TC dist) {
+        for (int k = 0; k < 3; ++k) {
+            TC mina = std::min(a0[k], a0[k] + da0[k]); mina = std::min(mina, a1[k]); mina = std::min(mina, a1[k] + da1[k]);
+            TC maxa = std::max(a0[k], a0[k] + da0[k]); maxa = std::max(maxa, a1[k]); maxa = std::max(maxa, a1[k] + da1[k]);
+            TC minb = std::min(b0[k], b0[k] + db0[k]); minb = std::min(minb, b1[k]); minb = std::min(minb, b1[k] + db1[k]);
+            TC maxb = std::max(b0[k], b0[k] + db0[k]); maxb = std::max(maxb, b1[k]); maxb = std::max(maxb, b1[k] + db1[k]);
+            if ((mina - maxb) > dist || (minb - maxa) > dist) return false;
+        }
+        return true;
+    }
+    static TC sqn(const TC* a) { return dot3(a, a); }
+    // additive CCD, point-triangle (ccdVertexTriangleToi, PdIpcGpuFunc.cu:2460-2529)
+    TC ccd_pt(TC* x0, TC* d0, TC* x1, TC* d1, TC* x2, TC* d2, TC* x3, TC* d3) const {
+        TC mov[3];
+        for (int k = 0; k < 3; ++k) mov[k] = (d0[k] + d1[k] + d2[k] + d3[k]) / (TC)4.0;
+        for (int k = 0; k < 3; ++k) { d0[k] -= mov[k]; d1[k] -= mov[k]; d2[k] -= mov[k]; d3[k] -= mov[k]; }
+        TC m2 = std::max(sqn(d1), sqn(d2));
+        m2 = std::max(m2, sqn(d3));
+        TC maxd = std::sqrt(sqn(d0)) + std::sqrt(m2);
+        if (maxd == (TC)0.0) return 1;
+        TC a, b, c, dd[3];
+        TC d2c = vtx_tri(x0, x1, x2, x3, &a, &b, &c, dd);
+        TC dc = std::sqrt(d2c);
+        TC gap = (TC)prm.ccd_eta * dc;
+        TC toc = 0;
+        for (int i = 0; i < prm.ccd_max_iter; ++i) {
+            TC lb = (TC)0.9 * d2c / (dc * maxd);
+            for (int k = 0; k < 3; ++k) { x0[k] += lb * d0[k]; x1[k] += lb * d1[k]; x2[k] += lb * d2[k]; x3[k] += lb * d3[k]; }
+            d2c = vtx_tri(x0, x1, x2, x3, &a, &b, &c, dd);
+            dc = std::sqrt(d2c);
+            if (toc != (TC)0 && dc < gap) break;
+            toc += lb;
+            if (toc > (TC)1.0) { toc = 1; break; }
+        }
+        return toc;
+    }
+    static TC pp_min(const TC* x0, const TC* x1, const TC* x2, const TC* x3) {
+        auto d2 = [](const TC* a, const TC* b) {
+            return (a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]);
+        };
+        TC r = d2(x0, x2);
+        r = std::min(d2(x0, x3), r);
+        r = std::min(d2(x1, x2), r);
+        r = std::min(d2(x1, x3), r);
+        return r;
+    }
+    // additive CCD, edge-edge (ccdEdgeEdgeToi, PdIpcGpuFunc.cu:2531-2607)
+    TC ccd_ee(TC* x0, TC* d0, TC* x1, TC* d1, TC* x2, TC* d2, TC* x3, TC* d3) const {
+        TC mov[3];
+        for (int k = 0; k < 3; ++k) mov[k] = (d0[k] + d1[k] + d2[k] + d3[k]) / (TC)4.0;
+        for (int k = 0; k < 3; ++k) { d0[k] -= mov[k]; d1[k] -= mov[k]; d2[k] -= mov[k]; d3[k] -= mov[k]; }
+        TC m0 = std::max(sqn(d0), sqn(d1)), m1 = std::max(sqn(d2), sqn(d3));
+        TC maxd = std::sqrt(m0) + std::sqrt(m1);
+        if (maxd == 0) return 1;
+        TC r, s, dd[3];
+        TC d2c = edge_edge_sq(x0, x1, x2, x3, &r, &s, dd);
+        TC f = d2c;
+        if (f <= 0) { d2c = pp_min(x0, x1, x2, x3); f = d2c; }
+        TC dc = std::sqrt(d2c);
+        TC gap = (TC)prm.ccd_eta * f / dc;
+        TC toc = 0;
+        for (int i = 0; i < prm.ccd_max_iter; ++i) {
+            TC lb = (TC)0.9 * f / (dc * maxd);
+            for (int k = 0; k < 3; ++k) { x0[k] += lb * d0[k]; x1[k] += lb * d1[k]; x2[k] += lb * d2[k]; x3[k] += lb * d3[k]; }
+            d2c = edge_edge_sq(x0, x1, x2, x3, &r, &s, dd);
+            f = d2c;
+            if (f <= 0) { d2c = pp_min(x0, x1, x2, x3); f = d2c; }
+            dc = std::sqrt(d2c);
+            if (toc != (TC)0 && (f / dc) < gap) break;
+            toc += lb;
+            if (toc > (TC)1.0) { toc = 1; break; }
+        }
+        return toc;
+    }
+    void load4(const std::vector<T>& x, const std::array<int, 4>& ids, TC out[4][3]) const {
+        for (int j = 0; j < 4; ++j)
+            for (int k = 0; k < 3; ++k) out[j][k] = (TC)x[3 * (size_t)ids[j] + k];
+    }
+    // getImpactOfTimeKernel (PdIpcGpuFunc.cu:2610-2704); per-candidate toi (1 when skipped)
+    TC toi_pt_one(const std::array<int, 4>& c, const std::vector<T>& xa, const std::vector<T>& xb) const {
+        if (c[0] == c[1] || c[0] == c[2] || c[0] == c[3]) return 1;
+        TC p[4][3], q[4][3], d[4][3];
+        load4(xa, c, p);
+        load4(xb, c, q);
+        for (int j = 0; j < 4; ++j) for (int k = 0; k < 3; ++k) d[j][k] = q[j][k] - p[j][k];
+        if (!pt_ccd_broad(p[0], p[1], p[2], p[3], d[0], d[1], d[2], d[3], (TC)prm.ccd_slack)) return 1;
+        return ccd_pt(p[0], d[0], p[1], d[1], p[2], d[2], p[3], d[3]);
+    }
+    TC toi_ee_one(const std::array<int, 4>& c, const std::vector<T>& xa, const std::vector<T>& xb) const {
+        if (c[0] == c[2] || c[0] == c[3] || c[1] == c[2] || c[1] == c[3]) return 1;
+        TC p[4][3], q[4][3], d[4][3];
+        load4(xa, c, p);
+        load4(xb, c, q);
+        for (int j = 0; j < 4; ++j) for (int k = 0; k < 3; ++k) d[j][k] = q[j][k] - p[j][k];
+        if (!ee_ccd_broad(p[0], p[1], p[2], p[3], d[0], d[1], d[2], d[3], (TC)prm.ccd_slack)) return 1;
+        return ccd_ee(p[0], d[0], p[1], d[1], p[2], d[2], p[3], d[3]);
+    }
+    // global toi: min over candidates (NaN results never win, as in the
+    // reference's `toi < toiList` test), then times 0.98 if below 1.
+    TC global_toi(const std::vector<T>& xa, const std::vector<T>& xb, std::vector<double>* tp_, std::vector<double>* te_) {
+        TC best = 1;
+        i64 npt = (i64)pt.size(), nee = (i64)ee.size();
+        if (tp_) tp_->assign(npt, 1.0);
+        if (te_) te_->assign(nee, 1.0);
+#pragma omp parallel num_threads(threads)
+        {
+            TC lb = 1;
+#pragma omp for schedule(static) nowait
+            for (i64 i = 0; i < npt; ++i) {
+                TC t = toi_pt_one(pt[i], xa, xb);
+                if (tp_) (*tp_)[i] = (double)t;
+                if (t < lb) lb = t;
+            }
+#pragma omp for schedule(static) nowait
+            for (i64 i = 0; i < nee; ++i) {
+                TC t = toi_ee_one(ee[i], xa, xb);
+                if (te_) (*te_)[i] = (double)t;
+                if (t < lb) lb = t;
+            }
+#pragma omp critical
+            if (lb < best) best = lb;
+        }
+        if (best < (TC)1.0) best = (TC)((double)best * prm.toi_scale);
+        return best;
+    }
+
+    // setCollisionConstraintsKernel (PdIpcGpuFunc.cu:2756-2892)
+    struct Contrib { int ids[4]; TC w; TC tgt[4][3]; bool on; };
+    TC barrier(TC d2, TC dh2, TC kap) const {
+        TC e = 0;
+        if (d2 < dh2) {
+            TC t2 = d2 - dh2;
+            e = -kap * t2 * t2 * std::log(d2 / dh2) / (dh2 * dh2);
+        }
+        return e;
+    }
+    void contact_one(int type, const std::array<int, 4>& c, const std::vector<T>& x, Contrib& out) const {
+        out.on = false;
+        TC dh = (TC)(T)prm.dhat;
+        TC dh2 = (TC)((T)prm.dhat * (T)prm.dhat);
+        TC kap = (TC)(T)prm.kappa;
+        TC dt = (TC)(T)prm.time_step;
+        TC p[4][3];
+        load4(x, c, p);
+        TC d[3], dist2, mp, mq;
+        if (type == 0) {
+            if (c[0] == c[1] || c[0] == c[2] || c[0] == c[3]) return;
+            for (int k = 0; k < 3; ++k) {  // point_triangle_cd_broadphase
+                TC tmin = mn3(p[1][k], p[2][k], p[3][k]), tmax = mx3(p[1][k], p[2][k], p[3][k]);
+                if ((p[0][k] - tmax) > dh || (tmin - p[0][k]) > dh) return;
+            }
+            TC a, b, cc;
+            dist2 = vtx_tri(p[0], p[1], p[2], p[3], &a, &b, &cc, d);
+            if (dist2 >= dh2) return;
+            mp = collMass[c[0]];
+            mq = a * collMass[c[1]] + b * collMass[c[2]] + cc * collMass[c[3]];
+        } else {
+            if (c[0] == c[2] || c[0] == c[3] || c[1] == c[2] || c[1] == c[3]) return;
+            for (int k = 0; k < 3; ++k) {  // edge_edge_cd_broadphase
+                TC mina = std::min(p[0][k], p[1][k]), maxa = std::max(p[0][k], p[1][k]);
+                TC minb = std::min(p[2][k], p[3][k]), maxb = std::max(p[2][k], p[3][k]);
+                if ((mina - maxb) > dh || (minb - maxa) > dh) return;
+            }
+            TC r, s;
+            dist2 = edge_edge_sq(p[0], p[1], p[2], p[3], &r, &s, d);
+            if (dist2 >= dh2) return;
+            mp = (1 - r) * collMass[c[0]] + r * collMass[c[1]];
+            mq = (1 - s) * collMass[c[2]] + s * collMass[c[3]];
+        }
+        TC dist = std::sqrt(dist2);
+        TC w = barrier(dist2, dh2, kap) + std::min(mp, mq) / (dt * dt);
+        TC rp = mq / (mp + mq), rq = mp / (mp + mq);
+        TC len = std::sqrt(dot3(d, d));
+        for (int k = 0; k < 3; ++k) d[k] /= len;
+        dist = dh - dist;
+        TC dp = dist * rp, dq = dist * rq;
+        out.on = true;
+        out.w = w;
+        for (int j = 0; j < 4; ++j) out.ids[j] = c[j];
+        for (int k = 0; k < 3; ++k) {
+            if (type == 0) {
+                out.tgt[0][k] = w * (p[0][k] + dp * d[k]);
+                out.tgt[1][k] = w * (p[1][k] - dq * d[k]);
+                out.tgt[2][k] = w * (p[2][k] - dq * d[k]);
+                out.tgt[3][k] = w * (p[3][k] - dq * d[k]);
+            } else {
+                out.tgt[0][k] = w * (p[0][k] + dp * d[k]);
+                out.tgt[1][k] = w * (p[1][k] + dp * d[k]);
+                out.tgt[2][k] = w * (p[2][k] - dq * d[k]);
+                out.tgt[3][k] = w * (p[3][k] - dq * d[k]);
+            }
+        }
+    }
+    i64 contacts(const std::vector<T>& x) {
+        std::fill(collDiag.begin(), collDiag.end(), T(0));
+        std::fill(collRhs.begin(), collRhs.end(), T(0));
+        i64 npt = (i64)pt.size(), nee = (i64)ee.size();
+        std::vector<Contrib> cb(npt + nee);
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (i64 i = 0; i < npt + nee; ++i) {
+            if (i < npt) contact_one(0, pt[i], x, cb[i]);
+            else contact_one(1, ee[i - npt], x, cb[i]);
+        }
+        i64 active = 0;
+        for (i64 i = 0; i < npt + nee; ++i) {
+            if (!cb[i].on) continue;
+            ++active;
+            for (int j = 0; j < 4; ++j) {
+                int v = cb[i].ids[j];
+                collDiag[v] += (T)cb[i].w;
+                for (int k = 0; k < 3; ++k) collRhs[3 * (size_t)v + k] += (T)cb[i].tgt[j][k];
+            }
+        }
+        return active;
+    }
+
+    // ---------------- PD kernels ----------------
+    // predictiveKernel (PdIpcGpuFunc.cu:88-147)
+    void predict(T dt) {
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (int i = 0; i < nsim; ++i) {
+            if (pinFlag[i] != -1) { V[3 * i] = V[3 * i + 1] = V[3 * i + 2] = T(0); continue; }
+            T m = invMass[i] * dt;
+            T y[3];
+            for (int k = 0; k < 3; ++k) {
+                T v = V[3 * i + k] + m * grav[3 * i + k];
+                v = v * dt;
+                y[k] = v + X[3 * i + k];
+            }
+            T mm = (T)(1.0 / (double)(dt * m));
+            Dinert[i] = (T)(1.0 / (double)(invMass[i] * dt * dt));
+            for (int k = 0; k < 3; ++k) {
+                rhs0[3 * i + k] = mm * y[k];
+                X[3 * i + k] = y[k];
+            }
+        }
+    }
+    // solveClothPointsStrainAndBendingConstraintKernel (PdIpcGpuFunc.cu:627-728)
+    // in gather form, plus the contact rhs and solvePointsConstraintKernel (cu:764-790).
+    void local_rhs(std::vector<T>& aq) {
+        aq.assign(3 * (size_t)nsim, T(0));
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (int i = 0; i < nsim; ++i) {
+            int o = lOff[i], n = lNum[i];
+            T a[3];
+            for (int k = 0; k < 3; ++k) a[k] = X[3 * i + k] * lLbo[o];
+            for (int s = 1; s < n; ++s) {
+                int j = lNbr[o + s];
+                for (int k = 0; k < 3; ++k) a[k] += X[3 * (size_t)j + k] * lLbo[o + s];
+            }
+            T nrm = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+            if (nrm >= T(1e-10)) {
+                T c = curvNorm[i] / nrm;
+                for (int k = 0; k < 3; ++k) a[k] *= c;
+            }
+            for (int k = 0; k < 3; ++k) aq[3 * (size_t)i + k] = a[k];
+        }
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (int i = 0; i < nsim; ++i) {
+            int o = lOff[i], n = lNum[i];
+            T x[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
+            T tx[3] = {0, 0, 0};
+            T strain = lStrain[o];
+            for (int s = 1; s < n; ++s) {
+                int j = lNbr[o + s];
+                T d[3];
+                for (int k = 0; k < 3; ++k) d[k] = x[k] - X[3 * (size_t)j + k];
+                T cl = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                T rc = strain * (lRest[o + s] / cl);
+                for (int k = 0; k < 3; ++k) tx[k] += rc * d[k];
+            }
+            for (int k = 0; k < 3; ++k) tx[k] += lBend[o] * aq[3 * (size_t)i + k];
+            T r[3];
+            for (int k = 0; k < 3; ++k) r[k] = rhs0[3 * i + k] + tx[k];
+            for (int s = 1; s < n; ++s) {
+                int j = lNbr[o + s];
+                for (int k = 0; k < 3; ++k) r[k] += lBendT[o + s] * aq[3 * (size_t)j + k];
+            }
+            for (int k = 0; k < 3; ++k) r[k] += collRhs[3 * (size_t)i + k];
+            if (pinFlag[i] >= 0) {
+                T ks = pinStiff[pinFlag[i]];
+                for (int k = 0; k < 3; ++k) r[k] += ks * Xrest_all[3 * (size_t)i + k];
+            }
+            for (int k = 0; k < 3; ++k) rhs[3 * i + k] = r[k];
+        }
+    }
+    // J sweep: y_i = (1-w) x_i + w ((sum_j N_ij x_j + b_i) / D_i)
+    void jsweep(const std::vector<T>& x, std::vector<T>& y, T w, const std::vector<T>& invD) {
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (int i = 0; i < nsim; ++i) {
+            T s[3] = {0, 0, 0};
+            for (int e = nPtr[i]; e < nPtr[i + 1]; ++e) {
+                int j = nCol[e];
+                for (int k = 0; k < 3; ++k) s[k] += nVal[e] * x[3 * (size_t)j + k];
+            }
+            for (int k = 0; k < 3; ++k)
+                y[3 * (size_t)i + k] = (T(1) - w) * x[3 * (size_t)i + k] + w * ((s[k] + rhs[3 * (size_t)i + k]) * invD[i]);
+        }
+    }
+    void global_jj() {
+        T w = (T)prm.jacobi_relax;
+        std::vector<T> invD(nsim);
+        for (int i = 0; i < nsim; ++i) invD[i] = T(1) / D[i];
+        size_t n3 = 3 * (size_t)nsim;
+        std::vector<T>& Y = xsweepY;
+        std::vector<T>& B = xsweepA;
+        Y.resize(n3); B.resize(n3);
+        std::vector<T> xcur(X.begin(), X.begin() + n3);
+        // x1 = S(S(x0))
+        jsweep(xcur, Y, w, invD);
+        std::vector<T> prev = xcur;
+        jsweep(Y, B, w, invD);
+        xcur = B;
+        T rho = (T)prm.cheby_rho;
+        rho = rho * rho;
+        T om = omega_first(rho);
+        for (int it = 1; it < prm.cheby_iterations; ++it) {
+            jsweep(xcur, Y, w, invD);
+            jsweep(Y, B, w, invD);
+#pragma omp parallel for schedule(static) num_threads(threads)
+            for (size_t q = 0; q < n3; ++q) B[q] = om * (B[q] - prev[q]) + prev[q];
+            prev.swap(xcur);
+            xcur = B;
+            om = omega_next(rho, om);
+        }
+        std::copy(xcur.begin(), xcur.end(), X.begin());
+    }
+    // Reference form: updateSuperJacobiOperatorsHost (cu:976-1038) then
+    // chebyshevJacobiR2SolverHost (cu:1245-1346).
+    void update_r2_ops() {
+        T w = (T)prm.jacobi_relax;
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (int i = 0; i < nsim; ++i)
+            for (int e = nPtr[i]; e < nPtr[i + 1]; ++e) r1Op[e] = nVal[e] / D[i];
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (int i = 0; i < nsim; ++i) {
+            for (int q = r2Ptr[i]; q < r2Ptr[i + 1]; ++q) {
+                T v = 0;
+                for (int p = pathPtr[q]; p < pathPtr[q + 1]; ++p) v += pathA[p] / (D[i] * D[pathK[p]]);
+                v *= w * w;
+                v += (T(1) - w) * (T(1) - w) * (T)r2Const[q];
+                if (r2First[q] > -1) v += T(2) * (T(1) - w) * w * r1Op[r2First[q]];
+                r2Val[q] = v;
+            }
+        }
+    }
+    void global_r2() {
+        T w = (T)prm.jacobi_relax;
+        size_t n3 = 3 * (size_t)nsim;
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (int i = 0; i < nsim; ++i) {
+            for (int k = 0; k < 3; ++k) {
+                T v = 0;
+                for (int e = nPtr[i]; e < nPtr[i + 1]; ++e) {
+                    int j = nCol[e];
+                    v += r1Op[e] * (rhs[3 * (size_t)j + k] / D[j]);
+                }
+                firstTerm[3 * (size_t)i + k] = w * w * v + (T(2) - w) * w * rhs[3 * (size_t)i + k] / D[i];
+            }
+        }
+        std::vector<T>& A = xsweepA;
+        std::vector<T>& Bn = xsweepB;
+        A.resize(n3); Bn.resize(n3);
+        std::vector<T> prev(X.begin(), X.begin() + n3), cur(n3);
+        auto r2mul = [&](const std::vector<T>& x, std::vector<T>& y) {
+#pragma omp parallel for schedule(static) num_threads(threads)
+            for (int i = 0; i < nsim; ++i)
+                for (int k = 0; k < 3; ++k) {
+                    T v = 0;
+                    for (int q = r2Ptr[i]; q < r2Ptr[i + 1]; ++q) v += r2Val[q] * x[3 * (size_t)r2Col[q] + k];
+                    y[3 * (size_t)i + k] = v + firstTerm[3 * (size_t)i + k];
+                }
+        };
+        r2mul(prev, cur);
+        T rho = (T)prm.cheby_rho;
+        rho = rho * rho;
+        T om = omega_first(rho);
+        for (int it = 1; it < prm.cheby_iterations; ++it) {
+            r2mul(cur, Bn);
+#pragma omp parallel for schedule(static) num_threads(threads)
+            for (size_t q = 0; q < n3; ++q) Bn[q] = om * (Bn[q] - prev[q]) + prev[q];
+            prev.swap(cur);
+            cur.swap(Bn);
+            om = omega_next(rho, om);
+        }
+        std::copy(cur.begin(), cur.end(), X.begin());
+    }
+
+    void pd_solve() {
+        // sysDiag = elastic + inertial (+ collision): cpp:1556-1560
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (int i = 0; i < nsim; ++i) D[i] = (Delastic[i] + Dinert[i]) + collDiag[i];
+        if (global_form == 0) update_r2_ops();
+        std::vector<T> aq;
+        for (int lg = 0; lg < prm.lg_iterations; ++lg) {
+            local_rhs(aq);
+            if (global_form == 0) global_r2();
+            else global_jj();
+        }
+    }
+
+    // advance (PdIpcSimulator.cpp:1683-1796)
+    int step_once() {
+        T dt = (T)prm.time_step;
+        size_t n3 = 3 * (size_t)nsim;
+        std::copy(X.begin(), X.begin() + n3, X0.begin());
+        std::copy(X.begin(), X.begin() + n3, Xold.begin());
+        std::fill(collDiag.begin(), collDiag.end(), T(0));
+        std::fill(collRhs.begin(), collRhs.end(), T(0));
+        predict(dt);
+        int outer = 0;
+        int max_outer = prm.fixed_outer > 0 ? prm.fixed_outer : prm.max_outer;
+        for (; outer < max_outer; ++outer) {
+            pd_solve();
+            for (size_t q = 0; q < n3; ++q) dir[q] = X[q] - Xold[q];
+            if (outer == 0) broadphase(Xold, dir);
+            TC toi = global_toi(Xold, X, nullptr, nullptr);
+            T tt = (T)toi;
+            for (size_t q = 0; q < n3; ++q) X[q] = Xold[q] + tt * dir[q];
+            st.active_contacts = contacts(X);
+            double res = 0;
+            for (size_t q = 0; q < n3; ++q) res += (double)dir[q] * (double)dir[q];
+            st.last_toi = (double)toi;
+            st.last_residual = res;
+            for (size_t q = 0; q < n3; ++q)
+                if (!std::isfinite((double)X[q])) return PDIPC_ERR_NONFINITE;
+            if (prm.fixed_outer <= 0 && res < prm.outer_tol && outer > 0) { ++outer; break; }
+            std::copy(X.begin(), X.begin() + n3, Xold.begin());
+        }
+        // updateVelocityKernel (cu:262-281) with damping = 1 - dt
+        T damping = (T)(1.0 - (double)dt);
+        T invt = (T)((1.0 / (double)dt) * (double)damping);
+        for (size_t q = 0; q < n3; ++q) V[q] = (X[q] - X0[q]) * invt;
+        st.last_outer_iters = outer;
+        st.total_outer_iters += outer;
+        st.max_outer_iters = std::max(st.max_outer_iters, outer);
+        st.steps_done++;
+        return PDIPC_OK;
+    }
+    // Prediction then one outer iteration's PD solve without contact terms,
+    // from a caller state; the simulation state is restored afterwards.
+    int stage_pd(const double* Xin, const double* Vin, double* out) {
+        if (!initialized) return PDIPC_ERR_STATE;
+        std::vector<T> sx = X, sv = V;
+        for (size_t q = 0; q < X.size(); ++q) X[q] = (T)Xin[q];
+        for (size_t q = 0; q < V.size(); ++q) V[q] = (T)Vin[q];
+        std::fill(collDiag.begin(), collDiag.end(), T(0));
+        std::fill(collRhs.begin(), collRhs.end(), T(0));
+        predict((T)prm.time_step);
+        pd_solve();
+        for (size_t q = 0; q < X.size(); ++q) out[q] = (double)X[q];
+        X = sx;
+        V = sv;
+        return PDIPC_OK;
+    }
+    int step(int n) {
+        if (!initialized) return PDIPC_ERR_STATE;
+        st.max_outer_iters = 0;
+        st.total_outer_iters = 0;
+        for (int s = 0; s < n; ++s) {
+            int r = step_once();
+            if (r != PDIPC_OK) return r;
+        }
+        return PDIPC_OK;
+    }
+};
+
+struct Ctx {
+    int prec = 0;
+    std::unique_ptr<Sim<float, float>> f32;
+    std::unique_ptr<Sim<double, double>> f64;
+    std::unique_ptr<Sim<float, double>> mix;
+};
+
+template <typename F>
+static int dispatch(Ctx* c, F&& f) {
+    if (!c) return PDIPC_ERR_ARG;
+    if (c->f32) return f(*c->f32);
+    if (c->f64) return f(*c->f64);
+    if (c->mix) return f(*c->mix);
+    return PDIPC_ERR_STATE;
+}
+
+}  // namespace orc
+
+using orc::Ctx;
+
+extern "C" {
+
+void* orc_create(const pdipc_params* p, int global_form, int threads) {
+    if (!p) return nullptr;
+    Ctx* c = new Ctx();
+    c->prec = p->precision;
+    if (p->precision == PDIPC_PREC_FP64) c->f64.reset(new orc::Sim<double, double>(*p, global_form, threads));
+    else if (p->precision == PDIPC_PREC_MIXED) c->mix.reset(new orc::Sim<float, double>(*p, global_form, threads));
+    else c->f32.reset(new orc::Sim<float, float>(*p, global_form, threads));
+    return c;
+}
+
+void orc_destroy(void* h) { delete (Ctx*)h; }
+
+static int add_model(Ctx* c, const double* X, int nv, const int* F, int nf, bool st, double density,
+                     double ks, double kb, const int* pins, int npins, double kp, int pd) {
+    if (!X || !F || nv <= 0 || nf <= 0 || pd <= 0) return PDIPC_ERR_ARG;
+    for (int i = 0; i < 3 * nf; ++i)
+        if (F[i] < 0 || F[i] >= nv) return PDIPC_ERR_ARG;
+    orc::ModelIn m;
+    m.X.assign(X, X + 3 * (size_t)nv);
+    m.F.assign(F, F + 3 * (size_t)nf);
+    m.nv = nv; m.nf = nf; m.is_static = st;
+    m.density = density; m.k_stretch = ks; m.k_bend = kb; m.k_pin = kp; m.patch_dim = pd;
+    if (pins && npins > 0) m.pins.assign(pins, pins + npins);
+    return orc::dispatch(c, [&](auto& s) {
+        if (s.initialized) return (int)PDIPC_ERR_STATE;
+        s.models.push_back(m);
+        return (int)PDIPC_OK;
+    });
+}
+
+int orc_add_cloth(void* h, const double* X, int nv, const int* F, int nf, double density, double ks, double kb,
+                  const int* pins, int npins, double kp, int pd) {
+    return add_model((Ctx*)h, X, nv, F, nf, false, density, ks, kb, pins, npins, kp, pd);
+}
+int orc_add_static(void* h, const double* X, int nv, const int* F, int nf, int pd) {
+    return add_model((Ctx*)h, X, nv, F, nf, true, 0, 0, 0, nullptr, 0, 0, pd);
+}
+int orc_initialize(void* h) { return orc::dispatch((Ctx*)h, [](auto& s) { return s.initialize(); }); }
+int orc_step(void* h, int n) { return orc::dispatch((Ctx*)h, [&](auto& s) { return s.step(n); }); }
+
+int orc_get_positions(void* h, double* out) {
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        if (!s.initialized || !out) return (int)PDIPC_ERR_STATE;
+        for (size_t q = 0; q < s.X.size(); ++q) out[q] = (double)s.X[q];
+        return (int)PDIPC_OK;
+    });
+}
+int orc_get_velocities(void* h, double* out) {
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        if (!s.initialized || !out) return (int)PDIPC_ERR_STATE;
+        for (size_t q = 0; q < s.V.size(); ++q) out[q] = (double)s.V[q];
+        return (int)PDIPC_OK;
+    });
+}
+int orc_set_state(void* h, const double* X, const double* V) {
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        using T = typename std::remove_reference<decltype(s.X)>::type::value_type;
+        if (!s.initialized || !X) return (int)PDIPC_ERR_STATE;
+        for (size_t q = 0; q < s.X.size(); ++q) s.X[q] = (T)X[q];
+        if (V)
+            for (size_t q = 0; q < s.V.size(); ++q) s.V[q] = (T)V[q];
+        return (int)PDIPC_OK;
+    });
+}
+int orc_get_stats(void* h, pdipc_stats* out) {
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        if (!out) return (int)PDIPC_ERR_ARG;
+        *out = s.st;
+        return (int)PDIPC_OK;
+    });
+}
+
+// Broad phase on caller positions (same contract as pdipc_stage_broadphase).
+int orc_broadphase(void* h, const double* xo, const double* dx, int* pairs, long long cap_pairs, long long* n_pairs,
+                   int* pt, long long cap_pt, long long* n_pt, int* ee, long long cap_ee, long long* n_ee) {
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        using T = typename std::remove_reference<decltype(s.X)>::type::value_type;
+        if (!s.initialized) return (int)PDIPC_ERR_STATE;
+        std::vector<T> a(s.X.size()), b(s.X.size());
+        for (size_t q = 0; q < a.size(); ++q) { a[q] = (T)xo[q]; b[q] = (T)dx[q]; }
+        s.broadphase(a, b);
+        *n_pairs = (long long)s.pairs.size();
+        *n_pt = (long long)s.pt.size();
+        *n_ee = (long long)s.ee.size();
+        if ((long long)s.pairs.size() > cap_pairs || (long long)s.pt.size() > cap_pt || (long long)s.ee.size() > cap_ee)
+            return (int)PDIPC_ERR_OVERFLOW;
+        for (size_t i = 0; i < s.pairs.size(); ++i) { pairs[2 * i] = s.pairs[i][0]; pairs[2 * i + 1] = s.pairs[i][1]; }
+        for (size_t i = 0; i < s.pt.size(); ++i) for (int k = 0; k < 4; ++k) pt[4 * i + k] = s.pt[i][k];
+        for (size_t i = 0; i < s.ee.size(); ++i) for (int k = 0; k < 4; ++k) ee[4 * i + k] = s.ee[i][k];
+        return (int)PDIPC_OK;
+    });
+}
+int orc_morton(void* h, unsigned long long* codes, int* order, int cap) {
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        if (!s.initialized) return (int)PDIPC_ERR_STATE;
+        if (cap < s.npatch) return (int)PDIPC_ERR_OVERFLOW;
+        for (int i = 0; i < s.npatch; ++i) { codes[i] = s.morton[i]; order[i] = s.order[i]; }
+        return (int)PDIPC_OK;
+    });
+}
+int orc_toi(void* h, const double* x0, const double* x1, double* tpt, double* tee, double* tg) {
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        using T = typename std::remove_reference<decltype(s.X)>::type::value_type;
+        if (!s.initialized) return (int)PDIPC_ERR_STATE;
+        std::vector<T> a(s.X.size()), b(s.X.size());
+        for (size_t q = 0; q < a.size(); ++q) { a[q] = (T)x0[q]; b[q] = (T)x1[q]; }
+        std::vector<double> vp, ve;
+        double g = (double)s.global_toi(a, b, &vp, &ve);
+        if (tpt) std::copy(vp.begin(), vp.end(), tpt);
+        if (tee) std::copy(ve.begin(), ve.end(), tee);
+        if (tg) *tg = g;
+        return (int)PDIPC_OK;
+    });
+}
+int orc_contact(void* h, const double* x, double* diag, double* rhs, long long* n_active) {
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        using T = typename std::remove_reference<decltype(s.X)>::type::value_type;
+        if (!s.initialized) return (int)PDIPC_ERR_STATE;
+        std::vector<T> a(s.X.size());
+        for (size_t q = 0; q < a.size(); ++q) a[q] = (T)x[q];
+        long long na = s.contacts(a);
+        if (n_active) *n_active = na;
+        for (int i = 0; i < s.ntot; ++i) diag[i] = (double)s.collDiag[i];
+        for (size_t q = 0; q < s.collRhs.size(); ++q) rhs[q] = (double)s.collRhs[q];
+        return (int)PDIPC_OK;
+    });
+}
+
+int orc_stage_pd(void* h, const double* X, const double* V, double* out) {
+    return orc::dispatch((Ctx*)h, [&](auto& s) { return s.stage_pd(X, V, out); });
+}
+
+// Topology of one standalone mesh, for the known-answer tests on the
+// reference example's cached boundary.dat / patchInfo.dat.
+// edges_out: 2*ne ints (cap_e pairs); patch_faces/patch_off: faces per patch
+// (CSR, patch_off has npatch+1 entries, cap_p patches, cap_pf faces).
+int orc_mesh_topology(const double* X, int nv, const int* F, int nf, int patch_dim, int* edges_out, int cap_e,
+                      int* ne, int* patch_off, int cap_p, int* patch_faces, int cap_pf, int* np,
+                      int* owned_pts_off, int* owned_pts, int* owned_edges_off, int* owned_edges) {
+    orc::Topology t;
+    t.nv = nv;
+    t.nf = nf;
+    t.faces.resize(nf);
+    for (int f = 0; f < nf; ++f) t.faces[f] = {F[3 * f], F[3 * f + 1], F[3 * f + 2]};
+    orc::build_edges(t);
+    if (!orc::build_ownership(t)) return PDIPC_ERR_ARG;
+    std::vector<double> Xv(X, X + 3 * (size_t)nv);
+    orc::build_patches(t, Xv, patch_dim);
+    *ne = (int)t.edges.size();
+    *np = (int)t.patches.size();
+    if (*ne > cap_e || *np > cap_p) return PDIPC_ERR_OVERFLOW;
+    for (int e = 0; e < *ne; ++e) { edges_out[2 * e] = t.edges[e][0]; edges_out[2 * e + 1] = t.edges[e][1]; }
+    int q = 0;
+    patch_off[0] = 0;
+    for (int p = 0; p < *np; ++p) {
+        for (int f : t.patches[p]) {
+            if (q >= cap_pf) return PDIPC_ERR_OVERFLOW;
+            patch_faces[q++] = f;
+        }
+        patch_off[p + 1] = q;
+    }
+    if (owned_pts_off) {
+        int a = 0, b = 0;
+        owned_pts_off[0] = 0;
+        owned_edges_off[0] = 0;
+        for (int f = 0; f < nf; ++f) {
+            for (int v : t.face_owned_points[f]) owned_pts[a++] = v;
+            for (int e : t.face_owned_edges[f]) owned_edges[b++] = e;
+            owned_pts_off[f + 1] = a;
+            owned_edges_off[f + 1] = b;
+        }
+    }
+    return PDIPC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,631 @@
+// collision_kernels.cu — broad phase, CCD and contact projection of the
+// PD-IPC cloth step.
+//
+// Reference kernels replaced (Simulator/PD-IPC/PdIpcGpuFunc.cu):
+//   updateCcdPatchBboxesKernel :1407-1473          -> k_patch_boxes (one warp per patch)
+//   AipcBvhs::init (CPU, AipcBvhs.cpp:134-213)      -> k_init_boxes, k_center_scale, k_morton,
+//                                                      radix sort, k_karras (GPU LBVH build)
+//   updateBvhsBboxesKernel :1506-1561 (1 block)     -> k_refit (bottom-up, atomic arrival flags)
+//   findPatchsICPairsKernel :1699-1732 + thrust scan
+//   + fillCompactPotentialPatchPairListKernel       -> k_traverse (count, scan, write)
+//   computeCcdPatchICPairsVfeeNumKernel :1811 + scan
+//   + getCcdPotentialICPairsListKernel :1838-1948   -> k_pair_counts, k_expand
+//   getImpactOfTimeKernel :2610-2704 + cublasIsamin -> k_toi_* (atomic min, no host copy)
+//   setCollisionConstraintsKernel :2756-2892        -> k_contact_*
+//
+// The set of overlapping patch pairs does not depend on the tree's shape, so
+// the Karras tree reports exactly the pairs of the reference's median-split
+// heap tree over the same boxes.
+#include <cfloat>
+
+#include "geometry.cuh"
+#include "kernels.cuh"
+
+namespace pdipc {
+
+namespace {
+
+constexpr int kBlock = 256;
+inline int blocks_for(int64_t n, int b = kBlock) { return (int)std::max<int64_t>(1, (n + b - 1) / b); }
+inline int grid_cap(int64_t n, int b = kBlock, int cap = 152 * 16) {
+    return (int)std::min<int64_t>(cap, std::max<int64_t>(1, (n + b - 1) / b));
+}
+
+template <typename T>
+__device__ __forceinline__ T tmax_val();
+template <>
+__device__ __forceinline__ float tmax_val<float>() { return FLT_MAX; }
+template <>
+__device__ __forceinline__ double tmax_val<double>() { return DBL_MAX; }
+
+template <typename T>
+__device__ __forceinline__ void warp_box_reduce(T lo[3], T hi[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = warp_min(lo[k]);
+        hi[k] = warp_max(hi[k]);
+    }
+}
+
+// Swept, inflated patch AABB: per face min/max over x and x+dx of its three
+// vertices, minus/plus the inflation radius (getFaceBbox, cu:1350-1375), then
+// reduced over the patch's faces.
+template <typename T>
+__global__ void k_patch_boxes(int npatch, const int* __restrict__ pfPtr, const int* __restrict__ pfIdx,
+                              const int4* __restrict__ Faces, const V4<T>* __restrict__ X,
+                              const V4<T>* __restrict__ D, T infl, Box6<T>* __restrict__ out) {
+    const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (p >= npatch) return;
+    T lo[3] = {tmax_val<T>(), tmax_val<T>(), tmax_val<T>()};
+    T hi[3] = {-tmax_val<T>(), -tmax_val<T>(), -tmax_val<T>()};
+    const int b = pfPtr[p], e = pfPtr[p + 1];
+    for (int q = b + lane; q < e; q += 32) {
+        const int4 f = Faces[pfIdx[q]];
+        const int vv[3] = {f.x, f.y, f.z};
+        T a[3][3], c[3][3];
+        for (int j = 0; j < 3; ++j) {
+            const V4<T> x = ld4(X, vv[j]);
+            a[j][0] = x.x;
+            a[j][1] = x.y;
+            a[j][2] = x.z;
+            if (D) {
+                const V4<T> d = ld4(D, vv[j]);
+                c[j][0] = x.x + d.x;
+                c[j][1] = x.y + d.y;
+                c[j][2] = x.z + d.z;
+            } else {
+                c[j][0] = x.x;
+                c[j][1] = x.y;
+                c[j][2] = x.z;
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            T mn = dmin(dmin(dmin(a[0][k], a[1][k]), a[2][k]), dmin(dmin(c[0][k], c[1][k]), c[2][k])) - infl;
+            T mx = dmax(dmax(dmax(a[0][k], a[1][k]), a[2][k]), dmax(dmax(c[0][k], c[1][k]), c[2][k])) + infl;
+            lo[k] = dmin(lo[k], mn);
+            hi[k] = dmax(hi[k], mx);
+        }
+    }
+    warp_box_reduce(lo, hi);
+    if (lane == 0) {
+        Box6<T> bx;
+        for (int k = 0; k < 3; ++k) {
+            bx.lo[k] = lo[k];
+            bx.hi[k] = hi[k];
+        }
+        out[p] = bx;
+    }
+}
+
+// Init-time patch boxes over every vertex of the patch's faces, inflated
+// (gpuCollisionInit, cpp:1279-1292).
+template <typename T>
+__global__ void k_init_boxes(int npatch, const int* __restrict__ pxPtr, const int* __restrict__ pxIdx,
+                             const V4<T>* __restrict__ X, T infl, Box6<T>* __restrict__ out) {
+    const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (p >= npatch) return;
+    T lo[3] = {tmax_val<T>(), tmax_val<T>(), tmax_val<T>()};
+    T hi[3] = {-tmax_val<T>(), -tmax_val<T>(), -tmax_val<T>()};
+    for (int q = pxPtr[p] + lane; q < pxPtr[p + 1]; q += 32) {
+        const V4<T> x = ld4(X, pxIdx[q]);
+        const T xs[3] = {x.x, x.y, x.z};
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = dmin(lo[k], xs[k] - infl);
+            hi[k] = dmax(hi[k], xs[k] + infl);
+        }
+    }
+    warp_box_reduce(lo, hi);
+    if (lane == 0) {
+        Box6<T> bx;
+        for (int k = 0; k < 3; ++k) {
+            bx.lo[k] = lo[k];
+            bx.hi[k] = hi[k];
+        }
+        out[p] = bx;
+    }
+}
+
+// Centre of the box-centre bounds and the infinity-norm half extent
+// (AipcBvhs.cpp:140-160).  One block; init-time only.
+template <typename T>
+__global__ void k_center_scale(int npatch, const Box6<T>* __restrict__ box, T* __restrict__ cs) {
+    __shared__ T smn[3][32], smx[3][32];
+    T mn[3] = {tmax_val<T>(), tmax_val<T>(), tmax_val<T>()};
+    T mx[3] = {-tmax_val<T>(), -tmax_val<T>(), -tmax_val<T>()};
+    for (int p = threadIdx.x; p < npatch; p += blockDim.x) {
+        const Box6<T> b = box[p];
+        for (int k = 0; k < 3; ++k) {
+            const T c = (b.lo[k] + b.hi[k]) / T(2);
+            mn[k] = dmin(mn[k], c);
+            mx[k] = dmax(mx[k], c);
+        }
+    }
+    warp_box_reduce(mn, mx);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+        for (int k = 0; k < 3; ++k) {
+            smn[k][w] = mn[k];
+            smx[k][w] = mx[k];
+        }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = lane < nw ? smn[k][lane] : tmax_val<T>();
+            mx[k] = lane < nw ? smx[k][lane] : -tmax_val<T>();
+        }
+        warp_box_reduce(mn, mx);
+        if (lane == 0) {
+            T scale = T(0);
+            for (int k = 0; k < 3; ++k) {
+                const T c = (mn[k] + mx[k]) / T(2);
+                cs[k] = c;
+                scale = dmax(scale, fabs(mx[k] - c));
+            }
+            cs[3] = scale;
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned long long spread21(unsigned long long v) {
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+__device__ __forceinline__ unsigned long long q21(int a) {
+    long long s = (long long)a + (1ll << 20);
+    s = s < 0 ? 0 : (s > (1ll << 21) - 1 ? (1ll << 21) - 1 : s);
+    return (unsigned long long)s;
+}
+
+// Morton code of each patch centre: centred, divided by the half extent when
+// it exceeds 100, times 1000, truncated (AipcBvhs.cpp:162-183).
+template <typename T>
+__global__ void k_morton(int npatch, const Box6<T>* __restrict__ box, const T* __restrict__ cs,
+                         unsigned long long* __restrict__ codes, unsigned long long* __restrict__ keys,
+                         int* __restrict__ vals) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npatch) return;
+    const Box6<T> b = box[p];
+    const T scale = cs[3];
+    int q[3];
+    for (int k = 0; k < 3; ++k) {
+        T v = (b.lo[k] + b.hi[k]) / T(2) - cs[k];
+        if (scale > T(100)) v = v / scale;
+        q[k] = (int)(v * T(1000));
+    }
+    const unsigned long long c = spread21(q21(q[0])) | (spread21(q21(q[1])) << 1) | (spread21(q21(q[2])) << 2);
+    codes[p] = c;
+    keys[p] = c;
+    vals[p] = p;
+}
+
+__device__ __forceinline__ int kdelta(const unsigned long long* __restrict__ c, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const unsigned long long a = c[i], b = c[j];
+    if (a == b) return 64 + __clz(i ^ j);
+    return __clzll(a ^ b);
+}
+
+// Karras (2012) binary radix tree over the sorted codes; equal codes are
+// split by position.  Internal node i in [0, n-1), leaf k is node n-1+k.
+__global__ void k_karras(int n, const unsigned long long* __restrict__ c, int2* __restrict__ child,
+                         int* __restrict__ parent) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) parent[0] = -1;
+    if (i >= n - 1) return;
+    const int d = (kdelta(c, n, i, i + 1) - kdelta(c, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin_ = kdelta(c, n, i, i - d);
+    int lmax = 2;
+    while (kdelta(c, n, i, i + lmax * d) > dmin_) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (kdelta(c, n, i, i + (l + t) * d) > dmin_) l += t;
+    const int j = i + l * d;
+    const int dnode = kdelta(c, n, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (kdelta(c, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int gamma = i + s * d + min(d, 0);
+    const int left = (min(i, j) == gamma) ? (n - 1 + gamma) : gamma;
+    const int right = (max(i, j) == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
+    child[i] = make_int2(left, right);
+    parent[left] = i;
+    parent[right] = i;
+}
+
+template <typename T>
+__device__ __forceinline__ Box6<T> load_box_cg(const Box6<T>* p) {
+    Box6<T> b;
+    const T* q = reinterpret_cast<const T*>(p);
+    for (int k = 0; k < 3; ++k) {
+        b.lo[k] = __ldcg(q + k);
+        b.hi[k] = __ldcg(q + 3 + k);
+    }
+    return b;
+}
+
+// Bottom-up refit: the second thread to reach an internal node merges its
+// children and climbs on (replaces the single-block level sweep, cu:1506-1561).
+template <typename T>
+__global__ void k_refit(int n, const int* __restrict__ leafPatch, const Box6<T>* __restrict__ patchBox,
+                        Box6<T>* __restrict__ nodeBox, const int2* __restrict__ child,
+                        const int* __restrict__ parent, int* __restrict__ flag) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int node = n - 1 + k;
+    nodeBox[node] = patchBox[leafPatch[k]];
+    node = parent[node];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(flag + node, 1) == 0) return;
+        __threadfence();
+        const int2 ch = child[node];
+        const Box6<T> a = load_box_cg(nodeBox + ch.x), b = load_box_cg(nodeBox + ch.y);
+        Box6<T> u;
+        for (int q = 0; q < 3; ++q) {
+            u.lo[q] = dmin(a.lo[q], b.lo[q]);
+            u.hi[q] = dmax(a.hi[q], b.hi[q]);
+        }
+        nodeBox[node] = u;
+        node = parent[node];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ bool overlap(const Box6<T>& a, const Box6<T>& b) {
+    // checkOverlap (cu:1612-1625): closed intervals
+    if (a.hi[0] < b.lo[0] || b.hi[0] < a.lo[0]) return false;
+    if (a.hi[1] < b.lo[1] || b.hi[1] < a.lo[1]) return false;
+    if (a.hi[2] < b.lo[2] || b.hi[2] < a.lo[2]) return false;
+    return true;
+}
+
+constexpr int kStack = 64;
+
+// Per query patch q: every patch p > q whose box overlaps q's, skipping pairs
+// of two static patches (they cannot move or receive contact forces).
+template <typename T>
+__global__ void k_traverse(int n, const Box6<T>* __restrict__ patchBox, const Box6<T>* __restrict__ nodeBox,
+                           const int2* __restrict__ child, const int* __restrict__ leafPatch,
+                           const uint8_t* __restrict__ pStatic, int* __restrict__ counts,
+                           const int* __restrict__ offsets, int2* __restrict__ out, unsigned int* __restrict__ err) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    int cnt = 0;
+    if (n > 1) {
+        const Box6<T> qb = patchBox[q];
+        const bool qs = pStatic[q] != 0;
+        const int base = out ? offsets[q] : 0;
+        int stack[kStack];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            const int node = stack[--sp];
+            const int2 ch = child[node];
+            const int cc[2] = {ch.x, ch.y};
+            for (int h = 0; h < 2; ++h) {
+                const int c = cc[h];
+                if (!overlap(qb, nodeBox[c])) continue;
+                if (c >= n - 1) {
+                    const int p = leafPatch[c - (n - 1)];
+                    if (q < p && !(qs && pStatic[p])) {
+                        if (out) out[base + cnt] = make_int2(q, p);
+                        ++cnt;
+                    }
+                } else if (sp < kStack) {
+                    stack[sp++] = c;
+                } else {
+                    atomicOr(err, (unsigned int)kErrTraversalStack);
+                }
+            }
+        }
+    }
+    if (!out) counts[q] = cnt;
+}
+
+__global__ void k_pair_counts(int64_t npairs, const int2* __restrict__ pairs, const int* __restrict__ pfPtr,
+                              const int* __restrict__ ppPtr, const int* __restrict__ pePtr, int64_t* __restrict__ cpt,
+                              int64_t* __restrict__ cee) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npairs) return;
+    const int2 pr = pairs[t];
+    const int64_t fa = pfPtr[pr.x + 1] - pfPtr[pr.x], fb = pfPtr[pr.y + 1] - pfPtr[pr.y];
+    const int64_t va = ppPtr[pr.x + 1] - ppPtr[pr.x], vb = ppPtr[pr.y + 1] - ppPtr[pr.y];
+    const int64_t ea = pePtr[pr.x + 1] - pePtr[pr.x], eb = pePtr[pr.y + 1] - pePtr[pr.y];
+    cpt[t] = va * fb + vb * fa;
+    cee[t] = ea * eb;
+}
+
+// Expansion of one patch pair (A,B) per warp into point-triangle records
+// (points of A x faces of B, then points of B x faces of A) and edge-edge
+// records (edges of A x edges of B), point-major as in cu:1900-1945.
+__global__ void k_expand(int64_t npairs, const int2* __restrict__ pairs, const int* __restrict__ pfPtr,
+                         const int* __restrict__ pfIdx, const int* __restrict__ ppPtr, const int* __restrict__ ppIdx,
+                         const int* __restrict__ pePtr, const int* __restrict__ peIdx, const int4* __restrict__ Faces,
+                         const int2* __restrict__ Edges, const int64_t* __restrict__ opt,
+                         const int64_t* __restrict__ oee, int4* __restrict__ PT, int4* __restrict__ EE) {
+    const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (t >= npairs) return;
+    const int2 pr = pairs[t];
+    const int A = pr.x, B = pr.y;
+    const int fa0 = pfPtr[A], fa = pfPtr[A + 1] - fa0, fb0 = pfPtr[B], fb = pfPtr[B + 1] - fb0;
+    const int va0 = ppPtr[A], va = ppPtr[A + 1] - va0, vb0 = ppPtr[B], vb = ppPtr[B + 1] - vb0;
+    const int ea0 = pePtr[A], ea = pePtr[A + 1] - ea0, eb0 = pePtr[B], eb = pePtr[B + 1] - eb0;
+    const int64_t bp = opt[t], be = oee[t];
+    const int nab = va * fb, nba = vb * fa;
+    for (int id = lane; id < nab + nba; id += 32) {
+        int v, f;
+        if (id < nab) {
+            v = ppIdx[va0 + id / fb];
+            f = pfIdx[fb0 + id % fb];
+        } else {
+            const int id2 = id - nab;
+            v = ppIdx[vb0 + id2 / fa];
+            f = pfIdx[fa0 + id2 % fa];
+        }
+        const int4 F = Faces[f];
+        PT[bp + id] = make_int4(v, F.x, F.y, F.z);
+    }
+    for (int id = lane; id < ea * eb; id += 32) {
+        const int2 a = Edges[peIdx[ea0 + id / eb]], b = Edges[peIdx[eb0 + id % eb]];
+        EE[be + id] = make_int4(a.x, a.y, b.x, b.y);
+    }
+}
+
+template <typename T, typename TC>
+__device__ __forceinline__ void gather4(const V4<T>* __restrict__ X, const int ids[4], TC out[4][3]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const V4<T> v = ld4(X, ids[j]);
+        out[j][0] = (TC)v.x;
+        out[j][1] = (TC)v.y;
+        out[j][2] = (TC)v.z;
+    }
+}
+
+template <typename TC>
+__device__ __forceinline__ void block_min_to(TC v, TC* dst) {
+    __shared__ TC red[kBlock / 32];
+    v = warp_min(v);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        TC w = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : TC(1);
+        w = warp_min(w);
+        if (threadIdx.x == 0 && w < TC(1)) atomic_min_nonneg(dst, w);
+    }
+}
+
+// getImpactOfTimeKernel (cu:2610-2704): skip pairs sharing a vertex, swept-AABB
+// filter with slack, additive CCD; global minimum by integer atomicMin.
+template <typename T, typename TC, bool kPT>
+__global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restrict__ cand,
+                                                const V4<T>* __restrict__ X0, const V4<T>* __restrict__ X1,
+                                                TC slack, TC eta, int max_iter, TC* __restrict__ per,
+                                                TC* __restrict__ toi_min) {
+    TC local = TC(1);
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int4 c = cand[t];
+        const int ids[4] = {c.x, c.y, c.z, c.w};
+        TC toi = TC(1);
+        const bool shared = kPT ? (c.x == c.y || c.x == c.z || c.x == c.w)
+                                : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w);
+        if (!shared) {
+            TC x[4][3], dx[4][3];
+            gather4<T, TC>(X0, ids, x);
+            gather4<T, TC>(X1, ids, dx);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) dx[j][k] -= x[j][k];
+            if (kPT) {
+                if (geo::pt_ccd_broad<TC>(x, dx, slack)) toi = geo::ccd_pt<TC>(x, dx, eta, max_iter);
+            } else {
+                if (geo::ee_ccd_broad<TC>(x, dx, slack)) toi = geo::ccd_ee<TC>(x, dx, eta, max_iter);
+            }
+        }
+        if (per) per[t] = toi;
+        if (toi < local) local = toi;
+    }
+    block_min_to(local, toi_min);
+}
+
+template <typename T, typename TC>
+__global__ void k_toi_finalize(TC* __restrict__ toi_min, T* __restrict__ toi, double scale) {
+    const TC m = *toi_min;
+    const TC t = (m < TC(1)) ? (TC)((double)m * scale) : TC(1);
+    *toi = (T)t;
+    *toi_min = TC(1);
+}
+
+template <typename TC>
+struct ContactConsts {
+    TC dh, dh2, kappa, dt;
+};
+
+// setCollisionConstraintsKernel (cu:2756-2892): a pair closer than dhat adds
+// w = kappa b(d^2) + min(m_p, m_q)/dt^2 to the diagonal of its 4 vertices and
+// w * target to their right-hand side; targets push the pair apart to dhat
+// along the closest-point direction, split by the mass ratio.
+template <typename T, typename TC, bool kPT>
+__global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __restrict__ cand,
+                                                    const V4<T>* __restrict__ X, const TC* __restrict__ mass,
+                                                    ContactConsts<TC> cc, T* __restrict__ diag,
+                                                    V4<T>* __restrict__ rhs, unsigned long long* __restrict__ active) {
+    unsigned int my = 0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int4 c = cand[t];
+        const int ids[4] = {c.x, c.y, c.z, c.w};
+        if (kPT ? (c.x == c.y || c.x == c.z || c.x == c.w) : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w))
+            continue;
+        TC p[4][3];
+        gather4<T, TC>(X, ids, p);
+        TC d[3], dist2, mp, mq;
+        bool far = false;
+        if (kPT) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {  // point_triangle_cd_broadphase (cu:2328-2345)
+                const TC tmin = geo::mn3(p[1][k], p[2][k], p[3][k]), tmax = geo::mx3(p[1][k], p[2][k], p[3][k]);
+                if ((p[0][k] - tmax) > cc.dh || (tmin - p[0][k]) > cc.dh) far = true;
+            }
+            if (far) continue;
+            TC a, b, cq;
+            dist2 = geo::vtx_tri(p[0], p[1], p[2], p[3], &a, &b, &cq, d);
+            if (dist2 >= cc.dh2) continue;
+            mp = mass[c.x];
+            mq = a * mass[c.y] + b * mass[c.z] + cq * mass[c.w];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {  // edge_edge_cd_broadphase (cu:2405-2424)
+                const TC mina = dmin(p[0][k], p[1][k]), maxa = dmax(p[0][k], p[1][k]);
+                const TC minb = dmin(p[2][k], p[3][k]), maxb = dmax(p[2][k], p[3][k]);
+                if ((mina - maxb) > cc.dh || (minb - maxa) > cc.dh) far = true;
+            }
+            if (far) continue;
+            TC r, s;
+            dist2 = geo::edge_edge_sq(p[0], p[1], p[2], p[3], &r, &s, d);
+            if (dist2 >= cc.dh2) continue;
+            mp = (TC(1) - r) * mass[c.x] + r * mass[c.y];
+            mq = (TC(1) - s) * mass[c.z] + s * mass[c.w];
+        }
+        ++my;
+        TC dist = dsqrt(dist2);
+        TC bar = TC(0);
+        if (dist2 < cc.dh2) {
+            const TC t2 = dist2 - cc.dh2;
+            bar = -cc.kappa * t2 * t2 * dlog(dist2 / cc.dh2) / (cc.dh2 * cc.dh2);
+        }
+        const TC w = bar + dmin(mp, mq) / (cc.dt * cc.dt);
+        const TC rp = mq / (mp + mq), rq = mp / (mp + mq);
+        const TC len = dsqrt(geo::dot3(d, d));
+        for (int k = 0; k < 3; ++k) d[k] /= len;
+        dist = cc.dh - dist;
+        const TC dp = dist * rp, dq = dist * rq;
+        for (int j = 0; j < 4; ++j) atomicAdd(diag + ids[j], (T)w);
+        for (int k = 0; k < 3; ++k) {
+            const TC t0 = w * (p[0][k] + dp * d[k]);
+            const TC t1 = kPT ? w * (p[1][k] - dq * d[k]) : w * (p[1][k] + dp * d[k]);
+            const TC t2 = w * (p[2][k] - dq * d[k]);
+            const TC t3 = w * (p[3][k] - dq * d[k]);
+            atomicAdd(&rhs[ids[0]].x + k, (T)t0);
+            atomicAdd(&rhs[ids[1]].x + k, (T)t1);
+            atomicAdd(&rhs[ids[2]].x + k, (T)t2);
+            atomicAdd(&rhs[ids[3]].x + k, (T)t3);
+        }
+    }
+    my = warp_sum(my);
+    if ((threadIdx.x & 31) == 0 && my) atomicAdd(active, (unsigned long long)my);
+}
+
+}  // namespace
+
+template <typename T, typename TC>
+void launch_patch_boxes(const Dev<T, TC>& d, const V4<T>* X, const V4<T>* D, T infl, cudaStream_t s) {
+    if (d.npatch == 0) return;
+    k_patch_boxes<T><<<blocks_for((int64_t)d.npatch * 32), kBlock, 0, s>>>(d.npatch, d.pfPtr, d.pfIdx, d.Faces, X,
+                                                                          D, infl, d.PatchBox);
+}
+template <typename T, typename TC>
+void launch_patch_init_boxes(const Dev<T, TC>& d, T infl, cudaStream_t s) {
+    if (d.npatch == 0) return;
+    k_init_boxes<T><<<blocks_for((int64_t)d.npatch * 32), kBlock, 0, s>>>(d.npatch, d.pxPtr, d.pxIdx, d.P, infl,
+                                                                         d.PatchBox);
+}
+template <typename T, typename TC>
+void launch_morton(const Dev<T, TC>& d, T* cs, unsigned long long* keys, int* vals, cudaStream_t s) {
+    if (d.npatch == 0) return;
+    k_center_scale<T><<<1, 1024, 0, s>>>(d.npatch, d.PatchBox, cs);
+    k_morton<T><<<blocks_for(d.npatch), kBlock, 0, s>>>(d.npatch, d.PatchBox, cs, d.Morton, keys, vals);
+}
+template <typename T, typename TC>
+void launch_karras(const Dev<T, TC>& d, const unsigned long long* sorted, cudaStream_t s) {
+    if (d.npatch == 0) return;
+    k_karras<<<blocks_for(d.npatch), kBlock, 0, s>>>(d.npatch, sorted, d.NodeChild, d.NodeParent);
+}
+template <typename T, typename TC>
+void launch_refit(const Dev<T, TC>& d, cudaStream_t s) {
+    if (d.npatch == 0) return;
+    if (d.npatch > 1) cudaMemsetAsync(d.RefitFlag, 0, sizeof(int) * (d.npatch - 1), s);
+    k_refit<T><<<blocks_for(d.npatch), kBlock, 0, s>>>(d.npatch, d.LeafPatch, d.PatchBox, d.NodeBox, d.NodeChild,
+                                                       d.NodeParent, d.RefitFlag);
+}
+template <typename T, typename TC>
+void launch_traverse(const Dev<T, TC>& d, int* counts, const int* offsets, int2* out, cudaStream_t s) {
+    if (d.npatch == 0) return;
+    k_traverse<T><<<blocks_for(d.npatch, 128), 128, 0, s>>>(d.npatch, d.PatchBox, d.NodeBox, d.NodeChild,
+                                                            d.LeafPatch, d.pStatic, counts, offsets, out,
+                                                            d.ErrFlags);
+}
+template <typename T, typename TC>
+void launch_pair_counts(const Dev<T, TC>& d, int64_t* cpt, int64_t* cee, cudaStream_t s) {
+    if (d.nPairs == 0) return;
+    k_pair_counts<<<blocks_for(d.nPairs), kBlock, 0, s>>>(d.nPairs, d.Pairs, d.pfPtr, d.ppPtr, d.pePtr, cpt, cee);
+}
+template <typename T, typename TC>
+void launch_expand(const Dev<T, TC>& d, const int64_t* opt, const int64_t* oee, cudaStream_t s) {
+    if (d.nPairs == 0) return;
+    k_expand<<<blocks_for(d.nPairs * 32), kBlock, 0, s>>>(d.nPairs, d.Pairs, d.pfPtr, d.pfIdx, d.ppPtr, d.ppIdx,
+                                                          d.pePtr, d.peIdx, d.Faces, d.Edges, opt, oee, d.PT, d.EE);
+}
+template <typename T, typename TC>
+void launch_toi(const Dev<T, TC>& d, const V4<T>* X0, const V4<T>* X1, const SolverConsts& c, TC* per_pt,
+                TC* per_ee, cudaStream_t s) {
+    if (d.nPT > 0)
+        k_toi<T, TC, true><<<grid_cap(d.nPT), kBlock, 0, s>>>(d.nPT, d.PT, X0, X1, (TC)c.ccd_slack, (TC)c.ccd_eta,
+                                                               c.ccd_max_iter, per_pt, d.ToiMin);
+    if (d.nEE > 0)
+        k_toi<T, TC, false><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X0, X1, (TC)c.ccd_slack,
+                                                                (TC)c.ccd_eta, c.ccd_max_iter, per_ee, d.ToiMin);
+}
+template <typename T, typename TC>
+void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s) {
+    k_toi_finalize<T, TC><<<1, 1, 0, s>>>(d.ToiMin, d.Toi, c.toi_scale);
+}
+template <typename T, typename TC>
+void launch_contact(const Dev<T, TC>& d, const V4<T>* X, const SolverConsts& c, cudaStream_t s) {
+    cudaMemsetAsync(d.CollDiag, 0, sizeof(T) * d.ntot, s);
+    cudaMemsetAsync(d.CollRhs, 0, sizeof(V4<T>) * d.ntot, s);
+    cudaMemsetAsync(d.ActiveCount, 0, sizeof(unsigned long long), s);
+    ContactConsts<TC> cc;
+    const T dh = (T)c.dhat;
+    cc.dh = (TC)dh;
+    cc.dh2 = (TC)(dh * dh);
+    cc.kappa = (TC)(T)c.kappa;
+    cc.dt = (TC)(T)c.dt;
+    if (d.nPT > 0)
+        k_contact<T, TC, true><<<grid_cap(d.nPT), kBlock, 0, s>>>(d.nPT, d.PT, X, d.CollMass, cc, d.CollDiag,
+                                                                   d.CollRhs, d.ActiveCount);
+    if (d.nEE > 0)
+        k_contact<T, TC, false><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X, d.CollMass, cc, d.CollDiag,
+                                                                    d.CollRhs, d.ActiveCount);
+}
+
+#define PDIPC_INST_COLL(T, TC)                                                                                \
+    template void launch_patch_boxes<T, TC>(const Dev<T, TC>&, const V4<T>*, const V4<T>*, T, cudaStream_t);  \
+    template void launch_patch_init_boxes<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                         \
+    template void launch_morton<T, TC>(const Dev<T, TC>&, T*, unsigned long long*, int*, cudaStream_t);     \
+    template void launch_karras<T, TC>(const Dev<T, TC>&, const unsigned long long*, cudaStream_t);           \
+    template void launch_refit<T, TC>(const Dev<T, TC>&, cudaStream_t);                                       \
+    template void launch_traverse<T, TC>(const Dev<T, TC>&, int*, const int*, int2*, cudaStream_t);           \
+    template void launch_pair_counts<T, TC>(const Dev<T, TC>&, int64_t*, int64_t*, cudaStream_t);             \
+    template void launch_expand<T, TC>(const Dev<T, TC>&, const int64_t*, const int64_t*, cudaStream_t);      \
+    template void launch_toi<T, TC>(const Dev<T, TC>&, const V4<T>*, const V4<T>*, const SolverConsts&, TC*,  \
+                                    TC*, cudaStream_t);                                                       \
+    template void launch_toi_finalize<T, TC>(const Dev<T, TC>&, const SolverConsts&, cudaStream_t);           \
+    template void launch_contact<T, TC>(const Dev<T, TC>&, const V4<T>*, const SolverConsts&, cudaStream_t);
+
+PDIPC_INST_COLL(float, float)
+PDIPC_INST_COLL(double, double)
+PDIPC_INST_COLL(float, double)
+
+}  // namespace pdipc

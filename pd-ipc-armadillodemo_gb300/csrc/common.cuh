@@ -1,0 +1,131 @@
+// common.cuh — types and small device helpers shared by the PD-IPC kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+
+namespace pdipc {
+
+// Position-like quantities are stored one vertex per aligned 4-vector
+// (x, y, z, pad) so a gather is one 16-byte (float) or two 16-byte (double)
+// loads instead of the reference's three scalar loads (PdIpcGpuFunc.cu:660-662).
+template <typename T>
+struct alignas(4 * sizeof(T) > 16 ? 16 : 4 * sizeof(T)) V4 {
+    T x, y, z, w;
+};
+
+template <typename T>
+struct Box6 {  // AABB: min xyz, max xyz
+    T lo[3];
+    T hi[3];
+};
+
+constexpr int kWarp = 32;
+constexpr int kSlice = 32;  // rows per SELL slice (one warp)
+
+template <typename T>
+__device__ __forceinline__ V4<T> ld4(const V4<T>* p, int i) {
+    return p[i];
+}
+__device__ __forceinline__ V4<float> ld4(const V4<float>* p, int i) {
+    float4 v = __ldg(reinterpret_cast<const float4*>(p) + i);
+    return V4<float>{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ V4<double> ld4(const V4<double>* p, int i) {
+    const double2* q = reinterpret_cast<const double2*>(p) + 2 * (size_t)i;
+    double2 a = __ldg(q), b = __ldg(q + 1);
+    return V4<double>{a.x, a.y, b.x, b.y};
+}
+// Plain (coherent) load for buffers written earlier in the same kernel or by
+// other blocks of a cooperative launch.
+template <typename T>
+__device__ __forceinline__ V4<T> ld4c(const V4<T>* p, int i) {
+    return p[i];
+}
+
+template <typename T>
+__device__ __forceinline__ void st4(V4<T>* p, int i, T x, T y, T z) {
+    p[i] = V4<T>{x, y, z, T(0)};
+}
+
+template <typename T>
+__device__ __forceinline__ T dsqrt(T v) {
+    return sqrt(v);
+}
+template <>
+__device__ __forceinline__ float dsqrt<float>(float v) {
+    return sqrtf(v);
+}
+template <typename T>
+__device__ __forceinline__ T dlog(T v) {
+    return log(v);
+}
+template <>
+__device__ __forceinline__ float dlog<float>(float v) {
+    return logf(v);
+}
+template <typename T>
+__device__ __forceinline__ T dmin(T a, T b) {
+    return fmin(a, b);
+}
+template <>
+__device__ __forceinline__ float dmin<float>(float a, float b) {
+    return fminf(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T dmax(T a, T b) {
+    return fmax(a, b);
+}
+template <>
+__device__ __forceinline__ float dmax<float>(float a, float b) {
+    return fmaxf(a, b);
+}
+
+// Order-preserving integer image of a non-negative float/double, so a global
+// minimum over non-negative values is one integer atomicMin.
+__device__ __forceinline__ unsigned int ordered_bits(float v) { return __float_as_uint(v); }
+__device__ __forceinline__ unsigned long long ordered_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v);
+}
+
+template <typename T>
+__device__ __forceinline__ void atomic_min_nonneg(T* addr, T v);
+template <>
+__device__ __forceinline__ void atomic_min_nonneg<float>(float* addr, float v) {
+    atomicMin(reinterpret_cast<unsigned int*>(addr), __float_as_uint(v));
+}
+template <>
+__device__ __forceinline__ void atomic_min_nonneg<double>(double* addr, double v) {
+    atomicMin(reinterpret_cast<unsigned long long*>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_min(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = dmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = dmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Device-side error flags (bit mask), read back by the host after a step.
+enum ErrFlag : unsigned int {
+    kErrNonFinite = 1u,
+    kErrTraversalStack = 2u,
+    kErrPairOverflow = 4u,
+    kErrCandidateOverflow = 8u,
+};
+
+}  // namespace pdipc

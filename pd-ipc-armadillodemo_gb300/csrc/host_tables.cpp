@@ -1,0 +1,396 @@
+// host_tables.cpp — init-time precompute of the PD-IPC cloth step.
+//
+// Follows, per cloth model, PdIpcClothModel::init (Simulator/PD-IPC/PdIpcClothModel.h:142-343),
+// the boundary topology of PdIpcModel::postProcessBoundaryInfo (PdIpcModel.h:84-172),
+// the grid collision patches of PdIpcClothModel::setCollisionPatches (:45-140),
+// the system assembly of PdIpcSimulator::setupHessMat (PdIpcSimulator.cpp:270-414)
+// and the patch lists of gpuCollisionInit (cpp:1151-1300).  Everything is
+// computed in FP64 with a fixed summation order and rounded to the working
+// precision at upload; the patch partition alone is computed in FP32 as the
+// reference does (qeal = float), so it is the same in every precision mode.
+#include "host_tables.h"
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <utility>
+
+namespace pdipc {
+
+namespace {
+
+inline uint64_t edge_key(int a, int b) {
+    if (a > b) std::swap(a, b);
+    return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
+}
+
+int find_edge(const std::vector<uint64_t>& keys, int a, int b) {
+    uint64_t k = edge_key(a, b);
+    auto it = std::lower_bound(keys.begin(), keys.end(), k);
+    return (it != keys.end() && *it == k) ? (int)(it - keys.begin()) : -1;
+}
+
+// Grid patch index of every face, or -1 if its centroid falls outside every
+// cell.  The reference scans the len x len cells in row-major order and takes
+// the first closed cell holding the centroid; the same cell is found here from
+// the floor estimate by checking its neighbours in that order.
+void grid_patches(const double* X, int nv, const int* F, int nf, int patch_dim,
+                  std::vector<std::vector<int>>& patches) {
+    const float inf = std::numeric_limits<float>::infinity();
+    float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+    for (int i = 0; i < nv; ++i)
+        for (int k = 0; k < 3; ++k) {
+            float p = (float)X[3 * i + k];
+            lo[k] = std::min(lo[k], p);
+            hi[k] = std::max(hi[k], p);
+        }
+    float sq = std::sqrt((float)nv);
+    int len = (int)(sq < (float)patch_dim ? sq : (float)patch_dim);
+    if (len < 1) len = 1;
+    float ext[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    // normal axis: the strictly thinnest one; on a tie (where the reference
+    // leaves the pair uninitialised) the last axis of minimum extent.
+    int nrm = -1;
+    for (int k = 0; k < 3; ++k)
+        if (ext[k] < ext[(k + 1) % 3] && ext[k] < ext[(k + 2) % 3]) nrm = k;
+    if (nrm < 0) {
+        float m = std::min(ext[0], std::min(ext[1], ext[2]));
+        for (int k = 0; k < 3; ++k)
+            if (ext[k] == m) nrm = k;
+    }
+    const int u = (nrm == 0) ? 1 : 0;
+    const int v = (nrm == 2) ? 1 : 2;
+    const float su = ext[u] / (float)len, sv = ext[v] / (float)len;
+    auto in_cell = [](float c, float b0, float s) {
+        float b1 = b0 + s;
+        return c >= b0 && c <= b1;
+    };
+    std::vector<std::vector<int>> cells((size_t)len * len);
+    for (int f = 0; f < nf; ++f) {
+        float c[3] = {0.f, 0.f, 0.f};
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) c[a] += (float)X[3 * F[3 * f + k] + a];
+        for (int a = 0; a < 3; ++a) c[a] /= 3.f;
+        auto first_index = [&](float cv, float lo0, float s) -> int {
+            int guess = (s > 0.f) ? (int)std::floor((cv - lo0) / s) : 0;
+            int start = std::max(0, std::min(len - 1, guess) - 1);
+            for (int r = start; r < len && r <= guess + 1; ++r)
+                if (in_cell(cv, lo0 + (float)r * s, s)) return r;
+            return -1;
+        };
+        int r = first_index(c[u], lo[u], su);
+        if (r < 0) continue;
+        int cc = first_index(c[v], lo[v], sv);
+        if (cc < 0) continue;
+        cells[(size_t)r * len + cc].push_back(f);
+    }
+    patches.clear();
+    for (auto& cl : cells)
+        if (!cl.empty()) patches.push_back(std::move(cl));
+}
+
+}  // namespace
+
+std::string build_mesh_topology(const double* X, int nv, const int* F, int nf, int patch_dim, MeshTopology& t) {
+    if (nv <= 0 || nf <= 0) return "empty mesh";
+    for (int i = 0; i < 3 * nf; ++i)
+        if (F[i] < 0 || F[i] >= nv) return "face index out of range";
+    // edges: sorted unique (min,max) pairs (Model/TriangleMesh/BaseSurfaceMesh.cpp:219-234)
+    std::vector<uint64_t> keys;
+    keys.reserve(3 * (size_t)nf);
+    for (int f = 0; f < nf; ++f)
+        for (int k = 0; k < 3; ++k) keys.push_back(edge_key(F[3 * f + k], F[3 * f + (k + 1) % 3]));
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    const int ne = (int)keys.size();
+    t.edges.resize(2 * (size_t)ne);
+    t.point_edges.assign(nv, {});
+    for (int e = 0; e < ne; ++e) {
+        int a = (int)(keys[e] >> 32), b = (int)(keys[e] & 0xffffffffu);
+        t.edges[2 * e] = a;
+        t.edges[2 * e + 1] = b;
+        t.point_edges[a].push_back(e);
+        t.point_edges[b].push_back(e);
+    }
+    // edge -> faces, point -> faces, ascending face id
+    t.edge_faces.assign(ne, {});
+    std::vector<std::vector<int>> point_faces(nv);
+    std::vector<int> face_edge(3 * (size_t)nf);  // edges (01, 12, 20) of each face
+    for (int f = 0; f < nf; ++f) {
+        for (int k = 0; k < 3; ++k) {
+            int e = find_edge(keys, F[3 * f + k], F[3 * f + (k + 1) % 3]);
+            face_edge[3 * f + k] = e;
+            t.edge_faces[e].push_back(f);
+            point_faces[F[3 * f + k]].push_back(f);
+        }
+    }
+    // ownership: smallest current owned list wins, first on ties (PdIpcModel.h:136-171)
+    t.face_edges_own.assign(nf, {});
+    for (int e = 0; e < ne; ++e) {
+        const auto& fl = t.edge_faces[e];
+        int best = fl[0];
+        for (size_t q = 1; q < fl.size(); ++q)
+            if (t.face_edges_own[fl[q]].size() < t.face_edges_own[best].size()) best = fl[q];
+        t.face_edges_own[best].push_back(e);
+    }
+    t.face_points_own.assign(nf, {});
+    for (int p = 0; p < nv; ++p) {
+        const auto& fl = point_faces[p];
+        if (fl.empty()) return "mesh has an isolated vertex";
+        int best = fl[0];
+        for (size_t q = 1; q < fl.size(); ++q)
+            if (t.face_points_own[fl[q]].size() < t.face_points_own[best].size()) best = fl[q];
+        t.face_points_own[best].push_back(p);
+    }
+    grid_patches(X, nv, F, nf, patch_dim, t.patches);
+    return "";
+}
+
+std::string build_host_tables(const std::vector<ModelInput>& models, double gravity, HostTables& H) {
+    H = HostTables();
+    std::vector<int> order;
+    for (int i = 0; i < (int)models.size(); ++i)
+        if (!models[i].is_static) order.push_back(i);
+    const int nclothModels = (int)order.size();
+    for (int i = 0; i < (int)models.size(); ++i)
+        if (models[i].is_static) order.push_back(i);
+    if (nclothModels == 0) return "no cloth model added";
+
+    std::vector<MeshTopology> topo(models.size());
+    std::vector<int> vbase(models.size()), fbase(models.size()), ebase(models.size());
+    int nv = 0, nf = 0, ne = 0, nsim = 0;
+    for (int q = 0; q < (int)order.size(); ++q) {
+        const ModelInput& m = models[order[q]];
+        std::string err = build_mesh_topology(m.X.data(), m.nv, m.F.data(), m.nf, m.patch_dim, topo[order[q]]);
+        if (!err.empty()) return err;
+        vbase[order[q]] = nv;
+        fbase[order[q]] = nf;
+        ebase[order[q]] = ne;
+        nv += m.nv;
+        nf += m.nf;
+        ne += (int)topo[order[q]].edges.size() / 2;
+        if (!m.is_static) nsim += m.nv;
+    }
+    H.nsim = nsim;
+    H.ntot = nv;
+    H.X.resize(3 * (size_t)nv);
+    for (int mi : order)
+        std::copy(models[mi].X.begin(), models[mi].X.end(), H.X.begin() + 3 * (size_t)vbase[mi]);
+
+    // ---- cloth precompute: PdIpcClothModel::init (ClothModel.h:177-328) ----
+    H.mass.assign(nsim, 0.0);
+    H.Delastic.assign(nsim, 0.0);
+    H.curvNorm.assign(nsim, 0.0);
+    H.strain.assign(nsim, 0.0);
+    H.pinSlot.assign(nsim, -1);
+    H.lPtr.assign(nsim + 1, 0);
+    std::vector<double> bendArea(nsim, 0.0);
+    for (int q = 0; q < nclothModels; ++q) {
+        const int mi = order[q];
+        const ModelInput& m = models[mi];
+        const MeshTopology& t = topo[mi];
+        const int o = vbase[mi];
+        auto P = [&](int i, int k) { return m.X[3 * i + k]; };
+        std::vector<double> area(m.nv, 0.0);
+        for (int f = 0; f < m.nf; ++f) {  // TriangleArea (Commom/GeometryComputation.cpp:3-6)
+            const int* Fv = &m.F[3 * f];
+            double a[3], b[3];
+            for (int k = 0; k < 3; ++k) {
+                a[k] = P(Fv[1], k) - P(Fv[0], k);
+                b[k] = P(Fv[2], k) - P(Fv[0], k);
+            }
+            double c[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+            double ar = 0.5 * std::fabs(std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
+            for (int k = 0; k < 3; ++k) area[Fv[k]] += ar / 3.0;
+        }
+        for (int i = 0; i < m.nv; ++i) {
+            const int g = o + i;
+            H.mass[g] = area[i] * m.density;
+            bendArea[g] = area[i] * m.k_bend;
+            H.strain[g] = m.k_stretch;
+            const int deg = (int)t.point_edges[i].size();
+            H.lPtr[g + 1] = deg + 1;  // counts for now
+        }
+    }
+    // prefix the stencil sizes, then fill the stencils
+    for (int g = 0; g < nsim; ++g) H.lPtr[g + 1] += H.lPtr[g];
+    const size_t nl = (size_t)H.lPtr[nsim];
+    H.lNbr.assign(nl, 0);
+    H.lRest.assign(nl, 0.0);
+    H.lLbo.assign(nl, 0.0);
+    H.lBend.assign(nl, 0.0);
+    H.lBendT.assign(nl, 0.0);
+    for (int q = 0; q < nclothModels; ++q) {
+        const int mi = order[q];
+        const ModelInput& m = models[mi];
+        const MeshTopology& t = topo[mi];
+        const int o = vbase[mi];
+        auto P = [&](int i, int k) { return m.X[3 * i + k]; };
+        // area and cotangent weights: -1/2 sum of cot of the angles opposite each edge
+        std::vector<double> area(m.nv, 0.0);
+        for (int f = 0; f < m.nf; ++f) {
+            const int* Fv = &m.F[3 * f];
+            double a[3], b[3];
+            for (int k = 0; k < 3; ++k) {
+                a[k] = P(Fv[1], k) - P(Fv[0], k);
+                b[k] = P(Fv[2], k) - P(Fv[0], k);
+            }
+            double c[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+            double ar = 0.5 * std::fabs(std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
+            for (int k = 0; k < 3; ++k) area[Fv[k]] += ar / 3.0;
+        }
+        const int mne = (int)t.edges.size() / 2;
+        std::vector<double> cotw(mne, 0.0);
+        for (int e = 0; e < mne; ++e) {
+            const int a = t.edges[2 * e], b = t.edges[2 * e + 1];
+            for (int f : t.edge_faces[e]) {
+                int opp = -1;
+                for (int k = 0; k < 3 && opp == -1; ++k) {
+                    int vk = m.F[3 * f + k];
+                    if (vk != a && vk != b) opp = vk;
+                }
+                double x10[3], x20[3];
+                for (int k = 0; k < 3; ++k) {
+                    x10[k] = P(a, k) - P(opp, k);
+                    x20[k] = P(b, k) - P(opp, k);
+                }
+                double l10 = std::sqrt(x10[0] * x10[0] + x10[1] * x10[1] + x10[2] * x10[2]);
+                double l20 = std::sqrt(x20[0] * x20[0] + x20[1] * x20[1] + x20[2] * x20[2]);
+                double th = std::acos((x10[0] * x20[0] + x10[1] * x20[1] + x10[2] * x20[2]) / (l10 * l20));
+                cotw[e] += -0.5 * (1.0 / std::tan(th));
+            }
+        }
+        for (int i = 0; i < m.nv; ++i) {
+            const int g = o + i;
+            const int base = H.lPtr[g];
+            const int deg = (int)t.point_edges[i].size();
+            H.lNbr[base] = g;
+            double sum = 0.0;
+            for (int k = 0; k < deg; ++k) {
+                const int e = t.point_edges[i][k];
+                const int ve = (t.edges[2 * e] == i) ? t.edges[2 * e + 1] : t.edges[2 * e];
+                H.lNbr[base + 1 + k] = ve + o;
+                double d[3] = {P(i, 0) - P(ve, 0), P(i, 1) - P(ve, 1), P(i, 2) - P(ve, 2)};
+                H.lRest[base + 1 + k] = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                const double ew = cotw[e] / area[i];
+                sum += ew;
+                H.lLbo[base + 1 + k] = ew;
+            }
+            H.lLbo[base] = -sum;
+            double cv[3] = {0.0, 0.0, 0.0};
+            for (int k = 0; k <= deg; ++k) {
+                const int vk = H.lNbr[base + k] - o;
+                for (int a = 0; a < 3; ++a) cv[a] += H.lLbo[base + k] * P(vk, a);
+                H.lBend[base + k] = H.lLbo[base + k] * m.k_bend * area[i];
+            }
+            H.curvNorm[g] = std::sqrt(cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2]);
+        }
+        for (int p : m.pins) {
+            if (p < 0 || p >= m.nv) return "pin index out of range";
+            if (H.pinSlot[o + p] == -1) {
+                H.pinSlot[o + p] = (int)H.pinK.size();
+                H.pinK.push_back(m.k_pin);
+            }
+        }
+    }
+    // transposed bending coefficient: what the stencil of neighbour k puts on i
+    for (int i = 0; i < nsim; ++i)
+        for (int s = H.lPtr[i]; s < H.lPtr[i + 1]; ++s) {
+            const int k = H.lNbr[s];
+            int pos = -1;
+            for (int r = H.lPtr[k]; r < H.lPtr[k + 1]; ++r)
+                if (H.lNbr[r] == i) {
+                    pos = r;
+                    break;
+                }
+            if (pos < 0) return "asymmetric neighbour lists";
+            H.lBendT[s] = H.lBend[pos];
+        }
+
+    // ---- system matrix: pins + springs + LBO bending (setupHessMat cpp:270-414) ----
+    std::vector<std::vector<std::pair<int, double>>> rows(nsim);
+    for (int i = 0; i < nsim; ++i)
+        if (H.pinSlot[i] >= 0) H.Delastic[i] += H.pinK[H.pinSlot[i]];
+    for (int i = 0; i < nsim; ++i) {
+        const double k = H.strain[i];
+        for (int s = H.lPtr[i] + 1; s < H.lPtr[i + 1]; ++s) {
+            H.Delastic[i] += k;
+            rows[i].push_back({H.lNbr[s], -k});
+        }
+    }
+    for (int i = 0; i < nsim; ++i) {
+        const int b0 = H.lPtr[i], n = H.lPtr[i + 1] - b0;
+        for (int r = 0; r < n; ++r)
+            for (int c = 0; c < n; ++c) {
+                const int a = H.lNbr[b0 + r], b = H.lNbr[b0 + c];
+                const double v = bendArea[i] * H.lLbo[b0 + r] * H.lLbo[b0 + c];
+                if (a == b) H.Delastic[a] += v;
+                else rows[a].push_back({b, v});
+            }
+    }
+    H.nPtr.assign(nsim + 1, 0);
+    for (int i = 0; i < nsim; ++i) {
+        auto& R = rows[i];
+        std::stable_sort(R.begin(), R.end(),
+                         [](const std::pair<int, double>& x, const std::pair<int, double>& y) { return x.first < y.first; });
+        size_t a = 0;
+        while (a < R.size()) {
+            size_t b = a;
+            double s = 0.0;
+            while (b < R.size() && R[b].first == R[a].first) s += R[b++].second;
+            if (!(std::fabs(s) < 1e-12)) {  // IG drop (gpuSolverInit cpp:656-658)
+                H.nCol.push_back(R[a].first);
+                H.nVal.push_back(-s);
+            }
+            a = b;
+        }
+        H.nPtr[i + 1] = (int)H.nCol.size();
+        std::vector<std::pair<int, double>>().swap(R);
+    }
+
+    // ---- collision topology (gpuCollisionInit cpp:1151-1300) ----
+    H.faces.reserve(3 * (size_t)nf);
+    H.edges.reserve(2 * (size_t)ne);
+    H.pfPtr.assign(1, 0);
+    H.ppPtr.assign(1, 0);
+    H.pePtr.assign(1, 0);
+    H.pxPtr.assign(1, 0);
+    for (int mi : order) {
+        const ModelInput& m = models[mi];
+        const MeshTopology& t = topo[mi];
+        const int o = vbase[mi], fo = fbase[mi], eo = ebase[mi];
+        for (int f = 0; f < m.nf; ++f)
+            for (int k = 0; k < 3; ++k) H.faces.push_back(m.F[3 * f + k] + o);
+        for (size_t q = 0; q < t.edges.size(); ++q) H.edges.push_back(t.edges[q] + o);
+        std::vector<int> es, ps, xs;
+        for (const auto& patch : t.patches) {
+            es.clear();
+            ps.clear();
+            xs.clear();
+            for (int f : patch) {
+                H.pfIdx.push_back(f + fo);
+                for (int e : t.face_edges_own[f]) es.push_back(e + eo);
+                for (int p : t.face_points_own[f]) ps.push_back(p + o);
+                for (int k = 0; k < 3; ++k) xs.push_back(m.F[3 * f + k] + o);
+            }
+            for (auto* vv : {&es, &ps, &xs}) {
+                std::sort(vv->begin(), vv->end());
+                vv->erase(std::unique(vv->begin(), vv->end()), vv->end());
+            }
+            H.peIdx.insert(H.peIdx.end(), es.begin(), es.end());
+            H.ppIdx.insert(H.ppIdx.end(), ps.begin(), ps.end());
+            H.pxIdx.insert(H.pxIdx.end(), xs.begin(), xs.end());
+            H.pfPtr.push_back((int)H.pfIdx.size());
+            H.pePtr.push_back((int)H.peIdx.size());
+            H.ppPtr.push_back((int)H.ppIdx.size());
+            H.pxPtr.push_back((int)H.pxIdx.size());
+            H.pStatic.push_back(m.is_static ? 1 : 0);
+        }
+    }
+    H.npatch = (int)H.pStatic.size();
+    H.collMassSim = H.mass;
+    (void)gravity;
+    return "";
+}
+
+}  // namespace pdipc

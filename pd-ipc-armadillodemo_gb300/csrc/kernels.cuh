@@ -1,0 +1,171 @@
+// kernels.cuh — device state of one PD-IPC context and the launchers of every
+// kernel of the step.  All launches go to the context's stream; nothing here
+// synchronises.
+#pragma once
+
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace pdipc {
+
+// Device buffers of one context.  Vertex arrays use the global numbering
+// (cloth vertices first, then static ones).  T is the state/solver scalar,
+// TC the CCD/contact scalar.
+template <typename T, typename TC>
+struct Dev {
+    int nsim = 0, ntot = 0, nface = 0, nedge = 0, npatch = 0;
+
+    // state
+    V4<T>* P = nullptr;      // positions [ntot]
+    V4<T>* Pold = nullptr;   // positions at the start of the outer iteration [ntot]
+    V4<T>* X0 = nullptr;     // positions at the start of the step [nsim]
+    V4<T>* Vel = nullptr;    // velocities [nsim]
+    V4<T>* Dir = nullptr;    // P - Pold before clamping [ntot]; static part stays 0
+    V4<T>* Xrest = nullptr;  // initial positions [ntot] (reset, pins)
+
+    // solver work
+    V4<T>* Y = nullptr;      // first half of a two-sweep step [nsim]
+    V4<T>* B = nullptr;      // odd Chebyshev iterates [nsim]
+    V4<T>* Aq = nullptr;     // rescaled curvature vector per vertex [nsim]
+    V4<T>* Rhs = nullptr;    // right-hand side of the current local-global iteration [nsim]
+    V4<T>* Rhs0 = nullptr;   // inertial right-hand side (m/dt^2) y [nsim]
+    V4<T>* Grav = nullptr;   // (0, g m, 0) [nsim]
+    V4<T>* PinRhs = nullptr; // k_pin * X_rest for pinned vertices, else 0 [nsim]
+    T* InvMass = nullptr;    // [nsim]
+    int* PinFlag = nullptr;  // -1 free, else pin slot [nsim]
+    T* Dinert = nullptr;     // m/dt^2 (0 for pinned vertices) [nsim]
+    T* Delastic = nullptr;   // [nsim]
+    T* InvD = nullptr;       // 1 / (elastic + inertial + collision) [nsim]
+    T* CollDiag = nullptr;   // [ntot]
+    V4<T>* CollRhs = nullptr;// [ntot]
+    TC* CollMass = nullptr;  // [ntot]
+
+    // local-step stencils (CSR over simulated vertices): [self, neighbours ascending]
+    int* lPtr = nullptr;
+    int* lNbr = nullptr;
+    T* lRest = nullptr;
+    T* lLbo = nullptr;
+    T* lBend = nullptr;
+    T* lBendT = nullptr;
+    T* Strain = nullptr;     // per vertex
+    T* CurvNorm = nullptr;   // per vertex
+
+    // N = -offdiag(A) in SELL-32: slice s holds rows [32 s, 32 s + 32); entry k
+    // of lane r sits at sOff[s] + 32 k + r; sLen[s] entries per row.
+    int nslice = 0;
+    int* sOff = nullptr;
+    int* sLen = nullptr;
+    int* sCol = nullptr;
+    T* sVal = nullptr;
+
+    // collision topology
+    int4* Faces = nullptr;   // (v0, v1, v2, -)
+    int2* Edges = nullptr;
+    int* pfPtr = nullptr;
+    int* pfIdx = nullptr;
+    int* ppPtr = nullptr;
+    int* ppIdx = nullptr;
+    int* pePtr = nullptr;
+    int* peIdx = nullptr;
+    int* pxPtr = nullptr;
+    int* pxIdx = nullptr;
+    uint8_t* pStatic = nullptr;
+
+    // patch BVH (Karras): internal nodes [0, npatch-1), leaves [npatch-1, 2 npatch-1)
+    Box6<T>* PatchBox = nullptr;   // [npatch]
+    Box6<T>* NodeBox = nullptr;    // [2 npatch - 1]
+    int2* NodeChild = nullptr;     // [npatch - 1]
+    int* NodeParent = nullptr;     // [2 npatch - 1]
+    int* LeafPatch = nullptr;      // [npatch] sorted order: leaf k -> patch id
+    int* RefitFlag = nullptr;      // [npatch - 1]
+    unsigned long long* Morton = nullptr;  // [npatch] codes by patch id
+
+    // candidates of the current step
+    int2* Pairs = nullptr;
+    int64_t capPairs = 0;
+    int4* PT = nullptr;
+    int64_t capPT = 0;
+    int4* EE = nullptr;
+    int64_t capEE = 0;
+    int64_t nPairs = 0, nPT = 0, nEE = 0;
+
+    // scalars
+    TC* ToiMin = nullptr;    // running min over candidates (reset to 1 after use)
+    T* Toi = nullptr;        // clamped step fraction of the outer iteration
+    double* ResidPart = nullptr;  // per-block partial sums of |dir|^2
+    double* Resid = nullptr;      // |dir|^2
+    unsigned int* ErrFlags = nullptr;
+    unsigned long long* ActiveCount = nullptr;
+};
+
+struct SolverConsts {
+    double dt, gravity, dhat, kappa, infl, relax, rho, toi_scale, ccd_slack, ccd_eta, static_mass;
+    int lg, cheby, ccd_max_iter;
+};
+
+// ---------------- PD kernels (pd_kernels.cu) ----------------
+template <typename T, typename TC>
+void launch_predict(const Dev<T, TC>& d, T dt, cudaStream_t s);
+template <typename T, typename TC>
+void launch_diag(const Dev<T, TC>& d, cudaStream_t s);
+template <typename T, typename TC>
+void launch_local_aq(const Dev<T, TC>& d, cudaStream_t s);
+// local step right-hand side fused with the first J sweep (Y = S(P))
+template <typename T, typename TC>
+void launch_local_rhs_sweep(const Dev<T, TC>& d, T relax, cudaStream_t s);
+// out = S(src) or, with prev, out = omega (S(src) - prev) + prev
+template <typename T, typename TC>
+void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T>* out, T relax, T omega,
+                  cudaStream_t s);
+template <typename T, typename TC>
+void launch_direction(const Dev<T, TC>& d, cudaStream_t s);
+template <typename T, typename TC>
+void launch_clamp(const Dev<T, TC>& d, cudaStream_t s);
+template <typename T, typename TC>
+void launch_velocity(const Dev<T, TC>& d, T invt, cudaStream_t s);
+template <typename T, typename TC>
+void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s);
+int direction_blocks(int nsim);
+
+// ---------------- collision kernels (collision_kernels.cu) ----------------
+// swept (Dir != null) or static patch boxes, inflated
+template <typename T, typename TC>
+void launch_patch_boxes(const Dev<T, TC>& d, const V4<T>* X, const V4<T>* D, T infl, cudaStream_t s);
+// init-time boxes over every vertex of the patch (AipcBvhs input, cpp:1279-1292)
+template <typename T, typename TC>
+void launch_patch_init_boxes(const Dev<T, TC>& d, T infl, cudaStream_t s);
+// Morton codes of the patch box centres; ctr_scale[0..3] = centre xyz, scale
+template <typename T, typename TC>
+void launch_morton(const Dev<T, TC>& d, T* ctr_scale_dev, unsigned long long* keys, int* vals, cudaStream_t s);
+template <typename T, typename TC>
+void launch_karras(const Dev<T, TC>& d, const unsigned long long* sorted_codes, cudaStream_t s);
+template <typename T, typename TC>
+void launch_refit(const Dev<T, TC>& d, cudaStream_t s);
+// count (out_pairs == null) or write overlapping patch pairs
+template <typename T, typename TC>
+void launch_traverse(const Dev<T, TC>& d, int* counts, const int* offsets, int2* out_pairs, cudaStream_t s);
+template <typename T, typename TC>
+void launch_pair_counts(const Dev<T, TC>& d, int64_t* cnt_pt, int64_t* cnt_ee, cudaStream_t s);
+template <typename T, typename TC>
+void launch_expand(const Dev<T, TC>& d, const int64_t* off_pt, const int64_t* off_ee, cudaStream_t s);
+template <typename T, typename TC>
+void launch_toi(const Dev<T, TC>& d, const V4<T>* X0, const V4<T>* X1, const SolverConsts& c, TC* per_pt,
+                TC* per_ee, cudaStream_t s);
+template <typename T, typename TC>
+void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s);
+template <typename T, typename TC>
+void launch_contact(const Dev<T, TC>& d, const V4<T>* X, const SolverConsts& c, cudaStream_t s);
+
+// ---------------- primitives (primitives.cu) ----------------
+// Exclusive scan of n int64 values (in may equal out); *total receives the sum.
+// tmp must hold scan_tmp_bytes(n) bytes.
+size_t scan_tmp_bytes(int64_t n);
+void scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, int64_t* total, void* tmp, cudaStream_t s);
+void scan_exclusive_i32(const int* in, int* out, int n, int* total, void* tmp, cudaStream_t s);
+// Stable LSD radix sort of 64-bit keys with int values (keys use the low 63 bits).
+size_t sort_tmp_bytes(int n);
+void radix_sort_u64(unsigned long long* keys, int* vals, int n, void* tmp, cudaStream_t s);
+void launch_reduce_sum_f64(const double* part, int n, double* out, cudaStream_t s);
+
+}  // namespace pdipc

@@ -1,0 +1,316 @@
+// pd_kernels.cu — projective-dynamics kernels of the PD-IPC cloth step.
+//
+// Reference kernels replaced (Simulator/PD-IPC/PdIpcGpuFunc.cu):
+//   predictiveKernel :88-147                         -> k_predict
+//   solveClothPointsStrainAndBendingConstraintKernel
+//     :627-728 + solvePointsConstraintKernel :764-790 -> k_local_aq + k_local_rhs_sweep
+//   updateR1/R2/R2Row OperatorsKernel :899-974,
+//   superJacobiR2FirstTermKernel :1041-1074,
+//   superJacobiR2IterationKernel :1076-1129,
+//   chebyshevJacobiR2IterationKernel :1185-1242     -> k_sweep (R2 applied as two J sweeps)
+//   computeDirectionKernel :185, clampDirectionKernel :222,
+//   updateVelocityKernel :262, cublasSdot (cpp:1774) -> k_direction, k_clamp, k_velocity
+//
+// Layout: one vertex per aligned 4-vector; the local step is a gather (no
+// atomics) and the system matrix is streamed from SELL-32 slices so a warp's
+// column/value loads are contiguous 128-byte lines.
+#include "kernels.cuh"
+
+namespace pdipc {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+inline int blocks_for(int n, int b = kBlock) { return (n + b - 1) / b; }
+
+template <typename T>
+__global__ void k_predict(int nsim, int ntot, T dt, V4<T>* __restrict__ P, V4<T>* __restrict__ Pold,
+                          V4<T>* __restrict__ X0, V4<T>* __restrict__ Vel, V4<T>* __restrict__ Rhs0,
+                          T* __restrict__ Dinert, const V4<T>* __restrict__ Grav, const T* __restrict__ InvMass,
+                          const int* __restrict__ PinFlag, T* __restrict__ CollDiag, V4<T>* __restrict__ CollRhs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntot) return;
+    CollDiag[i] = T(0);
+    CollRhs[i] = V4<T>{T(0), T(0), T(0), T(0)};
+    if (i >= nsim) return;
+    const V4<T> x = P[i];
+    X0[i] = x;
+    Pold[i] = x;
+    if (PinFlag[i] != -1) {  // pinned: velocity zeroed, nothing else written
+        Vel[i] = V4<T>{T(0), T(0), T(0), T(0)};
+        return;
+    }
+    const T im = InvMass[i];
+    const T m = im * dt;
+    const V4<T> v = Vel[i];
+    const V4<T> g = Grav[i];
+    T y0 = (v.x + m * g.x) * dt + x.x;
+    T y1 = (v.y + m * g.y) * dt + x.y;
+    T y2 = (v.z + m * g.z) * dt + x.z;
+    const T mm = T(1) / (dt * m);
+    Dinert[i] = T(1) / (im * dt * dt);
+    Rhs0[i] = V4<T>{mm * y0, mm * y1, mm * y2, T(0)};
+    P[i] = V4<T>{y0, y1, y2, T(0)};
+}
+
+template <typename T>
+__global__ void k_diag(int nsim, const T* __restrict__ De, const T* __restrict__ Di, const T* __restrict__ Dc,
+                       T* __restrict__ InvD) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim) return;
+    const T d = (De[i] + Di[i]) + Dc[i];  // sysDiag = elastic + inertial (+ collision), cpp:1556-1560
+    InvD[i] = T(1) / d;
+}
+
+// Curvature vector aq_i = sum_k lbo_ik x_k, rescaled to the rest norm
+// (PdIpcGpuFunc.cu:664-699).
+template <typename T>
+__global__ void k_local_aq(int nsim, const V4<T>* __restrict__ P, const int* __restrict__ lPtr,
+                           const int* __restrict__ lNbr, const T* __restrict__ lLbo, const T* __restrict__ CurvNorm,
+                           V4<T>* __restrict__ Aq) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim) return;
+    const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
+    const V4<T> x = ld4(P, i);
+    const T l0 = __ldg(lLbo + b);
+    T a0 = x.x * l0, a1 = x.y * l0, a2 = x.z * l0;
+    for (int s = b + 1; s < e; ++s) {
+        const V4<T> xj = ld4(P, __ldg(lNbr + s));
+        const T l = __ldg(lLbo + s);
+        a0 += xj.x * l;
+        a1 += xj.y * l;
+        a2 += xj.z * l;
+    }
+    const T nrm = dsqrt(a0 * a0 + a1 * a1 + a2 * a2);
+    if (nrm >= T(1e-10)) {
+        const T c = __ldg(CurvNorm + i) / nrm;
+        a0 *= c;
+        a1 *= c;
+        a2 *= c;
+    }
+    Aq[i] = V4<T>{a0, a1, a2, T(0)};
+}
+
+template <typename T>
+__device__ __forceinline__ void sell_row(int i, const int* __restrict__ sOff, const int* __restrict__ sLen,
+                                         const int* __restrict__ sCol, const T* __restrict__ sVal,
+                                         const V4<T>* __restrict__ X, T& s0, T& s1, T& s2) {
+    const int sl = i >> 5, lane = i & 31;
+    const int base = __ldg(sOff + sl) + lane;
+    const int len = __ldg(sLen + sl);
+    s0 = T(0);
+    s1 = T(0);
+    s2 = T(0);
+#pragma unroll 4
+    for (int k = 0; k < len; ++k) {
+        const int j = __ldg(sCol + base + 32 * k);
+        const T v = __ldg(sVal + base + 32 * k);
+        const V4<T> xj = ld4(X, j);
+        s0 += v * xj.x;
+        s1 += v * xj.y;
+        s2 += v * xj.z;
+    }
+}
+
+// rhs_i = ((rhs0_i + spring_i + bend_ii aq_i + sum_k bend_ki aq_k) + contact_i) + pin_i,
+// then the first weighted-Jacobi sweep Y = (1-w) x + w D^-1 (N x + rhs).
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_local_rhs_sweep(
+    int nsim, T relax, const V4<T>* __restrict__ P, const int* __restrict__ lPtr, const int* __restrict__ lNbr,
+    const T* __restrict__ lRest, const T* __restrict__ lBend, const T* __restrict__ lBendT,
+    const T* __restrict__ Strain, const V4<T>* __restrict__ Aq, const V4<T>* __restrict__ Rhs0,
+    const V4<T>* __restrict__ CollRhs, const V4<T>* __restrict__ PinRhs, const T* __restrict__ InvD,
+    const int* __restrict__ sOff, const int* __restrict__ sLen, const int* __restrict__ sCol,
+    const T* __restrict__ sVal, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim) return;
+    const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
+    const V4<T> x = ld4(P, i);
+    const T strain = __ldg(Strain + i);
+    T t0 = T(0), t1 = T(0), t2 = T(0);
+    for (int s = b + 1; s < e; ++s) {  // mass-spring projections (cu:670-690)
+        const V4<T> xj = ld4(P, __ldg(lNbr + s));
+        const T d0 = x.x - xj.x, d1 = x.y - xj.y, d2 = x.z - xj.z;
+        const T cl = dsqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        const T rc = strain * (__ldg(lRest + s) / cl);
+        t0 += rc * d0;
+        t1 += rc * d1;
+        t2 += rc * d2;
+    }
+    const V4<T> ai = ld4(Aq, i);
+    const T b0 = __ldg(lBend + b);
+    t0 += b0 * ai.x;
+    t1 += b0 * ai.y;
+    t2 += b0 * ai.z;
+    const V4<T> r0 = ld4(Rhs0, i);
+    T r_0 = r0.x + t0, r_1 = r0.y + t1, r_2 = r0.z + t2;
+    for (int s = b + 1; s < e; ++s) {  // bending terms the neighbours' stencils put on i
+        const V4<T> ak = ld4(Aq, __ldg(lNbr + s));
+        const T bt = __ldg(lBendT + s);
+        r_0 += bt * ak.x;
+        r_1 += bt * ak.y;
+        r_2 += bt * ak.z;
+    }
+    const V4<T> c = ld4(CollRhs, i);
+    r_0 += c.x;
+    r_1 += c.y;
+    r_2 += c.z;
+    const V4<T> pn = ld4(PinRhs, i);
+    r_0 += pn.x;
+    r_1 += pn.y;
+    r_2 += pn.z;
+    Rhs[i] = V4<T>{r_0, r_1, r_2, T(0)};
+    T s0, s1, s2;
+    sell_row(i, sOff, sLen, sCol, sVal, P, s0, s1, s2);
+    const T id = __ldg(InvD + i);
+    const T om = T(1) - relax;
+    Y[i] = V4<T>{om * x.x + relax * ((s0 + r_0) * id), om * x.y + relax * ((s1 + r_1) * id),
+                 om * x.z + relax * ((s2 + r_2) * id), T(0)};
+}
+
+// One weighted-Jacobi sweep S(x) = (1-w) x + w D^-1 (N x + rhs); with prev it
+// is the second half of a Chebyshev step: out = omega (S(src) - prev) + prev.
+template <typename T, bool kCheby>
+__global__ void __launch_bounds__(kBlock) k_sweep(int nsim, T relax, T omega, const V4<T>* __restrict__ src,
+                                                  const V4<T>* __restrict__ prev, V4<T>* __restrict__ out,
+                                                  const V4<T>* __restrict__ Rhs, const T* __restrict__ InvD,
+                                                  const int* __restrict__ sOff, const int* __restrict__ sLen,
+                                                  const int* __restrict__ sCol, const T* __restrict__ sVal) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim) return;
+    T s0, s1, s2;
+    sell_row(i, sOff, sLen, sCol, sVal, src, s0, s1, s2);
+    const V4<T> x = ld4(src, i);
+    const V4<T> r = ld4(Rhs, i);
+    const T id = __ldg(InvD + i);
+    const T om = T(1) - relax;
+    T y0 = om * x.x + relax * ((s0 + r.x) * id);
+    T y1 = om * x.y + relax * ((s1 + r.y) * id);
+    T y2 = om * x.z + relax * ((s2 + r.z) * id);
+    if (kCheby) {
+        const V4<T> p = ld4(prev, i);
+        y0 = omega * (y0 - p.x) + p.x;
+        y1 = omega * (y1 - p.y) + p.y;
+        y2 = omega * (y2 - p.z) + p.z;
+    }
+    out[i] = V4<T>{y0, y1, y2, T(0)};
+}
+
+template <typename T>
+__global__ void k_direction(int nsim, const V4<T>* __restrict__ P, const V4<T>* __restrict__ Pold,
+                            V4<T>* __restrict__ Dir, double* __restrict__ part) {
+    __shared__ double red[kBlock / 32];
+    double acc = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nsim; i += gridDim.x * blockDim.x) {
+        const V4<T> a = P[i], b = Pold[i];
+        const T d0 = a.x - b.x, d1 = a.y - b.y, d2 = a.z - b.z;
+        Dir[i] = V4<T>{d0, d1, d2, T(0)};
+        acc += (double)d0 * (double)d0 + (double)d1 * (double)d1 + (double)d2 * (double)d2;
+    }
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < kBlock / 32 ? red[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) part[blockIdx.x] = v;
+    }
+}
+
+template <typename T>
+__global__ void k_clamp(int nsim, const V4<T>* __restrict__ Pold, const V4<T>* __restrict__ Dir,
+                        const T* __restrict__ Toi, V4<T>* __restrict__ P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim) return;
+    const T t = *Toi;
+    const V4<T> a = Pold[i], d = Dir[i];
+    P[i] = V4<T>{a.x + t * d.x, a.y + t * d.y, a.z + t * d.z, T(0)};
+}
+
+template <typename T>
+__global__ void k_copy_old(int nsim, const V4<T>* __restrict__ P, V4<T>* __restrict__ Pold) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nsim) Pold[i] = P[i];
+}
+
+template <typename T>
+__global__ void k_velocity(int nsim, T invt, const V4<T>* __restrict__ P, const V4<T>* __restrict__ X0,
+                           V4<T>* __restrict__ Vel, unsigned int* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim) return;
+    const V4<T> a = P[i], b = X0[i];
+    if (!(isfinite(a.x) && isfinite(a.y) && isfinite(a.z))) atomicOr(err, (unsigned int)kErrNonFinite);
+    Vel[i] = V4<T>{(a.x - b.x) * invt, (a.y - b.y) * invt, (a.z - b.z) * invt, T(0)};
+}
+
+}  // namespace
+
+int direction_blocks(int nsim) { return std::min(1024, std::max(1, blocks_for(nsim))); }
+
+template <typename T, typename TC>
+void launch_predict(const Dev<T, TC>& d, T dt, cudaStream_t s) {
+    k_predict<T><<<blocks_for(d.ntot), kBlock, 0, s>>>(d.nsim, d.ntot, dt, d.P, d.Pold, d.X0, d.Vel, d.Rhs0,
+                                                         d.Dinert, d.Grav, d.InvMass, d.PinFlag, d.CollDiag,
+                                                         d.CollRhs);
+}
+template <typename T, typename TC>
+void launch_diag(const Dev<T, TC>& d, cudaStream_t s) {
+    k_diag<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Delastic, d.Dinert, d.CollDiag, d.InvD);
+}
+template <typename T, typename TC>
+void launch_local_aq(const Dev<T, TC>& d, cudaStream_t s) {
+    k_local_aq<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.lNbr, d.lLbo, d.CurvNorm, d.Aq);
+}
+template <typename T, typename TC>
+void launch_local_rhs_sweep(const Dev<T, TC>& d, T relax, cudaStream_t s) {
+    k_local_rhs_sweep<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(
+        d.nsim, relax, d.P, d.lPtr, d.lNbr, d.lRest, d.lBend, d.lBendT, d.Strain, d.Aq, d.Rhs0, d.CollRhs,
+        d.PinRhs, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal, d.Rhs, d.Y);
+}
+template <typename T, typename TC>
+void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T>* out, T relax, T omega,
+                  cudaStream_t s) {
+    if (prev)
+        k_sweep<T, true><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.Rhs, d.InvD,
+                                                              d.sOff, d.sLen, d.sCol, d.sVal);
+    else
+        k_sweep<T, false><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.Rhs,
+                                                               d.InvD, d.sOff, d.sLen, d.sCol, d.sVal);
+}
+template <typename T, typename TC>
+void launch_direction(const Dev<T, TC>& d, cudaStream_t s) {
+    const int nb = direction_blocks(d.nsim);
+    k_direction<T><<<nb, kBlock, 0, s>>>(d.nsim, d.P, d.Pold, d.Dir, d.ResidPart);
+    launch_reduce_sum_f64(d.ResidPart, nb, d.Resid, s);
+}
+template <typename T, typename TC>
+void launch_clamp(const Dev<T, TC>& d, cudaStream_t s) {
+    k_clamp<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Pold, d.Dir, d.Toi, d.P);
+}
+template <typename T, typename TC>
+void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s) {
+    k_copy_old<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.Pold);
+}
+template <typename T, typename TC>
+void launch_velocity(const Dev<T, TC>& d, T invt, cudaStream_t s) {
+    k_velocity<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, invt, d.P, d.X0, d.Vel, d.ErrFlags);
+}
+
+#define PDIPC_INST_PD(T, TC)                                                                                 \
+    template void launch_predict<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                                 \
+    template void launch_diag<T, TC>(const Dev<T, TC>&, cudaStream_t);                                       \
+    template void launch_local_aq<T, TC>(const Dev<T, TC>&, cudaStream_t);                                   \
+    template void launch_local_rhs_sweep<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                         \
+    template void launch_sweep<T, TC>(const Dev<T, TC>&, const V4<T>*, const V4<T>*, V4<T>*, T, T,           \
+                                      cudaStream_t);                                                         \
+    template void launch_direction<T, TC>(const Dev<T, TC>&, cudaStream_t);                                  \
+    template void launch_clamp<T, TC>(const Dev<T, TC>&, cudaStream_t);                                      \
+    template void launch_copy_old<T, TC>(const Dev<T, TC>&, cudaStream_t);                                   \
+    template void launch_velocity<T, TC>(const Dev<T, TC>&, T, cudaStream_t);
+
+PDIPC_INST_PD(float, float)
+PDIPC_INST_PD(double, double)
+PDIPC_INST_PD(float, double)
+
+}  // namespace pdipc

@@ -1,0 +1,724 @@
+// solver.cu — one PD-IPC context on one GPU: device tables, the step loop
+// (PdIpcSimulator::advance, Simulator/PD-IPC/PdIpcSimulator.cpp:1683-1796),
+// the patch broad phase (gpuCcdCulling, cpp:1799-1869) and the stage entry
+// points.
+//
+// Per outer iteration the host waits once, for the 8-byte residual that decides
+// the reference's stopping rule (cpp:1774-1779); the time of impact stays on the
+// device (the reference copies it to the host, cu:2738-2740).  The
+// projective-dynamics solve of an outer iteration (1 + lg x (2 + 2 cheby - 1)
+// kernels) is captured once as a CUDA graph and replayed.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "kernels.cuh"
+#include "solver.h"
+
+namespace pdipc {
+
+namespace {
+
+template <typename T>
+T omega_first(T rho2) {  // PdIpcGpuFunc.cu:1321: 2.0 / (2 - rho), stored in the working type
+    const T d = T(2) - rho2;
+    return (T)(2.0 / (double)d);
+}
+template <typename T>
+T omega_next(T rho2, T omega) {  // PdIpcGpuFunc.cu:1341
+    const T d = T(4) - rho2 * omega;
+    return (T)(4.0 / (double)d);
+}
+
+struct Pinned {
+    double resid;
+    int64_t n_pairs;
+    int64_t n_pt;
+    int64_t n_ee;
+    int n_pair_total_i32;
+    unsigned int err;
+    unsigned long long active;
+    double toi;
+    float toi_f;
+};
+
+}  // namespace
+
+#define PD_CK(call)                                                                       \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            err = std::string(#call) + ": " + cudaGetErrorString(e_);                     \
+            return PDIPC_ERR_CUDA;                                                        \
+        }                                                                                 \
+    } while (0)
+
+template <typename T, typename TC>
+class Solver final : public SolverBase {
+public:
+    Solver() = default;
+    ~Solver() override { release(); }
+
+    int n_sim() const override { return d_.nsim; }
+    int n_total() const override { return d_.ntot; }
+
+    pdipc_status init(const HostTables& H, const pdipc_params& p, std::string& err) override {
+        prm_ = p;
+        c_.dt = p.time_step;
+        c_.gravity = p.gravity;
+        c_.dhat = p.dhat;
+        c_.kappa = p.kappa;
+        c_.infl = p.inflation_radius < 0 ? 0.5 * p.dhat : p.inflation_radius;
+        c_.relax = p.jacobi_relax;
+        c_.rho = p.cheby_rho;
+        c_.toi_scale = p.toi_scale;
+        c_.ccd_slack = p.ccd_slack;
+        c_.ccd_eta = p.ccd_eta;
+        c_.static_mass = p.static_mass;
+        c_.lg = p.lg_iterations;
+        c_.cheby = p.cheby_iterations;
+        c_.ccd_max_iter = p.ccd_max_iter;
+        if (c_.lg < 1 || c_.cheby < 1 || p.max_outer < 1 || p.time_step <= 0) {
+            err = "lg_iterations, cheby_iterations, max_outer and time_step must be positive";
+            return PDIPC_ERR_ARG;
+        }
+        PD_CK(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
+        PD_CK(cudaEventCreate(&ev0_));
+        PD_CK(cudaEventCreate(&ev1_));
+        Dev<T, TC>& d = d_;
+        d.nsim = H.nsim;
+        d.ntot = H.ntot;
+        d.nface = (int)H.faces.size() / 3;
+        d.nedge = (int)H.edges.size() / 2;
+        d.npatch = H.npatch;
+        const int ns = d.nsim, nt = d.ntot;
+
+        // ---- vertex state ----
+        std::vector<V4<T>> X(nt);
+        for (int i = 0; i < nt; ++i) X[i] = V4<T>{(T)H.X[3 * i], (T)H.X[3 * i + 1], (T)H.X[3 * i + 2], T(0)};
+        PD_CK(up(d.P, X));
+        PD_CK(up(d.Xrest, X));
+        PD_CK(up(d.Pold, X));
+        PD_CK(zeros(d.X0, ns));
+        PD_CK(zeros(d.Vel, ns));
+        PD_CK(zeros(d.Dir, nt));
+        PD_CK(zeros(d.Y, ns));
+        PD_CK(zeros(d.B, ns));
+        PD_CK(zeros(d.Aq, ns));
+        PD_CK(zeros(d.Rhs, ns));
+        PD_CK(zeros(d.Rhs0, ns));
+        PD_CK(zeros(d.Dinert, ns));
+        PD_CK(zeros(d.InvD, ns));
+        PD_CK(zeros(d.CollDiag, nt));
+        PD_CK(zeros(d.CollRhs, nt));
+        PD_CK(zeros(scratch_, nt));
+        std::vector<V4<T>> grav(ns), pinr(ns);
+        std::vector<T> invm(ns), de(ns), cn(ns), st(ns);
+        std::vector<int> pinf(ns);
+        const T g = (T)p.gravity;
+        for (int i = 0; i < ns; ++i) {
+            grav[i] = V4<T>{T(0), g * (T)H.mass[i], T(0), T(0)};
+            invm[i] = (T)(1.0 / H.mass[i]);
+            de[i] = (T)H.Delastic[i];
+            cn[i] = (T)H.curvNorm[i];
+            st[i] = (T)H.strain[i];
+            pinf[i] = H.pinSlot[i];
+            if (H.pinSlot[i] >= 0) {
+                const T k = (T)H.pinK[H.pinSlot[i]];
+                pinr[i] = V4<T>{k * X[i].x, k * X[i].y, k * X[i].z, T(0)};
+            } else {
+                pinr[i] = V4<T>{T(0), T(0), T(0), T(0)};
+            }
+        }
+        PD_CK(up(d.Grav, grav));
+        PD_CK(up(d.PinRhs, pinr));
+        PD_CK(up(d.InvMass, invm));
+        PD_CK(up(d.Delastic, de));
+        PD_CK(up(d.CurvNorm, cn));
+        PD_CK(up(d.Strain, st));
+        PD_CK(up(d.PinFlag, pinf));
+        std::vector<TC> cm(nt, (TC)p.static_mass);
+        for (int i = 0; i < ns; ++i) cm[i] = (TC)(T)H.collMassSim[i];
+        PD_CK(up(d.CollMass, cm));
+
+        // ---- local-step stencils ----
+        PD_CK(up(d.lPtr, H.lPtr));
+        PD_CK(up(d.lNbr, H.lNbr));
+        PD_CK(up(d.lRest, conv(H.lRest)));
+        PD_CK(up(d.lLbo, conv(H.lLbo)));
+        PD_CK(up(d.lBend, conv(H.lBend)));
+        PD_CK(up(d.lBendT, conv(H.lBendT)));
+
+        // ---- system matrix in SELL-32 ----
+        d.nslice = (ns + kSlice - 1) / kSlice;
+        std::vector<int> soff(d.nslice + 1, 0), slen(d.nslice, 0);
+        for (int sl = 0; sl < d.nslice; ++sl) {
+            int w = 0;
+            for (int r = sl * kSlice; r < std::min(ns, (sl + 1) * kSlice); ++r) w = std::max(w, H.nPtr[r + 1] - H.nPtr[r]);
+            slen[sl] = w;
+            soff[sl + 1] = soff[sl] + kSlice * w;
+        }
+        std::vector<int> scol(soff[d.nslice], 0);
+        std::vector<T> sval(soff[d.nslice], T(0));
+        for (int sl = 0; sl < d.nslice; ++sl)
+            for (int lane = 0; lane < kSlice; ++lane) {
+                const int r = sl * kSlice + lane;
+                const int len = r < ns ? H.nPtr[r + 1] - H.nPtr[r] : 0;
+                for (int k = 0; k < slen[sl]; ++k) {
+                    const size_t at = (size_t)soff[sl] + (size_t)kSlice * k + lane;
+                    if (k < len) {
+                        scol[at] = H.nCol[H.nPtr[r] + k];
+                        sval[at] = (T)H.nVal[H.nPtr[r] + k];
+                    } else {
+                        scol[at] = r < ns ? r : 0;  // padding: own row, zero weight
+                        sval[at] = T(0);
+                    }
+                }
+            }
+        sell_entries_ = (int64_t)H.nPtr[ns];
+        sell_padded_ = (int64_t)soff[d.nslice];
+        PD_CK(up(d.sOff, soff));
+        PD_CK(up(d.sLen, slen));
+        PD_CK(up(d.sCol, scol));
+        PD_CK(up(d.sVal, sval));
+
+        // ---- collision topology ----
+        std::vector<int4> faces(d.nface);
+        for (int f = 0; f < d.nface; ++f) faces[f] = make_int4(H.faces[3 * f], H.faces[3 * f + 1], H.faces[3 * f + 2], 0);
+        std::vector<int2> edges(d.nedge);
+        for (int e = 0; e < d.nedge; ++e) edges[e] = make_int2(H.edges[2 * e], H.edges[2 * e + 1]);
+        PD_CK(up(d.Faces, faces));
+        PD_CK(up(d.Edges, edges));
+        PD_CK(up(d.pfPtr, H.pfPtr));
+        PD_CK(up(d.pfIdx, H.pfIdx));
+        PD_CK(up(d.ppPtr, H.ppPtr));
+        PD_CK(up(d.ppIdx, H.ppIdx));
+        PD_CK(up(d.pePtr, H.pePtr));
+        PD_CK(up(d.peIdx, H.peIdx));
+        PD_CK(up(d.pxPtr, H.pxPtr));
+        PD_CK(up(d.pxIdx, H.pxIdx));
+        PD_CK(up(d.pStatic, H.pStatic));
+        const int np = std::max(1, d.npatch);
+        PD_CK(zeros(d.PatchBox, np));
+        PD_CK(zeros(d.NodeBox, 2 * np));
+        PD_CK(zeros(d.NodeChild, np));
+        PD_CK(zeros(d.NodeParent, 2 * np));
+        PD_CK(zeros(d.LeafPatch, np));
+        PD_CK(zeros(d.RefitFlag, np));
+        PD_CK(zeros(d.Morton, np));
+        PD_CK(zeros(cnt_, np + 1));
+        PD_CK(zeros(off_, np + 1));
+
+        // ---- scalars ----
+        PD_CK(zeros(d.ToiMin, 1));
+        const TC one = TC(1);
+        PD_CK(cudaMemcpy(d.ToiMin, &one, sizeof(TC), cudaMemcpyHostToDevice));
+        PD_CK(zeros(d.Toi, 1));
+        PD_CK(zeros(d.ResidPart, direction_blocks(ns)));
+        PD_CK(zeros(d.Resid, 1));
+        PD_CK(zeros(d.ErrFlags, 1));
+        PD_CK(zeros(d.ActiveCount, 1));
+        PD_CK(cudaMallocHost(&pin_, sizeof(Pinned)));
+        std::memset(pin_, 0, sizeof(Pinned));
+        PD_CK(cudaMallocHost(&stage_, sizeof(V4<T>) * (size_t)std::max(nt, 1)));
+
+        // ---- patch tree at the rest positions (AipcBvhs::init at initialization) ----
+        pdipc_status r = build_tree(true, err);
+        if (r != PDIPC_OK) return r;
+        PD_CK(cudaStreamSynchronize(s_));
+        inited_ = true;
+        return PDIPC_OK;
+    }
+
+    pdipc_status step(int n, std::string& err) override {
+        if (!inited_) {
+            err = "not initialized";
+            return PDIPC_ERR_STATE;
+        }
+        if (n < 0) {
+            err = "negative step count";
+            return PDIPC_ERR_ARG;
+        }
+        launches_ = 0;
+        device_ms_ = 0.0;
+        st_.max_outer_iters = 0;
+        st_.total_outer_iters = 0;
+        for (int k = 0; k < n; ++k) {
+            PD_CK(cudaEventRecord(ev0_, s_));
+            pdipc_status r = step_once(err);
+            if (r != PDIPC_OK) return r;
+            PD_CK(cudaEventRecord(ev1_, s_));
+            PD_CK(cudaEventSynchronize(ev1_));
+            float ms = 0.f;
+            PD_CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
+            device_ms_ += ms;
+        }
+        return PDIPC_OK;
+    }
+
+    pdipc_status get_positions(double* out, std::string& err) override {
+        PD_CK(cudaMemcpyAsync(stage_, d_.P, sizeof(V4<T>) * d_.ntot, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        for (int i = 0; i < d_.ntot; ++i) {
+            out[3 * (size_t)i] = (double)stage_[i].x;
+            out[3 * (size_t)i + 1] = (double)stage_[i].y;
+            out[3 * (size_t)i + 2] = (double)stage_[i].z;
+        }
+        return PDIPC_OK;
+    }
+    pdipc_status get_velocities(double* out, std::string& err) override {
+        PD_CK(cudaMemcpyAsync(stage_, d_.Vel, sizeof(V4<T>) * d_.nsim, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        for (int i = 0; i < d_.nsim; ++i) {
+            out[3 * (size_t)i] = (double)stage_[i].x;
+            out[3 * (size_t)i + 1] = (double)stage_[i].y;
+            out[3 * (size_t)i + 2] = (double)stage_[i].z;
+        }
+        return PDIPC_OK;
+    }
+    pdipc_status upload_vec(V4<T>* dst, const double* src, int n, std::string& err) {
+        PD_CK(cudaStreamSynchronize(s_));
+        for (int i = 0; i < n; ++i)
+            stage_[i] = V4<T>{(T)src[3 * (size_t)i], (T)src[3 * (size_t)i + 1], (T)src[3 * (size_t)i + 2], T(0)};
+        PD_CK(cudaMemcpyAsync(dst, stage_, sizeof(V4<T>) * n, cudaMemcpyHostToDevice, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        return PDIPC_OK;
+    }
+    pdipc_status set_state(const double* X, const double* V, std::string& err) override {
+        pdipc_status r = upload_vec(d_.P, X, d_.ntot, err);
+        if (r != PDIPC_OK) return r;
+        if (V) return upload_vec(d_.Vel, V, d_.nsim, err);
+        return PDIPC_OK;
+    }
+    pdipc_status reset(std::string& err) override {
+        PD_CK(cudaMemcpyAsync(d_.P, d_.Xrest, sizeof(V4<T>) * d_.ntot, cudaMemcpyDeviceToDevice, s_));
+        PD_CK(cudaMemsetAsync(d_.Vel, 0, sizeof(V4<T>) * d_.nsim, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        st_.steps_done = 0;
+        return PDIPC_OK;
+    }
+    void stats(pdipc_stats* s) override {
+        *s = st_;
+        s->n_sim = d_.nsim;
+        s->n_total = d_.ntot;
+        s->n_patches = d_.npatch;
+        s->precision = prm_.precision;
+        s->device_bytes = bytes_;
+        s->kernel_launches = launches_;
+        s->device_ms = device_ms_;
+    }
+
+    // ---------------- stages ----------------
+    pdipc_status stage_broadphase(const double* xo, const double* dx, int* pairs, int64_t cap_pairs,
+                                  int64_t* n_pairs, int* pt, int64_t cap_pt, int64_t* n_pt, int* ee, int64_t cap_ee,
+                                  int64_t* n_ee, std::string& err) override {
+        pdipc_status r = upload_vec(d_.Pold, xo, d_.ntot, err);
+        if (r == PDIPC_OK) r = upload_vec(d_.Dir, dx, d_.ntot, err);
+        if (r == PDIPC_OK) r = broadphase(err);
+        if (r != PDIPC_OK) return r;
+        PD_CK(cudaMemsetAsync(d_.Dir, 0, sizeof(V4<T>) * d_.ntot, s_));
+        *n_pairs = d_.nPairs;
+        *n_pt = d_.nPT;
+        *n_ee = d_.nEE;
+        if (d_.nPairs > cap_pairs || d_.nPT > cap_pt || d_.nEE > cap_ee) {
+            PD_CK(cudaStreamSynchronize(s_));
+            return PDIPC_ERR_OVERFLOW;
+        }
+        if (d_.nPairs) PD_CK(cudaMemcpyAsync(pairs, d_.Pairs, sizeof(int2) * d_.nPairs, cudaMemcpyDeviceToHost, s_));
+        if (d_.nPT) PD_CK(cudaMemcpyAsync(pt, d_.PT, sizeof(int4) * d_.nPT, cudaMemcpyDeviceToHost, s_));
+        if (d_.nEE) PD_CK(cudaMemcpyAsync(ee, d_.EE, sizeof(int4) * d_.nEE, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        return PDIPC_OK;
+    }
+    pdipc_status stage_morton(uint64_t* codes, int* order, int cap, std::string& err) override {
+        if (cap < d_.npatch) return PDIPC_ERR_OVERFLOW;
+        if (d_.npatch == 0) return PDIPC_OK;
+        PD_CK(cudaMemcpyAsync(codes, d_.Morton, sizeof(uint64_t) * d_.npatch, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaMemcpyAsync(order, d_.LeafPatch, sizeof(int) * d_.npatch, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        return PDIPC_OK;
+    }
+    pdipc_status stage_toi(const double* x0, const double* x1, double* tpt, double* tee, double* tg,
+                           std::string& err) override {
+        pdipc_status r = upload_vec(d_.Pold, x0, d_.ntot, err);
+        if (r == PDIPC_OK) r = upload_vec(scratch_, x1, d_.ntot, err);
+        if (r != PDIPC_OK) return r;
+        TC *ppt = nullptr, *pee = nullptr;
+        if (d_.nPT) PD_CK(cudaMalloc(&ppt, sizeof(TC) * d_.nPT));
+        if (d_.nEE) PD_CK(cudaMalloc(&pee, sizeof(TC) * d_.nEE));
+        launch_toi(d_, d_.Pold, scratch_, c_, ppt, pee, s_);
+        launch_toi_finalize(d_, c_, s_);
+        T toi;
+        PD_CK(cudaMemcpyAsync(&toi, d_.Toi, sizeof(T), cudaMemcpyDeviceToHost, s_));
+        std::vector<TC> hp(d_.nPT), he(d_.nEE);
+        if (d_.nPT) PD_CK(cudaMemcpyAsync(hp.data(), ppt, sizeof(TC) * d_.nPT, cudaMemcpyDeviceToHost, s_));
+        if (d_.nEE) PD_CK(cudaMemcpyAsync(he.data(), pee, sizeof(TC) * d_.nEE, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        cudaFree(ppt);
+        cudaFree(pee);
+        if (tpt) for (int64_t i = 0; i < d_.nPT; ++i) tpt[i] = (double)hp[i];
+        if (tee) for (int64_t i = 0; i < d_.nEE; ++i) tee[i] = (double)he[i];
+        if (tg) *tg = (double)toi;
+        return PDIPC_OK;
+    }
+    pdipc_status stage_contact(const double* x, double* diag, double* rhs, int64_t* n_active,
+                               std::string& err) override {
+        pdipc_status r = upload_vec(scratch_, x, d_.ntot, err);
+        if (r != PDIPC_OK) return r;
+        launch_contact(d_, scratch_, c_, s_);
+        std::vector<T> hd(d_.ntot);
+        PD_CK(cudaMemcpyAsync(hd.data(), d_.CollDiag, sizeof(T) * d_.ntot, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaMemcpyAsync(stage_, d_.CollRhs, sizeof(V4<T>) * d_.ntot, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaMemcpyAsync(&pin_->active, d_.ActiveCount, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        for (int i = 0; i < d_.ntot; ++i) {
+            diag[i] = (double)hd[i];
+            rhs[3 * (size_t)i] = (double)stage_[i].x;
+            rhs[3 * (size_t)i + 1] = (double)stage_[i].y;
+            rhs[3 * (size_t)i + 2] = (double)stage_[i].z;
+        }
+        if (n_active) *n_active = (int64_t)pin_->active;
+        PD_CK(cudaMemsetAsync(d_.CollDiag, 0, sizeof(T) * d_.ntot, s_));
+        PD_CK(cudaMemsetAsync(d_.CollRhs, 0, sizeof(V4<T>) * d_.ntot, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        return PDIPC_OK;
+    }
+    pdipc_status stage_pd(const double* X, const double* V, double* out, std::string& err) override {
+        std::vector<double> saveX(3 * (size_t)d_.ntot), saveV(3 * (size_t)d_.nsim);
+        pdipc_status r = get_positions(saveX.data(), err);
+        if (r == PDIPC_OK) r = get_velocities(saveV.data(), err);
+        if (r == PDIPC_OK) r = set_state(X, V, err);
+        if (r != PDIPC_OK) return r;
+        launch_predict(d_, (T)c_.dt, s_);
+        enqueue_pd();
+        r = get_positions(out, err);
+        if (r == PDIPC_OK) r = set_state(saveX.data(), saveV.data(), err);
+        return r;
+    }
+
+    pdipc_status sweep_timing(int launches, double* avg_ms, double* bytes, std::string& err) override {
+        const T w = (T)c_.relax;
+        launch_diag(d_, s_);
+        launch_sweep<T, TC>(d_, d_.P, nullptr, d_.Y, w, T(0), s_);  // warm
+        PD_CK(cudaEventRecord(ev0_, s_));
+        for (int k = 0; k < launches; ++k) launch_sweep<T, TC>(d_, d_.P, nullptr, d_.Y, w, T(0), s_);
+        PD_CK(cudaEventRecord(ev1_, s_));
+        PD_CK(cudaEventSynchronize(ev1_));
+        float ms = 0.f;
+        PD_CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
+        *avg_ms = (double)ms / launches;
+        const double vec = 3.0 * sizeof(T);
+        *bytes = (double)sell_entries_ * (sizeof(int) + sizeof(T)) + (double)d_.nsim * (3.0 * vec + sizeof(T));
+        return PDIPC_OK;
+    }
+
+private:
+    // ---------------- allocation helpers ----------------
+    template <typename X>
+    cudaError_t alloc(X*& p, size_t n) {
+        n = std::max<size_t>(n, 1);
+        cudaError_t e = cudaMalloc(&p, sizeof(X) * n);
+        if (e == cudaSuccess) {
+            ptrs_.push_back({(void*)p, sizeof(X) * n});
+            bytes_ += (int64_t)(sizeof(X) * n);
+        }
+        return e;
+    }
+    template <typename X>
+    cudaError_t zeros(X*& p, size_t n) {
+        cudaError_t e = alloc(p, n);
+        if (e != cudaSuccess) return e;
+        return cudaMemset(p, 0, sizeof(X) * std::max<size_t>(n, 1));
+    }
+    template <typename X>
+    cudaError_t up(X*& p, const std::vector<X>& v) {
+        cudaError_t e = alloc(p, v.size());
+        if (e != cudaSuccess || v.empty()) return e;
+        return cudaMemcpy(p, v.data(), sizeof(X) * v.size(), cudaMemcpyHostToDevice);
+    }
+    template <typename X>
+    void dfree(X*& p) {
+        if (!p) return;
+        for (size_t i = 0; i < ptrs_.size(); ++i)
+            if (ptrs_[i].first == (void*)p) {
+                bytes_ -= (int64_t)ptrs_[i].second;
+                ptrs_.erase(ptrs_.begin() + i);
+                break;
+            }
+        cudaFree(p);
+        p = nullptr;
+    }
+    template <typename X>
+    cudaError_t grow(X*& p, int64_t& cap, int64_t need) {
+        if (need <= cap && p) return cudaSuccess;
+        const int64_t nc = std::max<int64_t>(need + need / 4, 1024);
+        dfree(p);
+        cudaError_t e = alloc(p, (size_t)nc);
+        cap = (e == cudaSuccess) ? nc : 0;
+        return e;
+    }
+    static std::vector<T> conv(const std::vector<double>& v) {
+        std::vector<T> o(v.size());
+        for (size_t i = 0; i < v.size(); ++i) o[i] = (T)v[i];
+        return o;
+    }
+    void release() {
+        if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+        if (graph_) cudaGraphDestroy(graph_);
+        graph_exec_ = nullptr;
+        graph_ = nullptr;
+        for (auto& pr : ptrs_) cudaFree(pr.first);
+        ptrs_.clear();
+        if (pin_) cudaFreeHost(pin_);
+        if (stage_) cudaFreeHost(stage_);
+        pin_ = nullptr;
+        stage_ = nullptr;
+        if (ev0_) cudaEventDestroy(ev0_);
+        if (ev1_) cudaEventDestroy(ev1_);
+        ev0_ = ev1_ = nullptr;
+        if (s_) cudaStreamDestroy(s_);
+        s_ = nullptr;
+    }
+
+    // ---------------- patch tree ----------------
+    pdipc_status build_tree(bool from_rest, std::string& err) {
+        Dev<T, TC>& d = d_;
+        if (d.npatch == 0) return PDIPC_OK;
+        const T infl = (T)c_.infl;
+        if (from_rest) {
+            launch_patch_init_boxes(d, infl, s_);
+            ++launches_;
+        }
+        T* cs = nullptr;
+        unsigned long long* keys = nullptr;
+        int* vals = nullptr;
+        void* tmp = nullptr;
+        PD_CK(cudaMalloc(&cs, sizeof(T) * 4));
+        PD_CK(cudaMalloc(&keys, sizeof(unsigned long long) * d.npatch));
+        PD_CK(cudaMalloc(&vals, sizeof(int) * d.npatch));
+        PD_CK(cudaMalloc(&tmp, sort_tmp_bytes(d.npatch)));
+        launch_morton(d, cs, keys, vals, s_);
+        radix_sort_u64(keys, vals, d.npatch, tmp, s_);
+        PD_CK(cudaMemcpyAsync(d.LeafPatch, vals, sizeof(int) * d.npatch, cudaMemcpyDeviceToDevice, s_));
+        launch_karras(d, keys, s_);
+        launches_ += 3 + 8 * 3;
+        PD_CK(cudaStreamSynchronize(s_));
+        cudaFree(cs);
+        cudaFree(keys);
+        cudaFree(vals);
+        cudaFree(tmp);
+        PD_CK(cudaGetLastError());
+        return PDIPC_OK;
+    }
+
+    pdipc_status ensure_scan_tmp(int64_t n, std::string& err) {
+        const int64_t need = (int64_t)scan_tmp_bytes(n);
+        if (need <= scan_tmp_cap_ && scan_tmp_) return PDIPC_OK;
+        if (scan_tmp_) dfree(scan_tmp_);
+        scan_tmp_cap_ = need * 2;
+        PD_CK(alloc(scan_tmp_, (size_t)scan_tmp_cap_));
+        return PDIPC_OK;
+    }
+
+    // gpuCcdCulling (cpp:1799-1869) from Pold and Dir.
+    pdipc_status broadphase(std::string& err) {
+        Dev<T, TC>& d = d_;
+        d.nPairs = d.nPT = d.nEE = 0;
+        if (d.npatch == 0) return PDIPC_OK;
+        const T infl = (T)c_.infl;
+        launch_patch_boxes(d, d.Pold, d.Dir, infl, s_);
+        ++launches_;
+        if (prm_.rebuild_bvh) {
+            pdipc_status r = build_tree(false, err);
+            if (r != PDIPC_OK) return r;
+        }
+        launch_refit(d, s_);
+        launch_traverse(d, cnt_, nullptr, nullptr, s_);
+        launches_ += 2;
+        pdipc_status r = ensure_scan_tmp(d.npatch + 1, err);
+        if (r != PDIPC_OK) return r;
+        scan_exclusive_i32(cnt_, off_, d.npatch, &off_[d.npatch], (int*)scan_tmp_, s_);
+        launches_ += 2;
+        PD_CK(cudaMemcpyAsync(&pin_->n_pair_total_i32, &off_[d.npatch], sizeof(int), cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        d.nPairs = pin_->n_pair_total_i32;
+        if (d.nPairs == 0) return PDIPC_OK;
+        const int64_t capBefore = d.capPairs;
+        PD_CK(grow(d.Pairs, d.capPairs, d.nPairs));
+        if (d.capPairs != capBefore || !cpt_) {
+            int64_t c1 = 0, c2 = 0, c3 = 0, c4 = 0;
+            if (cpt_) { dfree(cpt_); dfree(cee_); dfree(opt_); dfree(oee_); }
+            PD_CK(grow(cpt_, c1, d.capPairs));
+            PD_CK(grow(cee_, c2, d.capPairs));
+            PD_CK(grow(opt_, c3, d.capPairs + 1));
+            PD_CK(grow(oee_, c4, d.capPairs + 1));
+        }
+        launch_traverse(d, nullptr, off_, d.Pairs, s_);
+        launch_pair_counts(d, cpt_, cee_, s_);
+        launches_ += 2;
+        r = ensure_scan_tmp(d.nPairs + 1, err);
+        if (r != PDIPC_OK) return r;
+        scan_exclusive_i64(cpt_, opt_, d.nPairs, opt_ + d.nPairs, scan_tmp_, s_);
+        scan_exclusive_i64(cee_, oee_, d.nPairs, oee_ + d.nPairs, scan_tmp_, s_);
+        launches_ += 4;
+        PD_CK(cudaMemcpyAsync(&pin_->n_pt, opt_ + d.nPairs, sizeof(int64_t), cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaMemcpyAsync(&pin_->n_ee, oee_ + d.nPairs, sizeof(int64_t), cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        d.nPT = pin_->n_pt;
+        d.nEE = pin_->n_ee;
+        PD_CK(grow(d.PT, d.capPT, d.nPT));
+        PD_CK(grow(d.EE, d.capEE, d.nEE));
+        launch_expand(d, opt_, oee_, s_);
+        ++launches_;
+        st_.patch_pairs = d.nPairs;
+        st_.pt_candidates = d.nPT;
+        st_.ee_candidates = d.nEE;
+        PD_CK(cudaGetLastError());
+        return PDIPC_OK;
+    }
+
+    // ---------------- projective dynamics ----------------
+    // One outer iteration's solve: diagonal, then lg x (local step + Chebyshev
+    // accelerated Jacobi).  R2 x + c is evaluated as two weighted-Jacobi sweeps
+    // S(S(x)); the iterates rotate through P and B, the last lands in P.
+    int enqueue_pd() {
+        Dev<T, TC>& d = d_;
+        const T w = (T)c_.relax;
+        T rho2 = (T)c_.rho;
+        rho2 = rho2 * rho2;
+        int k = 0;
+        launch_diag(d, s_);
+        ++k;
+        for (int lg = 0; lg < c_.lg; ++lg) {
+            launch_local_aq(d, s_);
+            launch_local_rhs_sweep(d, w, s_);
+            launch_sweep<T, TC>(d, d.Y, nullptr, c_.cheby == 1 ? d.P : d.B, w, T(0), s_);
+            k += 3;
+            T om = omega_first(rho2);
+            for (int it = 1; it < c_.cheby; ++it) {
+                V4<T>* cur = (it & 1) ? d.B : d.P;
+                V4<T>* prv = (it & 1) ? d.P : d.B;
+                V4<T>* out = (it == c_.cheby - 1) ? d.P : prv;
+                launch_sweep<T, TC>(d, cur, nullptr, d.Y, w, T(0), s_);
+                launch_sweep<T, TC>(d, d.Y, prv, out, w, om, s_);
+                k += 2;
+                om = omega_next(rho2, om);
+            }
+        }
+        return k;
+    }
+
+    pdipc_status pd_solve(std::string& err) {
+        if (!prm_.use_graphs) {
+            launches_ += enqueue_pd();
+            return PDIPC_OK;
+        }
+        if (!graph_exec_) {
+            PD_CK(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
+            graph_nodes_ = enqueue_pd();
+            PD_CK(cudaStreamEndCapture(s_, &graph_));
+            PD_CK(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+        }
+        PD_CK(cudaGraphLaunch(graph_exec_, s_));
+        launches_ += graph_nodes_;
+        return PDIPC_OK;
+    }
+
+    // PdIpcSimulator::advance (cpp:1683-1796)
+    pdipc_status step_once(std::string& err) {
+        Dev<T, TC>& d = d_;
+        const T dt = (T)c_.dt;
+        launch_predict(d, dt, s_);
+        ++launches_;
+        const int max_outer = prm_.fixed_outer > 0 ? prm_.fixed_outer : prm_.max_outer;
+        int outer = 0;
+        for (; outer < max_outer; ++outer) {
+            pdipc_status r = pd_solve(err);
+            if (r != PDIPC_OK) return r;
+            launch_direction(d, s_);
+            launches_ += 2;
+            if (outer == 0) {
+                r = broadphase(err);
+                if (r != PDIPC_OK) return r;
+            }
+            launch_toi(d, d.Pold, d.P, c_, (TC*)nullptr, (TC*)nullptr, s_);
+            launch_toi_finalize(d, c_, s_);
+            launch_clamp(d, s_);
+            launch_contact(d, d.P, c_, s_);
+            launches_ += (d.nPT > 0) + (d.nEE > 0) + 1 + 1 + (d.nPT > 0) + (d.nEE > 0);
+            PD_CK(cudaMemcpyAsync(&pin_->resid, d.Resid, sizeof(double), cudaMemcpyDeviceToHost, s_));
+            PD_CK(cudaStreamSynchronize(s_));
+            const double res = pin_->resid;
+            st_.last_residual = res;
+            if (prm_.fixed_outer <= 0 && res < prm_.outer_tol && outer > 0) {
+                ++outer;
+                break;
+            }
+            launch_copy_old(d, s_);
+            ++launches_;
+        }
+        const T damping = (T)(1.0 - (double)dt);
+        const T invt = (T)((1.0 / (double)dt) * (double)damping);
+        launch_velocity(d, invt, s_);
+        ++launches_;
+        PD_CK(cudaMemcpyAsync(&pin_->err, d.ErrFlags, sizeof(unsigned int), cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaMemcpyAsync(&pin_->active, d.ActiveCount, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s_));
+        T toi;
+        PD_CK(cudaMemcpyAsync(&toi, d.Toi, sizeof(T), cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        PD_CK(cudaGetLastError());
+        st_.last_toi = (double)toi;
+        st_.active_contacts = (int64_t)pin_->active;
+        st_.last_outer_iters = outer;
+        st_.total_outer_iters += outer;
+        st_.max_outer_iters = std::max(st_.max_outer_iters, outer);
+        st_.steps_done++;
+        if (pin_->err) {
+            const unsigned int e = pin_->err;
+            pin_->err = 0;
+            cudaMemsetAsync(d.ErrFlags, 0, sizeof(unsigned int), s_);
+            if (e & kErrNonFinite) {
+                err = "non-finite position after the step";
+                return PDIPC_ERR_NONFINITE;
+            }
+            err = "broad-phase traversal stack overflow";
+            return PDIPC_ERR_OVERFLOW;
+        }
+        return PDIPC_OK;
+    }
+
+    Dev<T, TC> d_;
+    pdipc_params prm_{};
+    SolverConsts c_{};
+    cudaStream_t s_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    double device_ms_ = 0.0;
+    std::vector<std::pair<void*, size_t>> ptrs_;
+    int64_t bytes_ = 0;
+    int64_t launches_ = 0;
+    int64_t sell_entries_ = 0, sell_padded_ = 0;
+    V4<T>* scratch_ = nullptr;
+    int* cnt_ = nullptr;
+    int* off_ = nullptr;
+    int64_t* cpt_ = nullptr;
+    int64_t* cee_ = nullptr;
+    int64_t* opt_ = nullptr;
+    int64_t* oee_ = nullptr;
+    char* scan_tmp_ = nullptr;
+    int64_t scan_tmp_cap_ = 0;
+    Pinned* pin_ = nullptr;
+    V4<T>* stage_ = nullptr;
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    int graph_nodes_ = 0;
+    bool inited_ = false;
+    pdipc_stats st_{};
+};
+
+std::unique_ptr<SolverBase> make_solver(int precision) {
+    if (precision == PDIPC_PREC_FP64) return std::unique_ptr<SolverBase>(new Solver<double, double>());
+    if (precision == PDIPC_PREC_MIXED) return std::unique_ptr<SolverBase>(new Solver<float, double>());
+    return std::unique_ptr<SolverBase>(new Solver<float, float>());
+}
+
+}  // namespace pdipc

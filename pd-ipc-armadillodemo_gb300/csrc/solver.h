@@ -1,0 +1,39 @@
+// solver.h — precision-independent interface of one PD-IPC context's device solver.
+#pragma once
+
+#include <memory>
+#include <string>
+
+#include "../../include/pdipc.h"
+#include "host_tables.h"
+
+namespace pdipc {
+
+class SolverBase {
+public:
+    virtual ~SolverBase() = default;
+    // Upload the tables and build the patch tree.  Returns "" or an error.
+    virtual pdipc_status init(const HostTables& H, const pdipc_params& p, std::string& err) = 0;
+    virtual pdipc_status step(int n, std::string& err) = 0;
+    virtual pdipc_status get_positions(double* out, std::string& err) = 0;
+    virtual pdipc_status get_velocities(double* out, std::string& err) = 0;
+    virtual pdipc_status set_state(const double* X, const double* V, std::string& err) = 0;
+    virtual pdipc_status reset(std::string& err) = 0;
+    virtual void stats(pdipc_stats* s) = 0;
+    virtual pdipc_status stage_broadphase(const double* xo, const double* dx, int* pairs, int64_t cap_pairs,
+                                          int64_t* n_pairs, int* pt, int64_t cap_pt, int64_t* n_pt, int* ee,
+                                          int64_t cap_ee, int64_t* n_ee, std::string& err) = 0;
+    virtual pdipc_status stage_morton(uint64_t* codes, int* order, int cap, std::string& err) = 0;
+    virtual pdipc_status stage_toi(const double* x0, const double* x1, double* tpt, double* tee, double* tg,
+                                   std::string& err) = 0;
+    virtual pdipc_status stage_contact(const double* x, double* diag, double* rhs, int64_t* n_active,
+                                       std::string& err) = 0;
+    virtual pdipc_status stage_pd(const double* X, const double* V, double* out, std::string& err) = 0;
+    virtual pdipc_status sweep_timing(int launches, double* avg_ms, double* bytes, std::string& err) = 0;
+    virtual int n_sim() const = 0;
+    virtual int n_total() const = 0;
+};
+
+std::unique_ptr<SolverBase> make_solver(int precision);
+
+}  // namespace pdipc

@@ -1,0 +1,292 @@
+"""Python binding of libpdipc.so, the GB300 PD-IPC cloth step.
+
+``Simulator`` mirrors the reference's PD_IPC::PdIpcSimulator lifecycle
+(Simulator/PD-IPC/PdIpcSimulator.h): add models, ``initialization()``,
+``run(frame)`` / ``animate(frame)``, ``postRun()`` positions,
+``saveSimulator(frame)``.  Every call goes through the C ABI in
+include/pdipc.h.  There is no fallback: if the CUDA library is missing or no
+GB300 is present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import (PDIPC_ERR_CUDA, PDIPC_ERR_OVERFLOW, PDIPC_OK, PRECISIONS, STATUS_NAMES, Params, Stats,  # noqa: F401
+                  default_params, params_for_scene)
+from . import scenes  # noqa: F401
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "libpdipc.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_i64p = C.POINTER(C.c_int64)
+_lib = None
+
+# every entry point declared in include/pdipc.h
+EXPORTS = [
+    "pdipc_default_params", "pdipc_create", "pdipc_add_cloth", "pdipc_add_static", "pdipc_initialize",
+    "pdipc_step", "pdipc_animate", "pdipc_get_positions", "pdipc_get_velocities", "pdipc_set_state",
+    "pdipc_reset", "pdipc_get_stats", "pdipc_save", "pdipc_load", "pdipc_destroy", "pdipc_status_string",
+    "pdipc_last_error", "pdipc_abi_version", "pdipc_stage_broadphase", "pdipc_stage_morton", "pdipc_stage_toi",
+    "pdipc_stage_contact", "pdipc_stage_pd", "pdipc_mesh_topology",
+    "pdipc_stage_sweep_timing",
+]
+
+
+class PdipcError(RuntimeError):
+    def __init__(self, status: int, what: str, detail: str = ""):
+        self.status = status
+        msg = f"{what}: {STATUS_NAMES.get(status, status)}"
+        if detail:
+            msg += f" ({detail})"
+        super().__init__(msg)
+
+
+def load_library(path: str | None = None):
+    """Load libpdipc.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise ImportError(f"{path} not built: run __graft_entry__.build() or pdipc/build.py")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.pdipc_default_params.argtypes = [C.POINTER(Params)]
+    L.pdipc_default_params.restype = None
+    L.pdipc_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
+    L.pdipc_add_cloth.argtypes = [vp, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double, C.c_double, _ip,
+                                  C.c_int, C.c_double, C.c_int]
+    L.pdipc_add_static.argtypes = [vp, _dp, C.c_int, _ip, C.c_int, C.c_int]
+    L.pdipc_initialize.argtypes = [vp]
+    L.pdipc_step.argtypes = [vp, C.c_int]
+    L.pdipc_animate.argtypes = [vp, _dp]
+    L.pdipc_get_positions.argtypes = [vp, _dp]
+    L.pdipc_get_velocities.argtypes = [vp, _dp]
+    L.pdipc_set_state.argtypes = [vp, _dp, _dp]
+    L.pdipc_reset.argtypes = [vp]
+    L.pdipc_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    L.pdipc_save.argtypes = [vp, C.c_char_p]
+    L.pdipc_load.argtypes = [vp, C.c_char_p]
+    L.pdipc_destroy.argtypes = [vp]
+    L.pdipc_destroy.restype = None
+    L.pdipc_status_string.argtypes = [C.c_int]
+    L.pdipc_status_string.restype = C.c_char_p
+    L.pdipc_last_error.argtypes = [vp]
+    L.pdipc_last_error.restype = C.c_char_p
+    L.pdipc_abi_version.restype = C.c_int
+    L.pdipc_stage_broadphase.argtypes = [vp, _dp, _dp, _ip, C.c_int64, _i64p, _ip, C.c_int64, _i64p, _ip,
+                                         C.c_int64, _i64p]
+    L.pdipc_stage_morton.argtypes = [vp, C.POINTER(C.c_uint64), _ip, C.c_int]
+    L.pdipc_stage_toi.argtypes = [vp, _dp, _dp, _dp, _dp, _dp]
+    L.pdipc_stage_contact.argtypes = [vp, _dp, _dp, _dp, _i64p]
+    L.pdipc_stage_pd.argtypes = [vp, _dp, _dp, _dp]
+    L.pdipc_stage_sweep_timing.argtypes = [vp, C.c_int, _dp, _dp]
+    L.pdipc_mesh_topology.argtypes = [_dp, C.c_int, _ip, C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, C.c_int, _ip,
+                                      C.c_int, _ip, _ip, _ip]
+    _lib = L
+    return L
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+class Simulator:
+    """One PD-IPC context (one CUDA stream, all its device memory) on one GPU."""
+
+    def __init__(self, scene=None, precision="fp32", params: Params | None = None, initialize=True, **overrides):
+        L = load_library()
+        if params is None:
+            params = params_for_scene(scene, precision, **overrides) if scene is not None else default_params()
+        self.params = params
+        self.h = C.c_void_p()
+        rc = L.pdipc_create(C.byref(params), C.byref(self.h))
+        if rc != PDIPC_OK:
+            self.h = None
+            raise PdipcError(rc, "pdipc_create", "no usable GB300 (sm_103) device" if rc == PDIPC_ERR_CUDA else "")
+        self.n_sim = 0
+        self.n_total = 0
+        if scene is not None:
+            for c in scene.cloths:
+                self.add_cloth(c.X, c.F, c.pins, c.density, c.k_stretch, c.k_bend, c.k_pin, c.patch_dim)
+            for s in scene.statics:
+                self.add_static(s.X, s.F, s.patch_dim)
+            if initialize:
+                self.initialization()
+
+    # -- lifecycle -------------------------------------------------------------------------
+    def _check(self, rc, what):
+        if rc != PDIPC_OK:
+            detail = load_library().pdipc_last_error(self.h).decode(errors="replace") if self.h else ""
+            raise PdipcError(rc, what, detail)
+
+    def add_cloth(self, X, F, pins=(), density=0.1, k_stretch=1e4, k_bend=1e-3, k_pin=1e6, patch_dim=10):
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        F = np.ascontiguousarray(F, dtype=np.int32)
+        P = np.ascontiguousarray(pins, dtype=np.int32)
+        self._check(load_library().pdipc_add_cloth(self.h, _d(X), X.shape[0], _i(F), F.shape[0], density,
+                                                   k_stretch, k_bend, _i(P), P.shape[0], k_pin, patch_dim),
+                    "pdipc_add_cloth")
+        self.n_sim += X.shape[0]
+        self.n_total += X.shape[0]
+
+    def add_static(self, X, F, patch_dim=10):
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        F = np.ascontiguousarray(F, dtype=np.int32)
+        self._check(load_library().pdipc_add_static(self.h, _d(X), X.shape[0], _i(F), F.shape[0], patch_dim),
+                    "pdipc_add_static")
+        self.n_total += X.shape[0]
+
+    def initialization(self):
+        self._check(load_library().pdipc_initialize(self.h), "pdipc_initialize")
+        self._pos = np.empty((self.n_total, 3), np.float64)
+
+    def run(self, nsteps: int = 1):
+        self._check(load_library().pdipc_step(self.h, int(nsteps)), "pdipc_step")
+
+    step = run
+
+    def animate(self, out: np.ndarray | None = None) -> np.ndarray:
+        """run(frame); postRun(): one step and the positions copied to the host."""
+        out = self._pos if out is None else out
+        self._check(load_library().pdipc_animate(self.h, _d(out)), "pdipc_animate")
+        return out
+
+    def positions(self) -> np.ndarray:
+        out = np.empty((self.n_total, 3), np.float64)
+        self._check(load_library().pdipc_get_positions(self.h, _d(out)), "pdipc_get_positions")
+        return out
+
+    def velocities(self) -> np.ndarray:
+        out = np.empty((self.n_sim, 3), np.float64)
+        self._check(load_library().pdipc_get_velocities(self.h, _d(out)), "pdipc_get_velocities")
+        return out
+
+    def set_state(self, X, V=None):
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        Vp = None
+        if V is not None:
+            V = np.ascontiguousarray(V, dtype=np.float64)
+            Vp = _d(V)
+        self._check(load_library().pdipc_set_state(self.h, _d(X), Vp), "pdipc_set_state")
+
+    def reset(self):
+        self._check(load_library().pdipc_reset(self.h), "pdipc_reset")
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(load_library().pdipc_get_stats(self.h, C.byref(s)), "pdipc_get_stats")
+        return s.as_dict()
+
+    def save(self, path: str):
+        self._check(load_library().pdipc_save(self.h, path.encode()), "pdipc_save")
+
+    def load(self, path: str):
+        self._check(load_library().pdipc_load(self.h, path.encode()), "pdipc_load")
+
+    def close(self):
+        if self.h:
+            load_library().pdipc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- stages ----------------------------------------------------------------------------
+    def stage_broadphase(self, x_old, dx, cap=1 << 16):
+        x_old = np.ascontiguousarray(x_old, dtype=np.float64)
+        dx = np.ascontiguousarray(dx, dtype=np.float64)
+        n1, n2, n3 = C.c_int64(), C.c_int64(), C.c_int64()
+        L = load_library()
+        while True:
+            pairs = np.empty((cap, 2), np.int32)
+            pt = np.empty((cap, 4), np.int32)
+            ee = np.empty((cap, 4), np.int32)
+            rc = L.pdipc_stage_broadphase(self.h, _d(x_old), _d(dx), _i(pairs), cap, C.byref(n1), _i(pt), cap,
+                                          C.byref(n2), _i(ee), cap, C.byref(n3))
+            if rc == PDIPC_ERR_OVERFLOW:
+                cap = max(n1.value, n2.value, n3.value)
+                continue
+            self._check(rc, "pdipc_stage_broadphase")
+            return pairs[:n1.value].copy(), pt[:n2.value].copy(), ee[:n3.value].copy()
+
+    def stage_morton(self, npatch):
+        codes = np.empty(max(npatch, 1), np.uint64)
+        order = np.empty(max(npatch, 1), np.int32)
+        self._check(load_library().pdipc_stage_morton(self.h, codes.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                                      _i(order), npatch), "pdipc_stage_morton")
+        return codes[:npatch], order[:npatch]
+
+    def stage_toi(self, x0, x1, npt, nee):
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        x1 = np.ascontiguousarray(x1, dtype=np.float64)
+        tp = np.empty(max(npt, 1), np.float64)
+        te = np.empty(max(nee, 1), np.float64)
+        g = C.c_double()
+        self._check(load_library().pdipc_stage_toi(self.h, _d(x0), _d(x1), _d(tp), _d(te), C.byref(g)),
+                    "pdipc_stage_toi")
+        return tp[:npt], te[:nee], g.value
+
+    def stage_contact(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        diag = np.empty(self.n_total, np.float64)
+        rhs = np.empty((self.n_total, 3), np.float64)
+        na = C.c_int64()
+        self._check(load_library().pdipc_stage_contact(self.h, _d(x), _d(diag), _d(rhs), C.byref(na)),
+                    "pdipc_stage_contact")
+        return diag, rhs, na.value
+
+    def sweep_timing(self, launches=200):
+        """(mean ms per launch, algorithmic bytes per launch) of the J sweep kernel."""
+        ms, b = C.c_double(), C.c_double()
+        self._check(load_library().pdipc_stage_sweep_timing(self.h, int(launches), C.byref(ms), C.byref(b)),
+                    "pdipc_stage_sweep_timing")
+        return ms.value, b.value
+
+    def stage_pd(self, X, V):
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        out = np.empty((self.n_total, 3), np.float64)
+        self._check(load_library().pdipc_stage_pd(self.h, _d(X), _d(V), _d(out)), "pdipc_stage_pd")
+        return out
+
+
+def mesh_topology(X, F, patch_dim):
+    """Edges, grid patches and owner faces of one mesh (host precompute of the library)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    F = np.ascontiguousarray(F, dtype=np.int32)
+    nv, nf = X.shape[0], F.shape[0]
+    cap_e = 3 * nf
+    edges = np.empty((cap_e, 2), np.int32)
+    poff = np.empty(nf + 1, np.int32)
+    pf = np.empty(nf, np.int32)
+    own_p = np.full(nv, -1, np.int32)
+    own_e = np.full(cap_e, -1, np.int32)
+    ne, npch = C.c_int(), C.c_int()
+    rc = load_library().pdipc_mesh_topology(_d(X), nv, _i(F), nf, patch_dim, _i(edges), cap_e, C.byref(ne),
+                                            _i(poff), nf, _i(pf), nf, C.byref(npch), _i(own_p), _i(own_e))
+    if rc != PDIPC_OK:
+        raise PdipcError(rc, "pdipc_mesh_topology")
+    n_e, n_p = ne.value, npch.value
+    patches = [pf[poff[p]:poff[p + 1]].copy() for p in range(n_p)]
+    return edges[:n_e].copy(), patches, own_p, own_e[:n_e].copy()
+
+
+def create_simulator(sim_name: str, scene=None, **kw):
+    """createSimulator(simName, platform) (Simulator/SimulatorFactor.h:13-57): only
+    "pd_ipc_simulator" is provided by this library."""
+    if sim_name != "pd_ipc_simulator":
+        raise ValueError(f"unknown simulator {sim_name!r}; this library provides 'pd_ipc_simulator'")
+    return Simulator(scene, **kw)

@@ -1,0 +1,75 @@
+"""The C-ABI library loads on a host without a GPU, exports every entry point
+declared in include/pdipc.h, and fails cleanly (no fallback) without a GB300."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "pdipc.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(pdipc_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_the_binding_list():
+    import pdipc
+    assert sorted(pdipc.EXPORTS) == declared_symbols()
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", built_lib], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\sT\s(pdipc_\w+)", out))
+    missing = [s for s in declared_symbols() if s not in exported]
+    assert not missing, missing
+    L = C.CDLL(built_lib)
+    for s in declared_symbols():
+        assert hasattr(L, s)
+
+
+def test_default_params_match_reference_constants(built_lib):
+    import pdipc
+    from pdipc.abi import Params, default_params
+    L = pdipc.load_library()
+    p = Params()
+    L.pdipc_default_params(C.byref(p))
+    q = default_params()
+    for name, _ in Params._fields_:
+        if name == "reserved":
+            continue
+        assert getattr(p, name) == getattr(q, name), name
+    assert L.pdipc_abi_version() == 1
+    assert L.pdipc_status_string(3) == b"PDIPC_ERR_OVERFLOW"
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-device path")
+def test_create_without_gpu_fails_loudly(built_lib):
+    import pdipc
+    from pdipc import scenes
+    with pytest.raises(pdipc.PdipcError) as ei:
+        pdipc.Simulator(scenes.cloth_drop(8, 1))
+    assert ei.value.status == pdipc.PDIPC_ERR_CUDA
+
+
+def test_argument_errors_are_reported(built_lib):
+    import pdipc
+    import numpy as np
+    L = pdipc.load_library()
+    assert L.pdipc_create(None, None) == 1
+    assert L.pdipc_step(None, 1) == 1
+    X = np.zeros((3, 3))
+    F = np.array([[0, 1, 5]], np.int32)
+    with pytest.raises(pdipc.PdipcError):
+        pdipc.mesh_topology(X, F, 4)  # face index out of range
