@@ -88,7 +88,8 @@ def test_time_of_impact_matches(prec, rtol, built_lib):
     jg, jo = np.lexsort(eg.T[::-1]), np.lexsort(eo.T[::-1])
     np.testing.assert_allclose(teg[jg], teo[jo], rtol=rtol, atol=0)
     assert go < 1.0
-    assert abs(gg - go) <= rtol * go
+    # the clamped global toi is rounded to the state type (float in mixed mode)
+    assert abs(gg - go) <= max(rtol, 1e-7 if prec == "mixed" else 0.0) * go
     # no impact the oracle finds is missed: every candidate it clamps is clamped here
     assert np.all(tpg[ig][tpo[io] < 1.0] < 1.0)
     assert np.all(teg[jg][teo[jo] < 1.0] < 1.0)
