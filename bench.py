@@ -84,6 +84,12 @@ def max_over_ranks(dist, value: float, device=None) -> float:
     return float(t.item())
 
 
+def aggregate_steps_per_s(world_size: int, steps: int, max_ms: float) -> float:
+    """Whole-job throughput of independent replicas: every rank steps its own
+    copy of the workload, the job ends with the slowest rank."""
+    return world_size * steps / (max_ms * 1e-3)
+
+
 def barrier(dist, device=None):
     if dist is None:
         return
@@ -242,13 +248,39 @@ def run_ours(args):
     barrier(dist, dev)
     e2e_max = max_over_ranks(dist, e2e_wall, dev)
 
+    x_end = sim.positions()
+
+    # plain FP64 GPU form on the same trajectory: speed and the position error of this run
+    fp64 = None
+    if args.precision != "fp64" and args.fp64_steps > 0:
+        k64 = min(args.fp64_steps, args.steps)
+        ref = pdipc.Simulator(sc, "fp64", device=local)
+        ref.step(args.warmup)
+        ref.reset()
+        sim.reset()
+        ms64 = 0.0
+        for _ in range(k64):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ref.step(1)
+            ms64 += ref.stats()["device_ms"]
+        sim.step(k64)
+        err = float(np.abs(sim.positions() - ref.positions()).max())
+        fp64 = {"value": round(k64 / (ms64 * 1e-3), 4), "unit": UNIT, "steps": k64,
+                "ms_per_step": round(ms64 / k64, 3),
+                "outer_iterations_last_step": ref.stats()["last_outer_iters"],
+                "max_position_err_m_vs_this_run": err}
+        ref.close()
+        del ref
+
     # roofline of the dominant kernel (the J sweep), timed alone on this stream
+    sim.set_state(x_end)
     sweep_ms, sweep_bytes = sim.sweep_timing(400)
     peak, peak_kind = measured_peak_hbm()
     achieved = sweep_bytes / (sweep_ms * 1e-3) / 1e9
 
-    value = ws * args.steps / (dev_ms_max * 1e-3)
-    e2e = ws * args.steps / e2e_max
+    value = aggregate_steps_per_s(ws, args.steps, dev_ms_max)
+    e2e = aggregate_steps_per_s(ws, args.steps, e2e_max * 1e3)
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -257,7 +289,8 @@ def run_ours(args):
     res = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": {"fp32": "f32", "fp64": "f64", "mixed": "f32+f64"}[
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp32": "f32", "fp64": "f64", "mixed": "f32 (sweeps, state) + f64 (residual, CCD/contact refinement)"}[
             args.precision], "data": "synthetic (seeded generator; no public dataset for this path)",
         "config": {"workload": workload_desc(sc, args.precision), "steps_timed": f"0..{args.steps - 1}",
                    "parallelism": "replicas only" if ws > 1 else "single GPU",
@@ -281,8 +314,10 @@ def run_ours(args):
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
         "clocks": clk.summary(),
     }
+    if fp64 is not None:
+        res["fp64_gpu"] = fp64
     if not args.no_cpu_baseline:
-        res["cpu_baseline"] = cpu_reference_sample(sc, args.precision, args.cpu_outer_sample, mean_outer,
+        res["cpu_baseline"] = cpu_reference_sample(sc, "fp32", args.cpu_outer_sample, args.ref_outer_per_step,
                                                    os.cpu_count() or 1)
     print(json.dumps(res), flush=True)
     if dist is not None:
@@ -297,7 +332,7 @@ def run_reference(args):
     sc = workload(args.config)
     threads = os.cpu_count() or 1
     sample_outer = args.cpu_outer_sample
-    orc = Oracle(sc, args.precision, FORM_R2, threads=threads, fixed_outer=sample_outer)
+    orc = Oracle(sc, "fp32", FORM_R2, threads=threads, fixed_outer=sample_outer)
     for _ in range(min(args.warmup, 1)):
         orc.step(1)
     orc.set_state(np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics]),
@@ -311,12 +346,14 @@ def run_reference(args):
     per_outer = t_used / (n * sample_outer)
     outer_per_step = args.ref_outer_per_step
     value = 1.0 / (per_outer * outer_per_step)
+    resid = orc.stats()["last_residual"]
     sample = (f"{n} steps from step 0, each with {sample_outer} outer iterations, scaled to {outer_per_step} "
-              f"outer iterations per step (the reference stopping rule never fires at this size in FP32); "
-              f"reference R2-operator form restated on the CPU, {threads} threads")
+              f"outer iterations per step: the reference's stopping rule (|dx|^2 < 1e-5) never fires at this size "
+              f"in its FP32 arithmetic (residual after the sampled iterations {resid:.2e}); reference R2-operator "
+              f"form and FP32 arithmetic restated on the CPU, {threads} threads")
     res = {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": ws,
            "steps": n, "warmup": args.warmup, "ms_per_step": round(1e3 / value, 3), "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else args.precision,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic", "config": {"workload": workload_desc(sc, args.precision)},
            "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": threads, "kind": "port",
                             "sample": sample},
@@ -330,7 +367,8 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp32", "fp64", "mixed"])
+    ap.add_argument("--fp64-steps", type=int, default=100)
     ap.add_argument("--config", default="c1", choices=["c1", "c0"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-outer-sample", type=int, default=2)

@@ -79,7 +79,9 @@ typedef struct {
     int device;              /* CUDA device ordinal */
     int rebuild_bvh;         /* 0: build the patch BVH once at initialize and refit per step
                                 (reference behaviour, cpp:1296-1320); 1: rebuild every step */
-    int reserved[7];
+    int persistent;          /* 1: FP32/mixed PD solve of an outer iteration as one cooperative launch
+                                when the mesh allows it (matrix slice per CTA); 0: one launch per sweep */
+    int reserved[6];
 } pdipc_params;
 
 /* Per-context statistics of the most recent pdipc_step call. */
@@ -102,6 +104,9 @@ typedef struct {
     int64_t kernel_launches;     /* kernels launched by the last pdipc_step call (graph nodes included) */
     double device_ms;            /* device time of the last pdipc_step call: CUDA events recorded on the
                                     context's stream around every step, summed */
+    int32_t pd_path;             /* 0: one launch per sweep; 1: persistent, matrix from L2;
+                                    2: persistent, matrix values in shared memory */
+    int32_t pd_ctas;             /* CTAs of the persistent solve (0 if not used) */
 } pdipc_stats;
 
 /* Fill *p with the reference defaults listed beside each field. */

@@ -408,7 +408,11 @@ __device__ __forceinline__ void block_min_to(TC v, TC* dst) {
 
 // getImpactOfTimeKernel (cu:2610-2704): skip pairs sharing a vertex, swept-AABB
 // filter with slack, additive CCD; global minimum by integer atomicMin.
-template <typename T, typename TC, bool kPT>
+// kRel (mixed precision): coordinates relative to the pair's first vertex in
+// FP32 (a difference of nearby positions loses nothing), additive CCD in FP32,
+// and every candidate that would clamp the step (toi < 1) re-evaluated in FP64
+// from the same relative coordinates, so the minimum is an FP64 time of impact.
+template <typename T, typename TC, bool kPT, bool kRel>
 __global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restrict__ cand,
                                                 const V4<T>* __restrict__ X0, const V4<T>* __restrict__ X1,
                                                 TC slack, TC eta, int max_iter, TC* __restrict__ per,
@@ -421,17 +425,46 @@ __global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restric
         const bool shared = kPT ? (c.x == c.y || c.x == c.z || c.x == c.w)
                                 : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w);
         if (!shared) {
-            TC x[4][3], dx[4][3];
-            gather4<T, TC>(X0, ids, x);
-            gather4<T, TC>(X1, ids, dx);
+            if (kRel) {
+                T x[4][3], dx[4][3];
+                const V4<T> o = ld4(X0, ids[0]);
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
+                for (int j = 0; j < 4; ++j) {
+                    const V4<T> a = ld4(X0, ids[j]), b = ld4(X1, ids[j]);
+                    x[j][0] = a.x - o.x;
+                    x[j][1] = a.y - o.y;
+                    x[j][2] = a.z - o.z;
+                    dx[j][0] = b.x - a.x;
+                    dx[j][1] = b.y - a.y;
+                    dx[j][2] = b.z - a.z;
+                }
+                const bool hit = kPT ? geo::pt_ccd_broad<T>(x, dx, (T)slack) : geo::ee_ccd_broad<T>(x, dx, (T)slack);
+                if (hit) {
+                    TC xd[4][3], dd[4][3];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) dx[j][k] -= x[j][k];
-            if (kPT) {
-                if (geo::pt_ccd_broad<TC>(x, dx, slack)) toi = geo::ccd_pt<TC>(x, dx, eta, max_iter);
+                    for (int j = 0; j < 4; ++j)
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) {
+                            xd[j][k] = (TC)x[j][k];
+                            dd[j][k] = (TC)dx[j][k];
+                        }
+                    const T tf = kPT ? geo::ccd_pt<T>(x, dx, (T)eta, max_iter) : geo::ccd_ee<T>(x, dx, (T)eta, max_iter);
+                    if (tf < T(1))
+                        toi = kPT ? geo::ccd_pt<TC>(xd, dd, eta, max_iter) : geo::ccd_ee<TC>(xd, dd, eta, max_iter);
+                }
             } else {
-                if (geo::ee_ccd_broad<TC>(x, dx, slack)) toi = geo::ccd_ee<TC>(x, dx, eta, max_iter);
+                TC x[4][3], dx[4][3];
+                gather4<T, TC>(X0, ids, x);
+                gather4<T, TC>(X1, ids, dx);
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) dx[j][k] -= x[j][k];
+                if (kPT) {
+                    if (geo::pt_ccd_broad<TC>(x, dx, slack)) toi = geo::ccd_pt<TC>(x, dx, eta, max_iter);
+                } else {
+                    if (geo::ee_ccd_broad<TC>(x, dx, slack)) toi = geo::ccd_ee<TC>(x, dx, eta, max_iter);
+                }
             }
         }
         if (per) per[t] = toi;
@@ -457,7 +490,10 @@ struct ContactConsts {
 // w = kappa b(d^2) + min(m_p, m_q)/dt^2 to the diagonal of its 4 vertices and
 // w * target to their right-hand side; targets push the pair apart to dhat
 // along the closest-point direction, split by the mass ratio.
-template <typename T, typename TC, bool kPT>
+// kRel (mixed precision): relative coordinates, FP32 filter, FP64 distance and
+// weight for pairs within 1.1 dhat, and the right-hand side accumulated as
+// w * (target - x) so the later residual needs no cancellation.
+template <typename T, typename TC, bool kPT, bool kRel>
 __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __restrict__ cand,
                                                     const V4<T>* __restrict__ X, const TC* __restrict__ mass,
                                                     ContactConsts<TC> cc, T* __restrict__ diag,
@@ -469,29 +505,68 @@ __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __res
         if (kPT ? (c.x == c.y || c.x == c.z || c.x == c.w) : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w))
             continue;
         TC p[4][3];
-        gather4<T, TC>(X, ids, p);
-        TC d[3], dist2, mp, mq;
-        bool far = false;
-        if (kPT) {
+        if (kRel) {
+            T q[4][3];
+            const V4<T> o = ld4(X, ids[0]);
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {  // point_triangle_cd_broadphase (cu:2328-2345)
-                const TC tmin = geo::mn3(p[1][k], p[2][k], p[3][k]), tmax = geo::mx3(p[1][k], p[2][k], p[3][k]);
-                if ((p[0][k] - tmax) > cc.dh || (tmin - p[0][k]) > cc.dh) far = true;
+            for (int j = 0; j < 4; ++j) {
+                const V4<T> a = ld4(X, ids[j]);
+                q[j][0] = a.x - o.x;
+                q[j][1] = a.y - o.y;
+                q[j][2] = a.z - o.z;
+            }
+            const T dhf = (T)cc.dh;
+            bool far = false;
+            if (kPT) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const T tmin = geo::mn3(q[1][k], q[2][k], q[3][k]), tmax = geo::mx3(q[1][k], q[2][k], q[3][k]);
+                    if ((q[0][k] - tmax) > dhf || (tmin - q[0][k]) > dhf) far = true;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const T mina = dmin(q[0][k], q[1][k]), maxa = dmax(q[0][k], q[1][k]);
+                    const T minb = dmin(q[2][k], q[3][k]), maxb = dmax(q[2][k], q[3][k]);
+                    if ((mina - maxb) > dhf || (minb - maxa) > dhf) far = true;
+                }
             }
             if (far) continue;
+            T df[3], a_, b_, c_;
+            const T d2f = kPT ? geo::vtx_tri<T>(q[0], q[1], q[2], q[3], &a_, &b_, &c_, df)
+                              : geo::edge_edge_sq<T>(q[0], q[1], q[2], q[3], &a_, &b_, df);
+            if (!(d2f < (T)(1.21 * cc.dh2))) continue;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) p[j][k] = (TC)q[j][k];
+        } else {
+            gather4<T, TC>(X, ids, p);
+            bool far = false;
+            if (kPT) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {  // point_triangle_cd_broadphase (cu:2328-2345)
+                    const TC tmin = geo::mn3(p[1][k], p[2][k], p[3][k]), tmax = geo::mx3(p[1][k], p[2][k], p[3][k]);
+                    if ((p[0][k] - tmax) > cc.dh || (tmin - p[0][k]) > cc.dh) far = true;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {  // edge_edge_cd_broadphase (cu:2405-2424)
+                    const TC mina = dmin(p[0][k], p[1][k]), maxa = dmax(p[0][k], p[1][k]);
+                    const TC minb = dmin(p[2][k], p[3][k]), maxb = dmax(p[2][k], p[3][k]);
+                    if ((mina - maxb) > cc.dh || (minb - maxa) > cc.dh) far = true;
+                }
+            }
+            if (far) continue;
+        }
+        TC d[3], dist2, mp, mq;
+        if (kPT) {
             TC a, b, cq;
             dist2 = geo::vtx_tri(p[0], p[1], p[2], p[3], &a, &b, &cq, d);
             if (dist2 >= cc.dh2) continue;
             mp = mass[c.x];
             mq = a * mass[c.y] + b * mass[c.z] + cq * mass[c.w];
         } else {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {  // edge_edge_cd_broadphase (cu:2405-2424)
-                const TC mina = dmin(p[0][k], p[1][k]), maxa = dmax(p[0][k], p[1][k]);
-                const TC minb = dmin(p[2][k], p[3][k]), maxb = dmax(p[2][k], p[3][k]);
-                if ((mina - maxb) > cc.dh || (minb - maxa) > cc.dh) far = true;
-            }
-            if (far) continue;
             TC r, s;
             dist2 = geo::edge_edge_sq(p[0], p[1], p[2], p[3], &r, &s, d);
             if (dist2 >= cc.dh2) continue;
@@ -500,11 +575,8 @@ __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __res
         }
         ++my;
         TC dist = dsqrt(dist2);
-        TC bar = TC(0);
-        if (dist2 < cc.dh2) {
-            const TC t2 = dist2 - cc.dh2;
-            bar = -cc.kappa * t2 * t2 * dlog(dist2 / cc.dh2) / (cc.dh2 * cc.dh2);
-        }
+        const TC t2 = dist2 - cc.dh2;
+        const TC bar = -cc.kappa * t2 * t2 * dlog(dist2 / cc.dh2) / (cc.dh2 * cc.dh2);
         const TC w = bar + dmin(mp, mq) / (cc.dt * cc.dt);
         const TC rp = mq / (mp + mq), rq = mp / (mp + mq);
         const TC len = dsqrt(geo::dot3(d, d));
@@ -513,13 +585,21 @@ __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __res
         const TC dp = dist * rp, dq = dist * rq;
         for (int j = 0; j < 4; ++j) atomicAdd(diag + ids[j], (T)w);
         for (int k = 0; k < 3; ++k) {
-            const TC t0 = w * (p[0][k] + dp * d[k]);
-            const TC t1 = kPT ? w * (p[1][k] - dq * d[k]) : w * (p[1][k] + dp * d[k]);
-            const TC t2 = w * (p[2][k] - dq * d[k]);
-            const TC t3 = w * (p[3][k] - dq * d[k]);
+            TC t0, t1, t2_, t3;
+            if (kRel) {  // w (target - x)
+                t0 = w * (dp * d[k]);
+                t1 = kPT ? -w * (dq * d[k]) : w * (dp * d[k]);
+                t2_ = -w * (dq * d[k]);
+                t3 = -w * (dq * d[k]);
+            } else {
+                t0 = w * (p[0][k] + dp * d[k]);
+                t1 = kPT ? w * (p[1][k] - dq * d[k]) : w * (p[1][k] + dp * d[k]);
+                t2_ = w * (p[2][k] - dq * d[k]);
+                t3 = w * (p[3][k] - dq * d[k]);
+            }
             atomicAdd(&rhs[ids[0]].x + k, (T)t0);
             atomicAdd(&rhs[ids[1]].x + k, (T)t1);
-            atomicAdd(&rhs[ids[2]].x + k, (T)t2);
+            atomicAdd(&rhs[ids[2]].x + k, (T)t2_);
             atomicAdd(&rhs[ids[3]].x + k, (T)t3);
         }
     }
@@ -580,12 +660,14 @@ void launch_expand(const Dev<T, TC>& d, const int64_t* opt, const int64_t* oee, 
 template <typename T, typename TC>
 void launch_toi(const Dev<T, TC>& d, const V4<T>* X0, const V4<T>* X1, const SolverConsts& c, TC* per_pt,
                 TC* per_ee, cudaStream_t s) {
+    constexpr bool kRel = sizeof(T) == 4 && sizeof(TC) == 8;
     if (d.nPT > 0)
-        k_toi<T, TC, true><<<grid_cap(d.nPT), kBlock, 0, s>>>(d.nPT, d.PT, X0, X1, (TC)c.ccd_slack, (TC)c.ccd_eta,
-                                                               c.ccd_max_iter, per_pt, d.ToiMin);
+        k_toi<T, TC, true, kRel><<<grid_cap(d.nPT), kBlock, 0, s>>>(d.nPT, d.PT, X0, X1, (TC)c.ccd_slack,
+                                                                     (TC)c.ccd_eta, c.ccd_max_iter, per_pt, d.ToiMin);
     if (d.nEE > 0)
-        k_toi<T, TC, false><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X0, X1, (TC)c.ccd_slack,
-                                                                (TC)c.ccd_eta, c.ccd_max_iter, per_ee, d.ToiMin);
+        k_toi<T, TC, false, kRel><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X0, X1, (TC)c.ccd_slack,
+                                                                      (TC)c.ccd_eta, c.ccd_max_iter, per_ee,
+                                                                      d.ToiMin);
 }
 template <typename T, typename TC>
 void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s) {
@@ -602,12 +684,13 @@ void launch_contact(const Dev<T, TC>& d, const V4<T>* X, const SolverConsts& c, 
     cc.dh2 = (TC)(dh * dh);
     cc.kappa = (TC)(T)c.kappa;
     cc.dt = (TC)(T)c.dt;
+    constexpr bool kRel = sizeof(T) == 4 && sizeof(TC) == 8;
     if (d.nPT > 0)
-        k_contact<T, TC, true><<<grid_cap(d.nPT), kBlock, 0, s>>>(d.nPT, d.PT, X, d.CollMass, cc, d.CollDiag,
-                                                                   d.CollRhs, d.ActiveCount);
+        k_contact<T, TC, true, kRel><<<grid_cap(d.nPT), kBlock, 0, s>>>(d.nPT, d.PT, X, d.CollMass, cc,
+                                                                         d.CollDiag, d.CollRhs, d.ActiveCount);
     if (d.nEE > 0)
-        k_contact<T, TC, false><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X, d.CollMass, cc, d.CollDiag,
-                                                                    d.CollRhs, d.ActiveCount);
+        k_contact<T, TC, false, kRel><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X, d.CollMass, cc,
+                                                                          d.CollDiag, d.CollRhs, d.ActiveCount);
 }
 
 #define PDIPC_INST_COLL(T, TC)                                                                                \

@@ -120,12 +120,26 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+// Compensated FP32 sum (Knuth's TwoSum): s + c carries the exact sum of the
+// added terms to about twice FP32 precision, at six FP32 adds per term.
+struct Sum2 {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float t = s + x;
+        const float bp = t - s;
+        c += (s - (t - bp)) + (x - bp);
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return s + c; }
+};
+
 // Device-side error flags (bit mask), read back by the host after a step.
 enum ErrFlag : unsigned int {
     kErrNonFinite = 1u,
     kErrTraversalStack = 2u,
     kErrPairOverflow = 4u,
     kErrCandidateOverflow = 8u,
+    kErrBarrier = 16u,  // a grid barrier of the persistent solve timed out
 };
 
 }  // namespace pdipc

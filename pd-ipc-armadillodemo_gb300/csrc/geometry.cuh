@@ -172,6 +172,9 @@ __device__ R ccd_pt(R (*x)[3], R (*dx)[3], R eta, int max_iter) {
     R toc = R(0);
     for (int it = 0; it < max_iter; ++it) {
         const R lb = R(0.9) * d2 / (dc * maxd);
+        // at it == 0 toc is 0, so the gap test below cannot fire and a first
+        // bound above 1 returns 1 whatever the distance after the advance
+        if (it == 0 && lb > R(1)) return R(1);
         for (int j = 0; j < 4; ++j)
             for (int k = 0; k < 3; ++k) x[j][k] += lb * dx[j][k];
         d2 = vtx_tri(x[0], x[1], x[2], x[3], &a, &b, &c, dd);
@@ -220,6 +223,7 @@ __device__ R ccd_ee(R (*x)[3], R (*dx)[3], R eta, int max_iter) {
     R toc = R(0);
     for (int it = 0; it < max_iter; ++it) {
         const R lb = R(0.9) * f / (dc * maxd);
+        if (it == 0 && lb > R(1)) return R(1);  // as in ccd_pt
         for (int j = 0; j < 4; ++j)
             for (int k = 0; k < 3; ++k) x[j][k] += lb * dx[j][k];
         d2 = edge_edge_sq(x[0], x[1], x[2], x[3], &r, &s, dd);

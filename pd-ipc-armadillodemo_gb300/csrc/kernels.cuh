@@ -29,16 +29,19 @@ struct Dev {
     V4<T>* B = nullptr;      // odd Chebyshev iterates [nsim]
     V4<T>* Aq = nullptr;     // rescaled curvature vector per vertex [nsim]
     V4<T>* Rhs = nullptr;    // right-hand side of the current local-global iteration [nsim]
-    V4<T>* Rhs0 = nullptr;   // inertial right-hand side (m/dt^2) y [nsim]
+    V4<T>* Rhs0 = nullptr;   // inertial right-hand side (m/dt^2) y [nsim]; the predicted y itself in
+                             // the correction (mixed) form
+    V4<T>* C = nullptr;      // even correction iterates of the correction form [nsim]
     V4<T>* Grav = nullptr;   // (0, g m, 0) [nsim]
     V4<T>* PinRhs = nullptr; // k_pin * X_rest for pinned vertices, else 0 [nsim]
     T* InvMass = nullptr;    // [nsim]
     int* PinFlag = nullptr;  // -1 free, else pin slot [nsim]
+    T* PinK = nullptr;       // stiffness of each pin slot
     T* Dinert = nullptr;     // m/dt^2 (0 for pinned vertices) [nsim]
     T* Delastic = nullptr;   // [nsim]
     T* InvD = nullptr;       // 1 / (elastic + inertial + collision) [nsim]
     T* CollDiag = nullptr;   // [ntot]
-    V4<T>* CollRhs = nullptr;// [ntot]
+    V4<T>* CollRhs = nullptr;// [ntot] sum w*target; in the correction form sum w*(target - x_contact)
     TC* CollMass = nullptr;  // [ntot]
 
     // local-step stencils (CSR over simulated vertices): [self, neighbours ascending]
@@ -118,6 +121,16 @@ void launch_local_rhs_sweep(const Dev<T, TC>& d, T relax, cudaStream_t s);
 template <typename T, typename TC>
 void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T>* out, T relax, T omega,
                   cudaStream_t s);
+// Correction (mixed-precision) form of one local-global iteration's pieces:
+// residual r0 = b - A x from relative coordinates (FP64 accumulation) into Rhs
+// and the first sweep from delta = 0 into Y.
+template <typename T, typename TC>
+void launch_local_residual(const Dev<T, TC>& d, T relax, cudaStream_t s);
+// sweep on the correction: mode 0 plain, 1 Chebyshev, 2 Chebyshev with a zero
+// previous iterate, 3 Chebyshev whose result is added to the positions P.
+template <typename T, typename TC>
+void launch_sweep_delta(const Dev<T, TC>& d, int mode, const V4<T>* src, const V4<T>* prev, V4<T>* out, T relax,
+                        T omega, cudaStream_t s);
 template <typename T, typename TC>
 void launch_direction(const Dev<T, TC>& d, cudaStream_t s);
 template <typename T, typename TC>

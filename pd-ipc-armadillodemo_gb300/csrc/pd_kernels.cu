@@ -14,6 +14,8 @@
 // Layout: one vertex per aligned 4-vector; the local step is a gather (no
 // atomics) and the system matrix is streamed from SELL-32 slices so a warp's
 // column/value loads are contiguous 128-byte lines.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace pdipc {
@@ -24,7 +26,7 @@ constexpr int kBlock = 256;
 
 inline int blocks_for(int n, int b = kBlock) { return (n + b - 1) / b; }
 
-template <typename T>
+template <typename T, bool kDelta>
 __global__ void k_predict(int nsim, int ntot, T dt, V4<T>* __restrict__ P, V4<T>* __restrict__ Pold,
                           V4<T>* __restrict__ X0, V4<T>* __restrict__ Vel, V4<T>* __restrict__ Rhs0,
                           T* __restrict__ Dinert, const V4<T>* __restrict__ Grav, const T* __restrict__ InvMass,
@@ -50,7 +52,8 @@ __global__ void k_predict(int nsim, int ntot, T dt, V4<T>* __restrict__ P, V4<T>
     T y2 = (v.z + m * g.z) * dt + x.z;
     const T mm = T(1) / (dt * m);
     Dinert[i] = T(1) / (im * dt * dt);
-    Rhs0[i] = V4<T>{mm * y0, mm * y1, mm * y2, T(0)};
+    if (kDelta) Rhs0[i] = V4<T>{y0, y1, y2, T(0)};
+    else Rhs0[i] = V4<T>{mm * y0, mm * y1, mm * y2, T(0)};
     P[i] = V4<T>{y0, y1, y2, T(0)};
 }
 
@@ -197,6 +200,171 @@ __global__ void __launch_bounds__(kBlock) k_sweep(int nsim, T relax, T omega, co
     out[i] = V4<T>{y0, y1, y2, T(0)};
 }
 
+// Correction form, one vertex per thread.  With x the current positions,
+//   r0 = b - A x
+//      = Dinert (y - x) + k_pin (X_rest - x) + sum_c w_c (target_c - x_c) + Dcoll (x_c - x)
+//        + springs + bending + sum_j N_ij (x_j - x)
+// where x_c are the positions the contact projections were taken at (Pold).
+// The elastic rows of A sum to zero (springs and the LBO stencils are
+// translation invariant), which is used exactly: the rounded FP32 entries would
+// otherwise add a spurious pull toward the origin.  Every large term is formed
+// from a difference of nearby positions, so FP32 inputs lose nothing to
+// cancellation; the sum is accumulated with compensated (TwoSum) FP32 sums.  Then the first sweep from
+// delta = 0: Y = w r0 / D.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_local_residual(
+    int nsim, T relax, const V4<T>* __restrict__ P, const V4<T>* __restrict__ Pold, const V4<T>* __restrict__ Xrest,
+    const V4<T>* __restrict__ Ypred, const T* __restrict__ Dinert, const T* __restrict__ CollDiag,
+    const V4<T>* __restrict__ CollRes, const int* __restrict__ PinFlag, const T* __restrict__ PinK,
+    const int* __restrict__ lPtr, const int* __restrict__ lNbr, const T* __restrict__ lRest,
+    const T* __restrict__ lBend, const T* __restrict__ lBendT, const T* __restrict__ Strain,
+    const V4<T>* __restrict__ Aq, const T* __restrict__ InvD,
+    const int* __restrict__ sOff, const int* __restrict__ sLen, const int* __restrict__ sCol,
+    const T* __restrict__ sVal, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim) return;
+    const V4<T> x = ld4(P, i);
+    Sum2 r0, r1, r2;
+    {   // inertia
+        const V4<T> y = ld4(Ypred, i);
+        const T di = __ldg(Dinert + i);
+        r0.add(di * (y.x - x.x));
+        r1.add(di * (y.y - x.y));
+        r2.add(di * (y.z - x.z));
+    }
+    const int pf = __ldg(PinFlag + i);
+    if (pf >= 0) {
+        const V4<T> xr = ld4(Xrest, i);
+        const T k = __ldg(PinK + pf);
+        r0.add(k * (xr.x - x.x));
+        r1.add(k * (xr.y - x.y));
+        r2.add(k * (xr.z - x.z));
+    }
+    {   // contact projections taken at Pold
+        const V4<T> c = ld4(CollRes, i);
+        const V4<T> xo = ld4(Pold, i);
+        const T dc = __ldg(CollDiag + i);
+        r0.add(c.x);
+        r0.add(dc * (xo.x - x.x));
+        r1.add(c.y);
+        r1.add(dc * (xo.y - x.y));
+        r2.add(c.z);
+        r2.add(dc * (xo.z - x.z));
+    }
+    const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
+    const T strain = __ldg(Strain + i);
+    for (int s = b + 1; s < e; ++s) {  // mass-spring projections
+        const V4<T> xj = ld4(P, __ldg(lNbr + s));
+        const T d0 = x.x - xj.x, d1 = x.y - xj.y, d2 = x.z - xj.z;
+        const T cl = dsqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        const T rc = strain * (__ldg(lRest + s) / cl);
+        r0.add(rc * d0);
+        r1.add(rc * d1);
+        r2.add(rc * d2);
+    }
+    {   // bending: own stencil and the neighbours' stencils
+        const V4<T> ai = ld4(Aq, i);
+        const T b0 = __ldg(lBend + b);
+        r0.add(b0 * ai.x);
+        r1.add(b0 * ai.y);
+        r2.add(b0 * ai.z);
+        for (int s = b + 1; s < e; ++s) {
+            const V4<T> ak = ld4(Aq, __ldg(lNbr + s));
+            const T bt = __ldg(lBendT + s);
+            r0.add(bt * ak.x);
+            r1.add(bt * ak.y);
+            r2.add(bt * ak.z);
+        }
+    }
+    {   // sum_j N_ij (x_j - x_i)
+        const int sl = i >> 5, lane = i & 31;
+        const int base = __ldg(sOff + sl) + lane;
+        const int len = __ldg(sLen + sl);
+#pragma unroll 4
+        for (int k = 0; k < len; ++k) {
+            const int j = __ldg(sCol + base + 32 * k);
+            const T v = __ldg(sVal + base + 32 * k);
+            const V4<T> xj = ld4(P, j);
+            r0.add(v * (xj.x - x.x));
+            r1.add(v * (xj.y - x.y));
+            r2.add(v * (xj.z - x.z));
+        }
+    }
+    const T f0 = r0.value(), f1 = r1.value(), f2 = r2.value();
+    Rhs[i] = V4<T>{f0, f1, f2, T(0)};
+    const T wid = relax * __ldg(InvD + i);
+    Y[i] = V4<T>{wid * f0, wid * f1, wid * f2, T(0)};
+}
+
+// Sweep on the correction delta (rhs = residual r0).  kMode bits: 1 Chebyshev
+// step omega (S(src) - prev) + prev; 2 the previous iterate is zero (so the
+// step is omega S(src)); 4 the result is added to the positions (out = P).
+template <typename T, int kMode>
+__global__ void __launch_bounds__(kBlock) k_sweep_delta(int nsim, T relax, T omega, const V4<T>* __restrict__ src,
+                                                        const V4<T>* __restrict__ prev, V4<T>* __restrict__ out,
+                                                        const V4<T>* __restrict__ Rhs, const T* __restrict__ InvD,
+                                                        const int* __restrict__ sOff, const int* __restrict__ sLen,
+                                                        const int* __restrict__ sCol, const T* __restrict__ sVal) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim) return;
+    T s0, s1, s2;
+    sell_row(i, sOff, sLen, sCol, sVal, src, s0, s1, s2);
+    const V4<T> x = ld4(src, i);
+    const V4<T> r = ld4(Rhs, i);
+    const T id = __ldg(InvD + i);
+    const T om = T(1) - relax;
+    T y0 = om * x.x + relax * ((s0 + r.x) * id);
+    T y1 = om * x.y + relax * ((s1 + r.y) * id);
+    T y2 = om * x.z + relax * ((s2 + r.z) * id);
+    if (kMode & 1) {
+        if (kMode & 2) {
+            y0 *= omega;
+            y1 *= omega;
+            y2 *= omega;
+        } else {
+            const V4<T> p = ld4(prev, i);
+            y0 = omega * (y0 - p.x) + p.x;
+            y1 = omega * (y1 - p.y) + p.y;
+            y2 = omega * (y2 - p.z) + p.z;
+        }
+    }
+    if (kMode & 4) {
+        const V4<T> q = out[i];
+        out[i] = V4<T>{q.x + y0, q.y + y1, q.z + y2, T(0)};
+    } else {
+        out[i] = V4<T>{y0, y1, y2, T(0)};
+    }
+}
+
+// Relative form of the curvature vector for the correction form:
+// aq = sum_{k>0} lbo_k (x_k - x_i), using that the LBO weights of a stencil sum
+// to zero.
+template <typename T>
+__global__ void k_local_aq_rel(int nsim, const V4<T>* __restrict__ P, const int* __restrict__ lPtr,
+                               const int* __restrict__ lNbr, const T* __restrict__ lLbo,
+                               const T* __restrict__ CurvNorm, V4<T>* __restrict__ Aq) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim) return;
+    const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
+    const V4<T> x = ld4(P, i);
+    T a0 = T(0), a1 = T(0), a2 = T(0);
+    for (int s = b + 1; s < e; ++s) {
+        const V4<T> xj = ld4(P, __ldg(lNbr + s));
+        const T l = __ldg(lLbo + s);
+        a0 += l * (xj.x - x.x);
+        a1 += l * (xj.y - x.y);
+        a2 += l * (xj.z - x.z);
+    }
+    const T nrm = dsqrt(a0 * a0 + a1 * a1 + a2 * a2);
+    if (nrm >= T(1e-10)) {
+        const T c = __ldg(CurvNorm + i) / nrm;
+        a0 *= c;
+        a1 *= c;
+        a2 *= c;
+    }
+    Aq[i] = V4<T>{a0, a1, a2, T(0)};
+}
+
 template <typename T>
 __global__ void k_direction(int nsim, const V4<T>* __restrict__ P, const V4<T>* __restrict__ Pold,
                             V4<T>* __restrict__ Dir, double* __restrict__ part) {
@@ -249,10 +417,15 @@ __global__ void k_velocity(int nsim, T invt, const V4<T>* __restrict__ P, const 
 int direction_blocks(int nsim) { return std::min(1024, std::max(1, blocks_for(nsim))); }
 
 template <typename T, typename TC>
+constexpr bool correction_form() {
+    return sizeof(T) == 4 && sizeof(TC) == 8;
+}
+
+template <typename T, typename TC>
 void launch_predict(const Dev<T, TC>& d, T dt, cudaStream_t s) {
-    k_predict<T><<<blocks_for(d.ntot), kBlock, 0, s>>>(d.nsim, d.ntot, dt, d.P, d.Pold, d.X0, d.Vel, d.Rhs0,
-                                                         d.Dinert, d.Grav, d.InvMass, d.PinFlag, d.CollDiag,
-                                                         d.CollRhs);
+    k_predict<T, correction_form<T, TC>()><<<blocks_for(d.ntot), kBlock, 0, s>>>(
+        d.nsim, d.ntot, dt, d.P, d.Pold, d.X0, d.Vel, d.Rhs0, d.Dinert, d.Grav, d.InvMass, d.PinFlag, d.CollDiag,
+        d.CollRhs);
 }
 template <typename T, typename TC>
 void launch_diag(const Dev<T, TC>& d, cudaStream_t s) {
@@ -260,7 +433,38 @@ void launch_diag(const Dev<T, TC>& d, cudaStream_t s) {
 }
 template <typename T, typename TC>
 void launch_local_aq(const Dev<T, TC>& d, cudaStream_t s) {
-    k_local_aq<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.lNbr, d.lLbo, d.CurvNorm, d.Aq);
+    if (correction_form<T, TC>())
+        k_local_aq_rel<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.lNbr, d.lLbo, d.CurvNorm,
+                                                                 d.Aq);
+    else
+        k_local_aq<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.lNbr, d.lLbo, d.CurvNorm, d.Aq);
+}
+template <typename T, typename TC>
+void launch_local_residual(const Dev<T, TC>& d, T relax, cudaStream_t s) {
+    k_local_residual<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(
+        d.nsim, relax, d.P, d.Pold, d.Xrest, d.Rhs0, d.Dinert, d.CollDiag, d.CollRhs, d.PinFlag, d.PinK, d.lPtr,
+        d.lNbr, d.lRest, d.lBend, d.lBendT, d.Strain, d.Aq, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal, d.Rhs, d.Y);
+}
+template <typename T, typename TC>
+void launch_sweep_delta(const Dev<T, TC>& d, int mode, const V4<T>* src, const V4<T>* prev, V4<T>* out, T relax,
+                        T omega, cudaStream_t s) {
+    const int nb = blocks_for(d.nsim);
+#define PDIPC_SWEEP_DELTA(M)                                                                                   \
+    case M:                                                                                                    \
+        k_sweep_delta<T, M><<<nb, kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.Rhs, d.InvD, d.sOff, \
+                                                  d.sLen, d.sCol, d.sVal);                                     \
+        break;
+    switch (mode) {
+        PDIPC_SWEEP_DELTA(0)
+        PDIPC_SWEEP_DELTA(1)
+        PDIPC_SWEEP_DELTA(3)
+        PDIPC_SWEEP_DELTA(4)
+        PDIPC_SWEEP_DELTA(5)
+        PDIPC_SWEEP_DELTA(7)
+        default:
+            break;
+    }
+#undef PDIPC_SWEEP_DELTA
 }
 template <typename T, typename TC>
 void launch_local_rhs_sweep(const Dev<T, TC>& d, T relax, cudaStream_t s) {
@@ -302,6 +506,9 @@ void launch_velocity(const Dev<T, TC>& d, T invt, cudaStream_t s) {
     template void launch_diag<T, TC>(const Dev<T, TC>&, cudaStream_t);                                       \
     template void launch_local_aq<T, TC>(const Dev<T, TC>&, cudaStream_t);                                   \
     template void launch_local_rhs_sweep<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                         \
+    template void launch_local_residual<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                          \
+    template void launch_sweep_delta<T, TC>(const Dev<T, TC>&, int, const V4<T>*, const V4<T>*, V4<T>*, T, T, \
+                                            cudaStream_t);                                                   \
     template void launch_sweep<T, TC>(const Dev<T, TC>&, const V4<T>*, const V4<T>*, V4<T>*, T, T,           \
                                       cudaStream_t);                                                         \
     template void launch_direction<T, TC>(const Dev<T, TC>&, cudaStream_t);                                  \

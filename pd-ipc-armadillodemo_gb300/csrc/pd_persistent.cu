@@ -1,0 +1,417 @@
+// pd_persistent.cu — one cooperative launch per outer iteration for the whole
+// projective-dynamics solve (lg x [local step + 15 Chebyshev-accelerated R2
+// steps as 30 weighted-Jacobi sweeps]).
+//
+// Replaces, for FP32 state, the per-sweep launches of pd_kernels.cu (and the
+// reference's 3 + 15 launches per local-global iteration with a device
+// synchronisation after each, PdIpcGpuFunc.cu:1245-1346).  Layout:
+//   * every CTA owns a contiguous run of SELL-32 slices (rows); when it fits,
+//     its slice of the constant off-diagonal matrix N is copied once per launch
+//     into shared memory: the FP32 values, and the column offsets as a per-row
+//     index into a small table of distinct offset patterns (a structured mesh
+//     has a few dozen); otherwise the matrix is streamed from L2;
+//   * each thread owns R rows (one per slice it handles) and keeps their
+//     current/previous iterate, right-hand side and inverse diagonal in registers;
+//   * only the vector being gathered crosses CTAs (through L2, and through L1
+//     once the barrier's acquire has invalidated it), between grid barriers.
+// The grid barrier is a counter/generation pair with a clock-bounded wait: on
+// timeout it raises kErrBarrier and every later barrier returns at once, so the
+// kernel always terminates.  The launch is cooperative (all CTAs co-resident).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "kernels.cuh"
+#include "persistent.h"
+
+namespace pdipc {
+
+namespace {
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid barrier: every CTA's thread 0 arrives on one counter; the last arrival
+// resets it and bumps the generation everybody else waits on (measured 1.8 us
+// on 152 CTAs; a two-level counter tree was slower).  Waits are clock-bounded:
+// on timeout (or a timeout seen elsewhere) the error bit is set and the barrier
+// reports failure, so every CTA returns.  bar: [0] generation, [1] counter.
+// Returns false when the grid is in error.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* err, unsigned nblocks, unsigned& my_gen,
+                                             long long timeout_cycles) {
+    __syncthreads();
+    __shared__ int ok_s;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        if (ld_acquire_gpu(err) & kErrBarrier) {
+            ok = 0;
+        } else {
+            const unsigned g = my_gen;
+            __threadfence();
+            if (atomicAdd(bar + 1, 1u) + 1u == nblocks) {
+                atomicExch(bar + 1, 0u);
+                __threadfence();
+                atomicExch(bar, g + 1u);
+            } else {
+                const long long t0 = clock64();
+                while (ld_acquire_gpu(bar) == g) {
+                    if (clock64() - t0 > timeout_cycles || (ld_acquire_gpu(err) & kErrBarrier)) {
+                        atomicOr(err, (unsigned)kErrBarrier);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(8);
+                }
+            }
+            my_gen = g + 1u;
+        }
+        ok_s = ok;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+template <typename T>
+__device__ __forceinline__ V4<T> ldcg4(const V4<T>* p, int i) {
+    const float4 v = __ldcg(reinterpret_cast<const float4*>(p) + i);
+    return V4<T>{v.x, v.y, v.z, v.w};
+}
+// Coherent load that may hit in L1: data written by other CTAs before a grid
+// barrier is visible after it, because the barrier's gpu-scope acquire
+// invalidates this SM's L1 (PTX memory model: release -> acquire -> bar.sync).
+template <typename T>
+__device__ __forceinline__ V4<T> ldl14(const V4<T>* p, int i) {
+    const float4 v = *(reinterpret_cast<const float4*>(p) + i);
+    return V4<T>{v.x, v.y, v.z, v.w};
+}
+template <typename T>
+__device__ __forceinline__ void stcg4(V4<T>* p, int i, T x, T y, T z) {
+    __stcg(reinterpret_cast<float4*>(p) + i, make_float4(x, y, z, 0.f));
+}
+
+template <typename T, bool kCorr, bool kSmem, bool kL1, int R>
+__global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
+    auto ldv = [](const V4<T>* p, int i) { return kL1 ? ldl14(p, i) : ldcg4(p, i); };
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int cta = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // ---- this CTA's matrix values and the offset patterns into shared memory ----
+    const int eb = a.ctaEntry[cta], ee = a.ctaEntry[cta + 1];
+    const int E = ee - eb;
+    T* sval = reinterpret_cast<T*>(smem);
+    int16_t* spat = reinterpret_cast<int16_t*>(smem + ((size_t)E * sizeof(T) + 15) / 16 * 16);
+    if (kSmem) {
+        for (int q = threadIdx.x; q < E; q += blockDim.x) sval[q] = __ldg(a.sVal + eb + q);
+        for (int q = threadIdx.x; q < a.patterns * a.patW; q += blockDim.x) spat[q] = __ldg(a.patOff + q);
+    }
+    // ---- rows owned by this thread ----
+    int row[R], gb[R], sl[R], pid[R];
+    bool val[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int s = a.ctaSlice[cta] + warp * R + r;  // slice index
+        const bool sv = s < a.ctaSlice[cta + 1];
+        row[r] = s * 32 + lane;
+        val[r] = sv && row[r] < a.nsim;
+        gb[r] = sv ? a.sliceEntry[s] + lane : 0;
+        sl[r] = sv ? a.sliceLen[s] : 0;
+        pid[r] = (kSmem && val[r]) ? a.rowPattern[row[r]] * a.patW : 0;
+    }
+    // entry k of owned row r: value and gathered row
+    auto entry = [&](int r, int k, T& v, int& j) {
+        if (kSmem) {
+            v = sval[gb[r] - eb + 32 * k];
+            j = row[r] + (int)spat[pid[r] + k];
+        } else {
+            v = __ldg(a.sVal + gb[r] + 32 * k);
+            j = __ldg(a.sCol + gb[r] + 32 * k);
+        }
+    };
+    __syncthreads();
+    unsigned my_gen = 0;
+    if (threadIdx.x == 0) my_gen = ld_acquire_gpu(a.bar);
+    const T w = a.relax, om1 = T(1) - a.relax;
+    T id[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+        id[r] = val[r] ? T(1) / ((a.Delastic[row[r]] + a.Dinert[row[r]]) + a.CollDiag[row[r]]) : T(0);
+
+    // sum_k N_ik src_k for the owned rows, from shared memory
+    auto gather = [&](const V4<T>* src, int r, T& s0, T& s1, T& s2) {
+        s0 = T(0);
+        s1 = T(0);
+        s2 = T(0);
+#pragma unroll 4
+        for (int k = 0; k < sl[r]; ++k) {
+            T v;
+            int j;
+            entry(r, k, v, j);
+            const V4<T> xj = ldv(src, j);
+            s0 += v * xj.x;
+            s1 += v * xj.y;
+            s2 += v * xj.z;
+        }
+    };
+
+    for (int lg = 0; lg < a.lg; ++lg) {
+        // ---- curvature vectors of the owned rows ----
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (!val[r]) continue;
+            const int i = row[r];
+            const int b = a.lPtr[i], e = a.lPtr[i + 1];
+            const V4<T> x = ldv(a.P, i);
+            T a0, a1, a2;
+            if (kCorr) {
+                a0 = a1 = a2 = T(0);
+                for (int s = b + 1; s < e; ++s) {
+                    const V4<T> xj = ldv(a.P, a.lNbr[s]);
+                    const T l = a.lLbo[s];
+                    a0 += l * (xj.x - x.x);
+                    a1 += l * (xj.y - x.y);
+                    a2 += l * (xj.z - x.z);
+                }
+            } else {
+                const T l0 = a.lLbo[b];
+                a0 = x.x * l0;
+                a1 = x.y * l0;
+                a2 = x.z * l0;
+                for (int s = b + 1; s < e; ++s) {
+                    const V4<T> xj = ldv(a.P, a.lNbr[s]);
+                    const T l = a.lLbo[s];
+                    a0 += xj.x * l;
+                    a1 += xj.y * l;
+                    a2 += xj.z * l;
+                }
+            }
+            const T nrm = sqrtf(a0 * a0 + a1 * a1 + a2 * a2);
+            if (nrm >= T(1e-10)) {
+                const T c = a.CurvNorm[i] / nrm;
+                a0 *= c;
+                a1 *= c;
+                a2 *= c;
+            }
+            stcg4(a.Aq, i, a0, a1, a2);
+        }
+        if (!grid_barrier(a.bar, a.err, gridDim.x, my_gen, a.timeout)) return;
+
+        // ---- right-hand side (direct) or residual (correction) of the owned rows ----
+        T x0[R][3], rh[R][3];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            x0[r][0] = x0[r][1] = x0[r][2] = T(0);
+            rh[r][0] = rh[r][1] = rh[r][2] = T(0);
+            if (!val[r]) continue;
+            const int i = row[r];
+            const int b = a.lPtr[i], e = a.lPtr[i + 1];
+            const V4<T> x = ldv(a.P, i);
+            x0[r][0] = x.x;
+            x0[r][1] = x.y;
+            x0[r][2] = x.z;
+            const T strain = a.Strain[i];
+            if (kCorr) {
+                Sum2 r0, r1, r2;
+                {
+                    const V4<T> y = ldcg4(a.Rhs0, i);
+                    const T di = a.Dinert[i];
+                    r0.add(di * (y.x - x.x));
+                    r1.add(di * (y.y - x.y));
+                    r2.add(di * (y.z - x.z));
+                }
+                const int pf = a.PinFlag[i];
+                if (pf >= 0) {
+                    const V4<T> xr = ldcg4(a.Xrest, i);
+                    const T k = a.PinK[pf];
+                    r0.add(k * (xr.x - x.x));
+                    r1.add(k * (xr.y - x.y));
+                    r2.add(k * (xr.z - x.z));
+                }
+                {
+                    const V4<T> c = ldcg4(a.CollRhs, i);
+                    const V4<T> xo = ldcg4(a.Pold, i);
+                    const T dc = a.CollDiag[i];
+                    r0.add(c.x);
+                    r0.add(dc * (xo.x - x.x));
+                    r1.add(c.y);
+                    r1.add(dc * (xo.y - x.y));
+                    r2.add(c.z);
+                    r2.add(dc * (xo.z - x.z));
+                }
+                for (int s = b + 1; s < e; ++s) {
+                    const V4<T> xj = ldv(a.P, a.lNbr[s]);
+                    const T d0 = x.x - xj.x, d1 = x.y - xj.y, d2 = x.z - xj.z;
+                    const T cl = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+                    const T rc = strain * (a.lRest[s] / cl);
+                    r0.add(rc * d0);
+                    r1.add(rc * d1);
+                    r2.add(rc * d2);
+                }
+                const V4<T> ai = ldv(a.Aq, i);
+                const T b0 = a.lBend[b];
+                r0.add(b0 * ai.x);
+                r1.add(b0 * ai.y);
+                r2.add(b0 * ai.z);
+                for (int s = b + 1; s < e; ++s) {
+                    const V4<T> ak = ldv(a.Aq, a.lNbr[s]);
+                    const T bt = a.lBendT[s];
+                    r0.add(bt * ak.x);
+                    r1.add(bt * ak.y);
+                    r2.add(bt * ak.z);
+                }
+                for (int k = 0; k < sl[r]; ++k) {
+                    T v;
+                    int j;
+                    entry(r, k, v, j);
+                    const V4<T> xj = ldv(a.P, j);
+                    r0.add(v * (xj.x - x.x));
+                    r1.add(v * (xj.y - x.y));
+                    r2.add(v * (xj.z - x.z));
+                }
+                rh[r][0] = r0.value();
+                rh[r][1] = r1.value();
+                rh[r][2] = r2.value();
+            } else {
+                T t0 = T(0), t1 = T(0), t2 = T(0);
+                for (int s = b + 1; s < e; ++s) {
+                    const V4<T> xj = ldv(a.P, a.lNbr[s]);
+                    const T d0 = x.x - xj.x, d1 = x.y - xj.y, d2 = x.z - xj.z;
+                    const T cl = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+                    const T rc = strain * (a.lRest[s] / cl);
+                    t0 += rc * d0;
+                    t1 += rc * d1;
+                    t2 += rc * d2;
+                }
+                const V4<T> ai = ldv(a.Aq, i);
+                const T b0 = a.lBend[b];
+                t0 += b0 * ai.x;
+                t1 += b0 * ai.y;
+                t2 += b0 * ai.z;
+                const V4<T> q0 = ldcg4(a.Rhs0, i);
+                T u0 = q0.x + t0, u1 = q0.y + t1, u2 = q0.z + t2;
+                for (int s = b + 1; s < e; ++s) {
+                    const V4<T> ak = ldv(a.Aq, a.lNbr[s]);
+                    const T bt = a.lBendT[s];
+                    u0 += bt * ak.x;
+                    u1 += bt * ak.y;
+                    u2 += bt * ak.z;
+                }
+                const V4<T> c = ldcg4(a.CollRhs, i);
+                u0 += c.x;
+                u1 += c.y;
+                u2 += c.z;
+                const V4<T> pn = ldcg4(a.PinRhs, i);
+                u0 += pn.x;
+                u1 += pn.y;
+                u2 += pn.z;
+                rh[r][0] = u0;
+                rh[r][1] = u1;
+                rh[r][2] = u2;
+            }
+        }
+
+        // ---- Chebyshev-accelerated R2 iteration as two J sweeps per step ----
+        // direct form: iterate on x from x0 (gathered from P);
+        // correction form: iterate on delta from 0, add to x0 at the end.
+        T cx[R][3], px[R][3], yv[R][3];
+        // first sweep: Y = S(x0)
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            T s0 = T(0), s1 = T(0), s2 = T(0);
+            if (kCorr) {
+                cx[r][0] = cx[r][1] = cx[r][2] = T(0);
+            } else {
+                cx[r][0] = x0[r][0];
+                cx[r][1] = x0[r][1];
+                cx[r][2] = x0[r][2];
+                if (val[r]) gather(a.P, r, s0, s1, s2);
+            }
+            yv[r][0] = om1 * cx[r][0] + w * ((s0 + rh[r][0]) * id[r]);
+            yv[r][1] = om1 * cx[r][1] + w * ((s1 + rh[r][1]) * id[r]);
+            yv[r][2] = om1 * cx[r][2] + w * ((s2 + rh[r][2]) * id[r]);
+            if (val[r]) stcg4(a.GY, row[r], yv[r][0], yv[r][1], yv[r][2]);
+        }
+        if (!grid_barrier(a.bar, a.err, gridDim.x, my_gen, a.timeout)) return;
+        const int nsteps = a.cheby;
+        for (int it = 0; it < nsteps; ++it) {
+            const bool last = it == nsteps - 1;
+            // second sweep of the step: S(Y), Chebyshev-combined except for the first step
+            const T om = a.omega[it];
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                T s0 = T(0), s1 = T(0), s2 = T(0);
+                if (val[r]) gather(a.GY, r, s0, s1, s2);
+                T n0 = om1 * yv[r][0] + w * ((s0 + rh[r][0]) * id[r]);
+                T n1 = om1 * yv[r][1] + w * ((s1 + rh[r][1]) * id[r]);
+                T n2 = om1 * yv[r][2] + w * ((s2 + rh[r][2]) * id[r]);
+                if (it > 0) {
+                    n0 = om * (n0 - px[r][0]) + px[r][0];
+                    n1 = om * (n1 - px[r][1]) + px[r][1];
+                    n2 = om * (n2 - px[r][2]) + px[r][2];
+                }
+                px[r][0] = cx[r][0];
+                px[r][1] = cx[r][1];
+                px[r][2] = cx[r][2];
+                cx[r][0] = n0;
+                cx[r][1] = n1;
+                cx[r][2] = n2;
+                if (!val[r]) continue;
+                if (last) {
+                    if (kCorr) stcg4(a.P, row[r], x0[r][0] + n0, x0[r][1] + n1, x0[r][2] + n2);
+                    else stcg4(a.P, row[r], n0, n1, n2);
+                } else {
+                    stcg4(a.GX, row[r], n0, n1, n2);
+                }
+            }
+            if (!grid_barrier(a.bar, a.err, gridDim.x, my_gen, a.timeout)) return;
+            if (last) break;
+            // first sweep of the next step: Y = S(x)
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                T s0 = T(0), s1 = T(0), s2 = T(0);
+                if (val[r]) gather(a.GX, r, s0, s1, s2);
+                yv[r][0] = om1 * cx[r][0] + w * ((s0 + rh[r][0]) * id[r]);
+                yv[r][1] = om1 * cx[r][1] + w * ((s1 + rh[r][1]) * id[r]);
+                yv[r][2] = om1 * cx[r][2] + w * ((s2 + rh[r][2]) * id[r]);
+                if (val[r]) stcg4(a.GY, row[r], yv[r][0], yv[r][1], yv[r][2]);
+            }
+            if (!grid_barrier(a.bar, a.err, gridDim.x, my_gen, a.timeout)) return;
+        }
+    }
+}
+
+template <typename T, bool kCorr, bool kSmem, bool kL1>
+const void* kernel_for(int R) {
+    switch (R) {
+        case 1: return (const void*)k_pd_persistent<T, kCorr, kSmem, kL1, 1>;
+        case 2: return (const void*)k_pd_persistent<T, kCorr, kSmem, kL1, 2>;
+        case 3: return (const void*)k_pd_persistent<T, kCorr, kSmem, kL1, 3>;
+        default: return (const void*)k_pd_persistent<T, kCorr, kSmem, kL1, 4>;
+    }
+}
+
+template <bool kL1>
+const void* kernel_for_l1(bool correction, bool matrix_in_smem, int R) {
+    if (correction)
+        return matrix_in_smem ? kernel_for<float, true, true, kL1>(R) : kernel_for<float, true, false, kL1>(R);
+    return matrix_in_smem ? kernel_for<float, false, true, kL1>(R) : kernel_for<float, false, false, kL1>(R);
+}
+
+}  // namespace
+
+const void* persistent_kernel(bool correction, bool matrix_in_smem, bool l1_gather, int rows_per_thread) {
+    return l1_gather ? kernel_for_l1<true>(correction, matrix_in_smem, rows_per_thread)
+                     : kernel_for_l1<false>(correction, matrix_in_smem, rows_per_thread);
+}
+
+cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float>& args, bool correction,
+                                 cudaStream_t s) {
+    const void* f = persistent_kernel(correction, plan.matrix_in_smem, plan.l1_gather, plan.rows_per_thread);
+    void* params[] = {(void*)&args};
+    return cudaLaunchCooperativeKernel(f, dim3(plan.ctas), dim3(plan.threads), params, plan.smem_bytes, s);
+}
+
+}  // namespace pdipc

@@ -1,0 +1,80 @@
+// persistent.h — launch plan and arguments of the persistent PD solve
+// (pd_persistent.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace pdipc {
+
+constexpr int kMaxCheby = 64;
+
+struct PersistPlan {
+    bool enabled = false;
+    bool matrix_in_smem = false;  // values in shared memory, columns from the pattern table
+    bool l1_gather = true;        // gathers may hit in L1 (else L2-only .cg loads)
+    int ctas = 0;
+    int threads = 0;               // multiple of 32
+    int rows_per_thread = 1;       // R: slices per warp
+    int slices_per_cta = 0;
+    size_t smem_bytes = 0;
+    int patterns = 0;
+    int pattern_width = 0;
+};
+
+template <typename T>
+struct PersistArgs {
+    int nsim;
+    int lg;
+    int cheby;
+    T relax;
+    T omega[kMaxCheby];  // omega[it] of Chebyshev step it (it >= 1)
+    long long timeout;   // barrier wait limit in clock cycles
+    // state
+    V4<T>* P;
+    const V4<T>* Pold;
+    const V4<T>* Xrest;
+    const V4<T>* Rhs0;
+    const V4<T>* CollRhs;
+    const V4<T>* PinRhs;
+    V4<T>* Aq;
+    V4<T>* GX;
+    V4<T>* GY;
+    const T* Delastic;
+    const T* Dinert;
+    const T* CollDiag;
+    const int* PinFlag;
+    const T* PinK;
+    // local step stencils
+    const int* lPtr;
+    const int* lNbr;
+    const T* lRest;
+    const T* lLbo;
+    const T* lBend;
+    const T* lBendT;
+    const T* Strain;
+    const T* CurvNorm;
+    // matrix
+    const int* sliceEntry;  // SELL entry offset of every slice
+    const int* sliceLen;
+    const int* sCol;        // absolute columns (matrix streamed from global)
+    const T* sVal;
+    const int* ctaSlice;    // first slice of each CTA (ctas + 1)
+    const int* ctaEntry;    // first SELL entry of each CTA (ctas + 1)
+    const int* rowPattern;  // pattern id of every row (matrix in shared memory)
+    const int16_t* patOff;  // [patterns x pattern_width] column offsets
+    int patterns;
+    int patW;
+    // grid barrier: [0] generation, [1] arrival counter
+    unsigned* bar;
+    unsigned* err;
+};
+
+const void* persistent_kernel(bool correction, bool matrix_in_smem, bool l1_gather, int rows_per_thread);
+cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float>& args, bool correction,
+                                 cudaStream_t s);
+
+}  // namespace pdipc

@@ -12,7 +12,11 @@
 #include <cstring>
 #include <vector>
 
+#include <map>
+#include <type_traits>
+
 #include "kernels.cuh"
+#include "persistent.h"
 #include "solver.h"
 
 namespace pdipc {
@@ -137,6 +141,8 @@ public:
         PD_CK(up(d.CurvNorm, cn));
         PD_CK(up(d.Strain, st));
         PD_CK(up(d.PinFlag, pinf));
+        PD_CK(up(d.PinK, conv(H.pinK)));
+        PD_CK(zeros(d.C, ns));
         std::vector<TC> cm(nt, (TC)p.static_mass);
         for (int i = 0; i < ns; ++i) cm[i] = (TC)(T)H.collMassSim[i];
         PD_CK(up(d.CollMass, cm));
@@ -181,6 +187,8 @@ public:
         PD_CK(up(d.sLen, slen));
         PD_CK(up(d.sCol, scol));
         PD_CK(up(d.sVal, sval));
+        sliceOffH_ = soff;
+        sliceLenH_ = slen;
 
         // ---- collision topology ----
         std::vector<int4> faces(d.nface);
@@ -221,6 +229,10 @@ public:
         PD_CK(cudaMallocHost(&pin_, sizeof(Pinned)));
         std::memset(pin_, 0, sizeof(Pinned));
         PD_CK(cudaMallocHost(&stage_, sizeof(V4<T>) * (size_t)std::max(nt, 1)));
+
+        // ---- persistent PD solve plan (needs every buffer above) ----
+        pdipc_status pr = plan_persistent(H, sliceOffH_, sliceLenH_, err);
+        if (pr != PDIPC_OK) return pr;
 
         // ---- patch tree at the rest positions (AipcBvhs::init at initialization) ----
         pdipc_status r = build_tree(true, err);
@@ -306,6 +318,8 @@ public:
         s->device_bytes = bytes_;
         s->kernel_launches = launches_;
         s->device_ms = device_ms_;
+        s->pd_path = plan_.enabled ? (plan_.matrix_in_smem ? 2 : 1) : 0;
+        s->pd_ctas = plan_.enabled ? plan_.ctas : 0;
     }
 
     // ---------------- stages ----------------
@@ -376,6 +390,8 @@ public:
             rhs[3 * (size_t)i] = (double)stage_[i].x;
             rhs[3 * (size_t)i + 1] = (double)stage_[i].y;
             rhs[3 * (size_t)i + 2] = (double)stage_[i].z;
+            if (kCorrection)  // the correction form accumulates w (target - x); report sum w target
+                for (int k = 0; k < 3; ++k) rhs[3 * (size_t)i + k] += diag[i] * (double)(T)x[3 * (size_t)i + k];
         }
         if (n_active) *n_active = (int64_t)pin_->active;
         PD_CK(cudaMemsetAsync(d_.CollDiag, 0, sizeof(T) * d_.ntot, s_));
@@ -390,7 +406,8 @@ public:
         if (r == PDIPC_OK) r = set_state(X, V, err);
         if (r != PDIPC_OK) return r;
         launch_predict(d_, (T)c_.dt, s_);
-        enqueue_pd();
+        if (plan_.enabled) PD_CK(launch_persistent());
+        else enqueue_pd();
         r = get_positions(out, err);
         if (r == PDIPC_OK) r = set_state(saveX.data(), saveV.data(), err);
         return r;
@@ -478,6 +495,162 @@ private:
         ev0_ = ev1_ = nullptr;
         if (s_) cudaStreamDestroy(s_);
         s_ = nullptr;
+    }
+
+    // ---------------- persistent PD solve ----------------
+    // Partition of the SELL slices over co-resident CTAs (one per SM), with the
+    // matrix values in shared memory when they fit, and the argument block.
+    pdipc_status plan_persistent(const HostTables& H, const std::vector<int>& soff, const std::vector<int>& slen,
+                                 std::string& err) {
+        plan_ = PersistPlan();
+        if (!std::is_same<T, float>::value || !prm_.persistent || c_.cheby >= kMaxCheby) return PDIPC_OK;
+        Dev<T, TC>& d = d_;
+        const int ns = d.nsim, nsl = d.nslice;
+        int dev = 0, nsm = 0, smem_optin = 0, coop = 0;
+        PD_CK(cudaGetDevice(&dev));
+        PD_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        PD_CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        PD_CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        if (!coop || nsl == 0) return PDIPC_OK;
+        // distinct column-offset patterns of the rows
+        int patW = 0;
+        for (int w : slen) patW = std::max(patW, w);
+        std::map<std::vector<int16_t>, int> pats;
+        std::vector<int> rowPat(ns, 0);
+        bool fits16 = true;
+        for (int i = 0; i < ns && fits16; ++i) {
+            std::vector<int16_t> o(patW, 0);
+            for (int e = H.nPtr[i]; e < H.nPtr[i + 1]; ++e) {
+                const int off = H.nCol[e] - i;
+                if (off < -32768 || off > 32767) {
+                    fits16 = false;
+                    break;
+                }
+                o[e - H.nPtr[i]] = (int16_t)off;
+            }
+            auto it = pats.emplace(o, (int)pats.size()).first;
+            rowPat[i] = it->second;
+            if (pats.size() > 4096) fits16 = false;
+        }
+        const size_t patBytes = fits16 ? pats.size() * (size_t)patW * sizeof(int16_t) : 0;
+        auto cta_smem = [&](int spc, bool smem_mat) -> size_t {
+            if (!smem_mat) return 0;
+            size_t mx = 0;
+            for (int c = 0; c * spc < nsl; ++c) {
+                const int s0 = c * spc, s1 = std::min(nsl, s0 + spc);
+                const size_t E = (size_t)(soff[s1] - soff[s0]);
+                mx = std::max(mx, (E * sizeof(T) + 15) / 16 * 16 + patBytes);
+            }
+            return mx;
+        };
+        const size_t limit = (size_t)smem_optin - 1024;
+        for (int pass = 0; pass < 2 && !plan_.enabled; ++pass) {
+            const bool smem_mat = pass == 0 && fits16;
+            if (pass == 0 && !fits16) continue;
+            for (int R = 1; R <= 4; ++R) {
+                const int W = std::max(1, (nsl + nsm * R - 1) / (nsm * R));
+                if (W > 32) continue;
+                const int spc = W * R;
+                const int ctas = (nsl + spc - 1) / spc;
+                const size_t sm = cta_smem(spc, smem_mat);
+                if (sm > limit) continue;
+                const void* f = persistent_kernel(kCorrection, smem_mat, prm_.persistent != 2, R);
+                PD_CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
+                int per_sm = 0;
+                PD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, W * 32, sm));
+                if (per_sm < 1 || ctas > per_sm * nsm) continue;
+                plan_.enabled = true;
+                plan_.matrix_in_smem = smem_mat;
+                plan_.l1_gather = prm_.persistent != 2;
+                plan_.ctas = ctas;
+                plan_.threads = W * 32;
+                plan_.rows_per_thread = R;
+                plan_.slices_per_cta = spc;
+                plan_.smem_bytes = sm;
+                plan_.patterns = smem_mat ? (int)pats.size() : 0;
+                plan_.pattern_width = patW;
+                break;
+            }
+        }
+        if (!plan_.enabled) return PDIPC_OK;
+        std::vector<int> ctaSlice(plan_.ctas + 1), ctaEntry(plan_.ctas + 1);
+        for (int c = 0; c <= plan_.ctas; ++c) {
+            ctaSlice[c] = std::min(nsl, c * plan_.slices_per_cta);
+            ctaEntry[c] = soff[ctaSlice[c]];
+        }
+        std::vector<int16_t> patOff(std::max<size_t>(1, pats.size() * (size_t)patW), 0);
+        for (auto& kv : pats) std::copy(kv.first.begin(), kv.first.end(), patOff.begin() + (size_t)kv.second * patW);
+        PD_CK(up(pCtaSlice_, ctaSlice));
+        PD_CK(up(pCtaEntry_, ctaEntry));
+        PD_CK(up(pRowPat_, rowPat));
+        PD_CK(up(pPatOff_, patOff));
+        PD_CK(zeros(pBar_, 2));
+        if constexpr (std::is_same<T, float>::value) {
+            PersistArgs<float>& a = pargs_;
+            a.nsim = ns;
+            a.lg = c_.lg;
+            a.cheby = c_.cheby;
+            a.relax = (T)c_.relax;
+            T rho2 = (T)c_.rho;
+            rho2 = rho2 * rho2;
+            T om = omega_first(rho2);
+            for (int it = 0; it < kMaxCheby; ++it) a.omega[it] = T(0);
+            for (int it = 1; it < c_.cheby; ++it) {
+                a.omega[it] = om;
+                om = omega_next(rho2, om);
+            }
+            a.timeout = 4000000000ll;  // ~2 s at 2 GHz
+            a.P = d.P;
+            a.Pold = d.Pold;
+            a.Xrest = d.Xrest;
+            a.Rhs0 = d.Rhs0;
+            a.CollRhs = d.CollRhs;
+            a.PinRhs = d.PinRhs;
+            a.Aq = d.Aq;
+            a.GX = d.B;
+            a.GY = d.Y;
+            a.Delastic = d.Delastic;
+            a.Dinert = d.Dinert;
+            a.CollDiag = d.CollDiag;
+            a.PinFlag = d.PinFlag;
+            a.PinK = d.PinK;
+            a.lPtr = d.lPtr;
+            a.lNbr = d.lNbr;
+            a.lRest = d.lRest;
+            a.lLbo = d.lLbo;
+            a.lBend = d.lBend;
+            a.lBendT = d.lBendT;
+            a.Strain = d.Strain;
+            a.CurvNorm = d.CurvNorm;
+            a.sliceEntry = d.sOff;
+            a.sliceLen = d.sLen;
+            a.sCol = d.sCol;
+            a.sVal = d.sVal;
+            a.ctaSlice = pCtaSlice_;
+            a.ctaEntry = pCtaEntry_;
+            a.rowPattern = pRowPat_;
+            a.patOff = pPatOff_;
+            a.patterns = plan_.patterns;
+            a.patW = patW;
+            a.bar = pBar_;
+            a.err = d.ErrFlags;
+            const void* ptrs[] = {a.P, a.Pold, a.Xrest, a.Rhs0, a.CollRhs, a.PinRhs, a.Aq, a.GX, a.GY, a.Delastic,
+                                  a.Dinert, a.CollDiag, a.PinFlag, a.PinK, a.lPtr, a.lNbr, a.lRest, a.lLbo,
+                                  a.lBend, a.lBendT, a.Strain, a.CurvNorm, a.sliceEntry, a.sliceLen, a.sCol,
+                                  a.sVal, a.ctaSlice, a.ctaEntry, a.rowPattern, a.patOff, a.bar, a.err};
+            for (const void* q : ptrs)
+                if (!q) {
+                    plan_.enabled = false;
+                    err = "persistent solve: unallocated buffer";
+                    return PDIPC_ERR_STATE;
+                }
+        }
+        return PDIPC_OK;
+    }
+
+    cudaError_t launch_persistent() {
+        if constexpr (std::is_same<T, float>::value) return launch_pd_persistent(plan_, pargs_, kCorrection, s_);
+        return cudaErrorNotSupported;
     }
 
     // ---------------- patch tree ----------------
@@ -581,7 +754,42 @@ private:
     // One outer iteration's solve: diagonal, then lg x (local step + Chebyshev
     // accelerated Jacobi).  R2 x + c is evaluated as two weighted-Jacobi sweeps
     // S(S(x)); the iterates rotate through P and B, the last lands in P.
+    static constexpr bool kCorrection = sizeof(T) == 4 && sizeof(TC) == 8;
+
+    // Correction (mixed-precision) form: the same Chebyshev-accelerated Jacobi
+    // iteration on delta = x - x_start from delta_0 = 0, with the residual of
+    // x_start as right-hand side; the iterates rotate through B and C and the
+    // last one is added to P.
+    int enqueue_pd_correction() {
+        Dev<T, TC>& d = d_;
+        const T w = (T)c_.relax;
+        T rho2 = (T)c_.rho;
+        rho2 = rho2 * rho2;
+        int k = 0;
+        launch_diag(d, s_);
+        ++k;
+        for (int lg = 0; lg < c_.lg; ++lg) {
+            launch_local_aq(d, s_);
+            launch_local_residual(d, w, s_);
+            launch_sweep_delta<T, TC>(d, c_.cheby == 1 ? 4 : 0, d.Y, nullptr, c_.cheby == 1 ? d.P : d.B, w, T(0), s_);
+            k += 3;
+            T om = omega_first(rho2);
+            for (int it = 1; it < c_.cheby; ++it) {
+                V4<T>* cur = (it & 1) ? d.B : d.C;
+                V4<T>* prv = (it & 1) ? d.C : d.B;
+                const bool last = it == c_.cheby - 1;
+                const int mode = 1 | (it == 1 ? 2 : 0) | (last ? 4 : 0);
+                launch_sweep_delta<T, TC>(d, 0, cur, nullptr, d.Y, w, T(0), s_);
+                launch_sweep_delta<T, TC>(d, mode, d.Y, prv, last ? d.P : prv, w, om, s_);
+                k += 2;
+                om = omega_next(rho2, om);
+            }
+        }
+        return k;
+    }
+
     int enqueue_pd() {
+        if (kCorrection) return enqueue_pd_correction();
         Dev<T, TC>& d = d_;
         const T w = (T)c_.relax;
         T rho2 = (T)c_.rho;
@@ -609,6 +817,11 @@ private:
     }
 
     pdipc_status pd_solve(std::string& err) {
+        if (plan_.enabled) {
+            PD_CK(launch_persistent());
+            ++launches_;
+            return PDIPC_OK;
+        }
         if (!prm_.use_graphs) {
             launches_ += enqueue_pd();
             return PDIPC_OK;
@@ -677,6 +890,11 @@ private:
             const unsigned int e = pin_->err;
             pin_->err = 0;
             cudaMemsetAsync(d.ErrFlags, 0, sizeof(unsigned int), s_);
+            if (e & kErrBarrier) {
+                cudaMemsetAsync(pBar_ + 1, 0, sizeof(unsigned), s_);
+                err = "grid barrier of the persistent solve timed out";
+                return PDIPC_ERR_CUDA;
+            }
             if (e & kErrNonFinite) {
                 err = "non-finite position after the step";
                 return PDIPC_ERR_NONFINITE;
@@ -707,6 +925,14 @@ private:
     char* scan_tmp_ = nullptr;
     int64_t scan_tmp_cap_ = 0;
     Pinned* pin_ = nullptr;
+    PersistPlan plan_;
+    std::vector<int> sliceOffH_, sliceLenH_;
+    PersistArgs<float> pargs_{};
+    int* pCtaSlice_ = nullptr;
+    int* pCtaEntry_ = nullptr;
+    int* pRowPat_ = nullptr;
+    int16_t* pPatOff_ = nullptr;
+    unsigned* pBar_ = nullptr;
     V4<T>* stage_ = nullptr;
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;

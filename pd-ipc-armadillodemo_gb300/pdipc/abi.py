@@ -50,7 +50,8 @@ class Params(C.Structure):
         ("use_graphs", C.c_int),
         ("device", C.c_int),
         ("rebuild_bvh", C.c_int),
-        ("reserved", C.c_int * 7),
+        ("persistent", C.c_int),
+        ("reserved", C.c_int * 6),
     ]
 
 
@@ -78,6 +79,7 @@ def default_params() -> Params:
     p.use_graphs = 1
     p.device = 0
     p.rebuild_bvh = 0
+    p.persistent = 1
     return p
 
 
@@ -113,6 +115,8 @@ class Stats(C.Structure):
         ("device_bytes", C.c_int64),
         ("kernel_launches", C.c_int64),
         ("device_ms", C.c_double),
+        ("pd_path", C.c_int32),
+        ("pd_ctas", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

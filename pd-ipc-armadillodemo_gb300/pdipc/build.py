@@ -19,9 +19,13 @@ INC = os.path.join(ROOT, "include")
 OUT = os.path.join(PKG, "libpdipc.so")
 OBJ = os.path.join(PKG, "_build")
 
-SOURCES = ["pd_kernels.cu", "collision_kernels.cu", "primitives.cu", "solver.cu", "host_tables.cpp", "capi.cpp"]
+SOURCES = ["pd_kernels.cu", "pd_persistent.cu", "collision_kernels.cu", "primitives.cu", "solver.cu",
+           "host_tables.cpp", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC]
+# host code must not fuse multiply-adds: the patch grid is computed in FP32 exactly as
+# the reference does, and an Arm host compiler contracts a*b+c by default
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "-I" + INC, "-I" + CSRC]
 
 
 def nvcc() -> str:

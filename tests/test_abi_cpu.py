@@ -73,3 +73,19 @@ def test_argument_errors_are_reported(built_lib):
     F = np.array([[0, 1, 5]], np.int32)
     with pytest.raises(pdipc.PdipcError):
         pdipc.mesh_topology(X, F, 4)  # face index out of range
+
+
+def test_cxx_shim_compiles_links_and_reports(built_lib, tmp_path):
+    """The reference-style C++ class builds against include/ and libpdipc.so; on a
+    host without a GB300 initialization() reports PDIPC_ERR_CUDA instead of aborting."""
+    exe = tmp_path / "shim"
+    lib_dir = os.path.dirname(built_lib)
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cxx", "shim_main.cpp"), "-L" + lib_dir, "-lpdipc",
+                    "-Wl,-rpath," + lib_dir, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    if _has_gpu():
+        assert "animate PDIPC_OK" in out.stdout
+    else:
+        assert "init PDIPC_ERR_CUDA" in out.stdout

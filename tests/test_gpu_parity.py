@@ -7,7 +7,10 @@ Tolerances:
     1e-5 m after whole runs with contact;
   * FP32 mode: one PD solve within 2e-5 m of the FP32 oracle (the reference's
     own float Jacobi drifts ~1e-5 m per step from FP64, so FP32 runs are compared
-    over a few steps only); time of impact within 1e-5 relative.
+    over a few steps only); time of impact within 1e-5 relative;
+  * mixed mode (correction form, FP32 sweeps, FP64 residual / CCD refinement)
+    is checked against the FP64 oracle: time of impact within 1e-6 relative,
+    positions within 1e-4 m after whole runs.
 """
 import numpy as np
 import pytest
@@ -21,6 +24,10 @@ pytestmark = pytest.mark.gpu
 
 def small_scene(n=24, s=3, **kw):
     return scenes.cloth_drop(n, s, **kw)
+
+
+# the oracle run each library mode is held to
+ORACLE_PREC = {"fp32": "fp32", "fp64": "fp64", "mixed": "fp64"}
 
 
 def near_contact_state(scene, gap):
@@ -67,12 +74,14 @@ def test_broadphase_candidate_sets_bitexact(prec, built_lib):
     assert tg.shape[0] > 1000 and eg.shape[0] > 1000
 
 
-@pytest.mark.parametrize("prec,rtol", [("fp32", 1e-5), ("fp64", 1e-12), ("mixed", 1e-12)])
+@pytest.mark.parametrize("prec,rtol", [("fp32", 1e-5), ("fp64", 1e-12), ("mixed", 1e-6)])
 def test_time_of_impact_matches(prec, rtol, built_lib):
     sc = small_scene()
     sim = pdipc.Simulator(sc, prec)
-    orc = Oracle(sc, prec, FORM_JJ, threads=4)
+    orc = Oracle(sc, ORACLE_PREC[prec], FORM_JJ, threads=4)
     X = near_contact_state(sc, 1.5e-3)
+    if prec == "mixed":                # the library holds float positions; give the oracle the same inputs
+        X = X.astype(np.float32).astype(np.float64)
     dx = np.zeros_like(X)
     dx[:sc.n_sim, 1] = -4e-3           # drive the cloth into the sphere
     rng = np.random.default_rng(3)
@@ -80,13 +89,21 @@ def test_time_of_impact_matches(prec, rtol, built_lib):
     pg, tg, eg = sim.stage_broadphase(X, dx)
     po, to, eo = orc.broadphase(X, dx)
     X1 = X + dx
+    if prec == "mixed":
+        X1 = X1.astype(np.float32).astype(np.float64)
     tpg, teg, gg = sim.stage_toi(X, X1, tg.shape[0], eg.shape[0])
     tpo, teo, go = orc.toi(X, X1, to.shape[0], eo.shape[0])
     # match candidates by their vertex tuples
     ig, io = np.lexsort(tg.T[::-1]), np.lexsort(to.T[::-1])
-    np.testing.assert_allclose(tpg[ig], tpo[io], rtol=rtol, atol=0)
     jg, jo = np.lexsort(eg.T[::-1]), np.lexsort(eo.T[::-1])
-    np.testing.assert_allclose(teg[jg], teo[jo], rtol=rtol, atol=0)
+    if prec == "mixed":   # only candidates that clamp are evaluated in FP64; compare those
+        m = tpo[io] < 1.0
+        np.testing.assert_allclose(tpg[ig][m], tpo[io][m], rtol=rtol, atol=0)
+        m = teo[jo] < 1.0
+        np.testing.assert_allclose(teg[jg][m], teo[jo][m], rtol=rtol, atol=0)
+    else:
+        np.testing.assert_allclose(tpg[ig], tpo[io], rtol=rtol, atol=0)
+        np.testing.assert_allclose(teg[jg], teo[jo], rtol=rtol, atol=0)
     assert go < 1.0
     # the clamped global toi is rounded to the state type (float in mixed mode)
     assert abs(gg - go) <= max(rtol, 1e-7 if prec == "mixed" else 0.0) * go
@@ -95,12 +112,14 @@ def test_time_of_impact_matches(prec, rtol, built_lib):
     assert np.all(teg[jg][teo[jo] < 1.0] < 1.0)
 
 
-@pytest.mark.parametrize("prec,tol", [("fp32", 2e-6), ("fp64", 1e-12), ("mixed", 2e-6)])
+@pytest.mark.parametrize("prec,tol", [("fp32", 2e-6), ("fp64", 1e-12), ("mixed", 1e-6)])
 def test_contact_projection_matches(prec, tol, built_lib):
     sc = small_scene()
     sim = pdipc.Simulator(sc, prec)
-    orc = Oracle(sc, prec, FORM_JJ, threads=4)
+    orc = Oracle(sc, ORACLE_PREC[prec], FORM_JJ, threads=4)
     X = near_contact_state(sc, 4e-4)
+    if prec == "mixed":
+        X = X.astype(np.float32).astype(np.float64)
     sim.stage_broadphase(X, np.zeros_like(X))
     orc.broadphase(X, np.zeros_like(X))
     dg, rg, ng = sim.stage_contact(X)
@@ -111,14 +130,17 @@ def test_contact_projection_matches(prec, tol, built_lib):
     np.testing.assert_allclose(rg, ro, rtol=tol, atol=tol * np.abs(ro).max())
 
 
-@pytest.mark.parametrize("prec,atol", [("fp32", 2e-5), ("fp64", 1e-10), ("mixed", 2e-5)])
+@pytest.mark.parametrize("prec,atol", [("fp32", 2e-5), ("fp64", 1e-10), ("mixed", 1e-6)])
 def test_pd_solve_matches(prec, atol, built_lib):
     sc = small_scene(32, 2)
     sim = pdipc.Simulator(sc, prec)
-    orc = Oracle(sc, prec, FORM_JJ, threads=4)
+    orc = Oracle(sc, ORACLE_PREC[prec], FORM_JJ, threads=4)
     X = np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics])
     rng = np.random.default_rng(11)
     V = rng.uniform(-0.1, 0.1, (sc.n_sim, 3))
+    if prec == "mixed":
+        X = X.astype(np.float32).astype(np.float64)
+        V = V.astype(np.float32).astype(np.float64)
     xg = sim.stage_pd(X, V)
     xo = orc.stage_pd(X, V)
     assert np.abs(xg - xo).max() < atol
@@ -146,6 +168,39 @@ def test_fp64_run_with_contact_matches_oracle(built_lib):
     assert worst < 1e-5, worst
 
 
+def test_mixed_run_with_contact_within_1e4_of_fp64(built_lib):
+    """The correction (mixed-precision) form stays within 1e-4 m of the FP64 oracle
+    through contact, and converges in as few outer iterations."""
+    sc = scenes.cloth_drop(24, 3, height=-0.185, lg=10)
+    sim = pdipc.Simulator(sc, "mixed")
+    orc = Oracle(sc, "fp64", FORM_JJ, threads=8)
+    worst = 0.0
+    for k in range(6):
+        sim.step(10)
+        orc.step(10)
+        worst = max(worst, np.abs(sim.positions() - orc.positions()).max())
+    assert orc.stats()["active_contacts"] > 0
+    assert worst < 1e-4, worst
+
+
+def test_broadphase_full_size_bitexact(built_lib):
+    """512x512 cloth + subdivision-6 sphere at rest: the candidate sets of the
+    library's LBVH and the oracle's heap tree are identical."""
+    sc = scenes.config1()
+    sim = pdipc.Simulator(sc, "fp32")
+    orc = Oracle(sc, "fp32", FORM_JJ, threads=16)
+    X = np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics])
+    rng = np.random.default_rng(0)
+    dx = np.zeros_like(X)
+    dx[:sc.n_sim] = rng.uniform(-2e-4, 2e-4, (sc.n_sim, 3))
+    pg, tg, eg = sim.stage_broadphase(X, dx)
+    po, to, eo = orc.broadphase(X, dx)
+    assert sim.stats()["n_patches"] == orc.stats()["n_patches"]
+    assert np.array_equal(sort_rows(pg), sort_rows(po))
+    assert np.array_equal(sort_rows(tg), sort_rows(to))
+    assert np.array_equal(sort_rows(eg), sort_rows(eo))
+
+
 def test_fp32_steps_match_oracle_short_horizon(built_lib):
     sc = small_scene(32, 3)
     sim = pdipc.Simulator(sc, "fp32")
@@ -153,6 +208,24 @@ def test_fp32_steps_match_oracle_short_horizon(built_lib):
     sim.step(3)
     orc.step(3)
     assert np.abs(sim.positions() - orc.positions()).max() < 1e-4
+
+
+@pytest.mark.parametrize("prec,atol", [("fp32", 2e-5), ("mixed", 1e-6)])
+@pytest.mark.parametrize("n", [16, 48])
+@pytest.mark.parametrize("variant", [1, 2])
+def test_persistent_solve_matches_per_sweep_launches(prec, atol, n, variant, built_lib):
+    """One cooperative launch per outer iteration (gathers through L1, or L2
+    only) gives the same PD solve as one launch per sweep."""
+    sc = small_scene(n, 2)
+    a = pdipc.Simulator(sc, prec, persistent=variant)
+    b = pdipc.Simulator(sc, prec, persistent=0)
+    assert a.stats()["pd_path"] in (1, 2) and b.stats()["pd_path"] == 0
+    X = np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics])
+    V = np.random.default_rng(5).uniform(-0.1, 0.1, (sc.n_sim, 3))
+    assert np.abs(a.stage_pd(X, V) - b.stage_pd(X, V)).max() < atol
+    a.step(4)
+    b.step(4)
+    assert np.abs(a.positions() - b.positions()).max() < 10 * atol
 
 
 def test_graph_and_plain_launches_agree(built_lib):
@@ -200,4 +273,4 @@ def test_animate_returns_positions_and_counts_launches(built_lib):
     out = sim.animate()
     assert out.shape == (sc.n_total, 3) and np.isfinite(out).all()
     st = sim.stats()
-    assert st["kernel_launches"] > 100 and st["steps_done"] == 1
+    assert st["kernel_launches"] > 10 and st["steps_done"] == 1
