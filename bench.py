@@ -7,8 +7,9 @@ One step = PdIpcSimulator::run(frame) on the 512x512 workload: prediction,
 outer CCD iterations (each 20 local-global iterations of 15 Chebyshev-Jacobi
 R2 sweeps, CCD, contact), velocity update.  `value` is device time from CUDA
 events recorded on the library's own stream around every step (L2 flushed
-between steps); `e2e` is wall time of BaseSimulator::animate (step + postRun
-copy of all positions to host memory) through the C ABI.  With torchrun
+between steps); `e2e` is wall time through the C ABI with host buffers: the
+initial state uploaded from host memory (pdipc_set_state), then per step
+BaseSimulator::animate (step + postRun copy of all positions to host memory).  With torchrun
 (N > 1) every rank steps an independent replica on its own GPU (the path does
 not shard: "replicas only"); the value is all replicas' steps over the slowest
 rank's time.
@@ -167,8 +168,9 @@ def measured_peak_hbm():
 
 
 def profiled_traffic(prec: str):
-    """DRAM bytes per sweep launch from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", f"sweep_c1_{prec}.md")
+    """DRAM bytes per launch of the persistent PD solve from the committed ncu
+    summary, if present."""
+    p = os.path.join(ROOT, "profiles", f"pd_persistent_c1_{prec}.md")
     try:
         for ln in open(p):
             if ln.startswith("traffic_bytes_per_launch:"):
@@ -218,6 +220,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     barrier(dist, dev)
     dev_ms, launches, outers, wall = 0.0, 0, [], 0.0
+    pd_ms, pd_solves = 0.0, 0
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             flush.zero_()                    # L2 flush between timed steps (256 MB write)
@@ -229,16 +232,24 @@ def run_ours(args):
             dev_ms += st["device_ms"]
             launches += st["kernel_launches"]
             outers.append(st["last_outer_iters"])
+            pd_ms += st["pd_solve_ms"]
+            pd_solves += st["pd_solves"]
         torch.cuda.synchronize()
     barrier(dist, dev)
     dev_ms_max = max_over_ranks(dist, dev_ms, dev)
     st_end = sim.stats()
 
-    # e2e through the public API: animate = run + postRun (positions to host)
-    sim.reset()
+    # e2e through the public API with host buffers: the initial state from host
+    # memory, then animate = run + postRun (positions to host) every step
+    x_init = np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics])
+    v_init = np.zeros((sc.n_sim, 3))
     out = np.empty((sim.n_total, 3), np.float64)
     barrier(dist, dev)
-    e2e_wall = 0.0
+    flush.zero_()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.set_state(x_init, v_init)
+    e2e_wall = time.perf_counter() - t0
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -273,11 +284,20 @@ def run_ours(args):
         ref.close()
         del ref
 
-    # roofline of the dominant kernel (the J sweep), timed alone on this stream
+    # roofline of the dominant kernel: the PD solve of an outer iteration (one
+    # persistent launch), timed by the library's events around each solve over
+    # the timed steps; and one J sweep launched alone, for comparison
+    pd_bytes = float(st_end["pd_solve_bytes"])
+    pd_ms_per = pd_ms / max(pd_solves, 1)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = pd_bytes / (pd_ms_per * 1e-3) / 1e9
     sim.set_state(x_end)
     sweep_ms, sweep_bytes = sim.sweep_timing(400)
-    peak, peak_kind = measured_peak_hbm()
-    achieved = sweep_bytes / (sweep_ms * 1e-3) / 1e9
+    sweep_gbs = sweep_bytes / (sweep_ms * 1e-3) / 1e9
+    pd_kernel = {2: "k_pd_persistent (cooperative, matrix values in shared memory)",
+                 1: "k_pd_persistent (cooperative, matrix from L2)",
+                 0: "PD solve as a CUDA graph of per-sweep kernels"}[st_end["pd_path"]]
+    state_bytes = 16 if args.precision == "fp32" else 32
 
     value = aggregate_steps_per_s(ws, args.steps, dev_ms_max)
     e2e = aggregate_steps_per_s(ws, args.steps, e2e_max * 1e3)
@@ -286,11 +306,13 @@ def run_ours(args):
             dist.destroy_process_group()
         return
     mean_outer = float(np.mean(outers))
+    traffic = profiled_traffic(args.precision)
     res = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp32": "f32", "fp64": "f64", "mixed": "f32 (sweeps, state) + f64 (residual, CCD/contact refinement)"}[
+        "dtype": {"fp32": "f32", "fp64": "f64",
+                  "mixed": "f32 (local step, residual terms, sweeps) + f64 (state, CCD/contact refinement)"}[
             args.precision], "data": "synthetic (seeded generator; no public dataset for this path)",
         "config": {"workload": workload_desc(sc, args.precision), "steps_timed": f"0..{args.steps - 1}",
                    "parallelism": "replicas only" if ws > 1 else "single GPU",
@@ -303,15 +325,23 @@ def run_ours(args):
         "element_updates_per_s": round(sim.n_sim * sc.lg_iterations * float(np.sum(outers)) / (dev_ms / 1e3), 1),
         "wall_ms_per_step": round(1e3 * wall / args.steps, 4),
         "gpu_launches": int(launches),
-        "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": int(sim.n_total * 16 + 8 * round(mean_outer) + 32),
-                "note": "animate(): step + copy of every position to host; the step takes no host input "
-                        "(state stays on the device, as in the reference)"},
+        "e2e": {"value": round(e2e, 4), "unit": UNIT,
+                "h2d_bytes_per_step": int(round((sim.n_total + sc.n_sim) * state_bytes / args.steps)),
+                "d2h_bytes_per_step": int(sim.n_total * state_bytes + 8 * round(mean_outer) + 48),
+                "note": "set_state of the initial positions/velocities from host memory once, then animate() "
+                        "per step (step + copy of every position to host); the state stays on the device "
+                        "between steps, as in the reference"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.precision),
-                     "kernel": "k_sweep (weighted-Jacobi sweep, SELL-32)",
-                     "bytes_per_launch": int(sweep_bytes), "ms_per_launch": round(sweep_ms, 6),
-                     "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+                     "frac": round(achieved / peak, 4),
+                     "traffic": None if traffic is None else round(traffic),
+                     "kernel": pd_kernel, "launches_timed": int(pd_solves),
+                     "bytes_per_launch": round(pd_bytes), "ms_per_launch": round(pd_ms_per, 4),
+                     "bytes_rule": "per vertex and local-global iteration: local step 16 d + 68, 2 x cheby sweeps "
+                                   "of 8 n + 28, (cheby - 1) x 12 Chebyshev reads (FP32 sizes)",
+                     "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)",
+                     "sweep_alone": {"kernel": "one weighted-Jacobi sweep launch (SELL-32) timed alone",
+                                     "bytes_per_launch": int(sweep_bytes), "ms_per_launch": round(sweep_ms, 6),
+                                     "achieved": round(sweep_gbs, 1), "frac": round(sweep_gbs / peak, 4)}},
         "clocks": clk.summary(),
     }
     if fp64 is not None:

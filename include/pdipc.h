@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PDIPC_ABI_VERSION 1
+#define PDIPC_ABI_VERSION 2
 
 typedef struct pdipc_ctx pdipc_ctx;
 
@@ -51,7 +51,9 @@ typedef enum {
 typedef enum {
     PDIPC_PREC_FP32 = 0,  /* every kernel in float: the reference's own arithmetic (DataCore.h:8,19) */
     PDIPC_PREC_FP64 = 1,  /* every kernel in double: the plain FP64 GPU form */
-    PDIPC_PREC_MIXED = 2  /* float state / local step / sweeps / barrier, double CCD and contact distance */
+    PDIPC_PREC_MIXED = 2  /* double state (positions, velocities, step direction, toi); float local step,
+                             residual terms and sweeps on the correction; float CCD filter with double
+                             re-evaluation of clamping candidates; double contact distances */
 } pdipc_precision;
 
 /* Solver parameters.  Defaults (pdipc_default_params) are the reference's
@@ -107,6 +109,12 @@ typedef struct {
     int32_t pd_path;             /* 0: one launch per sweep; 1: persistent, matrix from L2;
                                     2: persistent, matrix values in shared memory */
     int32_t pd_ctas;             /* CTAs of the persistent solve (0 if not used) */
+    int64_t pd_solves;           /* projective-dynamics solves (one per outer iteration) in the last call */
+    double pd_solve_ms;          /* their device time: CUDA events on the context's stream around each solve */
+    double pd_solve_bytes;       /* algorithmic bytes of one solve: per vertex i and local-global iteration,
+                                    local step 16 d_i + 68 plus (2 cheby) sweeps of 8 n_i + 28 plus
+                                    (cheby - 1) Chebyshev reads of 12 (d_i stencil neighbours, n_i matrix
+                                    off-diagonals; FP32 sizes, doubled value sizes in FP64 mode) */
 } pdipc_stats;
 
 /* Fill *p with the reference defaults listed beside each field. */
@@ -217,13 +225,14 @@ pdipc_status pdipc_stage_contact(pdipc_ctx* ctx, const double* x,
  * positions.  The context's state is restored afterwards. */
 pdipc_status pdipc_stage_pd(pdipc_ctx* ctx, const double* X, const double* V, double* out_X);
 
-/* Times the dominant kernel of the step, one plain weighted-Jacobi sweep over
- * the system matrix (the R2 sweep of chebyshevJacobiR2IterationKernel,
- * PdIpcGpuFunc.cu:1076-1129, here applied as one of two J sweeps), on the
- * current state: `launches` back-to-back launches on the context's stream
- * between two CUDA events.  *avg_ms = mean duration of one launch;
- * *bytes = algorithmic bytes one launch must move (8 per stored matrix entry
- * + 40 per row: x, rhs and output xyz, inverse diagonal). */
+/* Times the unit of the projective-dynamics solve launched on its own: one
+ * plain weighted-Jacobi sweep over the system matrix (the R2 sweep of
+ * chebyshevJacobiR2IterationKernel, PdIpcGpuFunc.cu:1076-1129, here applied
+ * as one of two J sweeps; on the correction in the mixed mode), `launches`
+ * back-to-back launches on the context's stream between two CUDA events.
+ * *avg_ms = mean duration of one launch; *bytes = algorithmic bytes one launch
+ * must move (8 per stored matrix entry + 40 per row: x, rhs and output xyz,
+ * inverse diagonal; FP32 sizes, double value sizes in FP64 mode). */
 pdipc_status pdipc_stage_sweep_timing(pdipc_ctx* ctx, int launches, double* avg_ms, double* bytes);
 
 /* Topology precompute of one mesh, on the host (no device needed):

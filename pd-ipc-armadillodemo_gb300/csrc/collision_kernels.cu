@@ -49,11 +49,12 @@ __device__ __forceinline__ void warp_box_reduce(T lo[3], T hi[3]) {
 
 // Swept, inflated patch AABB: per face min/max over x and x+dx of its three
 // vertices, minus/plus the inflation radius (getFaceBbox, cu:1350-1375), then
-// reduced over the patch's faces.
-template <typename T>
+// reduced over the patch's faces.  Boxes are in T: FP64 state (S) is rounded
+// to T first, so the mixed form's boxes are the FP32 form's.
+template <typename T, typename S>
 __global__ void k_patch_boxes(int npatch, const int* __restrict__ pfPtr, const int* __restrict__ pfIdx,
-                              const int4* __restrict__ Faces, const V4<T>* __restrict__ X,
-                              const V4<T>* __restrict__ D, T infl, Box6<T>* __restrict__ out) {
+                              const int4* __restrict__ Faces, const V4<S>* __restrict__ X,
+                              const V4<S>* __restrict__ D, T infl, Box6<T>* __restrict__ out) {
     const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (p >= npatch) return;
@@ -65,12 +66,14 @@ __global__ void k_patch_boxes(int npatch, const int* __restrict__ pfPtr, const i
         const int vv[3] = {f.x, f.y, f.z};
         T a[3][3], c[3][3];
         for (int j = 0; j < 3; ++j) {
-            const V4<T> x = ld4(X, vv[j]);
+            const V4<S> xs = ld4(X, vv[j]);
+            const V4<T> x{(T)xs.x, (T)xs.y, (T)xs.z, T(0)};
             a[j][0] = x.x;
             a[j][1] = x.y;
             a[j][2] = x.z;
             if (D) {
-                const V4<T> d = ld4(D, vv[j]);
+                const V4<S> ds = ld4(D, vv[j]);
+                const V4<T> d{(T)ds.x, (T)ds.y, (T)ds.z, T(0)};
                 c[j][0] = x.x + d.x;
                 c[j][1] = x.y + d.y;
                 c[j][2] = x.z + d.z;
@@ -100,17 +103,17 @@ __global__ void k_patch_boxes(int npatch, const int* __restrict__ pfPtr, const i
 
 // Init-time patch boxes over every vertex of the patch's faces, inflated
 // (gpuCollisionInit, cpp:1279-1292).
-template <typename T>
+template <typename T, typename S>
 __global__ void k_init_boxes(int npatch, const int* __restrict__ pxPtr, const int* __restrict__ pxIdx,
-                             const V4<T>* __restrict__ X, T infl, Box6<T>* __restrict__ out) {
+                             const V4<S>* __restrict__ X, T infl, Box6<T>* __restrict__ out) {
     const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (p >= npatch) return;
     T lo[3] = {tmax_val<T>(), tmax_val<T>(), tmax_val<T>()};
     T hi[3] = {-tmax_val<T>(), -tmax_val<T>(), -tmax_val<T>()};
     for (int q = pxPtr[p] + lane; q < pxPtr[p + 1]; q += 32) {
-        const V4<T> x = ld4(X, pxIdx[q]);
-        const T xs[3] = {x.x, x.y, x.z};
+        const V4<S> x = ld4(X, pxIdx[q]);
+        const T xs[3] = {(T)x.x, (T)x.y, (T)x.z};
         for (int k = 0; k < 3; ++k) {
             lo[k] = dmin(lo[k], xs[k] - infl);
             hi[k] = dmax(hi[k], xs[k] + infl);
@@ -408,13 +411,13 @@ __device__ __forceinline__ void block_min_to(TC v, TC* dst) {
 
 // getImpactOfTimeKernel (cu:2610-2704): skip pairs sharing a vertex, swept-AABB
 // filter with slack, additive CCD; global minimum by integer atomicMin.
-// kRel (mixed precision): coordinates relative to the pair's first vertex in
-// FP32 (a difference of nearby positions loses nothing), additive CCD in FP32,
+// kRel (mixed precision): coordinates relative to the pair's first vertex,
+// formed in FP64 from the FP64 state, an FP32 additive CCD on their rounding,
 // and every candidate that would clamp the step (toi < 1) re-evaluated in FP64
-// from the same relative coordinates, so the minimum is an FP64 time of impact.
+// from the FP64 relative coordinates, so the minimum is an FP64 time of impact.
 template <typename T, typename TC, bool kPT, bool kRel>
 __global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restrict__ cand,
-                                                const V4<T>* __restrict__ X0, const V4<T>* __restrict__ X1,
+                                                const V4<TC>* __restrict__ X0, const V4<TC>* __restrict__ X1,
                                                 TC slack, TC eta, int max_iter, TC* __restrict__ per,
                                                 TC* __restrict__ toi_min) {
     TC local = TC(1);
@@ -427,35 +430,33 @@ __global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restric
         if (!shared) {
             if (kRel) {
                 T x[4][3], dx[4][3];
-                const V4<T> o = ld4(X0, ids[0]);
+                TC xd[4][3], dd[4][3];
+                const V4<TC> o = ld4(X0, ids[0]);
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    const V4<T> a = ld4(X0, ids[j]), b = ld4(X1, ids[j]);
-                    x[j][0] = a.x - o.x;
-                    x[j][1] = a.y - o.y;
-                    x[j][2] = a.z - o.z;
-                    dx[j][0] = b.x - a.x;
-                    dx[j][1] = b.y - a.y;
-                    dx[j][2] = b.z - a.z;
+                    const V4<TC> a = ld4(X0, ids[j]), b = ld4(X1, ids[j]);
+                    xd[j][0] = a.x - o.x;
+                    xd[j][1] = a.y - o.y;
+                    xd[j][2] = a.z - o.z;
+                    dd[j][0] = b.x - a.x;
+                    dd[j][1] = b.y - a.y;
+                    dd[j][2] = b.z - a.z;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        x[j][k] = (T)xd[j][k];
+                        dx[j][k] = (T)dd[j][k];
+                    }
                 }
                 const bool hit = kPT ? geo::pt_ccd_broad<T>(x, dx, (T)slack) : geo::ee_ccd_broad<T>(x, dx, (T)slack);
                 if (hit) {
-                    TC xd[4][3], dd[4][3];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j)
-#pragma unroll
-                        for (int k = 0; k < 3; ++k) {
-                            xd[j][k] = (TC)x[j][k];
-                            dd[j][k] = (TC)dx[j][k];
-                        }
                     const T tf = kPT ? geo::ccd_pt<T>(x, dx, (T)eta, max_iter) : geo::ccd_ee<T>(x, dx, (T)eta, max_iter);
                     if (tf < T(1))
                         toi = kPT ? geo::ccd_pt<TC>(xd, dd, eta, max_iter) : geo::ccd_ee<TC>(xd, dd, eta, max_iter);
                 }
             } else {
                 TC x[4][3], dx[4][3];
-                gather4<T, TC>(X0, ids, x);
-                gather4<T, TC>(X1, ids, dx);
+                gather4<TC, TC>(X0, ids, x);
+                gather4<TC, TC>(X1, ids, dx);
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
 #pragma unroll
@@ -473,11 +474,11 @@ __global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restric
     block_min_to(local, toi_min);
 }
 
-template <typename T, typename TC>
-__global__ void k_toi_finalize(TC* __restrict__ toi_min, T* __restrict__ toi, double scale) {
+template <typename TC>
+__global__ void k_toi_finalize(TC* __restrict__ toi_min, TC* __restrict__ toi, double scale) {
     const TC m = *toi_min;
     const TC t = (m < TC(1)) ? (TC)((double)m * scale) : TC(1);
-    *toi = (T)t;
+    *toi = t;
     *toi_min = TC(1);
 }
 
@@ -490,12 +491,13 @@ struct ContactConsts {
 // w = kappa b(d^2) + min(m_p, m_q)/dt^2 to the diagonal of its 4 vertices and
 // w * target to their right-hand side; targets push the pair apart to dhat
 // along the closest-point direction, split by the mass ratio.
-// kRel (mixed precision): relative coordinates, FP32 filter, FP64 distance and
-// weight for pairs within 1.1 dhat, and the right-hand side accumulated as
-// w * (target - x) so the later residual needs no cancellation.
+// kRel (mixed precision): relative coordinates formed in FP64, an FP32 filter
+// on their rounding, FP64 distance and weight for pairs within 1.1 dhat, and
+// the right-hand side accumulated as w * (target - x) so the later residual
+// needs no cancellation.
 template <typename T, typename TC, bool kPT, bool kRel>
 __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __restrict__ cand,
-                                                    const V4<T>* __restrict__ X, const TC* __restrict__ mass,
+                                                    const V4<TC>* __restrict__ X, const TC* __restrict__ mass,
                                                     ContactConsts<TC> cc, T* __restrict__ diag,
                                                     V4<T>* __restrict__ rhs, unsigned long long* __restrict__ active) {
     unsigned int my = 0;
@@ -507,13 +509,15 @@ __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __res
         TC p[4][3];
         if (kRel) {
             T q[4][3];
-            const V4<T> o = ld4(X, ids[0]);
+            const V4<TC> o = ld4(X, ids[0]);
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const V4<T> a = ld4(X, ids[j]);
-                q[j][0] = a.x - o.x;
-                q[j][1] = a.y - o.y;
-                q[j][2] = a.z - o.z;
+                const V4<TC> a = ld4(X, ids[j]);
+                p[j][0] = a.x - o.x;
+                p[j][1] = a.y - o.y;
+                p[j][2] = a.z - o.z;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) q[j][k] = (T)p[j][k];
             }
             const T dhf = (T)cc.dh;
             bool far = false;
@@ -536,12 +540,8 @@ __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __res
             const T d2f = kPT ? geo::vtx_tri<T>(q[0], q[1], q[2], q[3], &a_, &b_, &c_, df)
                               : geo::edge_edge_sq<T>(q[0], q[1], q[2], q[3], &a_, &b_, df);
             if (!(d2f < (T)(1.21 * cc.dh2))) continue;
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-#pragma unroll
-                for (int k = 0; k < 3; ++k) p[j][k] = (TC)q[j][k];
         } else {
-            gather4<T, TC>(X, ids, p);
+            gather4<TC, TC>(X, ids, p);
             bool far = false;
             if (kPT) {
 #pragma unroll
@@ -610,15 +610,15 @@ __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __res
 }  // namespace
 
 template <typename T, typename TC>
-void launch_patch_boxes(const Dev<T, TC>& d, const V4<T>* X, const V4<T>* D, T infl, cudaStream_t s) {
+void launch_patch_boxes(const Dev<T, TC>& d, const V4<TC>* X, const V4<TC>* D, T infl, cudaStream_t s) {
     if (d.npatch == 0) return;
-    k_patch_boxes<T><<<blocks_for((int64_t)d.npatch * 32), kBlock, 0, s>>>(d.npatch, d.pfPtr, d.pfIdx, d.Faces, X,
+    k_patch_boxes<T, TC><<<blocks_for((int64_t)d.npatch * 32), kBlock, 0, s>>>(d.npatch, d.pfPtr, d.pfIdx, d.Faces, X,
                                                                           D, infl, d.PatchBox);
 }
 template <typename T, typename TC>
 void launch_patch_init_boxes(const Dev<T, TC>& d, T infl, cudaStream_t s) {
     if (d.npatch == 0) return;
-    k_init_boxes<T><<<blocks_for((int64_t)d.npatch * 32), kBlock, 0, s>>>(d.npatch, d.pxPtr, d.pxIdx, d.P, infl,
+    k_init_boxes<T, TC><<<blocks_for((int64_t)d.npatch * 32), kBlock, 0, s>>>(d.npatch, d.pxPtr, d.pxIdx, d.P, infl,
                                                                          d.PatchBox);
 }
 template <typename T, typename TC>
@@ -658,7 +658,7 @@ void launch_expand(const Dev<T, TC>& d, const int64_t* opt, const int64_t* oee, 
                                                           d.pePtr, d.peIdx, d.Faces, d.Edges, opt, oee, d.PT, d.EE);
 }
 template <typename T, typename TC>
-void launch_toi(const Dev<T, TC>& d, const V4<T>* X0, const V4<T>* X1, const SolverConsts& c, TC* per_pt,
+void launch_toi(const Dev<T, TC>& d, const V4<TC>* X0, const V4<TC>* X1, const SolverConsts& c, TC* per_pt,
                 TC* per_ee, cudaStream_t s) {
     constexpr bool kRel = sizeof(T) == 4 && sizeof(TC) == 8;
     if (d.nPT > 0)
@@ -671,10 +671,10 @@ void launch_toi(const Dev<T, TC>& d, const V4<T>* X0, const V4<T>* X1, const Sol
 }
 template <typename T, typename TC>
 void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s) {
-    k_toi_finalize<T, TC><<<1, 1, 0, s>>>(d.ToiMin, d.Toi, c.toi_scale);
+    k_toi_finalize<TC><<<1, 1, 0, s>>>(d.ToiMin, d.Toi, c.toi_scale);
 }
 template <typename T, typename TC>
-void launch_contact(const Dev<T, TC>& d, const V4<T>* X, const SolverConsts& c, cudaStream_t s) {
+void launch_contact(const Dev<T, TC>& d, const V4<TC>* X, const SolverConsts& c, cudaStream_t s) {
     cudaMemsetAsync(d.CollDiag, 0, sizeof(T) * d.ntot, s);
     cudaMemsetAsync(d.CollRhs, 0, sizeof(V4<T>) * d.ntot, s);
     cudaMemsetAsync(d.ActiveCount, 0, sizeof(unsigned long long), s);
@@ -694,7 +694,7 @@ void launch_contact(const Dev<T, TC>& d, const V4<T>* X, const SolverConsts& c, 
 }
 
 #define PDIPC_INST_COLL(T, TC)                                                                                \
-    template void launch_patch_boxes<T, TC>(const Dev<T, TC>&, const V4<T>*, const V4<T>*, T, cudaStream_t);  \
+    template void launch_patch_boxes<T, TC>(const Dev<T, TC>&, const V4<TC>*, const V4<TC>*, T, cudaStream_t);\
     template void launch_patch_init_boxes<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                         \
     template void launch_morton<T, TC>(const Dev<T, TC>&, T*, unsigned long long*, int*, cudaStream_t);     \
     template void launch_karras<T, TC>(const Dev<T, TC>&, const unsigned long long*, cudaStream_t);           \
@@ -702,10 +702,10 @@ void launch_contact(const Dev<T, TC>& d, const V4<T>* X, const SolverConsts& c, 
     template void launch_traverse<T, TC>(const Dev<T, TC>&, int*, const int*, int2*, cudaStream_t);           \
     template void launch_pair_counts<T, TC>(const Dev<T, TC>&, int64_t*, int64_t*, cudaStream_t);             \
     template void launch_expand<T, TC>(const Dev<T, TC>&, const int64_t*, const int64_t*, cudaStream_t);      \
-    template void launch_toi<T, TC>(const Dev<T, TC>&, const V4<T>*, const V4<T>*, const SolverConsts&, TC*,  \
+    template void launch_toi<T, TC>(const Dev<T, TC>&, const V4<TC>*, const V4<TC>*, const SolverConsts&, TC*,\
                                     TC*, cudaStream_t);                                                       \
     template void launch_toi_finalize<T, TC>(const Dev<T, TC>&, const SolverConsts&, cudaStream_t);           \
-    template void launch_contact<T, TC>(const Dev<T, TC>&, const V4<T>*, const SolverConsts&, cudaStream_t);
+    template void launch_contact<T, TC>(const Dev<T, TC>&, const V4<TC>*, const SolverConsts&, cudaStream_t);
 
 PDIPC_INST_COLL(float, float)
 PDIPC_INST_COLL(double, double)

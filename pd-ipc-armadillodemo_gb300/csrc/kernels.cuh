@@ -10,26 +10,29 @@
 namespace pdipc {
 
 // Device buffers of one context.  Vertex arrays use the global numbering
-// (cloth vertices first, then static ones).  T is the state/solver scalar,
-// TC the CCD/contact scalar.
+// (cloth vertices first, then static ones).  T is the solver scalar (local
+// step, sweeps), TC the scalar of the state (positions, velocities, step
+// direction, time of impact) and of CCD/contact: float/float reproduces the
+// reference's arithmetic, double/double is the plain FP64 form, float/double
+// the mixed form (FP32 arithmetic on FP64 state).
 template <typename T, typename TC>
 struct Dev {
     int nsim = 0, ntot = 0, nface = 0, nedge = 0, npatch = 0;
 
     // state
-    V4<T>* P = nullptr;      // positions [ntot]
-    V4<T>* Pold = nullptr;   // positions at the start of the outer iteration [ntot]
-    V4<T>* X0 = nullptr;     // positions at the start of the step [nsim]
-    V4<T>* Vel = nullptr;    // velocities [nsim]
-    V4<T>* Dir = nullptr;    // P - Pold before clamping [ntot]; static part stays 0
-    V4<T>* Xrest = nullptr;  // initial positions [ntot] (reset, pins)
+    V4<TC>* P = nullptr;      // positions [ntot]
+    V4<TC>* Pold = nullptr;   // positions at the start of the outer iteration [ntot]
+    V4<TC>* X0 = nullptr;     // positions at the start of the step [nsim]
+    V4<TC>* Vel = nullptr;    // velocities [nsim]
+    V4<TC>* Dir = nullptr;    // P - Pold before clamping [ntot]; static part stays 0
+    V4<TC>* Xrest = nullptr;  // initial positions [ntot] (reset, pins)
 
     // solver work
     V4<T>* Y = nullptr;      // first half of a two-sweep step [nsim]
     V4<T>* B = nullptr;      // odd Chebyshev iterates [nsim]
     V4<T>* Aq = nullptr;     // rescaled curvature vector per vertex [nsim]
     V4<T>* Rhs = nullptr;    // right-hand side of the current local-global iteration [nsim]
-    V4<T>* Rhs0 = nullptr;   // inertial right-hand side (m/dt^2) y [nsim]; the predicted y itself in
+    V4<TC>* Rhs0 = nullptr;  // inertial right-hand side (m/dt^2) y [nsim]; the predicted y itself in
                              // the correction (mixed) form
     V4<T>* C = nullptr;      // even correction iterates of the correction form [nsim]
     V4<T>* Grav = nullptr;   // (0, g m, 0) [nsim]
@@ -95,7 +98,7 @@ struct Dev {
 
     // scalars
     TC* ToiMin = nullptr;    // running min over candidates (reset to 1 after use)
-    T* Toi = nullptr;        // clamped step fraction of the outer iteration
+    TC* Toi = nullptr;       // clamped step fraction of the outer iteration
     double* ResidPart = nullptr;  // per-block partial sums of |dir|^2
     double* Resid = nullptr;      // |dir|^2
     unsigned int* ErrFlags = nullptr;
@@ -109,7 +112,7 @@ struct SolverConsts {
 
 // ---------------- PD kernels (pd_kernels.cu) ----------------
 template <typename T, typename TC>
-void launch_predict(const Dev<T, TC>& d, T dt, cudaStream_t s);
+void launch_predict(const Dev<T, TC>& d, TC dt, cudaStream_t s);
 template <typename T, typename TC>
 void launch_diag(const Dev<T, TC>& d, cudaStream_t s);
 template <typename T, typename TC>
@@ -117,17 +120,17 @@ void launch_local_aq(const Dev<T, TC>& d, cudaStream_t s);
 // local step right-hand side fused with the first J sweep (Y = S(P))
 template <typename T, typename TC>
 void launch_local_rhs_sweep(const Dev<T, TC>& d, T relax, cudaStream_t s);
-// out = S(src) or, with prev, out = omega (S(src) - prev) + prev
+// out = S(src) or, with prev, out = omega (S(src) - prev) + prev (T == TC only)
 template <typename T, typename TC>
 void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T>* out, T relax, T omega,
                   cudaStream_t s);
 // Correction (mixed-precision) form of one local-global iteration's pieces:
-// residual r0 = b - A x from relative coordinates (FP64 accumulation) into Rhs
+// residual r0 = b - A x from relative coordinates (compensated FP32 sums) into Rhs
 // and the first sweep from delta = 0 into Y.
 template <typename T, typename TC>
 void launch_local_residual(const Dev<T, TC>& d, T relax, cudaStream_t s);
-// sweep on the correction: mode 0 plain, 1 Chebyshev, 2 Chebyshev with a zero
-// previous iterate, 3 Chebyshev whose result is added to the positions P.
+// sweep on the correction: mode bits 1 Chebyshev, 2 the previous iterate is
+// zero, 4 the result is added to the positions P instead of written to out.
 template <typename T, typename TC>
 void launch_sweep_delta(const Dev<T, TC>& d, int mode, const V4<T>* src, const V4<T>* prev, V4<T>* out, T relax,
                         T omega, cudaStream_t s);
@@ -136,7 +139,7 @@ void launch_direction(const Dev<T, TC>& d, cudaStream_t s);
 template <typename T, typename TC>
 void launch_clamp(const Dev<T, TC>& d, cudaStream_t s);
 template <typename T, typename TC>
-void launch_velocity(const Dev<T, TC>& d, T invt, cudaStream_t s);
+void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s);
 template <typename T, typename TC>
 void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s);
 int direction_blocks(int nsim);
@@ -144,7 +147,7 @@ int direction_blocks(int nsim);
 // ---------------- collision kernels (collision_kernels.cu) ----------------
 // swept (Dir != null) or static patch boxes, inflated
 template <typename T, typename TC>
-void launch_patch_boxes(const Dev<T, TC>& d, const V4<T>* X, const V4<T>* D, T infl, cudaStream_t s);
+void launch_patch_boxes(const Dev<T, TC>& d, const V4<TC>* X, const V4<TC>* D, T infl, cudaStream_t s);
 // init-time boxes over every vertex of the patch (AipcBvhs input, cpp:1279-1292)
 template <typename T, typename TC>
 void launch_patch_init_boxes(const Dev<T, TC>& d, T infl, cudaStream_t s);
@@ -163,12 +166,12 @@ void launch_pair_counts(const Dev<T, TC>& d, int64_t* cnt_pt, int64_t* cnt_ee, c
 template <typename T, typename TC>
 void launch_expand(const Dev<T, TC>& d, const int64_t* off_pt, const int64_t* off_ee, cudaStream_t s);
 template <typename T, typename TC>
-void launch_toi(const Dev<T, TC>& d, const V4<T>* X0, const V4<T>* X1, const SolverConsts& c, TC* per_pt,
+void launch_toi(const Dev<T, TC>& d, const V4<TC>* X0, const V4<TC>* X1, const SolverConsts& c, TC* per_pt,
                 TC* per_ee, cudaStream_t s);
 template <typename T, typename TC>
 void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s);
 template <typename T, typename TC>
-void launch_contact(const Dev<T, TC>& d, const V4<T>* X, const SolverConsts& c, cudaStream_t s);
+void launch_contact(const Dev<T, TC>& d, const V4<TC>* X, const SolverConsts& c, cudaStream_t s);
 
 // ---------------- primitives (primitives.cu) ----------------
 // Exclusive scan of n int64 values (in may equal out); *total receives the sum.

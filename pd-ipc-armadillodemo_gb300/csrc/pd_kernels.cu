@@ -15,6 +15,7 @@
 // atomics) and the system matrix is streamed from SELL-32 slices so a warp's
 // column/value loads are contiguous 128-byte lines.
 #include <algorithm>
+#include <type_traits>
 
 #include "kernels.cuh"
 
@@ -26,9 +27,11 @@ constexpr int kBlock = 256;
 
 inline int blocks_for(int n, int b = kBlock) { return (n + b - 1) / b; }
 
-template <typename T, bool kDelta>
-__global__ void k_predict(int nsim, int ntot, T dt, V4<T>* __restrict__ P, V4<T>* __restrict__ Pold,
-                          V4<T>* __restrict__ X0, V4<T>* __restrict__ Vel, V4<T>* __restrict__ Rhs0,
+// S is the state scalar (== T except in the correction form, where the
+// prediction is formed in FP64 from the FP32 mass and gravity terms).
+template <typename T, typename S, bool kDelta>
+__global__ void k_predict(int nsim, int ntot, S dt, V4<S>* __restrict__ P, V4<S>* __restrict__ Pold,
+                          V4<S>* __restrict__ X0, V4<S>* __restrict__ Vel, V4<S>* __restrict__ Rhs0,
                           T* __restrict__ Dinert, const V4<T>* __restrict__ Grav, const T* __restrict__ InvMass,
                           const int* __restrict__ PinFlag, T* __restrict__ CollDiag, V4<T>* __restrict__ CollRhs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -36,25 +39,25 @@ __global__ void k_predict(int nsim, int ntot, T dt, V4<T>* __restrict__ P, V4<T>
     CollDiag[i] = T(0);
     CollRhs[i] = V4<T>{T(0), T(0), T(0), T(0)};
     if (i >= nsim) return;
-    const V4<T> x = P[i];
+    const V4<S> x = P[i];
     X0[i] = x;
     Pold[i] = x;
     if (PinFlag[i] != -1) {  // pinned: velocity zeroed, nothing else written
-        Vel[i] = V4<T>{T(0), T(0), T(0), T(0)};
+        Vel[i] = V4<S>{S(0), S(0), S(0), S(0)};
         return;
     }
     const T im = InvMass[i];
-    const T m = im * dt;
-    const V4<T> v = Vel[i];
+    const S m = (S)im * dt;
+    const V4<S> v = Vel[i];
     const V4<T> g = Grav[i];
-    T y0 = (v.x + m * g.x) * dt + x.x;
-    T y1 = (v.y + m * g.y) * dt + x.y;
-    T y2 = (v.z + m * g.z) * dt + x.z;
-    const T mm = T(1) / (dt * m);
-    Dinert[i] = T(1) / (im * dt * dt);
-    if (kDelta) Rhs0[i] = V4<T>{y0, y1, y2, T(0)};
-    else Rhs0[i] = V4<T>{mm * y0, mm * y1, mm * y2, T(0)};
-    P[i] = V4<T>{y0, y1, y2, T(0)};
+    S y0 = (v.x + m * (S)g.x) * dt + x.x;
+    S y1 = (v.y + m * (S)g.y) * dt + x.y;
+    S y2 = (v.z + m * (S)g.z) * dt + x.z;
+    const S mm = S(1) / (dt * m);
+    Dinert[i] = (T)(S(1) / ((S)im * dt * dt));
+    if (kDelta) Rhs0[i] = V4<S>{y0, y1, y2, S(0)};
+    else Rhs0[i] = V4<S>{mm * y0, mm * y1, mm * y2, S(0)};
+    P[i] = V4<S>{y0, y1, y2, S(0)};
 }
 
 template <typename T>
@@ -210,11 +213,12 @@ __global__ void __launch_bounds__(kBlock) k_sweep(int nsim, T relax, T omega, co
 // otherwise add a spurious pull toward the origin.  Every large term is formed
 // from a difference of nearby positions, so FP32 inputs lose nothing to
 // cancellation; the sum is accumulated with compensated (TwoSum) FP32 sums.  Then the first sweep from
-// delta = 0: Y = w r0 / D.
-template <typename T>
+// delta = 0: Y = w r0 / D.  Positions are FP64 (S): each difference is formed
+// exactly-rounded in FP64 and enters the FP32 arithmetic as one rounding.
+template <typename T, typename S>
 __global__ void __launch_bounds__(kBlock) k_local_residual(
-    int nsim, T relax, const V4<T>* __restrict__ P, const V4<T>* __restrict__ Pold, const V4<T>* __restrict__ Xrest,
-    const V4<T>* __restrict__ Ypred, const T* __restrict__ Dinert, const T* __restrict__ CollDiag,
+    int nsim, T relax, const V4<S>* __restrict__ P, const V4<S>* __restrict__ Pold, const V4<S>* __restrict__ Xrest,
+    const V4<S>* __restrict__ Ypred, const T* __restrict__ Dinert, const T* __restrict__ CollDiag,
     const V4<T>* __restrict__ CollRes, const int* __restrict__ PinFlag, const T* __restrict__ PinK,
     const int* __restrict__ lPtr, const int* __restrict__ lNbr, const T* __restrict__ lRest,
     const T* __restrict__ lBend, const T* __restrict__ lBendT, const T* __restrict__ Strain,
@@ -223,39 +227,39 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
     const T* __restrict__ sVal, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
-    const V4<T> x = ld4(P, i);
+    const V4<S> x = ld4(P, i);
     Sum2 r0, r1, r2;
     {   // inertia
-        const V4<T> y = ld4(Ypred, i);
+        const V4<S> y = ld4(Ypred, i);
         const T di = __ldg(Dinert + i);
-        r0.add(di * (y.x - x.x));
-        r1.add(di * (y.y - x.y));
-        r2.add(di * (y.z - x.z));
+        r0.add(di * (T)(y.x - x.x));
+        r1.add(di * (T)(y.y - x.y));
+        r2.add(di * (T)(y.z - x.z));
     }
     const int pf = __ldg(PinFlag + i);
     if (pf >= 0) {
-        const V4<T> xr = ld4(Xrest, i);
+        const V4<S> xr = ld4(Xrest, i);
         const T k = __ldg(PinK + pf);
-        r0.add(k * (xr.x - x.x));
-        r1.add(k * (xr.y - x.y));
-        r2.add(k * (xr.z - x.z));
+        r0.add(k * (T)(xr.x - x.x));
+        r1.add(k * (T)(xr.y - x.y));
+        r2.add(k * (T)(xr.z - x.z));
     }
     {   // contact projections taken at Pold
         const V4<T> c = ld4(CollRes, i);
-        const V4<T> xo = ld4(Pold, i);
+        const V4<S> xo = ld4(Pold, i);
         const T dc = __ldg(CollDiag + i);
         r0.add(c.x);
-        r0.add(dc * (xo.x - x.x));
+        r0.add(dc * (T)(xo.x - x.x));
         r1.add(c.y);
-        r1.add(dc * (xo.y - x.y));
+        r1.add(dc * (T)(xo.y - x.y));
         r2.add(c.z);
-        r2.add(dc * (xo.z - x.z));
+        r2.add(dc * (T)(xo.z - x.z));
     }
     const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
     const T strain = __ldg(Strain + i);
     for (int s = b + 1; s < e; ++s) {  // mass-spring projections
-        const V4<T> xj = ld4(P, __ldg(lNbr + s));
-        const T d0 = x.x - xj.x, d1 = x.y - xj.y, d2 = x.z - xj.z;
+        const V4<S> xj = ld4(P, __ldg(lNbr + s));
+        const T d0 = (T)(x.x - xj.x), d1 = (T)(x.y - xj.y), d2 = (T)(x.z - xj.z);
         const T cl = dsqrt(d0 * d0 + d1 * d1 + d2 * d2);
         const T rc = strain * (__ldg(lRest + s) / cl);
         r0.add(rc * d0);
@@ -284,10 +288,10 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
         for (int k = 0; k < len; ++k) {
             const int j = __ldg(sCol + base + 32 * k);
             const T v = __ldg(sVal + base + 32 * k);
-            const V4<T> xj = ld4(P, j);
-            r0.add(v * (xj.x - x.x));
-            r1.add(v * (xj.y - x.y));
-            r2.add(v * (xj.z - x.z));
+            const V4<S> xj = ld4(P, j);
+            r0.add(v * (T)(xj.x - x.x));
+            r1.add(v * (T)(xj.y - x.y));
+            r2.add(v * (T)(xj.z - x.z));
         }
     }
     const T f0 = r0.value(), f1 = r1.value(), f2 = r2.value();
@@ -298,10 +302,12 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
 
 // Sweep on the correction delta (rhs = residual r0).  kMode bits: 1 Chebyshev
 // step omega (S(src) - prev) + prev; 2 the previous iterate is zero (so the
-// step is omega S(src)); 4 the result is added to the positions (out = P).
-template <typename T, int kMode>
+// step is omega S(src)); 4 the result is added to the FP64 positions P
+// instead of written to out.
+template <typename T, typename S, int kMode>
 __global__ void __launch_bounds__(kBlock) k_sweep_delta(int nsim, T relax, T omega, const V4<T>* __restrict__ src,
                                                         const V4<T>* __restrict__ prev, V4<T>* __restrict__ out,
+                                                        V4<S>* __restrict__ P,
                                                         const V4<T>* __restrict__ Rhs, const T* __restrict__ InvD,
                                                         const int* __restrict__ sOff, const int* __restrict__ sLen,
                                                         const int* __restrict__ sCol, const T* __restrict__ sVal) {
@@ -329,8 +335,8 @@ __global__ void __launch_bounds__(kBlock) k_sweep_delta(int nsim, T relax, T ome
         }
     }
     if (kMode & 4) {
-        const V4<T> q = out[i];
-        out[i] = V4<T>{q.x + y0, q.y + y1, q.z + y2, T(0)};
+        const V4<S> q = P[i];
+        P[i] = V4<S>{q.x + (S)y0, q.y + (S)y1, q.z + (S)y2, S(0)};
     } else {
         out[i] = V4<T>{y0, y1, y2, T(0)};
     }
@@ -339,21 +345,21 @@ __global__ void __launch_bounds__(kBlock) k_sweep_delta(int nsim, T relax, T ome
 // Relative form of the curvature vector for the correction form:
 // aq = sum_{k>0} lbo_k (x_k - x_i), using that the LBO weights of a stencil sum
 // to zero.
-template <typename T>
-__global__ void k_local_aq_rel(int nsim, const V4<T>* __restrict__ P, const int* __restrict__ lPtr,
+template <typename T, typename S>
+__global__ void k_local_aq_rel(int nsim, const V4<S>* __restrict__ P, const int* __restrict__ lPtr,
                                const int* __restrict__ lNbr, const T* __restrict__ lLbo,
                                const T* __restrict__ CurvNorm, V4<T>* __restrict__ Aq) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
     const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
-    const V4<T> x = ld4(P, i);
+    const V4<S> x = ld4(P, i);
     T a0 = T(0), a1 = T(0), a2 = T(0);
     for (int s = b + 1; s < e; ++s) {
-        const V4<T> xj = ld4(P, __ldg(lNbr + s));
+        const V4<S> xj = ld4(P, __ldg(lNbr + s));
         const T l = __ldg(lLbo + s);
-        a0 += l * (xj.x - x.x);
-        a1 += l * (xj.y - x.y);
-        a2 += l * (xj.z - x.z);
+        a0 += l * (T)(xj.x - x.x);
+        a1 += l * (T)(xj.y - x.y);
+        a2 += l * (T)(xj.z - x.z);
     }
     const T nrm = dsqrt(a0 * a0 + a1 * a1 + a2 * a2);
     if (nrm >= T(1e-10)) {
@@ -365,7 +371,7 @@ __global__ void k_local_aq_rel(int nsim, const V4<T>* __restrict__ P, const int*
     Aq[i] = V4<T>{a0, a1, a2, T(0)};
 }
 
-template <typename T>
+template <typename T>  // T: the state scalar
 __global__ void k_direction(int nsim, const V4<T>* __restrict__ P, const V4<T>* __restrict__ Pold,
                             V4<T>* __restrict__ Dir, double* __restrict__ part) {
     __shared__ double red[kBlock / 32];
@@ -422,8 +428,8 @@ constexpr bool correction_form() {
 }
 
 template <typename T, typename TC>
-void launch_predict(const Dev<T, TC>& d, T dt, cudaStream_t s) {
-    k_predict<T, correction_form<T, TC>()><<<blocks_for(d.ntot), kBlock, 0, s>>>(
+void launch_predict(const Dev<T, TC>& d, TC dt, cudaStream_t s) {
+    k_predict<T, TC, correction_form<T, TC>()><<<blocks_for(d.ntot), kBlock, 0, s>>>(
         d.nsim, d.ntot, dt, d.P, d.Pold, d.X0, d.Vel, d.Rhs0, d.Dinert, d.Grav, d.InvMass, d.PinFlag, d.CollDiag,
         d.CollRhs);
 }
@@ -433,15 +439,15 @@ void launch_diag(const Dev<T, TC>& d, cudaStream_t s) {
 }
 template <typename T, typename TC>
 void launch_local_aq(const Dev<T, TC>& d, cudaStream_t s) {
-    if (correction_form<T, TC>())
-        k_local_aq_rel<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.lNbr, d.lLbo, d.CurvNorm,
-                                                                 d.Aq);
+    if constexpr (correction_form<T, TC>())
+        k_local_aq_rel<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.lNbr, d.lLbo,
+                                                                     d.CurvNorm, d.Aq);
     else
         k_local_aq<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.lNbr, d.lLbo, d.CurvNorm, d.Aq);
 }
 template <typename T, typename TC>
 void launch_local_residual(const Dev<T, TC>& d, T relax, cudaStream_t s) {
-    k_local_residual<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(
+    k_local_residual<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(
         d.nsim, relax, d.P, d.Pold, d.Xrest, d.Rhs0, d.Dinert, d.CollDiag, d.CollRhs, d.PinFlag, d.PinK, d.lPtr,
         d.lNbr, d.lRest, d.lBend, d.lBendT, d.Strain, d.Aq, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal, d.Rhs, d.Y);
 }
@@ -451,8 +457,8 @@ void launch_sweep_delta(const Dev<T, TC>& d, int mode, const V4<T>* src, const V
     const int nb = blocks_for(d.nsim);
 #define PDIPC_SWEEP_DELTA(M)                                                                                   \
     case M:                                                                                                    \
-        k_sweep_delta<T, M><<<nb, kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.Rhs, d.InvD, d.sOff, \
-                                                  d.sLen, d.sCol, d.sVal);                                     \
+        k_sweep_delta<T, TC, M><<<nb, kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.P, d.Rhs, d.InvD, \
+                                                      d.sOff, d.sLen, d.sCol, d.sVal);                         \
         break;
     switch (mode) {
         PDIPC_SWEEP_DELTA(0)
@@ -468,9 +474,10 @@ void launch_sweep_delta(const Dev<T, TC>& d, int mode, const V4<T>* src, const V
 }
 template <typename T, typename TC>
 void launch_local_rhs_sweep(const Dev<T, TC>& d, T relax, cudaStream_t s) {
-    k_local_rhs_sweep<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(
-        d.nsim, relax, d.P, d.lPtr, d.lNbr, d.lRest, d.lBend, d.lBendT, d.Strain, d.Aq, d.Rhs0, d.CollRhs,
-        d.PinRhs, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal, d.Rhs, d.Y);
+    if constexpr (std::is_same<T, TC>::value)
+        k_local_rhs_sweep<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(
+            d.nsim, relax, d.P, d.lPtr, d.lNbr, d.lRest, d.lBend, d.lBendT, d.Strain, d.Aq, d.Rhs0, d.CollRhs,
+            d.PinRhs, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal, d.Rhs, d.Y);
 }
 template <typename T, typename TC>
 void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T>* out, T relax, T omega,
@@ -485,24 +492,24 @@ void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T
 template <typename T, typename TC>
 void launch_direction(const Dev<T, TC>& d, cudaStream_t s) {
     const int nb = direction_blocks(d.nsim);
-    k_direction<T><<<nb, kBlock, 0, s>>>(d.nsim, d.P, d.Pold, d.Dir, d.ResidPart);
+    k_direction<TC><<<nb, kBlock, 0, s>>>(d.nsim, d.P, d.Pold, d.Dir, d.ResidPart);
     launch_reduce_sum_f64(d.ResidPart, nb, d.Resid, s);
 }
 template <typename T, typename TC>
 void launch_clamp(const Dev<T, TC>& d, cudaStream_t s) {
-    k_clamp<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Pold, d.Dir, d.Toi, d.P);
+    k_clamp<TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Pold, d.Dir, d.Toi, d.P);
 }
 template <typename T, typename TC>
 void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s) {
-    k_copy_old<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.Pold);
+    k_copy_old<TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.Pold);
 }
 template <typename T, typename TC>
-void launch_velocity(const Dev<T, TC>& d, T invt, cudaStream_t s) {
-    k_velocity<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, invt, d.P, d.X0, d.Vel, d.ErrFlags);
+void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {
+    k_velocity<TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, invt, d.P, d.X0, d.Vel, d.ErrFlags);
 }
 
 #define PDIPC_INST_PD(T, TC)                                                                                 \
-    template void launch_predict<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                                 \
+    template void launch_predict<T, TC>(const Dev<T, TC>&, TC, cudaStream_t);                                 \
     template void launch_diag<T, TC>(const Dev<T, TC>&, cudaStream_t);                                       \
     template void launch_local_aq<T, TC>(const Dev<T, TC>&, cudaStream_t);                                   \
     template void launch_local_rhs_sweep<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                         \
@@ -514,7 +521,7 @@ void launch_velocity(const Dev<T, TC>& d, T invt, cudaStream_t s) {
     template void launch_direction<T, TC>(const Dev<T, TC>&, cudaStream_t);                                  \
     template void launch_clamp<T, TC>(const Dev<T, TC>&, cudaStream_t);                                      \
     template void launch_copy_old<T, TC>(const Dev<T, TC>&, cudaStream_t);                                   \
-    template void launch_velocity<T, TC>(const Dev<T, TC>&, T, cudaStream_t);
+    template void launch_velocity<T, TC>(const Dev<T, TC>&, TC, cudaStream_t);
 
 PDIPC_INST_PD(float, float)
 PDIPC_INST_PD(double, double)

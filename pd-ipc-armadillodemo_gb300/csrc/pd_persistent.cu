@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <type_traits>
 
 #include "kernels.cuh"
 #include "persistent.h"
@@ -75,27 +76,44 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* err, unsig
     return ok_s != 0;
 }
 
-template <typename T>
-__device__ __forceinline__ V4<T> ldcg4(const V4<T>* p, int i) {
+__device__ __forceinline__ V4<float> ldcg4(const V4<float>* p, int i) {
     const float4 v = __ldcg(reinterpret_cast<const float4*>(p) + i);
-    return V4<T>{v.x, v.y, v.z, v.w};
+    return V4<float>{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ V4<double> ldcg4(const V4<double>* p, int i) {
+    const double2* q = reinterpret_cast<const double2*>(p) + 2 * (size_t)i;
+    const double2 a = __ldcg(q), b = __ldcg(q + 1);
+    return V4<double>{a.x, a.y, b.x, b.y};
 }
 // Coherent load that may hit in L1: data written by other CTAs before a grid
 // barrier is visible after it, because the barrier's gpu-scope acquire
 // invalidates this SM's L1 (PTX memory model: release -> acquire -> bar.sync).
-template <typename T>
-__device__ __forceinline__ V4<T> ldl14(const V4<T>* p, int i) {
+__device__ __forceinline__ V4<float> ldl14(const V4<float>* p, int i) {
     const float4 v = *(reinterpret_cast<const float4*>(p) + i);
-    return V4<T>{v.x, v.y, v.z, v.w};
+    return V4<float>{v.x, v.y, v.z, v.w};
 }
-template <typename T>
-__device__ __forceinline__ void stcg4(V4<T>* p, int i, T x, T y, T z) {
+__device__ __forceinline__ V4<double> ldl14(const V4<double>* p, int i) {
+    const double2* q = reinterpret_cast<const double2*>(p) + 2 * (size_t)i;
+    const double2 a = q[0], b = q[1];
+    return V4<double>{a.x, a.y, b.x, b.y};
+}
+template <bool kL1, typename X>
+__device__ __forceinline__ V4<X> ldv(const V4<X>* p, int i) {
+    return kL1 ? ldl14(p, i) : ldcg4(p, i);
+}
+__device__ __forceinline__ void stcg4(V4<float>* p, int i, float x, float y, float z) {
     __stcg(reinterpret_cast<float4*>(p) + i, make_float4(x, y, z, 0.f));
 }
+__device__ __forceinline__ void stcg4(V4<double>* p, int i, double x, double y, double z) {
+    double2* q = reinterpret_cast<double2*>(p) + 2 * (size_t)i;
+    __stcg(q, make_double2(x, y));
+    __stcg(q + 1, make_double2(z, 0.0));
+}
 
-template <typename T, bool kCorr, bool kSmem, bool kL1, int R>
-__global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
-    auto ldv = [](const V4<T>* p, int i) { return kL1 ? ldl14(p, i) : ldcg4(p, i); };
+// S is the state scalar: T in the direct form, double in the correction form,
+// where positions enter the FP32 arithmetic only as rounded FP64 differences.
+template <typename T, typename S, bool kCorr, bool kSmem, bool kL1, int R>
+__global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int cta = blockIdx.x;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -150,7 +168,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
             T v;
             int j;
             entry(r, k, v, j);
-            const V4<T> xj = ldv(src, j);
+            const V4<T> xj = ldv<kL1>(src, j);
             s0 += v * xj.x;
             s1 += v * xj.y;
             s2 += v * xj.z;
@@ -164,16 +182,16 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
             if (!val[r]) continue;
             const int i = row[r];
             const int b = a.lPtr[i], e = a.lPtr[i + 1];
-            const V4<T> x = ldv(a.P, i);
+            const V4<S> x = ldv<kL1>(a.P, i);
             T a0, a1, a2;
-            if (kCorr) {
+            if constexpr (kCorr) {
                 a0 = a1 = a2 = T(0);
                 for (int s = b + 1; s < e; ++s) {
-                    const V4<T> xj = ldv(a.P, a.lNbr[s]);
+                    const V4<S> xj = ldv<kL1>(a.P, a.lNbr[s]);
                     const T l = a.lLbo[s];
-                    a0 += l * (xj.x - x.x);
-                    a1 += l * (xj.y - x.y);
-                    a2 += l * (xj.z - x.z);
+                    a0 += l * (T)(xj.x - x.x);
+                    a1 += l * (T)(xj.y - x.y);
+                    a2 += l * (T)(xj.z - x.z);
                 }
             } else {
                 const T l0 = a.lLbo[b];
@@ -181,7 +199,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
                 a1 = x.y * l0;
                 a2 = x.z * l0;
                 for (int s = b + 1; s < e; ++s) {
-                    const V4<T> xj = ldv(a.P, a.lNbr[s]);
+                    const V4<T> xj = ldv<kL1>(a.P, a.lNbr[s]);
                     const T l = a.lLbo[s];
                     a0 += xj.x * l;
                     a1 += xj.y * l;
@@ -208,55 +226,52 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
             if (!val[r]) continue;
             const int i = row[r];
             const int b = a.lPtr[i], e = a.lPtr[i + 1];
-            const V4<T> x = ldv(a.P, i);
-            x0[r][0] = x.x;
-            x0[r][1] = x.y;
-            x0[r][2] = x.z;
+            const V4<S> x = ldv<kL1>(a.P, i);
             const T strain = a.Strain[i];
-            if (kCorr) {
+            if constexpr (kCorr) {
                 Sum2 r0, r1, r2;
                 {
-                    const V4<T> y = ldcg4(a.Rhs0, i);
+                    const V4<S> y = ldcg4(a.Rhs0, i);
                     const T di = a.Dinert[i];
-                    r0.add(di * (y.x - x.x));
-                    r1.add(di * (y.y - x.y));
-                    r2.add(di * (y.z - x.z));
+                    r0.add(di * (T)(y.x - x.x));
+                    r1.add(di * (T)(y.y - x.y));
+                    r2.add(di * (T)(y.z - x.z));
                 }
                 const int pf = a.PinFlag[i];
                 if (pf >= 0) {
-                    const V4<T> xr = ldcg4(a.Xrest, i);
+                    const V4<S> xr = ldcg4(a.Xrest, i);
                     const T k = a.PinK[pf];
-                    r0.add(k * (xr.x - x.x));
-                    r1.add(k * (xr.y - x.y));
-                    r2.add(k * (xr.z - x.z));
+                    r0.add(k * (T)(xr.x - x.x));
+                    r1.add(k * (T)(xr.y - x.y));
+                    r2.add(k * (T)(xr.z - x.z));
                 }
                 {
                     const V4<T> c = ldcg4(a.CollRhs, i);
-                    const V4<T> xo = ldcg4(a.Pold, i);
+                    const V4<S> xo = ldcg4(a.Pold, i);
                     const T dc = a.CollDiag[i];
                     r0.add(c.x);
-                    r0.add(dc * (xo.x - x.x));
+                    r0.add(dc * (T)(xo.x - x.x));
                     r1.add(c.y);
-                    r1.add(dc * (xo.y - x.y));
+                    r1.add(dc * (T)(xo.y - x.y));
                     r2.add(c.z);
-                    r2.add(dc * (xo.z - x.z));
+                    r2.add(dc * (T)(xo.z - x.z));
                 }
                 for (int s = b + 1; s < e; ++s) {
-                    const V4<T> xj = ldv(a.P, a.lNbr[s]);
-                    const T d0 = x.x - xj.x, d1 = x.y - xj.y, d2 = x.z - xj.z;
+                    const V4<S> xj = ldv<kL1>(a.P, a.lNbr[s]);
+                    const T d0 = (T)(x.x - xj.x), d1 = (T)(x.y - xj.y), d2 = (T)(x.z - xj.z);
                     const T cl = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
                     const T rc = strain * (a.lRest[s] / cl);
                     r0.add(rc * d0);
                     r1.add(rc * d1);
                     r2.add(rc * d2);
                 }
-                const V4<T> ai = ldv(a.Aq, i);
+                const V4<T> ai = ldv<kL1>(a.Aq, i);
                 const T b0 = a.lBend[b];
                 r0.add(b0 * ai.x);
                 r1.add(b0 * ai.y);
                 r2.add(b0 * ai.z);
                 for (int s = b + 1; s < e; ++s) {
-                    const V4<T> ak = ldv(a.Aq, a.lNbr[s]);
+                    const V4<T> ak = ldv<kL1>(a.Aq, a.lNbr[s]);
                     const T bt = a.lBendT[s];
                     r0.add(bt * ak.x);
                     r1.add(bt * ak.y);
@@ -266,18 +281,21 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
                     T v;
                     int j;
                     entry(r, k, v, j);
-                    const V4<T> xj = ldv(a.P, j);
-                    r0.add(v * (xj.x - x.x));
-                    r1.add(v * (xj.y - x.y));
-                    r2.add(v * (xj.z - x.z));
+                    const V4<S> xj = ldv<kL1>(a.P, j);
+                    r0.add(v * (T)(xj.x - x.x));
+                    r1.add(v * (T)(xj.y - x.y));
+                    r2.add(v * (T)(xj.z - x.z));
                 }
                 rh[r][0] = r0.value();
                 rh[r][1] = r1.value();
                 rh[r][2] = r2.value();
             } else {
+                x0[r][0] = x.x;
+                x0[r][1] = x.y;
+                x0[r][2] = x.z;
                 T t0 = T(0), t1 = T(0), t2 = T(0);
                 for (int s = b + 1; s < e; ++s) {
-                    const V4<T> xj = ldv(a.P, a.lNbr[s]);
+                    const V4<T> xj = ldv<kL1>(a.P, a.lNbr[s]);
                     const T d0 = x.x - xj.x, d1 = x.y - xj.y, d2 = x.z - xj.z;
                     const T cl = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
                     const T rc = strain * (a.lRest[s] / cl);
@@ -285,7 +303,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
                     t1 += rc * d1;
                     t2 += rc * d2;
                 }
-                const V4<T> ai = ldv(a.Aq, i);
+                const V4<T> ai = ldv<kL1>(a.Aq, i);
                 const T b0 = a.lBend[b];
                 t0 += b0 * ai.x;
                 t1 += b0 * ai.y;
@@ -293,7 +311,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
                 const V4<T> q0 = ldcg4(a.Rhs0, i);
                 T u0 = q0.x + t0, u1 = q0.y + t1, u2 = q0.z + t2;
                 for (int s = b + 1; s < e; ++s) {
-                    const V4<T> ak = ldv(a.Aq, a.lNbr[s]);
+                    const V4<T> ak = ldv<kL1>(a.Aq, a.lNbr[s]);
                     const T bt = a.lBendT[s];
                     u0 += bt * ak.x;
                     u1 += bt * ak.y;
@@ -315,13 +333,13 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
 
         // ---- Chebyshev-accelerated R2 iteration as two J sweeps per step ----
         // direct form: iterate on x from x0 (gathered from P);
-        // correction form: iterate on delta from 0, add to x0 at the end.
+        // correction form: iterate on delta from 0, add it to P at the end.
         T cx[R][3], px[R][3], yv[R][3];
         // first sweep: Y = S(x0)
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             T s0 = T(0), s1 = T(0), s2 = T(0);
-            if (kCorr) {
+            if constexpr (kCorr) {
                 cx[r][0] = cx[r][1] = cx[r][2] = T(0);
             } else {
                 cx[r][0] = x0[r][0];
@@ -360,8 +378,12 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
                 cx[r][2] = n2;
                 if (!val[r]) continue;
                 if (last) {
-                    if (kCorr) stcg4(a.P, row[r], x0[r][0] + n0, x0[r][1] + n1, x0[r][2] + n2);
-                    else stcg4(a.P, row[r], n0, n1, n2);
+                    if constexpr (kCorr) {  // only this thread writes the row: its own earlier read is current
+                        const V4<S> x = ldcg4(a.P, row[r]);
+                        stcg4(a.P, row[r], x.x + (S)n0, x.y + (S)n1, x.z + (S)n2);
+                    } else {
+                        stcg4(a.P, row[r], n0, n1, n2);
+                    }
                 } else {
                     stcg4(a.GX, row[r], n0, n1, n2);
                 }
@@ -385,11 +407,12 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T> a) {
 
 template <typename T, bool kCorr, bool kSmem, bool kL1>
 const void* kernel_for(int R) {
+    using S = typename std::conditional<kCorr, double, T>::type;
     switch (R) {
-        case 1: return (const void*)k_pd_persistent<T, kCorr, kSmem, kL1, 1>;
-        case 2: return (const void*)k_pd_persistent<T, kCorr, kSmem, kL1, 2>;
-        case 3: return (const void*)k_pd_persistent<T, kCorr, kSmem, kL1, 3>;
-        default: return (const void*)k_pd_persistent<T, kCorr, kSmem, kL1, 4>;
+        case 1: return (const void*)k_pd_persistent<T, S, kCorr, kSmem, kL1, 1>;
+        case 2: return (const void*)k_pd_persistent<T, S, kCorr, kSmem, kL1, 2>;
+        case 3: return (const void*)k_pd_persistent<T, S, kCorr, kSmem, kL1, 3>;
+        default: return (const void*)k_pd_persistent<T, S, kCorr, kSmem, kL1, 4>;
     }
 }
 
@@ -407,11 +430,19 @@ const void* persistent_kernel(bool correction, bool matrix_in_smem, bool l1_gath
                      : kernel_for_l1<false>(correction, matrix_in_smem, rows_per_thread);
 }
 
-cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float>& args, bool correction,
-                                 cudaStream_t s) {
+template <typename S>
+cudaError_t launch_args(const PersistPlan& plan, const PersistArgs<float, S>& args, cudaStream_t s) {
+    const bool correction = std::is_same<S, double>::value;
     const void* f = persistent_kernel(correction, plan.matrix_in_smem, plan.l1_gather, plan.rows_per_thread);
     void* params[] = {(void*)&args};
     return cudaLaunchCooperativeKernel(f, dim3(plan.ctas), dim3(plan.threads), params, plan.smem_bytes, s);
+}
+
+cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, float>& args, cudaStream_t s) {
+    return launch_args(plan, args, s);
+}
+cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, double>& args, cudaStream_t s) {
+    return launch_args(plan, args, s);
 }
 
 }  // namespace pdipc

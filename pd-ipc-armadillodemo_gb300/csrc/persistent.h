@@ -25,7 +25,9 @@ struct PersistPlan {
     int pattern_width = 0;
 };
 
-template <typename T>
+// T: solver scalar; S: state scalar (T in the direct form, double in the
+// correction form).
+template <typename T, typename S>
 struct PersistArgs {
     int nsim;
     int lg;
@@ -34,10 +36,10 @@ struct PersistArgs {
     T omega[kMaxCheby];  // omega[it] of Chebyshev step it (it >= 1)
     long long timeout;   // barrier wait limit in clock cycles
     // state
-    V4<T>* P;
-    const V4<T>* Pold;
-    const V4<T>* Xrest;
-    const V4<T>* Rhs0;
+    V4<S>* P;
+    const V4<S>* Pold;
+    const V4<S>* Xrest;
+    const V4<S>* Rhs0;
     const V4<T>* CollRhs;
     const V4<T>* PinRhs;
     V4<T>* Aq;
@@ -74,7 +76,8 @@ struct PersistArgs {
 };
 
 const void* persistent_kernel(bool correction, bool matrix_in_smem, bool l1_gather, int rows_per_thread);
-cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float>& args, bool correction,
-                                 cudaStream_t s);
+// direct form (FP32 state) and correction form (FP64 state)
+cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, float>& args, cudaStream_t s);
+cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, double>& args, cudaStream_t s);
 
 }  // namespace pdipc

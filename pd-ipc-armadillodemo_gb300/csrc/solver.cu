@@ -89,6 +89,8 @@ public:
         PD_CK(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
         PD_CK(cudaEventCreate(&ev0_));
         PD_CK(cudaEventCreate(&ev1_));
+        PD_CK(cudaEventCreate(&evp0_));
+        PD_CK(cudaEventCreate(&evp1_));
         Dev<T, TC>& d = d_;
         d.nsim = H.nsim;
         d.ntot = H.ntot;
@@ -98,8 +100,8 @@ public:
         const int ns = d.nsim, nt = d.ntot;
 
         // ---- vertex state ----
-        std::vector<V4<T>> X(nt);
-        for (int i = 0; i < nt; ++i) X[i] = V4<T>{(T)H.X[3 * i], (T)H.X[3 * i + 1], (T)H.X[3 * i + 2], T(0)};
+        std::vector<V4<TC>> X(nt);
+        for (int i = 0; i < nt; ++i) X[i] = V4<TC>{(TC)H.X[3 * i], (TC)H.X[3 * i + 1], (TC)H.X[3 * i + 2], TC(0)};
         PD_CK(up(d.P, X));
         PD_CK(up(d.Xrest, X));
         PD_CK(up(d.Pold, X));
@@ -129,7 +131,7 @@ public:
             pinf[i] = H.pinSlot[i];
             if (H.pinSlot[i] >= 0) {
                 const T k = (T)H.pinK[H.pinSlot[i]];
-                pinr[i] = V4<T>{k * X[i].x, k * X[i].y, k * X[i].z, T(0)};
+                pinr[i] = V4<T>{k * (T)X[i].x, k * (T)X[i].y, k * (T)X[i].z, T(0)};
             } else {
                 pinr[i] = V4<T>{T(0), T(0), T(0), T(0)};
             }
@@ -182,6 +184,18 @@ public:
                 }
             }
         sell_entries_ = (int64_t)H.nPtr[ns];
+        {   // algorithmic bytes of one PD solve (the stats field pd_solve_bytes)
+            const double V = sizeof(T);
+            double b = 0.0;
+            for (int i = 0; i < ns; ++i) {
+                const double d1 = H.lPtr[i + 1] - H.lPtr[i];  // self + stencil neighbours
+                const double n = H.nPtr[i + 1] - H.nPtr[i];   // matrix off-diagonals
+                const double local = d1 * (4.0 + 3.0 * V) + 2.0 * V + 8.0 + 9.0 * V;
+                const double sweep = n * (4.0 + V) + 7.0 * V;
+                b += local + 2.0 * c_.cheby * sweep + (c_.cheby - 1) * 3.0 * V;
+            }
+            pd_bytes_ = b * c_.lg;
+        }
         sell_padded_ = (int64_t)soff[d.nslice];
         PD_CK(up(d.sOff, soff));
         PD_CK(up(d.sLen, slen));
@@ -228,7 +242,7 @@ public:
         PD_CK(zeros(d.ActiveCount, 1));
         PD_CK(cudaMallocHost(&pin_, sizeof(Pinned)));
         std::memset(pin_, 0, sizeof(Pinned));
-        PD_CK(cudaMallocHost(&stage_, sizeof(V4<T>) * (size_t)std::max(nt, 1)));
+        PD_CK(cudaMallocHost(&stage_, sizeof(V4<TC>) * (size_t)std::max(nt, 1)));
 
         // ---- persistent PD solve plan (needs every buffer above) ----
         pdipc_status pr = plan_persistent(H, sliceOffH_, sliceLenH_, err);
@@ -253,6 +267,8 @@ public:
         }
         launches_ = 0;
         device_ms_ = 0.0;
+        pd_ms_ = 0.0;
+        pd_solves_ = 0;
         st_.max_outer_iters = 0;
         st_.total_outer_iters = 0;
         for (int k = 0; k < n; ++k) {
@@ -269,7 +285,7 @@ public:
     }
 
     pdipc_status get_positions(double* out, std::string& err) override {
-        PD_CK(cudaMemcpyAsync(stage_, d_.P, sizeof(V4<T>) * d_.ntot, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaMemcpyAsync(stage_, d_.P, sizeof(V4<TC>) * d_.ntot, cudaMemcpyDeviceToHost, s_));
         PD_CK(cudaStreamSynchronize(s_));
         for (int i = 0; i < d_.ntot; ++i) {
             out[3 * (size_t)i] = (double)stage_[i].x;
@@ -279,7 +295,7 @@ public:
         return PDIPC_OK;
     }
     pdipc_status get_velocities(double* out, std::string& err) override {
-        PD_CK(cudaMemcpyAsync(stage_, d_.Vel, sizeof(V4<T>) * d_.nsim, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaMemcpyAsync(stage_, d_.Vel, sizeof(V4<TC>) * d_.nsim, cudaMemcpyDeviceToHost, s_));
         PD_CK(cudaStreamSynchronize(s_));
         for (int i = 0; i < d_.nsim; ++i) {
             out[3 * (size_t)i] = (double)stage_[i].x;
@@ -288,11 +304,11 @@ public:
         }
         return PDIPC_OK;
     }
-    pdipc_status upload_vec(V4<T>* dst, const double* src, int n, std::string& err) {
+    pdipc_status upload_vec(V4<TC>* dst, const double* src, int n, std::string& err) {
         PD_CK(cudaStreamSynchronize(s_));
         for (int i = 0; i < n; ++i)
-            stage_[i] = V4<T>{(T)src[3 * (size_t)i], (T)src[3 * (size_t)i + 1], (T)src[3 * (size_t)i + 2], T(0)};
-        PD_CK(cudaMemcpyAsync(dst, stage_, sizeof(V4<T>) * n, cudaMemcpyHostToDevice, s_));
+            stage_[i] = V4<TC>{(TC)src[3 * (size_t)i], (TC)src[3 * (size_t)i + 1], (TC)src[3 * (size_t)i + 2], TC(0)};
+        PD_CK(cudaMemcpyAsync(dst, stage_, sizeof(V4<TC>) * n, cudaMemcpyHostToDevice, s_));
         PD_CK(cudaStreamSynchronize(s_));
         return PDIPC_OK;
     }
@@ -303,8 +319,8 @@ public:
         return PDIPC_OK;
     }
     pdipc_status reset(std::string& err) override {
-        PD_CK(cudaMemcpyAsync(d_.P, d_.Xrest, sizeof(V4<T>) * d_.ntot, cudaMemcpyDeviceToDevice, s_));
-        PD_CK(cudaMemsetAsync(d_.Vel, 0, sizeof(V4<T>) * d_.nsim, s_));
+        PD_CK(cudaMemcpyAsync(d_.P, d_.Xrest, sizeof(V4<TC>) * d_.ntot, cudaMemcpyDeviceToDevice, s_));
+        PD_CK(cudaMemsetAsync(d_.Vel, 0, sizeof(V4<TC>) * d_.nsim, s_));
         PD_CK(cudaStreamSynchronize(s_));
         st_.steps_done = 0;
         return PDIPC_OK;
@@ -320,6 +336,9 @@ public:
         s->device_ms = device_ms_;
         s->pd_path = plan_.enabled ? (plan_.matrix_in_smem ? 2 : 1) : 0;
         s->pd_ctas = plan_.enabled ? plan_.ctas : 0;
+        s->pd_solves = pd_solves_;
+        s->pd_solve_ms = pd_ms_;
+        s->pd_solve_bytes = pd_bytes_;
     }
 
     // ---------------- stages ----------------
@@ -330,7 +349,7 @@ public:
         if (r == PDIPC_OK) r = upload_vec(d_.Dir, dx, d_.ntot, err);
         if (r == PDIPC_OK) r = broadphase(err);
         if (r != PDIPC_OK) return r;
-        PD_CK(cudaMemsetAsync(d_.Dir, 0, sizeof(V4<T>) * d_.ntot, s_));
+        PD_CK(cudaMemsetAsync(d_.Dir, 0, sizeof(V4<TC>) * d_.ntot, s_));
         *n_pairs = d_.nPairs;
         *n_pt = d_.nPT;
         *n_ee = d_.nEE;
@@ -362,8 +381,8 @@ public:
         if (d_.nEE) PD_CK(cudaMalloc(&pee, sizeof(TC) * d_.nEE));
         launch_toi(d_, d_.Pold, scratch_, c_, ppt, pee, s_);
         launch_toi_finalize(d_, c_, s_);
-        T toi;
-        PD_CK(cudaMemcpyAsync(&toi, d_.Toi, sizeof(T), cudaMemcpyDeviceToHost, s_));
+        TC toi;
+        PD_CK(cudaMemcpyAsync(&toi, d_.Toi, sizeof(TC), cudaMemcpyDeviceToHost, s_));
         std::vector<TC> hp(d_.nPT), he(d_.nEE);
         if (d_.nPT) PD_CK(cudaMemcpyAsync(hp.data(), ppt, sizeof(TC) * d_.nPT, cudaMemcpyDeviceToHost, s_));
         if (d_.nEE) PD_CK(cudaMemcpyAsync(he.data(), pee, sizeof(TC) * d_.nEE, cudaMemcpyDeviceToHost, s_));
@@ -381,17 +400,18 @@ public:
         if (r != PDIPC_OK) return r;
         launch_contact(d_, scratch_, c_, s_);
         std::vector<T> hd(d_.ntot);
+        std::vector<V4<T>> hr(d_.ntot);
         PD_CK(cudaMemcpyAsync(hd.data(), d_.CollDiag, sizeof(T) * d_.ntot, cudaMemcpyDeviceToHost, s_));
-        PD_CK(cudaMemcpyAsync(stage_, d_.CollRhs, sizeof(V4<T>) * d_.ntot, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaMemcpyAsync(hr.data(), d_.CollRhs, sizeof(V4<T>) * d_.ntot, cudaMemcpyDeviceToHost, s_));
         PD_CK(cudaMemcpyAsync(&pin_->active, d_.ActiveCount, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s_));
         PD_CK(cudaStreamSynchronize(s_));
         for (int i = 0; i < d_.ntot; ++i) {
             diag[i] = (double)hd[i];
-            rhs[3 * (size_t)i] = (double)stage_[i].x;
-            rhs[3 * (size_t)i + 1] = (double)stage_[i].y;
-            rhs[3 * (size_t)i + 2] = (double)stage_[i].z;
+            rhs[3 * (size_t)i] = (double)hr[i].x;
+            rhs[3 * (size_t)i + 1] = (double)hr[i].y;
+            rhs[3 * (size_t)i + 2] = (double)hr[i].z;
             if (kCorrection)  // the correction form accumulates w (target - x); report sum w target
-                for (int k = 0; k < 3; ++k) rhs[3 * (size_t)i + k] += diag[i] * (double)(T)x[3 * (size_t)i + k];
+                for (int k = 0; k < 3; ++k) rhs[3 * (size_t)i + k] += diag[i] * (double)(TC)x[3 * (size_t)i + k];
         }
         if (n_active) *n_active = (int64_t)pin_->active;
         PD_CK(cudaMemsetAsync(d_.CollDiag, 0, sizeof(T) * d_.ntot, s_));
@@ -405,7 +425,7 @@ public:
         if (r == PDIPC_OK) r = get_velocities(saveV.data(), err);
         if (r == PDIPC_OK) r = set_state(X, V, err);
         if (r != PDIPC_OK) return r;
-        launch_predict(d_, (T)c_.dt, s_);
+        launch_predict(d_, (TC)c_.dt, s_);
         if (plan_.enabled) PD_CK(launch_persistent());
         else enqueue_pd();
         r = get_positions(out, err);
@@ -414,11 +434,16 @@ public:
     }
 
     pdipc_status sweep_timing(int launches, double* avg_ms, double* bytes, std::string& err) override {
+        // one plain sweep of the solve's own kind (on the correction in the mixed form)
         const T w = (T)c_.relax;
+        auto sweep = [&]() {
+            if (kCorrection) launch_sweep_delta<T, TC>(d_, 0, d_.Y, nullptr, d_.B, w, T(0), s_);
+            else launch_sweep<T, TC>(d_, d_.Y, nullptr, d_.B, w, T(0), s_);
+        };
         launch_diag(d_, s_);
-        launch_sweep<T, TC>(d_, d_.P, nullptr, d_.Y, w, T(0), s_);  // warm
+        sweep();  // warm
         PD_CK(cudaEventRecord(ev0_, s_));
-        for (int k = 0; k < launches; ++k) launch_sweep<T, TC>(d_, d_.P, nullptr, d_.Y, w, T(0), s_);
+        for (int k = 0; k < launches; ++k) sweep();
         PD_CK(cudaEventRecord(ev1_, s_));
         PD_CK(cudaEventSynchronize(ev1_));
         float ms = 0.f;
@@ -492,7 +517,9 @@ private:
         stage_ = nullptr;
         if (ev0_) cudaEventDestroy(ev0_);
         if (ev1_) cudaEventDestroy(ev1_);
-        ev0_ = ev1_ = nullptr;
+        if (evp0_) cudaEventDestroy(evp0_);
+        if (evp1_) cudaEventDestroy(evp1_);
+        ev0_ = ev1_ = evp0_ = evp1_ = nullptr;
         if (s_) cudaStreamDestroy(s_);
         s_ = nullptr;
     }
@@ -586,7 +613,7 @@ private:
         PD_CK(up(pPatOff_, patOff));
         PD_CK(zeros(pBar_, 2));
         if constexpr (std::is_same<T, float>::value) {
-            PersistArgs<float>& a = pargs_;
+            PersistArgs<float, TC>& a = pargs_;
             a.nsim = ns;
             a.lg = c_.lg;
             a.cheby = c_.cheby;
@@ -649,7 +676,7 @@ private:
     }
 
     cudaError_t launch_persistent() {
-        if constexpr (std::is_same<T, float>::value) return launch_pd_persistent(plan_, pargs_, kCorrection, s_);
+        if constexpr (std::is_same<T, float>::value) return launch_pd_persistent(plan_, pargs_, s_);
         return cudaErrorNotSupported;
     }
 
@@ -771,7 +798,7 @@ private:
         for (int lg = 0; lg < c_.lg; ++lg) {
             launch_local_aq(d, s_);
             launch_local_residual(d, w, s_);
-            launch_sweep_delta<T, TC>(d, c_.cheby == 1 ? 4 : 0, d.Y, nullptr, c_.cheby == 1 ? d.P : d.B, w, T(0), s_);
+            launch_sweep_delta<T, TC>(d, c_.cheby == 1 ? 4 : 0, d.Y, nullptr, d.B, w, T(0), s_);
             k += 3;
             T om = omega_first(rho2);
             for (int it = 1; it < c_.cheby; ++it) {
@@ -780,7 +807,7 @@ private:
                 const bool last = it == c_.cheby - 1;
                 const int mode = 1 | (it == 1 ? 2 : 0) | (last ? 4 : 0);
                 launch_sweep_delta<T, TC>(d, 0, cur, nullptr, d.Y, w, T(0), s_);
-                launch_sweep_delta<T, TC>(d, mode, d.Y, prv, last ? d.P : prv, w, om, s_);
+                launch_sweep_delta<T, TC>(d, mode, d.Y, prv, prv, w, om, s_);  // mode 4: into P
                 k += 2;
                 om = omega_next(rho2, om);
             }
@@ -789,7 +816,9 @@ private:
     }
 
     int enqueue_pd() {
-        if (kCorrection) return enqueue_pd_correction();
+        if constexpr (kCorrection) {
+            return enqueue_pd_correction();
+        } else {
         Dev<T, TC>& d = d_;
         const T w = (T)c_.relax;
         T rho2 = (T)c_.rho;
@@ -814,6 +843,7 @@ private:
             }
         }
         return k;
+        }
     }
 
     pdipc_status pd_solve(std::string& err) {
@@ -840,14 +870,16 @@ private:
     // PdIpcSimulator::advance (cpp:1683-1796)
     pdipc_status step_once(std::string& err) {
         Dev<T, TC>& d = d_;
-        const T dt = (T)c_.dt;
+        const TC dt = (TC)c_.dt;
         launch_predict(d, dt, s_);
         ++launches_;
         const int max_outer = prm_.fixed_outer > 0 ? prm_.fixed_outer : prm_.max_outer;
         int outer = 0;
         for (; outer < max_outer; ++outer) {
+            PD_CK(cudaEventRecord(evp0_, s_));
             pdipc_status r = pd_solve(err);
             if (r != PDIPC_OK) return r;
+            PD_CK(cudaEventRecord(evp1_, s_));
             launch_direction(d, s_);
             launches_ += 2;
             if (outer == 0) {
@@ -861,6 +893,10 @@ private:
             launches_ += (d.nPT > 0) + (d.nEE > 0) + 1 + 1 + (d.nPT > 0) + (d.nEE > 0);
             PD_CK(cudaMemcpyAsync(&pin_->resid, d.Resid, sizeof(double), cudaMemcpyDeviceToHost, s_));
             PD_CK(cudaStreamSynchronize(s_));
+            float pms = 0.f;
+            PD_CK(cudaEventElapsedTime(&pms, evp0_, evp1_));
+            pd_ms_ += pms;
+            ++pd_solves_;
             const double res = pin_->resid;
             st_.last_residual = res;
             if (prm_.fixed_outer <= 0 && res < prm_.outer_tol && outer > 0) {
@@ -870,14 +906,14 @@ private:
             launch_copy_old(d, s_);
             ++launches_;
         }
-        const T damping = (T)(1.0 - (double)dt);
-        const T invt = (T)((1.0 / (double)dt) * (double)damping);
+        const TC damping = (TC)(1.0 - (double)dt);
+        const TC invt = (TC)((1.0 / (double)dt) * (double)damping);
         launch_velocity(d, invt, s_);
         ++launches_;
         PD_CK(cudaMemcpyAsync(&pin_->err, d.ErrFlags, sizeof(unsigned int), cudaMemcpyDeviceToHost, s_));
         PD_CK(cudaMemcpyAsync(&pin_->active, d.ActiveCount, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s_));
-        T toi;
-        PD_CK(cudaMemcpyAsync(&toi, d.Toi, sizeof(T), cudaMemcpyDeviceToHost, s_));
+        TC toi;
+        PD_CK(cudaMemcpyAsync(&toi, d.Toi, sizeof(TC), cudaMemcpyDeviceToHost, s_));
         PD_CK(cudaStreamSynchronize(s_));
         PD_CK(cudaGetLastError());
         st_.last_toi = (double)toi;
@@ -910,12 +946,15 @@ private:
     SolverConsts c_{};
     cudaStream_t s_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    cudaEvent_t evp0_ = nullptr, evp1_ = nullptr;  // around each PD solve
     double device_ms_ = 0.0;
+    double pd_ms_ = 0.0, pd_bytes_ = 0.0;
+    int64_t pd_solves_ = 0;
     std::vector<std::pair<void*, size_t>> ptrs_;
     int64_t bytes_ = 0;
     int64_t launches_ = 0;
     int64_t sell_entries_ = 0, sell_padded_ = 0;
-    V4<T>* scratch_ = nullptr;
+    V4<TC>* scratch_ = nullptr;
     int* cnt_ = nullptr;
     int* off_ = nullptr;
     int64_t* cpt_ = nullptr;
@@ -927,13 +966,13 @@ private:
     Pinned* pin_ = nullptr;
     PersistPlan plan_;
     std::vector<int> sliceOffH_, sliceLenH_;
-    PersistArgs<float> pargs_{};
+    PersistArgs<float, TC> pargs_{};
     int* pCtaSlice_ = nullptr;
     int* pCtaEntry_ = nullptr;
     int* pRowPat_ = nullptr;
     int16_t* pPatOff_ = nullptr;
     unsigned* pBar_ = nullptr;
-    V4<T>* stage_ = nullptr;
+    V4<TC>* stage_ = nullptr;  // pinned host staging of one state vector
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;
     int graph_nodes_ = 0;

@@ -37,6 +37,9 @@ EXPORTS = [
 ]
 
 
+ABI_VERSION = 2  # PDIPC_ABI_VERSION of include/pdipc.h
+
+
 class PdipcError(RuntimeError):
     def __init__(self, status: int, what: str, detail: str = ""):
         self.status = status
@@ -88,6 +91,9 @@ def load_library(path: str | None = None):
     L.pdipc_stage_sweep_timing.argtypes = [vp, C.c_int, _dp, _dp]
     L.pdipc_mesh_topology.argtypes = [_dp, C.c_int, _ip, C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, C.c_int, _ip,
                                       C.c_int, _ip, _ip, _ip]
+    if L.pdipc_abi_version() != ABI_VERSION:
+        raise ImportError(f"{path}: ABI version {L.pdipc_abi_version()}, this binding expects {ABI_VERSION}; "
+                          "rebuild the library")
     _lib = L
     return L
 

@@ -117,6 +117,9 @@ class Stats(C.Structure):
         ("device_ms", C.c_double),
         ("pd_path", C.c_int32),
         ("pd_ctas", C.c_int32),
+        ("pd_solves", C.c_int64),
+        ("pd_solve_ms", C.c_double),
+        ("pd_solve_bytes", C.c_double),
     ]
 
     def as_dict(self) -> dict:

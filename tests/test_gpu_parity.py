@@ -8,9 +8,9 @@ Tolerances:
   * FP32 mode: one PD solve within 2e-5 m of the FP32 oracle (the reference's
     own float Jacobi drifts ~1e-5 m per step from FP64, so FP32 runs are compared
     over a few steps only); time of impact within 1e-5 relative;
-  * mixed mode (correction form, FP32 sweeps, FP64 residual / CCD refinement)
-    is checked against the FP64 oracle: time of impact within 1e-6 relative,
-    positions within 1e-4 m after whole runs.
+  * mixed mode (FP64 state, FP32 local step and sweeps on the correction,
+    FP64 CCD refinement and contact) is checked against the FP64 oracle: time
+    of impact within 1e-6 relative, positions within 1e-4 m after whole runs.
 """
 import numpy as np
 import pytest
@@ -80,8 +80,6 @@ def test_time_of_impact_matches(prec, rtol, built_lib):
     sim = pdipc.Simulator(sc, prec)
     orc = Oracle(sc, ORACLE_PREC[prec], FORM_JJ, threads=4)
     X = near_contact_state(sc, 1.5e-3)
-    if prec == "mixed":                # the library holds float positions; give the oracle the same inputs
-        X = X.astype(np.float32).astype(np.float64)
     dx = np.zeros_like(X)
     dx[:sc.n_sim, 1] = -4e-3           # drive the cloth into the sphere
     rng = np.random.default_rng(3)
@@ -89,8 +87,6 @@ def test_time_of_impact_matches(prec, rtol, built_lib):
     pg, tg, eg = sim.stage_broadphase(X, dx)
     po, to, eo = orc.broadphase(X, dx)
     X1 = X + dx
-    if prec == "mixed":
-        X1 = X1.astype(np.float32).astype(np.float64)
     tpg, teg, gg = sim.stage_toi(X, X1, tg.shape[0], eg.shape[0])
     tpo, teo, go = orc.toi(X, X1, to.shape[0], eo.shape[0])
     # match candidates by their vertex tuples
@@ -105,8 +101,7 @@ def test_time_of_impact_matches(prec, rtol, built_lib):
         np.testing.assert_allclose(tpg[ig], tpo[io], rtol=rtol, atol=0)
         np.testing.assert_allclose(teg[jg], teo[jo], rtol=rtol, atol=0)
     assert go < 1.0
-    # the clamped global toi is rounded to the state type (float in mixed mode)
-    assert abs(gg - go) <= max(rtol, 1e-7 if prec == "mixed" else 0.0) * go
+    assert abs(gg - go) <= rtol * go
     # no impact the oracle finds is missed: every candidate it clamps is clamped here
     assert np.all(tpg[ig][tpo[io] < 1.0] < 1.0)
     assert np.all(teg[jg][teo[jo] < 1.0] < 1.0)
@@ -118,8 +113,6 @@ def test_contact_projection_matches(prec, tol, built_lib):
     sim = pdipc.Simulator(sc, prec)
     orc = Oracle(sc, ORACLE_PREC[prec], FORM_JJ, threads=4)
     X = near_contact_state(sc, 4e-4)
-    if prec == "mixed":
-        X = X.astype(np.float32).astype(np.float64)
     sim.stage_broadphase(X, np.zeros_like(X))
     orc.broadphase(X, np.zeros_like(X))
     dg, rg, ng = sim.stage_contact(X)
@@ -138,9 +131,6 @@ def test_pd_solve_matches(prec, atol, built_lib):
     X = np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics])
     rng = np.random.default_rng(11)
     V = rng.uniform(-0.1, 0.1, (sc.n_sim, 3))
-    if prec == "mixed":
-        X = X.astype(np.float32).astype(np.float64)
-        V = V.astype(np.float32).astype(np.float64)
     xg = sim.stage_pd(X, V)
     xo = orc.stage_pd(X, V)
     assert np.abs(xg - xo).max() < atol
@@ -148,7 +138,7 @@ def test_pd_solve_matches(prec, atol, built_lib):
         xr = Oracle(sc, "fp64", FORM_R2, threads=4).stage_pd(X, V)
         assert np.abs(xg - xr).max() < 1e-9
     # the state is untouched by the stage call
-    assert np.array_equal(sim.positions(), X.astype(np.float32).astype(np.float64) if prec != "fp64" else X)
+    assert np.array_equal(sim.positions(), X.astype(np.float32).astype(np.float64) if prec == "fp32" else X)
 
 
 def test_fp64_run_with_contact_matches_oracle(built_lib):
