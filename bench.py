@@ -218,16 +218,30 @@ def run_ours(args):
     sim.step(args.warmup)                    # captures the graph, grows candidate buffers
     sim.reset()
     torch.cuda.synchronize()
+
+    # Timed run through the public API with host buffers: the initial state is
+    # uploaded from host memory (set_state), then every step is animate() =
+    # run + postRun (positions to host).  `value` sums the device time of the
+    # steps (CUDA events on the library's stream); `e2e` is the wall time of the
+    # same calls, host<->device copies included.
+    x_init = np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics])
+    v_init = np.zeros((sc.n_sim, 3))
+    out = np.empty((sim.n_total, 3), np.float64)
     barrier(dist, dev)
-    dev_ms, launches, outers, wall = 0.0, 0, [], 0.0
+    dev_ms, launches, outers = 0.0, 0, []
     pd_ms, pd_solves = 0.0, 0
+    flush.zero_()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.set_state(x_init, v_init)
+    e2e_wall = time.perf_counter() - t0
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             flush.zero_()                    # L2 flush between timed steps (256 MB write)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            sim.step(1)
-            wall += time.perf_counter() - t0
+            sim.animate(out)
+            e2e_wall += time.perf_counter() - t0
             st = sim.stats()
             dev_ms += st["device_ms"]
             launches += st["kernel_launches"]
@@ -237,50 +251,45 @@ def run_ours(args):
         torch.cuda.synchronize()
     barrier(dist, dev)
     dev_ms_max = max_over_ranks(dist, dev_ms, dev)
-    st_end = sim.stats()
-
-    # e2e through the public API with host buffers: the initial state from host
-    # memory, then animate = run + postRun (positions to host) every step
-    x_init = np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics])
-    v_init = np.zeros((sc.n_sim, 3))
-    out = np.empty((sim.n_total, 3), np.float64)
-    barrier(dist, dev)
-    flush.zero_()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sim.set_state(x_init, v_init)
-    e2e_wall = time.perf_counter() - t0
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        sim.animate(out)
-        e2e_wall += time.perf_counter() - t0
-    barrier(dist, dev)
     e2e_max = max_over_ranks(dist, e2e_wall, dev)
+    st_end = sim.stats()
+    x_end = out.copy()
 
-    x_end = sim.positions()
-
-    # plain FP64 GPU form on the same trajectory: speed and the position error of this run
+    # plain FP64 GPU form over the same steps: its speed, the position error of
+    # this run after them, and the one-step error of this mode started from the
+    # FP64 run's own state every 10 steps
     fp64 = None
     if args.precision != "fp64" and args.fp64_steps > 0:
         k64 = min(args.fp64_steps, args.steps)
         ref = pdipc.Simulator(sc, "fp64", device=local)
         ref.step(args.warmup)
         ref.reset()
-        sim.reset()
-        ms64 = 0.0
-        for _ in range(k64):
+        ms64, outers64, one_step = 0.0, [], []
+        for k in range(k64):
+            probe = k % 10 == 0
+            if probe:
+                sim.set_state(ref.positions(), ref.velocities())
+                sim.step(1)
+                x_probe = sim.positions()
             flush.zero_()
             torch.cuda.synchronize()
             ref.step(1)
             ms64 += ref.stats()["device_ms"]
-        sim.step(k64)
-        err = float(np.abs(sim.positions() - ref.positions()).max())
+            outers64.append(ref.stats()["last_outer_iters"])
+            if probe:
+                one_step.append((k, float(np.abs(x_probe - ref.positions()).max())))
+        err = float(np.abs(x_end - ref.positions()).max()) if k64 == args.steps else None
         fp64 = {"value": round(k64 / (ms64 * 1e-3), 4), "unit": UNIT, "steps": k64,
                 "ms_per_step": round(ms64 / k64, 3),
-                "outer_iterations_last_step": ref.stats()["last_outer_iters"],
-                "max_position_err_m_vs_this_run": err}
+                "outer_iterations_per_step": {"mean": float(np.mean(outers64)), "max": int(max(outers64))},
+                "max_position_err_m_after_steps": err,
+                "one_step_err_m_from_fp64_state": {"max": max(e for _, e in one_step),
+                                                   "at_steps": [k for k, _ in one_step],
+                                                   "values": [float("%.3g" % e) for _, e in one_step]},
+                "note": "the trajectory error after many steps is bounded below by the FP64 path's own "
+                        "sensitivity once contact starts (an FP64 run perturbed by 1e-9 m departs by mm "
+                        "within 50 steps at this size: bench.py --accuracy-study); the one-step error "
+                        "from the same state is the precision mode's own contribution"}
         ref.close()
         del ref
 
@@ -323,14 +332,13 @@ def run_ours(args):
                    "patch_pairs": st_end["patch_pairs"], "pt_candidates": st_end["pt_candidates"],
                    "ee_candidates": st_end["ee_candidates"], "device_bytes": st_end["device_bytes"]},
         "element_updates_per_s": round(sim.n_sim * sc.lg_iterations * float(np.sum(outers)) / (dev_ms / 1e3), 1),
-        "wall_ms_per_step": round(1e3 * wall / args.steps, 4),
         "gpu_launches": int(launches),
         "e2e": {"value": round(e2e, 4), "unit": UNIT,
                 "h2d_bytes_per_step": int(round((sim.n_total + sc.n_sim) * state_bytes / args.steps)),
                 "d2h_bytes_per_step": int(sim.n_total * state_bytes + 8 * round(mean_outer) + 48),
-                "note": "set_state of the initial positions/velocities from host memory once, then animate() "
-                        "per step (step + copy of every position to host); the state stays on the device "
-                        "between steps, as in the reference"},
+                "note": "wall time of the timed run itself: set_state of the initial positions/velocities "
+                        "from host memory once, then animate() per step (step + copy of every position to "
+                        "host); the state stays on the device between steps, as in the reference"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": None if traffic is None else round(traffic),
@@ -391,6 +399,37 @@ def run_reference(args):
     print(json.dumps(res), flush=True)
 
 
+def run_accuracy_study(args):
+    """Position error of the chosen precision mode against the FP64 form along
+    the same run, next to the FP64 form's own sensitivity: a second FP64 run
+    whose simulated vertices start perturbed by a seeded uniform 1e-9 m."""
+    import pdipc
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    sc = workload(args.config)
+    a = pdipc.Simulator(sc, "fp64", device=local)
+    b = pdipc.Simulator(sc, "fp64", device=local)
+    c = pdipc.Simulator(sc, args.precision, device=local)
+    x = b.positions()
+    x[:sc.n_sim] += np.random.default_rng(1).uniform(-1e-9, 1e-9, (sc.n_sim, 3))
+    b.set_state(x)
+    rows = []
+    for k in range(args.steps):
+        oa = []
+        for sim in (a, b, c):
+            sim.step(1)
+            oa.append(sim.stats()["last_outer_iters"])
+        if (k + 1) % 10 == 0 or k + 1 == args.steps:
+            xa = a.positions()[:sc.n_sim]
+            rows.append({"step": k + 1, "active_contacts": a.stats()["active_contacts"],
+                         "fp64_vs_fp64_perturbed_1e-9_m": float(np.abs(xa - b.positions()[:sc.n_sim]).max()),
+                         f"{args.precision}_vs_fp64_m": float(np.abs(xa - c.positions()[:sc.n_sim]).max()),
+                         "outer_iterations_fp64_fp64p_mode": oa})
+    print(json.dumps({"study": "accuracy", "workload": workload_desc(sc, args.precision), "rows": rows}),
+          flush=True)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -404,10 +443,14 @@ def main(argv=None):
     ap.add_argument("--cpu-outer-sample", type=int, default=2)
     ap.add_argument("--ref-outer-per-step", type=float, default=30.0)
     ap.add_argument("--ref-budget-s", type=float, default=60.0)
+    ap.add_argument("--accuracy-study", action="store_true",
+                    help="print the error-vs-FP64 table of the precision mode instead of the bench line")
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
-    if args.impl == "reference":
+    if args.accuracy_study:
+        run_accuracy_study(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

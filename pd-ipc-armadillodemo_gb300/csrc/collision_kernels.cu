@@ -50,11 +50,13 @@ __device__ __forceinline__ void warp_box_reduce(T lo[3], T hi[3]) {
 // Swept, inflated patch AABB: per face min/max over x and x+dx of its three
 // vertices, minus/plus the inflation radius (getFaceBbox, cu:1350-1375), then
 // reduced over the patch's faces.  Boxes are in T: FP64 state (S) is rounded
-// to T first, so the mixed form's boxes are the FP32 form's.
+// to T first (read from the T-rounded copies Xh, Dh when given), so the mixed
+// form's boxes are the FP32 form's.
 template <typename T, typename S>
 __global__ void k_patch_boxes(int npatch, const int* __restrict__ pfPtr, const int* __restrict__ pfIdx,
                               const int4* __restrict__ Faces, const V4<S>* __restrict__ X,
-                              const V4<S>* __restrict__ D, T infl, Box6<T>* __restrict__ out) {
+                              const V4<S>* __restrict__ D, const V4<T>* __restrict__ Xh,
+                              const V4<T>* __restrict__ Dh, T infl, Box6<T>* __restrict__ out) {
     const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (p >= npatch) return;
@@ -66,14 +68,24 @@ __global__ void k_patch_boxes(int npatch, const int* __restrict__ pfPtr, const i
         const int vv[3] = {f.x, f.y, f.z};
         T a[3][3], c[3][3];
         for (int j = 0; j < 3; ++j) {
-            const V4<S> xs = ld4(X, vv[j]);
-            const V4<T> x{(T)xs.x, (T)xs.y, (T)xs.z, T(0)};
+            V4<T> x;
+            if (Xh) {
+                x = ld4(Xh, vv[j]);
+            } else {
+                const V4<S> xs = ld4(X, vv[j]);
+                x = V4<T>{(T)xs.x, (T)xs.y, (T)xs.z, T(0)};
+            }
             a[j][0] = x.x;
             a[j][1] = x.y;
             a[j][2] = x.z;
             if (D) {
-                const V4<S> ds = ld4(D, vv[j]);
-                const V4<T> d{(T)ds.x, (T)ds.y, (T)ds.z, T(0)};
+                V4<T> d;
+                if (Dh) {
+                    d = ld4(Dh, vv[j]);
+                } else {
+                    const V4<S> ds = ld4(D, vv[j]);
+                    d = V4<T>{(T)ds.x, (T)ds.y, (T)ds.z, T(0)};
+                }
                 c[j][0] = x.x + d.x;
                 c[j][1] = x.y + d.y;
                 c[j][2] = x.z + d.z;
@@ -412,12 +424,15 @@ __device__ __forceinline__ void block_min_to(TC v, TC* dst) {
 // getImpactOfTimeKernel (cu:2610-2704): skip pairs sharing a vertex, swept-AABB
 // filter with slack, additive CCD; global minimum by integer atomicMin.
 // kRel (mixed precision): coordinates relative to the pair's first vertex,
-// formed in FP64 from the FP64 state, an FP32 additive CCD on their rounding,
-// and every candidate that would clamp the step (toi < 1) re-evaluated in FP64
-// from the FP64 relative coordinates, so the minimum is an FP64 time of impact.
+// formed in FP32 from the float-float mirrors of the FP64 state, an FP32
+// additive CCD on them, and every candidate that would clamp the step
+// (toi < 1) re-evaluated in FP64 from the FP64 state, so the minimum is an
+// FP64 time of impact.
 template <typename T, typename TC, bool kPT, bool kRel>
 __global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restrict__ cand,
                                                 const V4<TC>* __restrict__ X0, const V4<TC>* __restrict__ X1,
+                                                const V4<T>* __restrict__ X0h, const V4<T>* __restrict__ X0l,
+                                                const V4<T>* __restrict__ X1h, const V4<T>* __restrict__ X1l,
                                                 TC slack, TC eta, int max_iter, TC* __restrict__ per,
                                                 TC* __restrict__ toi_min) {
     TC local = TC(1);
@@ -428,30 +443,38 @@ __global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restric
         const bool shared = kPT ? (c.x == c.y || c.x == c.z || c.x == c.w)
                                 : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w);
         if (!shared) {
-            if (kRel) {
+            if constexpr (kRel) {
                 T x[4][3], dx[4][3];
-                TC xd[4][3], dd[4][3];
-                const V4<TC> o = ld4(X0, ids[0]);
+                const V4<T> oh = ld4(X0h, ids[0]), ol = ld4(X0l, ids[0]);
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    const V4<TC> a = ld4(X0, ids[j]), b = ld4(X1, ids[j]);
-                    xd[j][0] = a.x - o.x;
-                    xd[j][1] = a.y - o.y;
-                    xd[j][2] = a.z - o.z;
-                    dd[j][0] = b.x - a.x;
-                    dd[j][1] = b.y - a.y;
-                    dd[j][2] = b.z - a.z;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        x[j][k] = (T)xd[j][k];
-                        dx[j][k] = (T)dd[j][k];
-                    }
+                    const V4<T> ah = ld4(X0h, ids[j]), al = ld4(X0l, ids[j]);
+                    const V4<T> bh = ld4(X1h, ids[j]), bl = ld4(X1l, ids[j]);
+                    x[j][0] = diff_ff(ah.x, al.x, oh.x, ol.x);
+                    x[j][1] = diff_ff(ah.y, al.y, oh.y, ol.y);
+                    x[j][2] = diff_ff(ah.z, al.z, oh.z, ol.z);
+                    dx[j][0] = diff_ff(bh.x, bl.x, ah.x, al.x);
+                    dx[j][1] = diff_ff(bh.y, bl.y, ah.y, al.y);
+                    dx[j][2] = diff_ff(bh.z, bl.z, ah.z, al.z);
                 }
                 const bool hit = kPT ? geo::pt_ccd_broad<T>(x, dx, (T)slack) : geo::ee_ccd_broad<T>(x, dx, (T)slack);
                 if (hit) {
                     const T tf = kPT ? geo::ccd_pt<T>(x, dx, (T)eta, max_iter) : geo::ccd_ee<T>(x, dx, (T)eta, max_iter);
-                    if (tf < T(1))
+                    if (tf < T(1)) {
+                        TC xd[4][3], dd[4][3];
+                        const V4<TC> o = ld4(X0, ids[0]);
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const V4<TC> a = ld4(X0, ids[j]), b = ld4(X1, ids[j]);
+                            xd[j][0] = a.x - o.x;
+                            xd[j][1] = a.y - o.y;
+                            xd[j][2] = a.z - o.z;
+                            dd[j][0] = b.x - a.x;
+                            dd[j][1] = b.y - a.y;
+                            dd[j][2] = b.z - a.z;
+                        }
                         toi = kPT ? geo::ccd_pt<TC>(xd, dd, eta, max_iter) : geo::ccd_ee<TC>(xd, dd, eta, max_iter);
+                    }
                 }
             } else {
                 TC x[4][3], dx[4][3];
@@ -497,7 +520,8 @@ struct ContactConsts {
 // needs no cancellation.
 template <typename T, typename TC, bool kPT, bool kRel>
 __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __restrict__ cand,
-                                                    const V4<TC>* __restrict__ X, const TC* __restrict__ mass,
+                                                    const V4<TC>* __restrict__ X, const V4<T>* __restrict__ Xh,
+                                                    const V4<T>* __restrict__ Xl, const TC* __restrict__ mass,
                                                     ContactConsts<TC> cc, T* __restrict__ diag,
                                                     V4<T>* __restrict__ rhs, unsigned long long* __restrict__ active) {
     unsigned int my = 0;
@@ -507,17 +531,15 @@ __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __res
         if (kPT ? (c.x == c.y || c.x == c.z || c.x == c.w) : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w))
             continue;
         TC p[4][3];
-        if (kRel) {
+        if constexpr (kRel) {
             T q[4][3];
-            const V4<TC> o = ld4(X, ids[0]);
+            const V4<T> oh = ld4(Xh, ids[0]), ol = ld4(Xl, ids[0]);
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const V4<TC> a = ld4(X, ids[j]);
-                p[j][0] = a.x - o.x;
-                p[j][1] = a.y - o.y;
-                p[j][2] = a.z - o.z;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) q[j][k] = (T)p[j][k];
+                const V4<T> ah = ld4(Xh, ids[j]), al = ld4(Xl, ids[j]);
+                q[j][0] = diff_ff(ah.x, al.x, oh.x, ol.x);
+                q[j][1] = diff_ff(ah.y, al.y, oh.y, ol.y);
+                q[j][2] = diff_ff(ah.z, al.z, oh.z, ol.z);
             }
             const T dhf = (T)cc.dh;
             bool far = false;
@@ -540,6 +562,14 @@ __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __res
             const T d2f = kPT ? geo::vtx_tri<T>(q[0], q[1], q[2], q[3], &a_, &b_, &c_, df)
                               : geo::edge_edge_sq<T>(q[0], q[1], q[2], q[3], &a_, &b_, df);
             if (!(d2f < (T)(1.21 * cc.dh2))) continue;
+            const V4<TC> o = ld4(X, ids[0]);  // close pair: FP64 relative coordinates
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const V4<TC> a = ld4(X, ids[j]);
+                p[j][0] = a.x - o.x;
+                p[j][1] = a.y - o.y;
+                p[j][2] = a.z - o.z;
+            }
         } else {
             gather4<TC, TC>(X, ids, p);
             bool far = false;
@@ -610,10 +640,11 @@ __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __res
 }  // namespace
 
 template <typename T, typename TC>
-void launch_patch_boxes(const Dev<T, TC>& d, const V4<TC>* X, const V4<TC>* D, T infl, cudaStream_t s) {
+void launch_patch_boxes(const Dev<T, TC>& d, const V4<TC>* X, const V4<TC>* D, const V4<T>* Xh, const V4<T>* Dh,
+                        T infl, cudaStream_t s) {
     if (d.npatch == 0) return;
     k_patch_boxes<T, TC><<<blocks_for((int64_t)d.npatch * 32), kBlock, 0, s>>>(d.npatch, d.pfPtr, d.pfIdx, d.Faces, X,
-                                                                          D, infl, d.PatchBox);
+                                                                              D, Xh, Dh, infl, d.PatchBox);
 }
 template <typename T, typename TC>
 void launch_patch_init_boxes(const Dev<T, TC>& d, T infl, cudaStream_t s) {
@@ -658,23 +689,24 @@ void launch_expand(const Dev<T, TC>& d, const int64_t* opt, const int64_t* oee, 
                                                           d.pePtr, d.peIdx, d.Faces, d.Edges, opt, oee, d.PT, d.EE);
 }
 template <typename T, typename TC>
-void launch_toi(const Dev<T, TC>& d, const V4<TC>* X0, const V4<TC>* X1, const SolverConsts& c, TC* per_pt,
+void launch_toi(const Dev<T, TC>& d, Pos<T, TC> X0, Pos<T, TC> X1, const SolverConsts& c, TC* per_pt,
                 TC* per_ee, cudaStream_t s) {
     constexpr bool kRel = sizeof(T) == 4 && sizeof(TC) == 8;
     if (d.nPT > 0)
-        k_toi<T, TC, true, kRel><<<grid_cap(d.nPT), kBlock, 0, s>>>(d.nPT, d.PT, X0, X1, (TC)c.ccd_slack,
-                                                                     (TC)c.ccd_eta, c.ccd_max_iter, per_pt, d.ToiMin);
+        k_toi<T, TC, true, kRel><<<grid_cap(d.nPT), kBlock, 0, s>>>(
+            d.nPT, d.PT, X0.x, X1.x, X0.hi, X0.lo, X1.hi, X1.lo, (TC)c.ccd_slack, (TC)c.ccd_eta, c.ccd_max_iter,
+            per_pt, d.ToiMin);
     if (d.nEE > 0)
-        k_toi<T, TC, false, kRel><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X0, X1, (TC)c.ccd_slack,
-                                                                      (TC)c.ccd_eta, c.ccd_max_iter, per_ee,
-                                                                      d.ToiMin);
+        k_toi<T, TC, false, kRel><<<grid_cap(d.nEE), kBlock, 0, s>>>(
+            d.nEE, d.EE, X0.x, X1.x, X0.hi, X0.lo, X1.hi, X1.lo, (TC)c.ccd_slack, (TC)c.ccd_eta, c.ccd_max_iter,
+            per_ee, d.ToiMin);
 }
 template <typename T, typename TC>
 void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s) {
     k_toi_finalize<TC><<<1, 1, 0, s>>>(d.ToiMin, d.Toi, c.toi_scale);
 }
 template <typename T, typename TC>
-void launch_contact(const Dev<T, TC>& d, const V4<TC>* X, const SolverConsts& c, cudaStream_t s) {
+void launch_contact(const Dev<T, TC>& d, Pos<T, TC> X, const SolverConsts& c, cudaStream_t s) {
     cudaMemsetAsync(d.CollDiag, 0, sizeof(T) * d.ntot, s);
     cudaMemsetAsync(d.CollRhs, 0, sizeof(V4<T>) * d.ntot, s);
     cudaMemsetAsync(d.ActiveCount, 0, sizeof(unsigned long long), s);
@@ -686,15 +718,17 @@ void launch_contact(const Dev<T, TC>& d, const V4<TC>* X, const SolverConsts& c,
     cc.dt = (TC)(T)c.dt;
     constexpr bool kRel = sizeof(T) == 4 && sizeof(TC) == 8;
     if (d.nPT > 0)
-        k_contact<T, TC, true, kRel><<<grid_cap(d.nPT), kBlock, 0, s>>>(d.nPT, d.PT, X, d.CollMass, cc,
-                                                                         d.CollDiag, d.CollRhs, d.ActiveCount);
+        k_contact<T, TC, true, kRel><<<grid_cap(d.nPT), kBlock, 0, s>>>(d.nPT, d.PT, X.x, X.hi, X.lo, d.CollMass,
+                                                                         cc, d.CollDiag, d.CollRhs, d.ActiveCount);
     if (d.nEE > 0)
-        k_contact<T, TC, false, kRel><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X, d.CollMass, cc,
-                                                                          d.CollDiag, d.CollRhs, d.ActiveCount);
+        k_contact<T, TC, false, kRel><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X.x, X.hi, X.lo,
+                                                                          d.CollMass, cc, d.CollDiag, d.CollRhs,
+                                                                          d.ActiveCount);
 }
 
 #define PDIPC_INST_COLL(T, TC)                                                                                \
-    template void launch_patch_boxes<T, TC>(const Dev<T, TC>&, const V4<TC>*, const V4<TC>*, T, cudaStream_t);\
+    template void launch_patch_boxes<T, TC>(const Dev<T, TC>&, const V4<TC>*, const V4<TC>*, const V4<T>*,     \
+                                            const V4<T>*, T, cudaStream_t);                                   \
     template void launch_patch_init_boxes<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                         \
     template void launch_morton<T, TC>(const Dev<T, TC>&, T*, unsigned long long*, int*, cudaStream_t);     \
     template void launch_karras<T, TC>(const Dev<T, TC>&, const unsigned long long*, cudaStream_t);           \
@@ -702,10 +736,10 @@ void launch_contact(const Dev<T, TC>& d, const V4<TC>* X, const SolverConsts& c,
     template void launch_traverse<T, TC>(const Dev<T, TC>&, int*, const int*, int2*, cudaStream_t);           \
     template void launch_pair_counts<T, TC>(const Dev<T, TC>&, int64_t*, int64_t*, cudaStream_t);             \
     template void launch_expand<T, TC>(const Dev<T, TC>&, const int64_t*, const int64_t*, cudaStream_t);      \
-    template void launch_toi<T, TC>(const Dev<T, TC>&, const V4<TC>*, const V4<TC>*, const SolverConsts&, TC*,\
+    template void launch_toi<T, TC>(const Dev<T, TC>&, Pos<T, TC>, Pos<T, TC>, const SolverConsts&, TC*,      \
                                     TC*, cudaStream_t);                                                       \
     template void launch_toi_finalize<T, TC>(const Dev<T, TC>&, const SolverConsts&, cudaStream_t);           \
-    template void launch_contact<T, TC>(const Dev<T, TC>&, const V4<TC>*, const SolverConsts&, cudaStream_t);
+    template void launch_contact<T, TC>(const Dev<T, TC>&, Pos<T, TC>, const SolverConsts&, cudaStream_t);
 
 PDIPC_INST_COLL(float, float)
 PDIPC_INST_COLL(double, double)

@@ -133,6 +133,19 @@ struct Sum2 {
     __device__ __forceinline__ float value() const { return s + c; }
 };
 
+// Float-float split of a double (Dekker): hi = rn(x), lo = rn(x - hi), so hi + lo
+// carries x to about 2^-48 relative.  The mixed form mirrors its FP64 positions
+// this way so the hot loops form position differences in FP32 only:
+// (hi_j - hi_i) + (lo_j - lo_i) is the difference rounded about once to FP32
+// (the hi difference of nearby values is exact by Sterbenz's lemma).  GB300's
+// FP64 rate is a small fraction of its FP32 rate, so FP64 arithmetic stays out
+// of the per-neighbour loops.
+__device__ __forceinline__ void split_ff(double x, float& hi, float& lo) {
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(x - (double)hi);
+}
+__device__ __forceinline__ float diff_ff(float hj, float lj, float hi, float li) { return (hj - hi) + (lj - li); }
+
 // Device-side error flags (bit mask), read back by the host after a step.
 enum ErrFlag : unsigned int {
     kErrNonFinite = 1u,

@@ -26,6 +26,13 @@ struct Dev {
     V4<TC>* Vel = nullptr;    // velocities [nsim]
     V4<TC>* Dir = nullptr;    // P - Pold before clamping [ntot]; static part stays 0
     V4<TC>* Xrest = nullptr;  // initial positions [ntot] (reset, pins)
+    // correction form only: float-float mirrors (hi, lo) of P and Pold and the
+    // rounded step direction, rewritten by every kernel that writes their source
+    V4<T>* Ph = nullptr;      // [ntot]
+    V4<T>* Pl = nullptr;      // [ntot]
+    V4<T>* Poh = nullptr;     // [ntot]
+    V4<T>* Pol = nullptr;     // [ntot]
+    V4<T>* Dh = nullptr;      // (float) Dir [ntot]
 
     // solver work
     V4<T>* Y = nullptr;      // first half of a two-sweep step [nsim]
@@ -105,6 +112,14 @@ struct Dev {
     unsigned long long* ActiveCount = nullptr;
 };
 
+// A position array and its float-float mirror (null outside the correction form).
+template <typename T, typename TC>
+struct Pos {
+    const V4<TC>* x = nullptr;
+    const V4<T>* hi = nullptr;
+    const V4<T>* lo = nullptr;
+};
+
 struct SolverConsts {
     double dt, gravity, dhat, kappa, infl, relax, rho, toi_scale, ccd_slack, ccd_eta, static_mass;
     int lg, cheby, ccd_max_iter;
@@ -142,12 +157,18 @@ template <typename T, typename TC>
 void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s);
 template <typename T, typename TC>
 void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s);
+// correction form: write the float-float mirror (hi, lo; lo may be null) of n
+// positions X, after a host write of X
+template <typename T, typename TC>
+void launch_split(const Dev<T, TC>& d, const V4<TC>* X, V4<T>* hi, V4<T>* lo, int n, cudaStream_t s);
 int direction_blocks(int nsim);
 
 // ---------------- collision kernels (collision_kernels.cu) ----------------
-// swept (Dir != null) or static patch boxes, inflated
+// swept (D != null) or static patch boxes, inflated; Xh, Dh: T-rounded copies
+// of X and D when the state is wider than T (correction form), else null
 template <typename T, typename TC>
-void launch_patch_boxes(const Dev<T, TC>& d, const V4<TC>* X, const V4<TC>* D, T infl, cudaStream_t s);
+void launch_patch_boxes(const Dev<T, TC>& d, const V4<TC>* X, const V4<TC>* D, const V4<T>* Xh, const V4<T>* Dh,
+                        T infl, cudaStream_t s);
 // init-time boxes over every vertex of the patch (AipcBvhs input, cpp:1279-1292)
 template <typename T, typename TC>
 void launch_patch_init_boxes(const Dev<T, TC>& d, T infl, cudaStream_t s);
@@ -166,12 +187,12 @@ void launch_pair_counts(const Dev<T, TC>& d, int64_t* cnt_pt, int64_t* cnt_ee, c
 template <typename T, typename TC>
 void launch_expand(const Dev<T, TC>& d, const int64_t* off_pt, const int64_t* off_ee, cudaStream_t s);
 template <typename T, typename TC>
-void launch_toi(const Dev<T, TC>& d, const V4<TC>* X0, const V4<TC>* X1, const SolverConsts& c, TC* per_pt,
+void launch_toi(const Dev<T, TC>& d, Pos<T, TC> X0, Pos<T, TC> X1, const SolverConsts& c, TC* per_pt,
                 TC* per_ee, cudaStream_t s);
 template <typename T, typename TC>
 void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s);
 template <typename T, typename TC>
-void launch_contact(const Dev<T, TC>& d, const V4<TC>* X, const SolverConsts& c, cudaStream_t s);
+void launch_contact(const Dev<T, TC>& d, Pos<T, TC> X, const SolverConsts& c, cudaStream_t s);
 
 // ---------------- primitives (primitives.cu) ----------------
 // Exclusive scan of n int64 values (in may equal out); *total receives the sum.

@@ -27,13 +27,29 @@ constexpr int kBlock = 256;
 
 inline int blocks_for(int n, int b = kBlock) { return (n + b - 1) / b; }
 
+// FP64 positions with FP32 arithmetic: the correction form keeps a float-float
+// mirror (Ph, Pl) of P.
+template <typename T, typename S>
+constexpr bool kMirror = std::is_same<T, float>::value && std::is_same<S, double>::value;
+
+__device__ __forceinline__ void store_split(V4<float>* Ph, V4<float>* Pl, int i, double x, double y, double z) {
+    float h0, l0, h1, l1, h2, l2;
+    split_ff(x, h0, l0);
+    split_ff(y, h1, l1);
+    split_ff(z, h2, l2);
+    Ph[i] = V4<float>{h0, h1, h2, 0.f};
+    Pl[i] = V4<float>{l0, l1, l2, 0.f};
+}
+
 // S is the state scalar (== T except in the correction form, where the
 // prediction is formed in FP64 from the FP32 mass and gravity terms).
 template <typename T, typename S, bool kDelta>
 __global__ void k_predict(int nsim, int ntot, S dt, V4<S>* __restrict__ P, V4<S>* __restrict__ Pold,
                           V4<S>* __restrict__ X0, V4<S>* __restrict__ Vel, V4<S>* __restrict__ Rhs0,
                           T* __restrict__ Dinert, const V4<T>* __restrict__ Grav, const T* __restrict__ InvMass,
-                          const int* __restrict__ PinFlag, T* __restrict__ CollDiag, V4<T>* __restrict__ CollRhs) {
+                          const int* __restrict__ PinFlag, T* __restrict__ CollDiag, V4<T>* __restrict__ CollRhs,
+                          V4<T>* __restrict__ Ph, V4<T>* __restrict__ Pl, V4<T>* __restrict__ Poh,
+                          V4<T>* __restrict__ Pol) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ntot) return;
     CollDiag[i] = T(0);
@@ -42,6 +58,10 @@ __global__ void k_predict(int nsim, int ntot, S dt, V4<S>* __restrict__ P, V4<S>
     const V4<S> x = P[i];
     X0[i] = x;
     Pold[i] = x;
+    if constexpr (kMirror<T, S>) {
+        Poh[i] = Ph[i];
+        Pol[i] = Pl[i];
+    }
     if (PinFlag[i] != -1) {  // pinned: velocity zeroed, nothing else written
         Vel[i] = V4<S>{S(0), S(0), S(0), S(0)};
         return;
@@ -58,6 +78,7 @@ __global__ void k_predict(int nsim, int ntot, S dt, V4<S>* __restrict__ P, V4<S>
     if (kDelta) Rhs0[i] = V4<S>{y0, y1, y2, S(0)};
     else Rhs0[i] = V4<S>{mm * y0, mm * y1, mm * y2, S(0)};
     P[i] = V4<S>{y0, y1, y2, S(0)};
+    if constexpr (kMirror<T, S>) store_split(Ph, Pl, i, y0, y1, y2);
 }
 
 template <typename T>
@@ -213,11 +234,13 @@ __global__ void __launch_bounds__(kBlock) k_sweep(int nsim, T relax, T omega, co
 // otherwise add a spurious pull toward the origin.  Every large term is formed
 // from a difference of nearby positions, so FP32 inputs lose nothing to
 // cancellation; the sum is accumulated with compensated (TwoSum) FP32 sums.  Then the first sweep from
-// delta = 0: Y = w r0 / D.  Positions are FP64 (S): each difference is formed
-// exactly-rounded in FP64 and enters the FP32 arithmetic as one rounding.
+// delta = 0: Y = w r0 / D.  Positions are FP64 (S): the vertex's own terms
+// subtract in FP64 once, the neighbour differences come from the float-float
+// mirror (Ph, Pl) in FP32; each enters the FP32 arithmetic as about one rounding.
 template <typename T, typename S>
 __global__ void __launch_bounds__(kBlock) k_local_residual(
-    int nsim, T relax, const V4<S>* __restrict__ P, const V4<S>* __restrict__ Pold, const V4<S>* __restrict__ Xrest,
+    int nsim, T relax, const V4<S>* __restrict__ P, const V4<T>* __restrict__ Ph, const V4<T>* __restrict__ Pl,
+    const V4<S>* __restrict__ Pold, const V4<S>* __restrict__ Xrest,
     const V4<S>* __restrict__ Ypred, const T* __restrict__ Dinert, const T* __restrict__ CollDiag,
     const V4<T>* __restrict__ CollRes, const int* __restrict__ PinFlag, const T* __restrict__ PinK,
     const int* __restrict__ lPtr, const int* __restrict__ lNbr, const T* __restrict__ lRest,
@@ -257,9 +280,12 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
     }
     const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
     const T strain = __ldg(Strain + i);
+    const V4<T> h = ld4(Ph, i), l = ld4(Pl, i);
     for (int s = b + 1; s < e; ++s) {  // mass-spring projections
-        const V4<S> xj = ld4(P, __ldg(lNbr + s));
-        const T d0 = (T)(x.x - xj.x), d1 = (T)(x.y - xj.y), d2 = (T)(x.z - xj.z);
+        const int j = __ldg(lNbr + s);
+        const V4<T> hj = ld4(Ph, j), lj = ld4(Pl, j);
+        const T d0 = diff_ff(h.x, l.x, hj.x, lj.x), d1 = diff_ff(h.y, l.y, hj.y, lj.y),
+                d2 = diff_ff(h.z, l.z, hj.z, lj.z);
         const T cl = dsqrt(d0 * d0 + d1 * d1 + d2 * d2);
         const T rc = strain * (__ldg(lRest + s) / cl);
         r0.add(rc * d0);
@@ -288,10 +314,10 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
         for (int k = 0; k < len; ++k) {
             const int j = __ldg(sCol + base + 32 * k);
             const T v = __ldg(sVal + base + 32 * k);
-            const V4<S> xj = ld4(P, j);
-            r0.add(v * (T)(xj.x - x.x));
-            r1.add(v * (T)(xj.y - x.y));
-            r2.add(v * (T)(xj.z - x.z));
+            const V4<T> hj = ld4(Ph, j), lj = ld4(Pl, j);
+            r0.add(v * diff_ff(hj.x, lj.x, h.x, l.x));
+            r1.add(v * diff_ff(hj.y, lj.y, h.y, l.y));
+            r2.add(v * diff_ff(hj.z, lj.z, h.z, l.z));
         }
     }
     const T f0 = r0.value(), f1 = r1.value(), f2 = r2.value();
@@ -307,7 +333,8 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
 template <typename T, typename S, int kMode>
 __global__ void __launch_bounds__(kBlock) k_sweep_delta(int nsim, T relax, T omega, const V4<T>* __restrict__ src,
                                                         const V4<T>* __restrict__ prev, V4<T>* __restrict__ out,
-                                                        V4<S>* __restrict__ P,
+                                                        V4<S>* __restrict__ P, V4<T>* __restrict__ Ph,
+                                                        V4<T>* __restrict__ Pl,
                                                         const V4<T>* __restrict__ Rhs, const T* __restrict__ InvD,
                                                         const int* __restrict__ sOff, const int* __restrict__ sLen,
                                                         const int* __restrict__ sCol, const T* __restrict__ sVal) {
@@ -336,7 +363,9 @@ __global__ void __launch_bounds__(kBlock) k_sweep_delta(int nsim, T relax, T ome
     }
     if (kMode & 4) {
         const V4<S> q = P[i];
-        P[i] = V4<S>{q.x + (S)y0, q.y + (S)y1, q.z + (S)y2, S(0)};
+        const S n0 = q.x + (S)y0, n1 = q.y + (S)y1, n2 = q.z + (S)y2;
+        P[i] = V4<S>{n0, n1, n2, S(0)};
+        if constexpr (kMirror<T, S>) store_split(Ph, Pl, i, n0, n1, n2);
     } else {
         out[i] = V4<T>{y0, y1, y2, T(0)};
     }
@@ -345,21 +374,23 @@ __global__ void __launch_bounds__(kBlock) k_sweep_delta(int nsim, T relax, T ome
 // Relative form of the curvature vector for the correction form:
 // aq = sum_{k>0} lbo_k (x_k - x_i), using that the LBO weights of a stencil sum
 // to zero.
-template <typename T, typename S>
-__global__ void k_local_aq_rel(int nsim, const V4<S>* __restrict__ P, const int* __restrict__ lPtr,
-                               const int* __restrict__ lNbr, const T* __restrict__ lLbo,
-                               const T* __restrict__ CurvNorm, V4<T>* __restrict__ Aq) {
+__global__ void k_local_aq_rel(int nsim, const V4<float>* __restrict__ Ph, const V4<float>* __restrict__ Pl,
+                               const int* __restrict__ lPtr, const int* __restrict__ lNbr,
+                               const float* __restrict__ lLbo, const float* __restrict__ CurvNorm,
+                               V4<float>* __restrict__ Aq) {
+    using T = float;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
     const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
-    const V4<S> x = ld4(P, i);
+    const V4<T> h = ld4(Ph, i), l = ld4(Pl, i);
     T a0 = T(0), a1 = T(0), a2 = T(0);
     for (int s = b + 1; s < e; ++s) {
-        const V4<S> xj = ld4(P, __ldg(lNbr + s));
-        const T l = __ldg(lLbo + s);
-        a0 += l * (T)(xj.x - x.x);
-        a1 += l * (T)(xj.y - x.y);
-        a2 += l * (T)(xj.z - x.z);
+        const int j = __ldg(lNbr + s);
+        const V4<T> hj = ld4(Ph, j), lj = ld4(Pl, j);
+        const T w = __ldg(lLbo + s);
+        a0 += w * diff_ff(hj.x, lj.x, h.x, l.x);
+        a1 += w * diff_ff(hj.y, lj.y, h.y, l.y);
+        a2 += w * diff_ff(hj.z, lj.z, h.z, l.z);
     }
     const T nrm = dsqrt(a0 * a0 + a1 * a1 + a2 * a2);
     if (nrm >= T(1e-10)) {
@@ -371,15 +402,16 @@ __global__ void k_local_aq_rel(int nsim, const V4<S>* __restrict__ P, const int*
     Aq[i] = V4<T>{a0, a1, a2, T(0)};
 }
 
-template <typename T>  // T: the state scalar
-__global__ void k_direction(int nsim, const V4<T>* __restrict__ P, const V4<T>* __restrict__ Pold,
-                            V4<T>* __restrict__ Dir, double* __restrict__ part) {
+template <typename T, typename S>  // S: the state scalar
+__global__ void k_direction(int nsim, const V4<S>* __restrict__ P, const V4<S>* __restrict__ Pold,
+                            V4<S>* __restrict__ Dir, V4<T>* __restrict__ Dh, double* __restrict__ part) {
     __shared__ double red[kBlock / 32];
     double acc = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nsim; i += gridDim.x * blockDim.x) {
-        const V4<T> a = P[i], b = Pold[i];
-        const T d0 = a.x - b.x, d1 = a.y - b.y, d2 = a.z - b.z;
-        Dir[i] = V4<T>{d0, d1, d2, T(0)};
+        const V4<S> a = P[i], b = Pold[i];
+        const S d0 = a.x - b.x, d1 = a.y - b.y, d2 = a.z - b.z;
+        Dir[i] = V4<S>{d0, d1, d2, S(0)};
+        if constexpr (kMirror<T, S>) Dh[i] = V4<T>{(T)d0, (T)d1, (T)d2, T(0)};
         acc += (double)d0 * (double)d0 + (double)d1 * (double)d1 + (double)d2 * (double)d2;
     }
     acc = warp_sum(acc);
@@ -392,20 +424,43 @@ __global__ void k_direction(int nsim, const V4<T>* __restrict__ P, const V4<T>* 
     }
 }
 
-template <typename T>
-__global__ void k_clamp(int nsim, const V4<T>* __restrict__ Pold, const V4<T>* __restrict__ Dir,
-                        const T* __restrict__ Toi, V4<T>* __restrict__ P) {
+template <typename T, typename S>  // S: the state scalar
+__global__ void k_clamp(int nsim, const V4<S>* __restrict__ Pold, const V4<S>* __restrict__ Dir,
+                        const S* __restrict__ Toi, V4<S>* __restrict__ P, V4<T>* __restrict__ Ph,
+                        V4<T>* __restrict__ Pl) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
-    const T t = *Toi;
-    const V4<T> a = Pold[i], d = Dir[i];
-    P[i] = V4<T>{a.x + t * d.x, a.y + t * d.y, a.z + t * d.z, T(0)};
+    const S t = *Toi;
+    const V4<S> a = Pold[i], d = Dir[i];
+    const S x = a.x + t * d.x, y = a.y + t * d.y, z = a.z + t * d.z;
+    P[i] = V4<S>{x, y, z, S(0)};
+    if constexpr (kMirror<T, S>) store_split(Ph, Pl, i, x, y, z);
 }
 
-template <typename T>
-__global__ void k_copy_old(int nsim, const V4<T>* __restrict__ P, V4<T>* __restrict__ Pold) {
+// hi = rn(x); lo = rn(x - hi) unless lo is null
+__global__ void k_split(int n, const V4<double>* __restrict__ X, V4<float>* __restrict__ hi,
+                        V4<float>* __restrict__ lo) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < nsim) Pold[i] = P[i];
+    if (i >= n) return;
+    const V4<double> x = X[i];
+    if (lo) {
+        store_split(hi, lo, i, x.x, x.y, x.z);
+    } else {
+        hi[i] = V4<float>{(float)x.x, (float)x.y, (float)x.z, 0.f};
+    }
+}
+
+template <typename T, typename S>
+__global__ void k_copy_old(int nsim, const V4<S>* __restrict__ P, V4<S>* __restrict__ Pold,
+                           const V4<T>* __restrict__ Ph, const V4<T>* __restrict__ Pl, V4<T>* __restrict__ Poh,
+                           V4<T>* __restrict__ Pol) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim) return;
+    Pold[i] = P[i];
+    if constexpr (kMirror<T, S>) {
+        Poh[i] = Ph[i];
+        Pol[i] = Pl[i];
+    }
 }
 
 template <typename T>
@@ -431,7 +486,7 @@ template <typename T, typename TC>
 void launch_predict(const Dev<T, TC>& d, TC dt, cudaStream_t s) {
     k_predict<T, TC, correction_form<T, TC>()><<<blocks_for(d.ntot), kBlock, 0, s>>>(
         d.nsim, d.ntot, dt, d.P, d.Pold, d.X0, d.Vel, d.Rhs0, d.Dinert, d.Grav, d.InvMass, d.PinFlag, d.CollDiag,
-        d.CollRhs);
+        d.CollRhs, d.Ph, d.Pl, d.Poh, d.Pol);
 }
 template <typename T, typename TC>
 void launch_diag(const Dev<T, TC>& d, cudaStream_t s) {
@@ -440,16 +495,19 @@ void launch_diag(const Dev<T, TC>& d, cudaStream_t s) {
 template <typename T, typename TC>
 void launch_local_aq(const Dev<T, TC>& d, cudaStream_t s) {
     if constexpr (correction_form<T, TC>())
-        k_local_aq_rel<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.lNbr, d.lLbo,
-                                                                     d.CurvNorm, d.Aq);
+        k_local_aq_rel<<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Ph, d.Pl, d.lPtr, d.lNbr, d.lLbo,
+                                                              d.CurvNorm, d.Aq);
     else
         k_local_aq<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.lNbr, d.lLbo, d.CurvNorm, d.Aq);
 }
 template <typename T, typename TC>
 void launch_local_residual(const Dev<T, TC>& d, T relax, cudaStream_t s) {
-    k_local_residual<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(
-        d.nsim, relax, d.P, d.Pold, d.Xrest, d.Rhs0, d.Dinert, d.CollDiag, d.CollRhs, d.PinFlag, d.PinK, d.lPtr,
-        d.lNbr, d.lRest, d.lBend, d.lBendT, d.Strain, d.Aq, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal, d.Rhs, d.Y);
+    if constexpr (kMirror<T, TC>) {
+        k_local_residual<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(
+            d.nsim, relax, d.P, d.Ph, d.Pl, d.Pold, d.Xrest, d.Rhs0, d.Dinert, d.CollDiag, d.CollRhs, d.PinFlag,
+            d.PinK, d.lPtr, d.lNbr, d.lRest, d.lBend, d.lBendT, d.Strain, d.Aq, d.InvD, d.sOff, d.sLen, d.sCol,
+            d.sVal, d.Rhs, d.Y);
+    }
 }
 template <typename T, typename TC>
 void launch_sweep_delta(const Dev<T, TC>& d, int mode, const V4<T>* src, const V4<T>* prev, V4<T>* out, T relax,
@@ -457,8 +515,8 @@ void launch_sweep_delta(const Dev<T, TC>& d, int mode, const V4<T>* src, const V
     const int nb = blocks_for(d.nsim);
 #define PDIPC_SWEEP_DELTA(M)                                                                                   \
     case M:                                                                                                    \
-        k_sweep_delta<T, TC, M><<<nb, kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.P, d.Rhs, d.InvD, \
-                                                      d.sOff, d.sLen, d.sCol, d.sVal);                         \
+        k_sweep_delta<T, TC, M><<<nb, kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.P, d.Ph, d.Pl,  \
+                                                      d.Rhs, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal);          \
         break;
     switch (mode) {
         PDIPC_SWEEP_DELTA(0)
@@ -492,16 +550,22 @@ void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T
 template <typename T, typename TC>
 void launch_direction(const Dev<T, TC>& d, cudaStream_t s) {
     const int nb = direction_blocks(d.nsim);
-    k_direction<TC><<<nb, kBlock, 0, s>>>(d.nsim, d.P, d.Pold, d.Dir, d.ResidPart);
+    k_direction<T, TC><<<nb, kBlock, 0, s>>>(d.nsim, d.P, d.Pold, d.Dir, d.Dh, d.ResidPart);
     launch_reduce_sum_f64(d.ResidPart, nb, d.Resid, s);
 }
 template <typename T, typename TC>
 void launch_clamp(const Dev<T, TC>& d, cudaStream_t s) {
-    k_clamp<TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Pold, d.Dir, d.Toi, d.P);
+    k_clamp<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Pold, d.Dir, d.Toi, d.P, d.Ph, d.Pl);
+}
+template <typename T, typename TC>
+void launch_split(const Dev<T, TC>& d, const V4<TC>* X, V4<T>* hi, V4<T>* lo, int n, cudaStream_t s) {
+    if constexpr (kMirror<T, TC>) {
+        if (n > 0) k_split<<<blocks_for(n), kBlock, 0, s>>>(n, X, hi, lo);
+    }
 }
 template <typename T, typename TC>
 void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s) {
-    k_copy_old<TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.Pold);
+    k_copy_old<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.Pold, d.Ph, d.Pl, d.Poh, d.Pol);
 }
 template <typename T, typename TC>
 void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {
@@ -521,6 +585,7 @@ void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {
     template void launch_direction<T, TC>(const Dev<T, TC>&, cudaStream_t);                                  \
     template void launch_clamp<T, TC>(const Dev<T, TC>&, cudaStream_t);                                      \
     template void launch_copy_old<T, TC>(const Dev<T, TC>&, cudaStream_t);                                   \
+    template void launch_split<T, TC>(const Dev<T, TC>&, const V4<TC>*, V4<T>*, V4<T>*, int, cudaStream_t);  \
     template void launch_velocity<T, TC>(const Dev<T, TC>&, TC, cudaStream_t);
 
 PDIPC_INST_PD(float, float)

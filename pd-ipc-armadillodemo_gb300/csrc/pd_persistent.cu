@@ -111,7 +111,8 @@ __device__ __forceinline__ void stcg4(V4<double>* p, int i, double x, double y, 
 }
 
 // S is the state scalar: T in the direct form, double in the correction form,
-// where positions enter the FP32 arithmetic only as rounded FP64 differences.
+// where positions enter the FP32 arithmetic as differences formed from their
+// float-float mirror (Ph, Pl): no FP64 arithmetic in the per-neighbour loops.
 template <typename T, typename S, bool kCorr, bool kSmem, bool kL1, int R>
 __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -182,18 +183,20 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
             if (!val[r]) continue;
             const int i = row[r];
             const int b = a.lPtr[i], e = a.lPtr[i + 1];
-            const V4<S> x = ldv<kL1>(a.P, i);
             T a0, a1, a2;
             if constexpr (kCorr) {
+                const V4<T> h = ldv<kL1>(a.Ph, i), l = ldv<kL1>(a.Pl, i);
                 a0 = a1 = a2 = T(0);
                 for (int s = b + 1; s < e; ++s) {
-                    const V4<S> xj = ldv<kL1>(a.P, a.lNbr[s]);
-                    const T l = a.lLbo[s];
-                    a0 += l * (T)(xj.x - x.x);
-                    a1 += l * (T)(xj.y - x.y);
-                    a2 += l * (T)(xj.z - x.z);
+                    const int j = a.lNbr[s];
+                    const V4<T> hj = ldv<kL1>(a.Ph, j), lj = ldv<kL1>(a.Pl, j);
+                    const T wl = a.lLbo[s];
+                    a0 += wl * diff_ff(hj.x, lj.x, h.x, l.x);
+                    a1 += wl * diff_ff(hj.y, lj.y, h.y, l.y);
+                    a2 += wl * diff_ff(hj.z, lj.z, h.z, l.z);
                 }
             } else {
+                const V4<S> x = ldv<kL1>(a.P, i);
                 const T l0 = a.lLbo[b];
                 a0 = x.x * l0;
                 a1 = x.y * l0;
@@ -256,9 +259,12 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
                     r2.add(c.z);
                     r2.add(dc * (T)(xo.z - x.z));
                 }
+                const V4<T> h = ldv<kL1>(a.Ph, i), l = ldv<kL1>(a.Pl, i);
                 for (int s = b + 1; s < e; ++s) {
-                    const V4<S> xj = ldv<kL1>(a.P, a.lNbr[s]);
-                    const T d0 = (T)(x.x - xj.x), d1 = (T)(x.y - xj.y), d2 = (T)(x.z - xj.z);
+                    const int j = a.lNbr[s];
+                    const V4<T> hj = ldv<kL1>(a.Ph, j), lj = ldv<kL1>(a.Pl, j);
+                    const T d0 = diff_ff(h.x, l.x, hj.x, lj.x), d1 = diff_ff(h.y, l.y, hj.y, lj.y),
+                            d2 = diff_ff(h.z, l.z, hj.z, lj.z);
                     const T cl = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
                     const T rc = strain * (a.lRest[s] / cl);
                     r0.add(rc * d0);
@@ -281,10 +287,10 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
                     T v;
                     int j;
                     entry(r, k, v, j);
-                    const V4<S> xj = ldv<kL1>(a.P, j);
-                    r0.add(v * (T)(xj.x - x.x));
-                    r1.add(v * (T)(xj.y - x.y));
-                    r2.add(v * (T)(xj.z - x.z));
+                    const V4<T> hj = ldv<kL1>(a.Ph, j), lj = ldv<kL1>(a.Pl, j);
+                    r0.add(v * diff_ff(hj.x, lj.x, h.x, l.x));
+                    r1.add(v * diff_ff(hj.y, lj.y, h.y, l.y));
+                    r2.add(v * diff_ff(hj.z, lj.z, h.z, l.z));
                 }
                 rh[r][0] = r0.value();
                 rh[r][1] = r1.value();
@@ -380,7 +386,14 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
                 if (last) {
                     if constexpr (kCorr) {  // only this thread writes the row: its own earlier read is current
                         const V4<S> x = ldcg4(a.P, row[r]);
-                        stcg4(a.P, row[r], x.x + (S)n0, x.y + (S)n1, x.z + (S)n2);
+                        const S q0 = x.x + (S)n0, q1 = x.y + (S)n1, q2 = x.z + (S)n2;
+                        stcg4(a.P, row[r], q0, q1, q2);
+                        float h0, l0, h1, l1, h2, l2;
+                        split_ff(q0, h0, l0);
+                        split_ff(q1, h1, l1);
+                        split_ff(q2, h2, l2);
+                        stcg4(a.Ph, row[r], h0, h1, h2);
+                        stcg4(a.Pl, row[r], l0, l1, l2);
                     } else {
                         stcg4(a.P, row[r], n0, n1, n2);
                     }

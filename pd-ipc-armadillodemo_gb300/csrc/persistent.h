@@ -35,8 +35,10 @@ struct PersistArgs {
     T relax;
     T omega[kMaxCheby];  // omega[it] of Chebyshev step it (it >= 1)
     long long timeout;   // barrier wait limit in clock cycles
-    // state
+    // state (correction form: Ph, Pl the float-float mirror of P)
     V4<S>* P;
+    V4<T>* Ph;
+    V4<T>* Pl;
     const V4<S>* Pold;
     const V4<S>* Xrest;
     const V4<S>* Rhs0;

@@ -105,6 +105,17 @@ public:
         PD_CK(up(d.P, X));
         PD_CK(up(d.Xrest, X));
         PD_CK(up(d.Pold, X));
+        if (kCorrection) {
+            PD_CK(zeros(d.Ph, nt));
+            PD_CK(zeros(d.Pl, nt));
+            PD_CK(zeros(d.Poh, nt));
+            PD_CK(zeros(d.Pol, nt));
+            PD_CK(zeros(d.Dh, nt));
+            PD_CK(zeros(sh_, nt));
+            PD_CK(zeros(sl_, nt));
+            launch_split(d, d.P, d.Ph, d.Pl, nt, s_);
+            launch_split(d, d.Pold, d.Poh, d.Pol, nt, s_);
+        }
         PD_CK(zeros(d.X0, ns));
         PD_CK(zeros(d.Vel, ns));
         PD_CK(zeros(d.Dir, nt));
@@ -234,7 +245,7 @@ public:
         // ---- scalars ----
         PD_CK(zeros(d.ToiMin, 1));
         const TC one = TC(1);
-        PD_CK(cudaMemcpy(d.ToiMin, &one, sizeof(TC), cudaMemcpyHostToDevice));
+        PD_CK(cudaMemcpyAsync(d.ToiMin, &one, sizeof(TC), cudaMemcpyHostToDevice, s_));
         PD_CK(zeros(d.Toi, 1));
         PD_CK(zeros(d.ResidPart, direction_blocks(ns)));
         PD_CK(zeros(d.Resid, 1));
@@ -315,11 +326,13 @@ public:
     pdipc_status set_state(const double* X, const double* V, std::string& err) override {
         pdipc_status r = upload_vec(d_.P, X, d_.ntot, err);
         if (r != PDIPC_OK) return r;
+        launch_split(d_, d_.P, d_.Ph, d_.Pl, d_.ntot, s_);
         if (V) return upload_vec(d_.Vel, V, d_.nsim, err);
         return PDIPC_OK;
     }
     pdipc_status reset(std::string& err) override {
         PD_CK(cudaMemcpyAsync(d_.P, d_.Xrest, sizeof(V4<TC>) * d_.ntot, cudaMemcpyDeviceToDevice, s_));
+        launch_split(d_, d_.P, d_.Ph, d_.Pl, d_.ntot, s_);
         PD_CK(cudaMemsetAsync(d_.Vel, 0, sizeof(V4<TC>) * d_.nsim, s_));
         PD_CK(cudaStreamSynchronize(s_));
         st_.steps_done = 0;
@@ -347,9 +360,13 @@ public:
                                   int64_t* n_ee, std::string& err) override {
         pdipc_status r = upload_vec(d_.Pold, xo, d_.ntot, err);
         if (r == PDIPC_OK) r = upload_vec(d_.Dir, dx, d_.ntot, err);
-        if (r == PDIPC_OK) r = broadphase(err);
+        if (r != PDIPC_OK) return r;
+        launch_split(d_, d_.Pold, d_.Poh, d_.Pol, d_.ntot, s_);
+        launch_split(d_, d_.Dir, d_.Dh, (V4<T>*)nullptr, d_.ntot, s_);
+        r = broadphase(err);
         if (r != PDIPC_OK) return r;
         PD_CK(cudaMemsetAsync(d_.Dir, 0, sizeof(V4<TC>) * d_.ntot, s_));
+        if (d_.Dh) PD_CK(cudaMemsetAsync(d_.Dh, 0, sizeof(V4<T>) * d_.ntot, s_));
         *n_pairs = d_.nPairs;
         *n_pt = d_.nPT;
         *n_ee = d_.nEE;
@@ -376,10 +393,12 @@ public:
         pdipc_status r = upload_vec(d_.Pold, x0, d_.ntot, err);
         if (r == PDIPC_OK) r = upload_vec(scratch_, x1, d_.ntot, err);
         if (r != PDIPC_OK) return r;
+        launch_split(d_, d_.Pold, d_.Poh, d_.Pol, d_.ntot, s_);
+        launch_split(d_, scratch_, sh_, sl_, d_.ntot, s_);
         TC *ppt = nullptr, *pee = nullptr;
         if (d_.nPT) PD_CK(cudaMalloc(&ppt, sizeof(TC) * d_.nPT));
         if (d_.nEE) PD_CK(cudaMalloc(&pee, sizeof(TC) * d_.nEE));
-        launch_toi(d_, d_.Pold, scratch_, c_, ppt, pee, s_);
+        launch_toi(d_, pos_old(), Pos<T, TC>{scratch_, sh_, sl_}, c_, ppt, pee, s_);
         launch_toi_finalize(d_, c_, s_);
         TC toi;
         PD_CK(cudaMemcpyAsync(&toi, d_.Toi, sizeof(TC), cudaMemcpyDeviceToHost, s_));
@@ -398,7 +417,8 @@ public:
                                std::string& err) override {
         pdipc_status r = upload_vec(scratch_, x, d_.ntot, err);
         if (r != PDIPC_OK) return r;
-        launch_contact(d_, scratch_, c_, s_);
+        launch_split(d_, scratch_, sh_, sl_, d_.ntot, s_);
+        launch_contact(d_, Pos<T, TC>{scratch_, sh_, sl_}, c_, s_);
         std::vector<T> hd(d_.ntot);
         std::vector<V4<T>> hr(d_.ntot);
         PD_CK(cudaMemcpyAsync(hd.data(), d_.CollDiag, sizeof(T) * d_.ntot, cudaMemcpyDeviceToHost, s_));
@@ -455,7 +475,13 @@ public:
     }
 
 private:
+    Pos<T, TC> pos() const { return Pos<T, TC>{d_.P, d_.Ph, d_.Pl}; }
+    Pos<T, TC> pos_old() const { return Pos<T, TC>{d_.Pold, d_.Poh, d_.Pol}; }
+
     // ---------------- allocation helpers ----------------
+    // Initialisation and uploads are ordered on the context's stream (created
+    // non-blocking, so the legacy default stream gives no ordering with it);
+    // uploads come from pageable memory, staged before the call returns.
     template <typename X>
     cudaError_t alloc(X*& p, size_t n) {
         n = std::max<size_t>(n, 1);
@@ -470,13 +496,13 @@ private:
     cudaError_t zeros(X*& p, size_t n) {
         cudaError_t e = alloc(p, n);
         if (e != cudaSuccess) return e;
-        return cudaMemset(p, 0, sizeof(X) * std::max<size_t>(n, 1));
+        return cudaMemsetAsync(p, 0, sizeof(X) * std::max<size_t>(n, 1), s_);
     }
     template <typename X>
     cudaError_t up(X*& p, const std::vector<X>& v) {
         cudaError_t e = alloc(p, v.size());
         if (e != cudaSuccess || v.empty()) return e;
-        return cudaMemcpy(p, v.data(), sizeof(X) * v.size(), cudaMemcpyHostToDevice);
+        return cudaMemcpyAsync(p, v.data(), sizeof(X) * v.size(), cudaMemcpyHostToDevice, s_);
     }
     template <typename X>
     void dfree(X*& p) {
@@ -628,6 +654,8 @@ private:
             }
             a.timeout = 4000000000ll;  // ~2 s at 2 GHz
             a.P = d.P;
+            a.Ph = d.Ph;
+            a.Pl = d.Pl;
             a.Pold = d.Pold;
             a.Xrest = d.Xrest;
             a.Rhs0 = d.Rhs0;
@@ -665,6 +693,11 @@ private:
                                   a.Dinert, a.CollDiag, a.PinFlag, a.PinK, a.lPtr, a.lNbr, a.lRest, a.lLbo,
                                   a.lBend, a.lBendT, a.Strain, a.CurvNorm, a.sliceEntry, a.sliceLen, a.sCol,
                                   a.sVal, a.ctaSlice, a.ctaEntry, a.rowPattern, a.patOff, a.bar, a.err};
+            if (kCorrection && (!a.Ph || !a.Pl)) {
+                plan_.enabled = false;
+                err = "persistent solve: unallocated position mirror";
+                return PDIPC_ERR_STATE;
+            }
             for (const void* q : ptrs)
                 if (!q) {
                     plan_.enabled = false;
@@ -726,7 +759,7 @@ private:
         d.nPairs = d.nPT = d.nEE = 0;
         if (d.npatch == 0) return PDIPC_OK;
         const T infl = (T)c_.infl;
-        launch_patch_boxes(d, d.Pold, d.Dir, infl, s_);
+        launch_patch_boxes(d, d.Pold, d.Dir, (const V4<T>*)d.Poh, (const V4<T>*)d.Dh, infl, s_);
         ++launches_;
         if (prm_.rebuild_bvh) {
             pdipc_status r = build_tree(false, err);
@@ -886,10 +919,10 @@ private:
                 r = broadphase(err);
                 if (r != PDIPC_OK) return r;
             }
-            launch_toi(d, d.Pold, d.P, c_, (TC*)nullptr, (TC*)nullptr, s_);
+            launch_toi(d, pos_old(), pos(), c_, (TC*)nullptr, (TC*)nullptr, s_);
             launch_toi_finalize(d, c_, s_);
             launch_clamp(d, s_);
-            launch_contact(d, d.P, c_, s_);
+            launch_contact(d, pos(), c_, s_);
             launches_ += (d.nPT > 0) + (d.nEE > 0) + 1 + 1 + (d.nPT > 0) + (d.nEE > 0);
             PD_CK(cudaMemcpyAsync(&pin_->resid, d.Resid, sizeof(double), cudaMemcpyDeviceToHost, s_));
             PD_CK(cudaStreamSynchronize(s_));
@@ -955,6 +988,8 @@ private:
     int64_t launches_ = 0;
     int64_t sell_entries_ = 0, sell_padded_ = 0;
     V4<TC>* scratch_ = nullptr;
+    V4<T>* sh_ = nullptr;  // float-float mirror of scratch_ (correction form)
+    V4<T>* sl_ = nullptr;
     int* cnt_ = nullptr;
     int* off_ = nullptr;
     int64_t* cpt_ = nullptr;
