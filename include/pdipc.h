@@ -212,6 +212,28 @@ pdipc_status pdipc_stage_morton(pdipc_ctx* ctx, uint64_t* codes, int* order, int
 pdipc_status pdipc_stage_toi(pdipc_ctx* ctx, const double* x0, const double* x1,
                              double* toi_pt, double* toi_ee, double* toi_global);
 
+/* No-allocation variant of pdipc_stage_toi; this entry point has no counterpart
+ * in the reference.  Same inputs and outputs (FP64 and mixed modes only:
+ * PDIPC_ERR_ARG in FP32 mode), but it allocates nothing on the device or the
+ * host: the per-candidate times of impact are written to one file-scope device
+ * array of 2^20 doubles (8 MiB, reserved when the library's module loads) and
+ * copied from there to toi_pt / toi_ee.  For callers that must not allocate
+ * between steps: cudaFree synchronises the whole device, which stalls a host
+ * that keeps other work queued, and cudaMalloc can fail when another allocator
+ * already holds the device's memory.
+ *   - Limit: n_pt + n_ee <= 2^20 candidates of the last broad phase, else
+ *     PDIPC_ERR_OVERFLOW (with the counts in pdipc_last_error) and nothing runs.
+ *   - The first call on a device looks up the array's address
+ *     (cudaGetSymbolAddress) and caches it; make that first call before any
+ *     stream capture begins.
+ *   - Nothing has to start at zero: each call writes entries [0, n) before
+ *     reading them.
+ *   - The array is shared by every context of the process on that device, so
+ *     overlapping calls would race on it; the library serialises them with a
+ *     per-device lock held until the results are on the host. */
+pdipc_status pdipc_stage_toi_noalloc(pdipc_ctx* ctx, const double* x0, const double* x1,
+                                     double* toi_pt, double* toi_ee, double* toi_global);
+
 /* setCollisionConstraintsHost (PdIpcGpuFunc.cu:2894-2930) over the candidate set
  * of the last broad phase at positions x (3*n_total): collision diagonal
  * (n_total) and right-hand side (3*n_total); *n_active gets the pair count. */

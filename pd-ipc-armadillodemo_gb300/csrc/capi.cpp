@@ -317,6 +317,16 @@ pdipc_status pdipc_stage_toi(pdipc_ctx* ctx, const double* x0, const double* x1,
     return guarded(ctx, [&]() { return ctx->solver->stage_toi(x0, x1, toi_pt, toi_ee, toi_global, ctx->err); });
 }
 
+pdipc_status pdipc_stage_toi_noalloc(pdipc_ctx* ctx, const double* x0, const double* x1, double* toi_pt,
+                                     double* toi_ee, double* toi_global) {
+    pdipc_status s = need_init(ctx);
+    if (s != PDIPC_OK) return s;
+    if (!x0 || !x1) return fail(ctx, PDIPC_ERR_ARG, "null argument");
+    return guarded(ctx, [&]() {
+        return ctx->solver->stage_toi_noalloc(x0, x1, toi_pt, toi_ee, toi_global, ctx->err);
+    });
+}
+
 pdipc_status pdipc_stage_contact(pdipc_ctx* ctx, const double* x, double* coll_diag, double* coll_rhs,
                                  int64_t* n_active) {
     pdipc_status s = need_init(ctx);

@@ -17,6 +17,7 @@
 // the Karras tree reports exactly the pairs of the reference's median-split
 // heap tree over the same boxes.
 #include <cfloat>
+#include <mutex>
 
 #include "geometry.cuh"
 #include "kernels.cuh"
@@ -724,6 +725,34 @@ void launch_contact(const Dev<T, TC>& d, Pos<T, TC> X, const SolverConsts& c, cu
         k_contact<T, TC, false, kRel><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X.x, X.hi, X.lo,
                                                                           d.CollMass, cc, d.CollDiag, d.CollRhs,
                                                                           d.ActiveCount);
+}
+
+// ---------------- no-allocation scratch of the per-candidate toi pass ----------------
+// File-scope device array: module load reserves it, so the no-allocation stage
+// entry needs no cudaMalloc.  Entries [0, n) are written by the toi kernels
+// before they are read; nothing in it has to start at zero.
+static __device__ __align__(256) double g_toi_scratch[kToiScratchEntries];
+
+cudaError_t toi_scratch(ToiScratch* out) {
+    constexpr int kMaxDevices = 64;
+    static std::mutex setup;
+    static std::mutex locks[kMaxDevices];
+    static double* ptrs[kMaxDevices] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> g(setup);
+    if (!ptrs[dev]) {  // first call on this device: look the symbol up once
+        double* ptr = nullptr;
+        e = cudaGetSymbolAddress((void**)&ptr, g_toi_scratch);
+        if (e != cudaSuccess) return e;
+        ptrs[dev] = ptr;
+    }
+    out->ptr = ptrs[dev];
+    out->entries = kToiScratchEntries;
+    out->lock = &locks[dev];
+    return cudaSuccess;
 }
 
 #define PDIPC_INST_COLL(T, TC)                                                                                \

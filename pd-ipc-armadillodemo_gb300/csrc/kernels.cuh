@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -193,6 +194,18 @@ template <typename T, typename TC>
 void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s);
 template <typename T, typename TC>
 void launch_contact(const Dev<T, TC>& d, Pos<T, TC> X, const SolverConsts& c, cudaStream_t s);
+
+// Scratch of the no-allocation per-candidate toi pass: a file-scope device array
+// of kToiScratchEntries doubles (8 MiB), its address looked up once per device on
+// first use.  One array per device is shared by every context of the process:
+// callers hold *lock from launch until their results are back on the host.
+constexpr int64_t kToiScratchEntries = int64_t(1) << 20;
+struct ToiScratch {
+    double* ptr = nullptr;
+    int64_t entries = 0;
+    std::mutex* lock = nullptr;
+};
+cudaError_t toi_scratch(ToiScratch* out);
 
 // ---------------- primitives (primitives.cu) ----------------
 // Exclusive scan of n int64 values (in may equal out); *total receives the sum.

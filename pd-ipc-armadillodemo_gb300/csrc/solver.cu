@@ -413,6 +413,42 @@ public:
         if (tg) *tg = (double)toi;
         return PDIPC_OK;
     }
+    // stage_toi without any allocation: the per-candidate results go to the
+    // library's static device scratch and from there straight to the caller's
+    // arrays.  Needs a double CCD scalar (FP64 and mixed modes).
+    pdipc_status stage_toi_noalloc(const double* x0, const double* x1, double* tpt, double* tee, double* tg,
+                                   std::string& err) override {
+        if constexpr (!std::is_same<TC, double>::value) {
+            err = "pdipc_stage_toi_noalloc: needs the FP64 or mixed precision mode";
+            return PDIPC_ERR_ARG;
+        } else {
+            ToiScratch sc;
+            PD_CK(toi_scratch(&sc));
+            const int64_t n = d_.nPT + d_.nEE;
+            if (n > sc.entries) {
+                err = "pdipc_stage_toi_noalloc: " + std::to_string(n) + " candidates exceed the " +
+                      std::to_string(sc.entries) + "-entry scratch";
+                return PDIPC_ERR_OVERFLOW;
+            }
+            std::lock_guard<std::mutex> hold(*sc.lock);
+            pdipc_status r = upload_vec(d_.Pold, x0, d_.ntot, err);
+            if (r == PDIPC_OK) r = upload_vec(scratch_, x1, d_.ntot, err);
+            if (r != PDIPC_OK) return r;
+            launch_split(d_, d_.Pold, d_.Poh, d_.Pol, d_.ntot, s_);
+            launch_split(d_, scratch_, sh_, sl_, d_.ntot, s_);
+            launch_toi(d_, pos_old(), Pos<T, TC>{scratch_, sh_, sl_}, c_, sc.ptr, sc.ptr + d_.nPT, s_);
+            launch_toi_finalize(d_, c_, s_);
+            TC toi = TC(1);
+            PD_CK(cudaMemcpyAsync(&toi, d_.Toi, sizeof(TC), cudaMemcpyDeviceToHost, s_));
+            if (tpt && d_.nPT)
+                PD_CK(cudaMemcpyAsync(tpt, sc.ptr, sizeof(double) * d_.nPT, cudaMemcpyDeviceToHost, s_));
+            if (tee && d_.nEE)
+                PD_CK(cudaMemcpyAsync(tee, sc.ptr + d_.nPT, sizeof(double) * d_.nEE, cudaMemcpyDeviceToHost, s_));
+            PD_CK(cudaStreamSynchronize(s_));
+            if (tg) *tg = (double)toi;
+            return PDIPC_OK;
+        }
+    }
     pdipc_status stage_contact(const double* x, double* diag, double* rhs, int64_t* n_active,
                                std::string& err) override {
         pdipc_status r = upload_vec(scratch_, x, d_.ntot, err);

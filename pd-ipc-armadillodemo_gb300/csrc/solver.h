@@ -26,6 +26,8 @@ public:
     virtual pdipc_status stage_morton(uint64_t* codes, int* order, int cap, std::string& err) = 0;
     virtual pdipc_status stage_toi(const double* x0, const double* x1, double* tpt, double* tee, double* tg,
                                    std::string& err) = 0;
+    virtual pdipc_status stage_toi_noalloc(const double* x0, const double* x1, double* tpt, double* tee,
+                                           double* tg, std::string& err) = 0;
     virtual pdipc_status stage_contact(const double* x, double* diag, double* rhs, int64_t* n_active,
                                        std::string& err) = 0;
     virtual pdipc_status stage_pd(const double* X, const double* V, double* out, std::string& err) = 0;

@@ -33,7 +33,7 @@ EXPORTS = [
     "pdipc_reset", "pdipc_get_stats", "pdipc_save", "pdipc_load", "pdipc_destroy", "pdipc_status_string",
     "pdipc_last_error", "pdipc_abi_version", "pdipc_stage_broadphase", "pdipc_stage_morton", "pdipc_stage_toi",
     "pdipc_stage_contact", "pdipc_stage_pd", "pdipc_mesh_topology",
-    "pdipc_stage_sweep_timing",
+    "pdipc_stage_sweep_timing", "pdipc_stage_toi_noalloc",
 ]
 
 
@@ -86,6 +86,7 @@ def load_library(path: str | None = None):
                                          C.c_int64, _i64p]
     L.pdipc_stage_morton.argtypes = [vp, C.POINTER(C.c_uint64), _ip, C.c_int]
     L.pdipc_stage_toi.argtypes = [vp, _dp, _dp, _dp, _dp, _dp]
+    L.pdipc_stage_toi_noalloc.argtypes = [vp, _dp, _dp, _dp, _dp, _dp]
     L.pdipc_stage_contact.argtypes = [vp, _dp, _dp, _dp, _i64p]
     L.pdipc_stage_pd.argtypes = [vp, _dp, _dp, _dp]
     L.pdipc_stage_sweep_timing.argtypes = [vp, C.c_int, _dp, _dp]
@@ -243,6 +244,20 @@ class Simulator:
         g = C.c_double()
         self._check(load_library().pdipc_stage_toi(self.h, _d(x0), _d(x1), _d(tp), _d(te), C.byref(g)),
                     "pdipc_stage_toi")
+        return tp[:npt], te[:nee], g.value
+
+    def stage_toi_noalloc(self, x0, x1, npt, nee, per_candidate=True):
+        """stage_toi through the no-allocation entry point (FP64 and mixed modes)."""
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        x1 = np.ascontiguousarray(x1, dtype=np.float64)
+        tp = np.empty(max(npt, 1), np.float64) if per_candidate else None
+        te = np.empty(max(nee, 1), np.float64) if per_candidate else None
+        g = C.c_double()
+        self._check(load_library().pdipc_stage_toi_noalloc(self.h, _d(x0), _d(x1), _d(tp) if per_candidate else None,
+                                                           _d(te) if per_candidate else None, C.byref(g)),
+                    "pdipc_stage_toi_noalloc")
+        if not per_candidate:
+            return None, None, g.value
         return tp[:npt], te[:nee], g.value
 
     def stage_contact(self, x):
