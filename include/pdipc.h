@@ -81,8 +81,10 @@ typedef struct {
     int device;              /* CUDA device ordinal */
     int rebuild_bvh;         /* 0: build the patch BVH once at initialize and refit per step
                                 (reference behaviour, cpp:1296-1320); 1: rebuild every step */
-    int persistent;          /* 1: FP32/mixed PD solve of an outer iteration as one cooperative launch
-                                when the mesh allows it (matrix slice per CTA); 0: one launch per sweep */
+    int persistent;          /* FP32/mixed PD solve of an outer iteration as one cooperative launch when
+                                the mesh allows it (matrix slice per CTA): 1 CTAs wait only for the CTAs
+                                they exchange rows with, gathers through L1; 2 the same with L2-only
+                                gathers; 3 grid-wide barriers, gathers through L1; 0 one launch per sweep */
     int reserved[6];
 } pdipc_params;
 

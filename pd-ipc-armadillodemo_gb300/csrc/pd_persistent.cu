@@ -13,10 +13,13 @@
 //   * each thread owns R rows (one per slice it handles) and keeps their
 //     current/previous iterate, right-hand side and inverse diagonal in registers;
 //   * only the vector being gathered crosses CTAs (through L2, and through L1
-//     once the barrier's acquire has invalidated it), between grid barriers.
-// The grid barrier is a counter/generation pair with a clock-bounded wait: on
-// timeout it raises kErrBarrier and every later barrier returns at once, so the
-// kernel always terminates.  The launch is cooperative (all CTAs co-resident).
+//     once the synchronisation's acquire has invalidated it), between phases;
+//   * a phase ends with neighbour synchronisation (each CTA waits only for the
+//     CTAs it exchanges rows with) or, optionally, a grid barrier (a
+//     counter/generation pair).
+// Every wait is clock-bounded: on timeout it raises kErrBarrier and every later
+// wait returns at once, so the kernel always terminates.  The launch is
+// cooperative (all CTAs co-resident).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -74,6 +77,46 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned* err, unsig
     }
     __syncthreads();
     return ok_s != 0;
+}
+
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Neighbour synchronisation: a Jacobi sweep only reads the rows of the CTAs a
+// CTA's matrix rows reach, so instead of a grid barrier each CTA publishes its
+// phase count and waits for those CTAs only (the range is closed under "reads
+// or is read by", so no CTA overwrites rows a neighbour is still reading).
+// Neighbours can then be at most one phase apart.  Lanes of warp 0 poll one
+// neighbour flag each; every wait is clock-bounded and gives up, raising
+// kErrBarrier, when it times out or sees the error raised elsewhere.
+__device__ __forceinline__ bool nbr_barrier(unsigned* flags, unsigned* err, int cta, int2 range, unsigned epoch,
+                                            long long timeout_cycles) {
+    __syncthreads();
+    __shared__ int nok_s;
+    if (threadIdx.x < 32) {
+        if (threadIdx.x == 0) {
+            __threadfence();
+            st_release_gpu(flags + cta, epoch);
+        }
+        int ok = (ld_acquire_gpu(err) & kErrBarrier) ? 0 : 1;
+        for (int n = range.x + (int)threadIdx.x; ok && n <= range.y; n += 32) {
+            if (n == cta) continue;
+            const long long t0 = clock64();
+            while ((int)(ld_acquire_gpu(flags + n) - epoch) < 0) {
+                if (clock64() - t0 > timeout_cycles || (ld_acquire_gpu(err) & kErrBarrier)) {
+                    atomicOr(err, (unsigned)kErrBarrier);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(8);
+            }
+        }
+        ok = __all_sync(0xffffffffu, ok);
+        if (threadIdx.x == 0) nok_s = ok;
+    }
+    __syncthreads();
+    return nok_s != 0;
 }
 
 __device__ __forceinline__ V4<float> ldcg4(const V4<float>* p, int i) {
@@ -153,6 +196,13 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
     __syncthreads();
     unsigned my_gen = 0;
     if (threadIdx.x == 0) my_gen = ld_acquire_gpu(a.bar);
+    const int2 nrange = a.nbr ? a.nbr[cta] : make_int2(0, -1);
+    unsigned epoch = a.epoch0;
+    // end of a phase: neighbour synchronisation or the grid barrier
+    auto sync = [&]() -> bool {
+        if (a.nbr) return nbr_barrier(a.flags, a.err, cta, nrange, ++epoch, a.timeout);
+        return grid_barrier(a.bar, a.err, gridDim.x, my_gen, a.timeout);
+    };
     const T w = a.relax, om1 = T(1) - a.relax;
     T id[R];
 #pragma unroll
@@ -218,7 +268,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
             }
             stcg4(a.Aq, i, a0, a1, a2);
         }
-        if (!grid_barrier(a.bar, a.err, gridDim.x, my_gen, a.timeout)) return;
+        if (!sync()) return;
 
         // ---- right-hand side (direct) or residual (correction) of the owned rows ----
         T x0[R][3], rh[R][3];
@@ -358,7 +408,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
             yv[r][2] = om1 * cx[r][2] + w * ((s2 + rh[r][2]) * id[r]);
             if (val[r]) stcg4(a.GY, row[r], yv[r][0], yv[r][1], yv[r][2]);
         }
-        if (!grid_barrier(a.bar, a.err, gridDim.x, my_gen, a.timeout)) return;
+        if (!sync()) return;
         const int nsteps = a.cheby;
         for (int it = 0; it < nsteps; ++it) {
             const bool last = it == nsteps - 1;
@@ -401,7 +451,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
                     stcg4(a.GX, row[r], n0, n1, n2);
                 }
             }
-            if (!grid_barrier(a.bar, a.err, gridDim.x, my_gen, a.timeout)) return;
+            if (!sync()) return;
             if (last) break;
             // first sweep of the next step: Y = S(x)
 #pragma unroll
@@ -413,7 +463,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
                 yv[r][2] = om1 * cx[r][2] + w * ((s2 + rh[r][2]) * id[r]);
                 if (val[r]) stcg4(a.GY, row[r], yv[r][0], yv[r][1], yv[r][2]);
             }
-            if (!grid_barrier(a.bar, a.err, gridDim.x, my_gen, a.timeout)) return;
+            if (!sync()) return;
         }
     }
 }

@@ -16,6 +16,7 @@ struct PersistPlan {
     bool enabled = false;
     bool matrix_in_smem = false;  // values in shared memory, columns from the pattern table
     bool l1_gather = true;        // gathers may hit in L1 (else L2-only .cg loads)
+    bool local_sync = true;       // CTAs wait for their row-exchange neighbours only (else grid barrier)
     int ctas = 0;
     int threads = 0;               // multiple of 32
     int rows_per_thread = 1;       // R: slices per warp
@@ -75,6 +76,12 @@ struct PersistArgs {
     // grid barrier: [0] generation, [1] arrival counter
     unsigned* bar;
     unsigned* err;
+    // neighbour synchronisation (nbr != null): CTA c publishes the number of
+    // phases it completed, epoch0 + k, in flags[c] and, before phase k + 1,
+    // waits until every CTA in [nbr[c].x, nbr[c].y] has published epoch0 + k
+    unsigned* flags;
+    const int2* nbr;
+    unsigned epoch0;
 };
 
 const void* persistent_kernel(bool correction, bool matrix_in_smem, bool l1_gather, int rows_per_thread);

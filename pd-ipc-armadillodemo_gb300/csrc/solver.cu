@@ -651,6 +651,7 @@ private:
                 plan_.enabled = true;
                 plan_.matrix_in_smem = smem_mat;
                 plan_.l1_gather = prm_.persistent != 2;
+                plan_.local_sync = prm_.persistent != 3;
                 plan_.ctas = ctas;
                 plan_.threads = W * 32;
                 plan_.rows_per_thread = R;
@@ -669,6 +670,34 @@ private:
         }
         std::vector<int16_t> patOff(std::max<size_t>(1, pats.size() * (size_t)patW), 0);
         for (auto& kv : pats) std::copy(kv.first.begin(), kv.first.end(), patOff.begin() + (size_t)kv.second * patW);
+        // CTAs each CTA exchanges rows with: the CTAs owning the columns of its
+        // matrix rows and stencils, closed under "is read by", as one range
+        std::vector<int> ctaOfRow(ns, 0);
+        for (int c = 0; c < plan_.ctas; ++c)
+            for (int r = ctaSlice[c] * kSlice; r < std::min(ns, ctaSlice[c + 1] * kSlice); ++r) ctaOfRow[r] = c;
+        std::vector<int2> rng(plan_.ctas);
+        for (int c = 0; c < plan_.ctas; ++c) {
+            int lo = c, hi = c;
+            for (int r = ctaSlice[c] * kSlice; r < std::min(ns, ctaSlice[c + 1] * kSlice); ++r) {
+                for (int e = H.nPtr[r]; e < H.nPtr[r + 1]; ++e) {
+                    lo = std::min(lo, ctaOfRow[H.nCol[e]]);
+                    hi = std::max(hi, ctaOfRow[H.nCol[e]]);
+                }
+                for (int e = H.lPtr[r]; e < H.lPtr[r + 1]; ++e) {
+                    lo = std::min(lo, ctaOfRow[H.lNbr[e]]);
+                    hi = std::max(hi, ctaOfRow[H.lNbr[e]]);
+                }
+            }
+            rng[c] = make_int2(lo, hi);
+        }
+        std::vector<int2> nbr = rng;
+        for (int c = 0; c < plan_.ctas; ++c)
+            for (int d2 = rng[c].x; d2 <= rng[c].y; ++d2) {
+                nbr[d2].x = std::min(nbr[d2].x, c);
+                nbr[d2].y = std::max(nbr[d2].y, c);
+            }
+        PD_CK(up(pNbr_, nbr));
+        PD_CK(zeros(pFlags_, plan_.ctas));
         PD_CK(up(pCtaSlice_, ctaSlice));
         PD_CK(up(pCtaEntry_, ctaEntry));
         PD_CK(up(pRowPat_, rowPat));
@@ -725,6 +754,9 @@ private:
             a.patW = patW;
             a.bar = pBar_;
             a.err = d.ErrFlags;
+            a.flags = pFlags_;
+            a.nbr = plan_.local_sync ? pNbr_ : nullptr;
+            a.epoch0 = 0;
             const void* ptrs[] = {a.P, a.Pold, a.Xrest, a.Rhs0, a.CollRhs, a.PinRhs, a.Aq, a.GX, a.GY, a.Delastic,
                                   a.Dinert, a.CollDiag, a.PinFlag, a.PinK, a.lPtr, a.lNbr, a.lRest, a.lLbo,
                                   a.lBend, a.lBendT, a.Strain, a.CurvNorm, a.sliceEntry, a.sliceLen, a.sCol,
@@ -745,7 +777,12 @@ private:
     }
 
     cudaError_t launch_persistent() {
-        if constexpr (std::is_same<T, float>::value) return launch_pd_persistent(plan_, pargs_, s_);
+        if constexpr (std::is_same<T, float>::value) {
+            // fresh phase numbers for this launch: every flag from earlier launches is below them
+            pargs_.epoch0 = epoch_;
+            epoch_ += (unsigned)(c_.lg * (2 * c_.cheby + 1) + 1);
+            return launch_pd_persistent(plan_, pargs_, s_);
+        }
         return cudaErrorNotSupported;
     }
 
@@ -1043,6 +1080,9 @@ private:
     int* pRowPat_ = nullptr;
     int16_t* pPatOff_ = nullptr;
     unsigned* pBar_ = nullptr;
+    unsigned* pFlags_ = nullptr;  // per-CTA phase counts of the neighbour synchronisation
+    int2* pNbr_ = nullptr;        // per-CTA range of CTAs to wait for
+    unsigned epoch_ = 1;
     V4<TC>* stage_ = nullptr;  // pinned host staging of one state vector
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;
