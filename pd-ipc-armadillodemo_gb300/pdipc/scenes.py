@@ -204,14 +204,56 @@ def config1(seed: int = 0) -> Scene:
 
 def stack(layers: int = 4, n: int = 256, subdiv: int = 5, gap: float = 5e-3,
           seed: int = 0, lg: int = 20, steps: int = 100,
-          dhat: float = 5e-4) -> Scene:
-    """Layers of n x n cloth stacked ``gap`` apart above an icosphere."""
+          dhat: float = 5e-4, pinned: bool = False, drop: float = 0.2) -> Scene:
+    """Layers of n x n cloth stacked ``gap`` apart (layer 0 lowest), each with
+    its own jitter stream, falling onto a radius-0.3 m icosphere whose top is
+    ``drop`` below the lowest layer's centre (0.2 m: centre 0.5 m below).  The
+    layers collide with each other and with themselves (the patch broad phase
+    pairs every two patches, of one model or two)."""
     cloths = []
     for L in range(layers):
         X, F = grid_cloth(n, 1.0, L * gap, 1e-4, seed + 7919 * L)
-        cloths.append(ClothSpec(X, F, np.array([0, n - 1], dtype=np.int32),
-                                patch_dim=n))
-    SX, SF = icosphere(subdiv, 0.3, (0.5, -0.5, 0.5))
+        pins = np.array([0, n - 1], dtype=np.int32) if pinned else np.zeros(0, np.int32)
+        cloths.append(ClothSpec(X, F, pins, patch_dim=n))
+    SX, SF = icosphere(subdiv, 0.3, (0.5, -0.3 - drop, 0.5))
     return Scene(f"stack{layers}x{n}_sphere{subdiv}", cloths,
                  [StaticSpec(SX, SF, patch_dim=sphere_patch_dim(SF.shape[0]))],
                  dhat=dhat, lg_iterations=lg, steps=steps)
+
+
+def config4(seed: int = 0) -> Scene:
+    """4 layers of 256x256 cloth 5 mm apart onto an icosphere (subdivision 5),
+    dhat 5e-4 m, 20 PD iterations, 100 steps."""
+    sc = stack(4, 256, 5, 5e-3, seed=seed, lg=20, steps=100, dhat=5e-4)
+    sc.name = "c4_stack4x256_sphere5"
+    return sc
+
+
+def batched(count: int = 256, nmin: int = 16, nmax: int = 128, seed: int = 0,
+            lg: int = 10, steps: int = 100, spacing: float = 2.0) -> Scene:
+    """``count`` independent drops in one scene: cloth k has a side of
+    U{nmin..nmax} vertices (1 m), stretch stiffness log-uniform in [1e3, 1e5]
+    and two pinned corners, above its own icosphere (subdivision U{2..4},
+    radius U(0.2, 0.4)) 0.5 m below its centre; drops sit on a square lattice
+    ``spacing`` m apart so no two of them can touch."""
+    u = uniform01(seed ^ 0x5EED, 4 * count).reshape(count, 4)
+    side = int(math.ceil(math.sqrt(count)))
+    cloths, statics = [], []
+    for k in range(count):
+        n = nmin + min(nmax - nmin, int(u[k, 0] * (nmax - nmin + 1)))
+        ks = 10.0 ** (3.0 + 2.0 * u[k, 1])
+        sub = 2 + min(2, int(u[k, 2] * 3))
+        rad = 0.2 + 0.2 * u[k, 3]
+        ox, oz = (k % side) * spacing, (k // side) * spacing
+        X, F = grid_cloth(n, 1.0, 0.0, 1e-4, seed + 104729 * (k + 1), origin=(ox, oz))
+        cloths.append(ClothSpec(X, F, np.array([0, n - 1], dtype=np.int32), k_stretch=ks, patch_dim=n))
+        SX, SF = icosphere(sub, rad, (ox + 0.5, -0.5, oz + 0.5))
+        statics.append(StaticSpec(SX, SF, patch_dim=sphere_patch_dim(SF.shape[0])))
+    return Scene(f"batched{count}_{nmin}to{nmax}", cloths, statics, lg_iterations=lg, steps=steps)
+
+
+def config2(seed: int = 0) -> Scene:
+    """256 independent drops, cloth sides U{16..128}, in one context, 100 steps."""
+    sc = batched(256, 16, 128, seed=seed, lg=10, steps=100)
+    sc.name = "c2_batched256"
+    return sc
