@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PDIPC_ABI_VERSION 2
+#define PDIPC_ABI_VERSION 3
 
 typedef struct pdipc_ctx pdipc_ctx;
 
@@ -134,6 +134,65 @@ pdipc_status pdipc_create(const pdipc_params* p, pdipc_ctx** out);
 pdipc_status pdipc_add_cloth(pdipc_ctx* ctx, const double* X, int nv, const int* F, int nf,
                              double density, double k_stretch, double k_bend,
                              const int* pins, int npins, double k_pin, int patch_dim);
+
+/* Add a simulated tetrahedral (volumetric) model: PdIpcSimulator::addModelFromConfigFile
+ * with <type> 1 k_strain k_volume k_pin, <density>, <patchDim> (PdIpcSimulator.h:462-534,
+ * PdIpcVolumetricModel(s0, s1, s2), PdIpcVolumetricModel.h:21-25) read from a tetgen
+ * .node/.ele pair.  X: 3*nv float64, T: 4*nt int32 (0-based), pins: local vertex ids.
+ * Node mass is density times the summed volume of the node's tets (the reference's
+ * BaseTetMeshHandle::computeVolume); every tet adds the strain constraint of
+ * solveVolumetricStrainConstraintKernel (PdIpcGpuFunc.cu:439-599) with weight
+ * k_strain * volume.  k_volume is accepted and unused, as in the reference (its
+ * volume-constraint list is never filled).  The tets' boundary faces (faces of one tet)
+ * collide; collision patches are a patch_dim^3 grid (PdIpcVolumetricModel.h:114-182). */
+pdipc_status pdipc_add_volumetric(pdipc_ctx* ctx, const double* X, int nv, const int* T, int nt,
+                                  double density, double k_strain, double k_volume,
+                                  const int* pins, int npins, double k_pin, int patch_dim);
+
+/* Boundary surface of a tetrahedral mesh, on the host (no device needed): the faces
+ * that belong to exactly one tet, turned to face away from it
+ * (PdIpcVolumetricModel::registerBoundaryInfo, PdIpcVolumetricModel.h:27-112; the
+ * reference walks a hash map, here faces come in ascending order of their sorted
+ * vertex triple).  These are the faces pdipc_add_volumetric makes collide.
+ * faces: 3*cap_faces ints; *n_faces gets the count even when it exceeds cap_faces
+ * (PDIPC_ERR_OVERFLOW). */
+pdipc_status pdipc_tet_surface(const double* X, int nv, const int* T, int nt,
+                               int* faces, int cap_faces, int* n_faces);
+
+/* ---------------------------------------------------------------------------
+ * Scene files (host only).  pdipc_scene_load reads a reference config.xml:
+ * <timeStep>, <gravity>, <dhat>, <kappa> and every <object>/<static_object>
+ * with its <name>/<name>.obj, tetgen .node/.ele (volumetric_mesh="tet"),
+ * fixed_points.txt, and placement (origin/uniform attributes, <scale>,
+ * <translation>, <rotation>) as BaseSimulator::readSimulatorFromConfigFile and
+ * PdIpcSimulator::addModelFromConfigFile do (Simulator/BaseSimulator.cpp:4-65,
+ * PdIpcSimulator.h:462-642, Model/BaseModel.cpp:21-66, 411-471).
+ * ------------------------------------------------------------------------- */
+typedef struct pdipc_scene pdipc_scene;
+
+typedef struct {
+    const char* name;     /* the object's name attribute */
+    int kind;             /* 0 cloth (<type> 0), 1 volumetric (<type> 1), 2 static */
+    int nv, nf, nt, npins;
+    const double* X;      /* 3*nv placed positions (the tet nodes of a volumetric model) */
+    const int* F;         /* 3*nf OBJ faces, 0-based (render surface of a volumetric model) */
+    const int* T;         /* 4*nt tets, 0-based, or NULL */
+    const int* pins;      /* fixed_points.txt ids, or NULL */
+    double density;
+    double k[3];          /* <type> stiffness triple: cloth (stretch, bend, pin),
+                             volumetric (strain, volume, pin) */
+    int patch_dim;
+} pdipc_scene_model;
+
+/* err (err_len bytes) receives a message on failure; *out owns every array. */
+pdipc_status pdipc_scene_load(const char* config_path, pdipc_scene** out, char* err, int err_len);
+int pdipc_scene_model_count(const pdipc_scene* s);
+pdipc_status pdipc_scene_get_model(const pdipc_scene* s, int i, pdipc_scene_model* out);
+/* time_step, gravity, dhat and kappa the config sets; other fields are kept */
+pdipc_status pdipc_scene_apply_params(const pdipc_scene* s, pdipc_params* p);
+/* pdipc_add_cloth / pdipc_add_volumetric / pdipc_add_static for every model, in file order */
+pdipc_status pdipc_scene_add_models(const pdipc_scene* s, pdipc_ctx* ctx);
+void pdipc_scene_free(pdipc_scene* s);
 
 /* Add a static (kinematically fixed) triangle mesh:
  * PdIpcSimulator::addStaticModelFromConfigFile (PdIpcSimulator.h:536-600). */

@@ -82,6 +82,17 @@ public:
         models_.push_back(std::move(m));
         return true;
     }
+    // <object volumetric_mesh="tet"> with <type> 1 k_strain k_volume k_pin
+    // (PdIpcVolumetricModel(s0, s1, s2)); X, T from the tetgen .node/.ele pair
+    bool addVolumetricModel(const std::vector<double>& X, const std::vector<int>& T, const std::vector<int>& fixedIds,
+                            double density, double strainStiffness, double volumeStiffness, double positionStiffness,
+                            int patchDim = 10) {
+        Model m{X, {}, fixedIds, false, density, strainStiffness, 0.0, positionStiffness, patchDim};
+        m.T = T;
+        m.k_volume = volumeStiffness;
+        models_.push_back(std::move(m));
+        return true;
+    }
     // <static_object> (addStaticModelFromConfigFile, PdIpcSimulator.h:536-600)
     bool addStaticModel(const std::vector<double>& X, const std::vector<int>& F, int patchDim = 10) {
         Model m{X, F, {}, true, 0.0, 0.0, 0.0, 0.0, patchDim};
@@ -96,11 +107,16 @@ public:
         if ((status_ = pdipc_create(&params_, &ctx_)) != PDIPC_OK) return;
         for (const Model& m : models_) {
             const int nv = (int)m.X.size() / 3, nf = (int)m.F.size() / 3;
-            status_ = m.is_static
-                          ? pdipc_add_static(ctx_, m.X.data(), nv, m.F.data(), nf, m.patch_dim)
-                          : pdipc_add_cloth(ctx_, m.X.data(), nv, m.F.data(), nf, m.density, m.k_stretch, m.k_bend,
-                                            m.pins.empty() ? nullptr : m.pins.data(), (int)m.pins.size(), m.k_pin,
-                                            m.patch_dim);
+            const int* pins = m.pins.empty() ? nullptr : m.pins.data();
+            if (m.is_static)
+                status_ = pdipc_add_static(ctx_, m.X.data(), nv, m.F.data(), nf, m.patch_dim);
+            else if (!m.T.empty())
+                status_ = pdipc_add_volumetric(ctx_, m.X.data(), nv, m.T.data(), (int)m.T.size() / 4, m.density,
+                                               m.k_stretch, m.k_volume, pins, (int)m.pins.size(), m.k_pin,
+                                               m.patch_dim);
+            else
+                status_ = pdipc_add_cloth(ctx_, m.X.data(), nv, m.F.data(), nf, m.density, m.k_stretch, m.k_bend,
+                                          pins, (int)m.pins.size(), m.k_pin, m.patch_dim);
             if (status_ != PDIPC_OK) return;
         }
         if ((status_ = pdipc_initialize(ctx_)) != PDIPC_OK) return;
@@ -142,8 +158,10 @@ private:
         std::vector<int> F;
         std::vector<int> pins;
         bool is_static;
-        double density, k_stretch, k_bend, k_pin;
+        double density, k_stretch, k_bend, k_pin;  // k_stretch: the strain stiffness of a volumetric model
         int patch_dim;
+        std::vector<int> T;  // tets of a volumetric model
+        double k_volume = 0.0;
     };
     bool ready() { return ctx_ && status_ == PDIPC_OK; }
 

@@ -38,6 +38,11 @@ def lib():
         L.orc_add_cloth.argtypes = [C.c_void_p, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double,
                                     C.c_double, _ip, C.c_int, C.c_double, C.c_int]
         L.orc_add_static.argtypes = [C.c_void_p, _dp, C.c_int, _ip, C.c_int, C.c_int]
+        L.orc_add_volumetric.argtypes = [C.c_void_p, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double, _ip,
+                                         C.c_int, C.c_double, C.c_int]
+        L.orc_tet_project.argtypes = [C.c_int, _dp, _dp, _dp, _dp]
+        L.orc_svd3.argtypes = [_dp, _dp, _dp, _dp]
+        L.orc_tet_surface.argtypes = [_dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip]
         L.orc_initialize.argtypes = [C.c_void_p]
         L.orc_step.argtypes = [C.c_void_p, C.c_int]
         L.orc_get_positions.argtypes = [C.c_void_p, _dp]
@@ -92,6 +97,12 @@ class Oracle:
             P = np.ascontiguousarray(c.pins, dtype=np.int32)
             _check(L.orc_add_cloth(self.h, _d(X), X.shape[0], _i(F), F.shape[0], c.density, c.k_stretch,
                                    c.k_bend, _i(P), P.shape[0], c.k_pin, c.patch_dim), "add_cloth")
+        for v in getattr(scene, "solids", []):
+            X = np.ascontiguousarray(v.X, dtype=np.float64)
+            T = np.ascontiguousarray(v.T, dtype=np.int32)
+            P = np.ascontiguousarray(v.pins, dtype=np.int32)
+            _check(L.orc_add_volumetric(self.h, _d(X), X.shape[0], _i(T), T.shape[0], v.density, v.k_strain,
+                                        _i(P), P.shape[0], v.k_pin, v.patch_dim), "add_volumetric")
         for s in scene.statics:
             X = np.ascontiguousarray(s.X, dtype=np.float64)
             F = np.ascontiguousarray(s.F, dtype=np.int32)
@@ -207,3 +218,34 @@ def mesh_topology(X, F, patch_dim):
     owned_points = [op[opo[f]:opo[f + 1]].copy() for f in range(nf)]
     owned_edges = [oe[oeo[f]:oeo[f + 1]].copy() for f in range(nf)]
     return edges[:n_e].copy(), patches, owned_points, owned_edges
+
+
+def tet_project(x, idm, w):
+    """The oracle's tet strain projection on its own: x (n, 4, 3) positions,
+    idm (n, 3, 3) row-major Dm^-1, w (n,) -> (n, 4, 3) = w R G per vertex."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    idm = np.ascontiguousarray(idm, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    out = np.empty((x.shape[0], 4, 3), np.float64)
+    _check(lib().orc_tet_project(x.shape[0], _d(x), _d(idm), _d(w), _d(out)), "tet_project")
+    return out
+
+
+def svd3(F):
+    """The oracle's SVD of one 3x3 matrix: (U, s, V), U and V proper rotations,
+    the sign of det F on s[2]."""
+    F = np.ascontiguousarray(F, dtype=np.float64)
+    U, V, sv = np.empty((3, 3)), np.empty((3, 3)), np.empty(3)
+    _check(lib().orc_svd3(_d(F), _d(U), _d(sv), _d(V)), "svd3")
+    return U, sv, V
+
+
+def tet_surface(X, T):
+    """The oracle's boundary faces of a tet mesh (ascending sorted triple, outward)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.int32)
+    cap = 4 * T.shape[0]
+    out = np.empty((cap, 3), np.int32)
+    nf = C.c_int()
+    _check(lib().orc_tet_surface(_d(X), X.shape[0], _i(T), T.shape[0], _i(out), cap, C.byref(nf)), "tet_surface")
+    return out[:nf.value].copy()

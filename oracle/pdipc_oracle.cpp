@@ -94,7 +94,7 @@ static void build_edges(Topology& t) {
 // Ownership: every edge and every point is handed to exactly one incident face,
 // the first one (in incidence order) whose owned list is currently smallest
 // (PdIpcModel.h:136-171).  Patch-pair expansion then never repeats a primitive.
-static bool build_ownership(Topology& t) {
+static bool build_ownership(Topology& t, bool volumetric = false) {
     std::vector<std::vector<int>> point_faces(t.nv);
     for (int f = 0; f < t.nf; ++f)
         for (int k = 0; k < 3; ++k) point_faces[t.faces[f][k]].push_back(f);
@@ -121,7 +121,10 @@ static bool build_ownership(Topology& t) {
     }
     t.face_owned_points.assign(t.nf, {});
     for (int p = 0; p < t.nv; ++p) {
-        if (point_faces[p].empty()) return false;  // isolated vertex: the reference reads past the list
+        if (point_faces[p].empty()) {
+            if (volumetric) continue;  // interior node of a tet mesh
+            return false;              // isolated vertex: the reference reads past the list
+        }
         int best = point_faces[p][0];
         size_t bs = t.face_owned_points[best].size();
         for (size_t k = 1; k < point_faces[p].size(); ++k) {
@@ -190,15 +193,208 @@ static void build_patches(Topology& t, const std::vector<double>& X, int patch_d
         if (!p.empty()) t.patches.push_back(p);
 }
 
+// Boundary surface of a tet mesh (PdIpcVolumetricModel::registerBoundaryInfo,
+// PdIpcVolumetricModel.h:27-112): faces (3,1,0), (3,2,1), (3,0,2), (2,1,0) of
+// every tet; a face met once is boundary, turned away from its tet's centroid.
+// The reference walks an unordered_map; here the faces come in ascending order
+// of their sorted vertex triple.
+static std::vector<std::array<int, 3>> tet_surface(const std::vector<double>& X, const std::vector<int>& T, int nt) {
+    static const int fi[4][3] = {{3, 1, 0}, {3, 2, 1}, {3, 0, 2}, {2, 1, 0}};
+    std::map<std::array<int, 3>, std::vector<std::array<int, 4>>> m;
+    for (int e = 0; e < nt; ++e)
+        for (auto& q : fi) {
+            std::array<int, 3> f = {T[4 * e + q[0]], T[4 * e + q[1]], T[4 * e + q[2]]};
+            std::array<int, 3> key = f;
+            std::sort(key.begin(), key.end());
+            m[key].push_back({f[0], f[1], f[2], e});
+        }
+    std::vector<std::array<int, 3>> out;
+    for (auto& kv : m) {
+        if (kv.second.size() != 1) continue;
+        const auto& d = kv.second[0];
+        double cent[3] = {0, 0, 0}, fc[3] = {0, 0, 0}, a[3], b[3];
+        for (int k = 0; k < 3; ++k) {
+            for (int q = 0; q < 4; ++q) cent[k] += X[3 * T[4 * d[3] + q] + k] / 4.0;
+            for (int q = 0; q < 3; ++q) fc[k] += X[3 * d[q] + k] / 3.0;
+            a[k] = X[3 * d[1] + k] - X[3 * d[0] + k];
+            b[k] = X[3 * d[2] + k] - X[3 * d[0] + k];
+        }
+        double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+        double dot = 0;
+        for (int k = 0; k < 3; ++k) dot += n[k] * (cent[k] - fc[k]);
+        if (dot > 0) out.push_back({d[0], d[2], d[1]});
+        else out.push_back({d[0], d[1], d[2]});
+    }
+    return out;
+}
+
+// Volumetric collision patches (PdIpcVolumetricModel.h:114-182): a
+// patch_dim^3 grid over the box of the boundary points, in float; a face goes
+// to the first cell in (x, y, z) order whose closed box holds its centroid.
+// The cell test is a product of per-axis tests, so the first cell is the first
+// index along each axis.
+static void build_patches3(Topology& t, const std::vector<double>& X, int patch_dim) {
+    const float FMAX = std::numeric_limits<float>::infinity();
+    float mn[3] = {FMAX, FMAX, FMAX}, mx[3] = {-FMAX, -FMAX, -FMAX};
+    for (auto& f : t.faces)
+        for (int q = 0; q < 3; ++q)
+            for (int k = 0; k < 3; ++k) {
+                float p = (float)X[3 * f[q] + k];
+                mn[k] = std::min(mn[k], p);
+                mx[k] = std::max(mx[k], p);
+            }
+    const int len = std::max(1, patch_dim);
+    float size[3];
+    for (int k = 0; k < 3; ++k) size[k] = (mx[k] - mn[k]) / (float)len;
+    std::vector<std::vector<int>> pocket((size_t)len * len * len);
+    for (int f = 0; f < t.nf; ++f) {
+        float c[3] = {0.f, 0.f, 0.f};
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) c[a] += (float)X[3 * t.faces[f][k] + a];
+        for (int a = 0; a < 3; ++a) c[a] /= 3.f;
+        int id[3] = {-1, -1, -1};
+        for (int a = 0; a < 3; ++a)
+            for (int r = 0; r < len; ++r) {
+                float b0 = mn[a] + (float)r * size[a], b1 = b0 + size[a];
+                if (c[a] >= b0 && c[a] <= b1) { id[a] = r; break; }
+            }
+        if (id[0] < 0 || id[1] < 0 || id[2] < 0) continue;
+        pocket[((size_t)id[0] * len + id[1]) * len + id[2]].push_back(f);
+    }
+    t.patches.clear();
+    for (auto& p : pocket)
+        if (!p.empty()) t.patches.push_back(p);
+}
+
 struct ModelIn {
     std::vector<double> X;
     std::vector<int> F;
-    int nv = 0, nf = 0;
+    std::vector<int> T;  // 4 per tet (volumetric)
+    int nv = 0, nf = 0, nt = 0;
     bool is_static = false;
-    double density = 0, k_stretch = 0, k_bend = 0, k_pin = 0;
+    bool is_volumetric = false;
+    double density = 0, k_stretch = 0, k_bend = 0, k_pin = 0, k_strain = 0;
     std::vector<int> pins;
     int patch_dim = 10;
 };
+
+// Singular value decomposition F = U diag(s) V^T of a row-major 3x3 matrix with
+// U, V proper rotations, |s0| >= |s1| >= |s2| and the sign of det F carried by
+// s2 (the convention of the reference's GPU SVD, whose result it post-processes
+// in solveVolumetricStrainConstraintKernel, PdIpcGpuFunc.cu:487-525).  One-sided
+// Jacobi (Hestenes): rotate column pairs of A = F (and of V) until orthogonal.
+template <typename R>
+static void svd3_onesided(const R* F, R* U, R* s, R* V) {
+    R A[3][3], W[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) A[i][j] = F[3 * i + j];
+    const R eps = std::numeric_limits<R>::epsilon();
+    for (int sweep = 0; sweep < 40; ++sweep) {
+        bool rotated = false;
+        const int pq[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+        for (auto& pr : pq) {
+            const int p = pr[0], q = pr[1];
+            R al = 0, be = 0, ga = 0;
+            for (int i = 0; i < 3; ++i) {
+                al += A[i][p] * A[i][p];
+                be += A[i][q] * A[i][q];
+                ga += A[i][p] * A[i][q];
+            }
+            if (!(std::fabs(ga) > eps * std::sqrt(al * be))) continue;
+            rotated = true;
+            const R zeta = (be - al) / (R(2) * ga);
+            const R t = (zeta >= 0 ? R(1) : R(-1)) / (std::fabs(zeta) + std::sqrt(R(1) + zeta * zeta));
+            const R c = R(1) / std::sqrt(R(1) + t * t), sn = c * t;
+            for (int i = 0; i < 3; ++i) {
+                const R ap = A[i][p], aq = A[i][q];
+                A[i][p] = c * ap - sn * aq;
+                A[i][q] = sn * ap + c * aq;
+                const R wp = W[i][p], wq = W[i][q];
+                W[i][p] = c * wp - sn * wq;
+                W[i][q] = sn * wp + c * wq;
+            }
+        }
+        if (!rotated) break;
+    }
+    R nrm[3];
+    for (int j = 0; j < 3; ++j) nrm[j] = std::sqrt(A[0][j] * A[0][j] + A[1][j] * A[1][j] + A[2][j] * A[2][j]);
+    int ord[3] = {0, 1, 2};
+    std::sort(ord, ord + 3, [&](int a, int b) { return nrm[a] > nrm[b]; });
+    R Us[3][3], Vs[3][3];
+    for (int j = 0; j < 3; ++j) {
+        s[j] = nrm[ord[j]];
+        for (int i = 0; i < 3; ++i) {
+            Us[i][j] = s[j] > R(0) ? A[i][ord[j]] / s[j] : R(0);
+            Vs[i][j] = W[i][ord[j]];
+        }
+    }
+    auto det3 = [](R M[3][3]) {
+        return M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) - M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+               M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+    };
+    // complete U where singular values vanish
+    if (!(s[1] > R(0))) {  // rank <= 1: any unit vector orthogonal to u0, then the cross product
+        R a[3] = {Us[0][0], Us[1][0], Us[2][0]};
+        if (!(s[0] > R(0))) { a[0] = 1; a[1] = 0; a[2] = 0; for (int i = 0; i < 3; ++i) Us[i][0] = a[i]; }
+        R e[3] = {0, 0, 0};
+        e[std::fabs(a[0]) < R(0.6) ? 0 : 1] = 1;
+        R d = a[0] * e[0] + a[1] * e[1] + a[2] * e[2], b[3], bn = 0;
+        for (int i = 0; i < 3; ++i) { b[i] = e[i] - d * a[i]; bn += b[i] * b[i]; }
+        for (int i = 0; i < 3; ++i) Us[i][1] = b[i] / std::sqrt(bn);
+    }
+    if (!(s[2] > R(0))) {
+        Us[0][2] = Us[1][0] * Us[2][1] - Us[2][0] * Us[1][1];
+        Us[1][2] = Us[2][0] * Us[0][1] - Us[0][0] * Us[2][1];
+        Us[2][2] = Us[0][0] * Us[1][1] - Us[1][0] * Us[0][1];
+    }
+    if (det3(Vs) < 0)  // keep F = U S V^T: flip the last column of both
+        for (int i = 0; i < 3; ++i) { Vs[i][2] = -Vs[i][2]; Us[i][2] = -Us[i][2]; }
+    if (det3(Us) < 0) {  // the sign of det F goes to the smallest singular value
+        for (int i = 0; i < 3; ++i) Us[i][2] = -Us[i][2];
+        s[2] = -s[2];
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) { U[3 * i + j] = Us[i][j]; V[3 * i + j] = Vs[i][j]; }
+}
+
+// solveVolumetricStrainConstraintKernel (PdIpcGpuFunc.cu:439-599): F = Ds Dm^-1,
+// SVD, a negative determinant flipped onto the smallest singular value, the
+// singular values clamped to [0.999, 1.001] (clamp, cu:307-316), R = U S' V^T,
+// and w R G scattered to the tet's four vertices (here returned per vertex).
+template <typename R>
+static void tet_project(const R* x0, const R* x1, const R* x2, const R* x3, const R* idm, R w, R out[4][3]) {
+    R Ds[9];
+    for (int k = 0; k < 3; ++k) {
+        Ds[3 * k + 0] = x1[k] - x0[k];
+        Ds[3 * k + 1] = x2[k] - x0[k];
+        Ds[3 * k + 2] = x3[k] - x0[k];
+    }
+    R F[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) F[3 * i + j] = Ds[3 * i] * idm[j] + Ds[3 * i + 1] * idm[3 + j] + Ds[3 * i + 2] * idm[6 + j];
+    R U[9], sv[3], V[9];
+    svd3_onesided(F, U, sv, V);
+    if (sv[0] * sv[1] * sv[2] < 0) sv[2] = -sv[2];
+    std::sort(sv, sv + 3, [](R a, R b) { return a > b; });
+    R sc[3];
+    for (int k = 0; k < 3; ++k) {
+        R r = sv[k] < R(1.001) ? sv[k] : R(1.001);
+        sc[k] = r < R(0.999) ? R(0.999) : r;
+    }
+    R Rm[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Rm[3 * i + j] = U[3 * i] * sc[0] * V[3 * j] + U[3 * i + 1] * sc[1] * V[3 * j + 1] +
+                                                  U[3 * i + 2] * sc[2] * V[3 * j + 2];
+    R G[3][4];
+    for (int i = 0; i < 3; ++i) {
+        G[i][1] = idm[i];
+        G[i][2] = idm[3 + i];
+        G[i][3] = idm[6 + i];
+        G[i][0] = -(G[i][1] + G[i][2] + G[i][3]);
+    }
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 3; ++r) out[c][r] = w * (Rm[3 * r] * G[0][c] + Rm[3 * r + 1] * G[1][c] + Rm[3 * r + 2] * G[2][c]);
+}
 
 // Morton code of a quantised, centred patch centre.  The reference calls the
 // un-vendored Resorting::MortonCode64(int,int,int) (AipcBvhs.cpp:181); this is
@@ -257,6 +453,11 @@ struct Sim {
     // system off-diagonals N_ij = -A_ij (CSR, ascending columns)
     std::vector<int> nPtr, nCol;
     std::vector<T> nVal;
+    // tet strain constraints: global ids, row-major Dm^-1, weight; vertex -> 4*tet+slot
+    int ntet = 0;
+    std::vector<std::array<int, 4>> tets;
+    std::vector<T> tetIdm, tetW, tetOut;
+    std::vector<int> vtPtr, vtIdx;
     // reference R2 form
     std::vector<int> r2Ptr, r2Col, r2Const, r2First, pathPtr, pathK;
     std::vector<T> pathA, r2Val, r1Op, firstTerm;
@@ -307,16 +508,23 @@ struct Sim {
             auto& m = models[mi];
             Topology& t = topo[mi];
             t.nv = m.nv;
-            t.nf = m.nf;
-            t.faces.resize(m.nf);
-            for (int f = 0; f < m.nf; ++f) t.faces[f] = {m.F[3 * f], m.F[3 * f + 1], m.F[3 * f + 2]};
+            if (m.is_volumetric) {
+                t.faces = tet_surface(m.X, m.T, m.nt);
+                t.nf = (int)t.faces.size();
+            } else {
+                t.nf = m.nf;
+                t.faces.resize(m.nf);
+                for (int f = 0; f < m.nf; ++f) t.faces[f] = {m.F[3 * f], m.F[3 * f + 1], m.F[3 * f + 2]};
+            }
+            if (t.nf == 0) return PDIPC_ERR_ARG;
             build_edges(t);
-            if (!build_ownership(t)) return PDIPC_ERR_ARG;
-            build_patches(t, m.X, m.patch_dim);
+            if (!build_ownership(t, m.is_volumetric)) return PDIPC_ERR_ARG;
+            if (m.is_volumetric) build_patches3(t, m.X, m.patch_dim);
+            else build_patches(t, m.X, m.patch_dim);
             voff[mi] = vo; foff[mi] = fo; eoff[mi] = eo;
             for (int i = 0; i < m.nv; ++i)
                 for (int k = 0; k < 3; ++k) X[3 * (size_t)(vo + i) + k] = (T)m.X[3 * i + k];
-            vo += m.nv; fo += m.nf; eo += (int)t.edges.size();
+            vo += m.nv; fo += t.nf; eo += (int)t.edges.size();
         }
         // --- per-vertex cloth tables (PdIpcClothModel.h:177-328) ---
         invMass.assign(nsim, T(0));
@@ -329,11 +537,70 @@ struct Sim {
         std::vector<double> bendArea(nsim, 0.0);       // A_i * b
         std::vector<std::vector<double>> lboD(nsim);
         std::vector<double> strainD(nsim, 0.0);
+        tets.clear(); tetIdm.clear(); tetW.clear();
+        std::vector<double> tetIdmD, tetWD;
         for (int mi : morder) {
             auto& m = models[mi];
             if (m.is_static) continue;
             Topology& t = topo[mi];
             int o = voff[mi];
+            if (m.is_volumetric) {
+                // node mass = density * sum of incident tet volumes (BaseTetMeshHandle.cpp:107-124)
+                auto P = [&](int i, int k) { return m.X[3 * i + k]; };
+                for (int e = 0; e < m.nt; ++e) {
+                    const int* q = &m.T[4 * e];
+                    double E[3][3];  // rows p_{r+1} - p_0 (setupHessMat cpp:313-318)
+                    for (int r = 0; r < 3; ++r)
+                        for (int k = 0; k < 3; ++k) E[r][k] = P(q[r + 1], k) - P(q[0], k);
+                    double det = E[0][0] * (E[1][1] * E[2][2] - E[1][2] * E[2][1]) -
+                                 E[0][1] * (E[1][0] * E[2][2] - E[1][2] * E[2][0]) +
+                                 E[0][2] * (E[1][0] * E[2][1] - E[1][1] * E[2][0]);
+                    if (det == 0.0) return PDIPC_ERR_ARG;
+                    double vol = std::fabs(det / 6.0);
+                    for (int k = 0; k < 4; ++k) massD[o + q[k]] += vol * m.density;
+                    // rest = E^-1 (Gauss-Jordan); Dm^-1 row-major = rest^T
+                    double a[3][6];
+                    for (int r = 0; r < 3; ++r)
+                        for (int c = 0; c < 6; ++c) a[r][c] = c < 3 ? E[r][c] : (c - 3 == r ? 1.0 : 0.0);
+                    for (int c = 0; c < 3; ++c) {
+                        int piv = c;
+                        for (int r = c + 1; r < 3; ++r) if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+                        for (int k = 0; k < 6; ++k) std::swap(a[c][k], a[piv][k]);
+                        double d = a[c][c];
+                        for (int k = 0; k < 6; ++k) a[c][k] /= d;
+                        for (int r = 0; r < 3; ++r)
+                            if (r != c) {
+                                double f = a[r][c];
+                                for (int k = 0; k < 6; ++k) a[r][k] -= f * a[c][k];
+                            }
+                    }
+                    for (int r = 0; r < 3; ++r)
+                        for (int c = 0; c < 3; ++c) tetIdmD.push_back(a[c][3 + r]);
+                    tets.push_back({o + q[0], o + q[1], o + q[2], o + q[3]});
+                    tetWD.push_back(m.k_strain * vol);
+                }
+                for (int i = 0; i < m.nv; ++i) {
+                    int g = o + i;
+                    if (!(massD[g] > 0.0)) return PDIPC_ERR_ARG;
+                    invMass[g] = (T)(1.0 / massD[g]);
+                    lOff[g] = (int)lNbr.size();
+                    lNum[g] = 1;  // no springs or bending: stencil = self
+                    lNbr.push_back(g);
+                    lStrain.push_back(T(0));
+                    lRest.push_back(T(0));
+                    lLbo.push_back(T(0));
+                    lBend.push_back(T(0));
+                    lboD[g] = {0.0};
+                }
+                for (int p : m.pins) {
+                    if (p < 0 || p >= m.nv) return PDIPC_ERR_ARG;
+                    if (pinFlag[o + p] == -1) {
+                        pinFlag[o + p] = (int)pinStiff.size();
+                        pinStiff.push_back((T)m.k_pin);
+                    }
+                }
+                continue;
+            }
             std::vector<double> area(m.nv, 0.0);
             auto P = [&](int i, int k) { return m.X[3 * i + k]; };
             for (int f = 0; f < m.nf; ++f) {
@@ -453,6 +720,36 @@ struct Sim {
                     else rows[a][b] += v;
                 }
         }
+        // tet strain terms w G^T G (setupHessMat cpp:302-354)
+        ntet = (int)tets.size();
+        for (int e = 0; e < ntet; ++e) {
+            const double* idm = &tetIdmD[9 * (size_t)e];
+            double G[3][4];
+            for (int i = 0; i < 3; ++i) {
+                G[i][1] = idm[i]; G[i][2] = idm[3 + i]; G[i][3] = idm[6 + i];
+                G[i][0] = -(G[i][1] + G[i][2] + G[i][3]);
+            }
+            for (int r = 0; r < 4; ++r)
+                for (int c = 0; c < 4; ++c) {
+                    double v = 0.0;
+                    for (int k = 0; k < 3; ++k) v += G[k][r] * G[k][c];
+                    v *= tetWD[e];
+                    int a = tets[e][r], b = tets[e][c];
+                    if (a == b) diagE[a] += v;
+                    else rows[a][b] += v;
+                }
+        }
+        tetIdm.assign(tetIdmD.begin(), tetIdmD.end());
+        tetW.assign(tetWD.begin(), tetWD.end());
+        vtPtr.assign(nsim + 1, 0);
+        for (auto& q : tets) for (int k = 0; k < 4; ++k) ++vtPtr[q[k] + 1];
+        for (int i = 0; i < nsim; ++i) vtPtr[i + 1] += vtPtr[i];
+        vtIdx.assign(vtPtr[nsim], 0);
+        {
+            std::vector<int> fill(vtPtr.begin(), vtPtr.end() - 1);
+            for (int e = 0; e < ntet; ++e) for (int k = 0; k < 4; ++k) vtIdx[fill[tets[e][k]]++] = 4 * e + k;
+        }
+        tetOut.assign(12 * (size_t)ntet, T(0));
         Delastic.assign(nsim, T(0));
         for (int i = 0; i < nsim; ++i) Delastic[i] = (T)diagE[i];
         nPtr.assign(nsim + 1, 0);
@@ -1056,6 +1353,15 @@ struct Sim {
             for (int k = 0; k < 3; ++k) aq[3 * (size_t)i + k] = a[k];
         }
 #pragma omp parallel for schedule(static) num_threads(threads)
+        for (int e = 0; e < ntet; ++e) {
+            T out[4][3];
+            const auto& q = tets[e];
+            tet_project<T>(&X[3 * (size_t)q[0]], &X[3 * (size_t)q[1]], &X[3 * (size_t)q[2]], &X[3 * (size_t)q[3]],
+                           &tetIdm[9 * (size_t)e], tetW[e], out);
+            for (int c = 0; c < 4; ++c)
+                for (int k = 0; k < 3; ++k) tetOut[12 * (size_t)e + 3 * c + k] = out[c][k];
+        }
+#pragma omp parallel for schedule(static) num_threads(threads)
         for (int i = 0; i < nsim; ++i) {
             int o = lOff[i], n = lNum[i];
             T x[3] = {X[3 * i], X[3 * i + 1], X[3 * i + 2]};
@@ -1076,6 +1382,8 @@ struct Sim {
                 int j = lNbr[o + s];
                 for (int k = 0; k < 3; ++k) r[k] += lBendT[o + s] * aq[3 * (size_t)j + k];
             }
+            for (int q = vtPtr[i]; q < vtPtr[i + 1]; ++q)  // tet projections, ascending tet
+                for (int k = 0; k < 3; ++k) r[k] += tetOut[3 * (size_t)vtIdx[q] + k];
             for (int k = 0; k < 3; ++k) r[k] += collRhs[3 * (size_t)i + k];
             if (pinFlag[i] >= 0) {
                 T ks = pinStiff[pinFlag[i]];
@@ -1315,6 +1623,54 @@ static int add_model(Ctx* c, const double* X, int nv, const int* F, int nf, bool
         s.models.push_back(m);
         return (int)PDIPC_OK;
     });
+}
+
+int orc_add_volumetric(void* h, const double* X, int nv, const int* T, int nt, double density, double k_strain,
+                       const int* pins, int npins, double kp, int pd) {
+    if (!X || !T || nv <= 0 || nt <= 0 || pd <= 0) return PDIPC_ERR_ARG;
+    for (int i = 0; i < 4 * nt; ++i)
+        if (T[i] < 0 || T[i] >= nv) return PDIPC_ERR_ARG;
+    orc::ModelIn m;
+    m.X.assign(X, X + 3 * (size_t)nv);
+    m.T.assign(T, T + 4 * (size_t)nt);
+    m.nv = nv; m.nt = nt; m.is_volumetric = true;
+    m.density = density; m.k_strain = k_strain; m.k_pin = kp; m.patch_dim = pd;
+    if (pins && npins > 0) m.pins.assign(pins, pins + npins);
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        if (s.initialized) return (int)PDIPC_ERR_STATE;
+        s.models.push_back(m);
+        return (int)PDIPC_OK;
+    });
+}
+
+// tet projection of the oracle alone, for the SVD known-answer tests: n tets
+// of positions x (12 doubles each: four vertices), row-major Dm^-1 (9 each),
+// weights w; out receives 12 doubles per tet (w R G, vertex-major).
+int orc_tet_project(int n, const double* x, const double* idm, const double* w, double* out) {
+    for (int e = 0; e < n; ++e) {
+        double o[4][3];
+        const double* p = x + 12 * (size_t)e;
+        orc::tet_project<double>(p, p + 3, p + 6, p + 9, idm + 9 * (size_t)e, w[e], o);
+        for (int c = 0; c < 4; ++c)
+            for (int k = 0; k < 3; ++k) out[12 * (size_t)e + 3 * c + k] = o[c][k];
+    }
+    return PDIPC_OK;
+}
+
+int orc_tet_surface(const double* X, int nv, const int* T, int nt, int* faces, int cap, int* nf) {
+    std::vector<double> x(X, X + 3 * (size_t)nv);
+    std::vector<int> t(T, T + 4 * (size_t)nt);
+    auto f = orc::tet_surface(x, t, nt);
+    *nf = (int)f.size();
+    if ((int)f.size() > cap) return PDIPC_ERR_OVERFLOW;
+    for (size_t i = 0; i < f.size(); ++i)
+        for (int k = 0; k < 3; ++k) faces[3 * i + k] = f[i][k];
+    return PDIPC_OK;
+}
+
+int orc_svd3(const double* F, double* U, double* s, double* V) {
+    orc::svd3_onesided<double>(F, U, s, V);
+    return PDIPC_OK;
 }
 
 int orc_add_cloth(void* h, const double* X, int nv, const int* F, int nf, double density, double ks, double kb,

@@ -176,6 +176,53 @@ pdipc_status pdipc_add_cloth(pdipc_ctx* ctx, const double* X, int nv, const int*
     return add_model(ctx, X, nv, F, nf, false, density, k_stretch, k_bend, pins, npins, k_pin, patch_dim);
 }
 
+pdipc_status pdipc_add_volumetric(pdipc_ctx* ctx, const double* X, int nv, const int* T, int nt, double density,
+                                  double k_strain, double k_volume, const int* pins, int npins, double k_pin,
+                                  int patch_dim) {
+    if (!ctx) return PDIPC_ERR_ARG;
+    if (ctx->initialized) return fail(ctx, PDIPC_ERR_STATE, "models must be added before initialize");
+    if (!X || !T || nv <= 0 || nt <= 0) return fail(ctx, PDIPC_ERR_ARG, "empty tetrahedral mesh");
+    if (npins < 0 || (npins > 0 && !pins)) return fail(ctx, PDIPC_ERR_ARG, "bad pin list");
+    if (patch_dim < 1) return fail(ctx, PDIPC_ERR_ARG, "patch_dim must be positive");
+    if (!(density > 0.0) || !(k_strain >= 0.0) || !(k_pin >= 0.0))
+        return fail(ctx, PDIPC_ERR_ARG, "density must be positive and stiffnesses non-negative");
+    for (int i = 0; i < 4 * nt; ++i)
+        if (T[i] < 0 || T[i] >= nv) return fail(ctx, PDIPC_ERR_ARG, "tet index out of range");
+    for (int i = 0; i < npins; ++i)
+        if (pins[i] < 0 || pins[i] >= nv) return fail(ctx, PDIPC_ERR_ARG, "pin index out of range");
+    return guarded(ctx, [&]() {
+        pdipc::ModelInput m;
+        m.X.assign(X, X + 3 * (size_t)nv);
+        m.T.assign(T, T + 4 * (size_t)nt);
+        m.nv = nv;
+        m.nt = nt;
+        m.is_volumetric = true;
+        m.density = density;
+        m.k_strain = k_strain;
+        m.k_volume = k_volume;
+        m.k_pin = k_pin;
+        if (npins > 0) m.pins.assign(pins, pins + npins);
+        m.patch_dim = patch_dim;
+        ctx->models.push_back(std::move(m));
+        return PDIPC_OK;
+    });
+}
+
+pdipc_status pdipc_tet_surface(const double* X, int nv, const int* T, int nt, int* faces, int cap_faces,
+                               int* n_faces) {
+    if (!X || !T || !n_faces || nv <= 0 || nt <= 0 || (cap_faces > 0 && !faces)) return PDIPC_ERR_ARG;
+    try {
+        std::vector<int> f;
+        if (!pdipc::tet_boundary_faces(X, nv, T, nt, f).empty()) return PDIPC_ERR_ARG;
+        *n_faces = (int)f.size() / 3;
+        if (*n_faces > cap_faces) return PDIPC_ERR_OVERFLOW;
+        std::copy(f.begin(), f.end(), faces);
+        return PDIPC_OK;
+    } catch (const std::bad_alloc&) {
+        return PDIPC_ERR_ALLOC;
+    }
+}
+
 pdipc_status pdipc_add_static(pdipc_ctx* ctx, const double* X, int nv, const int* F, int nf, int patch_dim) {
     return add_model(ctx, X, nv, F, nf, true, 0.0, 0.0, 0.0, nullptr, 0, 0.0, patch_dim);
 }

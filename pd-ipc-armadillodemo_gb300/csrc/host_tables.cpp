@@ -11,6 +11,7 @@
 #include "host_tables.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <limits>
 #include <utility>
@@ -89,9 +90,115 @@ void grid_patches(const double* X, int nv, const int* F, int nf, int patch_dim,
         if (!cl.empty()) patches.push_back(std::move(cl));
 }
 
+// Volumetric models: a patch_dim^3 grid over the box of the boundary points,
+// each boundary face in the first closed cell (x-major, then y, then z) that
+// holds its centroid (PdIpcVolumetricModel::setCollisionPatches,
+// PdIpcVolumetricModel.h:114-182; FP32 as the reference).  The first cell of
+// a product of per-axis interval tests is the per-axis first index.
+void grid3_patches(const double* X, int nv, const int* F, int nf, int patch_dim,
+                   std::vector<std::vector<int>>& patches) {
+    const float inf = std::numeric_limits<float>::infinity();
+    float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+    std::vector<char> on(nv, 0);
+    for (int q = 0; q < 3 * nf; ++q) on[F[q]] = 1;
+    for (int i = 0; i < nv; ++i)
+        if (on[i])
+            for (int k = 0; k < 3; ++k) {
+                float p = (float)X[3 * i + k];
+                lo[k] = std::min(lo[k], p);
+                hi[k] = std::max(hi[k], p);
+            }
+    const int len = std::max(1, patch_dim);
+    float step[3];
+    for (int k = 0; k < 3; ++k) step[k] = (hi[k] - lo[k]) / (float)len;
+    auto first_index = [&](float cv, float lo0, float s) -> int {
+        int guess = (s > 0.f) ? (int)std::floor((cv - lo0) / s) : 0;
+        int start = std::max(0, std::min(len - 1, guess) - 1);
+        for (int r = start; r < len && r <= guess + 1; ++r) {
+            const float b0 = lo0 + (float)r * s, b1 = b0 + s;
+            if (cv >= b0 && cv <= b1) return r;
+        }
+        return -1;
+    };
+    std::vector<std::vector<int>> cells((size_t)len * len * len);
+    for (int f = 0; f < nf; ++f) {
+        float c[3] = {0.f, 0.f, 0.f};
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) c[a] += (float)X[3 * F[3 * f + k] + a];
+        for (int a = 0; a < 3; ++a) c[a] /= 3.f;
+        int id[3];
+        bool ok = true;
+        for (int a = 0; a < 3 && ok; ++a) ok = (id[a] = first_index(c[a], lo[a], step[a])) >= 0;
+        if (ok) cells[((size_t)id[0] * len + id[1]) * len + id[2]].push_back(f);
+    }
+    patches.clear();
+    for (auto& cl : cells)
+        if (!cl.empty()) patches.push_back(std::move(cl));
+}
+
+std::string build_topology(const double* X, int nv, const int* F, int nf, int patch_dim, bool volumetric,
+                           MeshTopology& t);
+
 }  // namespace
 
 std::string build_mesh_topology(const double* X, int nv, const int* F, int nf, int patch_dim, MeshTopology& t) {
+    return build_topology(X, nv, F, nf, patch_dim, false, t);
+}
+
+std::string tet_boundary_faces(const double* X, int nv, const int* T, int nt, std::vector<int>& faces) {
+    static const int kFace[4][3] = {{3, 1, 0}, {3, 2, 1}, {3, 0, 2}, {2, 1, 0}};  // PdIpcVolumetricModel.h:32-36
+    struct Rec {
+        std::array<int, 3> key;
+        int f[3];
+        int tet;
+    };
+    std::vector<Rec> recs;
+    recs.reserve(4 * (size_t)nt);
+    for (int e = 0; e < nt; ++e) {
+        for (int q = 0; q < 4; ++q)
+            if (T[4 * e + q] < 0 || T[4 * e + q] >= nv) return "tet index out of range";
+        for (int k = 0; k < 4; ++k) {
+            Rec r;
+            for (int j = 0; j < 3; ++j) r.f[j] = T[4 * e + kFace[k][j]];
+            r.key = {r.f[0], r.f[1], r.f[2]};
+            std::sort(r.key.begin(), r.key.end());
+            r.tet = e;
+            recs.push_back(r);
+        }
+    }
+    std::stable_sort(recs.begin(), recs.end(), [](const Rec& a, const Rec& b) { return a.key < b.key; });
+    faces.clear();
+    for (size_t a = 0; a < recs.size();) {
+        size_t b = a;
+        while (b < recs.size() && recs[b].key == recs[a].key) ++b;
+        if (b - a == 1) {
+            const Rec& r = recs[a];
+            auto P = [&](int i, int k) { return X[3 * i + k]; };
+            double cent[3] = {0, 0, 0}, fc[3] = {0, 0, 0};
+            for (int k = 0; k < 3; ++k) {
+                for (int q = 0; q < 4; ++q) cent[k] += P(T[4 * r.tet + q], k) / 4.0;
+                for (int q = 0; q < 3; ++q) fc[k] += P(r.f[q], k) / 3.0;
+            }
+            double u[3], v[3];
+            for (int k = 0; k < 3; ++k) {
+                u[k] = P(r.f[1], k) - P(r.f[0], k);
+                v[k] = P(r.f[2], k) - P(r.f[0], k);
+            }
+            const double n[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+            const double dot = n[0] * (cent[0] - fc[0]) + n[1] * (cent[1] - fc[1]) + n[2] * (cent[2] - fc[2]);
+            if (dot > 0) faces.insert(faces.end(), {r.f[0], r.f[2], r.f[1]});
+            else faces.insert(faces.end(), {r.f[0], r.f[1], r.f[2]});
+        }
+        a = b;
+    }
+    if (faces.empty()) return "tetrahedral mesh has no boundary face";
+    return "";
+}
+
+namespace {
+
+std::string build_topology(const double* X, int nv, const int* F, int nf, int patch_dim, bool volumetric,
+                           MeshTopology& t) {
     if (nv <= 0 || nf <= 0) return "empty mesh";
     for (int i = 0; i < 3 * nf; ++i)
         if (F[i] < 0 || F[i] >= nv) return "face index out of range";
@@ -136,15 +243,21 @@ std::string build_mesh_topology(const double* X, int nv, const int* F, int nf, i
     t.face_points_own.assign(nf, {});
     for (int p = 0; p < nv; ++p) {
         const auto& fl = point_faces[p];
-        if (fl.empty()) return "mesh has an isolated vertex";
+        if (fl.empty()) {
+            if (volumetric) continue;  // interior node of a tetrahedral mesh: not on the surface
+            return "mesh has an isolated vertex";
+        }
         int best = fl[0];
         for (size_t q = 1; q < fl.size(); ++q)
             if (t.face_points_own[fl[q]].size() < t.face_points_own[best].size()) best = fl[q];
         t.face_points_own[best].push_back(p);
     }
-    grid_patches(X, nv, F, nf, patch_dim, t.patches);
+    if (volumetric) grid3_patches(X, nv, F, nf, patch_dim, t.patches);
+    else grid_patches(X, nv, F, nf, patch_dim, t.patches);
     return "";
 }
+
+}  // namespace
 
 std::string build_host_tables(const std::vector<ModelInput>& models, double gravity, HostTables& H) {
     H = HostTables();
@@ -157,17 +270,24 @@ std::string build_host_tables(const std::vector<ModelInput>& models, double grav
     if (nclothModels == 0) return "no cloth model added";
 
     std::vector<MeshTopology> topo(models.size());
+    std::vector<std::vector<int>> mF(models.size());  // collision faces: given, or a tet mesh's boundary
     std::vector<int> vbase(models.size()), fbase(models.size()), ebase(models.size());
     int nv = 0, nf = 0, ne = 0, nsim = 0;
     for (int q = 0; q < (int)order.size(); ++q) {
         const ModelInput& m = models[order[q]];
-        std::string err = build_mesh_topology(m.X.data(), m.nv, m.F.data(), m.nf, m.patch_dim, topo[order[q]]);
+        std::string err;
+        if (m.is_volumetric) err = tet_boundary_faces(m.X.data(), m.nv, m.T.data(), m.nt, mF[order[q]]);
+        else mF[order[q]] = m.F;
+        if (!err.empty()) return err;
+        const int mnf = (int)mF[order[q]].size() / 3;
+        err = build_topology(m.X.data(), m.nv, mF[order[q]].data(), mnf, m.patch_dim, m.is_volumetric,
+                             topo[order[q]]);
         if (!err.empty()) return err;
         vbase[order[q]] = nv;
         fbase[order[q]] = nf;
         ebase[order[q]] = ne;
         nv += m.nv;
-        nf += m.nf;
+        nf += mnf;
         ne += (int)topo[order[q]].edges.size() / 2;
         if (!m.is_static) nsim += m.nv;
     }
@@ -191,6 +311,26 @@ std::string build_host_tables(const std::vector<ModelInput>& models, double grav
         const MeshTopology& t = topo[mi];
         const int o = vbase[mi];
         auto P = [&](int i, int k) { return m.X[3 * i + k]; };
+        if (m.is_volumetric) {
+            // node mass = density * sum of the incident tets' volumes, no 1/4
+            // (BaseTetMeshHandle::computeVolume, BaseTetMeshHandle.cpp:107-124;
+            // PdIpcVolumetricModel.h:224-233); no springs or bending: stencil = self
+            for (int e = 0; e < m.nt; ++e) {
+                const int* Tv = &m.T[4 * e];
+                double D[9];
+                for (int r = 0; r < 3; ++r)
+                    for (int k = 0; k < 3; ++k) D[3 * r + k] = P(Tv[r + 1], k) - P(Tv[0], k);
+                const double det = D[0] * (D[4] * D[8] - D[5] * D[7]) - D[1] * (D[3] * D[8] - D[5] * D[6]) +
+                                   D[2] * (D[3] * D[7] - D[4] * D[6]);
+                const double vol = std::fabs(det / 6.0);
+                for (int k = 0; k < 4; ++k) H.mass[o + Tv[k]] += vol * m.density;
+            }
+            for (int i = 0; i < m.nv; ++i) {
+                if (!(H.mass[o + i] > 0.0)) return "tetrahedral mesh has a node in no tet";
+                H.lPtr[o + i + 1] = 1;
+            }
+            continue;
+        }
         std::vector<double> area(m.nv, 0.0);
         for (int f = 0; f < m.nf; ++f) {  // TriangleArea (Commom/GeometryComputation.cpp:3-6)
             const int* Fv = &m.F[3 * f];
@@ -226,6 +366,38 @@ std::string build_host_tables(const std::vector<ModelInput>& models, double grav
         const MeshTopology& t = topo[mi];
         const int o = vbase[mi];
         auto P = [&](int i, int k) { return m.X[3 * i + k]; };
+        if (m.is_volumetric) {
+            for (int i = 0; i < m.nv; ++i) H.lNbr[H.lPtr[o + i]] = o + i;  // lLbo, lBend stay 0
+            for (int p : m.pins) {
+                if (p < 0 || p >= m.nv) return "pin index out of range";
+                if (H.pinSlot[o + p] == -1) {
+                    H.pinSlot[o + p] = (int)H.pinK.size();
+                    H.pinK.push_back(m.k_pin);
+                }
+            }
+            // strain constraints (setupHessMat, PdIpcSimulator.cpp:302-354): rest = (rows
+            // p1-p0, p2-p0, p3-p0)^-1, weight k_strain * |det| / 6
+            for (int e = 0; e < m.nt; ++e) {
+                const int* Tv = &m.T[4 * e];
+                double D[9];  // row r = p_{r+1} - p_0
+                for (int r = 0; r < 3; ++r)
+                    for (int k = 0; k < 3; ++k) D[3 * r + k] = P(Tv[r + 1], k) - P(Tv[0], k);
+                const double c00 = D[4] * D[8] - D[5] * D[7], c01 = D[5] * D[6] - D[3] * D[8],
+                             c02 = D[3] * D[7] - D[4] * D[6];
+                const double det = D[0] * c00 + D[1] * c01 + D[2] * c02;
+                if (!(std::fabs(det) > 0.0)) return "degenerate tetrahedron";
+                // inverse of the row matrix D: inv[r][c] = cofactor[c][r] / det
+                const double inv[9] = {c00 / det, (D[2] * D[7] - D[1] * D[8]) / det, (D[1] * D[5] - D[2] * D[4]) / det,
+                                       c01 / det, (D[0] * D[8] - D[2] * D[6]) / det, (D[2] * D[3] - D[0] * D[5]) / det,
+                                       c02 / det, (D[1] * D[6] - D[0] * D[7]) / det, (D[0] * D[4] - D[1] * D[3]) / det};
+                // Dm^-1 row-major = inv transposed (rest's column-major data in the reference)
+                for (int r = 0; r < 3; ++r)
+                    for (int c = 0; c < 3; ++c) H.tetIdm.push_back(inv[3 * c + r]);
+                for (int k = 0; k < 4; ++k) H.tets.push_back(o + Tv[k]);
+                H.tetW.push_back(m.k_strain * std::fabs(det / 6.0));
+            }
+            continue;
+        }
         // area and cotangent weights: -1/2 sum of cot of the angles opposite each edge
         std::vector<double> area(m.nv, 0.0);
         for (int f = 0; f < m.nf; ++f) {
@@ -328,6 +500,38 @@ std::string build_host_tables(const std::vector<ModelInput>& models, double grav
                 else rows[a].push_back({b, v});
             }
     }
+    // tet strain terms: w G^T G with G = [-sum_k Dm^-T(:,k) | Dm^-T] (3 x 4)
+    H.ntet = (int)H.tetW.size();
+    for (int e = 0; e < H.ntet; ++e) {
+        const double* idm = &H.tetIdm[9 * (size_t)e];
+        double G[3][4];
+        for (int i = 0; i < 3; ++i) {
+            G[i][1] = idm[i];
+            G[i][2] = idm[3 + i];
+            G[i][3] = idm[6 + i];
+            G[i][0] = -(G[i][1] + G[i][2] + G[i][3]);
+        }
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) {
+                double v = 0.0;
+                for (int k = 0; k < 3; ++k) v += G[k][r] * G[k][c];
+                v *= H.tetW[e];
+                const int a = H.tets[4 * (size_t)e + r], b = H.tets[4 * (size_t)e + c];
+                if (a == b) H.Delastic[a] += v;
+                else rows[a].push_back({b, v});
+            }
+    }
+    // vertex -> (tet, slot) incidence, ascending tet
+    H.vtPtr.assign(nsim + 1, 0);
+    for (int e = 0; e < H.ntet; ++e)
+        for (int k = 0; k < 4; ++k) ++H.vtPtr[H.tets[4 * (size_t)e + k] + 1];
+    for (int i = 0; i < nsim; ++i) H.vtPtr[i + 1] += H.vtPtr[i];
+    H.vtIdx.assign(H.vtPtr[nsim], 0);
+    {
+        std::vector<int> fill(H.vtPtr.begin(), H.vtPtr.end() - 1);
+        for (int e = 0; e < H.ntet; ++e)
+            for (int k = 0; k < 4; ++k) H.vtIdx[fill[H.tets[4 * (size_t)e + k]]++] = (e << 2) | k;
+    }
     H.nPtr.assign(nsim + 1, 0);
     for (int i = 0; i < nsim; ++i) {
         auto& R = rows[i];
@@ -358,9 +562,9 @@ std::string build_host_tables(const std::vector<ModelInput>& models, double grav
     for (int mi : order) {
         const ModelInput& m = models[mi];
         const MeshTopology& t = topo[mi];
+        const std::vector<int>& F = mF[mi];
         const int o = vbase[mi], fo = fbase[mi], eo = ebase[mi];
-        for (int f = 0; f < m.nf; ++f)
-            for (int k = 0; k < 3; ++k) H.faces.push_back(m.F[3 * f + k] + o);
+        for (size_t q = 0; q < F.size(); ++q) H.faces.push_back(F[q] + o);
         for (size_t q = 0; q < t.edges.size(); ++q) H.edges.push_back(t.edges[q] + o);
         std::vector<int> es, ps, xs;
         for (const auto& patch : t.patches) {
@@ -371,7 +575,7 @@ std::string build_host_tables(const std::vector<ModelInput>& models, double grav
                 H.pfIdx.push_back(f + fo);
                 for (int e : t.face_edges_own[f]) es.push_back(e + eo);
                 for (int p : t.face_points_own[f]) ps.push_back(p + o);
-                for (int k = 0; k < 3; ++k) xs.push_back(m.F[3 * f + k] + o);
+                for (int k = 0; k < 3; ++k) xs.push_back(F[3 * f + k] + o);
             }
             for (auto* vv : {&es, &ps, &xs}) {
                 std::sort(vv->begin(), vv->end());

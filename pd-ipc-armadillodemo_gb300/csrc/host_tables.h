@@ -10,10 +10,13 @@ namespace pdipc {
 
 struct ModelInput {
     std::vector<double> X;  // 3*nv
-    std::vector<int> F;     // 3*nf
-    int nv = 0, nf = 0;
+    std::vector<int> F;     // 3*nf (cloth, static); the boundary surface is derived for a volumetric model
+    std::vector<int> T;     // 4*nt tetrahedra (volumetric model)
+    int nv = 0, nf = 0, nt = 0;
     bool is_static = false;
+    bool is_volumetric = false;
     double density = 0, k_stretch = 0, k_bend = 0, k_pin = 0;
+    double k_strain = 0, k_volume = 0;  // volumetric: strain and (unused by the reference) volume stiffness
     std::vector<int> pins;
     int patch_dim = 10;
 };
@@ -35,6 +38,15 @@ struct HostTables {
     // local-step stencil per simulated vertex: [self, neighbours ascending]
     std::vector<int> lPtr, lNbr;
     std::vector<double> lRest, lLbo, lBend, lBendT;
+
+    // tetrahedral strain constraints (solveVolumetricStrainConstraintKernel,
+    // PdIpcGpuFunc.cu:439-599): global vertex ids, row-major Dm^-1 (9 per tet),
+    // weight k_strain * |V|; vertex -> (tet << 2 | slot) incidence, ascending tet
+    int ntet = 0;
+    std::vector<int> tets;        // 4 per tet
+    std::vector<double> tetIdm;   // 9 per tet
+    std::vector<double> tetW;
+    std::vector<int> vtPtr, vtIdx;
 
     // off-diagonal system matrix N = -A_offdiag, CSR with ascending columns
     std::vector<int> nPtr, nCol;
@@ -66,5 +78,10 @@ struct MeshTopology {
     std::vector<std::vector<int>> patches;         // faces of each non-empty grid cell
 };
 std::string build_mesh_topology(const double* X, int nv, const int* F, int nf, int patch_dim, MeshTopology& t);
+
+// Boundary surface of a tetrahedral mesh: faces of exactly one tet, turned to
+// face away from that tet's centroid (PdIpcVolumetricModel::registerBoundaryInfo,
+// PdIpcVolumetricModel.h:27-112), in ascending order of their sorted vertex triple.
+std::string tet_boundary_faces(const double* X, int nv, const int* T, int nt, std::vector<int>& faces);
 
 }  // namespace pdipc

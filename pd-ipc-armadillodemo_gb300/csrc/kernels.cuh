@@ -65,6 +65,17 @@ struct Dev {
     T* Strain = nullptr;     // per vertex
     T* CurvNorm = nullptr;   // per vertex
 
+    // tetrahedral strain constraints: vertices, row-major Dm^-1 (9 per tet),
+    // weights; per-tet projections w R G (4 per tet, vertex-major), gathered
+    // per vertex through the incidence list vtIdx = 4 tet + slot (ascending tet)
+    int ntet = 0;
+    int4* Tets = nullptr;
+    T* TetIdm = nullptr;
+    T* TetW = nullptr;
+    V4<T>* TetOut = nullptr;
+    int* vtPtr = nullptr;
+    int* vtIdx = nullptr;
+
     // N = -offdiag(A) in SELL-32: slice s holds rows [32 s, 32 s + 32); entry k
     // of lane r sits at sOff[s] + 32 k + r; sLen[s] entries per row.
     int nslice = 0;
@@ -131,6 +142,9 @@ template <typename T, typename TC>
 void launch_predict(const Dev<T, TC>& d, TC dt, cudaStream_t s);
 template <typename T, typename TC>
 void launch_diag(const Dev<T, TC>& d, cudaStream_t s);
+// tet strain projections of the current positions into TetOut (no-op without tets)
+template <typename T, typename TC>
+void launch_tet_project(const Dev<T, TC>& d, cudaStream_t s);
 template <typename T, typename TC>
 void launch_local_aq(const Dev<T, TC>& d, cudaStream_t s);
 // local step right-hand side fused with the first J sweep (Y = S(P))

@@ -18,6 +18,7 @@
 #include <type_traits>
 
 #include "kernels.cuh"
+#include "svd3.cuh"
 
 namespace pdipc {
 
@@ -90,6 +91,48 @@ __global__ void k_diag(int nsim, const T* __restrict__ De, const T* __restrict__
     InvD[i] = T(1) / d;
 }
 
+// Tet strain projection (solveVolumetricStrainConstraintKernel,
+// PdIpcGpuFunc.cu:439-599), one thread per tet; the four vertex contributions
+// w R G go to TetOut and are gathered per vertex by the local-step kernels
+// (the reference scatters them with atomics).  Edge vectors come from the
+// float-float mirror in the correction form.
+template <typename T, typename S>
+__global__ void k_tet_project(int ntet, const int4* __restrict__ Tets, const T* __restrict__ Idm,
+                              const T* __restrict__ W, const V4<S>* __restrict__ P, const V4<T>* __restrict__ Ph,
+                              const V4<T>* __restrict__ Pl, V4<T>* __restrict__ Out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ntet) return;
+    const int4 q = Tets[e];
+    const int id[4] = {q.x, q.y, q.z, q.w};
+    T Ds[3][3];
+    if constexpr (kMirror<T, S>) {
+        const V4<T> h0 = ld4(Ph, id[0]), l0 = ld4(Pl, id[0]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const V4<T> h = ld4(Ph, id[c + 1]), l = ld4(Pl, id[c + 1]);
+            Ds[0][c] = diff_ff(h.x, l.x, h0.x, l0.x);
+            Ds[1][c] = diff_ff(h.y, l.y, h0.y, l0.y);
+            Ds[2][c] = diff_ff(h.z, l.z, h0.z, l0.z);
+        }
+    } else {
+        const V4<S> x0 = ld4(P, id[0]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const V4<S> x = ld4(P, id[c + 1]);
+            Ds[0][c] = x.x - x0.x;
+            Ds[1][c] = x.y - x0.y;
+            Ds[2][c] = x.z - x0.z;
+        }
+    }
+    T idm[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) idm[k] = __ldg(Idm + 9 * (size_t)e + k);
+    T out[4][3];
+    svd::tet_project<T>(Ds, idm, __ldg(W + e), out);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) Out[4 * (size_t)e + c] = V4<T>{out[c][0], out[c][1], out[c][2], T(0)};
+}
+
 // Curvature vector aq_i = sum_k lbo_ik x_k, rescaled to the rest norm
 // (PdIpcGpuFunc.cu:664-699).
 template <typename T>
@@ -149,7 +192,8 @@ __global__ void __launch_bounds__(kBlock) k_local_rhs_sweep(
     const T* __restrict__ Strain, const V4<T>* __restrict__ Aq, const V4<T>* __restrict__ Rhs0,
     const V4<T>* __restrict__ CollRhs, const V4<T>* __restrict__ PinRhs, const T* __restrict__ InvD,
     const int* __restrict__ sOff, const int* __restrict__ sLen, const int* __restrict__ sCol,
-    const T* __restrict__ sVal, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
+    const T* __restrict__ sVal, const int* __restrict__ vtPtr, const int* __restrict__ vtIdx,
+    const V4<T>* __restrict__ TetOut, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
     const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
@@ -179,6 +223,13 @@ __global__ void __launch_bounds__(kBlock) k_local_rhs_sweep(
         r_1 += bt * ak.y;
         r_2 += bt * ak.z;
     }
+    if (vtPtr)
+        for (int q = __ldg(vtPtr + i); q < __ldg(vtPtr + i + 1); ++q) {  // tet projections, ascending tet
+            const V4<T> t = ld4(TetOut, __ldg(vtIdx + q));
+            r_0 += t.x;
+            r_1 += t.y;
+            r_2 += t.z;
+        }
     const V4<T> c = ld4(CollRhs, i);
     r_0 += c.x;
     r_1 += c.y;
@@ -247,7 +298,8 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
     const T* __restrict__ lBend, const T* __restrict__ lBendT, const T* __restrict__ Strain,
     const V4<T>* __restrict__ Aq, const T* __restrict__ InvD,
     const int* __restrict__ sOff, const int* __restrict__ sLen, const int* __restrict__ sCol,
-    const T* __restrict__ sVal, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
+    const T* __restrict__ sVal, const int* __restrict__ vtPtr, const int* __restrict__ vtIdx,
+    const V4<T>* __restrict__ TetOut, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
     const V4<S> x = ld4(P, i);
@@ -306,6 +358,13 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
             r2.add(bt * ak.z);
         }
     }
+    if (vtPtr)
+        for (int q = __ldg(vtPtr + i); q < __ldg(vtPtr + i + 1); ++q) {  // tet projections w R G
+            const V4<T> t = ld4(TetOut, __ldg(vtIdx + q));
+            r0.add(t.x);
+            r1.add(t.y);
+            r2.add(t.z);
+        }
     {   // sum_j N_ij (x_j - x_i)
         const int sl = i >> 5, lane = i & 31;
         const int base = __ldg(sOff + sl) + lane;
@@ -493,6 +552,12 @@ void launch_diag(const Dev<T, TC>& d, cudaStream_t s) {
     k_diag<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Delastic, d.Dinert, d.CollDiag, d.InvD);
 }
 template <typename T, typename TC>
+void launch_tet_project(const Dev<T, TC>& d, cudaStream_t s) {
+    if (d.ntet == 0) return;
+    k_tet_project<T, TC><<<blocks_for(d.ntet, 128), 128, 0, s>>>(d.ntet, d.Tets, d.TetIdm, d.TetW, d.P, d.Ph, d.Pl,
+                                                                d.TetOut);
+}
+template <typename T, typename TC>
 void launch_local_aq(const Dev<T, TC>& d, cudaStream_t s) {
     if constexpr (correction_form<T, TC>())
         k_local_aq_rel<<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Ph, d.Pl, d.lPtr, d.lNbr, d.lLbo,
@@ -506,7 +571,7 @@ void launch_local_residual(const Dev<T, TC>& d, T relax, cudaStream_t s) {
         k_local_residual<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(
             d.nsim, relax, d.P, d.Ph, d.Pl, d.Pold, d.Xrest, d.Rhs0, d.Dinert, d.CollDiag, d.CollRhs, d.PinFlag,
             d.PinK, d.lPtr, d.lNbr, d.lRest, d.lBend, d.lBendT, d.Strain, d.Aq, d.InvD, d.sOff, d.sLen, d.sCol,
-            d.sVal, d.Rhs, d.Y);
+            d.sVal, d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs, d.Y);
     }
 }
 template <typename T, typename TC>
@@ -535,7 +600,8 @@ void launch_local_rhs_sweep(const Dev<T, TC>& d, T relax, cudaStream_t s) {
     if constexpr (std::is_same<T, TC>::value)
         k_local_rhs_sweep<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(
             d.nsim, relax, d.P, d.lPtr, d.lNbr, d.lRest, d.lBend, d.lBendT, d.Strain, d.Aq, d.Rhs0, d.CollRhs,
-            d.PinRhs, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal, d.Rhs, d.Y);
+            d.PinRhs, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal, d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs,
+            d.Y);
 }
 template <typename T, typename TC>
 void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T>* out, T relax, T omega,
@@ -575,6 +641,7 @@ void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {
 #define PDIPC_INST_PD(T, TC)                                                                                 \
     template void launch_predict<T, TC>(const Dev<T, TC>&, TC, cudaStream_t);                                 \
     template void launch_diag<T, TC>(const Dev<T, TC>&, cudaStream_t);                                       \
+    template void launch_tet_project<T, TC>(const Dev<T, TC>&, cudaStream_t);                                \
     template void launch_local_aq<T, TC>(const Dev<T, TC>&, cudaStream_t);                                   \
     template void launch_local_rhs_sweep<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                         \
     template void launch_local_residual<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                          \

@@ -160,6 +160,20 @@ public:
         for (int i = 0; i < ns; ++i) cm[i] = (TC)(T)H.collMassSim[i];
         PD_CK(up(d.CollMass, cm));
 
+        // ---- tetrahedral strain constraints ----
+        d.ntet = H.ntet;
+        if (d.ntet > 0) {
+            std::vector<int4> tets(d.ntet);
+            for (int e = 0; e < d.ntet; ++e)
+                tets[e] = make_int4(H.tets[4 * e], H.tets[4 * e + 1], H.tets[4 * e + 2], H.tets[4 * e + 3]);
+            PD_CK(up(d.Tets, tets));
+            PD_CK(up(d.TetIdm, conv(H.tetIdm)));
+            PD_CK(up(d.TetW, conv(H.tetW)));
+            PD_CK(zeros(d.TetOut, 4 * (size_t)d.ntet));
+            PD_CK(up(d.vtPtr, H.vtPtr));
+            PD_CK(up(d.vtIdx, H.vtIdx));
+        }
+
         // ---- local-step stencils ----
         PD_CK(up(d.lPtr, H.lPtr));
         PD_CK(up(d.lNbr, H.lNbr));
@@ -592,7 +606,9 @@ private:
     pdipc_status plan_persistent(const HostTables& H, const std::vector<int>& soff, const std::vector<int>& slen,
                                  std::string& err) {
         plan_ = PersistPlan();
-        if (!std::is_same<T, float>::value || !prm_.persistent || c_.cheby >= kMaxCheby) return PDIPC_OK;
+        // the persistent solve covers cloth stencils only: tet models take the per-sweep path
+        if (!std::is_same<T, float>::value || !prm_.persistent || c_.cheby >= kMaxCheby || H.ntet > 0)
+            return PDIPC_OK;
         Dev<T, TC>& d = d_;
         const int ns = d.nsim, nsl = d.nslice;
         int dev = 0, nsm = 0, smem_optin = 0, coop = 0;
@@ -903,6 +919,8 @@ private:
         ++k;
         for (int lg = 0; lg < c_.lg; ++lg) {
             launch_local_aq(d, s_);
+            launch_tet_project(d, s_);
+            k += d.ntet > 0;
             launch_local_residual(d, w, s_);
             launch_sweep_delta<T, TC>(d, c_.cheby == 1 ? 4 : 0, d.Y, nullptr, d.B, w, T(0), s_);
             k += 3;
@@ -934,6 +952,8 @@ private:
         ++k;
         for (int lg = 0; lg < c_.lg; ++lg) {
             launch_local_aq(d, s_);
+            launch_tet_project(d, s_);
+            k += d.ntet > 0;
             launch_local_rhs_sweep(d, w, s_);
             launch_sweep<T, TC>(d, d.Y, nullptr, c_.cheby == 1 ? d.P : d.B, w, T(0), s_);
             k += 3;

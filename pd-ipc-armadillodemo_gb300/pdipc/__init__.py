@@ -14,8 +14,8 @@ import os
 
 import numpy as np
 
-from .abi import (PDIPC_ERR_CUDA, PDIPC_ERR_OVERFLOW, PDIPC_OK, PRECISIONS, STATUS_NAMES, Params, Stats,  # noqa: F401
-                  default_params, params_for_scene)
+from .abi import (PDIPC_ERR_CUDA, PDIPC_ERR_OVERFLOW, PDIPC_OK, PRECISIONS, STATUS_NAMES, Params,  # noqa: F401
+                  SceneModel, Stats, default_params, params_for_scene)
 from . import scenes  # noqa: F401
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -33,11 +33,13 @@ EXPORTS = [
     "pdipc_reset", "pdipc_get_stats", "pdipc_save", "pdipc_load", "pdipc_destroy", "pdipc_status_string",
     "pdipc_last_error", "pdipc_abi_version", "pdipc_stage_broadphase", "pdipc_stage_morton", "pdipc_stage_toi",
     "pdipc_stage_contact", "pdipc_stage_pd", "pdipc_mesh_topology",
-    "pdipc_stage_sweep_timing", "pdipc_stage_toi_noalloc",
+    "pdipc_stage_sweep_timing", "pdipc_stage_toi_noalloc", "pdipc_add_volumetric", "pdipc_tet_surface",
+    "pdipc_scene_load", "pdipc_scene_model_count", "pdipc_scene_get_model", "pdipc_scene_apply_params",
+    "pdipc_scene_add_models", "pdipc_scene_free",
 ]
 
 
-ABI_VERSION = 2  # PDIPC_ABI_VERSION of include/pdipc.h
+ABI_VERSION = 3  # PDIPC_ABI_VERSION of include/pdipc.h
 
 
 class PdipcError(RuntimeError):
@@ -65,6 +67,17 @@ def load_library(path: str | None = None):
     L.pdipc_add_cloth.argtypes = [vp, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double, C.c_double, _ip,
                                   C.c_int, C.c_double, C.c_int]
     L.pdipc_add_static.argtypes = [vp, _dp, C.c_int, _ip, C.c_int, C.c_int]
+    L.pdipc_tet_surface.argtypes = [_dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip]
+    L.pdipc_scene_load.argtypes = [C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_int]
+    L.pdipc_scene_model_count.argtypes = [vp]
+    L.pdipc_scene_model_count.restype = C.c_int
+    L.pdipc_scene_get_model.argtypes = [vp, C.c_int, C.POINTER(SceneModel)]
+    L.pdipc_scene_apply_params.argtypes = [vp, C.POINTER(Params)]
+    L.pdipc_scene_add_models.argtypes = [vp, vp]
+    L.pdipc_scene_free.argtypes = [vp]
+    L.pdipc_scene_free.restype = None
+    L.pdipc_add_volumetric.argtypes = [vp, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double, C.c_double, _ip,
+                                       C.c_int, C.c_double, C.c_int]
     L.pdipc_initialize.argtypes = [vp]
     L.pdipc_step.argtypes = [vp, C.c_int]
     L.pdipc_animate.argtypes = [vp, _dp]
@@ -125,6 +138,8 @@ class Simulator:
         if scene is not None:
             for c in scene.cloths:
                 self.add_cloth(c.X, c.F, c.pins, c.density, c.k_stretch, c.k_bend, c.k_pin, c.patch_dim)
+            for v in getattr(scene, "solids", []):
+                self.add_volumetric(v.X, v.T, v.pins, v.density, v.k_strain, v.k_volume, v.k_pin, v.patch_dim)
             for s in scene.statics:
                 self.add_static(s.X, s.F, s.patch_dim)
             if initialize:
@@ -143,6 +158,16 @@ class Simulator:
         self._check(load_library().pdipc_add_cloth(self.h, _d(X), X.shape[0], _i(F), F.shape[0], density,
                                                    k_stretch, k_bend, _i(P), P.shape[0], k_pin, patch_dim),
                     "pdipc_add_cloth")
+        self.n_sim += X.shape[0]
+        self.n_total += X.shape[0]
+
+    def add_volumetric(self, X, T, pins=(), density=1000.0, k_strain=1e6, k_volume=1e3, k_pin=1e12, patch_dim=10):
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        T = np.ascontiguousarray(T, dtype=np.int32)
+        P = np.ascontiguousarray(pins, dtype=np.int32)
+        self._check(load_library().pdipc_add_volumetric(self.h, _d(X), X.shape[0], _i(T), T.shape[0], density,
+                                                        k_strain, k_volume, _i(P), P.shape[0], k_pin, patch_dim),
+                    "pdipc_add_volumetric")
         self.n_sim += X.shape[0]
         self.n_total += X.shape[0]
 
@@ -311,3 +336,52 @@ def create_simulator(sim_name: str, scene=None, **kw):
     if sim_name != "pd_ipc_simulator":
         raise ValueError(f"unknown simulator {sim_name!r}; this library provides 'pd_ipc_simulator'")
     return Simulator(scene, **kw)
+
+
+def tet_surface(X, T):
+    """Boundary faces of a tetrahedral mesh (pdipc_tet_surface; host only)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.int32)
+    cap = 4 * T.shape[0]
+    out = np.empty((cap, 3), np.int32)
+    nf = C.c_int()
+    rc = load_library().pdipc_tet_surface(_d(X), X.shape[0], _i(T), T.shape[0], _i(out), cap, C.byref(nf))
+    if rc != PDIPC_OK:
+        raise PdipcError(rc, "pdipc_tet_surface")
+    return out[:nf.value].copy()
+
+
+def read_scene(config_path: str, lg_iterations: int = 10):
+    """A reference config.xml (and the mesh files beside it) as a scenes.Scene,
+    read by the library's host reader (pdipc_scene_load).  Cloths come first,
+    then volumetric models, then static ones, each group in file order."""
+    L = load_library()
+    h = C.c_void_p()
+    err = C.create_string_buffer(512)
+    rc = L.pdipc_scene_load(config_path.encode(), C.byref(h), err, 512)
+    if rc != PDIPC_OK:
+        raise PdipcError(rc, "pdipc_scene_load", err.value.decode(errors="replace"))
+    try:
+        p = default_params()
+        L.pdipc_scene_apply_params(h, C.byref(p))
+        cloths, solids, statics = [], [], []
+        for i in range(L.pdipc_scene_model_count(h)):
+            m = SceneModel()
+            L.pdipc_scene_get_model(h, i, C.byref(m))
+            X = np.ctypeslib.as_array(m.X, (m.nv, 3)).copy()
+            F = np.ctypeslib.as_array(m.F, (m.nf, 3)).copy()
+            pins = np.ctypeslib.as_array(m.pins, (m.npins,)).copy() if m.npins else np.zeros(0, np.int32)
+            if m.kind == 0:
+                cloths.append(scenes.ClothSpec(X, F, pins.astype(np.int32), m.density, m.k[0], m.k[1], m.k[2],
+                                               m.patch_dim))
+            elif m.kind == 1:
+                T = np.ctypeslib.as_array(m.T, (m.nt, 4)).copy()
+                solids.append(scenes.SolidSpec(X, T, pins.astype(np.int32), m.density, m.k[0], m.k[1], m.k[2],
+                                               m.patch_dim))
+            else:
+                statics.append(scenes.StaticSpec(X, F, m.patch_dim))
+        name = os.path.basename(os.path.dirname(os.path.abspath(config_path)))
+        return scenes.Scene(name, cloths, statics, dt=p.time_step, gravity=p.gravity, dhat=p.dhat, kappa=p.kappa,
+                            lg_iterations=lg_iterations, solids=solids)
+    finally:
+        L.pdipc_scene_free(h)

@@ -96,6 +96,24 @@ def params_for_scene(scene, precision="fp32", **overrides) -> Params:
     return p
 
 
+class SceneModel(C.Structure):
+    _fields_ = [
+        ("name", C.c_char_p),
+        ("kind", C.c_int),
+        ("nv", C.c_int),
+        ("nf", C.c_int),
+        ("nt", C.c_int),
+        ("npins", C.c_int),
+        ("X", C.POINTER(C.c_double)),
+        ("F", C.POINTER(C.c_int)),
+        ("T", C.POINTER(C.c_int)),
+        ("pins", C.POINTER(C.c_int)),
+        ("density", C.c_double),
+        ("k", C.c_double * 3),
+        ("patch_dim", C.c_int),
+    ]
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("steps_done", C.c_int64),

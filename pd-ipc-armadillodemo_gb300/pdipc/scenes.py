@@ -148,6 +148,20 @@ class StaticSpec:
 
 
 @dataclasses.dataclass
+class SolidSpec:
+    """A tetrahedral (volumetric) model: PdIpcVolumetricModel(strain, volume,
+    position stiffness) with <density> and <patchDim>."""
+    X: np.ndarray
+    T: np.ndarray
+    pins: np.ndarray
+    density: float = 1000.0
+    k_strain: float = 1e6
+    k_volume: float = 1e3
+    k_pin: float = 1e12
+    patch_dim: int = 10
+
+
+@dataclasses.dataclass
 class Scene:
     name: str
     cloths: list
@@ -158,10 +172,11 @@ class Scene:
     kappa: float = 1e4
     lg_iterations: int = 10
     steps: int = 200
+    solids: list = dataclasses.field(default_factory=list)  # simulated after the cloths
 
     @property
     def n_sim(self) -> int:
-        return sum(c.X.shape[0] for c in self.cloths)
+        return sum(c.X.shape[0] for c in self.cloths) + sum(v.X.shape[0] for v in self.solids)
 
     @property
     def n_total(self) -> int:
@@ -257,3 +272,51 @@ def config2(seed: int = 0) -> Scene:
     sc = batched(256, 16, 128, seed=seed, lg=10, steps=100)
     sc.name = "c2_batched256"
     return sc
+
+
+def tet_block(nx: int, ny: int, nz: int, size=(0.2, 0.2, 0.2), origin=(0.0, 0.0, 0.0),
+              jitter: float = 0.0, seed: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    """Box of nx*ny*nz cubes, each split into 6 tetrahedra around its main
+    diagonal (a conforming Freudenthal split).  Returns (X float64[(nx+1)(ny+1)(nz+1), 3],
+    T int32[6 nx ny nz, 4])."""
+    g = np.stack(np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij"), -1)
+    g = g.reshape(-1, 3).astype(np.float64)
+    X = np.asarray(origin, np.float64) + g * (np.asarray(size, np.float64) / np.array([nx, ny, nz]))
+    if jitter > 0.0:
+        X += (2.0 * uniform01(seed, X.size).reshape(X.shape) - 1.0) * jitter
+
+    def vid(i, j, k):
+        return (i * (ny + 1) + j) * (nz + 1) + k
+
+    paths = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    T = []
+    for i in range(nx):
+        for j in range(ny):
+            for k in range(nz):
+                for p in paths:
+                    c = [i, j, k]
+                    v = [vid(*c)]
+                    for ax in p:
+                        c[ax] += 1
+                        v.append(vid(*c))
+                    T.append(v)
+    return X, np.asarray(T, dtype=np.int32)
+
+
+def block_drop(n: int = 4, subdiv: int = 3, *, cloth_n: int = 0, lg: int = 10, steps: int = 100,
+               size: float = 0.2, gap: float = 0.02, k_strain: float = 1e6, density: float = 1000.0,
+               patch_dim: int = 8, seed: int = 0) -> Scene:
+    """An n^3-cube tetrahedral block (size m, 6 tets per cube) falling from
+    ``gap`` above a fixed icosphere (radius 0.3 m) and, with cloth_n > 0, a
+    cloth_n x cloth_n cloth (1 m, two corners pinned) draped between them."""
+    sph_top = -0.2
+    X, T = tet_block(n, n, n, (size, size, size), (0.5 - size / 2, sph_top + gap, 0.5 - size / 2), 1e-5, seed)
+    solid = SolidSpec(X, T, np.zeros(0, np.int32), density=density, k_strain=k_strain, patch_dim=patch_dim)
+    cloths = []
+    if cloth_n > 0:
+        CX, CF = grid_cloth(cloth_n, 1.0, sph_top + gap / 2, 1e-4, seed + 1)
+        cloths.append(ClothSpec(CX, CF, np.array([0, cloth_n - 1], dtype=np.int32), patch_dim=cloth_n))
+    SX, SF = icosphere(subdiv, 0.3, (0.5, -0.5, 0.5))
+    return Scene(f"block{n}_cloth{cloth_n}_sphere{subdiv}", cloths,
+                 [StaticSpec(SX, SF, patch_dim=sphere_patch_dim(SF.shape[0]))],
+                 lg_iterations=lg, steps=steps, solids=[solid])
