@@ -40,17 +40,22 @@ METRIC = "512x512 cloth PD-IPC steps/sec: mixed/batched vs plain GPU vs CPU at <
 UNIT = "steps/s"
 
 
-def workload(name: str):
+def workload(name: str, scene_path: str | None = None):
     from pdipc import scenes
+    if scene_path:
+        import pdipc
+        return pdipc.read_scene(scene_path)
     return {"c0": scenes.config0, "c1": scenes.config1, "c2": scenes.config2, "c4": scenes.config4}[name](seed=0)
 
 
 def workload_desc(sc, prec: str) -> str:
-    if len(sc.cloths) > 1:
+    if len(sc.cloths) != 1 or sc.solids or not sc.statics:
+        nt = sum(v.T.shape[0] for v in sc.solids)
         nf = sum(c.F.shape[0] for c in sc.cloths)
-        return (f"{sc.name}: {len(sc.cloths)} cloths ({sc.n_sim} v / {nf} f), {len(sc.statics)} fixed icosphere(s) "
-                f"({sc.n_total - sc.n_sim} v); dt 1/240 s, {sc.lg_iterations} PD iterations x 15 Chebyshev-Jacobi "
-                f"R2 sweeps, dhat {sc.dhat:g} m, kappa {sc.kappa:g}; {prec}")
+        return (f"{sc.name}: {len(sc.cloths)} cloths ({nf} f), {len(sc.solids)} tet models ({nt} tets), "
+                f"{sc.n_sim} simulated v, {len(sc.statics)} fixed meshes ({sc.n_total - sc.n_sim} v); "
+                f"dt {sc.dt:g} s, {sc.lg_iterations} PD iterations x 15 Chebyshev-Jacobi R2 sweeps, "
+                f"dhat {sc.dhat:g} m, kappa {sc.kappa:g}; {prec}")
     c = sc.cloths[0]
     s = sc.statics[0]
     n = int(round(c.X.shape[0] ** 0.5))
@@ -212,7 +217,7 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     dist = init_dist(ws, "nccl")
-    sc = workload(args.config)
+    sc = workload(args.config, args.scene)
     sim = pdipc.Simulator(sc, args.precision, device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -225,7 +230,7 @@ def run_ours(args):
     # run + postRun (positions to host).  `value` sums the device time of the
     # steps (CUDA events on the library's stream); `e2e` is the wall time of the
     # same calls, host<->device copies included.
-    x_init = np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics])
+    x_init = sc.initial_positions()
     v_init = np.zeros((sc.n_sim, 3))
     out = np.empty((sim.n_total, 3), np.float64)
     barrier(dist, dev)
@@ -316,7 +321,7 @@ def run_ours(args):
             dist.destroy_process_group()
         return
     mean_outer = float(np.mean(outers))
-    traffic = profiled_traffic(args.precision) if args.config == "c1" else None
+    traffic = profiled_traffic(args.precision) if args.config == "c1" and not args.scene else None
     res = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 4), "higher_is_better": True,
@@ -368,13 +373,13 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle.oracle import FORM_R2, Oracle
-    sc = workload(args.config)
+    sc = workload(args.config, args.scene)
     threads = os.cpu_count() or 1
     sample_outer = args.cpu_outer_sample
     orc = Oracle(sc, "fp32", FORM_R2, threads=threads, fixed_outer=sample_outer)
     for _ in range(min(args.warmup, 1)):
         orc.step(1)
-    orc.set_state(np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics]),
+    orc.set_state(sc.initial_positions(),
                   np.zeros((sc.n_sim, 3)))
     budget, t_used, n = args.ref_budget_s, 0.0, 0
     while n < args.steps and t_used < budget:
@@ -408,7 +413,7 @@ def run_accuracy_study(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return
-    sc = workload(args.config)
+    sc = workload(args.config, args.scene)
     a = pdipc.Simulator(sc, "fp64", device=local)
     b = pdipc.Simulator(sc, "fp64", device=local)
     c = pdipc.Simulator(sc, args.precision, device=local)
@@ -441,6 +446,8 @@ def main(argv=None):
     ap.add_argument("--fp64-steps", type=int, default=100)
     ap.add_argument("--config", default="c1", choices=["c1", "c0", "c2", "c4"],
                     help="c1 is the benchmark workload; the others are for reference measurements")
+    ap.add_argument("--scene", default=None,
+                    help="a reference-format config.xml to run instead of --config (reference measurement)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-outer-sample", type=int, default=2)
     ap.add_argument("--ref-outer-per-step", type=float, default=30.0)

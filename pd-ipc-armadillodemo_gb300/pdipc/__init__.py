@@ -190,6 +190,8 @@ class Simulator:
     def animate(self, out: np.ndarray | None = None) -> np.ndarray:
         """run(frame); postRun(): one step and the positions copied to the host."""
         out = self._pos if out is None else out
+        if out.shape != (self.n_total, 3) or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError(f"animate: out must be a C-contiguous float64 array of shape ({self.n_total}, 3)")
         self._check(load_library().pdipc_animate(self.h, _d(out)), "pdipc_animate")
         return out
 
@@ -203,11 +205,17 @@ class Simulator:
         self._check(load_library().pdipc_get_velocities(self.h, _d(out)), "pdipc_get_velocities")
         return out
 
+    def _vec(self, A, n, what):
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        if A.shape != (n, 3):
+            raise ValueError(f"{what}: expected shape ({n}, 3), got {A.shape}")
+        return A
+
     def set_state(self, X, V=None):
-        X = np.ascontiguousarray(X, dtype=np.float64)
+        X = self._vec(X, self.n_total, "positions")
         Vp = None
         if V is not None:
-            V = np.ascontiguousarray(V, dtype=np.float64)
+            V = self._vec(V, self.n_sim, "velocities")
             Vp = _d(V)
         self._check(load_library().pdipc_set_state(self.h, _d(X), Vp), "pdipc_set_state")
 
@@ -238,8 +246,8 @@ class Simulator:
 
     # -- stages ----------------------------------------------------------------------------
     def stage_broadphase(self, x_old, dx, cap=1 << 16):
-        x_old = np.ascontiguousarray(x_old, dtype=np.float64)
-        dx = np.ascontiguousarray(dx, dtype=np.float64)
+        x_old = self._vec(x_old, self.n_total, "x_old")
+        dx = self._vec(dx, self.n_total, "dx")
         n1, n2, n3 = C.c_int64(), C.c_int64(), C.c_int64()
         L = load_library()
         while True:
@@ -262,8 +270,8 @@ class Simulator:
         return codes[:npatch], order[:npatch]
 
     def stage_toi(self, x0, x1, npt, nee):
-        x0 = np.ascontiguousarray(x0, dtype=np.float64)
-        x1 = np.ascontiguousarray(x1, dtype=np.float64)
+        x0 = self._vec(x0, self.n_total, "x0")
+        x1 = self._vec(x1, self.n_total, "x1")
         tp = np.empty(max(npt, 1), np.float64)
         te = np.empty(max(nee, 1), np.float64)
         g = C.c_double()
@@ -273,8 +281,8 @@ class Simulator:
 
     def stage_toi_noalloc(self, x0, x1, npt, nee, per_candidate=True):
         """stage_toi through the no-allocation entry point (FP64 and mixed modes)."""
-        x0 = np.ascontiguousarray(x0, dtype=np.float64)
-        x1 = np.ascontiguousarray(x1, dtype=np.float64)
+        x0 = self._vec(x0, self.n_total, "x0")
+        x1 = self._vec(x1, self.n_total, "x1")
         tp = np.empty(max(npt, 1), np.float64) if per_candidate else None
         te = np.empty(max(nee, 1), np.float64) if per_candidate else None
         g = C.c_double()
@@ -286,7 +294,7 @@ class Simulator:
         return tp[:npt], te[:nee], g.value
 
     def stage_contact(self, x):
-        x = np.ascontiguousarray(x, dtype=np.float64)
+        x = self._vec(x, self.n_total, "x")
         diag = np.empty(self.n_total, np.float64)
         rhs = np.empty((self.n_total, 3), np.float64)
         na = C.c_int64()
@@ -302,8 +310,8 @@ class Simulator:
         return ms.value, b.value
 
     def stage_pd(self, X, V):
-        X = np.ascontiguousarray(X, dtype=np.float64)
-        V = np.ascontiguousarray(V, dtype=np.float64)
+        X = self._vec(X, self.n_total, "X")
+        V = self._vec(V, self.n_sim, "V")
         out = np.empty((self.n_total, 3), np.float64)
         self._check(load_library().pdipc_stage_pd(self.h, _d(X), _d(V), _d(out)), "pdipc_stage_pd")
         return out

@@ -182,6 +182,11 @@ class Scene:
     def n_total(self) -> int:
         return self.n_sim + sum(s.X.shape[0] for s in self.statics)
 
+    def initial_positions(self) -> np.ndarray:
+        """Every vertex in the library's order: cloths, tet models, static meshes."""
+        return np.concatenate([c.X for c in self.cloths] + [v.X for v in self.solids] +
+                              [s.X for s in self.statics])
+
 
 def sphere_patch_dim(nfaces: int) -> int:
     """Grid resolution giving about two faces per patch cell on each cap."""
