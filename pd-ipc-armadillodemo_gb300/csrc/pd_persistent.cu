@@ -166,6 +166,12 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
     const int E = ee - eb;
     T* sval = reinterpret_cast<T*>(smem);
     int16_t* spat = reinterpret_cast<int16_t*>(smem + ((size_t)E * sizeof(T) + 15) / 16 * 16);
+    const size_t patBytes = ((size_t)a.patterns * a.patW * sizeof(int16_t) + 15) / 16 * 16;
+    T* bx = reinterpret_cast<T*>(smem + ((size_t)E * sizeof(T) + 15) / 16 * 16 + patBytes);
+    T* by = bx + a.bandMax;
+    T* bz = by + a.bandMax;
+    const bool band = kSmem && a.band != nullptr;
+    const int2 brange = band ? a.band[cta] : make_int2(0, 0);
     if (kSmem) {
         for (int q = threadIdx.x; q < E; q += blockDim.x) sval[q] = __ldg(a.sVal + eb + q);
         for (int q = threadIdx.x; q < a.patterns * a.patW; q += blockDim.x) spat[q] = __ldg(a.patOff + q);
@@ -209,8 +215,37 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
     for (int r = 0; r < R; ++r)
         id[r] = val[r] ? T(1) / ((a.Delastic[row[r]] + a.Dinert[row[r]]) + a.CollDiag[row[r]]) : T(0);
 
-    // sum_k N_ik src_k for the owned rows, from shared memory
+    // stage the band of src (all threads; the caller's rows then gather from it)
+    auto stage = [&](const V4<T>* src) {
+        if (!band) return;
+        const int n = brange.y - brange.x;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+            const V4<T> v = ldv<kL1>(src, brange.x + q);
+            bx[q] = v.x;
+            by[q] = v.y;
+            bz[q] = v.z;
+        }
+        __syncthreads();
+    };
+    // sum_k N_ik src_k for the owned rows: matrix from shared memory, src from
+    // the staged band or gathered from global memory
     auto gather = [&](const V4<T>* src, int r, T& s0, T& s1, T& s2) {
+        if (band) {
+            s0 = T(0);
+            s1 = T(0);
+            s2 = T(0);
+#pragma unroll 4
+            for (int k = 0; k < sl[r]; ++k) {
+                T v;
+                int j;
+                entry(r, k, v, j);
+                const int q = j - brange.x;
+                s0 += v * bx[q];
+                s1 += v * by[q];
+                s2 += v * bz[q];
+            }
+            return;
+        }
         s0 = T(0);
         s1 = T(0);
         s2 = T(0);
@@ -392,6 +427,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
         // correction form: iterate on delta from 0, add it to P at the end.
         T cx[R][3], px[R][3], yv[R][3];
         // first sweep: Y = S(x0)
+        if constexpr (!kCorr) stage(a.P);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             T s0 = T(0), s1 = T(0), s2 = T(0);
@@ -414,6 +450,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
             const bool last = it == nsteps - 1;
             // second sweep of the step: S(Y), Chebyshev-combined except for the first step
             const T om = a.omega[it];
+            stage(a.GY);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 T s0 = T(0), s1 = T(0), s2 = T(0);
@@ -454,6 +491,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
             if (!sync()) return;
             if (last) break;
             // first sweep of the next step: Y = S(x)
+            stage(a.GX);
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 T s0 = T(0), s1 = T(0), s2 = T(0);

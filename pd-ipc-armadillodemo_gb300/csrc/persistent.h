@@ -24,6 +24,7 @@ struct PersistPlan {
     size_t smem_bytes = 0;
     int patterns = 0;
     int pattern_width = 0;
+    int band_max = 0;             // > 0: each sweep stages the CTA's column band in shared memory
 };
 
 // T: solver scalar; S: state scalar (T in the direct form, double in the
@@ -82,6 +83,13 @@ struct PersistArgs {
     unsigned* flags;
     const int2* nbr;
     unsigned epoch0;
+    // staged band (band != null, matrix in shared memory): before each sweep a
+    // CTA copies columns [band[c].x, band[c].y) of the gathered vector into
+    // shared memory as three planar arrays of bandMax floats, and gathers
+    // from there (one 4-byte shared load per component instead of an
+    // unaligned 16-byte global gather)
+    const int2* band;
+    int bandMax;
 };
 
 const void* persistent_kernel(bool correction, bool matrix_in_smem, bool l1_gather, int rows_per_thread);

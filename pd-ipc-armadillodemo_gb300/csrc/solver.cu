@@ -638,16 +638,37 @@ private:
             if (pats.size() > 4096) fits16 = false;
         }
         const size_t patBytes = fits16 ? pats.size() * (size_t)patW * sizeof(int16_t) : 0;
-        auto cta_smem = [&](int spc, bool smem_mat) -> size_t {
+        auto a16 = [](size_t b) { return (b + 15) / 16 * 16; };
+        auto cta_smem = [&](int spc, bool smem_mat, size_t band_bytes) -> size_t {
             if (!smem_mat) return 0;
             size_t mx = 0;
             for (int c = 0; c * spc < nsl; ++c) {
                 const int s0 = c * spc, s1 = std::min(nsl, s0 + spc);
                 const size_t E = (size_t)(soff[s1] - soff[s0]);
-                mx = std::max(mx, (E * sizeof(T) + 15) / 16 * 16 + patBytes);
+                mx = std::max(mx, a16(E * sizeof(T)) + a16(patBytes) + band_bytes);
             }
             return mx;
         };
+        // columns each CTA's matrix rows read, as a range: the gathered vector's
+        // band that a CTA stages in shared memory once per sweep
+        auto col_ranges = [&](int spc, std::vector<int2>& rg) -> int {
+            const int ctas = (nsl + spc - 1) / spc;
+            rg.assign(ctas, make_int2(0, 0));
+            int mx = 0;
+            for (int c = 0; c < ctas; ++c) {
+                const int r0 = c * spc * kSlice, r1 = std::min(ns, (c + 1) * spc * kSlice);
+                int lo = r0, hi = std::max(r0, r1 - 1);
+                for (int r = r0; r < r1; ++r)
+                    for (int e = H.nPtr[r]; e < H.nPtr[r + 1]; ++e) {
+                        lo = std::min(lo, H.nCol[e]);
+                        hi = std::max(hi, H.nCol[e]);
+                    }
+                rg[c] = make_int2(lo, hi + 1);
+                mx = std::max(mx, hi + 1 - lo);
+            }
+            return mx;
+        };
+        std::vector<int2> bandRange;
         const size_t limit = (size_t)smem_optin - 1024;
         for (int pass = 0; pass < 2 && !plan_.enabled; ++pass) {
             const bool smem_mat = pass == 0 && fits16;
@@ -657,8 +678,19 @@ private:
                 if (W > 32) continue;
                 const int spc = W * R;
                 const int ctas = (nsl + spc - 1) / spc;
-                const size_t sm = cta_smem(spc, smem_mat);
+                size_t sm = cta_smem(spc, smem_mat, 0);
                 if (sm > limit) continue;
+                int bandMax = 0;
+                if (smem_mat && prm_.persistent != 4) {
+                    std::vector<int2> rg;
+                    const int mx = col_ranges(spc, rg);
+                    const size_t smb = cta_smem(spc, smem_mat, a16(3 * (size_t)mx * sizeof(T)));
+                    if (smb <= limit) {
+                        sm = smb;
+                        bandMax = mx;
+                        bandRange.swap(rg);
+                    }
+                }
                 const void* f = persistent_kernel(kCorrection, smem_mat, prm_.persistent != 2, R);
                 PD_CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
                 int per_sm = 0;
@@ -675,6 +707,7 @@ private:
                 plan_.smem_bytes = sm;
                 plan_.patterns = smem_mat ? (int)pats.size() : 0;
                 plan_.pattern_width = patW;
+                plan_.band_max = bandMax;
                 break;
             }
         }
@@ -713,6 +746,7 @@ private:
                 nbr[d2].y = std::max(nbr[d2].y, c);
             }
         PD_CK(up(pNbr_, nbr));
+        if (plan_.band_max > 0) PD_CK(up(pBand_, bandRange));
         PD_CK(zeros(pFlags_, plan_.ctas));
         PD_CK(up(pCtaSlice_, ctaSlice));
         PD_CK(up(pCtaEntry_, ctaEntry));
@@ -772,6 +806,8 @@ private:
             a.err = d.ErrFlags;
             a.flags = pFlags_;
             a.nbr = plan_.local_sync ? pNbr_ : nullptr;
+            a.band = plan_.band_max > 0 ? pBand_ : nullptr;
+            a.bandMax = plan_.band_max;
             a.epoch0 = 0;
             const void* ptrs[] = {a.P, a.Pold, a.Xrest, a.Rhs0, a.CollRhs, a.PinRhs, a.Aq, a.GX, a.GY, a.Delastic,
                                   a.Dinert, a.CollDiag, a.PinFlag, a.PinK, a.lPtr, a.lNbr, a.lRest, a.lLbo,
@@ -1102,6 +1138,7 @@ private:
     unsigned* pBar_ = nullptr;
     unsigned* pFlags_ = nullptr;  // per-CTA phase counts of the neighbour synchronisation
     int2* pNbr_ = nullptr;        // per-CTA range of CTAs to wait for
+    int2* pBand_ = nullptr;       // per-CTA [first, last + 1) column of its rows (staged band)
     unsigned epoch_ = 1;
     V4<TC>* stage_ = nullptr;  // pinned host staging of one state vector
     cudaGraph_t graph_ = nullptr;

@@ -202,11 +202,11 @@ def test_fp32_steps_match_oracle_short_horizon(built_lib):
 
 @pytest.mark.parametrize("prec,atol", [("fp32", 2e-5), ("mixed", 1e-6)])
 @pytest.mark.parametrize("n", [16, 48])
-@pytest.mark.parametrize("variant", [1, 2, 3])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4])
 def test_persistent_solve_matches_per_sweep_launches(prec, atol, n, variant, built_lib):
-    """One cooperative launch per outer iteration (neighbour synchronisation with
-    gathers through L1 or L2 only, or grid barriers) gives the same PD solve as
-    one launch per sweep."""
+    """One cooperative launch per outer iteration (neighbour synchronisation or
+    grid barriers; sweeps gathering from a staged shared-memory band, through L1
+    or L2 only) gives the same PD solve as one launch per sweep."""
     sc = small_scene(n, 2)
     a = pdipc.Simulator(sc, prec, persistent=variant)
     b = pdipc.Simulator(sc, prec, persistent=0)
