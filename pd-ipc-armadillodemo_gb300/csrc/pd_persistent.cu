@@ -83,22 +83,65 @@ __device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// ---- bulk copies (TMA engine) into shared memory, completed on an mbarrier ----
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// one arrival that also expects `bytes` of copies to complete on the barrier
+__device__ __forceinline__ void mbar_arrive_expect(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// a plain arrival (no bytes expected): completes the phase without a copy
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+// global -> shared bulk copy; addresses 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
 // Neighbour synchronisation: a Jacobi sweep only reads the rows of the CTAs a
 // CTA's matrix rows reach, so instead of a grid barrier each CTA publishes its
 // phase count and waits for those CTAs only (the range is closed under "reads
 // or is read by", so no CTA overwrites rows a neighbour is still reading).
-// Neighbours can then be at most one phase apart.  Lanes of warp 0 poll one
-// neighbour flag each; every wait is clock-bounded and gives up, raising
-// kErrBarrier, when it times out or sees the error raised elsewhere.
-__device__ __forceinline__ bool nbr_barrier(unsigned* flags, unsigned* err, int cta, int2 range, unsigned epoch,
-                                            long long timeout_cycles) {
-    __syncthreads();
+// Neighbours can then be at most one phase apart.  Publishing and waiting are
+// separate steps so that a CTA can work on its own rows in between.
+//
+// nbr_publish: the caller has passed a __syncthreads() after its writes of the
+// phase; thread 0 releases the phase count (cumulative over the CTA's writes).
+__device__ __forceinline__ void nbr_publish(unsigned* flags, int cta, unsigned epoch) {
+    if (threadIdx.x == 0) {
+        __threadfence();
+        st_release_gpu(flags + cta, epoch);
+    }
+}
+
+// nbr_wait: lanes of warp 0 poll one neighbour flag each until it reaches
+// epoch; ends with __syncthreads(), after which the neighbours' writes of that
+// phase are visible to every thread.  Every wait is clock-bounded and gives up,
+// raising kErrBarrier, when it times out or sees the error raised elsewhere.
+__device__ __forceinline__ bool nbr_wait(const unsigned* flags, unsigned* err, int cta, int2 range, unsigned epoch,
+                                         long long timeout_cycles) {
     __shared__ int nok_s;
     if (threadIdx.x < 32) {
-        if (threadIdx.x == 0) {
-            __threadfence();
-            st_release_gpu(flags + cta, epoch);
-        }
         int ok = (ld_acquire_gpu(err) & kErrBarrier) ? 0 : 1;
         for (int n = range.x + (int)threadIdx.x; ok && n <= range.y; n += 32) {
             if (n == cta) continue;
@@ -117,6 +160,13 @@ __device__ __forceinline__ bool nbr_barrier(unsigned* flags, unsigned* err, int 
     }
     __syncthreads();
     return nok_s != 0;
+}
+
+__device__ __forceinline__ bool nbr_barrier(unsigned* flags, unsigned* err, int cta, int2 range, unsigned epoch,
+                                            long long timeout_cycles) {
+    __syncthreads();
+    nbr_publish(flags, cta, epoch);
+    return nbr_wait(flags, err, cta, range, epoch, timeout_cycles);
 }
 
 __device__ __forceinline__ V4<float> ldcg4(const V4<float>* p, int i) {
@@ -156,9 +206,13 @@ __device__ __forceinline__ void stcg4(V4<double>* p, int i, double x, double y, 
 // S is the state scalar: T in the direct form, double in the correction form,
 // where positions enter the FP32 arithmetic as differences formed from their
 // float-float mirror (Ph, Pl): no FP64 arithmetic in the per-neighbour loops.
-template <typename T, typename S, bool kCorr, bool kSmem, bool kL1, int R>
-__global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) {
+// kMode: 0 matrix streamed from L2; 1 matrix in shared memory, gathers from
+// global memory; 2 matrix and the band of the iterate in shared memory
+template <typename T, typename S, bool kCorr, int kMode, bool kL1, int R>
+__global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(PersistArgs<T, S> a) {
+    constexpr bool kSmem = kMode >= 1;
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int abort_s;  // band path: a neighbour wait failed, every warp returns
     const int cta = blockIdx.x;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // ---- this CTA's matrix values and the offset patterns into shared memory ----
@@ -167,33 +221,48 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
     T* sval = reinterpret_cast<T*>(smem);
     int16_t* spat = reinterpret_cast<int16_t*>(smem + ((size_t)E * sizeof(T) + 15) / 16 * 16);
     const size_t patBytes = ((size_t)a.patterns * a.patW * sizeof(int16_t) + 15) / 16 * 16;
-    T* bx = reinterpret_cast<T*>(smem + ((size_t)E * sizeof(T) + 15) / 16 * 16 + patBytes);
-    T* by = bx + a.bandMax;
-    T* bz = by + a.bandMax;
-    const bool band = kSmem && a.band != nullptr;
+    // the band of the iterate: own rows as three planar arrays, the halo as
+    // 16-byte vertices (copied in bulk), then the copies' mbarrier
+    unsigned char* bandp = smem + ((size_t)E * sizeof(T) + 15) / 16 * 16 + patBytes;
+    T* ox = reinterpret_cast<T*>(bandp);
+    T* oy = ox + a.ownMax;
+    T* oz = oy + a.ownMax;
+    V4<T>* hv = reinterpret_cast<V4<T>*>(bandp + (3 * (size_t)a.ownMax * sizeof(T) + 15) / 16 * 16);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(hv + a.haloMax);
+    constexpr bool band = kMode == 2;
     const int2 brange = band ? a.band[cta] : make_int2(0, 0);
     if (kSmem) {
         for (int q = threadIdx.x; q < E; q += blockDim.x) sval[q] = __ldg(a.sVal + eb + q);
         for (int q = threadIdx.x; q < a.patterns * a.patW; q += blockDim.x) spat[q] = __ldg(a.patOff + q);
     }
-    // ---- rows owned by this thread ----
-    int row[R], gb[R], sl[R], pid[R];
+    if (band && threadIdx.x == 0) {
+        mbar_init(mbar, 1);
+        abort_s = 0;
+    }
+    // ---- rows owned by this thread: one per slice, the warp's R slices
+    // consecutive; the band path's last warp has no rows ----
+    // pk[r] packs the row's entry count (bits 0-9) and, on the band path, the
+    // bounds of its entries on own rows (bits 10-19, 20-29)
+    const int nrw = (int)(blockDim.x >> 5) - (band ? 1 : 0);
+    const int row0 = (a.ctaSlice[cta] + warp * R) * 32 + lane;
+    auto rowof = [&](int r) { return row0 + 32 * r; };
+    int gb[R], pk[R], pid[R];
     bool val[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-        const int s = a.ctaSlice[cta] + warp * R + r;  // slice index
-        const bool sv = s < a.ctaSlice[cta + 1];
-        row[r] = s * 32 + lane;
-        val[r] = sv && row[r] < a.nsim;
+        const int s = a.ctaSlice[cta] + warp * R + r;
+        const bool sv = warp < nrw && s < a.ctaSlice[cta + 1];
+        val[r] = sv && rowof(r) < a.nsim;
         gb[r] = sv ? a.sliceEntry[s] + lane : 0;
-        sl[r] = sv ? a.sliceLen[s] : 0;
-        pid[r] = (kSmem && val[r]) ? a.rowPattern[row[r]] * a.patW : 0;
+        pk[r] = sv ? a.sliceLen[s] : 0;
+        pid[r] = (kSmem && val[r]) ? a.rowPattern[rowof(r)] * a.patW : 0;
     }
+    auto slen = [&](int r) { return pk[r] & 1023; };
     // entry k of owned row r: value and gathered row
     auto entry = [&](int r, int k, T& v, int& j) {
         if (kSmem) {
             v = sval[gb[r] - eb + 32 * k];
-            j = row[r] + (int)spat[pid[r] + k];
+            j = rowof(r) + (int)spat[pid[r] + k];
         } else {
             v = __ldg(a.sVal + gb[r] + 32 * k);
             j = __ldg(a.sCol + gb[r] + 32 * k);
@@ -213,44 +282,136 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
     T id[R];
 #pragma unroll
     for (int r = 0; r < R; ++r)
-        id[r] = val[r] ? T(1) / ((a.Delastic[row[r]] + a.Dinert[row[r]]) + a.CollDiag[row[r]]) : T(0);
+        id[r] = val[r] ? T(1) / ((a.Delastic[rowof(r)] + a.Dinert[rowof(r)]) + a.CollDiag[rowof(r)]) : T(0);
 
-    // stage the band of src (all threads; the caller's rows then gather from it)
-    auto stage = [&](const V4<T>* src) {
-        if (!band) return;
-        const int n = brange.y - brange.x;
-        for (int q = threadIdx.x; q < n; q += blockDim.x) {
-            const V4<T> v = ldv<kL1>(src, brange.x + q);
-            bx[q] = v.x;
-            by[q] = v.y;
-            bz[q] = v.z;
+    // ---- the band: this CTA's own rows and the halo its matrix rows reach ----
+    // Own rows [own0, own1) live in the planar arrays; between sweeps each
+    // thread writes its rows' new values there.  The halo, columns
+    // [brange.x, own0) and [own1, brange.y), is copied from global memory in
+    // two bulk copies once the neighbours have published it.
+    const int own0 = a.ctaSlice[cta] * 32, own1 = min(a.ctaSlice[cta + 1] * 32, a.nsim);
+    const int nlo = band ? own0 - brange.x : 0, nhi = band ? brange.y - own1 : 0;
+    const int hiBase = own1 - nlo;  // halo slot of column j >= own1: j - hiBase
+    // The band path runs one extra warp, the last, with no rows: it publishes
+    // each sweep, polls the neighbours' flags and issues the halo copies, so
+    // the compute warps never wait on a flag.  Compute warps wait for a copy
+    // on the mbarrier (clock-bounded); abort_s ends the launch for all warps
+    // when a neighbour wait has failed.
+    const bool syncw = band && warp == (int)(blockDim.x >> 5) - 1;
+    const unsigned ncomp = blockDim.x - 32u;
+    unsigned mphase = 0;
+    // sync warp: optionally wait until the neighbours have published phase
+    // `epoch`, then copy the halo of src
+    auto issue_halo = [&](const V4<T>* src, bool poll) -> bool {
+        int ok = (ld_acquire_gpu(a.err) & kErrBarrier) ? 0 : 1;
+        for (int n = nrange.x + lane; poll && ok && n <= nrange.y; n += 32) {
+            if (n == cta) continue;
+            const long long t0 = clock64();
+            while ((int)(ld_acquire_gpu(a.flags + n) - epoch) < 0) {
+                if (clock64() - t0 > a.timeout || (ld_acquire_gpu(a.err) & kErrBarrier)) {
+                    atomicOr(a.err, (unsigned)kErrBarrier);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(8);
+            }
         }
-        __syncthreads();
+        ok = __all_sync(0xffffffffu, ok);
+        if (lane == 0) {
+            if (ok) {
+                // the neighbours' generic-proxy writes (acquired) and this CTA's
+                // earlier reads of the halo area come before the async-proxy copy
+                asm volatile("fence.proxy.async.global;" ::: "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive_expect(mbar, (unsigned)(nlo + nhi) * (unsigned)sizeof(V4<T>));
+                if (nlo > 0) bulk_load(hv, src + brange.x, (unsigned)nlo * (unsigned)sizeof(V4<T>), mbar);
+                if (nhi > 0) bulk_load(hv + nlo, src + own1, (unsigned)nhi * (unsigned)sizeof(V4<T>), mbar);
+            } else {
+                abort_s = 1;
+                mbar_arrive(mbar);
+            }
+        }
+        __syncwarp();
+        return ok != 0;
     };
-    // sum_k N_ik src_k for the owned rows: matrix from shared memory, src from
-    // the staged band or gathered from global memory
-    auto gather = [&](const V4<T>* src, int r, T& s0, T& s1, T& s2) {
-        if (band) {
-            s0 = T(0);
-            s1 = T(0);
-            s2 = T(0);
-#pragma unroll 4
-            for (int k = 0; k < sl[r]; ++k) {
+    // compute warps: wait for the halo copy; false when the launch is ending
+    auto halo_ready = [&]() -> bool {
+        const long long t0 = clock64();
+        while (!mbar_try_wait(mbar, mphase)) {
+            if (clock64() - t0 > 2 * a.timeout) {  // longer than the sync warp's own waits
+                atomicOr(a.err, (unsigned)kErrBarrier);
+                return false;
+            }
+        }
+        mphase ^= 1u;
+        return *((volatile int*)&abort_s) == 0;
+    };
+    // Entries are in column order, so an owned row's entries split into
+    // [0, kb) on the low halo, [kb, ke) on own rows and [ke, len) on the high
+    // halo; the padding repeats the last entry's column with value 0.
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        int b = slen(r), e = slen(r);
+        if (band && val[r]) {
+            for (int k = 0; k < slen(r); ++k) {
                 T v;
                 int j;
                 entry(r, k, v, j);
-                const int q = j - brange.x;
-                s0 += v * bx[q];
-                s1 += v * by[q];
-                s2 += v * bz[q];
+                if (j >= own0 && j < own1) {
+                    if (b == slen(r)) b = k;
+                } else if (b < slen(r) && e == slen(r)) {
+                    e = k;
+                }
             }
-            return;
+            if (b == slen(r)) {  // no own entry: split at the first column past the own block
+                for (b = 0; b < slen(r); ++b) {
+                    T v;
+                    int j;
+                    entry(r, b, v, j);
+                    if (j >= own1) break;
+                }
+                e = b;
+            }
         }
+        pk[r] |= (b << 10) | (e << 20);
+    }
+    auto own_sum = [&](int r, T& s0, T& s1, T& s2) {
+        const int k1 = pk[r] >> 20;
+#pragma unroll 4
+        for (int k = (pk[r] >> 10) & 1023; k < k1; ++k) {
+            T v;
+            int j;
+            entry(r, k, v, j);
+            const int q = j - own0;
+            s0 += v * ox[q];
+            s1 += v * oy[q];
+            s2 += v * oz[q];
+        }
+    };
+    auto halo_range = [&](int r, int k0, int k1, int base, T& s0, T& s1, T& s2) {
+#pragma unroll 4
+        for (int k = k0; k < k1; ++k) {
+            T v;
+            int j;
+            entry(r, k, v, j);
+            const V4<T> h = hv[j - base];
+            s0 += v * h.x;
+            s1 += v * h.y;
+            s2 += v * h.z;
+        }
+    };
+    auto halo_part = [&](int r, T& s0, T& s1, T& s2) {
+        halo_range(r, 0, (pk[r] >> 10) & 1023, brange.x, s0, s1, s2);
+        halo_range(r, pk[r] >> 20, slen(r), hiBase, s0, s1, s2);
+    };
+    // sum_k N_ik src_k for the owned rows (paths without the band): matrix
+    // from shared memory or L2, src gathered from global memory
+    auto gather = [&](const V4<T>* src, int r, T& s0, T& s1, T& s2) {
         s0 = T(0);
         s1 = T(0);
         s2 = T(0);
 #pragma unroll 4
-        for (int k = 0; k < sl[r]; ++k) {
+        for (int k = 0; k < slen(r); ++k) {
             T v;
             int j;
             entry(r, k, v, j);
@@ -266,7 +427,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             if (!val[r]) continue;
-            const int i = row[r];
+            const int i = rowof(r);
             const int b = a.lPtr[i], e = a.lPtr[i + 1];
             T a0, a1, a2;
             if constexpr (kCorr) {
@@ -312,7 +473,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
             x0[r][0] = x0[r][1] = x0[r][2] = T(0);
             rh[r][0] = rh[r][1] = rh[r][2] = T(0);
             if (!val[r]) continue;
-            const int i = row[r];
+            const int i = rowof(r);
             const int b = a.lPtr[i], e = a.lPtr[i + 1];
             const V4<S> x = ldv<kL1>(a.P, i);
             const T strain = a.Strain[i];
@@ -368,7 +529,7 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
                     r1.add(bt * ak.y);
                     r2.add(bt * ak.z);
                 }
-                for (int k = 0; k < sl[r]; ++k) {
+                for (int k = 0; k < slen(r); ++k) {
                     T v;
                     int j;
                     entry(r, k, v, j);
@@ -425,116 +586,244 @@ __global__ void __launch_bounds__(1024, 1) k_pd_persistent(PersistArgs<T, S> a) 
         // ---- Chebyshev-accelerated R2 iteration as two J sweeps per step ----
         // direct form: iterate on x from x0 (gathered from P);
         // correction form: iterate on delta from 0, add it to P at the end.
-        T cx[R][3], px[R][3], yv[R][3];
-        // first sweep: Y = S(x0)
-        if constexpr (!kCorr) stage(a.P);
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            T s0 = T(0), s1 = T(0), s2 = T(0);
-            if constexpr (kCorr) {
-                cx[r][0] = cx[r][1] = cx[r][2] = T(0);
-            } else {
-                cx[r][0] = x0[r][0];
-                cx[r][1] = x0[r][1];
-                cx[r][2] = x0[r][2];
-                if (val[r]) gather(a.P, r, s0, s1, s2);
-            }
-            yv[r][0] = om1 * cx[r][0] + w * ((s0 + rh[r][0]) * id[r]);
-            yv[r][1] = om1 * cx[r][1] + w * ((s1 + rh[r][1]) * id[r]);
-            yv[r][2] = om1 * cx[r][2] + w * ((s2 + rh[r][2]) * id[r]);
-            if (val[r]) stcg4(a.GY, row[r], yv[r][0], yv[r][1], yv[r][2]);
-        }
-        if (!sync()) return;
-        const int nsteps = a.cheby;
-        for (int it = 0; it < nsteps; ++it) {
-            const bool last = it == nsteps - 1;
-            // second sweep of the step: S(Y), Chebyshev-combined except for the first step
+        // first sweep of a step: y = S(c) from the gathered sum s and the row's own c
+        auto finish_y = [&](int r, T s0, T s1, T s2, const T (&c)[3], T (&y)[3]) {
+            y[0] = om1 * c[0] + w * ((s0 + rh[r][0]) * id[r]);
+            y[1] = om1 * c[1] + w * ((s1 + rh[r][1]) * id[r]);
+            y[2] = om1 * c[2] + w * ((s2 + rh[r][2]) * id[r]);
+            if (val[r]) stcg4(a.GY, rowof(r), y[0], y[1], y[2]);
+        };
+        // second sweep of step it: S(y), Chebyshev-combined with the previous
+        // second-sweep iterate p except for the first step; the last one
+        // updates the positions
+        auto finish_x = [&](int r, T s0, T s1, T s2, const T (&y)[3], const T (&p)[3], int it, bool last,
+                            V4<T>* xout, T (&n)[3]) {
             const T om = a.omega[it];
-            stage(a.GY);
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                T s0 = T(0), s1 = T(0), s2 = T(0);
-                if (val[r]) gather(a.GY, r, s0, s1, s2);
-                T n0 = om1 * yv[r][0] + w * ((s0 + rh[r][0]) * id[r]);
-                T n1 = om1 * yv[r][1] + w * ((s1 + rh[r][1]) * id[r]);
-                T n2 = om1 * yv[r][2] + w * ((s2 + rh[r][2]) * id[r]);
-                if (it > 0) {
-                    n0 = om * (n0 - px[r][0]) + px[r][0];
-                    n1 = om * (n1 - px[r][1]) + px[r][1];
-                    n2 = om * (n2 - px[r][2]) + px[r][2];
+            n[0] = om1 * y[0] + w * ((s0 + rh[r][0]) * id[r]);
+            n[1] = om1 * y[1] + w * ((s1 + rh[r][1]) * id[r]);
+            n[2] = om1 * y[2] + w * ((s2 + rh[r][2]) * id[r]);
+            if (it > 0) {
+                n[0] = om * (n[0] - p[0]) + p[0];
+                n[1] = om * (n[1] - p[1]) + p[1];
+                n[2] = om * (n[2] - p[2]) + p[2];
+            }
+            if (!val[r]) return;
+            if (last) {
+                if constexpr (kCorr) {  // only this thread writes the row: its own earlier read is current
+                    const V4<S> x = ldcg4(a.P, rowof(r));
+                    const S q0 = x.x + (S)n[0], q1 = x.y + (S)n[1], q2 = x.z + (S)n[2];
+                    stcg4(a.P, rowof(r), q0, q1, q2);
+                    float h0, l0, h1, l1, h2, l2;
+                    split_ff(q0, h0, l0);
+                    split_ff(q1, h1, l1);
+                    split_ff(q2, h2, l2);
+                    stcg4(a.Ph, rowof(r), h0, h1, h2);
+                    stcg4(a.Pl, rowof(r), l0, l1, l2);
+                } else {
+                    stcg4(a.P, rowof(r), n[0], n[1], n[2]);
                 }
-                px[r][0] = cx[r][0];
-                px[r][1] = cx[r][1];
-                px[r][2] = cx[r][2];
-                cx[r][0] = n0;
-                cx[r][1] = n1;
-                cx[r][2] = n2;
-                if (!val[r]) continue;
-                if (last) {
-                    if constexpr (kCorr) {  // only this thread writes the row: its own earlier read is current
-                        const V4<S> x = ldcg4(a.P, row[r]);
-                        const S q0 = x.x + (S)n0, q1 = x.y + (S)n1, q2 = x.z + (S)n2;
-                        stcg4(a.P, row[r], q0, q1, q2);
-                        float h0, l0, h1, l1, h2, l2;
-                        split_ff(q0, h0, l0);
-                        split_ff(q1, h1, l1);
-                        split_ff(q2, h2, l2);
-                        stcg4(a.Ph, row[r], h0, h1, h2);
-                        stcg4(a.Pl, row[r], l0, l1, l2);
-                    } else {
-                        stcg4(a.P, row[r], n0, n1, n2);
+            } else {
+                stcg4(xout, rowof(r), n[0], n[1], n[2]);
+            }
+        };
+        const int nsteps = a.cheby;
+        if constexpr (band) {
+            // The own slots always hold the latest iterate of the own rows, so a
+            // row keeps only its right-hand side and partial sums in registers:
+            // y and the current x come from its slot.  Second-sweep iterates
+            // alternate between GX (even steps) and GX2 (odd steps), so the one
+            // from two steps back that the Chebyshev combination needs is still
+            // in the buffer the row overwrites (this thread's rows only); GX2
+            // starts as x0 = 0.  A sweep sums a row's entries on own rows while
+            // the halo is in flight, then the halo entries (correction form
+            // only: the direct form keeps the reference's summation order).
+            T so[R][3], nv[R][3];
+            auto own_part = [&]() {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    so[r][0] = so[r][1] = so[r][2] = T(0);
+                    if (val[r]) own_sum(r, so[r][0], so[r][1], so[r][2]);
+                }
+            };
+            auto own_slot = [&](int r, T (&c)[3]) {
+                const int q = val[r] ? rowof(r) - own0 : 0;
+                c[0] = ox[q];
+                c[1] = oy[q];
+                c[2] = oz[q];
+            };
+            auto write_own = [&]() {
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+                    if (val[r]) {
+                        const int q = rowof(r) - own0;
+                        ox[q] = nv[r][0];
+                        oy[q] = nv[r][1];
+                        oz[q] = nv[r][2];
+                    }
+            };
+            auto comp_bar = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(ncomp) : "memory"); };
+            // end of a sweep: every row's global stores are issued and nobody
+            // reads the band; the sync warp publishes the phase while the
+            // compute warps move their new iterate into the own slots
+            auto end_sweep = [&]() {
+                __syncthreads();
+                ++epoch;
+                if (syncw) {
+                    if (lane == 0) {
+                        __threadfence();
+                        st_release_gpu(a.flags + cta, epoch);
                     }
                 } else {
-                    stcg4(a.GX, row[r], n0, n1, n2);
+                    write_own();
+                    comp_bar();
+                }
+            };
+            // sums of a sweep for the owned rows (compute warps); false: the launch ends
+            static_assert(kCorr || !band, "the band path runs the correction form");
+            auto sweep_sums = [&](T (&sm)[R][3]) -> bool {
+                own_part();
+                if (!halo_ready()) return false;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    sm[r][0] = so[r][0];
+                    sm[r][1] = so[r][1];
+                    sm[r][2] = so[r][2];
+                    if (val[r]) halo_part(r, sm[r][0], sm[r][1], sm[r][2]);
+                }
+                return true;
+            };
+            // first sweep: y = S(0)
+            if (!syncw) {
+                const T zero[3] = {T(0), T(0), T(0)};
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    if (val[r]) stcg4(a.GX2, rowof(r), T(0), T(0), T(0));
+                    finish_y(r, T(0), T(0), T(0), zero, nv[r]);
                 }
             }
-            if (!sync()) return;
-            if (last) break;
-            // first sweep of the next step: Y = S(x)
-            stage(a.GX);
+            end_sweep();
+            for (int it = 0; it < nsteps; ++it) {
+                const bool last = it == nsteps - 1;
+                V4<T>* xb = (it & 1) ? a.GX2 : a.GX;
+                // x = S(y)
+                if (syncw) {
+                    if (!issue_halo(a.GY, true)) return;
+                } else {
+                    T p[R][3], sm[R][3];
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        p[r][0] = p[r][1] = p[r][2] = T(0);
+                        if (it > 0 && val[r]) {
+                            const V4<T> g = ldcg4(xb, rowof(r));
+                            p[r][0] = g.x;
+                            p[r][1] = g.y;
+                            p[r][2] = g.z;
+                        }
+                    }
+                    if (!sweep_sums(sm)) return;
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        T y[3];
+                        own_slot(r, y);
+                        finish_x(r, sm[r][0], sm[r][1], sm[r][2], y, p[r], it, last, xb, nv[r]);
+                    }
+                }
+                end_sweep();
+                if (last) break;
+                // y = S(x)
+                if (syncw) {
+                    if (!issue_halo(xb, true)) return;
+                } else {
+                    T sm[R][3];
+                    if (!sweep_sums(sm)) return;
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        T c[3];
+                        own_slot(r, c);
+                        finish_y(r, sm[r][0], sm[r][1], sm[r][2], c, nv[r]);
+                    }
+                }
+                end_sweep();
+            }
+            // the next phase reads the neighbours' positions
+            if (!nbr_wait(a.flags, a.err, cta, nrange, epoch, a.timeout)) return;
+        } else {
+            T cx[R][3], px[R][3], yv[R][3];
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 T s0 = T(0), s1 = T(0), s2 = T(0);
-                if (val[r]) gather(a.GX, r, s0, s1, s2);
-                yv[r][0] = om1 * cx[r][0] + w * ((s0 + rh[r][0]) * id[r]);
-                yv[r][1] = om1 * cx[r][1] + w * ((s1 + rh[r][1]) * id[r]);
-                yv[r][2] = om1 * cx[r][2] + w * ((s2 + rh[r][2]) * id[r]);
-                if (val[r]) stcg4(a.GY, row[r], yv[r][0], yv[r][1], yv[r][2]);
+                if constexpr (kCorr) {
+                    cx[r][0] = cx[r][1] = cx[r][2] = T(0);
+                } else {
+                    cx[r][0] = x0[r][0];
+                    cx[r][1] = x0[r][1];
+                    cx[r][2] = x0[r][2];
+                    if (val[r]) gather(a.P, r, s0, s1, s2);
+                }
+                finish_y(r, s0, s1, s2, cx[r], yv[r]);
             }
             if (!sync()) return;
+            for (int it = 0; it < nsteps; ++it) {
+                const bool last = it == nsteps - 1;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    T s0 = T(0), s1 = T(0), s2 = T(0), n[3];
+                    if (val[r]) gather(a.GY, r, s0, s1, s2);
+                    finish_x(r, s0, s1, s2, yv[r], px[r], it, last, a.GX, n);
+                    px[r][0] = cx[r][0];
+                    px[r][1] = cx[r][1];
+                    px[r][2] = cx[r][2];
+                    cx[r][0] = n[0];
+                    cx[r][1] = n[1];
+                    cx[r][2] = n[2];
+                }
+                if (!sync()) return;
+                if (last) break;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    T s0 = T(0), s1 = T(0), s2 = T(0);
+                    if (val[r]) gather(a.GX, r, s0, s1, s2);
+                    finish_y(r, s0, s1, s2, cx[r], yv[r]);
+                }
+                if (!sync()) return;
+            }
         }
     }
 }
 
-template <typename T, bool kCorr, bool kSmem, bool kL1>
+template <typename T, bool kCorr, int kMode, bool kL1>
 const void* kernel_for(int R) {
     using S = typename std::conditional<kCorr, double, T>::type;
     switch (R) {
-        case 1: return (const void*)k_pd_persistent<T, S, kCorr, kSmem, kL1, 1>;
-        case 2: return (const void*)k_pd_persistent<T, S, kCorr, kSmem, kL1, 2>;
-        case 3: return (const void*)k_pd_persistent<T, S, kCorr, kSmem, kL1, 3>;
-        default: return (const void*)k_pd_persistent<T, S, kCorr, kSmem, kL1, 4>;
+        case 1: return (const void*)k_pd_persistent<T, S, kCorr, kMode, kL1, 1>;
+        case 2: return (const void*)k_pd_persistent<T, S, kCorr, kMode, kL1, 2>;
+        case 3: return (const void*)k_pd_persistent<T, S, kCorr, kMode, kL1, 3>;
+        default: return (const void*)k_pd_persistent<T, S, kCorr, kMode, kL1, 4>;
     }
 }
 
 template <bool kL1>
-const void* kernel_for_l1(bool correction, bool matrix_in_smem, int R) {
-    if (correction)
-        return matrix_in_smem ? kernel_for<float, true, true, kL1>(R) : kernel_for<float, true, false, kL1>(R);
-    return matrix_in_smem ? kernel_for<float, false, true, kL1>(R) : kernel_for<float, false, false, kL1>(R);
+const void* kernel_for_l1(bool correction, int mode, int R) {
+    if (correction) {
+        if (mode == 2) return kernel_for<float, true, 2, kL1>(R);
+        return mode == 1 ? kernel_for<float, true, 1, kL1>(R) : kernel_for<float, true, 0, kL1>(R);
+    }
+    return mode >= 1 ? kernel_for<float, false, 1, kL1>(R) : kernel_for<float, false, 0, kL1>(R);
 }
 
 }  // namespace
 
-const void* persistent_kernel(bool correction, bool matrix_in_smem, bool l1_gather, int rows_per_thread) {
-    return l1_gather ? kernel_for_l1<true>(correction, matrix_in_smem, rows_per_thread)
-                     : kernel_for_l1<false>(correction, matrix_in_smem, rows_per_thread);
+const void* persistent_kernel(bool correction, bool matrix_in_smem, bool band, bool l1_gather, int rows_per_thread) {
+    const int mode = band ? 2 : (matrix_in_smem ? 1 : 0);
+    return l1_gather ? kernel_for_l1<true>(correction, mode, rows_per_thread)
+                     : kernel_for_l1<false>(correction, mode, rows_per_thread);
 }
 
 template <typename S>
 cudaError_t launch_args(const PersistPlan& plan, const PersistArgs<float, S>& args, cudaStream_t s) {
     const bool correction = std::is_same<S, double>::value;
-    const void* f = persistent_kernel(correction, plan.matrix_in_smem, plan.l1_gather, plan.rows_per_thread);
+    const void* f = persistent_kernel(correction, plan.matrix_in_smem, plan.own_max > 0, plan.l1_gather,
+                                      plan.rows_per_thread);
     void* params[] = {(void*)&args};
     return cudaLaunchCooperativeKernel(f, dim3(plan.ctas), dim3(plan.threads), params, plan.smem_bytes, s);
 }

@@ -11,6 +11,8 @@
 namespace pdipc {
 
 constexpr int kMaxCheby = 64;
+// warps per CTA of the persistent solve (its launch bound: 72 registers per thread)
+constexpr int kMaxPersistWarps = 28;
 
 struct PersistPlan {
     bool enabled = false;
@@ -24,7 +26,8 @@ struct PersistPlan {
     size_t smem_bytes = 0;
     int patterns = 0;
     int pattern_width = 0;
-    int band_max = 0;             // > 0: each sweep stages the CTA's column band in shared memory
+    int own_max = 0;              // > 0: the CTA's column band lives in shared memory (needs local_sync)
+    int halo_max = 0;
 };
 
 // T: solver scalar; S: state scalar (T in the direct form, double in the
@@ -47,8 +50,9 @@ struct PersistArgs {
     const V4<T>* CollRhs;
     const V4<T>* PinRhs;
     V4<T>* Aq;
-    V4<T>* GX;
-    V4<T>* GY;
+    V4<T>* GX;   // second-sweep iterates (odd steps in GX2 on the band path)
+    V4<T>* GX2;
+    V4<T>* GY;   // first-sweep iterates
     const T* Delastic;
     const T* Dinert;
     const T* CollDiag;
@@ -83,16 +87,18 @@ struct PersistArgs {
     unsigned* flags;
     const int2* nbr;
     unsigned epoch0;
-    // staged band (band != null, matrix in shared memory): before each sweep a
-    // CTA copies columns [band[c].x, band[c].y) of the gathered vector into
-    // shared memory as three planar arrays of bandMax floats, and gathers
-    // from there (one 4-byte shared load per component instead of an
-    // unaligned 16-byte global gather)
+    // band of the iterate in shared memory (band != null, matrix in shared
+    // memory, neighbour synchronisation): CTA c's matrix rows read columns
+    // [band[c].x, band[c].y).  Its own rows stay in three planar arrays of
+    // ownMax floats that its threads update after every sweep; the halo (the
+    // columns outside its own rows, at most haloMax vertices) is copied from
+    // global memory in two bulk copies per sweep
     const int2* band;
-    int bandMax;
+    int ownMax;
+    int haloMax;
 };
 
-const void* persistent_kernel(bool correction, bool matrix_in_smem, bool l1_gather, int rows_per_thread);
+const void* persistent_kernel(bool correction, bool matrix_in_smem, bool band, bool l1_gather, int rows_per_thread);
 // direct form (FP32 state) and correction form (FP64 state)
 cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, float>& args, cudaStream_t s);
 cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, double>& args, cudaStream_t s);

@@ -633,6 +633,10 @@ private:
                 }
                 o[e - H.nPtr[i]] = (int16_t)off;
             }
+            // padding (value 0) repeats the last column, so a row's columns stay
+            // in order: low halo, own rows, high halo
+            const int len = H.nPtr[i + 1] - H.nPtr[i];
+            for (int k = len; k < patW && len > 0; ++k) o[k] = o[len - 1];
             auto it = pats.emplace(o, (int)pats.size()).first;
             rowPat[i] = it->second;
             if (pats.size() > 4096) fits16 = false;
@@ -649,8 +653,9 @@ private:
             }
             return mx;
         };
-        // columns each CTA's matrix rows read, as a range: the gathered vector's
-        // band that a CTA stages in shared memory once per sweep
+        // columns each CTA's matrix rows read, as a range: the band of the
+        // iterate a CTA keeps in shared memory; returns the largest halo (the
+        // columns outside the CTA's own rows)
         auto col_ranges = [&](int spc, std::vector<int2>& rg) -> int {
             const int ctas = (nsl + spc - 1) / spc;
             rg.assign(ctas, make_int2(0, 0));
@@ -664,7 +669,7 @@ private:
                         hi = std::max(hi, H.nCol[e]);
                     }
                 rg[c] = make_int2(lo, hi + 1);
-                mx = std::max(mx, hi + 1 - lo);
+                mx = std::max(mx, (r0 - lo) + (hi + 1 - r1));
             }
             return mx;
         };
@@ -675,39 +680,49 @@ private:
             if (pass == 0 && !fits16) continue;
             for (int R = 1; R <= 4; ++R) {
                 const int W = std::max(1, (nsl + nsm * R - 1) / (nsm * R));
-                if (W > 32) continue;
+                if (W > kMaxPersistWarps) continue;
                 const int spc = W * R;
                 const int ctas = (nsl + spc - 1) / spc;
                 size_t sm = cta_smem(spc, smem_mat, 0);
                 if (sm > limit) continue;
-                int bandMax = 0;
-                if (smem_mat && prm_.persistent != 4) {
+                int ownMax = 0, haloMax = 0;
+                if (kCorrection && smem_mat && prm_.persistent != 4 && prm_.persistent != 3 &&
+                    W + 1 <= kMaxPersistWarps) {
+                    // correction form: own rows planar, halo as 16-byte vertices, the
+                    // copies' mbarrier; one more warp (no rows) for the neighbour
+                    // flags and the copies.  The direct form keeps the reference's
+                    // summation order (gathers through L1).
                     std::vector<int2> rg;
-                    const int mx = col_ranges(spc, rg);
-                    const size_t smb = cta_smem(spc, smem_mat, a16(3 * (size_t)mx * sizeof(T)));
+                    const int hx = col_ranges(spc, rg);
+                    const int om = spc * kSlice;
+                    const size_t smb =
+                        cta_smem(spc, smem_mat, a16(3 * (size_t)om * sizeof(T)) + (size_t)hx * sizeof(V4<T>) + 16);
                     if (smb <= limit) {
                         sm = smb;
-                        bandMax = mx;
+                        ownMax = om;
+                        haloMax = hx;
                         bandRange.swap(rg);
                     }
                 }
-                const void* f = persistent_kernel(kCorrection, smem_mat, prm_.persistent != 2, R);
+                const int threads = (W + (ownMax > 0 ? 1 : 0)) * 32;
+                const void* f = persistent_kernel(kCorrection, smem_mat, ownMax > 0, prm_.persistent != 2, R);
                 PD_CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
                 int per_sm = 0;
-                PD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, W * 32, sm));
+                PD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, threads, sm));
                 if (per_sm < 1 || ctas > per_sm * nsm) continue;
                 plan_.enabled = true;
                 plan_.matrix_in_smem = smem_mat;
                 plan_.l1_gather = prm_.persistent != 2;
                 plan_.local_sync = prm_.persistent != 3;
                 plan_.ctas = ctas;
-                plan_.threads = W * 32;
+                plan_.threads = threads;
                 plan_.rows_per_thread = R;
                 plan_.slices_per_cta = spc;
                 plan_.smem_bytes = sm;
                 plan_.patterns = smem_mat ? (int)pats.size() : 0;
                 plan_.pattern_width = patW;
-                plan_.band_max = bandMax;
+                plan_.own_max = ownMax;
+                plan_.halo_max = haloMax;
                 break;
             }
         }
@@ -746,7 +761,7 @@ private:
                 nbr[d2].y = std::max(nbr[d2].y, c);
             }
         PD_CK(up(pNbr_, nbr));
-        if (plan_.band_max > 0) PD_CK(up(pBand_, bandRange));
+        if (plan_.own_max > 0) PD_CK(up(pBand_, bandRange));
         PD_CK(zeros(pFlags_, plan_.ctas));
         PD_CK(up(pCtaSlice_, ctaSlice));
         PD_CK(up(pCtaEntry_, ctaEntry));
@@ -778,6 +793,7 @@ private:
             a.PinRhs = d.PinRhs;
             a.Aq = d.Aq;
             a.GX = d.B;
+            a.GX2 = d.C;
             a.GY = d.Y;
             a.Delastic = d.Delastic;
             a.Dinert = d.Dinert;
@@ -806,10 +822,11 @@ private:
             a.err = d.ErrFlags;
             a.flags = pFlags_;
             a.nbr = plan_.local_sync ? pNbr_ : nullptr;
-            a.band = plan_.band_max > 0 ? pBand_ : nullptr;
-            a.bandMax = plan_.band_max;
+            a.band = plan_.own_max > 0 ? pBand_ : nullptr;
+            a.ownMax = plan_.own_max;
+            a.haloMax = plan_.halo_max;
             a.epoch0 = 0;
-            const void* ptrs[] = {a.P, a.Pold, a.Xrest, a.Rhs0, a.CollRhs, a.PinRhs, a.Aq, a.GX, a.GY, a.Delastic,
+            const void* ptrs[] = {a.P, a.Pold, a.Xrest, a.Rhs0, a.CollRhs, a.PinRhs, a.Aq, a.GX, a.GX2, a.GY, a.Delastic,
                                   a.Dinert, a.CollDiag, a.PinFlag, a.PinK, a.lPtr, a.lNbr, a.lRest, a.lLbo,
                                   a.lBend, a.lBendT, a.Strain, a.CurvNorm, a.sliceEntry, a.sliceLen, a.sCol,
                                   a.sVal, a.ctaSlice, a.ctaEntry, a.rowPattern, a.patOff, a.bar, a.err};
