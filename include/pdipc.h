@@ -83,12 +83,12 @@ typedef struct {
                                 (reference behaviour, cpp:1296-1320); 1: rebuild every step */
     int persistent;          /* FP32/mixed PD solve of an outer iteration as one cooperative launch when
                                 the mesh allows it (matrix slice per CTA): 1 CTAs wait only for the CTAs
-                                they exchange rows with; the CTA's column band of the iterate lives in
-                                shared memory when it fits (else gathers through L1), and each sweep sums
-                                the entries on the CTA's own rows while the neighbours' rows are in
-                                flight; 2 neighbour waits, L2-only gathers; 3 grid-wide barriers, gathers
-                                through L1; 4 neighbour waits, gathers through L1 (no band); 0 one launch
-                                per sweep */
+                                they exchange rows with; in mixed precision the CTA's column band of the
+                                iterate lives in shared memory when it fits and each sweep sums the
+                                entries on the CTA's own rows while the neighbours' rows are copied in
+                                (else, and in FP32, gathers through L1); 2 neighbour waits, L2-only
+                                gathers; 3 grid-wide barriers, gathers through L1; 4 neighbour waits,
+                                gathers through L1 (no band); 0 one launch per sweep */
     int reserved[6];
 } pdipc_params;
 
