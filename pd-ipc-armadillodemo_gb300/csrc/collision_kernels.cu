@@ -445,6 +445,31 @@ __global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restric
                                 : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w);
         if (!shared) {
             if constexpr (kRel) {
+                // the swept-box filter first on the high parts alone, with the
+                // distance widened past the largest effect of the dropped low
+                // parts (|low| <= 2^-24 |x|, plus the roundings: < 2^-18 of the
+                // largest coordinate); only the survivors load the low parts and
+                // take the exact filter below
+                bool maybe;
+                {
+                    T xh[4][3], dh[4][3], m = T(0);
+                    const V4<T> o = ld4(X0h, ids[0]);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const V4<T> ah = ld4(X0h, ids[j]), bh = ld4(X1h, ids[j]);
+                        xh[j][0] = ah.x - o.x;
+                        xh[j][1] = ah.y - o.y;
+                        xh[j][2] = ah.z - o.z;
+                        dh[j][0] = bh.x - ah.x;
+                        dh[j][1] = bh.y - ah.y;
+                        dh[j][2] = bh.z - ah.z;
+                        m = dmax(m, dmax(dmax(fabsf(ah.x), fabsf(ah.y)), dmax(fabsf(ah.z), fabsf(bh.x))));
+                        m = dmax(m, dmax(fabsf(bh.y), fabsf(bh.z)));
+                    }
+                    const T wide = (T)slack + m * T(1.0 / 65536.0);
+                    maybe = kPT ? geo::pt_ccd_broad<T>(xh, dh, wide) : geo::ee_ccd_broad<T>(xh, dh, wide);
+                }
+                if (maybe) {
                 T x[4][3], dx[4][3];
                 const V4<T> oh = ld4(X0h, ids[0]), ol = ld4(X0l, ids[0]);
 #pragma unroll
@@ -476,6 +501,7 @@ __global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restric
                         }
                         toi = kPT ? geo::ccd_pt<TC>(xd, dd, eta, max_iter) : geo::ccd_ee<TC>(xd, dd, eta, max_iter);
                     }
+                }
                 }
             } else {
                 TC x[4][3], dx[4][3];
@@ -533,6 +559,41 @@ __global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __res
             continue;
         TC p[4][3];
         if constexpr (kRel) {
+            {  // the box filter on the high parts alone, widened as in k_toi
+                T qh[4][3], m = T(0);
+                const V4<T> o = ld4(Xh, ids[0]);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const V4<T> ah = ld4(Xh, ids[j]);
+                    qh[j][0] = ah.x - o.x;
+                    qh[j][1] = ah.y - o.y;
+                    qh[j][2] = ah.z - o.z;
+                    m = dmax(m, dmax(fabsf(ah.x), dmax(fabsf(ah.y), fabsf(ah.z))));
+                }
+                const T wide = (T)cc.dh + m * T(1.0 / 65536.0);
+                bool farh = false;
+                if (kPT) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const T tmin = geo::mn3(qh[1][k], qh[2][k], qh[3][k]);
+                        const T tmax = geo::mx3(qh[1][k], qh[2][k], qh[3][k]);
+                        if ((qh[0][k] - tmax) > wide || (tmin - qh[0][k]) > wide) farh = true;
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const T mina = dmin(qh[0][k], qh[1][k]), maxa = dmax(qh[0][k], qh[1][k]);
+                        const T minb = dmin(qh[2][k], qh[3][k]), maxb = dmax(qh[2][k], qh[3][k]);
+                        if ((mina - maxb) > wide || (minb - maxa) > wide) farh = true;
+                    }
+                }
+                if (farh) continue;
+                // the boxes' Euclidean gap also bounds the distance from below: a
+                // pair beyond sqrt(2) dhat (after the widening) fails the filter below
+                const T g = dsqrt(kPT ? geo::box_gap2<T, 1, 3>(qh, qh + 1) : geo::box_gap2<T, 2, 2>(qh, qh + 2)) -
+                            T(2) * (wide - (T)cc.dh);
+                if (g > T(0) && g * g > T(2) * (T)cc.dh2) continue;
+            }
             T q[4][3];
             const V4<T> oh = ld4(Xh, ids[0]), ol = ld4(Xl, ids[0]);
 #pragma unroll

@@ -154,6 +154,30 @@ __device__ __forceinline__ bool ee_ccd_broad(const R (*x)[3], const R (*dx)[3], 
 template <typename R>
 __device__ __forceinline__ R sqn(const R* a) { return dot3(a, a); }
 
+// Squared gap between the bounding boxes of points a[0..na) and b[0..nb): a
+// lower bound of the squared distance between the primitives they span.
+template <typename R, int NA, int NB>
+__device__ __forceinline__ R box_gap2(const R (*a)[3], const R (*b)[3]) {
+    R g2 = R(0);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        R amin = a[0][k], amax = a[0][k], bmin = b[0][k], bmax = b[0][k];
+#pragma unroll
+        for (int j = 1; j < NA; ++j) {
+            amin = dmin(amin, a[j][k]);
+            amax = dmax(amax, a[j][k]);
+        }
+#pragma unroll
+        for (int j = 1; j < NB; ++j) {
+            bmin = dmin(bmin, b[j][k]);
+            bmax = dmax(bmax, b[j][k]);
+        }
+        const R sep = dmax(dmax(bmin - amax, amin - bmax), R(0));
+        g2 += sep * sep;
+    }
+    return g2;
+}
+
 // ccdVertexTriangleToi (cu:2460-2529): additive CCD, at most max_iter conservative steps
 template <typename R>
 __device__ R ccd_pt(R (*x)[3], R (*dx)[3], R eta, int max_iter) {
@@ -165,6 +189,10 @@ __device__ R ccd_pt(R (*x)[3], R (*dx)[3], R eta, int max_iter) {
     m2 = dmax(m2, sqn(dx[3]));
     const R maxd = dsqrt(sqn(dx[0])) + dsqrt(m2);
     if (maxd == R(0)) return R(1);
+    // The first conservative step below returns 1 when 0.9 d > maxd.  The box
+    // gap bounds d from below: when even half of it clears maxd, return that 1
+    // without the distance (the factor 2 is far above the distance's rounding).
+    if (R(0.81) * box_gap2<R, 1, 3>(x, x + 1) > R(4) * maxd * maxd) return R(1);
     R a, b, c, dd[3];
     R d2 = vtx_tri(x[0], x[1], x[2], x[3], &a, &b, &c, dd);
     R dc = dsqrt(d2);
@@ -211,6 +239,7 @@ __device__ R ccd_ee(R (*x)[3], R (*dx)[3], R eta, int max_iter) {
     const R m0 = dmax(sqn(dx[0]), sqn(dx[1])), m1 = dmax(sqn(dx[2]), sqn(dx[3]));
     const R maxd = dsqrt(m0) + dsqrt(m1);
     if (maxd == R(0)) return R(1);
+    if (R(0.81) * box_gap2<R, 2, 2>(x, x + 2) > R(4) * maxd * maxd) return R(1);  // as in ccd_pt
     R r, s, dd[3];
     R d2 = edge_edge_sq(x[0], x[1], x[2], x[3], &r, &s, dd);
     R f = d2;

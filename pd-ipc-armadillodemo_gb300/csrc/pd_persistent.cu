@@ -209,8 +209,9 @@ __device__ __forceinline__ void stcg4(V4<double>* p, int i, double x, double y, 
 // kMode: 0 matrix streamed from L2; 1 matrix in shared memory, gathers from
 // global memory; 2 matrix and the band of the iterate in shared memory
 template <typename T, typename S, bool kCorr, int kMode, bool kL1, int R>
-__global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(PersistArgs<T, S> a) {
+__global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(const __grid_constant__ PersistArgs<T, S> a) {
     constexpr bool kSmem = kMode >= 1;
+    constexpr bool band = kMode == 2;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int abort_s;  // band path: a neighbour wait failed, every warp returns
     const int cta = blockIdx.x;
@@ -220,7 +221,8 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(Pers
     const int E = ee - eb;
     T* sval = reinterpret_cast<T*>(smem);
     int16_t* spat = reinterpret_cast<int16_t*>(smem + ((size_t)E * sizeof(T) + 15) / 16 * 16);
-    const size_t patBytes = ((size_t)a.patterns * a.patW * sizeof(int16_t) + 15) / 16 * 16;
+    // (the band path reads the patterns from parameter space)
+    const size_t patBytes = band ? 0 : ((size_t)a.patterns * a.patW * sizeof(int16_t) + 15) / 16 * 16;
     // the band of the iterate: own rows as three planar arrays, the halo as
     // 16-byte vertices (copied in bulk), then the copies' mbarrier
     unsigned char* bandp = smem + ((size_t)E * sizeof(T) + 15) / 16 * 16 + patBytes;
@@ -229,11 +231,11 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(Pers
     T* oz = oy + a.ownMax;
     V4<T>* hv = reinterpret_cast<V4<T>*>(bandp + (3 * (size_t)a.ownMax * sizeof(T) + 15) / 16 * 16);
     uint64_t* mbar = reinterpret_cast<uint64_t*>(hv + a.haloMax);
-    constexpr bool band = kMode == 2;
     const int2 brange = band ? a.band[cta] : make_int2(0, 0);
     if (kSmem) {
         for (int q = threadIdx.x; q < E; q += blockDim.x) sval[q] = __ldg(a.sVal + eb + q);
-        for (int q = threadIdx.x; q < a.patterns * a.patW; q += blockDim.x) spat[q] = __ldg(a.patOff + q);
+        if (!band)
+            for (int q = threadIdx.x; q < a.patterns * a.patW; q += blockDim.x) spat[q] = __ldg(a.patOff + q);
     }
     if (band && threadIdx.x == 0) {
         mbar_init(mbar, 1);
@@ -262,7 +264,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(Pers
     auto entry = [&](int r, int k, T& v, int& j) {
         if (kSmem) {
             v = sval[gb[r] - eb + 32 * k];
-            j = rowof(r) + (int)spat[pid[r] + k];
+            j = rowof(r) + (int)(band ? a.patc[pid[r] + k] : spat[pid[r] + k]);
         } else {
             v = __ldg(a.sVal + gb[r] + 32 * k);
             j = __ldg(a.sCol + gb[r] + 32 * k);
@@ -377,7 +379,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(Pers
     }
     auto own_sum = [&](int r, T& s0, T& s1, T& s2) {
         const int k1 = pk[r] >> 20;
-#pragma unroll 4
+#pragma unroll 8
         for (int k = (pk[r] >> 10) & 1023; k < k1; ++k) {
             T v;
             int j;
@@ -389,7 +391,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(Pers
         }
     };
     auto halo_range = [&](int r, int k0, int k1, int base, T& s0, T& s1, T& s2) {
-#pragma unroll 4
+#pragma unroll 8
         for (int k = k0; k < k1; ++k) {
             T v;
             int j;

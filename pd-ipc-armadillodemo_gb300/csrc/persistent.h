@@ -13,6 +13,9 @@ namespace pdipc {
 constexpr int kMaxCheby = 64;
 // warps per CTA of the persistent solve (its launch bound: 72 registers per thread)
 constexpr int kMaxPersistWarps = 28;
+// band path: the column-offset patterns travel in the launch's parameter space
+// (read through the constant cache, off the shared-memory pipe)
+constexpr int kParamPatterns = 4096;
 
 struct PersistPlan {
     bool enabled = false;
@@ -76,6 +79,7 @@ struct PersistArgs {
     const int* ctaEntry;    // first SELL entry of each CTA (ctas + 1)
     const int* rowPattern;  // pattern id of every row (matrix in shared memory)
     const int16_t* patOff;  // [patterns x pattern_width] column offsets
+    int16_t patc[kParamPatterns];  // band path: the same table (patterns x pattern_width <= kParamPatterns)
     int patterns;
     int patW;
     // grid barrier: [0] generation, [1] arrival counter

@@ -643,13 +643,15 @@ private:
         }
         const size_t patBytes = fits16 ? pats.size() * (size_t)patW * sizeof(int16_t) : 0;
         auto a16 = [](size_t b) { return (b + 15) / 16 * 16; };
+        // matrix values (+ the pattern table, except on the band path, which reads
+        // it from parameter space) + the band
         auto cta_smem = [&](int spc, bool smem_mat, size_t band_bytes) -> size_t {
             if (!smem_mat) return 0;
             size_t mx = 0;
             for (int c = 0; c * spc < nsl; ++c) {
                 const int s0 = c * spc, s1 = std::min(nsl, s0 + spc);
                 const size_t E = (size_t)(soff[s1] - soff[s0]);
-                mx = std::max(mx, a16(E * sizeof(T)) + a16(patBytes) + band_bytes);
+                mx = std::max(mx, a16(E * sizeof(T)) + (band_bytes ? 0 : a16(patBytes)) + band_bytes);
             }
             return mx;
         };
@@ -687,7 +689,7 @@ private:
                 if (sm > limit) continue;
                 int ownMax = 0, haloMax = 0;
                 if (kCorrection && smem_mat && prm_.persistent != 4 && prm_.persistent != 3 &&
-                    W + 1 <= kMaxPersistWarps) {
+                    W + 1 <= kMaxPersistWarps && pats.size() * (size_t)patW <= (size_t)kParamPatterns) {
                     // correction form: own rows planar, halo as 16-byte vertices, the
                     // copies' mbarrier; one more warp (no rows) for the neighbour
                     // flags and the copies.  The direct form keeps the reference's
@@ -816,6 +818,8 @@ private:
             a.ctaEntry = pCtaEntry_;
             a.rowPattern = pRowPat_;
             a.patOff = pPatOff_;
+            std::fill(a.patc, a.patc + kParamPatterns, (int16_t)0);
+            if (plan_.own_max > 0) std::copy(patOff.begin(), patOff.end(), a.patc);
             a.patterns = plan_.patterns;
             a.patW = patW;
             a.bar = pBar_;
