@@ -309,7 +309,9 @@ def run_ours(args):
     sim.set_state(x_end)
     sweep_ms, sweep_bytes = sim.sweep_timing(400)
     sweep_gbs = sweep_bytes / (sweep_ms * 1e-3) / 1e9
-    pd_kernel = {2: "k_pd_persistent (cooperative, matrix values in shared memory)",
+    pd_kernel = {3: "k_pd_persistent (cooperative, matrix values and the iterate's band in shared memory, "
+                    "halo by bulk copies)",
+                 2: "k_pd_persistent (cooperative, matrix values in shared memory)",
                  1: "k_pd_persistent (cooperative, matrix from L2)",
                  0: "PD solve as a CUDA graph of per-sweep kernels"}[st_end["pd_path"]]
     state_bytes = 16 if args.precision == "fp32" else 32

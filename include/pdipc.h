@@ -113,7 +113,8 @@ typedef struct {
     double device_ms;            /* device time of the last pdipc_step call: CUDA events recorded on the
                                     context's stream around every step, summed */
     int32_t pd_path;             /* 0: one launch per sweep; 1: persistent, matrix from L2;
-                                    2: persistent, matrix values in shared memory */
+                                    2: persistent, matrix values in shared memory; 3: persistent,
+                                    matrix values and the iterate's band in shared memory */
     int32_t pd_ctas;             /* CTAs of the persistent solve (0 if not used) */
     int64_t pd_solves;           /* projective-dynamics solves (one per outer iteration) in the last call */
     double pd_solve_ms;          /* their device time: CUDA events on the context's stream around each solve */

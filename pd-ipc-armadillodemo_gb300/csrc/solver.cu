@@ -361,7 +361,7 @@ public:
         s->device_bytes = bytes_;
         s->kernel_launches = launches_;
         s->device_ms = device_ms_;
-        s->pd_path = plan_.enabled ? (plan_.matrix_in_smem ? 2 : 1) : 0;
+        s->pd_path = plan_.enabled ? (plan_.own_max > 0 ? 3 : plan_.matrix_in_smem ? 2 : 1) : 0;
         s->pd_ctas = plan_.enabled ? plan_.ctas : 0;
         s->pd_solves = pd_solves_;
         s->pd_solve_ms = pd_ms_;
@@ -688,7 +688,7 @@ private:
                 size_t sm = cta_smem(spc, smem_mat, 0);
                 if (sm > limit) continue;
                 int ownMax = 0, haloMax = 0;
-                if (kCorrection && smem_mat && prm_.persistent != 4 && prm_.persistent != 3 &&
+                if (kCorrection && smem_mat && prm_.persistent == 1 &&
                     W + 1 <= kMaxPersistWarps && pats.size() * (size_t)patW <= (size_t)kParamPatterns) {
                     // correction form: own rows planar, halo as 16-byte vertices, the
                     // copies' mbarrier; one more warp (no rows) for the neighbour

@@ -211,7 +211,9 @@ def test_persistent_solve_matches_per_sweep_launches(prec, atol, n, variant, bui
     sc = small_scene(n, 2)
     a = pdipc.Simulator(sc, prec, persistent=variant)
     b = pdipc.Simulator(sc, prec, persistent=0)
-    assert a.stats()["pd_path"] in (1, 2) and b.stats()["pd_path"] == 0
+    assert a.stats()["pd_path"] in (1, 2, 3) and b.stats()["pd_path"] == 0
+    # the band (path 3) is the default persistent path of the mixed mode only
+    assert (a.stats()["pd_path"] == 3) == (variant == 1 and prec == "mixed")
     X = np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics])
     V = np.random.default_rng(5).uniform(-0.1, 0.1, (sc.n_sim, 3))
     assert np.abs(a.stage_pd(X, V) - b.stage_pd(X, V)).max() < atol
