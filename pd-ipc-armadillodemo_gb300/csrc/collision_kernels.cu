@@ -422,6 +422,34 @@ __device__ __forceinline__ void block_min_to(TC v, TC* dst) {
     }
 }
 
+// Resident blocks per SM asked of the candidate kernels: they are latency-bound
+// gathers, and four blocks (64 registers) measured 25% faster than two for the
+// FP32 arithmetic of the mixed and FP32 modes, despite a few spills; the FP64
+// mode keeps the compiler's choice.
+template <typename T>
+constexpr int kCandBlocks = sizeof(T) == 4 ? 4 : 1;
+
+// The FP64 time of impact of one candidate from the FP64 state (coordinates
+// relative to its first vertex).  Out of line: few candidates reach it, and
+// keeping its registers out of k_toi's main loop keeps that loop's occupancy.
+template <typename TC, bool kPT>
+__device__ __noinline__ TC toi_refine(const V4<TC>* __restrict__ X0, const V4<TC>* __restrict__ X1, const int* ids,
+                                      TC eta, int max_iter) {
+    TC xd[4][3], dd[4][3];
+    const V4<TC> o = ld4(X0, ids[0]);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const V4<TC> a = ld4(X0, ids[j]), b = ld4(X1, ids[j]);
+        xd[j][0] = a.x - o.x;
+        xd[j][1] = a.y - o.y;
+        xd[j][2] = a.z - o.z;
+        dd[j][0] = b.x - a.x;
+        dd[j][1] = b.y - a.y;
+        dd[j][2] = b.z - a.z;
+    }
+    return kPT ? geo::ccd_pt<TC>(xd, dd, eta, max_iter) : geo::ccd_ee<TC>(xd, dd, eta, max_iter);
+}
+
 // getImpactOfTimeKernel (cu:2610-2704): skip pairs sharing a vertex, swept-AABB
 // filter with slack, additive CCD; global minimum by integer atomicMin.
 // kRel (mixed precision): coordinates relative to the pair's first vertex,
@@ -430,7 +458,7 @@ __device__ __forceinline__ void block_min_to(TC v, TC* dst) {
 // (toi < 1) re-evaluated in FP64 from the FP64 state, so the minimum is an
 // FP64 time of impact.
 template <typename T, typename TC, bool kPT, bool kRel>
-__global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restrict__ cand,
+__global__ void __launch_bounds__(kBlock, kCandBlocks<T>) k_toi(int64_t n, const int4* __restrict__ cand,
                                                 const V4<TC>* __restrict__ X0, const V4<TC>* __restrict__ X1,
                                                 const V4<T>* __restrict__ X0h, const V4<T>* __restrict__ X0l,
                                                 const V4<T>* __restrict__ X1h, const V4<T>* __restrict__ X1l,
@@ -486,21 +514,7 @@ __global__ void __launch_bounds__(kBlock) k_toi(int64_t n, const int4* __restric
                 const bool hit = kPT ? geo::pt_ccd_broad<T>(x, dx, (T)slack) : geo::ee_ccd_broad<T>(x, dx, (T)slack);
                 if (hit) {
                     const T tf = kPT ? geo::ccd_pt<T>(x, dx, (T)eta, max_iter) : geo::ccd_ee<T>(x, dx, (T)eta, max_iter);
-                    if (tf < T(1)) {
-                        TC xd[4][3], dd[4][3];
-                        const V4<TC> o = ld4(X0, ids[0]);
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            const V4<TC> a = ld4(X0, ids[j]), b = ld4(X1, ids[j]);
-                            xd[j][0] = a.x - o.x;
-                            xd[j][1] = a.y - o.y;
-                            xd[j][2] = a.z - o.z;
-                            dd[j][0] = b.x - a.x;
-                            dd[j][1] = b.y - a.y;
-                            dd[j][2] = b.z - a.z;
-                        }
-                        toi = kPT ? geo::ccd_pt<TC>(xd, dd, eta, max_iter) : geo::ccd_ee<TC>(xd, dd, eta, max_iter);
-                    }
+                    if (tf < T(1)) toi = toi_refine<TC, kPT>(X0, X1, ids, eta, max_iter);
                 }
                 }
             } else {
@@ -546,7 +560,7 @@ struct ContactConsts {
 // the right-hand side accumulated as w * (target - x) so the later residual
 // needs no cancellation.
 template <typename T, typename TC, bool kPT, bool kRel>
-__global__ void __launch_bounds__(kBlock) k_contact(int64_t n, const int4* __restrict__ cand,
+__global__ void __launch_bounds__(kBlock, kCandBlocks<T>) k_contact(int64_t n, const int4* __restrict__ cand,
                                                     const V4<TC>* __restrict__ X, const V4<T>* __restrict__ Xh,
                                                     const V4<T>* __restrict__ Xl, const TC* __restrict__ mass,
                                                     ContactConsts<TC> cc, T* __restrict__ diag,
