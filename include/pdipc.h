@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PDIPC_ABI_VERSION 3
+#define PDIPC_ABI_VERSION 4
 
 typedef struct pdipc_ctx pdipc_ctx;
 
@@ -322,6 +322,52 @@ pdipc_status pdipc_stage_pd(pdipc_ctx* ctx, const double* X, const double* V, do
  * must move (8 per stored matrix entry + 40 per row: x, rhs and output xyz,
  * inverse diagonal; FP32 sizes, double value sizes in FP64 mode). */
 pdipc_status pdipc_stage_sweep_timing(pdipc_ctx* ctx, int launches, double* avg_ms, double* bytes);
+
+/* The reference's penalty / discrete-collision contact path
+ * (Simulator/PD-IPC/PdIpcGpuFunc.cu:2933-3740).  The reference declares these
+ * kernels beside the IPC path, but its step never calls them (PdIpcSimulator.cpp
+ * only allocates the zero force buffer that predictiveKernel reads), so the
+ * library offers them as stages on a context's tables and the step does not
+ * use them either.
+ *   - Each penalty stage starts from zero forces and hit counts, accumulates a
+ *     per-vertex penalty force (force: 3*n_total) and hit count (times: n_total),
+ *     then applies uniformPenaltyForceKernal (cu:3140-3195) to the n_sim
+ *     simulated vertices with at least one hit: the force becomes its mean over
+ *     the hits minus damping*v, and v (V: 3*n_sim, read and overwritten) keeps
+ *     0.9 of its part across the mean force and -0.4 of its part along it.
+ *   - Arithmetic in the state precision (double in the FP64 and mixed modes). */
+
+/* prediticeDCPositionKernel (cu:2933-2981): sn = x + dt (v + dt m^-1 f_gravity)
+ * for the n_sim simulated vertices (X, sn: 3*n_sim); a pinned vertex keeps x and
+ * its velocity in V (3*n_sim, in/out) becomes 0. */
+pdipc_status pdipc_stage_penalty_predict(pdipc_ctx* ctx, const double* X, double* V, double* sn);
+
+/* computePenaltyForceHost (cu:3198-3246) over the candidates of the last broad
+ * phase: a pair sharing no vertex whose swept boxes (from x0 along dir, both
+ * 3*n_total) meet within 1e-4 and whose additive CCD time of impact is below 1
+ * is pushed apart at x0 + dir with stiffness * distance along the closest-point
+ * vector (point-triangle: -3f on the point, f on each face vertex, f = n d k/3;
+ * edge-edge: -f on the first edge's vertices, f on the second's, f = n d k/2). */
+pdipc_status pdipc_stage_penalty_ccd(pdipc_ctx* ctx, const double* x0, const double* dir, double stiffness,
+                                     double damping, double* V, double* force, int* times);
+
+/* applyPenaltyForceForFloorHost (cu:3273-3305): a simulated vertex of x
+ * (3*n_total) below y = 0 gets the force (0, -y*stiffness, 0) and one hit. */
+pdipc_status pdipc_stage_penalty_floor(pdipc_ctx* ctx, const double* x, double stiffness, double damping,
+                                       double* V, double* force, int* times);
+
+/* computeDcdPenaltyForceHost (cu:3690-3738) over n_pairs face pairs (2 ints
+ * each: indices into the context's collision faces, numbered like its vertices:
+ * cloths and volumetric boundaries in add order, then statics): a pair sharing
+ * no vertex whose triangles intersect (separating-axis test, triContact
+ * cu:3391-3468) pushes each vertex of a triangle whose first vertex is simulated
+ * out of the other triangle's plane (through its second vertex) along that
+ * plane's unit normal with stiffness * depth, when it lies behind the plane; the
+ * other triangle's vertices take -1/3 of each such force.  Two faces of the
+ * same model use self_stiffness.  PDIPC_ERR_ARG for a face index out of range. */
+pdipc_status pdipc_stage_penalty_dcd(pdipc_ctx* ctx, const double* x, const int* face_pairs, int64_t n_pairs,
+                                     double stiffness, double self_stiffness, double damping, double* V,
+                                     double* force, int* times);
 
 /* Topology precompute of one mesh, on the host (no device needed):
  * sorted unique edges (Model/TriangleMesh/BaseSurfaceMesh.cpp:219-275), the grid

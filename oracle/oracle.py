@@ -55,6 +55,9 @@ def lib():
         L.orc_toi.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
         L.orc_contact.argtypes = [C.c_void_p, _dp, _dp, _dp, _i64p]
         L.orc_stage_pd.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.orc_penalty_predict.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.orc_penalty.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _ip, C.c_longlong, C.c_double, C.c_double,
+                                  C.c_double, _dp, _dp, _ip]
         L.orc_mesh_topology.argtypes = [_dp, C.c_int, _ip, C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, C.c_int,
                                         _ip, C.c_int, _ip, _ip, _ip, _ip, _ip]
         _lib = L
@@ -180,6 +183,34 @@ class Oracle:
         g = C.c_double()
         _check(lib().orc_toi(self.h, _d(x0), _d(x1), _d(tp), _d(te), C.byref(g)), "toi")
         return tp[:npt], te[:nee], g.value
+
+    # -- the reference's penalty / discrete-collision path (PdIpcGpuFunc.cu:2933-3740) --------
+    def penalty_predict(self, X, V):
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        V = np.array(V, dtype=np.float64, order="C")
+        sn = np.empty((self.n_sim, 3), np.float64)
+        _check(lib().orc_penalty_predict(self.h, _d(X), _d(V), _d(sn)), "penalty_predict")
+        return sn, V
+
+    def _penalty(self, kind, x, d, fp, k, kself, damping, V):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        d = np.ascontiguousarray(d if d is not None else x, dtype=np.float64)
+        fp = np.ascontiguousarray(fp if fp is not None else np.zeros((0, 2)), dtype=np.int32).reshape(-1, 2)
+        V = np.array(V, dtype=np.float64, order="C")
+        F = np.empty((self.n_total, 3), np.float64)
+        t = np.empty(self.n_total, np.int32)
+        _check(lib().orc_penalty(self.h, kind, _d(x), _d(d), _i(fp) if fp.size else None, fp.shape[0], k, kself,
+                                 damping, _d(V), _d(F), _i(t)), "penalty")
+        return F, t, V
+
+    def penalty_ccd(self, x0, d, stiffness, damping, V):
+        return self._penalty(0, x0, d, None, stiffness, 0.0, damping, V)
+
+    def penalty_floor(self, x, stiffness, damping, V):
+        return self._penalty(1, x, None, None, stiffness, 0.0, damping, V)
+
+    def penalty_dcd(self, x, face_pairs, stiffness, self_stiffness, damping, V):
+        return self._penalty(2, x, None, face_pairs, stiffness, self_stiffness, damping, V)
 
     def stage_pd(self, X, V):
         X = np.ascontiguousarray(X, dtype=np.float64)

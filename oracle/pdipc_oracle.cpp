@@ -35,6 +35,8 @@
 #include <numeric>
 #include <set>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -1573,6 +1575,216 @@ struct Sim {
     }
 };
 
+// ---------------- penalty / discrete-collision path ----------------
+// The reference's alternative contact path (PdIpcGpuFunc.cu:2933-3740), never
+// called by its step.  Restated on a Sim's tables: candidate lists of the last
+// broad phase, collision faces, masses, gravity and pins.  Arithmetic in the
+// CCD/contact scalar TC; forces and hits accumulate in candidate (or pair) order.
+template <typename TC>
+static TC pen_dot(const TC* a, const TC* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+template <typename TC>
+static void pen_cross(const TC* a, const TC* b, TC* r) {
+    r[0] = a[1] * b[2] - a[2] * b[1];
+    r[1] = a[2] * b[0] - a[0] * b[2];
+    r[2] = a[0] * b[1] - a[1] * b[0];
+}
+// project6 (cu:3371-3389)
+template <typename TC>
+static bool pen_project6(const TC* ax, const TC (*p)[3], const TC (*q)[3]) {
+    TC P[3], Q[3];
+    for (int j = 0; j < 3; ++j) { P[j] = pen_dot(ax, p[j]); Q[j] = pen_dot(ax, q[j]); }
+    TC mx1 = P[0], mn1 = P[0], mx2 = Q[0], mn2 = Q[0];
+    for (int j = 1; j < 3; ++j) {
+        if (P[j] > mx1) mx1 = P[j];
+        if (P[j] < mn1) mn1 = P[j];
+        if (Q[j] > mx2) mx2 = Q[j];
+        if (Q[j] < mn2) mn2 = Q[j];
+    }
+    if (mn1 > mx2) return false;
+    if (mn2 > mx1) return false;
+    return true;
+}
+// triContact (cu:3391-3468): separating axes n1, m1, e_a x f_b, e_a x n1, f_b x m1
+template <typename TC>
+static bool pen_tri_contact(const TC (*A)[3], const TC (*B)[3]) {
+    TC p[3][3], q[3][3], e[3][3], f[3][3], n1[3], m1[3], ax[3];
+    for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) { p[j][k] = A[j][k] - A[0][k]; q[j][k] = B[j][k] - A[0][k]; }
+    for (int k = 0; k < 3; ++k) {
+        e[0][k] = p[1][k] - p[0][k]; e[1][k] = p[2][k] - p[1][k]; e[2][k] = p[0][k] - p[2][k];
+        f[0][k] = q[1][k] - q[0][k]; f[1][k] = q[2][k] - q[1][k]; f[2][k] = q[0][k] - q[2][k];
+    }
+    pen_cross(e[0], e[1], n1);
+    pen_cross(f[0], f[1], m1);
+    if (!pen_project6(n1, p, q) || !pen_project6(m1, p, q)) return false;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) { pen_cross(e[a], f[b], ax); if (!pen_project6(ax, p, q)) return false; }
+    for (int a = 0; a < 3; ++a) { pen_cross(e[a], n1, ax); if (!pen_project6(ax, p, q)) return false; }
+    for (int b = 0; b < 3; ++b) { pen_cross(f[b], m1, ax); if (!pen_project6(ax, p, q)) return false; }
+    return true;
+}
+
+template <typename SimT>
+struct Penalty {
+    using T = typename std::remove_reference<decltype(std::declval<SimT>().X)>::type::value_type;
+    using TC = typename std::remove_reference<decltype(std::declval<SimT>().collMass)>::type::value_type;
+    SimT& s;
+    std::vector<TC> F;
+    std::vector<int> times;
+    explicit Penalty(SimT& sim) : s(sim), F(3 * (size_t)sim.ntot, TC(0)), times(sim.ntot, 0) {}
+
+    void add(int i, TC fx, TC fy, TC fz) { F[3 * (size_t)i] += fx; F[3 * (size_t)i + 1] += fy; F[3 * (size_t)i + 2] += fz; }
+
+    // prediticeDCPositionKernel (cu:2933-2981)
+    void predict(const double* X, double* V, double* sn) {
+        const TC dt = (TC)s.prm.time_step;
+        for (int i = 0; i < s.nsim; ++i) {
+            if (s.pinFlag[i] != -1) {
+                for (int k = 0; k < 3; ++k) { V[3 * i + k] = 0.0; sn[3 * i + k] = (double)(TC)X[3 * i + k]; }
+                continue;
+            }
+            const TC m = (TC)s.invMass[i] * dt;
+            for (int k = 0; k < 3; ++k) {
+                TC v = (TC)V[3 * i + k] + m * (TC)s.grav[3 * (size_t)i + k];
+                v *= dt;
+                sn[3 * i + k] = (double)((TC)X[3 * i + k] + v);
+            }
+        }
+    }
+    // computePenaltyForceKernal (cu:3013-3138)
+    void ccd(const double* x0, const double* d, TC k) {
+        auto one = [&](const std::array<int, 4>& c, bool isPT) {
+            if (isPT ? (c[0] == c[1] || c[0] == c[2] || c[0] == c[3])
+                     : (c[0] == c[2] || c[0] == c[3] || c[1] == c[2] || c[1] == c[3]))
+                return;
+            TC x[4][3], dx[4][3], tx[4][3];
+            for (int j = 0; j < 4; ++j)
+                for (int q = 0; q < 3; ++q) {
+                    x[j][q] = (TC)x0[3 * (size_t)c[j] + q];
+                    dx[j][q] = (TC)d[3 * (size_t)c[j] + q];
+                    tx[j][q] = x[j][q] + dx[j][q];
+                }
+            const TC slack = (TC)1e-4;
+            const bool broad = isPT ? SimT::pt_ccd_broad(x[0], x[1], x[2], x[3], dx[0], dx[1], dx[2], dx[3], slack)
+                                    : SimT::ee_ccd_broad(x[0], x[1], x[2], x[3], dx[0], dx[1], dx[2], dx[3], slack);
+            if (!broad) return;
+            const TC toi = isPT ? s.ccd_pt(x[0], dx[0], x[1], dx[1], x[2], dx[2], x[3], dx[3])
+                                : s.ccd_ee(x[0], dx[0], x[1], dx[1], x[2], dx[2], x[3], dx[3]);
+            if (!(toi < (TC)1)) return;
+            TC dir[3], f[3];
+            if (isPT) {
+                TC a, b, cc;
+                const TC dist = std::sqrt(SimT::vtx_tri(tx[0], tx[1], tx[2], tx[3], &a, &b, &cc, dir));
+                for (int q = 0; q < 3; ++q) f[q] = dir[q] * dist * k / (TC)3;
+                add(c[0], -f[0] * (TC)3, -f[1] * (TC)3, -f[2] * (TC)3);
+                for (int j = 1; j < 4; ++j) add(c[j], f[0], f[1], f[2]);
+            } else {
+                TC r, ss;
+                const TC dist = std::sqrt(SimT::edge_edge_sq(tx[0], tx[1], tx[2], tx[3], &r, &ss, dir));
+                for (int q = 0; q < 3; ++q) f[q] = dir[q] * dist * k / (TC)2;
+                add(c[0], -f[0], -f[1], -f[2]);
+                add(c[1], -f[0], -f[1], -f[2]);
+                add(c[2], f[0], f[1], f[2]);
+                add(c[3], f[0], f[1], f[2]);
+            }
+            for (int j = 0; j < 4; ++j) ++times[c[j]];
+        };
+        for (const auto& c : s.pt) one(c, true);
+        for (const auto& c : s.ee) one(c, false);
+    }
+    // applyPenaltyForceForFloorKernal (cu:3248-3271)
+    void floor(const double* x, TC k) {
+        for (int i = 0; i < s.nsim; ++i) {
+            const TC y = (TC)x[3 * (size_t)i + 1];
+            if (y < (TC)0) {
+                F[3 * (size_t)i] = 0;
+                F[3 * (size_t)i + 1] = -y * k;
+                F[3 * (size_t)i + 2] = 0;
+                times[i] = 1;
+            }
+        }
+    }
+    // computeDcdPenaltyForceKernal (cu:3487-3688) over face pairs
+    void dcd(const double* x, const int* fp, long long np, TC k, TC kself) {
+        std::vector<int> model(s.ntot, 0);
+        {
+            int base = 0, id = 0;
+            for (int pass = 0; pass < 2; ++pass)
+                for (const auto& m : s.models)
+                    if ((pass == 0) != m.is_static) {
+                        std::fill(model.begin() + base, model.begin() + base + m.nv, id++);
+                        base += m.nv;
+                    }
+        }
+        auto normal = [](const TC (*P)[3], TC* n) {
+            TC a[3], b[3];
+            for (int q = 0; q < 3; ++q) { a[q] = P[1][q] - P[0][q]; b[q] = P[2][q] - P[0][q]; }
+            pen_cross(a, b, n);
+            const TC len = std::sqrt(pen_dot(n, n));
+            for (int q = 0; q < 3; ++q) n[q] /= len;
+        };
+        // projectToTriangle (cu:3470-3485): the plane through the other triangle's second vertex
+        auto push = [&](const std::array<int, 3>& pv, const TC (*P)[3], const std::array<int, 3>& qv, const TC (*Q)[3],
+                        const TC* nq, TC stiff) {
+            for (int j = 0; j < 3; ++j) {
+                TC w[3], dir[3];
+                for (int q = 0; q < 3; ++q) w[q] = P[j][q] - Q[1][q];
+                const TC c = pen_dot(w, nq);
+                for (int q = 0; q < 3; ++q) dir[q] = c * nq[q];
+                const TC len = std::sqrt(pen_dot(dir, dir));
+                for (int q = 0; q < 3; ++q) dir[q] /= len;
+                if (pen_dot(dir, nq) < (TC)0) {
+                    const TC f0 = nq[0] * len * stiff, f1 = nq[1] * len * stiff, f2 = nq[2] * len * stiff;
+                    add(pv[j], f0, f1, f2);
+                    for (int m = 0; m < 3; ++m) add(qv[m], -f0 / (TC)3, -f1 / (TC)3, -f2 / (TC)3);
+                    ++times[pv[j]];
+                    for (int m = 0; m < 3; ++m) ++times[qv[m]];
+                }
+            }
+        };
+        for (long long t = 0; t < np; ++t) {
+            const auto& fa = s.faces[fp[2 * t]];
+            const auto& fb = s.faces[fp[2 * t + 1]];
+            bool shared = false;
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) shared |= fa[i] == fb[j];
+            if (shared) continue;
+            TC A[3][3], B[3][3];
+            for (int j = 0; j < 3; ++j)
+                for (int q = 0; q < 3; ++q) { A[j][q] = (TC)x[3 * (size_t)fa[j] + q]; B[j][q] = (TC)x[3 * (size_t)fb[j] + q]; }
+            if (!pen_tri_contact<TC>(A, B)) continue;
+            const TC stiff = model[fa[0]] == model[fb[0]] ? kself : k;
+            TC na[3], nb[3];
+            normal(A, na);
+            normal(B, nb);
+            if (fa[0] < s.nsim) push(fa, A, fb, B, nb, stiff);
+            if (fb[0] < s.nsim) push(fb, B, fa, A, na, stiff);
+        }
+    }
+    // uniformPenaltyForceKernal (cu:3140-3195) and the outputs
+    void finish(TC damping, double* V, double* force, int* times_out) {
+        for (int i = 0; i < s.nsim; ++i) {
+            const int h = times[i];
+            if (h == 0) continue;
+            TC f[3], v[3];
+            for (int q = 0; q < 3; ++q) { f[q] = F[3 * (size_t)i + q] / (TC)h; v[q] = (TC)V[3 * i + q]; }
+            for (int q = 0; q < 3; ++q) F[3 * (size_t)i + q] = f[q] - damping * v[q];
+            const TC len = std::sqrt(pen_dot(f, f));
+            for (int q = 0; q < 3; ++q) f[q] /= len;
+            const TC cc = pen_dot(v, f);
+            for (int q = 0; q < 3; ++q) {
+                TC vn = cc * f[q];
+                TC vt = v[q] - vn;
+                vn *= (TC)-0.4;
+                vt = vt * (TC)0.9;
+                V[3 * i + q] = (double)(vn + vt);
+            }
+        }
+        for (size_t q = 0; q < F.size(); ++q) force[q] = (double)F[q];
+        std::copy(times.begin(), times.end(), times_out);
+    }
+};
+
 struct Ctx {
     int prec = 0;
     std::unique_ptr<Sim<float, float>> f32;
@@ -1767,6 +1979,34 @@ int orc_contact(void* h, const double* x, double* diag, double* rhs, long long* 
         if (n_active) *n_active = na;
         for (int i = 0; i < s.ntot; ++i) diag[i] = (double)s.collDiag[i];
         for (size_t q = 0; q < s.collRhs.size(); ++q) rhs[q] = (double)s.collRhs[q];
+        return (int)PDIPC_OK;
+    });
+}
+
+int orc_penalty_predict(void* h, const double* X, double* V, double* sn) {
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        if (!s.initialized) return (int)PDIPC_ERR_STATE;
+        orc::Penalty<std::remove_reference_t<decltype(s)>> p(s);
+        p.predict(X, V, sn);
+        return (int)PDIPC_OK;
+    });
+}
+// kind: 0 CCD candidates of the last broad phase (x, dir), 1 floor (x), 2 face pairs (x)
+int orc_penalty(void* h, int kind, const double* x, const double* dir, const int* fp, long long np, double k,
+                double kself, double damping, double* V, double* force, int* times) {
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        if (!s.initialized) return (int)PDIPC_ERR_STATE;
+        using P = orc::Penalty<std::remove_reference_t<decltype(s)>>;
+        using TC = typename P::TC;
+        P p(s);
+        if (kind == 0) p.ccd(x, dir, (TC)k);
+        else if (kind == 1) p.floor(x, (TC)k);
+        else {
+            for (long long i = 0; i < 2 * np; ++i)
+                if (fp[i] < 0 || fp[i] >= (int)s.faces.size()) return (int)PDIPC_ERR_ARG;
+            p.dcd(x, fp, np, (TC)k, (TC)kself);
+        }
+        p.finish((TC)damping, V, force, times);
         return (int)PDIPC_OK;
     });
 }

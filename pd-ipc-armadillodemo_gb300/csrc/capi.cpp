@@ -396,6 +396,48 @@ pdipc_status pdipc_stage_sweep_timing(pdipc_ctx* ctx, int launches, double* avg_
     return guarded(ctx, [&]() { return ctx->solver->sweep_timing(launches, avg_ms, bytes, ctx->err); });
 }
 
+pdipc_status pdipc_stage_penalty_predict(pdipc_ctx* ctx, const double* X, double* V, double* sn) {
+    pdipc_status s = need_init(ctx);
+    if (s != PDIPC_OK) return s;
+    if (!X || !V || !sn) return fail(ctx, PDIPC_ERR_ARG, "null argument");
+    return guarded(ctx, [&]() { return ctx->solver->stage_penalty_predict(X, V, sn, ctx->err); });
+}
+
+pdipc_status pdipc_stage_penalty_ccd(pdipc_ctx* ctx, const double* x0, const double* dir, double stiffness,
+                                     double damping, double* V, double* force, int* times) {
+    pdipc_status s = need_init(ctx);
+    if (s != PDIPC_OK) return s;
+    if (!x0 || !dir || !V || !force || !times) return fail(ctx, PDIPC_ERR_ARG, "null argument");
+    return guarded(ctx, [&]() {
+        return ctx->solver->stage_penalty(0, x0, dir, nullptr, 0, stiffness, 0.0, damping, V, force, times,
+                                          ctx->err);
+    });
+}
+
+pdipc_status pdipc_stage_penalty_floor(pdipc_ctx* ctx, const double* x, double stiffness, double damping, double* V,
+                                       double* force, int* times) {
+    pdipc_status s = need_init(ctx);
+    if (s != PDIPC_OK) return s;
+    if (!x || !V || !force || !times) return fail(ctx, PDIPC_ERR_ARG, "null argument");
+    return guarded(ctx, [&]() {
+        return ctx->solver->stage_penalty(1, x, nullptr, nullptr, 0, stiffness, 0.0, damping, V, force, times,
+                                          ctx->err);
+    });
+}
+
+pdipc_status pdipc_stage_penalty_dcd(pdipc_ctx* ctx, const double* x, const int* face_pairs, int64_t n_pairs,
+                                     double stiffness, double self_stiffness, double damping, double* V,
+                                     double* force, int* times) {
+    pdipc_status s = need_init(ctx);
+    if (s != PDIPC_OK) return s;
+    if (!x || !V || !force || !times || n_pairs < 0 || (n_pairs > 0 && !face_pairs))
+        return fail(ctx, PDIPC_ERR_ARG, "null argument or negative pair count");
+    return guarded(ctx, [&]() {
+        return ctx->solver->stage_penalty(2, x, nullptr, face_pairs, n_pairs, stiffness, self_stiffness, damping,
+                                          V, force, times, ctx->err);
+    });
+}
+
 pdipc_status pdipc_mesh_topology(const double* X, int nv, const int* F, int nf, int patch_dim, int* edges,
                                  int cap_edges, int* n_edges, int* patch_off, int cap_patches, int* patch_faces,
                                  int cap_faces, int* n_patches, int* owner_of_point, int* owner_of_edge) {

@@ -296,6 +296,10 @@ std::string build_host_tables(const std::vector<ModelInput>& models, double grav
     H.X.resize(3 * (size_t)nv);
     for (int mi : order)
         std::copy(models[mi].X.begin(), models[mi].X.end(), H.X.begin() + 3 * (size_t)vbase[mi]);
+    H.vertexModel.resize(nv);
+    for (int q = 0; q < (int)order.size(); ++q)
+        std::fill(H.vertexModel.begin() + vbase[order[q]], H.vertexModel.begin() + vbase[order[q]] + models[order[q]].nv,
+                  q);
 
     // ---- cloth precompute: PdIpcClothModel::init (ClothModel.h:177-328) ----
     H.mass.assign(nsim, 0.0);

@@ -26,6 +26,7 @@ struct ModelInput {
 struct HostTables {
     int nsim = 0, ntot = 0;
     std::vector<double> X;  // 3*ntot initial positions
+    std::vector<int> vertexModel;  // ntot: position of the vertex's model in the global order
 
     // per simulated vertex
     std::vector<double> mass;       // lumped area/3 * density (PdIpcClothModel.h:177-195)

@@ -209,6 +209,21 @@ void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_
 template <typename T, typename TC>
 void launch_contact(const Dev<T, TC>& d, Pos<T, TC> X, const SolverConsts& c, cudaStream_t s);
 
+// ---------------- penalty / discrete-collision stages (penalty_kernels.cu) ----------------
+template <typename T, typename TC>
+void launch_pen_predict(const Dev<T, TC>& d, const V4<TC>* X, V4<TC>* V, TC dt, V4<TC>* Sn, cudaStream_t s);
+// over the candidate lists of the last broad phase
+template <typename T, typename TC>
+void launch_pen_ccd(const Dev<T, TC>& d, const V4<TC>* X0, const V4<TC>* D, TC k, TC eta, int max_iter,
+                    V4<TC>* F, int* times, cudaStream_t s);
+template <typename T, typename TC>
+void launch_pen_floor(const Dev<T, TC>& d, const V4<TC>* X, TC k, V4<TC>* F, int* times, cudaStream_t s);
+template <typename T, typename TC>
+void launch_pen_dcd(const Dev<T, TC>& d, const int2* pairs, int64_t n, const int* model, const V4<TC>* X, TC k,
+                    TC kself, V4<TC>* F, int* times, cudaStream_t s);
+template <typename T, typename TC>
+void launch_pen_uniform(const Dev<T, TC>& d, V4<TC>* F, const int* times, TC damping, V4<TC>* V, cudaStream_t s);
+
 // Scratch of the no-allocation per-candidate toi pass: a file-scope device array
 // of kToiScratchEntries doubles (8 MiB), its address looked up once per device on
 // first use.  One array per device is shared by every context of the process:

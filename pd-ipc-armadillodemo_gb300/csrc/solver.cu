@@ -129,6 +129,7 @@ public:
         PD_CK(zeros(d.CollDiag, nt));
         PD_CK(zeros(d.CollRhs, nt));
         PD_CK(zeros(scratch_, nt));
+        PD_CK(up(vModel_, H.vertexModel));
         std::vector<V4<T>> grav(ns), pinr(ns);
         std::vector<T> invm(ns), de(ns), cn(ns), st(ns);
         std::vector<int> pinf(ns);
@@ -501,6 +502,80 @@ public:
         r = get_positions(out, err);
         if (r == PDIPC_OK) r = set_state(saveX.data(), saveV.data(), err);
         return r;
+    }
+
+    // ---------------- penalty / discrete-collision stages ----------------
+    pdipc_status ensure_pen(std::string& err) {
+        if (!pen_f_) {
+            PD_CK(zeros(pen_d_, d_.ntot));
+            PD_CK(zeros(pen_f_, d_.ntot));
+            PD_CK(zeros(pen_v_, d_.nsim));
+            PD_CK(zeros(pen_t_, d_.ntot));
+        }
+        return PDIPC_OK;
+    }
+    pdipc_status download_vec(const V4<TC>* src, double* dst, int n, std::string& err) {
+        PD_CK(cudaMemcpyAsync(stage_, src, sizeof(V4<TC>) * n, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        for (int i = 0; i < n; ++i) {
+            dst[3 * (size_t)i] = (double)stage_[i].x;
+            dst[3 * (size_t)i + 1] = (double)stage_[i].y;
+            dst[3 * (size_t)i + 2] = (double)stage_[i].z;
+        }
+        return PDIPC_OK;
+    }
+    pdipc_status stage_penalty_predict(const double* X, double* V, double* sn, std::string& err) override {
+        pdipc_status r = ensure_pen(err);
+        if (r == PDIPC_OK) r = upload_vec(scratch_, X, d_.nsim, err);
+        if (r == PDIPC_OK) r = upload_vec(pen_v_, V, d_.nsim, err);
+        if (r != PDIPC_OK) return r;
+        launch_pen_predict(d_, scratch_, pen_v_, (TC)c_.dt, pen_f_, s_);
+        PD_CK(cudaGetLastError());
+        r = download_vec(pen_f_, sn, d_.nsim, err);
+        if (r == PDIPC_OK) r = download_vec(pen_v_, V, d_.nsim, err);
+        return r;
+    }
+    pdipc_status stage_penalty(int kind, const double* x, const double* dir, const int* fp, int64_t np, double k,
+                               double ks, double damping, double* V, double* force, int* times,
+                               std::string& err) override {
+        pdipc_status r = ensure_pen(err);
+        if (r != PDIPC_OK) return r;
+        if (kind == 2) {
+            for (int64_t i = 0; i < 2 * np; ++i)
+                if (fp[i] < 0 || fp[i] >= d_.nface) {
+                    err = "face index out of range";
+                    return PDIPC_ERR_ARG;
+                }
+            if (np > penPairCap_) {
+                dfree(penPairs_);
+                PD_CK(alloc(penPairs_, (size_t)np));
+                penPairCap_ = np;
+            }
+            if (np > 0) {
+                PD_CK(cudaMemcpyAsync(penPairs_, fp, sizeof(int2) * np, cudaMemcpyHostToDevice, s_));
+                PD_CK(cudaStreamSynchronize(s_));
+            }
+        }
+        r = upload_vec(scratch_, x, d_.ntot, err);
+        if (r == PDIPC_OK) r = upload_vec(pen_v_, V, d_.nsim, err);
+        if (r == PDIPC_OK && kind == 0) r = upload_vec(pen_d_, dir, d_.ntot, err);
+        if (r != PDIPC_OK) return r;
+        PD_CK(cudaMemsetAsync(pen_f_, 0, sizeof(V4<TC>) * d_.ntot, s_));
+        PD_CK(cudaMemsetAsync(pen_t_, 0, sizeof(int) * d_.ntot, s_));
+        if (kind == 0)
+            launch_pen_ccd(d_, scratch_, pen_d_, (TC)k, (TC)c_.ccd_eta, c_.ccd_max_iter, pen_f_, pen_t_, s_);
+        else if (kind == 1)
+            launch_pen_floor(d_, scratch_, (TC)k, pen_f_, pen_t_, s_);
+        else
+            launch_pen_dcd(d_, penPairs_, np, vModel_, scratch_, (TC)k, (TC)ks, pen_f_, pen_t_, s_);
+        launch_pen_uniform(d_, pen_f_, pen_t_, (TC)damping, pen_v_, s_);
+        PD_CK(cudaGetLastError());
+        r = download_vec(pen_f_, force, d_.ntot, err);
+        if (r == PDIPC_OK) r = download_vec(pen_v_, V, d_.nsim, err);
+        if (r != PDIPC_OK) return r;
+        PD_CK(cudaMemcpyAsync(times, pen_t_, sizeof(int) * d_.ntot, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        return PDIPC_OK;
     }
 
     pdipc_status sweep_timing(int launches, double* avg_ms, double* bytes, std::string& err) override {
@@ -1138,6 +1213,14 @@ private:
     int64_t launches_ = 0;
     int64_t sell_entries_ = 0, sell_padded_ = 0;
     V4<TC>* scratch_ = nullptr;
+    // penalty stages: direction, force, velocity, hit counts, face pairs; per-vertex model index
+    V4<TC>* pen_d_ = nullptr;
+    V4<TC>* pen_f_ = nullptr;
+    V4<TC>* pen_v_ = nullptr;
+    int* pen_t_ = nullptr;
+    int2* penPairs_ = nullptr;
+    int64_t penPairCap_ = 0;
+    int* vModel_ = nullptr;
     V4<T>* sh_ = nullptr;  // float-float mirror of scratch_ (correction form)
     V4<T>* sl_ = nullptr;
     int* cnt_ = nullptr;

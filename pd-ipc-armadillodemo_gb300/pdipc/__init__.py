@@ -35,11 +35,12 @@ EXPORTS = [
     "pdipc_stage_contact", "pdipc_stage_pd", "pdipc_mesh_topology",
     "pdipc_stage_sweep_timing", "pdipc_stage_toi_noalloc", "pdipc_add_volumetric", "pdipc_tet_surface",
     "pdipc_scene_load", "pdipc_scene_model_count", "pdipc_scene_get_model", "pdipc_scene_apply_params",
-    "pdipc_scene_add_models", "pdipc_scene_free",
+    "pdipc_scene_add_models", "pdipc_scene_free", "pdipc_stage_penalty_predict", "pdipc_stage_penalty_ccd",
+    "pdipc_stage_penalty_floor", "pdipc_stage_penalty_dcd",
 ]
 
 
-ABI_VERSION = 3  # PDIPC_ABI_VERSION of include/pdipc.h
+ABI_VERSION = 4  # PDIPC_ABI_VERSION of include/pdipc.h
 
 
 class PdipcError(RuntimeError):
@@ -99,6 +100,11 @@ def load_library(path: str | None = None):
                                          C.c_int64, _i64p]
     L.pdipc_stage_morton.argtypes = [vp, C.POINTER(C.c_uint64), _ip, C.c_int]
     L.pdipc_stage_toi.argtypes = [vp, _dp, _dp, _dp, _dp, _dp]
+    L.pdipc_stage_penalty_predict.argtypes = [vp, _dp, _dp, _dp]
+    L.pdipc_stage_penalty_ccd.argtypes = [vp, _dp, _dp, C.c_double, C.c_double, _dp, _dp, _ip]
+    L.pdipc_stage_penalty_floor.argtypes = [vp, _dp, C.c_double, C.c_double, _dp, _dp, _ip]
+    L.pdipc_stage_penalty_dcd.argtypes = [vp, _dp, _ip, C.c_int64, C.c_double, C.c_double, C.c_double, _dp, _dp,
+                                          _ip]
     L.pdipc_stage_toi_noalloc.argtypes = [vp, _dp, _dp, _dp, _dp, _dp]
     L.pdipc_stage_contact.argtypes = [vp, _dp, _dp, _dp, _i64p]
     L.pdipc_stage_pd.argtypes = [vp, _dp, _dp, _dp]
@@ -278,6 +284,48 @@ class Simulator:
         self._check(load_library().pdipc_stage_toi(self.h, _d(x0), _d(x1), _d(tp), _d(te), C.byref(g)),
                     "pdipc_stage_toi")
         return tp[:npt], te[:nee], g.value
+
+    # -- penalty / discrete-collision stages (PdIpcGpuFunc.cu:2933-3740) -------------------
+    def penalty_predict(self, X, V):
+        """prediticeDCPositionKernel: predicted positions sn (n_sim x 3) and the velocities
+        (pinned ones zeroed)."""
+        X = self._vec(X, self.n_sim, "X")
+        V = self._vec(V, self.n_sim, "V").copy()
+        sn = np.empty((self.n_sim, 3), np.float64)
+        self._check(load_library().pdipc_stage_penalty_predict(self.h, _d(X), _d(V), _d(sn)),
+                    "pdipc_stage_penalty_predict")
+        return sn, V
+
+    def _penalty_out(self, V):
+        V = self._vec(V, self.n_sim, "V").copy()
+        return V, np.empty((self.n_total, 3), np.float64), np.empty(self.n_total, np.int32)
+
+    def penalty_ccd(self, x0, d, stiffness, damping, V):
+        """computePenaltyForceHost over the candidates of the last broad phase: (force, hits, V)."""
+        x0 = self._vec(x0, self.n_total, "x0")
+        d = self._vec(d, self.n_total, "dir")
+        V, F, t = self._penalty_out(V)
+        self._check(load_library().pdipc_stage_penalty_ccd(self.h, _d(x0), _d(d), stiffness, damping, _d(V),
+                                                           _d(F), _i(t)), "pdipc_stage_penalty_ccd")
+        return F, t, V
+
+    def penalty_floor(self, x, stiffness, damping, V):
+        """applyPenaltyForceForFloorHost: (force, hits, V)."""
+        x = self._vec(x, self.n_total, "x")
+        V, F, t = self._penalty_out(V)
+        self._check(load_library().pdipc_stage_penalty_floor(self.h, _d(x), stiffness, damping, _d(V), _d(F),
+                                                             _i(t)), "pdipc_stage_penalty_floor")
+        return F, t, V
+
+    def penalty_dcd(self, x, face_pairs, stiffness, self_stiffness, damping, V):
+        """computeDcdPenaltyForceHost over face pairs (m x 2 collision-face indices): (force, hits, V)."""
+        x = self._vec(x, self.n_total, "x")
+        fp = np.ascontiguousarray(face_pairs, dtype=np.int32).reshape(-1, 2)
+        V, F, t = self._penalty_out(V)
+        self._check(load_library().pdipc_stage_penalty_dcd(self.h, _d(x), _i(fp) if fp.size else None,
+                                                           fp.shape[0], stiffness, self_stiffness, damping,
+                                                           _d(V), _d(F), _i(t)), "pdipc_stage_penalty_dcd")
+        return F, t, V
 
     def stage_toi_noalloc(self, x0, x1, npt, nee, per_candidate=True):
         """stage_toi through the no-allocation entry point (FP64 and mixed modes)."""
