@@ -235,7 +235,7 @@ def run_ours(args):
     out = np.empty((sim.n_total, 3), np.float64)
     barrier(dist, dev)
     dev_ms, launches, outers = 0.0, 0, []
-    pd_ms, pd_solves = 0.0, 0
+    pd_ms, pd_solves, ccd_ms, contact_ms = 0.0, 0, 0.0, 0.0
     flush.zero_()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -254,6 +254,8 @@ def run_ours(args):
             outers.append(st["last_outer_iters"])
             pd_ms += st["pd_solve_ms"]
             pd_solves += st["pd_solves"]
+            ccd_ms += st["ccd_ms"]
+            contact_ms += st["contact_ms"]
         torch.cuda.synchronize()
     barrier(dist, dev)
     dev_ms_max = max_over_ranks(dist, dev_ms, dev)
@@ -341,6 +343,10 @@ def run_ours(args):
                    "ee_candidates": st_end["ee_candidates"], "device_bytes": st_end["device_bytes"]},
         "element_updates_per_s": round(sim.n_sim * sc.lg_iterations * float(np.sum(outers)) / (dev_ms / 1e3), 1),
         "gpu_launches": int(launches),
+        "step_breakdown_ms": {"pd_solve": round(pd_ms / args.steps, 3), "ccd": round(ccd_ms / args.steps, 3),
+                              "contact": round(contact_ms / args.steps, 3),
+                              "rest": round((dev_ms - pd_ms - ccd_ms - contact_ms) / args.steps, 3),
+                              "note": "per timed step, CUDA events on the library's stream"},
         "e2e": {"value": round(e2e, 4), "unit": UNIT,
                 "h2d_bytes_per_step": int(round((sim.n_total + sc.n_sim) * state_bytes / args.steps)),
                 "d2h_bytes_per_step": int(sim.n_total * state_bytes + 8 * round(mean_outer) + 48),

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PDIPC_ABI_VERSION 4
+#define PDIPC_ABI_VERSION 5
 
 typedef struct pdipc_ctx pdipc_ctx;
 
@@ -122,6 +122,10 @@ typedef struct {
                                     local step 16 d_i + 68 plus (2 cheby) sweeps of 8 n_i + 28 plus
                                     (cheby - 1) Chebyshev reads of 12 (d_i stencil neighbours, n_i matrix
                                     off-diagonals; FP32 sizes, doubled value sizes in FP64 mode) */
+    double ccd_ms;               /* device time of the time-of-impact passes (point-triangle and edge-edge
+                                    candidates, global minimum) of the last call, CUDA events per outer
+                                    iteration */
+    double contact_ms;           /* device time of the contact-constraint passes of the last call */
 } pdipc_stats;
 
 /* Fill *p with the reference defaults listed beside each field. */

@@ -91,6 +91,10 @@ public:
         PD_CK(cudaEventCreate(&ev1_));
         PD_CK(cudaEventCreate(&evp0_));
         PD_CK(cudaEventCreate(&evp1_));
+        PD_CK(cudaEventCreate(&evc0_));
+        PD_CK(cudaEventCreate(&evc1_));
+        PD_CK(cudaEventCreate(&evq0_));
+        PD_CK(cudaEventCreate(&evq1_));
         Dev<T, TC>& d = d_;
         d.nsim = H.nsim;
         d.ntot = H.ntot;
@@ -295,6 +299,8 @@ public:
         device_ms_ = 0.0;
         pd_ms_ = 0.0;
         pd_solves_ = 0;
+        ccd_ms_ = 0.0;
+        contact_ms_ = 0.0;
         st_.max_outer_iters = 0;
         st_.total_outer_iters = 0;
         for (int k = 0; k < n; ++k) {
@@ -367,6 +373,8 @@ public:
         s->pd_solves = pd_solves_;
         s->pd_solve_ms = pd_ms_;
         s->pd_solve_bytes = pd_bytes_;
+        s->ccd_ms = ccd_ms_;
+        s->contact_ms = contact_ms_;
     }
 
     // ---------------- stages ----------------
@@ -670,6 +678,11 @@ private:
         if (ev1_) cudaEventDestroy(ev1_);
         if (evp0_) cudaEventDestroy(evp0_);
         if (evp1_) cudaEventDestroy(evp1_);
+        if (evc0_) cudaEventDestroy(evc0_);
+        if (evc1_) cudaEventDestroy(evc1_);
+        if (evq0_) cudaEventDestroy(evq0_);
+        if (evq1_) cudaEventDestroy(evq1_);
+        evc0_ = evc1_ = evq0_ = evq1_ = nullptr;
         ev0_ = ev1_ = evp0_ = evp1_ = nullptr;
         if (s_) cudaStreamDestroy(s_);
         s_ = nullptr;
@@ -1144,16 +1157,24 @@ private:
                 r = broadphase(err);
                 if (r != PDIPC_OK) return r;
             }
+            PD_CK(cudaEventRecord(evc0_, s_));
             launch_toi(d, pos_old(), pos(), c_, (TC*)nullptr, (TC*)nullptr, s_);
             launch_toi_finalize(d, c_, s_);
+            PD_CK(cudaEventRecord(evc1_, s_));
             launch_clamp(d, s_);
+            PD_CK(cudaEventRecord(evq0_, s_));
             launch_contact(d, pos(), c_, s_);
+            PD_CK(cudaEventRecord(evq1_, s_));
             launches_ += (d.nPT > 0) + (d.nEE > 0) + 1 + 1 + (d.nPT > 0) + (d.nEE > 0);
             PD_CK(cudaMemcpyAsync(&pin_->resid, d.Resid, sizeof(double), cudaMemcpyDeviceToHost, s_));
             PD_CK(cudaStreamSynchronize(s_));
             float pms = 0.f;
             PD_CK(cudaEventElapsedTime(&pms, evp0_, evp1_));
             pd_ms_ += pms;
+            PD_CK(cudaEventElapsedTime(&pms, evc0_, evc1_));
+            ccd_ms_ += pms;
+            PD_CK(cudaEventElapsedTime(&pms, evq0_, evq1_));
+            contact_ms_ += pms;
             ++pd_solves_;
             const double res = pin_->resid;
             st_.last_residual = res;
@@ -1205,6 +1226,8 @@ private:
     cudaStream_t s_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
     cudaEvent_t evp0_ = nullptr, evp1_ = nullptr;  // around each PD solve
+    cudaEvent_t evc0_ = nullptr, evc1_ = nullptr, evq0_ = nullptr, evq1_ = nullptr;  // toi, contact
+    double ccd_ms_ = 0.0, contact_ms_ = 0.0;
     double device_ms_ = 0.0;
     double pd_ms_ = 0.0, pd_bytes_ = 0.0;
     int64_t pd_solves_ = 0;

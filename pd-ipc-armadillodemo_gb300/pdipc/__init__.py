@@ -40,7 +40,7 @@ EXPORTS = [
 ]
 
 
-ABI_VERSION = 4  # PDIPC_ABI_VERSION of include/pdipc.h
+ABI_VERSION = 5  # PDIPC_ABI_VERSION of include/pdipc.h
 
 
 class PdipcError(RuntimeError):

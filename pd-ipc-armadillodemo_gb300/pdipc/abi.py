@@ -138,6 +138,8 @@ class Stats(C.Structure):
         ("pd_solves", C.c_int64),
         ("pd_solve_ms", C.c_double),
         ("pd_solve_bytes", C.c_double),
+        ("ccd_ms", C.c_double),
+        ("contact_ms", C.c_double),
     ]
 
     def as_dict(self) -> dict:
