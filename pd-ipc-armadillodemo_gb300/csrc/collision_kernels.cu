@@ -450,13 +450,90 @@ __device__ __noinline__ TC toi_refine(const V4<TC>* __restrict__ X0, const V4<TC
     return kPT ? geo::ccd_pt<TC>(xd, dd, eta, max_iter) : geo::ccd_ee<TC>(xd, dd, eta, max_iter);
 }
 
+// Mixed mode, one candidate: the pair's coordinates relative to its first
+// vertex and its motion, in FP32 from the float-float mirrors.
+template <typename T>
+__device__ __forceinline__ void toi_rel(const int* ids, const V4<T>* __restrict__ X0h, const V4<T>* __restrict__ X0l,
+                                        const V4<T>* __restrict__ X1h, const V4<T>* __restrict__ X1l, T (&x)[4][3],
+                                        T (&dx)[4][3]) {
+    const V4<T> oh = ld4(X0h, ids[0]), ol = ld4(X0l, ids[0]);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const V4<T> ah = ld4(X0h, ids[j]), al = ld4(X0l, ids[j]);
+        const V4<T> bh = ld4(X1h, ids[j]), bl = ld4(X1l, ids[j]);
+        x[j][0] = diff_ff(ah.x, al.x, oh.x, ol.x);
+        x[j][1] = diff_ff(ah.y, al.y, oh.y, ol.y);
+        x[j][2] = diff_ff(ah.z, al.z, oh.z, ol.z);
+        dx[j][0] = diff_ff(bh.x, bl.x, ah.x, al.x);
+        dx[j][1] = diff_ff(bh.y, bl.y, ah.y, al.y);
+        dx[j][2] = diff_ff(bh.z, bl.z, ah.z, al.z);
+    }
+}
+
+// Mixed mode, stage 1 of a candidate: false when its time of impact is 1
+// without any CCD iteration (shared vertex; the swept-box filter, first on the
+// high parts alone with the distance widened past the largest effect of the
+// dropped low parts (|low| <= 2^-24 |x|, plus the roundings: < 2^-18 of the
+// largest coordinate), then exactly; no motion, or the CCD's box-gap exit).
+template <typename T, bool kPT>
+__device__ __forceinline__ bool toi_needs_ccd(const int4 c, const V4<T>* __restrict__ X0h, const V4<T>* __restrict__ X0l,
+                                              const V4<T>* __restrict__ X1h, const V4<T>* __restrict__ X1l, T slack) {
+    if (kPT ? (c.x == c.y || c.x == c.z || c.x == c.w) : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w))
+        return false;
+    const int ids[4] = {c.x, c.y, c.z, c.w};
+    {
+        T xh[4][3], dh[4][3], m = T(0);
+        const V4<T> o = ld4(X0h, ids[0]);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const V4<T> ah = ld4(X0h, ids[j]), bh = ld4(X1h, ids[j]);
+            xh[j][0] = ah.x - o.x;
+            xh[j][1] = ah.y - o.y;
+            xh[j][2] = ah.z - o.z;
+            dh[j][0] = bh.x - ah.x;
+            dh[j][1] = bh.y - ah.y;
+            dh[j][2] = bh.z - ah.z;
+            m = dmax(m, dmax(dmax(fabsf(ah.x), fabsf(ah.y)), dmax(fabsf(ah.z), fabsf(bh.x))));
+            m = dmax(m, dmax(fabsf(bh.y), fabsf(bh.z)));
+        }
+        const T wide = slack + m * T(1.0 / 65536.0);
+        if (!(kPT ? geo::pt_ccd_broad<T>(xh, dh, wide) : geo::ee_ccd_broad<T>(xh, dh, wide))) return false;
+        // the CCD's box-gap exit from the high parts too: they are within
+        // 2^-22 m of the exact relative coordinates and motion per component
+        // (m bounds |x|), so the margins below keep it conservative; most pairs
+        // settle here without loading the low parts
+        const T eps = m * T(1.0 / 1048576.0);
+        if (geo::ccd_trivial_approx<T, kPT>(xh, dh, T(4) * eps, T(8) * eps)) return false;
+    }
+    T x[4][3], dx[4][3];
+    toi_rel<T>(ids, X0h, X0l, X1h, X1l, x, dx);
+    if (!(kPT ? geo::pt_ccd_broad<T>(x, dx, slack) : geo::ee_ccd_broad<T>(x, dx, slack))) return false;
+    return !(kPT ? geo::ccd_pt_trivial<T>(x, dx) : geo::ccd_ee_trivial<T>(x, dx));
+}
+
+// Mixed mode, stage 2: the FP32 additive CCD, and for a time of impact below 1
+// its FP64 re-evaluation from the FP64 state.
+template <typename T, typename TC, bool kPT>
+__device__ __forceinline__ TC toi_ccd(const int4 c, const V4<TC>* __restrict__ X0, const V4<TC>* __restrict__ X1,
+                                      const V4<T>* __restrict__ X0h, const V4<T>* __restrict__ X0l,
+                                      const V4<T>* __restrict__ X1h, const V4<T>* __restrict__ X1l, TC eta,
+                                      int max_iter) {
+    const int ids[4] = {c.x, c.y, c.z, c.w};
+    T x[4][3], dx[4][3];
+    toi_rel<T>(ids, X0h, X0l, X1h, X1l, x, dx);
+    const T tf = kPT ? geo::ccd_pt<T>(x, dx, (T)eta, max_iter) : geo::ccd_ee<T>(x, dx, (T)eta, max_iter);
+    return tf < T(1) ? toi_refine<TC, kPT>(X0, X1, ids, eta, max_iter) : TC(1);
+}
+
 // getImpactOfTimeKernel (cu:2610-2704): skip pairs sharing a vertex, swept-AABB
 // filter with slack, additive CCD; global minimum by integer atomicMin.
 // kRel (mixed precision): coordinates relative to the pair's first vertex,
 // formed in FP32 from the float-float mirrors of the FP64 state, an FP32
 // additive CCD on them, and every candidate that would clamp the step
 // (toi < 1) re-evaluated in FP64 from the FP64 state, so the minimum is an
-// FP64 time of impact.
+// FP64 time of impact.  The stage-1 tests settle most candidates; each warp
+// queues the rest in shared memory and runs the CCD iterations on 32 of them
+// at a time, so they run on full warps.
 template <typename T, typename TC, bool kPT, bool kRel>
 __global__ void __launch_bounds__(kBlock, kCandBlocks<T>) k_toi(int64_t n, const int4* __restrict__ cand,
                                                 const V4<TC>* __restrict__ X0, const V4<TC>* __restrict__ X1,
@@ -465,59 +542,44 @@ __global__ void __launch_bounds__(kBlock, kCandBlocks<T>) k_toi(int64_t n, const
                                                 TC slack, TC eta, int max_iter, TC* __restrict__ per,
                                                 TC* __restrict__ toi_min) {
     TC local = TC(1);
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        const int4 c = cand[t];
-        const int ids[4] = {c.x, c.y, c.z, c.w};
-        TC toi = TC(1);
-        const bool shared = kPT ? (c.x == c.y || c.x == c.z || c.x == c.w)
-                                : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w);
-        if (!shared) {
-            if constexpr (kRel) {
-                // the swept-box filter first on the high parts alone, with the
-                // distance widened past the largest effect of the dropped low
-                // parts (|low| <= 2^-24 |x|, plus the roundings: < 2^-18 of the
-                // largest coordinate); only the survivors load the low parts and
-                // take the exact filter below
-                bool maybe;
-                {
-                    T xh[4][3], dh[4][3], m = T(0);
-                    const V4<T> o = ld4(X0h, ids[0]);
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const V4<T> ah = ld4(X0h, ids[j]), bh = ld4(X1h, ids[j]);
-                        xh[j][0] = ah.x - o.x;
-                        xh[j][1] = ah.y - o.y;
-                        xh[j][2] = ah.z - o.z;
-                        dh[j][0] = bh.x - ah.x;
-                        dh[j][1] = bh.y - ah.y;
-                        dh[j][2] = bh.z - ah.z;
-                        m = dmax(m, dmax(dmax(fabsf(ah.x), fabsf(ah.y)), dmax(fabsf(ah.z), fabsf(bh.x))));
-                        m = dmax(m, dmax(fabsf(bh.y), fabsf(bh.z)));
-                    }
-                    const T wide = (T)slack + m * T(1.0 / 65536.0);
-                    maybe = kPT ? geo::pt_ccd_broad<T>(xh, dh, wide) : geo::ee_ccd_broad<T>(xh, dh, wide);
-                }
-                if (maybe) {
-                T x[4][3], dx[4][3];
-                const V4<T> oh = ld4(X0h, ids[0]), ol = ld4(X0l, ids[0]);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const V4<T> ah = ld4(X0h, ids[j]), al = ld4(X0l, ids[j]);
-                    const V4<T> bh = ld4(X1h, ids[j]), bl = ld4(X1l, ids[j]);
-                    x[j][0] = diff_ff(ah.x, al.x, oh.x, ol.x);
-                    x[j][1] = diff_ff(ah.y, al.y, oh.y, ol.y);
-                    x[j][2] = diff_ff(ah.z, al.z, oh.z, ol.z);
-                    dx[j][0] = diff_ff(bh.x, bl.x, ah.x, al.x);
-                    dx[j][1] = diff_ff(bh.y, bl.y, ah.y, al.y);
-                    dx[j][2] = diff_ff(bh.z, bl.z, ah.z, al.z);
-                }
-                const bool hit = kPT ? geo::pt_ccd_broad<T>(x, dx, (T)slack) : geo::ee_ccd_broad<T>(x, dx, (T)slack);
-                if (hit) {
-                    const T tf = kPT ? geo::ccd_pt<T>(x, dx, (T)eta, max_iter) : geo::ccd_ee<T>(x, dx, (T)eta, max_iter);
-                    if (tf < T(1)) toi = toi_refine<TC, kPT>(X0, X1, ids, eta, max_iter);
-                }
-                }
-            } else {
+    if constexpr (kRel) {
+        __shared__ int64_t queue[kBlock / 32][64];
+        const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        int qn = 0;
+        const int64_t step = (int64_t)gridDim.x * (kBlock / 32) * 32;
+        for (int64_t base = ((int64_t)blockIdx.x * (kBlock / 32) + w) * 32; base < n; base += step) {
+            const int64_t t = base + lane;
+            const bool need = t < n && toi_needs_ccd<T, kPT>(cand[t], X0h, X0l, X1h, X1l, (T)slack);
+            if (t < n && !need && per) per[t] = TC(1);
+            const unsigned m = __ballot_sync(0xffffffffu, need);
+            if (need) queue[w][qn + __popc(m & ((1u << lane) - 1u))] = t;
+            qn += __popc(m);
+            __syncwarp();
+            if (qn >= 32) {
+                const int64_t tq = queue[w][lane];
+                __syncwarp();
+                if (lane < qn - 32) queue[w][lane] = queue[w][lane + 32];
+                __syncwarp();
+                qn -= 32;
+                const TC toi = toi_ccd<T, TC, kPT>(cand[tq], X0, X1, X0h, X0l, X1h, X1l, eta, max_iter);
+                if (per) per[tq] = toi;
+                if (toi < local) local = toi;
+            }
+        }
+        if (lane < qn) {
+            const int64_t tq = queue[w][lane];
+            const TC toi = toi_ccd<T, TC, kPT>(cand[tq], X0, X1, X0h, X0l, X1h, X1l, eta, max_iter);
+            if (per) per[tq] = toi;
+            if (toi < local) local = toi;
+        }
+    } else {
+        for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+            const int4 c = cand[t];
+            const int ids[4] = {c.x, c.y, c.z, c.w};
+            TC toi = TC(1);
+            const bool shared = kPT ? (c.x == c.y || c.x == c.z || c.x == c.w)
+                                    : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w);
+            if (!shared) {
                 TC x[4][3], dx[4][3];
                 gather4<TC, TC>(X0, ids, x);
                 gather4<TC, TC>(X1, ids, dx);
@@ -531,9 +593,9 @@ __global__ void __launch_bounds__(kBlock, kCandBlocks<T>) k_toi(int64_t n, const
                     if (geo::ee_ccd_broad<TC>(x, dx, slack)) toi = geo::ccd_ee<TC>(x, dx, eta, max_iter);
                 }
             }
+            if (per) per[t] = toi;
+            if (toi < local) local = toi;
         }
-        if (per) per[t] = toi;
-        if (toi < local) local = toi;
     }
     block_min_to(local, toi_min);
 }
@@ -559,6 +621,160 @@ struct ContactConsts {
 // on their rounding, FP64 distance and weight for pairs within 1.1 dhat, and
 // the right-hand side accumulated as w * (target - x) so the later residual
 // needs no cancellation.
+// One contact candidate (setCollisionConstraintsKernel, cu:2756-2892).  kStage 0:
+// the whole test and, for a pair closer than dhat, its diagonal and right-hand
+// side terms; 1 (mixed mode): only the shared-vertex test and the box filters on
+// the high parts of the mirrors (1: the pair survives them); 2 (mixed mode): the
+// rest, for a pair that survived stage 1.  Returns 1 for an active pair.
+template <typename T, typename TC, bool kPT, bool kRel, int kStage>
+__device__ __forceinline__ unsigned contact_candidate(const int4 c, const V4<TC>* __restrict__ X,
+                                                      const V4<T>* __restrict__ Xh, const V4<T>* __restrict__ Xl,
+                                                      const TC* __restrict__ mass, const ContactConsts<TC>& cc,
+                                                      T* __restrict__ diag, V4<T>* __restrict__ rhs) {
+    const int ids[4] = {c.x, c.y, c.z, c.w};
+    if (kStage != 2 &&
+        (kPT ? (c.x == c.y || c.x == c.z || c.x == c.w) : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w)))
+        return 0u;
+    TC p[4][3];
+    if constexpr (kRel) {
+        if (kStage != 2) {  // the box filter on the high parts alone, widened as in k_toi
+            T qh[4][3], m = T(0);
+            const V4<T> o = ld4(Xh, ids[0]);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const V4<T> ah = ld4(Xh, ids[j]);
+                qh[j][0] = ah.x - o.x;
+                qh[j][1] = ah.y - o.y;
+                qh[j][2] = ah.z - o.z;
+                m = dmax(m, dmax(fabsf(ah.x), dmax(fabsf(ah.y), fabsf(ah.z))));
+            }
+            const T wide = (T)cc.dh + m * T(1.0 / 65536.0);
+            bool farh = false;
+            if (kPT) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const T tmin = geo::mn3(qh[1][k], qh[2][k], qh[3][k]);
+                    const T tmax = geo::mx3(qh[1][k], qh[2][k], qh[3][k]);
+                    if ((qh[0][k] - tmax) > wide || (tmin - qh[0][k]) > wide) farh = true;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const T mina = dmin(qh[0][k], qh[1][k]), maxa = dmax(qh[0][k], qh[1][k]);
+                    const T minb = dmin(qh[2][k], qh[3][k]), maxb = dmax(qh[2][k], qh[3][k]);
+                    if ((mina - maxb) > wide || (minb - maxa) > wide) farh = true;
+                }
+            }
+            if (farh) return 0u;
+            // the boxes' Euclidean gap also bounds the distance from below: a
+            // pair beyond sqrt(2) dhat (after the widening) fails the filter below
+            const T g = dsqrt(kPT ? geo::box_gap2<T, 1, 3>(qh, qh + 1) : geo::box_gap2<T, 2, 2>(qh, qh + 2)) -
+                        T(2) * (wide - (T)cc.dh);
+            if (g > T(0) && g * g > T(2) * (T)cc.dh2) return 0u;
+            if (kStage == 1) return 1u;
+        }
+        T q[4][3];
+        const V4<T> oh = ld4(Xh, ids[0]), ol = ld4(Xl, ids[0]);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const V4<T> ah = ld4(Xh, ids[j]), al = ld4(Xl, ids[j]);
+            q[j][0] = diff_ff(ah.x, al.x, oh.x, ol.x);
+            q[j][1] = diff_ff(ah.y, al.y, oh.y, ol.y);
+            q[j][2] = diff_ff(ah.z, al.z, oh.z, ol.z);
+        }
+        const T dhf = (T)cc.dh;
+        bool far = false;
+        if (kPT) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const T tmin = geo::mn3(q[1][k], q[2][k], q[3][k]), tmax = geo::mx3(q[1][k], q[2][k], q[3][k]);
+                if ((q[0][k] - tmax) > dhf || (tmin - q[0][k]) > dhf) far = true;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const T mina = dmin(q[0][k], q[1][k]), maxa = dmax(q[0][k], q[1][k]);
+                const T minb = dmin(q[2][k], q[3][k]), maxb = dmax(q[2][k], q[3][k]);
+                if ((mina - maxb) > dhf || (minb - maxa) > dhf) far = true;
+            }
+        }
+        if (far) return 0u;
+        T df[3], a_, b_, c_;
+        const T d2f = kPT ? geo::vtx_tri<T>(q[0], q[1], q[2], q[3], &a_, &b_, &c_, df)
+                          : geo::edge_edge_sq<T>(q[0], q[1], q[2], q[3], &a_, &b_, df);
+        if (!(d2f < (T)(1.21 * cc.dh2))) return 0u;
+        const V4<TC> o = ld4(X, ids[0]);  // close pair: FP64 relative coordinates
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const V4<TC> a = ld4(X, ids[j]);
+            p[j][0] = a.x - o.x;
+            p[j][1] = a.y - o.y;
+            p[j][2] = a.z - o.z;
+        }
+    } else {
+        gather4<TC, TC>(X, ids, p);
+        bool far = false;
+        if (kPT) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {  // point_triangle_cd_broadphase (cu:2328-2345)
+                const TC tmin = geo::mn3(p[1][k], p[2][k], p[3][k]), tmax = geo::mx3(p[1][k], p[2][k], p[3][k]);
+                if ((p[0][k] - tmax) > cc.dh || (tmin - p[0][k]) > cc.dh) far = true;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {  // edge_edge_cd_broadphase (cu:2405-2424)
+                const TC mina = dmin(p[0][k], p[1][k]), maxa = dmax(p[0][k], p[1][k]);
+                const TC minb = dmin(p[2][k], p[3][k]), maxb = dmax(p[2][k], p[3][k]);
+                if ((mina - maxb) > cc.dh || (minb - maxa) > cc.dh) far = true;
+            }
+        }
+        if (far) return 0u;
+    }
+    TC d[3], dist2, mp, mq;
+    if (kPT) {
+        TC a, b, cq;
+        dist2 = geo::vtx_tri(p[0], p[1], p[2], p[3], &a, &b, &cq, d);
+        if (dist2 >= cc.dh2) return 0u;
+        mp = mass[c.x];
+        mq = a * mass[c.y] + b * mass[c.z] + cq * mass[c.w];
+    } else {
+        TC r, s;
+        dist2 = geo::edge_edge_sq(p[0], p[1], p[2], p[3], &r, &s, d);
+        if (dist2 >= cc.dh2) return 0u;
+        mp = (TC(1) - r) * mass[c.x] + r * mass[c.y];
+        mq = (TC(1) - s) * mass[c.z] + s * mass[c.w];
+    }
+    TC dist = dsqrt(dist2);
+    const TC t2 = dist2 - cc.dh2;
+    const TC bar = -cc.kappa * t2 * t2 * dlog(dist2 / cc.dh2) / (cc.dh2 * cc.dh2);
+    const TC w = bar + dmin(mp, mq) / (cc.dt * cc.dt);
+    const TC rp = mq / (mp + mq), rq = mp / (mp + mq);
+    const TC len = dsqrt(geo::dot3(d, d));
+    for (int k = 0; k < 3; ++k) d[k] /= len;
+    dist = cc.dh - dist;
+    const TC dp = dist * rp, dq = dist * rq;
+    for (int j = 0; j < 4; ++j) atomicAdd(diag + ids[j], (T)w);
+    for (int k = 0; k < 3; ++k) {
+        TC t0, t1, t2_, t3;
+        if (kRel) {  // w (target - x)
+            t0 = w * (dp * d[k]);
+            t1 = kPT ? -w * (dq * d[k]) : w * (dp * d[k]);
+            t2_ = -w * (dq * d[k]);
+            t3 = -w * (dq * d[k]);
+        } else {
+            t0 = w * (p[0][k] + dp * d[k]);
+            t1 = kPT ? w * (p[1][k] - dq * d[k]) : w * (p[1][k] + dp * d[k]);
+            t2_ = w * (p[2][k] - dq * d[k]);
+            t3 = w * (p[3][k] - dq * d[k]);
+        }
+        atomicAdd(&rhs[ids[0]].x + k, (T)t0);
+        atomicAdd(&rhs[ids[1]].x + k, (T)t1);
+        atomicAdd(&rhs[ids[2]].x + k, (T)t2_);
+        atomicAdd(&rhs[ids[3]].x + k, (T)t3);
+    }
+    return 1u;
+}
+
 template <typename T, typename TC, bool kPT, bool kRel>
 __global__ void __launch_bounds__(kBlock, kCandBlocks<T>) k_contact(int64_t n, const int4* __restrict__ cand,
                                                     const V4<TC>* __restrict__ X, const V4<T>* __restrict__ Xh,
@@ -566,148 +782,35 @@ __global__ void __launch_bounds__(kBlock, kCandBlocks<T>) k_contact(int64_t n, c
                                                     ContactConsts<TC> cc, T* __restrict__ diag,
                                                     V4<T>* __restrict__ rhs, unsigned long long* __restrict__ active) {
     unsigned int my = 0;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        const int4 c = cand[t];
-        const int ids[4] = {c.x, c.y, c.z, c.w};
-        if (kPT ? (c.x == c.y || c.x == c.z || c.x == c.w) : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w))
-            continue;
-        TC p[4][3];
-        if constexpr (kRel) {
-            {  // the box filter on the high parts alone, widened as in k_toi
-                T qh[4][3], m = T(0);
-                const V4<T> o = ld4(Xh, ids[0]);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const V4<T> ah = ld4(Xh, ids[j]);
-                    qh[j][0] = ah.x - o.x;
-                    qh[j][1] = ah.y - o.y;
-                    qh[j][2] = ah.z - o.z;
-                    m = dmax(m, dmax(fabsf(ah.x), dmax(fabsf(ah.y), fabsf(ah.z))));
-                }
-                const T wide = (T)cc.dh + m * T(1.0 / 65536.0);
-                bool farh = false;
-                if (kPT) {
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        const T tmin = geo::mn3(qh[1][k], qh[2][k], qh[3][k]);
-                        const T tmax = geo::mx3(qh[1][k], qh[2][k], qh[3][k]);
-                        if ((qh[0][k] - tmax) > wide || (tmin - qh[0][k]) > wide) farh = true;
-                    }
-                } else {
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        const T mina = dmin(qh[0][k], qh[1][k]), maxa = dmax(qh[0][k], qh[1][k]);
-                        const T minb = dmin(qh[2][k], qh[3][k]), maxb = dmax(qh[2][k], qh[3][k]);
-                        if ((mina - maxb) > wide || (minb - maxa) > wide) farh = true;
-                    }
-                }
-                if (farh) continue;
-                // the boxes' Euclidean gap also bounds the distance from below: a
-                // pair beyond sqrt(2) dhat (after the widening) fails the filter below
-                const T g = dsqrt(kPT ? geo::box_gap2<T, 1, 3>(qh, qh + 1) : geo::box_gap2<T, 2, 2>(qh, qh + 2)) -
-                            T(2) * (wide - (T)cc.dh);
-                if (g > T(0) && g * g > T(2) * (T)cc.dh2) continue;
+    if constexpr (kRel) {
+        // Most candidates fail the cheap stage-1 filter.  Each warp filters 32
+        // consecutive candidates at a time and queues the survivors in shared
+        // memory; whenever 32 are queued the whole warp runs the rest of the
+        // test on them, so the distance work runs on full warps.
+        __shared__ int64_t queue[kBlock / 32][64];
+        const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        int qn = 0;
+        const int64_t step = (int64_t)gridDim.x * (kBlock / 32) * 32;
+        for (int64_t base = ((int64_t)blockIdx.x * (kBlock / 32) + w) * 32; base < n; base += step) {
+            const int64_t t = base + lane;
+            const bool pass = t < n && contact_candidate<T, TC, kPT, kRel, 1>(cand[t], X, Xh, Xl, mass, cc, diag, rhs);
+            const unsigned m = __ballot_sync(0xffffffffu, pass);
+            if (pass) queue[w][qn + __popc(m & ((1u << lane) - 1u))] = t;
+            qn += __popc(m);
+            __syncwarp();
+            if (qn >= 32) {
+                const int64_t tq = queue[w][lane];
+                __syncwarp();
+                if (lane < qn - 32) queue[w][lane] = queue[w][lane + 32];
+                __syncwarp();
+                qn -= 32;
+                my += contact_candidate<T, TC, kPT, kRel, 2>(cand[tq], X, Xh, Xl, mass, cc, diag, rhs);
             }
-            T q[4][3];
-            const V4<T> oh = ld4(Xh, ids[0]), ol = ld4(Xl, ids[0]);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const V4<T> ah = ld4(Xh, ids[j]), al = ld4(Xl, ids[j]);
-                q[j][0] = diff_ff(ah.x, al.x, oh.x, ol.x);
-                q[j][1] = diff_ff(ah.y, al.y, oh.y, ol.y);
-                q[j][2] = diff_ff(ah.z, al.z, oh.z, ol.z);
-            }
-            const T dhf = (T)cc.dh;
-            bool far = false;
-            if (kPT) {
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const T tmin = geo::mn3(q[1][k], q[2][k], q[3][k]), tmax = geo::mx3(q[1][k], q[2][k], q[3][k]);
-                    if ((q[0][k] - tmax) > dhf || (tmin - q[0][k]) > dhf) far = true;
-                }
-            } else {
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const T mina = dmin(q[0][k], q[1][k]), maxa = dmax(q[0][k], q[1][k]);
-                    const T minb = dmin(q[2][k], q[3][k]), maxb = dmax(q[2][k], q[3][k]);
-                    if ((mina - maxb) > dhf || (minb - maxa) > dhf) far = true;
-                }
-            }
-            if (far) continue;
-            T df[3], a_, b_, c_;
-            const T d2f = kPT ? geo::vtx_tri<T>(q[0], q[1], q[2], q[3], &a_, &b_, &c_, df)
-                              : geo::edge_edge_sq<T>(q[0], q[1], q[2], q[3], &a_, &b_, df);
-            if (!(d2f < (T)(1.21 * cc.dh2))) continue;
-            const V4<TC> o = ld4(X, ids[0]);  // close pair: FP64 relative coordinates
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const V4<TC> a = ld4(X, ids[j]);
-                p[j][0] = a.x - o.x;
-                p[j][1] = a.y - o.y;
-                p[j][2] = a.z - o.z;
-            }
-        } else {
-            gather4<TC, TC>(X, ids, p);
-            bool far = false;
-            if (kPT) {
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {  // point_triangle_cd_broadphase (cu:2328-2345)
-                    const TC tmin = geo::mn3(p[1][k], p[2][k], p[3][k]), tmax = geo::mx3(p[1][k], p[2][k], p[3][k]);
-                    if ((p[0][k] - tmax) > cc.dh || (tmin - p[0][k]) > cc.dh) far = true;
-                }
-            } else {
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {  // edge_edge_cd_broadphase (cu:2405-2424)
-                    const TC mina = dmin(p[0][k], p[1][k]), maxa = dmax(p[0][k], p[1][k]);
-                    const TC minb = dmin(p[2][k], p[3][k]), maxb = dmax(p[2][k], p[3][k]);
-                    if ((mina - maxb) > cc.dh || (minb - maxa) > cc.dh) far = true;
-                }
-            }
-            if (far) continue;
         }
-        TC d[3], dist2, mp, mq;
-        if (kPT) {
-            TC a, b, cq;
-            dist2 = geo::vtx_tri(p[0], p[1], p[2], p[3], &a, &b, &cq, d);
-            if (dist2 >= cc.dh2) continue;
-            mp = mass[c.x];
-            mq = a * mass[c.y] + b * mass[c.z] + cq * mass[c.w];
-        } else {
-            TC r, s;
-            dist2 = geo::edge_edge_sq(p[0], p[1], p[2], p[3], &r, &s, d);
-            if (dist2 >= cc.dh2) continue;
-            mp = (TC(1) - r) * mass[c.x] + r * mass[c.y];
-            mq = (TC(1) - s) * mass[c.z] + s * mass[c.w];
-        }
-        ++my;
-        TC dist = dsqrt(dist2);
-        const TC t2 = dist2 - cc.dh2;
-        const TC bar = -cc.kappa * t2 * t2 * dlog(dist2 / cc.dh2) / (cc.dh2 * cc.dh2);
-        const TC w = bar + dmin(mp, mq) / (cc.dt * cc.dt);
-        const TC rp = mq / (mp + mq), rq = mp / (mp + mq);
-        const TC len = dsqrt(geo::dot3(d, d));
-        for (int k = 0; k < 3; ++k) d[k] /= len;
-        dist = cc.dh - dist;
-        const TC dp = dist * rp, dq = dist * rq;
-        for (int j = 0; j < 4; ++j) atomicAdd(diag + ids[j], (T)w);
-        for (int k = 0; k < 3; ++k) {
-            TC t0, t1, t2_, t3;
-            if (kRel) {  // w (target - x)
-                t0 = w * (dp * d[k]);
-                t1 = kPT ? -w * (dq * d[k]) : w * (dp * d[k]);
-                t2_ = -w * (dq * d[k]);
-                t3 = -w * (dq * d[k]);
-            } else {
-                t0 = w * (p[0][k] + dp * d[k]);
-                t1 = kPT ? w * (p[1][k] - dq * d[k]) : w * (p[1][k] + dp * d[k]);
-                t2_ = w * (p[2][k] - dq * d[k]);
-                t3 = w * (p[3][k] - dq * d[k]);
-            }
-            atomicAdd(&rhs[ids[0]].x + k, (T)t0);
-            atomicAdd(&rhs[ids[1]].x + k, (T)t1);
-            atomicAdd(&rhs[ids[2]].x + k, (T)t2_);
-            atomicAdd(&rhs[ids[3]].x + k, (T)t3);
-        }
+        if (lane < qn) my += contact_candidate<T, TC, kPT, kRel, 2>(cand[queue[w][lane]], X, Xh, Xl, mass, cc, diag, rhs);
+    } else {
+        for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+            my += contact_candidate<T, TC, kPT, kRel, 0>(cand[t], X, Xh, Xl, mass, cc, diag, rhs);
     }
     my = warp_sum(my);
     if ((threadIdx.x & 31) == 0 && my) atomicAdd(active, (unsigned long long)my);

@@ -178,6 +178,55 @@ __device__ __forceinline__ R box_gap2(const R (*a)[3], const R (*b)[3]) {
     return g2;
 }
 
+// True when ccd_pt / ccd_ee below return 1 before computing any distance (no
+// relative motion, or the box-gap exit of their first step): the same
+// arithmetic as their opening lines, on copies.
+template <typename R>
+__device__ __forceinline__ bool ccd_pt_trivial(const R (*x)[3], const R (*dx)[3]) {
+    R mov[3], d[4][3];
+    for (int k = 0; k < 3; ++k) mov[k] = (dx[0][k] + dx[1][k] + dx[2][k] + dx[3][k]) / R(4);
+    for (int j = 0; j < 4; ++j)
+        for (int k = 0; k < 3; ++k) d[j][k] = dx[j][k] - mov[k];
+    R m2 = dmax(sqn(d[1]), sqn(d[2]));
+    m2 = dmax(m2, sqn(d[3]));
+    const R maxd = dsqrt(sqn(d[0])) + dsqrt(m2);
+    return maxd == R(0) || R(0.81) * box_gap2<R, 1, 3>(x, x + 1) > R(4) * maxd * maxd;
+}
+template <typename R>
+__device__ __forceinline__ bool ccd_ee_trivial(const R (*x)[3], const R (*dx)[3]) {
+    R mov[3], d[4][3];
+    for (int k = 0; k < 3; ++k) mov[k] = (dx[0][k] + dx[1][k] + dx[2][k] + dx[3][k]) / R(4);
+    for (int j = 0; j < 4; ++j)
+        for (int k = 0; k < 3; ++k) d[j][k] = dx[j][k] - mov[k];
+    const R m0 = dmax(sqn(d[0]), sqn(d[1])), m1 = dmax(sqn(d[2]), sqn(d[3]));
+    const R maxd = dsqrt(m0) + dsqrt(m1);
+    return maxd == R(0) || R(0.81) * box_gap2<R, 2, 2>(x, x + 2) > R(4) * maxd * maxd;
+}
+
+// The same exit decided from approximate coordinates: x and dx within eps of
+// the exact ones per component.  The motion bound is taken eps_m larger and the
+// box gap eps_g smaller (eps_m >= 8 eps, eps_g >= 4 eps cover the mean
+// subtraction, the norms and the box corners), so a true result implies the
+// exact test's.
+template <typename R, bool kPT>
+__device__ __forceinline__ bool ccd_trivial_approx(const R (*x)[3], const R (*dx)[3], R eps_g, R eps_m) {
+    R mov[3], d[4][3];
+    for (int k = 0; k < 3; ++k) mov[k] = (dx[0][k] + dx[1][k] + dx[2][k] + dx[3][k]) / R(4);
+    for (int j = 0; j < 4; ++j)
+        for (int k = 0; k < 3; ++k) d[j][k] = dx[j][k] - mov[k];
+    R maxd;
+    if (kPT) {
+        R m2 = dmax(sqn(d[1]), sqn(d[2]));
+        m2 = dmax(m2, sqn(d[3]));
+        maxd = dsqrt(sqn(d[0])) + dsqrt(m2);
+    } else {
+        maxd = dsqrt(dmax(sqn(d[0]), sqn(d[1]))) + dsqrt(dmax(sqn(d[2]), sqn(d[3])));
+    }
+    maxd += eps_m;
+    const R gap = dsqrt(kPT ? box_gap2<R, 1, 3>(x, x + 1) : box_gap2<R, 2, 2>(x, x + 2)) - eps_g;
+    return gap > R(0) && R(0.81) * gap * gap > R(4) * maxd * maxd;
+}
+
 // ccdVertexTriangleToi (cu:2460-2529): additive CCD, at most max_iter conservative steps
 template <typename R>
 __device__ R ccd_pt(R (*x)[3], R (*dx)[3], R eta, int max_iter) {
