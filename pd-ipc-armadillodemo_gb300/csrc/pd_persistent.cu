@@ -2,8 +2,8 @@
 // projective-dynamics solve (lg x [local step + 15 Chebyshev-accelerated R2
 // steps as 30 weighted-Jacobi sweeps]).
 //
-// Replaces, for FP32 state, the per-sweep launches of pd_kernels.cu (and the
-// reference's 3 + 15 launches per local-global iteration with a device
+// Replaces, for FP32 solver arithmetic, the per-sweep launches of pd_kernels.cu
+// (and the reference's 3 + 15 launches per local-global iteration with a device
 // synchronisation after each, PdIpcGpuFunc.cu:1245-1346).  Layout:
 //   * every CTA owns a contiguous run of SELL-32 slices (rows); when it fits,
 //     its slice of the constant off-diagonal matrix N is copied once per launch
@@ -11,12 +11,17 @@
 //     index into a small table of distinct offset patterns (a structured mesh
 //     has a few dozen); otherwise the matrix is streamed from L2;
 //   * each thread owns R rows (one per slice it handles) and keeps their
-//     current/previous iterate, right-hand side and inverse diagonal in registers;
-//   * only the vector being gathered crosses CTAs (through L2, and through L1
-//     once the synchronisation's acquire has invalidated it), between phases;
+//     right-hand side and inverse diagonal in registers;
 //   * a phase ends with neighbour synchronisation (each CTA waits only for the
 //     CTAs it exchanges rows with) or, optionally, a grid barrier (a
-//     counter/generation pair).
+//     counter/generation pair);
+//   * band path (mixed precision, kMode 2): the iterate's band of the CTA stays
+//     in shared memory (own rows as planar floats, the halo as 16-byte vertices
+//     filled by cp.async.bulk copies on an mbarrier), the offset patterns come
+//     from parameter space, and one extra warp without rows publishes each
+//     sweep, polls the neighbours and issues the copies while the row warps sum
+//     their entries on own rows; other paths gather the iterate from global
+//     memory (through L1 once the synchronisation's acquire has invalidated it).
 // Every wait is clock-bounded: on timeout it raises kErrBarrier and every later
 // wait returns at once, so the kernel always terminates.  The launch is
 // cooperative (all CTAs co-resident).
