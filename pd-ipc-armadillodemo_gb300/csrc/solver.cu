@@ -1265,7 +1265,7 @@ private:
     unsigned* pBar_ = nullptr;
     unsigned* pFlags_ = nullptr;  // per-CTA phase counts of the neighbour synchronisation
     int2* pNbr_ = nullptr;        // per-CTA range of CTAs to wait for
-    int2* pBand_ = nullptr;       // per-CTA [first, last + 1) column of its rows (staged band)
+    int2* pBand_ = nullptr;       // per-CTA [first, last + 1) column of its rows (band path)
     unsigned epoch_ = 1;
     V4<TC>* stage_ = nullptr;  // pinned host staging of one state vector
     cudaGraph_t graph_ = nullptr;

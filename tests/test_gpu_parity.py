@@ -222,6 +222,29 @@ def test_persistent_solve_matches_per_sweep_launches(prec, atol, n, variant, bui
     assert np.abs(a.positions() - b.positions()).max() < 10 * atol
 
 
+@pytest.mark.parametrize("which", ["stack", "batched"])
+def test_mixed_persistent_solve_on_multi_cloth_scenes(which, built_lib):
+    """Several cloths in one context: three equal layers (the band path: CTA
+    blocks and halos cross cloth boundaries) and uneven batched instances
+    (whichever persistent path their offset patterns allow) give the same
+    mixed-precision PD solve and steps as one launch per sweep."""
+    if which == "stack":
+        sc = scenes.stack(3, 24, 3, gap=2e-3, lg=10, steps=30, dhat=5e-4, drop=3e-3)
+    else:
+        sc = scenes.batched(6, 8, 20, seed=3, steps=60)
+    a = pdipc.Simulator(sc, "mixed")
+    b = pdipc.Simulator(sc, "mixed", persistent=0)
+    assert a.stats()["pd_path"] in (1, 2, 3) and b.stats()["pd_path"] == 0
+    if which == "stack":
+        assert a.stats()["pd_path"] == 3
+    X = sc.initial_positions()
+    V = np.random.default_rng(6).uniform(-0.1, 0.1, (sc.n_sim, 3))
+    assert np.abs(a.stage_pd(X, V) - b.stage_pd(X, V)).max() < 1e-6
+    a.step(5)
+    b.step(5)
+    assert np.abs(a.positions() - b.positions()).max() < 1e-5
+
+
 def test_graph_and_plain_launches_agree(built_lib):
     sc = small_scene(16, 2)
     a = pdipc.Simulator(sc, "fp64", use_graphs=1)
