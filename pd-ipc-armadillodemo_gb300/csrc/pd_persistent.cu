@@ -33,6 +33,7 @@
 
 #include "kernels.cuh"
 #include "persistent.h"
+#include "svd3.cuh"
 
 namespace pdipc {
 
@@ -206,6 +207,44 @@ __device__ __forceinline__ void stcg4(V4<double>* p, int i, double x, double y, 
     double2* q = reinterpret_cast<double2*>(p) + 2 * (size_t)i;
     __stcg(q, make_double2(x, y));
     __stcg(q + 1, make_double2(z, 0.0));
+}
+
+// One tet's strain projection (solveVolumetricStrainConstraintKernel,
+// PdIpcGpuFunc.cu:439-599) inside the persistent solve: Ds from the current
+// positions (the float-float mirror in the correction form), w R G to TetOut.
+// Out of line: it runs once per tet and local-global iteration, and its
+// registers stay out of the sweeps.  Positions come from L2 (written by other
+// CTAs earlier in the launch).
+template <typename S, bool kCorr>
+__device__ __noinline__ void tet_project_one(int e, const int4* __restrict__ Tets, const float* __restrict__ Idm,
+                                             const float* __restrict__ W, const V4<S>* __restrict__ P,
+                                             const V4<float>* __restrict__ Ph, const V4<float>* __restrict__ Pl,
+                                             V4<float>* __restrict__ Out) {
+    const int4 q = Tets[e];
+    const int id[4] = {q.x, q.y, q.z, q.w};
+    float Ds[3][3];
+    if constexpr (kCorr) {
+        const V4<float> h0 = ldcg4(Ph, id[0]), l0 = ldcg4(Pl, id[0]);
+        for (int c = 0; c < 3; ++c) {
+            const V4<float> h = ldcg4(Ph, id[c + 1]), l = ldcg4(Pl, id[c + 1]);
+            Ds[0][c] = diff_ff(h.x, l.x, h0.x, l0.x);
+            Ds[1][c] = diff_ff(h.y, l.y, h0.y, l0.y);
+            Ds[2][c] = diff_ff(h.z, l.z, h0.z, l0.z);
+        }
+    } else {
+        const V4<S> x0 = ldcg4(P, id[0]);
+        for (int c = 0; c < 3; ++c) {
+            const V4<S> x = ldcg4(P, id[c + 1]);
+            Ds[0][c] = x.x - x0.x;
+            Ds[1][c] = x.y - x0.y;
+            Ds[2][c] = x.z - x0.z;
+        }
+    }
+    float idm[9];
+    for (int k = 0; k < 9; ++k) idm[k] = __ldg(Idm + 9 * (size_t)e + k);
+    float out[4][3];
+    svd::tet_project<float>(Ds, idm, __ldg(W + e), out);
+    for (int c = 0; c < 4; ++c) __stcg(reinterpret_cast<float4*>(Out) + 4 * (size_t)e + c, make_float4(out[c][0], out[c][1], out[c][2], 0.f));
 }
 
 // S is the state scalar: T in the direct form, double in the correction form,
@@ -471,6 +510,10 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
             }
             stcg4(a.Aq, i, a0, a1, a2);
         }
+        // ---- tet strain projections of the tets this CTA owns ----
+        if (a.ntet > 0)
+            for (int q = a.ctaTetPtr[cta] + (int)threadIdx.x; q < a.ctaTetPtr[cta + 1]; q += (int)blockDim.x)
+                tet_project_one<S, kCorr>(a.ctaTetIdx[q], a.Tets, a.TetIdm, a.TetW, a.P, a.Ph, a.Pl, a.TetOut);
         if (!sync()) return;
 
         // ---- right-hand side (direct) or residual (correction) of the owned rows ----
@@ -536,6 +579,13 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     r1.add(bt * ak.y);
                     r2.add(bt * ak.z);
                 }
+                if (a.ntet > 0)
+                    for (int q = a.vtPtr[i]; q < a.vtPtr[i + 1]; ++q) {  // tet projections w R G, ascending tet
+                        const V4<T> t = ldcg4(a.TetOut, a.vtIdx[q]);
+                        r0.add(t.x);
+                        r1.add(t.y);
+                        r2.add(t.z);
+                    }
                 for (int k = 0; k < slen(r); ++k) {
                     T v;
                     int j;
@@ -576,6 +626,13 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     u1 += bt * ak.y;
                     u2 += bt * ak.z;
                 }
+                if (a.ntet > 0)
+                    for (int q = a.vtPtr[i]; q < a.vtPtr[i + 1]; ++q) {  // tet projections, ascending tet
+                        const V4<T> t = ldcg4(a.TetOut, a.vtIdx[q]);
+                        u0 += t.x;
+                        u1 += t.y;
+                        u2 += t.z;
+                    }
                 const V4<T> c = ldcg4(a.CollRhs, i);
                 u0 += c.x;
                 u1 += c.y;

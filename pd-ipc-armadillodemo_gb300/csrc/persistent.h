@@ -70,6 +70,18 @@ struct PersistArgs {
     const T* lBendT;
     const T* Strain;
     const T* CurvNorm;
+    // tetrahedral strain constraints: CTA c projects tets ctaTetIdx[ctaTetPtr[c] ..
+    // ctaTetPtr[c + 1]) (those whose first vertex it owns) in its curvature phase;
+    // rows gather their projections through vtPtr / vtIdx in the residual phase
+    int ntet;
+    const int4* Tets;
+    const T* TetIdm;
+    const T* TetW;
+    V4<T>* TetOut;
+    const int* vtPtr;
+    const int* vtIdx;
+    const int* ctaTetPtr;
+    const int* ctaTetIdx;
     // matrix
     const int* sliceEntry;  // SELL entry offset of every slice
     const int* sliceLen;

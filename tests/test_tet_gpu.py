@@ -15,7 +15,9 @@ pytestmark = pytest.mark.gpu
 def run_against(scene, prec, oracle_prec, steps, every, threads=8, check_outer=True):
     sim = pdipc.Simulator(scene, prec)
     orc = Oracle(scene, oracle_prec, FORM_JJ, threads=threads)
-    assert sim.stats()["pd_path"] == 0          # tets take the per-sweep path
+    # FP64 solves launch per sweep; FP32 and mixed ones run the persistent kernel,
+    # which projects the tets in its curvature phase
+    assert (sim.stats()["pd_path"] == 0) == (prec == "fp64")
     worst, contacts = 0.0, 0
     for _ in range(steps // every):
         sim.step(every)
@@ -76,3 +78,21 @@ def test_block_pd_solve_matches_oracle(built_lib):
         xg = pdipc.Simulator(sc, prec).stage_pd(X, V)
         xo = Oracle(sc, "fp64", FORM_JJ, threads=8).stage_pd(X, V)
         assert np.abs(xg - xo).max() < atol, (prec, np.abs(xg - xo).max())
+
+
+@pytest.mark.parametrize("prec,atol", [("fp32", 2e-5), ("mixed", 1e-6)])
+@pytest.mark.parametrize("with_cloth", [False, True])
+def test_persistent_solve_with_tets_matches_per_sweep_launches(prec, atol, with_cloth, built_lib):
+    """The persistent kernel's tet projections (curvature phase, one CTA per
+    tet) and their gathers give the per-sweep path's PD solve, alone and with a
+    cloth in the same context."""
+    sc = scenes.block_drop(3, 2, cloth_n=16) if with_cloth else scenes.block_drop(4, 2)
+    a = pdipc.Simulator(sc, prec)
+    b = pdipc.Simulator(sc, prec, persistent=0)
+    assert a.stats()["pd_path"] in (1, 2, 3) and b.stats()["pd_path"] == 0
+    X = sc.initial_positions()
+    V = np.random.default_rng(12).uniform(-0.2, 0.2, (sc.n_sim, 3))
+    assert np.abs(a.stage_pd(X, V) - b.stage_pd(X, V)).max() < atol
+    a.step(3)
+    b.step(3)
+    assert np.abs(a.positions() - b.positions()).max() < 10 * atol
