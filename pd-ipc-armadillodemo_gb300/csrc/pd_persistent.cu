@@ -250,12 +250,15 @@ __device__ __noinline__ void tet_project_one(int e, const int4* __restrict__ Tet
 // S is the state scalar: T in the direct form, double in the correction form,
 // where positions enter the FP32 arithmetic as differences formed from their
 // float-float mirror (Ph, Pl): no FP64 arithmetic in the per-neighbour loops.
-// kMode: 0 matrix streamed from L2; 1 matrix in shared memory, gathers from
-// global memory; 2 matrix and the band of the iterate in shared memory
+// kMode bits 0-1: 0 matrix streamed from L2; 1 matrix in shared memory, gathers
+// from global memory; 2 matrix and the band of the iterate in shared memory.
+// Bit 2: the scene has tets (compiled in only then: the projection's call
+// costs the cloth-only kernel 7% through register allocation).
 template <typename T, typename S, bool kCorr, int kMode, bool kL1, int R>
 __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(const __grid_constant__ PersistArgs<T, S> a) {
-    constexpr bool kSmem = kMode >= 1;
-    constexpr bool band = kMode == 2;
+    constexpr bool kTets = (kMode & 4) != 0;
+    constexpr bool kSmem = (kMode & 3) >= 1;
+    constexpr bool band = (kMode & 3) == 2;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int abort_s;  // band path: a neighbour wait failed, every warp returns
     const int cta = blockIdx.x;
@@ -511,7 +514,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
             stcg4(a.Aq, i, a0, a1, a2);
         }
         // ---- tet strain projections of the tets this CTA owns ----
-        if (a.ntet > 0)
+        if constexpr (kTets)
             for (int q = a.ctaTetPtr[cta] + (int)threadIdx.x; q < a.ctaTetPtr[cta + 1]; q += (int)blockDim.x)
                 tet_project_one<S, kCorr>(a.ctaTetIdx[q], a.Tets, a.TetIdm, a.TetW, a.P, a.Ph, a.Pl, a.TetOut);
         if (!sync()) return;
@@ -579,7 +582,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     r1.add(bt * ak.y);
                     r2.add(bt * ak.z);
                 }
-                if (a.ntet > 0)
+                if constexpr (kTets)
                     for (int q = a.vtPtr[i]; q < a.vtPtr[i + 1]; ++q) {  // tet projections w R G, ascending tet
                         const V4<T> t = ldcg4(a.TetOut, a.vtIdx[q]);
                         r0.add(t.x);
@@ -626,7 +629,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     u1 += bt * ak.y;
                     u2 += bt * ak.z;
                 }
-                if (a.ntet > 0)
+                if constexpr (kTets)
                     for (int q = a.vtPtr[i]; q < a.vtPtr[i + 1]; ++q) {  // tet projections, ascending tet
                         const V4<T> t = ldcg4(a.TetOut, a.vtIdx[q]);
                         u0 += t.x;
@@ -865,6 +868,13 @@ const void* kernel_for(int R) {
         default: return (const void*)k_pd_persistent<T, S, kCorr, kMode, kL1, 4>;
     }
 }
+// with tets: gathers through L1, one or two rows per thread
+template <typename T, bool kCorr, int kMode>
+const void* kernel_for_tets(int R) {
+    using S = typename std::conditional<kCorr, double, T>::type;
+    return R == 1 ? (const void*)k_pd_persistent<T, S, kCorr, kMode | 4, true, 1>
+                  : (const void*)k_pd_persistent<T, S, kCorr, kMode | 4, true, 2>;
+}
 
 template <bool kL1>
 const void* kernel_for_l1(bool correction, int mode, int R) {
@@ -877,8 +887,18 @@ const void* kernel_for_l1(bool correction, int mode, int R) {
 
 }  // namespace
 
-const void* persistent_kernel(bool correction, bool matrix_in_smem, bool band, bool l1_gather, int rows_per_thread) {
+const void* persistent_kernel(bool correction, bool matrix_in_smem, bool band, bool l1_gather, int rows_per_thread,
+                              bool tets) {
     const int mode = band ? 2 : (matrix_in_smem ? 1 : 0);
+    if (tets) {
+        if (!l1_gather || rows_per_thread > 2) return nullptr;
+        if (correction)
+            return mode == 2 ? kernel_for_tets<float, true, 2>(rows_per_thread)
+                             : mode == 1 ? kernel_for_tets<float, true, 1>(rows_per_thread)
+                                         : kernel_for_tets<float, true, 0>(rows_per_thread);
+        return mode >= 1 ? kernel_for_tets<float, false, 1>(rows_per_thread)
+                         : kernel_for_tets<float, false, 0>(rows_per_thread);
+    }
     return l1_gather ? kernel_for_l1<true>(correction, mode, rows_per_thread)
                      : kernel_for_l1<false>(correction, mode, rows_per_thread);
 }
@@ -887,7 +907,8 @@ template <typename S>
 cudaError_t launch_args(const PersistPlan& plan, const PersistArgs<float, S>& args, cudaStream_t s) {
     const bool correction = std::is_same<S, double>::value;
     const void* f = persistent_kernel(correction, plan.matrix_in_smem, plan.own_max > 0, plan.l1_gather,
-                                      plan.rows_per_thread);
+                                      plan.rows_per_thread, args.ntet > 0);
+    if (!f) return cudaErrorInvalidConfiguration;
     void* params[] = {(void*)&args};
     return cudaLaunchCooperativeKernel(f, dim3(plan.ctas), dim3(plan.threads), params, plan.smem_bytes, s);
 }

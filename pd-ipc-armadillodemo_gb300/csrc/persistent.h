@@ -114,7 +114,9 @@ struct PersistArgs {
     int haloMax;
 };
 
-const void* persistent_kernel(bool correction, bool matrix_in_smem, bool band, bool l1_gather, int rows_per_thread);
+// nullptr: no such kernel (tets need L1 gathers and at most two rows per thread)
+const void* persistent_kernel(bool correction, bool matrix_in_smem, bool band, bool l1_gather, int rows_per_thread,
+                              bool tets);
 // direct form (FP32 state) and correction form (FP64 state)
 cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, float>& args, cudaStream_t s);
 cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, double>& args, cudaStream_t s);

@@ -795,7 +795,8 @@ private:
                     }
                 }
                 const int threads = (W + (ownMax > 0 ? 1 : 0)) * 32;
-                const void* f = persistent_kernel(kCorrection, smem_mat, ownMax > 0, prm_.persistent != 2, R);
+                const void* f = persistent_kernel(kCorrection, smem_mat, ownMax > 0, prm_.persistent != 2, R, H.ntet > 0);
+                if (!f) continue;
                 PD_CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
                 int per_sm = 0;
                 PD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, threads, sm));
