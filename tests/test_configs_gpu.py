@@ -8,7 +8,9 @@ the GPU against the CPU oracle.
   * config 2 (batched independent drops): a reduced batch of cloths of uneven
     sizes and stiffnesses in one context, FP64 within 1e-5 m of the oracle;
   * config 4 (stacked layers with self-collision): a reduced stack, FP64 within
-    1e-5 m of the oracle through layer-layer contact.
+    1e-5 m of the oracle through layer-layer contact;
+  * config 1 at full size (512x512): the mixed mode's band path, one step at a
+    time from the plain FP64 GPU form's own state, within 1e-5 m.
 """
 import numpy as np
 import pytest
@@ -103,3 +105,21 @@ def test_stacked_layers_self_collision_fp64_match_oracle(built_lib):
         contacts = max(contacts, orc.stats()["active_contacts"])
     assert contacts > 0
     assert worst < 1e-5, worst
+
+
+def test_config1_full_size_mixed_steps_from_fp64_state(built_lib):
+    """512x512 cloth: each of the first steps of the mixed mode (persistent
+    solve with the shared-memory band), started from the FP64 form's state,
+    lands within 1e-5 m of the FP64 form's next state."""
+    sc = scenes.config1()
+    mixed = pdipc.Simulator(sc, "mixed")
+    ref = pdipc.Simulator(sc, "fp64")
+    worst = 0.0
+    for _ in range(3):
+        mixed.set_state(ref.positions(), ref.velocities())
+        mixed.step(1)
+        ref.step(1)
+        assert mixed.stats()["pd_path"] == 3
+        assert abs(mixed.stats()["last_outer_iters"] - ref.stats()["last_outer_iters"]) <= 1
+        worst = max(worst, float(np.abs(mixed.positions() - ref.positions()).max()))
+    assert np.isfinite(worst) and worst < 1e-5, worst
