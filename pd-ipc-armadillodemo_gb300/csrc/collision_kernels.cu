@@ -540,7 +540,8 @@ __global__ void __launch_bounds__(kBlock, kCandBlocks<T>) k_toi(int64_t n, const
                                                 const V4<T>* __restrict__ X0h, const V4<T>* __restrict__ X0l,
                                                 const V4<T>* __restrict__ X1h, const V4<T>* __restrict__ X1l,
                                                 TC slack, TC eta, int max_iter, TC* __restrict__ per,
-                                                TC* __restrict__ toi_min) {
+                                                TC* __restrict__ toi_min, const OuterGate* __restrict__ gate) {
+    if (outer_stopped(gate)) return;
     TC local = TC(1);
     if constexpr (kRel) {
         __shared__ int64_t queue[kBlock / 32][64];
@@ -601,11 +602,25 @@ __global__ void __launch_bounds__(kBlock, kCandBlocks<T>) k_toi(int64_t n, const
 }
 
 template <typename TC>
-__global__ void k_toi_finalize(TC* __restrict__ toi_min, TC* __restrict__ toi, double scale) {
+__global__ void k_toi_finalize(TC* __restrict__ toi_min, TC* __restrict__ toi, double scale,
+                               const OuterGate* __restrict__ gate) {
+    if (outer_stopped(gate)) return;
     const TC m = *toi_min;
     const TC t = (m < TC(1)) ? (TC)((double)m * scale) : TC(1);
     *toi = t;
     *toi_min = TC(1);
+}
+
+// the contact pass's accumulators start from zero
+template <typename T>
+__global__ void k_contact_clear(int n, T* __restrict__ diag, V4<T>* __restrict__ rhs,
+                                unsigned long long* __restrict__ active, const OuterGate* __restrict__ gate) {
+    if (outer_stopped(gate)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *active = 0ull;
+    if (i >= n) return;
+    diag[i] = T(0);
+    rhs[i] = V4<T>{T(0), T(0), T(0), T(0)};
 }
 
 template <typename TC>
@@ -780,7 +795,9 @@ __global__ void __launch_bounds__(kBlock, kCandBlocks<T>) k_contact(int64_t n, c
                                                     const V4<TC>* __restrict__ X, const V4<T>* __restrict__ Xh,
                                                     const V4<T>* __restrict__ Xl, const TC* __restrict__ mass,
                                                     ContactConsts<TC> cc, T* __restrict__ diag,
-                                                    V4<T>* __restrict__ rhs, unsigned long long* __restrict__ active) {
+                                                    V4<T>* __restrict__ rhs, unsigned long long* __restrict__ active,
+                                                    const OuterGate* __restrict__ gate) {
+    if (outer_stopped(gate)) return;
     unsigned int my = 0;
     if constexpr (kRel) {
         // Most candidates fail the cheap stage-1 filter.  Each warp filters 32
@@ -874,21 +891,19 @@ void launch_toi(const Dev<T, TC>& d, Pos<T, TC> X0, Pos<T, TC> X1, const SolverC
     if (d.nPT > 0)
         k_toi<T, TC, true, kRel><<<grid_cap(d.nPT), kBlock, 0, s>>>(
             d.nPT, d.PT, X0.x, X1.x, X0.hi, X0.lo, X1.hi, X1.lo, (TC)c.ccd_slack, (TC)c.ccd_eta, c.ccd_max_iter,
-            per_pt, d.ToiMin);
+            per_pt, d.ToiMin, d.Gate);
     if (d.nEE > 0)
         k_toi<T, TC, false, kRel><<<grid_cap(d.nEE), kBlock, 0, s>>>(
             d.nEE, d.EE, X0.x, X1.x, X0.hi, X0.lo, X1.hi, X1.lo, (TC)c.ccd_slack, (TC)c.ccd_eta, c.ccd_max_iter,
-            per_ee, d.ToiMin);
+            per_ee, d.ToiMin, d.Gate);
 }
 template <typename T, typename TC>
 void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s) {
-    k_toi_finalize<TC><<<1, 1, 0, s>>>(d.ToiMin, d.Toi, c.toi_scale);
+    k_toi_finalize<TC><<<1, 1, 0, s>>>(d.ToiMin, d.Toi, c.toi_scale, d.Gate);
 }
 template <typename T, typename TC>
 void launch_contact(const Dev<T, TC>& d, Pos<T, TC> X, const SolverConsts& c, cudaStream_t s) {
-    cudaMemsetAsync(d.CollDiag, 0, sizeof(T) * d.ntot, s);
-    cudaMemsetAsync(d.CollRhs, 0, sizeof(V4<T>) * d.ntot, s);
-    cudaMemsetAsync(d.ActiveCount, 0, sizeof(unsigned long long), s);
+    k_contact_clear<T><<<blocks_for(d.ntot), kBlock, 0, s>>>(d.ntot, d.CollDiag, d.CollRhs, d.ActiveCount, d.Gate);
     ContactConsts<TC> cc;
     const T dh = (T)c.dhat;
     cc.dh = (TC)dh;
@@ -898,11 +913,12 @@ void launch_contact(const Dev<T, TC>& d, Pos<T, TC> X, const SolverConsts& c, cu
     constexpr bool kRel = sizeof(T) == 4 && sizeof(TC) == 8;
     if (d.nPT > 0)
         k_contact<T, TC, true, kRel><<<grid_cap(d.nPT), kBlock, 0, s>>>(d.nPT, d.PT, X.x, X.hi, X.lo, d.CollMass,
-                                                                         cc, d.CollDiag, d.CollRhs, d.ActiveCount);
+                                                                         cc, d.CollDiag, d.CollRhs, d.ActiveCount,
+                                                                         d.Gate);
     if (d.nEE > 0)
         k_contact<T, TC, false, kRel><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X.x, X.hi, X.lo,
                                                                           d.CollMass, cc, d.CollDiag, d.CollRhs,
-                                                                          d.ActiveCount);
+                                                                          d.ActiveCount, d.Gate);
 }
 
 // ---------------- no-allocation scratch of the per-candidate toi pass ----------------

@@ -155,4 +155,17 @@ enum ErrFlag : unsigned int {
     kErrBarrier = 16u,  // a grid barrier of the persistent solve timed out
 };
 
+// Stopping test of the outer loop, made on the device.  k_outer_gate writes it
+// after each outer iteration's contact pass; every kernel launched by a later
+// outer iteration of the step (and the iteration's own copy of the positions
+// into Pold) reads `stop` at entry and returns without work once it is set.
+// That lets the host enqueue outer iteration k+1 before it has read
+// iteration k's residual.
+struct OuterGate {
+    unsigned stop;   // the stopping rule held at an earlier outer iteration
+    int iters;       // outer iterations run so far in this step
+    double resid;    // |dir|^2 of the last iteration run
+};
+__device__ __forceinline__ bool outer_stopped(const OuterGate* g) { return g && g->stop; }
+
 }  // namespace pdipc

@@ -122,6 +122,10 @@ struct Dev {
     double* Resid = nullptr;      // |dir|^2
     unsigned int* ErrFlags = nullptr;
     unsigned long long* ActiveCount = nullptr;
+    // set only while a step runs: the kernels of the outer loop (direction,
+    // CCD, clamp, contact, copy into Pold, persistent solve) return at entry
+    // once Gate->stop is set; null everywhere else (stage entry points)
+    OuterGate* Gate = nullptr;
 };
 
 // A position array and its float-float mirror (null outside the correction form).
@@ -172,6 +176,10 @@ template <typename T, typename TC>
 void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s);
 template <typename T, typename TC>
 void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s);
+// the outer loop's stopping test on the device (d.Gate must be set): after
+// outer iteration `outer`, stop when test && outer > 0 && Resid < tol
+template <typename T, typename TC>
+void launch_outer_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cudaStream_t s);
 // correction form: write the float-float mirror (hi, lo; lo may be null) of n
 // positions X, after a host write of X
 template <typename T, typename TC>

@@ -463,8 +463,10 @@ __global__ void k_local_aq_rel(int nsim, const V4<float>* __restrict__ Ph, const
 
 template <typename T, typename S>  // S: the state scalar
 __global__ void k_direction(int nsim, const V4<S>* __restrict__ P, const V4<S>* __restrict__ Pold,
-                            V4<S>* __restrict__ Dir, V4<T>* __restrict__ Dh, double* __restrict__ part) {
+                            V4<S>* __restrict__ Dir, V4<T>* __restrict__ Dh, double* __restrict__ part,
+                            const OuterGate* __restrict__ gate) {
     __shared__ double red[kBlock / 32];
+    if (outer_stopped(gate)) return;
     double acc = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nsim; i += gridDim.x * blockDim.x) {
         const V4<S> a = P[i], b = Pold[i];
@@ -486,9 +488,9 @@ __global__ void k_direction(int nsim, const V4<S>* __restrict__ P, const V4<S>* 
 template <typename T, typename S>  // S: the state scalar
 __global__ void k_clamp(int nsim, const V4<S>* __restrict__ Pold, const V4<S>* __restrict__ Dir,
                         const S* __restrict__ Toi, V4<S>* __restrict__ P, V4<T>* __restrict__ Ph,
-                        V4<T>* __restrict__ Pl) {
+                        V4<T>* __restrict__ Pl, const OuterGate* __restrict__ gate) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nsim) return;
+    if (i >= nsim || outer_stopped(gate)) return;
     const S t = *Toi;
     const V4<S> a = Pold[i], d = Dir[i];
     const S x = a.x + t * d.x, y = a.y + t * d.y, z = a.z + t * d.z;
@@ -512,14 +514,25 @@ __global__ void k_split(int n, const V4<double>* __restrict__ X, V4<float>* __re
 template <typename T, typename S>
 __global__ void k_copy_old(int nsim, const V4<S>* __restrict__ P, V4<S>* __restrict__ Pold,
                            const V4<T>* __restrict__ Ph, const V4<T>* __restrict__ Pl, V4<T>* __restrict__ Poh,
-                           V4<T>* __restrict__ Pol) {
+                           V4<T>* __restrict__ Pol, const OuterGate* __restrict__ gate) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nsim) return;
+    if (i >= nsim || outer_stopped(gate)) return;
     Pold[i] = P[i];
     if constexpr (kMirror<T, S>) {
         Poh[i] = Ph[i];
         Pol[i] = Pl[i];
     }
+}
+
+// one thread: the stopping rule of the outer loop (PdIpcSimulator::advance,
+// cpp:1683-1796: stop once |dir|^2 < tol after the first iteration)
+__global__ void k_outer_gate(OuterGate* __restrict__ g, const double* __restrict__ resid, int outer, double tol,
+                             int test) {
+    if (g->stop) return;
+    const double r = *resid;
+    g->resid = r;
+    g->iters = outer + 1;
+    if (test && outer > 0 && r < tol) g->stop = 1u;
 }
 
 template <typename T>
@@ -616,12 +629,12 @@ void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T
 template <typename T, typename TC>
 void launch_direction(const Dev<T, TC>& d, cudaStream_t s) {
     const int nb = direction_blocks(d.nsim);
-    k_direction<T, TC><<<nb, kBlock, 0, s>>>(d.nsim, d.P, d.Pold, d.Dir, d.Dh, d.ResidPart);
+    k_direction<T, TC><<<nb, kBlock, 0, s>>>(d.nsim, d.P, d.Pold, d.Dir, d.Dh, d.ResidPart, d.Gate);
     launch_reduce_sum_f64(d.ResidPart, nb, d.Resid, s);
 }
 template <typename T, typename TC>
 void launch_clamp(const Dev<T, TC>& d, cudaStream_t s) {
-    k_clamp<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Pold, d.Dir, d.Toi, d.P, d.Ph, d.Pl);
+    k_clamp<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Pold, d.Dir, d.Toi, d.P, d.Ph, d.Pl, d.Gate);
 }
 template <typename T, typename TC>
 void launch_split(const Dev<T, TC>& d, const V4<TC>* X, V4<T>* hi, V4<T>* lo, int n, cudaStream_t s) {
@@ -631,7 +644,11 @@ void launch_split(const Dev<T, TC>& d, const V4<TC>* X, V4<T>* hi, V4<T>* lo, in
 }
 template <typename T, typename TC>
 void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s) {
-    k_copy_old<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.Pold, d.Ph, d.Pl, d.Poh, d.Pol);
+    k_copy_old<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.Pold, d.Ph, d.Pl, d.Poh, d.Pol, d.Gate);
+}
+template <typename T, typename TC>
+void launch_outer_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cudaStream_t s) {
+    k_outer_gate<<<1, 1, 0, s>>>(d.Gate, d.Resid, outer, tol, test ? 1 : 0);
 }
 template <typename T, typename TC>
 void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {
@@ -652,6 +669,7 @@ void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {
     template void launch_direction<T, TC>(const Dev<T, TC>&, cudaStream_t);                                  \
     template void launch_clamp<T, TC>(const Dev<T, TC>&, cudaStream_t);                                      \
     template void launch_copy_old<T, TC>(const Dev<T, TC>&, cudaStream_t);                                   \
+    template void launch_outer_gate<T, TC>(const Dev<T, TC>&, int, double, bool, cudaStream_t);              \
     template void launch_split<T, TC>(const Dev<T, TC>&, const V4<TC>*, V4<T>*, V4<T>*, int, cudaStream_t);  \
     template void launch_velocity<T, TC>(const Dev<T, TC>&, TC, cudaStream_t);
 

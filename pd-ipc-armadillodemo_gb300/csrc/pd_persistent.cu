@@ -261,6 +261,10 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     constexpr bool band = (kMode & 3) == 2;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int abort_s;  // band path: a neighbour wait failed, every warp returns
+    // the outer loop stopped at an earlier iteration: every CTA returns before
+    // its first phase; flags and barrier counters stay as they are (the next
+    // launch's phase numbers lie above them all the same)
+    if (outer_stopped(a.gate)) return;
     const int cta = blockIdx.x;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // ---- this CTA's matrix values and the offset patterns into shared memory ----

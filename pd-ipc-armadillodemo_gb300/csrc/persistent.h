@@ -97,6 +97,9 @@ struct PersistArgs {
     // grid barrier: [0] generation, [1] arrival counter
     unsigned* bar;
     unsigned* err;
+    // stop of the outer loop (null outside a step): once set, the launch
+    // returns at entry, before any phase, and publishes nothing
+    const OuterGate* gate;
     // neighbour synchronisation (nbr != null): CTA c publishes the number of
     // phases it completed, epoch0 + k, in flags[c] and, before phase k + 1,
     // waits until every CTA in [nbr[c].x, nbr[c].y] has published epoch0 + k

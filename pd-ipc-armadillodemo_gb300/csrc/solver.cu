@@ -3,11 +3,14 @@
 // the patch broad phase (gpuCcdCulling, cpp:1799-1869) and the stage entry
 // points.
 //
-// Per outer iteration the host waits once, for the 8-byte residual that decides
-// the reference's stopping rule (cpp:1774-1779); the time of impact stays on the
-// device (the reference copies it to the host, cu:2738-2740).  The
-// projective-dynamics solve of an outer iteration (1 + lg x (2 + 2 cheby - 1)
-// kernels) is captured once as a CUDA graph and replayed.
+// The reference's stopping rule (cpp:1774-1779) is tested on the device after
+// each outer iteration; the host reads its 16-byte record, and with the
+// persistent solve it has already enqueued the next iteration, whose kernels
+// return at entry if the rule stopped the loop.  The time of impact stays on
+// the device (the reference copies it to the host, cu:2738-2740).  On the
+// per-sweep path the projective-dynamics solve of an outer iteration
+// (1 + lg x (2 + 2 cheby - 1) kernels) is captured once as a CUDA graph and
+// replayed.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -35,7 +38,6 @@ T omega_next(T rho2, T omega) {  // PdIpcGpuFunc.cu:1341
 }
 
 struct Pinned {
-    double resid;
     int64_t n_pairs;
     int64_t n_pt;
     int64_t n_ee;
@@ -44,6 +46,7 @@ struct Pinned {
     unsigned long long active;
     double toi;
     float toi_f;
+    OuterGate gate[2];  // stopping-test records of the last two outer iterations
 };
 
 }  // namespace
@@ -89,12 +92,8 @@ public:
         PD_CK(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
         PD_CK(cudaEventCreate(&ev0_));
         PD_CK(cudaEventCreate(&ev1_));
-        PD_CK(cudaEventCreate(&evp0_));
-        PD_CK(cudaEventCreate(&evp1_));
-        PD_CK(cudaEventCreate(&evc0_));
-        PD_CK(cudaEventCreate(&evc1_));
-        PD_CK(cudaEventCreate(&evq0_));
-        PD_CK(cudaEventCreate(&evq1_));
+        for (auto& ring : evo_)
+            for (cudaEvent_t& e : ring) PD_CK(cudaEventCreate(&e));
         Dev<T, TC>& d = d_;
         d.nsim = H.nsim;
         d.ntot = H.ntot;
@@ -270,6 +269,7 @@ public:
         PD_CK(zeros(d.Resid, 1));
         PD_CK(zeros(d.ErrFlags, 1));
         PD_CK(zeros(d.ActiveCount, 1));
+        PD_CK(zeros(gate_, 1));
         PD_CK(cudaMallocHost(&pin_, sizeof(Pinned)));
         std::memset(pin_, 0, sizeof(Pinned));
         PD_CK(cudaMallocHost(&stage_, sizeof(V4<TC>) * (size_t)std::max(nt, 1)));
@@ -676,14 +676,12 @@ private:
         stage_ = nullptr;
         if (ev0_) cudaEventDestroy(ev0_);
         if (ev1_) cudaEventDestroy(ev1_);
-        if (evp0_) cudaEventDestroy(evp0_);
-        if (evp1_) cudaEventDestroy(evp1_);
-        if (evc0_) cudaEventDestroy(evc0_);
-        if (evc1_) cudaEventDestroy(evc1_);
-        if (evq0_) cudaEventDestroy(evq0_);
-        if (evq1_) cudaEventDestroy(evq1_);
-        evc0_ = evc1_ = evq0_ = evq1_ = nullptr;
-        ev0_ = ev1_ = evp0_ = evp1_ = nullptr;
+        for (auto& ring : evo_)
+            for (cudaEvent_t& e : ring) {
+                if (e) cudaEventDestroy(e);
+                e = nullptr;
+            }
+        ev0_ = ev1_ = nullptr;
         if (s_) cudaStreamDestroy(s_);
         s_ = nullptr;
     }
@@ -991,6 +989,7 @@ private:
             // fresh phase numbers for this launch: every flag from earlier launches is below them
             pargs_.epoch0 = epoch_;
             epoch_ += (unsigned)(c_.lg * (2 * c_.cheby + 1) + 1);
+            pargs_.gate = d_.Gate;
             return launch_pd_persistent(plan_, pargs_, s_);
         }
         return cudaErrorNotSupported;
@@ -1187,52 +1186,95 @@ private:
         return PDIPC_OK;
     }
 
-    // PdIpcSimulator::advance (cpp:1683-1796)
+    // One outer iteration of the step, enqueued without waiting: PD solve,
+    // direction, the broad phase (first iteration only), toi pass, clamp,
+    // contact pass, the stopping test on the device with its 16-byte record
+    // copied to pinned memory, then the copy of the positions into Pold,
+    // which the test skips when it stops the loop.
+    pdipc_status enqueue_outer(int outer, std::string& err) {
+        Dev<T, TC>& d = d_;
+        cudaEvent_t* ev = evo_[outer & 1];
+        PD_CK(cudaEventRecord(ev[kEvP0], s_));
+        pdipc_status r = pd_solve(err);
+        if (r != PDIPC_OK) return r;
+        PD_CK(cudaEventRecord(ev[kEvP1], s_));
+        launch_direction(d, s_);
+        launches_ += 2;
+        if (outer == 0) {
+            r = broadphase(err);
+            if (r != PDIPC_OK) return r;
+        }
+        PD_CK(cudaEventRecord(ev[kEvC0], s_));
+        launch_toi(d, pos_old(), pos(), c_, (TC*)nullptr, (TC*)nullptr, s_);
+        launch_toi_finalize(d, c_, s_);
+        PD_CK(cudaEventRecord(ev[kEvC1], s_));
+        launch_clamp(d, s_);
+        PD_CK(cudaEventRecord(ev[kEvQ0], s_));
+        launch_contact(d, pos(), c_, s_);
+        PD_CK(cudaEventRecord(ev[kEvQ1], s_));
+        launch_outer_gate(d, outer, prm_.outer_tol, prm_.fixed_outer <= 0, s_);
+        PD_CK(cudaMemcpyAsync(&pin_->gate[outer & 1], d.Gate, sizeof(OuterGate), cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaEventRecord(ev[kEvGate], s_));
+        launch_copy_old(d, s_);
+        // toi x2, finalize, clamp, contact clear, contact x2, gate, copy into Pold
+        launches_ += 2 * ((d.nPT > 0) + (d.nEE > 0)) + 5;
+        return PDIPC_OK;
+    }
+
+    // Sets the device stopping test for the kernels of one step; stage entry
+    // points outside a step launch the same kernels without it.
+    struct GateScope {
+        Dev<T, TC>& d;
+        GateScope(Dev<T, TC>& dev, OuterGate* g) : d(dev) { d.Gate = g; }
+        ~GateScope() { d.Gate = nullptr; }
+    };
+
+    // PdIpcSimulator::advance (cpp:1683-1796): predict, then outer iterations
+    // until |dir|^2 < outer_tol after the first one (or max_outer), then the
+    // velocity update.  With the persistent solve, iteration k+1 is enqueued
+    // before the host waits for iteration k's stopping test, so the GPU never
+    // idles on the host's round trip; when the test stops the loop at k, every
+    // kernel of iteration k+1 returns at entry.  The per-sweep solve (plain
+    // launches or a CUDA graph of them) has no entry test, so that path waits
+    // for each test before enqueueing the next iteration.
     pdipc_status step_once(std::string& err) {
         Dev<T, TC>& d = d_;
         const TC dt = (TC)c_.dt;
+        GateScope scope(d_, gate_);
+        PD_CK(cudaMemsetAsync(gate_, 0, sizeof(OuterGate), s_));
         launch_predict(d, dt, s_);
         ++launches_;
         const int max_outer = prm_.fixed_outer > 0 ? prm_.fixed_outer : prm_.max_outer;
-        int outer = 0;
-        for (; outer < max_outer; ++outer) {
-            PD_CK(cudaEventRecord(evp0_, s_));
-            pdipc_status r = pd_solve(err);
+        const int ahead = plan_.enabled ? 1 : 0;
+        int enq = 0, outer = 0;
+        for (; enq <= ahead && enq < max_outer; ++enq) {
+            pdipc_status r = enqueue_outer(enq, err);
             if (r != PDIPC_OK) return r;
-            PD_CK(cudaEventRecord(evp1_, s_));
-            launch_direction(d, s_);
-            launches_ += 2;
-            if (outer == 0) {
-                r = broadphase(err);
-                if (r != PDIPC_OK) return r;
-            }
-            PD_CK(cudaEventRecord(evc0_, s_));
-            launch_toi(d, pos_old(), pos(), c_, (TC*)nullptr, (TC*)nullptr, s_);
-            launch_toi_finalize(d, c_, s_);
-            PD_CK(cudaEventRecord(evc1_, s_));
-            launch_clamp(d, s_);
-            PD_CK(cudaEventRecord(evq0_, s_));
-            launch_contact(d, pos(), c_, s_);
-            PD_CK(cudaEventRecord(evq1_, s_));
-            launches_ += (d.nPT > 0) + (d.nEE > 0) + 1 + 1 + (d.nPT > 0) + (d.nEE > 0);
-            PD_CK(cudaMemcpyAsync(&pin_->resid, d.Resid, sizeof(double), cudaMemcpyDeviceToHost, s_));
-            PD_CK(cudaStreamSynchronize(s_));
+        }
+        for (int k = 0; k < max_outer; ++k) {
+            cudaEvent_t* ev = evo_[k & 1];
+            PD_CK(cudaEventSynchronize(ev[kEvGate]));
             float pms = 0.f;
-            PD_CK(cudaEventElapsedTime(&pms, evp0_, evp1_));
+            PD_CK(cudaEventElapsedTime(&pms, ev[kEvP0], ev[kEvP1]));
             pd_ms_ += pms;
-            PD_CK(cudaEventElapsedTime(&pms, evc0_, evc1_));
+            PD_CK(cudaEventElapsedTime(&pms, ev[kEvC0], ev[kEvC1]));
             ccd_ms_ += pms;
-            PD_CK(cudaEventElapsedTime(&pms, evq0_, evq1_));
+            PD_CK(cudaEventElapsedTime(&pms, ev[kEvQ0], ev[kEvQ1]));
             contact_ms_ += pms;
             ++pd_solves_;
-            const double res = pin_->resid;
-            st_.last_residual = res;
-            if (prm_.fixed_outer <= 0 && res < prm_.outer_tol && outer > 0) {
-                ++outer;
-                break;
+            const OuterGate g = pin_->gate[k & 1];
+            if (g.iters != k + 1) {
+                err = "outer-loop stopping test out of step with the host";
+                return PDIPC_ERR_STATE;
             }
-            launch_copy_old(d, s_);
-            ++launches_;
+            st_.last_residual = g.resid;
+            outer = k + 1;
+            if (g.stop) break;
+            if (enq < max_outer) {
+                pdipc_status r = enqueue_outer(enq, err);
+                if (r != PDIPC_OK) return r;
+                ++enq;
+            }
         }
         const TC damping = (TC)(1.0 - (double)dt);
         const TC invt = (TC)((1.0 / (double)dt) * (double)damping);
@@ -1274,8 +1316,11 @@ private:
     SolverConsts c_{};
     cudaStream_t s_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
-    cudaEvent_t evp0_ = nullptr, evp1_ = nullptr;  // around each PD solve
-    cudaEvent_t evc0_ = nullptr, evc1_ = nullptr, evq0_ = nullptr, evq1_ = nullptr;  // toi, contact
+    // per outer iteration (two in flight): around the PD solve, the toi pass
+    // and the contact pass, and after the stopping test's copy to the host
+    enum { kEvP0, kEvP1, kEvC0, kEvC1, kEvQ0, kEvQ1, kEvGate, kEvPerOuter };
+    cudaEvent_t evo_[2][kEvPerOuter] = {};
+    OuterGate* gate_ = nullptr;  // the device's stopping test of the outer loop
     double ccd_ms_ = 0.0, contact_ms_ = 0.0;
     double device_ms_ = 0.0;
     double pd_ms_ = 0.0, pd_bytes_ = 0.0;
