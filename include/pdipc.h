@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PDIPC_ABI_VERSION 5
+#define PDIPC_ABI_VERSION 6
 
 typedef struct pdipc_ctx pdipc_ctx;
 
@@ -372,6 +372,31 @@ pdipc_status pdipc_stage_penalty_floor(pdipc_ctx* ctx, const double* x, double s
 pdipc_status pdipc_stage_penalty_dcd(pdipc_ctx* ctx, const double* x, const int* face_pairs, int64_t n_pairs,
                                      double stiffness, double self_stiffness, double damping, double* V,
                                      double* force, int* times);
+
+/* Discrete adjoint of a recorded rollout (no counterpart in the reference,
+ * whose simulator is not differentiable).  pdipc_adjoint_record(ctx, k) with
+ * k > 0 starts recording the following pdipc_step calls, keeping the state of
+ * the simulated vertices at the start of every k-th step; k = 0 drops the
+ * recording, and so do pdipc_set_state, pdipc_reset and pdipc_load.
+ * pdipc_adjoint_backward takes the gradient of a loss with respect to the
+ * simulated vertices' positions (dl_dx, 3*n_sim) and velocities (dl_dv, 3*n_sim,
+ * NULL = 0) after the last recorded step and returns the gradient with
+ * respect to their positions and velocities before the first recorded step
+ * (dl_dx0, dl_dv0, 3*n_sim), and, if dl_dstrain is not NULL, with respect to each
+ * simulated vertex's stretch stiffness (n_sim; the per-vertex strain weight
+ * that the model's k_stretch sets, PdIpcClothModel.h:177-328).  It is the exact
+ * derivative of the executed iteration: every local-global iteration, every
+ * weighted-Jacobi sweep and Chebyshev step, the prediction and the velocity
+ * update, for the outer-iteration counts the recorded steps ran (fix them with
+ * pdipc_params.fixed_outer for a smooth rollout).  It replays the recorded
+ * steps from the checkpoints (two replays per step) and leaves the context's
+ * state and stats as they were.  PDIPC_ERR_STATE unless the context is in the
+ * plain FP64 form (PDIPC_PREC_FP64) with cloth models only, steps were
+ * recorded, and every replayed outer iteration ran a full, contact-free step
+ * (time of impact 1, no active contact constraints). */
+pdipc_status pdipc_adjoint_record(pdipc_ctx* ctx, int checkpoint_every);
+pdipc_status pdipc_adjoint_backward(pdipc_ctx* ctx, const double* dl_dx, const double* dl_dv, double* dl_dx0,
+                                    double* dl_dv0, double* dl_dstrain);
 
 /* Topology precompute of one mesh, on the host (no device needed):
  * sorted unique edges (Model/TriangleMesh/BaseSurfaceMesh.cpp:219-275), the grid

@@ -438,6 +438,22 @@ pdipc_status pdipc_stage_penalty_dcd(pdipc_ctx* ctx, const double* x, const int*
     });
 }
 
+pdipc_status pdipc_adjoint_record(pdipc_ctx* ctx, int checkpoint_every) {
+    pdipc_status s = need_init(ctx);
+    if (s != PDIPC_OK) return s;
+    return guarded(ctx, [&]() { return ctx->solver->adjoint_record(checkpoint_every, ctx->err); });
+}
+
+pdipc_status pdipc_adjoint_backward(pdipc_ctx* ctx, const double* dl_dx, const double* dl_dv, double* dl_dx0,
+                                    double* dl_dv0, double* dl_dstrain) {
+    pdipc_status s = need_init(ctx);
+    if (s != PDIPC_OK) return s;
+    if (!dl_dx || !dl_dx0 || !dl_dv0) return fail(ctx, PDIPC_ERR_ARG, "null argument");
+    return guarded(ctx, [&]() {
+        return ctx->solver->adjoint_backward(dl_dx, dl_dv, dl_dx0, dl_dv0, dl_dstrain, ctx->err);
+    });
+}
+
 pdipc_status pdipc_mesh_topology(const double* X, int nv, const int* F, int nf, int patch_dim, int* edges,
                                  int cap_edges, int* n_edges, int* patch_off, int cap_patches, int* patch_faces,
                                  int cap_faces, int* n_patches, int* owner_of_point, int* owner_of_edge) {

@@ -162,9 +162,11 @@ enum ErrFlag : unsigned int {
 // That lets the host enqueue outer iteration k+1 before it has read
 // iteration k's residual.
 struct OuterGate {
-    unsigned stop;   // the stopping rule held at an earlier outer iteration
-    int iters;       // outer iterations run so far in this step
-    double resid;    // |dir|^2 of the last iteration run
+    unsigned stop;             // the stopping rule held at an earlier outer iteration
+    int iters;                 // outer iterations run so far in this step
+    double resid;              // |dir|^2 of the last iteration run
+    double toi;                // its clamped step fraction
+    unsigned long long active; // its active contact constraints
 };
 __device__ __forceinline__ bool outer_stopped(const OuterGate* g) { return g && g->stop; }
 

@@ -232,6 +232,28 @@ void launch_pen_dcd(const Dev<T, TC>& d, const int2* pairs, int64_t n, const int
 template <typename T, typename TC>
 void launch_pen_uniform(const Dev<T, TC>& d, V4<TC>* F, const int* times, TC damping, V4<TC>* V, cudaStream_t s);
 
+// ---------------- discrete adjoint of the contact-free step (adjoint_kernels.cu, FP64 only) ----------------
+// transposed LBO weights per stencil slot [lPtr[nsim]] and transposed matrix
+// values in the SELL layout of sVal
+template <typename T, typename TC>
+void launch_adj_tables(const Dev<T, TC>& d, T* lLboT, T* NTval, cudaStream_t s);
+// one sweep's adjoint at input z with output adjoint scale * in:
+// out (= or +=) J^T u, rho += u, kbar += dS/dk . u, other += (1 - scale) in
+template <typename T, typename TC>
+void launch_adj_sweep(const Dev<T, TC>& d, const T* NTval, T relax, T scale, const V4<T>* in, V4<T>* other,
+                      const V4<T>* z, V4<T>* out, bool accumulate, V4<T>* rho, T* kbar, cudaStream_t s);
+// the local step's adjoint at x from rho (sum of the sweeps' output adjoints):
+// rb, qb scratch; r0b += w D^-1 rho; xb += d(rhs)/dx^T rb; kbar += d(rhs)/dk . rb
+template <typename T, typename TC>
+void launch_adj_local(const Dev<T, TC>& d, const T* lLboT, T relax, const V4<T>* x, const V4<T>* rho, V4<T>* rb,
+                      V4<T>* qb, V4<T>* r0b, V4<T>* xb, T* kbar, cudaStream_t s);
+// step output adjoints -> adjoint of the solved positions (pb) and of X0 (vb); r0b = 0
+template <typename T, typename TC>
+void launch_adj_step_begin(const Dev<T, TC>& d, T invt, V4<T>* pb, V4<T>* vb, V4<T>* r0b, cudaStream_t s);
+// through the prediction: pb, vb := adjoints of the step's input positions and velocities
+template <typename T, typename TC>
+void launch_adj_step_end(const Dev<T, TC>& d, T dt, V4<T>* pb, V4<T>* vb, const V4<T>* r0b, cudaStream_t s);
+
 // Scratch of the no-allocation per-candidate toi pass: a file-scope device array
 // of kToiScratchEntries doubles (8 MiB), its address looked up once per device on
 // first use.  One array per device is shared by every context of the process:

@@ -526,12 +526,15 @@ __global__ void k_copy_old(int nsim, const V4<S>* __restrict__ P, V4<S>* __restr
 
 // one thread: the stopping rule of the outer loop (PdIpcSimulator::advance,
 // cpp:1683-1796: stop once |dir|^2 < tol after the first iteration)
-__global__ void k_outer_gate(OuterGate* __restrict__ g, const double* __restrict__ resid, int outer, double tol,
-                             int test) {
+template <typename TC>
+__global__ void k_outer_gate(OuterGate* __restrict__ g, const double* __restrict__ resid, const TC* __restrict__ toi,
+                             const unsigned long long* __restrict__ active, int outer, double tol, int test) {
     if (g->stop) return;
     const double r = *resid;
     g->resid = r;
     g->iters = outer + 1;
+    g->toi = (double)*toi;
+    g->active = *active;
     if (test && outer > 0 && r < tol) g->stop = 1u;
 }
 
@@ -648,7 +651,7 @@ void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s) {
 }
 template <typename T, typename TC>
 void launch_outer_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cudaStream_t s) {
-    k_outer_gate<<<1, 1, 0, s>>>(d.Gate, d.Resid, outer, tol, test ? 1 : 0);
+    k_outer_gate<TC><<<1, 1, 0, s>>>(d.Gate, d.Resid, d.Toi, d.ActiveCount, outer, tol, test ? 1 : 0);
 }
 template <typename T, typename TC>
 void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {

@@ -304,6 +304,10 @@ public:
         st_.max_outer_iters = 0;
         st_.total_outer_iters = 0;
         for (int k = 0; k < n; ++k) {
+            if (adj_every_ > 0) {
+                pdipc_status r = adjoint_checkpoint(err);
+                if (r != PDIPC_OK) return r;
+            }
             PD_CK(cudaEventRecord(ev0_, s_));
             pdipc_status r = step_once(err);
             if (r != PDIPC_OK) return r;
@@ -345,6 +349,7 @@ public:
         return PDIPC_OK;
     }
     pdipc_status set_state(const double* X, const double* V, std::string& err) override {
+        adjoint_clear();  // the recorded trajectory no longer leads here
         pdipc_status r = upload_vec(d_.P, X, d_.ntot, err);
         if (r != PDIPC_OK) return r;
         launch_split(d_, d_.P, d_.Ph, d_.Pl, d_.ntot, s_);
@@ -352,6 +357,7 @@ public:
         return PDIPC_OK;
     }
     pdipc_status reset(std::string& err) override {
+        adjoint_clear();
         PD_CK(cudaMemcpyAsync(d_.P, d_.Xrest, sizeof(V4<TC>) * d_.ntot, cudaMemcpyDeviceToDevice, s_));
         launch_split(d_, d_.P, d_.Ph, d_.Pl, d_.ntot, s_);
         PD_CK(cudaMemsetAsync(d_.Vel, 0, sizeof(V4<TC>) * d_.nsim, s_));
@@ -610,6 +616,267 @@ public:
 private:
     Pos<T, TC> pos() const { return Pos<T, TC>{d_.P, d_.Ph, d_.Pl}; }
     Pos<T, TC> pos_old() const { return Pos<T, TC>{d_.Pold, d_.Poh, d_.Pol}; }
+
+    // ---------------- discrete adjoint (FP64 form, contact-free steps) ----------------
+    // Recording keeps the state (positions and velocities of the simulated
+    // vertices) at the start of every `every`-th step.  The backward pass walks
+    // the checkpoint segments from the last: it replays a segment's steps to
+    // regain each step's start state, then for each step from the last replays
+    // it once more with the positions at the start of every local-global
+    // iteration taped, and runs the step's adjoint (adjoint_kernels.cu) over
+    // the tape, last iteration first.  A replayed outer iteration with a
+    // clamped step or active contacts ends the pass with PDIPC_ERR_STATE: the
+    // adjoint covers contact-free steps.
+    static constexpr bool kAdjoint = std::is_same<T, double>::value && std::is_same<TC, double>::value;
+
+    void adjoint_clear() {
+        for (V4<TC>*& c : adj_ckpt_) dfree(c);
+        adj_ckpt_.clear();
+        adj_every_ = 0;
+        adj_steps_ = 0;
+    }
+
+    pdipc_status adjoint_checkpoint(std::string& err) {
+        if (adj_steps_ % adj_every_ == 0) {
+            V4<TC>* c = nullptr;
+            PD_CK(alloc(c, 2 * (size_t)d_.nsim));
+            adj_ckpt_.push_back(c);
+            PD_CK(cudaMemcpyAsync(c, d_.P, sizeof(V4<TC>) * d_.nsim, cudaMemcpyDeviceToDevice, s_));
+            PD_CK(cudaMemcpyAsync(c + d_.nsim, d_.Vel, sizeof(V4<TC>) * d_.nsim, cudaMemcpyDeviceToDevice, s_));
+        }
+        ++adj_steps_;
+        return PDIPC_OK;
+    }
+
+    pdipc_status adjoint_record(int every, std::string& err) override {
+        if (every < 0) {
+            err = "adjoint_record: negative checkpoint interval";
+            return PDIPC_ERR_ARG;
+        }
+        adjoint_clear();
+        if (every == 0) return PDIPC_OK;
+        if (!kAdjoint) {
+            err = "adjoint: the plain FP64 form only (precision PDIPC_PREC_FP64)";
+            return PDIPC_ERR_STATE;
+        }
+        if (d_.ntet > 0) {
+            err = "adjoint: cloth models only (the scene has tets)";
+            return PDIPC_ERR_STATE;
+        }
+        adj_every_ = every;
+        return PDIPC_OK;
+    }
+
+    // copy a saved state (P then Vel, nsim each) into the context, or out of it
+    pdipc_status adj_load(const V4<TC>* st, std::string& err) {
+        PD_CK(cudaMemcpyAsync(d_.P, st, sizeof(V4<TC>) * d_.nsim, cudaMemcpyDeviceToDevice, s_));
+        PD_CK(cudaMemcpyAsync(d_.Vel, st + d_.nsim, sizeof(V4<TC>) * d_.nsim, cudaMemcpyDeviceToDevice, s_));
+        return PDIPC_OK;
+    }
+    pdipc_status adj_save(V4<TC>* st, std::string& err) {
+        PD_CK(cudaMemcpyAsync(st, d_.P, sizeof(V4<TC>) * d_.nsim, cudaMemcpyDeviceToDevice, s_));
+        PD_CK(cudaMemcpyAsync(st + d_.nsim, d_.Vel, sizeof(V4<TC>) * d_.nsim, cudaMemcpyDeviceToDevice, s_));
+        return PDIPC_OK;
+    }
+
+    pdipc_status adj_buffers(std::string& err) {
+        const int ns = d_.nsim, cb = c_.cheby;
+        const int max_outer = prm_.fixed_outer > 0 ? prm_.fixed_outer : prm_.max_outer;
+        const int tape = max_outer * c_.lg;
+        if (adj_tape_cap_ < tape) {
+            dfree(adj_tape_);
+            PD_CK(alloc(adj_tape_, (size_t)tape * ns));
+            adj_tape_cap_ = tape;
+        }
+        if ((int)adj_seg_.size() < adj_every_) {
+            for (V4<TC>*& c : adj_seg_) dfree(c);
+            adj_seg_.assign(adj_every_, nullptr);
+            for (V4<TC>*& c : adj_seg_) PD_CK(alloc(c, 2 * (size_t)ns));
+        }
+        if (adj_ready_) return PDIPC_OK;
+        int nslot = 0;
+        PD_CK(cudaMemcpyAsync(&nslot, d_.lPtr + ns, sizeof(int), cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        PD_CK(alloc(adj_lboT_, (size_t)nslot));
+        PD_CK(alloc(adj_ntval_, (size_t)sell_padded_));
+        PD_CK(alloc(adj_final_, 2 * (size_t)ns));
+        PD_CK(alloc(adj_kb_, (size_t)ns));
+        for (V4<TC>** b : {&adj_pb_, &adj_vb_, &adj_r0b_, &adj_rb_, &adj_qb_, &adj_u_, &adj_rho_})
+            PD_CK(alloc(*b, (size_t)ns));
+        adj_xb_.assign(cb + 1, nullptr);
+        adj_xs_.assign(cb + 1, nullptr);
+        adj_ys_.assign(cb, nullptr);
+        for (auto* v : {&adj_xb_, &adj_xs_, &adj_ys_})
+            for (V4<TC>*& b : *v) PD_CK(alloc(b, (size_t)ns));
+        if constexpr (kAdjoint) launch_adj_tables(d_, adj_lboT_, adj_ntval_, s_);
+        PD_CK(cudaGetLastError());
+        adj_ready_ = true;
+        return PDIPC_OK;
+    }
+
+    // the adjoint of one step over its tape; adj_pb_/adj_vb_ hold the adjoints
+    // of the step's output positions and velocities on entry and of its input
+    // positions and velocities on return
+    pdipc_status adjoint_step(std::string& err) {
+        if constexpr (kAdjoint) {
+            Dev<T, TC>& d = d_;
+            const int ns = d.nsim, cb = c_.cheby;
+            const T w = (T)c_.relax;
+            const TC dt = (TC)c_.dt;
+            const TC invt = (TC)((1.0 / (double)dt) * (double)(TC)(1.0 - (double)dt));  // as step_once
+            std::vector<T> oms;
+            {
+                T rho2 = (T)c_.rho;
+                rho2 = rho2 * rho2;
+                T om = omega_first(rho2);
+                for (int it = 1; it < cb; ++it) {
+                    oms.push_back(om);
+                    om = omega_next(rho2, om);
+                }
+            }
+            launch_adj_step_begin(d, invt, adj_pb_, adj_vb_, adj_r0b_, s_);
+            const size_t vb = sizeof(V4<TC>) * ns;
+            for (int l = adj_tape_n_ - 1; l >= 0; --l) {
+                V4<T>* x = adj_tape_ + (size_t)l * ns;
+                // the iteration's forward iterates: X_0 = x, Y_t = S(X_t), X_{t+1} from Y_t
+                PD_CK(cudaMemcpyAsync(d.P, x, vb, cudaMemcpyDeviceToDevice, s_));
+                launch_local_aq(d, s_);
+                launch_local_rhs_sweep(d, w, s_);
+                PD_CK(cudaMemcpyAsync(adj_ys_[0], d.Y, vb, cudaMemcpyDeviceToDevice, s_));
+                PD_CK(cudaMemcpyAsync(adj_xs_[0], x, vb, cudaMemcpyDeviceToDevice, s_));
+                if (cb > 1) launch_sweep<T, TC>(d, adj_ys_[0], nullptr, adj_xs_[1], w, T(0), s_);
+                for (int it = 1; it < cb; ++it) {
+                    launch_sweep<T, TC>(d, adj_xs_[it], nullptr, adj_ys_[it], w, T(0), s_);
+                    if (it + 1 < cb)
+                        launch_sweep<T, TC>(d, adj_ys_[it], adj_xs_[it - 1], adj_xs_[it + 1], w, oms[it - 1], s_);
+                }
+                // reverse: Xb[cb] is the adjoint of the iteration's result
+                for (int t = 0; t < cb; ++t) PD_CK(cudaMemsetAsync(adj_xb_[t], 0, vb, s_));
+                PD_CK(cudaMemsetAsync(adj_rho_, 0, vb, s_));
+                std::swap(adj_xb_[cb], adj_pb_);
+                for (int it = cb - 1; it >= 1; --it) {
+                    launch_adj_sweep(d, adj_ntval_, w, oms[it - 1], adj_xb_[it + 1], adj_xb_[it - 1], adj_ys_[it],
+                                     adj_u_, false, adj_rho_, adj_kb_, s_);
+                    launch_adj_sweep(d, adj_ntval_, w, T(1), adj_u_, (V4<T>*)nullptr, adj_xs_[it], adj_xb_[it], true,
+                                     adj_rho_, adj_kb_, s_);
+                }
+                launch_adj_sweep(d, adj_ntval_, w, T(1), adj_xb_[1], (V4<T>*)nullptr, adj_ys_[0], adj_u_, false,
+                                 adj_rho_, adj_kb_, s_);
+                launch_adj_sweep(d, adj_ntval_, w, T(1), adj_u_, (V4<T>*)nullptr, adj_xs_[0], adj_xb_[0], true,
+                                 adj_rho_, adj_kb_, s_);
+                launch_adj_local(d, adj_lboT_, w, x, adj_rho_, adj_rb_, adj_qb_, adj_r0b_, adj_xb_[0], adj_kb_, s_);
+                std::swap(adj_xb_[0], adj_pb_);  // the adjoint of the previous iteration's result
+            }
+            launch_adj_step_end(d, (T)dt, adj_pb_, adj_vb_, adj_r0b_, s_);
+            PD_CK(cudaGetLastError());
+            return PDIPC_OK;
+        } else {
+            err = "adjoint: the plain FP64 form only";
+            return PDIPC_ERR_STATE;
+        }
+    }
+
+    pdipc_status adjoint_backward(const double* gx, const double* gv, double* gx0, double* gv0, double* gk,
+                                  std::string& err) override {
+        if (!kAdjoint) {
+            err = "adjoint: the plain FP64 form only (precision PDIPC_PREC_FP64)";
+            return PDIPC_ERR_STATE;
+        }
+        if (adj_every_ <= 0 || adj_steps_ == 0) {
+            err = "adjoint_backward: no recorded steps (pdipc_adjoint_record, then pdipc_step)";
+            return PDIPC_ERR_STATE;
+        }
+        if (!gx || !gx0 || !gv0) {
+            err = "adjoint_backward: null gradient buffer";
+            return PDIPC_ERR_ARG;
+        }
+        pdipc_status r = adj_buffers(err);
+        if (r != PDIPC_OK) return r;
+        const int ns = d_.nsim;
+        const pdipc_stats st_saved = st_;
+        const int64_t launches_saved = launches_;
+        const double ms_saved = device_ms_, pd_saved = pd_ms_, ccd_saved = ccd_ms_, contact_saved = contact_ms_;
+        const int64_t solves_saved = pd_solves_;
+        r = adj_save(adj_final_, err);
+        if (r != PDIPC_OK) return r;
+        r = upload_vec(adj_pb_, gx, ns, err);
+        if (r != PDIPC_OK) return r;
+        if (gv) {
+            r = upload_vec(adj_vb_, gv, ns, err);
+            if (r != PDIPC_OK) return r;
+        } else {
+            PD_CK(cudaMemsetAsync(adj_vb_, 0, sizeof(V4<TC>) * ns, s_));
+        }
+        PD_CK(cudaMemsetAsync(adj_kb_, 0, sizeof(T) * ns, s_));
+        const int nseg = (adj_steps_ + adj_every_ - 1) / adj_every_;
+        for (int c = nseg - 1; c >= 0 && r == PDIPC_OK; --c) {
+            const int s0 = c * adj_every_, s1 = std::min(s0 + adj_every_, adj_steps_);
+            // start states of the segment's steps
+            r = adj_load(adj_ckpt_[c], err);
+            if (r == PDIPC_OK) r = adj_save(adj_seg_[0], err);
+            for (int s = s0 + 1; s < s1 && r == PDIPC_OK; ++s) {
+                r = step_once(err);
+                if (r == PDIPC_OK) r = adj_save(adj_seg_[s - s0], err);
+            }
+            for (int s = s1 - 1; s >= s0 && r == PDIPC_OK; --s) {
+                r = adj_load(adj_seg_[s - s0], err);
+                if (r != PDIPC_OK) break;
+                taping_ = true;
+                adj_tape_n_ = 0;
+                adj_contact_ = false;
+                r = step_once(err);
+                taping_ = false;
+                if (r != PDIPC_OK) break;
+                if (adj_contact_) {
+                    err = "adjoint_backward: recorded step " + std::to_string(s) +
+                          " has an outer iteration with a clamped step or active contacts; the adjoint covers "
+                          "contact-free steps";
+                    r = PDIPC_ERR_STATE;
+                    break;
+                }
+                if (adj_tape_n_ > adj_tape_cap_) {
+                    err = "adjoint_backward: local-global tape overflow";
+                    r = PDIPC_ERR_STATE;
+                    break;
+                }
+                r = adjoint_step(err);
+            }
+        }
+        taping_ = false;
+        std::string e2;
+        const pdipc_status rl = adj_load(adj_final_, e2);
+        st_ = st_saved;
+        launches_ = launches_saved;
+        device_ms_ = ms_saved;
+        pd_ms_ = pd_saved;
+        ccd_ms_ = ccd_saved;
+        contact_ms_ = contact_saved;
+        pd_solves_ = solves_saved;
+        if (r != PDIPC_OK) return r;
+        if (rl != PDIPC_OK) {
+            err = e2;
+            return rl;
+        }
+        PD_CK(cudaMemcpyAsync(stage_, adj_pb_, sizeof(V4<TC>) * ns, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        for (int i = 0; i < ns; ++i) {
+            gx0[3 * (size_t)i] = (double)stage_[i].x;
+            gx0[3 * (size_t)i + 1] = (double)stage_[i].y;
+            gx0[3 * (size_t)i + 2] = (double)stage_[i].z;
+        }
+        PD_CK(cudaMemcpyAsync(stage_, adj_vb_, sizeof(V4<TC>) * ns, cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        for (int i = 0; i < ns; ++i) {
+            gv0[3 * (size_t)i] = (double)stage_[i].x;
+            gv0[3 * (size_t)i + 1] = (double)stage_[i].y;
+            gv0[3 * (size_t)i + 2] = (double)stage_[i].z;
+        }
+        if (gk) {
+            PD_CK(cudaMemcpyAsync(gk, adj_kb_, sizeof(T) * ns, cudaMemcpyDeviceToHost, s_));
+            PD_CK(cudaStreamSynchronize(s_));
+        }
+        return PDIPC_OK;
+    }
 
     // ---------------- allocation helpers ----------------
     // Initialisation and uploads are ordered on the context's stream (created
@@ -1144,6 +1411,12 @@ private:
         launch_diag(d, s_);
         ++k;
         for (int lg = 0; lg < c_.lg; ++lg) {
+            if (taping_) {  // positions at the start of every local-global iteration
+                if (adj_tape_n_ < adj_tape_cap_)
+                    cudaMemcpyAsync(adj_tape_ + (size_t)adj_tape_n_ * d.nsim, d.P, sizeof(V4<TC>) * d.nsim,
+                                    cudaMemcpyDeviceToDevice, s_);
+                ++adj_tape_n_;
+            }
             launch_local_aq(d, s_);
             launch_tet_project(d, s_);
             k += d.ntet > 0;
@@ -1171,7 +1444,7 @@ private:
             ++launches_;
             return PDIPC_OK;
         }
-        if (!prm_.use_graphs) {
+        if (!prm_.use_graphs || taping_) {
             launches_ += enqueue_pd();
             return PDIPC_OK;
         }
@@ -1268,6 +1541,7 @@ private:
                 return PDIPC_ERR_STATE;
             }
             st_.last_residual = g.resid;
+            if (taping_ && (g.toi != 1.0 || g.active != 0)) adj_contact_ = true;
             outer = k + 1;
             if (g.stop) break;
             if (enq < max_outer) {
@@ -1349,6 +1623,19 @@ private:
     char* scan_tmp_ = nullptr;
     int64_t scan_tmp_cap_ = 0;
     Pinned* pin_ = nullptr;
+    // discrete adjoint: checkpoints, tape and work vectors (FP64 form)
+    int adj_every_ = 0, adj_steps_ = 0;
+    std::vector<V4<TC>*> adj_ckpt_, adj_seg_;
+    V4<TC>* adj_tape_ = nullptr;
+    int adj_tape_cap_ = 0, adj_tape_n_ = 0;
+    bool taping_ = false, adj_contact_ = false, adj_ready_ = false;
+    T* adj_lboT_ = nullptr;
+    T* adj_ntval_ = nullptr;
+    T* adj_kb_ = nullptr;
+    V4<TC>* adj_final_ = nullptr;
+    V4<TC>*adj_pb_ = nullptr, *adj_vb_ = nullptr, *adj_r0b_ = nullptr, *adj_rb_ = nullptr, *adj_qb_ = nullptr,
+           *adj_u_ = nullptr, *adj_rho_ = nullptr;
+    std::vector<V4<TC>*> adj_xb_, adj_xs_, adj_ys_;
     PersistPlan plan_;
     std::vector<int> sliceOffH_, sliceLenH_;
     PersistArgs<float, TC> pargs_{};

@@ -37,6 +37,11 @@ public:
     virtual pdipc_status stage_penalty(int kind, const double* x, const double* dir, const int* face_pairs,
                                        int64_t n_pairs, double k, double k_self, double damping, double* V,
                                        double* force, int* times, std::string& err) = 0;
+    // discrete adjoint of recorded contact-free steps (FP64 form): every > 0
+    // starts recording with a checkpoint every `every` steps, 0 drops it
+    virtual pdipc_status adjoint_record(int every, std::string& err) = 0;
+    virtual pdipc_status adjoint_backward(const double* gx, const double* gv, double* gx0, double* gv0, double* gk,
+                                          std::string& err) = 0;
     virtual int n_sim() const = 0;
     virtual int n_total() const = 0;
 };

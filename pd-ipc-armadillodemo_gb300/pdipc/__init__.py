@@ -36,11 +36,11 @@ EXPORTS = [
     "pdipc_stage_sweep_timing", "pdipc_stage_toi_noalloc", "pdipc_add_volumetric", "pdipc_tet_surface",
     "pdipc_scene_load", "pdipc_scene_model_count", "pdipc_scene_get_model", "pdipc_scene_apply_params",
     "pdipc_scene_add_models", "pdipc_scene_free", "pdipc_stage_penalty_predict", "pdipc_stage_penalty_ccd",
-    "pdipc_stage_penalty_floor", "pdipc_stage_penalty_dcd",
+    "pdipc_stage_penalty_floor", "pdipc_stage_penalty_dcd", "pdipc_adjoint_record", "pdipc_adjoint_backward",
 ]
 
 
-ABI_VERSION = 5  # PDIPC_ABI_VERSION of include/pdipc.h
+ABI_VERSION = 6  # PDIPC_ABI_VERSION of include/pdipc.h
 
 
 class PdipcError(RuntimeError):
@@ -106,6 +106,8 @@ def load_library(path: str | None = None):
     L.pdipc_stage_penalty_dcd.argtypes = [vp, _dp, _ip, C.c_int64, C.c_double, C.c_double, C.c_double, _dp, _dp,
                                           _ip]
     L.pdipc_stage_toi_noalloc.argtypes = [vp, _dp, _dp, _dp, _dp, _dp]
+    L.pdipc_adjoint_record.argtypes = [vp, C.c_int]
+    L.pdipc_adjoint_backward.argtypes = [vp, _dp, _dp, _dp, _dp, _dp]
     L.pdipc_stage_contact.argtypes = [vp, _dp, _dp, _dp, _i64p]
     L.pdipc_stage_pd.argtypes = [vp, _dp, _dp, _dp]
     L.pdipc_stage_sweep_timing.argtypes = [vp, C.c_int, _dp, _dp]
@@ -326,6 +328,25 @@ class Simulator:
                                                            fp.shape[0], stiffness, self_stiffness, damping,
                                                            _d(V), _d(F), _i(t)), "pdipc_stage_penalty_dcd")
         return F, t, V
+
+    def adjoint_record(self, checkpoint_every=1):
+        """Record the following steps for adjoint_backward, keeping a checkpoint
+        every `checkpoint_every` steps (0 drops the recording)."""
+        self._check(load_library().pdipc_adjoint_record(self.h, int(checkpoint_every)), "pdipc_adjoint_record")
+
+    def adjoint_backward(self, dl_dx, dl_dv=None):
+        """Gradients through the recorded steps: given dL/d(positions) and
+        dL/d(velocities) of the simulated vertices after the last recorded step,
+        return dL/d(positions), dL/d(velocities) before the first one and
+        dL/d(stretch stiffness) per simulated vertex."""
+        gx = self._vec(dl_dx, self.n_sim, "dl_dx")
+        gv = None if dl_dv is None else self._vec(dl_dv, self.n_sim, "dl_dv")
+        gx0 = np.empty((self.n_sim, 3), np.float64)
+        gv0 = np.empty((self.n_sim, 3), np.float64)
+        gk = np.empty(self.n_sim, np.float64)
+        self._check(load_library().pdipc_adjoint_backward(self.h, _d(gx), _d(gv) if gv is not None else None,
+                                                          _d(gx0), _d(gv0), _d(gk)), "pdipc_adjoint_backward")
+        return gx0, gv0, gk
 
     def stage_toi_noalloc(self, x0, x1, npt, nee, per_candidate=True):
         """stage_toi through the no-allocation entry point (FP64 and mixed modes)."""

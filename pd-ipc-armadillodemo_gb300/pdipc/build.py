@@ -20,7 +20,7 @@ OUT = os.path.join(PKG, "libpdipc.so")
 OBJ = os.path.join(PKG, "_build")
 
 SOURCES = ["pd_kernels.cu", "pd_persistent.cu", "collision_kernels.cu", "penalty_kernels.cu", "primitives.cu",
-           "solver.cu",
+           "adjoint_kernels.cu", "solver.cu",
            "host_tables.cpp", "capi.cpp", "scene_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code must not fuse multiply-adds: the patch grid is computed in FP32 exactly as

@@ -1,0 +1,253 @@
+"""The discrete adjoint of the contact-free projective-dynamics step, restated
+in numpy on random tables and checked against central differences on the CPU.
+
+The forward restates the plain FP64 form of pd_kernels.cu on a 4x4 grid with
+random stencil weights (LBO weights, bending coefficients and their
+transposes, rest lengths, per-vertex strain weights, a symmetric bending
+part of the matrix plus the strain weights on the spring neighbours, two
+pinned vertices): prediction, local steps (spring projections, rescaled
+curvature vectors, bending terms), the two-sweep Chebyshev-Jacobi global step,
+and the velocity update.  The adjoint follows the same recurrences as
+adjoint_kernels.cu and the reverse pass of solver.cu (adjoint_step): transposed
+sweeps, the right-hand side's adjoint w D^-1 sum(u), the local step's gathers,
+and the per-vertex stretch-stiffness terms of the rhs, N and D.  It pins the
+method; the kernels are checked against differences of the GPU forward by
+test_adjoint_gpu.py."""
+import numpy as np
+
+rng = np.random.default_rng(1)  # the random tables
+G = 4
+n = G * G
+def vid(r, c): return r * G + c
+nbrs = []
+for r in range(G):
+    for c in range(G):
+        s = []
+        for dr in (-1, 0, 1):
+            for dc in (-1, 0, 1):
+                if (dr or dc) and 0 <= r + dr < G and 0 <= c + dc < G:
+                    s.append(vid(r + dr, c + dc))
+        nbrs.append(sorted(s))
+lPtr = [0]
+lNbr = []
+for i in range(n):
+    lNbr += [i] + nbrs[i]
+    lPtr.append(len(lNbr))
+lPtr = np.array(lPtr); lNbr = np.array(lNbr)
+ns = len(lNbr)
+rev = np.zeros(ns, int)
+for i in range(n):
+    for s in range(lPtr[i], lPtr[i + 1]):
+        j = lNbr[s]
+        rev[s] = next(t for t in range(lPtr[j], lPtr[j + 1]) if lNbr[t] == i)
+X = np.array([[vid(r, c) % G * 0.1, 0.0, vid(r, c) // G * 0.1] for r in range(G) for c in range(G)]) + rng.uniform(-0.01, 0.01, (n, 3))
+lRest = np.zeros(ns)
+for i in range(n):
+    for s in range(lPtr[i] + 1, lPtr[i + 1]):
+        lRest[s] = np.linalg.norm(X[i] - X[lNbr[s]]) * (1 + 0.05 * ((i + lNbr[s]) % 3))
+lLbo = rng.uniform(-1, 1, ns)
+lBend = rng.uniform(-0.1, 0.1, ns) * 1e-2
+lBendT = lBend[rev]
+strain = rng.uniform(50, 150, n)
+curv = rng.uniform(0.5, 2.0, n)
+invm = rng.uniform(50, 100, n)
+grav = np.tile([0.0, -9.8, 0.0], (n, 1)) / invm[:, None]
+pinned = np.zeros(n, bool); pinned[[0, G - 1]] = True
+pinK = 1e3
+pinRhs = np.where(pinned[:, None], pinK * X, 0.0)
+Bsym = np.zeros((n, n))
+for i in range(n):
+    for j in nbrs[i]:
+        if j > i:
+            Bsym[i, j] = Bsym[j, i] = rng.uniform(-0.2, 0.2)
+dt = 1 / 240.0
+w, rho = 2 / 3, 0.9992
+LG, CHEBY, K = 3, 4, 2
+
+def tables(k):
+    N = Bsym.copy()
+    De = np.zeros(n)
+    for i in range(n):
+        for j in nbrs[i]:
+            N[i, j] += k[i]
+        De[i] = len(nbrs[i]) * k[i] + 3.0 + (pinK if pinned[i] else 0.0)
+    return N, De
+
+def omegas():
+    r2 = rho * rho
+    om = 2 / (2 - r2)
+    out = []
+    for it in range(1, CHEBY):
+        out.append(om)
+        om = 4 / (4 - r2 * om)
+    return out
+
+def local(x, k, Rhs0):
+    q = np.zeros((n, 3))
+    for i in range(n):
+        for s in range(lPtr[i], lPtr[i + 1]):
+            q[i] += lLbo[s] * x[lNbr[s]]
+    a = q.copy()
+    for i in range(n):
+        nr = np.linalg.norm(q[i])
+        if nr >= 1e-10: a[i] = q[i] * (curv[i] / nr)
+    r = np.zeros((n, 3))
+    for i in range(n):
+        t = np.zeros(3)
+        for s in range(lPtr[i] + 1, lPtr[i + 1]):
+            d = x[i] - x[lNbr[s]]
+            t += k[i] * (lRest[s] / np.linalg.norm(d)) * d
+        t += lBend[lPtr[i]] * a[i]
+        ri = Rhs0[i] + t
+        for s in range(lPtr[i] + 1, lPtr[i + 1]):
+            ri = ri + lBendT[s] * a[lNbr[s]]
+        r[i] = ri + pinRhs[i]
+    return r, q
+
+def sweep(z, r, N, invD):
+    return (1 - w) * z + w * (invD[:, None] * (N @ z + r))
+
+def lg_forward(x, k, Rhs0, N, invD, tape=False):
+    r, q = local(x, k, Rhs0)
+    Xs = [x]
+    Ys = []
+    Y = sweep(x, r, N, invD); Ys.append(Y)
+    Xs.append(sweep(Y, r, N, invD))
+    for it, om in enumerate(omegas(), start=1):
+        Y = sweep(Xs[it], r, N, invD); Ys.append(Y)
+        Xs.append(om * (sweep(Y, r, N, invD) - Xs[it - 1]) + Xs[it - 1])
+    return (Xs[-1], Xs, Ys, r) if tape else Xs[-1]
+
+def step(x, v, k):
+    N, De = tables(k)
+    im = invm
+    m = im * dt
+    Di = np.where(pinned, 0.0, 1 / (im * dt * dt))
+    invD = 1 / (De + Di)
+    y = (v + m[:, None] * grav) * dt + x
+    Rhs0 = np.where(pinned[:, None], 0.0, (1 / (dt * m))[:, None] * y)
+    P = np.where(pinned[:, None], x, y)
+    for o in range(K):
+        for l in range(LG):
+            P = lg_forward(P, k, Rhs0, N, invD)
+    invt = (1 / dt) * (1 - dt)
+    V = (P - x) * invt
+    return P, V
+
+def step_adj(x, v, k, Pb_T, Vb_T):
+    N, De = tables(k)
+    im = invm; m = im * dt
+    Di = np.where(pinned, 0.0, 1 / (im * dt * dt))
+    invD = 1 / (De + Di)
+    deg = np.array([len(nbrs[i]) for i in range(n)])
+    y = (v + m[:, None] * grav) * dt + x
+    Rhs0 = np.where(pinned[:, None], 0.0, (1 / (dt * m))[:, None] * y)
+    P = np.where(pinned[:, None], x, y)
+    tapeX = []
+    for o in range(K):
+        for l in range(LG):
+            tapeX.append(P)
+            P = lg_forward(P, k, Rhs0, N, invD)
+    invt = (1 / dt) * (1 - dt)
+    Pb = Pb_T + invt * Vb_T
+    X0b = -invt * Vb_T
+    r0b = np.zeros((n, 3))
+    kb = np.zeros(n)
+    NT = N.T
+    oms = omegas()
+    def stiff(ub, z, r):
+        nz = N @ z + r
+        sz = np.array([z[nbrs[i]].sum(0) for i in range(n)])
+        return w * invD * np.sum(ub * (sz - (deg * invD)[:, None] * nz), axis=1)
+    def JT(ub):
+        return (1 - w) * ub + NT @ (w * invD[:, None] * ub)
+    for xl in reversed(tapeX):
+        _, Xs, Ys, r = lg_forward(xl, k, Rhs0, N, invD, tape=True)
+        Xb = [np.zeros((n, 3)) for _ in range(CHEBY + 1)]
+        Xb[CHEBY] = Pb.copy()
+        rhob = np.zeros((n, 3))
+        for it in range(CHEBY - 1, 0, -1):
+            om = oms[it - 1]
+            u2 = om * Xb[it + 1]
+            Xb[it - 1] += (1 - om) * Xb[it + 1]
+            rhob += u2; kb += stiff(u2, Ys[it], r)
+            u1 = JT(u2)
+            rhob += u1; kb += stiff(u1, Xs[it], r)
+            Xb[it] += JT(u1)
+        u2 = Xb[1]
+        rhob += u2; kb += stiff(u2, Ys[0], r)
+        u1 = JT(u2)
+        rhob += u1; kb += stiff(u1, Xs[0], r)
+        Xb[0] += JT(u1)
+        rb = w * invD[:, None] * rhob
+        r0b += rb
+        # local step adjoint at xl
+        q = np.zeros((n, 3))
+        for i in range(n):
+            for s in range(lPtr[i], lPtr[i + 1]):
+                q[i] += lLbo[s] * xl[lNbr[s]]
+        ab = np.zeros((n, 3))
+        for kk in range(n):
+            for s in range(lPtr[kk], lPtr[kk + 1]):
+                ab[kk] += lBend[s] * rb[lNbr[s]]
+        qb = ab.copy()
+        for i in range(n):
+            nr = np.linalg.norm(q[i])
+            if nr >= 1e-10:
+                qh = q[i] / nr
+                qb[i] = (curv[i] / nr) * (ab[i] - qh * (qh @ ab[i]))
+        xb = Xb[0].copy()
+        for mm in range(n):
+            for s in range(lPtr[mm], lPtr[mm + 1]):
+                xb[mm] += lLbo[rev[s]] * qb[lNbr[s]]
+            for s in range(lPtr[mm] + 1, lPtr[mm + 1]):
+                j = lNbr[s]
+                d = xl[mm] - xl[j]
+                L = np.linalg.norm(d); dh = d / L
+                u = k[mm] * lRest[s] * rb[mm] - k[j] * lRest[s] * rb[j]
+                xb[mm] += (u - dh * (dh @ u)) / L
+                kb[mm] += lRest[s] * (rb[mm] @ dh)
+        Pb = xb
+    mm_ = 1 / (dt * m)
+    yb = np.where(pinned[:, None], 0.0, Pb + mm_[:, None] * r0b)
+    xb0 = X0b + np.where(pinned[:, None], Pb, yb)
+    vb0 = dt * yb
+    return xb0, vb0, kb
+
+def rollout(x, v, k, T):
+    for _ in range(T):
+        x, v = step(x, v, k)
+    return x, v
+
+
+def test_adjoint_recurrences_match_central_differences():
+    T = 3
+    x0 = X.copy()
+    v0 = rng.uniform(-0.1, 0.1, (n, 3))
+    v0[pinned] = 0
+    k0 = strain.copy()
+    cx, cv = rng.normal(size=(n, 3)), rng.normal(size=(n, 3))
+
+    def loss(x, v, k):
+        P, V = rollout(x, v, k, T)
+        return np.sum(cx * P) + np.sum(cv * V) + 0.5 * np.sum(P * P)
+
+    states = [(x0, v0)]
+    x, v = x0, v0
+    for _ in range(T):
+        x, v = step(x, v, k0)
+        states.append((x, v))
+    Pb, Vb = cx + states[-1][0], cv.copy()
+    kb = np.zeros(n)
+    for t in range(T - 1, -1, -1):
+        Pb, Vb, kbt = step_adj(*states[t], k0, Pb, Vb)
+        kb += kbt
+    eps = 1e-6
+    cases = (("v", Vb, lambda d, e: (x0, v0 + e * d, k0)), ("x", Pb, lambda d, e: (x0 + e * d, v0, k0)),
+             ("k", kb, lambda d, e: (x0, v0, k0 + e * d)))
+    for name, g, pert in cases:
+        for trial in range(3):
+            d = rng.normal(size=g.shape)
+            fd = (loss(*pert(d, eps)) - loss(*pert(d, -eps))) / (2 * eps)
+            ad = float(np.sum(g * d))
+            assert abs(fd - ad) <= 1e-4 * max(abs(fd), abs(ad)), (name, trial, fd, ad)
