@@ -69,6 +69,8 @@ def test_argument_errors_are_reported(built_lib):
     L = pdipc.load_library()
     assert L.pdipc_create(None, None) == 1
     assert L.pdipc_step(None, 1) == 1
+    assert L.pdipc_adjoint_record(None, 1) == 1
+    assert L.pdipc_adjoint_backward(None, None, None, None, None, None) == 1
     X = np.zeros((3, 3))
     F = np.array([[0, 1, 5]], np.int32)
     with pytest.raises(pdipc.PdipcError):
