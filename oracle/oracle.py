@@ -55,6 +55,7 @@ def lib():
         L.orc_toi.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
         L.orc_contact.argtypes = [C.c_void_p, _dp, _dp, _dp, _i64p]
         L.orc_stage_pd.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.orc_adjoint_rollout.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_penalty_predict.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.orc_penalty.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _ip, C.c_longlong, C.c_double, C.c_double,
                                   C.c_double, _dp, _dp, _ip]
@@ -218,6 +219,21 @@ class Oracle:
         out = np.empty((self.n_total, 3), np.float64)
         _check(lib().orc_stage_pd(self.h, _d(X), _d(V), _d(out)), "stage_pd")
         return out
+
+    def adjoint_rollout(self, steps, X, V, dl_dx, dl_dv=None):
+        """A contact-free rollout of `steps` from (X, V) and its discrete
+        adjoint (FP64, two-sweep form): (dL/dX0, dL/dV0, dL/dk per simulated
+        vertex) for dL/d(final positions, velocities) = (dl_dx, dl_dv)."""
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        gx = np.ascontiguousarray(dl_dx, dtype=np.float64)
+        gv = None if dl_dv is None else np.ascontiguousarray(dl_dv, dtype=np.float64)
+        gx0 = np.empty((self.n_sim, 3), np.float64)
+        gv0 = np.empty((self.n_sim, 3), np.float64)
+        gk = np.empty(self.n_sim, np.float64)
+        _check(lib().orc_adjoint_rollout(self.h, int(steps), _d(X), _d(V), _d(gx), _d(gv) if gv is not None else None,
+                                         _d(gx0), _d(gv0), _d(gk)), "adjoint_rollout")
+        return gx0, gv0, gk
 
     def contact(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)

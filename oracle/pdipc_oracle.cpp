@@ -481,6 +481,10 @@ struct Sim {
     // stats
     pdipc_stats st{};
     std::vector<T> xsweepA, xsweepB, xsweepY;
+    // adjoint: positions at the start of every local-global iteration of a
+    // taped step, and whether an outer iteration clamped the step or had contacts
+    std::vector<std::vector<T>>* lgTape = nullptr;
+    bool contactSeen = false;
     int threads = 1;
 
     explicit Sim(const pdipc_params& p, int form, int nthreads) : prm(p), global_form(form) {
@@ -1503,6 +1507,7 @@ struct Sim {
         if (global_form == 0) update_r2_ops();
         std::vector<T> aq;
         for (int lg = 0; lg < prm.lg_iterations; ++lg) {
+            if (lgTape) lgTape->emplace_back(X.begin(), X.begin() + 3 * (size_t)nsim);
             local_rhs(aq);
             if (global_form == 0) global_r2();
             else global_jj();
@@ -1528,6 +1533,7 @@ struct Sim {
             T tt = (T)toi;
             for (size_t q = 0; q < n3; ++q) X[q] = Xold[q] + tt * dir[q];
             st.active_contacts = contacts(X);
+            if (toi != TC(1) || st.active_contacts != 0) contactSeen = true;
             double res = 0;
             for (size_t q = 0; q < n3; ++q) res += (double)dir[q] * (double)dir[q];
             st.last_toi = (double)toi;
@@ -1561,6 +1567,229 @@ struct Sim {
         for (size_t q = 0; q < X.size(); ++q) out[q] = (double)X[q];
         X = sx;
         V = sv;
+        return PDIPC_OK;
+    }
+
+    // ---------------- discrete adjoint of contact-free steps (two-sweep form) ----------------
+    // The library's reverse pass (adjoint_kernels.cu; solver.cu adjoint_step)
+    // restated sequentially on this oracle's tables.  The step's forward:
+    // predict (cu:88-147), lg local steps (cu:627-790, gather form) each
+    // followed by the two-sweep Chebyshev-Jacobi solve, the identity clamp of
+    // a contact-free outer iteration, the velocity update (cu:262-281).
+    // X, V hold the step's start state; pb, vb (3 nsim) hold dL/d(positions,
+    // velocities) after the step on entry and before it on return; kb (nsim)
+    // collects dL/d(strain weight).  X, V are left at the step's end.
+    int adjoint_step(std::vector<T>& pb, std::vector<T>& vb, std::vector<T>& kb) {
+        if (global_form != 1 || ntet > 0) return PDIPC_ERR_STATE;
+        std::vector<std::vector<T>> tape;
+        lgTape = &tape;
+        contactSeen = false;
+        const int r = step_once();
+        lgTape = nullptr;
+        if (r != PDIPC_OK) return r;
+        if (contactSeen) return PDIPC_ERR_STATE;
+        const size_t n3 = 3 * (size_t)nsim;
+        const int cb = prm.cheby_iterations;
+        const T w = (T)prm.jacobi_relax;
+        const T dt = (T)prm.time_step;
+        const T invt = (T)((1.0 / (double)dt) * (double)(T)(1.0 - (double)dt));
+        std::vector<T> invD(nsim);
+        for (int i = 0; i < nsim; ++i) invD[i] = T(1) / D[i];
+        std::vector<T> oms;
+        {
+            T rho2 = (T)prm.cheby_rho;
+            rho2 = rho2 * rho2;
+            T om = omega_first(rho2);
+            for (int it = 1; it < cb; ++it) {
+                oms.push_back(om);
+                om = omega_next(rho2, om);
+            }
+        }
+        // transposed LBO weights: slot s of row i pointing at j -> weight of row j at i
+        std::vector<T> lboT(lLbo.size(), T(0));
+        for (int i = 0; i < nsim; ++i) {
+            const int o = lOff[i];
+            lboT[o] = lLbo[o];
+            for (int s2 = 1; s2 < lNum[i]; ++s2) {
+                const int j = lNbr[o + s2];
+                for (int t = 1; t < lNum[j]; ++t)
+                    if (lNbr[lOff[j] + t] == i) { lboT[o + s2] = lLbo[lOff[j] + t]; break; }
+            }
+        }
+        auto S = [&](const std::vector<T>& z, std::vector<T>& y) { jsweep(z, y, w, invD); };
+        // out (= or +=) J^T u = (1-w) u + N^T (w D^-1 u)
+        auto JT = [&](const std::vector<T>& u, std::vector<T>& out, bool acc) {
+            std::vector<T> y(n3, T(0));
+            for (int j = 0; j < nsim; ++j)
+                for (int e = nPtr[j]; e < nPtr[j + 1]; ++e) {
+                    const int i = nCol[e];
+                    for (int k = 0; k < 3; ++k) y[3 * (size_t)i + k] += nVal[e] * (w * invD[j] * u[3 * (size_t)j + k]);
+                }
+            for (size_t q = 0; q < n3; ++q) out[q] = (acc ? out[q] : T(0)) + (T(1) - w) * u[q] + y[q];
+        };
+        // kb_i += u_i . dS_i/dk_i: k_i sits on row i's spring entries of N and deg_i times in D_i
+        auto stiff = [&](const std::vector<T>& u, const std::vector<T>& z) {
+            for (int i = 0; i < nsim; ++i) {
+                const int o = lOff[i], deg = lNum[i] - 1;
+                T acc = 0;
+                for (int k = 0; k < 3; ++k) {
+                    T nz = rhs[3 * (size_t)i + k], sz = 0;
+                    for (int e = nPtr[i]; e < nPtr[i + 1]; ++e) nz += nVal[e] * z[3 * (size_t)nCol[e] + k];
+                    for (int s2 = 1; s2 <= deg; ++s2) sz += z[3 * (size_t)lNbr[o + s2] + k];
+                    acc += u[3 * (size_t)i + k] * (sz - T(deg) * invD[i] * nz);
+                }
+                kb[i] += w * invD[i] * acc;
+            }
+        };
+        std::vector<T> r0b(n3, T(0)), X0b(n3);
+        for (size_t q = 0; q < n3; ++q) {
+            X0b[q] = -invt * vb[q];
+            pb[q] += invt * vb[q];
+        }
+        std::vector<std::vector<T>> Xs(cb + 1, std::vector<T>(n3)), Ys(cb, std::vector<T>(n3));
+        std::vector<std::vector<T>> Xb(cb + 1, std::vector<T>(n3));
+        std::vector<T> aq, u(n3), rho(n3), rb(n3), qb(n3), tmp(n3);
+        for (int l = (int)tape.size() - 1; l >= 0; --l) {
+            const std::vector<T>& x = tape[l];
+            std::copy(x.begin(), x.end(), X.begin());
+            local_rhs(aq);
+            Xs[0] = x;
+            S(Xs[0], Ys[0]);
+            if (cb > 1) S(Ys[0], Xs[1]);
+            for (int it = 1; it < cb; ++it) {
+                S(Xs[it], Ys[it]);
+                if (it + 1 < cb) {
+                    S(Ys[it], tmp);
+                    for (size_t q = 0; q < n3; ++q) Xs[it + 1][q] = oms[it - 1] * (tmp[q] - Xs[it - 1][q]) + Xs[it - 1][q];
+                }
+            }
+            for (int t = 0; t < cb; ++t) std::fill(Xb[t].begin(), Xb[t].end(), T(0));
+            Xb[cb] = pb;
+            std::fill(rho.begin(), rho.end(), T(0));
+            for (int it = cb - 1; it >= 1; --it) {
+                const T om = oms[it - 1];
+                for (size_t q = 0; q < n3; ++q) {
+                    tmp[q] = om * Xb[it + 1][q];
+                    Xb[it - 1][q] += (T(1) - om) * Xb[it + 1][q];
+                    rho[q] += tmp[q];
+                }
+                stiff(tmp, Ys[it]);
+                JT(tmp, u, false);
+                for (size_t q = 0; q < n3; ++q) rho[q] += u[q];
+                stiff(u, Xs[it]);
+                JT(u, Xb[it], true);
+            }
+            for (size_t q = 0; q < n3; ++q) rho[q] += Xb[1][q];
+            stiff(Xb[1], Ys[0]);
+            JT(Xb[1], u, false);
+            for (size_t q = 0; q < n3; ++q) rho[q] += u[q];
+            stiff(u, Xs[0]);
+            JT(u, Xb[0], true);
+            for (int i = 0; i < nsim; ++i)
+                for (int k = 0; k < 3; ++k) {
+                    rb[3 * (size_t)i + k] = w * invD[i] * rho[3 * (size_t)i + k];
+                    r0b[3 * (size_t)i + k] += rb[3 * (size_t)i + k];
+                }
+            // curvature vectors: abar_k = sum_s bend_s rb_nbr(s), then through a = q c / |q|
+            for (int i = 0; i < nsim; ++i) {
+                const int o = lOff[i];
+                T q[3] = {0, 0, 0}, a[3] = {0, 0, 0};
+                for (int s2 = 0; s2 < lNum[i]; ++s2) {
+                    const int j = lNbr[o + s2];
+                    for (int k = 0; k < 3; ++k) {
+                        q[k] += lLbo[o + s2] * x[3 * (size_t)j + k];
+                        a[k] += lBend[o + s2] * rb[3 * (size_t)j + k];
+                    }
+                }
+                const T nrm = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+                if (nrm >= T(1e-10)) {
+                    const T pr = (q[0] * a[0] + q[1] * a[1] + q[2] * a[2]) / nrm;
+                    const T c = curvNorm[i] / nrm;
+                    for (int k = 0; k < 3; ++k) a[k] = c * (a[k] - q[k] / nrm * pr);
+                }
+                for (int k = 0; k < 3; ++k) qb[3 * (size_t)i + k] = a[k];
+            }
+            // positions: transposed LBO gather of qb, spring projections; strain weights
+            for (int m = 0; m < nsim; ++m) {
+                const int o = lOff[m];
+                T acc[3];
+                for (int k = 0; k < 3; ++k) acc[k] = Xb[0][3 * (size_t)m + k];
+                for (int s2 = 0; s2 < lNum[m]; ++s2) {
+                    const int j = lNbr[o + s2];
+                    for (int k = 0; k < 3; ++k) acc[k] += lboT[o + s2] * qb[3 * (size_t)j + k];
+                    if (s2 == 0) continue;
+                    T d[3];
+                    for (int k = 0; k < 3; ++k) d[k] = x[3 * (size_t)m + k] - x[3 * (size_t)j + k];
+                    const T len = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                    const T rest = lRest[o + s2];
+                    const T cm = lStrain[o] * rest, cj = lStrain[lOff[j]] * rest;
+                    T uu[3], pr = 0, kr = 0;
+                    for (int k = 0; k < 3; ++k) {
+                        uu[k] = cm * rb[3 * (size_t)m + k] - cj * rb[3 * (size_t)j + k];
+                        pr += d[k] / len * uu[k];
+                        kr += rb[3 * (size_t)m + k] * d[k] / len;
+                    }
+                    for (int k = 0; k < 3; ++k) acc[k] += (uu[k] - d[k] / len * pr) / len;
+                    kb[m] += rest * kr;
+                }
+                for (int k = 0; k < 3; ++k) pb[3 * (size_t)m + k] = acc[k];
+            }
+        }
+        // through the prediction (pinned vertices start at x with v = 0)
+        for (int i = 0; i < nsim; ++i)
+            for (int k = 0; k < 3; ++k) {
+                const size_t q = 3 * (size_t)i + k;
+                if (pinFlag[i] != -1) {
+                    pb[q] = X0b[q] + pb[q];
+                    vb[q] = T(0);
+                } else {
+                    const T m = invMass[i] * dt;
+                    const T mm = (T)(1.0 / (double)(dt * m));
+                    const T y = pb[q] + mm * r0b[q];
+                    pb[q] = X0b[q] + y;
+                    vb[q] = dt * y;
+                }
+            }
+        return PDIPC_OK;
+    }
+    // A rollout of nsteps from (Xin, Vin) and its adjoint: gradients of a loss
+    // with dL/d(final positions, velocities) = gx, gv with respect to the
+    // initial positions, velocities and strain weights.  The state is left at
+    // the rollout's end.
+    int adjoint_rollout(int nsteps, const double* Xin, const double* Vin, const double* gx, const double* gv,
+                        double* gx0, double* gv0, double* gk) {
+        if (!initialized) return PDIPC_ERR_STATE;
+        if (nsteps < 1) return PDIPC_ERR_ARG;
+        const size_t n3 = 3 * (size_t)nsim;
+        for (size_t q = 0; q < X.size(); ++q) X[q] = (T)Xin[q];
+        for (size_t q = 0; q < n3; ++q) V[q] = (T)Vin[q];
+        std::vector<std::vector<T>> xs, vs;
+        for (int s2 = 0; s2 < nsteps; ++s2) {
+            xs.emplace_back(X.begin(), X.begin() + n3);
+            vs.emplace_back(V.begin(), V.begin() + n3);
+            const int r = step_once();
+            if (r != PDIPC_OK) return r;
+        }
+        const std::vector<T> xEnd(X.begin(), X.begin() + n3), vEnd(V.begin(), V.begin() + n3);
+        std::vector<T> pb(n3), vb(n3), kb(nsim, T(0));
+        for (size_t q = 0; q < n3; ++q) {
+            pb[q] = (T)gx[q];
+            vb[q] = gv ? (T)gv[q] : T(0);
+        }
+        int r = PDIPC_OK;
+        for (int s2 = nsteps - 1; s2 >= 0 && r == PDIPC_OK; --s2) {
+            std::copy(xs[s2].begin(), xs[s2].end(), X.begin());
+            std::copy(vs[s2].begin(), vs[s2].end(), V.begin());
+            r = adjoint_step(pb, vb, kb);
+        }
+        std::copy(xEnd.begin(), xEnd.end(), X.begin());
+        std::copy(vEnd.begin(), vEnd.end(), V.begin());
+        if (r != PDIPC_OK) return r;
+        for (size_t q = 0; q < n3; ++q) {
+            gx0[q] = (double)pb[q];
+            gv0[q] = (double)vb[q];
+        }
+        for (int i = 0; i < nsim; ++i) gk[i] = (double)kb[i];
         return PDIPC_OK;
     }
     int step(int n) {
@@ -2013,6 +2242,15 @@ int orc_penalty(void* h, int kind, const double* x, const double* dir, const int
 
 int orc_stage_pd(void* h, const double* X, const double* V, double* out) {
     return orc::dispatch((Ctx*)h, [&](auto& s) { return s.stage_pd(X, V, out); });
+}
+
+// Discrete adjoint of a contact-free rollout (FP64, two-sweep form only).
+int orc_adjoint_rollout(void* h, int nsteps, const double* X, const double* V, const double* gx, const double* gv,
+                        double* gx0, double* gv0, double* gk) {
+    Ctx* c = (Ctx*)h;
+    if (!c || !X || !V || !gx || !gx0 || !gv0 || !gk) return PDIPC_ERR_ARG;
+    if (!c->f64) return PDIPC_ERR_STATE;
+    return c->f64->adjoint_rollout(nsteps, X, V, gx, gv, gx0, gv0, gk);
 }
 
 // Topology of one standalone mesh, for the known-answer tests on the

@@ -11,8 +11,10 @@ and the velocity update.  The adjoint follows the same recurrences as
 adjoint_kernels.cu and the reverse pass of solver.cu (adjoint_step): transposed
 sweeps, the right-hand side's adjoint w D^-1 sum(u), the local step's gathers,
 and the per-vertex stretch-stiffness terms of the rhs, N and D.  It pins the
-method; the kernels are checked against differences of the GPU forward by
-test_adjoint_gpu.py."""
+method.  The oracle's C++ restatement of the same reverse pass on real scene
+tables is checked here against central differences of the oracle's own
+forward; test_adjoint_gpu.py checks the kernels against differences of the GPU
+forward and against the oracle's adjoint."""
 import numpy as np
 
 rng = np.random.default_rng(1)  # the random tables
@@ -251,3 +253,53 @@ def test_adjoint_recurrences_match_central_differences():
             fd = (loss(*pert(d, eps)) - loss(*pert(d, -eps))) / (2 * eps)
             ad = float(np.sum(g * d))
             assert abs(fd - ad) <= 1e-4 * max(abs(fd), abs(ad)), (name, trial, fd, ad)
+
+
+def test_oracle_adjoint_matches_its_own_central_differences():
+    """The oracle's restatement of the adjoint (FP64, two-sweep form) on a real
+    scene's tables: a 10x10 cloth with two pinned corners, three steps, against
+    central differences of the oracle's forward (stiffness: Richardson
+    extrapolation of two central differences of rebuilt contexts)."""
+    from oracle.oracle import FORM_JJ, Oracle
+    from pdipc import scenes
+
+    for lg, cheby, outer in ((1, 1, 1), (2, 4, 1), (10, 15, 2)):
+        def scene(k=1e4):
+            return scenes.cloth_drop(10, 1, with_sphere=False, lg=lg, k_stretch=k)
+
+        kw = dict(cheby_iterations=cheby, fixed_outer=outer)
+        sc = scene()
+        orc = Oracle(sc, "fp64", FORM_JJ, threads=2, **kw)
+        r = np.random.default_rng(7 + lg)
+        nv, T = sc.n_sim, 3
+        x0 = sc.initial_positions()
+        v0 = r.uniform(-0.1, 0.1, (nv, 3))
+        cx, cv = r.normal(size=(nv, 3)), r.normal(size=(nv, 3))
+        tgt = x0 + r.uniform(-0.05, 0.05, x0.shape)
+
+        def run(o, x, v):
+            o.set_state(x, v)
+            o.step(T)
+            return o.positions()[:nv].copy(), o.velocities().copy()
+
+        def loss(x, v):
+            return float(np.sum(cx * x) + np.sum(cv * v) + 0.5 * np.sum((x - tgt) ** 2))
+
+        x, v = run(orc, x0, v0)
+        gx0, gv0, gk = orc.adjoint_rollout(T, x0, v0, cx + (x - tgt), cv)
+        for trial in range(2):
+            d = r.normal(size=(nv, 3))
+            fd = (loss(*run(orc, x0, v0 + 1e-5 * d)) - loss(*run(orc, x0, v0 - 1e-5 * d))) / 2e-5
+            ad = float(np.sum(gv0 * d))
+            assert abs(fd - ad) <= 1e-5 * abs(fd), ("v", lg, cheby, outer, fd, ad)
+            fd = (loss(*run(orc, x0 + 1e-7 * d, v0)) - loss(*run(orc, x0 - 1e-7 * d, v0))) / 2e-7
+            ad = float(np.sum(gx0 * d))
+            assert abs(fd - ad) <= 1e-5 * abs(fd), ("x", lg, cheby, outer, fd, ad)
+
+        def cd(h):
+            lp = loss(*run(Oracle(scene(1e4 + h), "fp64", FORM_JJ, threads=2, **kw), x0, v0))
+            lm = loss(*run(Oracle(scene(1e4 - h), "fp64", FORM_JJ, threads=2, **kw), x0, v0))
+            return (lp - lm) / (2 * h)
+
+        fd = (4.0 * cd(1.0) - cd(2.0)) / 3.0
+        assert abs(fd - gk.sum()) <= 1e-4 * abs(fd), ("k", lg, cheby, outer, fd, gk.sum())
