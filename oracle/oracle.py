@@ -56,6 +56,7 @@ def lib():
         L.orc_contact.argtypes = [C.c_void_p, _dp, _dp, _dp, _i64p]
         L.orc_stage_pd.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.orc_adjoint_rollout.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.orc_tangent_rollout.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_penalty_predict.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.orc_penalty.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _ip, C.c_longlong, C.c_double, C.c_double,
                                   C.c_double, _dp, _dp, _ip]
@@ -234,6 +235,21 @@ class Oracle:
         _check(lib().orc_adjoint_rollout(self.h, int(steps), _d(X), _d(V), _d(gx), _d(gv) if gv is not None else None,
                                          _d(gx0), _d(gv0), _d(gk)), "adjoint_rollout")
         return gx0, gv0, gk
+
+    def tangent_rollout(self, steps, X, V, dX, dV, dk):
+        """A contact-free rollout of `steps` from (X, V) with the forward-mode
+        tangent (dX, dV, dk per simulated vertex) carried along (FP64,
+        two-sweep form): the tangents of the final positions and velocities."""
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        dX = np.ascontiguousarray(dX, dtype=np.float64)
+        dV = np.ascontiguousarray(dV, dtype=np.float64)
+        dk = np.ascontiguousarray(dk, dtype=np.float64)
+        ox = np.empty((self.n_sim, 3), np.float64)
+        ov = np.empty((self.n_sim, 3), np.float64)
+        _check(lib().orc_tangent_rollout(self.h, int(steps), _d(X), _d(V), _d(dX), _d(dV), _d(dk), _d(ox), _d(ov)),
+               "tangent_rollout")
+        return ox, ov
 
     def contact(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)

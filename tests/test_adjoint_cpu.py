@@ -15,7 +15,10 @@ method.  The oracle's C++ restatement of the same reverse pass on real scene
 tables is checked here against central differences of the oracle's own
 forward; test_adjoint_gpu.py checks the kernels against differences of the GPU
 forward and against the oracle's adjoint."""
+import os
+
 import numpy as np
+import pytest
 
 rng = np.random.default_rng(1)  # the random tables
 G = 4
@@ -303,3 +306,47 @@ def test_oracle_adjoint_matches_its_own_central_differences():
 
         fd = (4.0 * cd(1.0) - cd(2.0)) / 3.0
         assert abs(fd - gk.sum()) <= 1e-4 * abs(fd), ("k", lg, cheby, outer, fd, gk.sum())
+
+
+def _oracle_identity(n, T, lg, cheby, outer, threads=8, seed=7):
+    """<dL/dout, tangent of out> against <dL/din, tangent of in> for separate
+    position, velocity and stiffness directions, with the summed magnitude of
+    the first product's terms (its round-off scale)."""
+    from oracle.oracle import FORM_JJ, Oracle
+    from pdipc import scenes
+
+    sc = scenes.cloth_drop(n, 1, with_sphere=False, lg=lg)
+    orc = Oracle(sc, "fp64", FORM_JJ, threads=threads, cheby_iterations=cheby, fixed_outer=outer)
+    r = np.random.default_rng(seed)
+    nv = sc.n_sim
+    x0 = sc.initial_positions()
+    v0 = r.uniform(-0.1, 0.1, (nv, 3))
+    gx, gv = r.normal(size=(nv, 3)), r.normal(size=(nv, 3))
+    gx0, gv0, gk = orc.adjoint_rollout(T, x0, v0, gx, gv)
+    zero3, zero1 = np.zeros((nv, 3)), np.zeros(nv)
+    out = []
+    for name, dX, dV, dk, g, d in (("x", r.normal(size=(nv, 3)), zero3, zero1, gx0, 0),
+                                   ("v", zero3, r.normal(size=(nv, 3)), zero1, gv0, 1),
+                                   ("k", zero3, zero3, r.normal(size=nv), gk, 2)):
+        tx, tv = orc.tangent_rollout(T, x0, v0, dX, dV, dk)
+        lhs = float(np.sum(gx * tx) + np.sum(gv * tv))
+        rhs = float(np.sum(g * (dX, dV, dk)[d]))
+        out.append((name, lhs, rhs, float(np.sum(np.abs(gx * tx)) + np.sum(np.abs(gv * tv)))))
+    return out
+
+
+def test_oracle_adjoint_is_the_transpose_of_its_forward_tangent():
+    """The oracle's adjoint against its forward-mode tangent of the same
+    iteration: exact to round-off at any rollout length, where central
+    differences of this strongly curved forward stop converging."""
+    for case in ((10, 3, 1, 1, 1), (10, 3, 10, 15, 2), (32, 10, 10, 15, 3)):
+        for name, lhs, rhs, scale in _oracle_identity(*case):
+            assert abs(lhs - rhs) <= 1e-10 * scale, (case, name, lhs, rhs, scale)
+
+
+@pytest.mark.skipif(not os.environ.get("PDIPC_LONG_TESTS"), reason="set PDIPC_LONG_TESTS=1 (minutes on the CPU)")
+def test_oracle_adjoint_tangent_identity_128_cloth_50_steps():
+    """The differentiable-rollout workload's shape on the oracle: 128x128 cloth,
+    50 steps, 3 outer iterations of 10 local-global iterations per step."""
+    for name, lhs, rhs, scale in _oracle_identity(128, 50, 10, 15, 3):
+        assert abs(lhs - rhs) <= 1e-10 * scale, (name, lhs, rhs, scale)
