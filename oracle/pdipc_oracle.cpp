@@ -1628,17 +1628,36 @@ struct Sim {
         }
         auto S = [&](const std::vector<T>& z, std::vector<T>& y) { jsweep(z, y, w, invD); };
         // out (= or +=) J^T u = (1-w) u + N^T (w D^-1 u)
-        auto JT = [&](const std::vector<T>& u, std::vector<T>& out, bool acc) {
-            std::vector<T> y(n3, T(0));
+        // N^T as a CSR of its own (row i: the entries N_ji, ascending j), so the
+        // transposed product is a gather
+        std::vector<int> tPtr(nsim + 1, 0), tCol(nPtr[nsim]);
+        std::vector<T> tVal(nPtr[nsim]);
+        for (int e = 0; e < nPtr[nsim]; ++e) ++tPtr[nCol[e] + 1];
+        for (int i = 0; i < nsim; ++i) tPtr[i + 1] += tPtr[i];
+        {
+            std::vector<int> fill(tPtr.begin(), tPtr.end() - 1);
             for (int j = 0; j < nsim; ++j)
                 for (int e = nPtr[j]; e < nPtr[j + 1]; ++e) {
-                    const int i = nCol[e];
-                    for (int k = 0; k < 3; ++k) y[3 * (size_t)i + k] += nVal[e] * (w * invD[j] * u[3 * (size_t)j + k]);
+                    tCol[fill[nCol[e]]] = j;
+                    tVal[fill[nCol[e]]++] = nVal[e];
                 }
-            for (size_t q = 0; q < n3; ++q) out[q] = (acc ? out[q] : T(0)) + (T(1) - w) * u[q] + y[q];
+        }
+        auto JT = [&](const std::vector<T>& u, std::vector<T>& out, bool acc) {
+#pragma omp parallel for schedule(static) num_threads(threads)
+            for (int i = 0; i < nsim; ++i)
+                for (int k = 0; k < 3; ++k) {
+                    T y = 0;
+                    for (int e = tPtr[i]; e < tPtr[i + 1]; ++e) {
+                        const int j = tCol[e];
+                        y += tVal[e] * (w * invD[j] * u[3 * (size_t)j + k]);
+                    }
+                    const size_t q = 3 * (size_t)i + k;
+                    out[q] = (acc ? out[q] : T(0)) + (T(1) - w) * u[q] + y;
+                }
         };
         // kb_i += u_i . dS_i/dk_i: k_i sits on row i's spring entries of N and deg_i times in D_i
         auto stiff = [&](const std::vector<T>& u, const std::vector<T>& z) {
+#pragma omp parallel for schedule(static) num_threads(threads)
             for (int i = 0; i < nsim; ++i) {
                 const int o = lOff[i], deg = lNum[i] - 1;
                 T acc = 0;
@@ -1701,6 +1720,7 @@ struct Sim {
                     r0b[3 * (size_t)i + k] += rb[3 * (size_t)i + k];
                 }
             // curvature vectors: abar_k = sum_s bend_s rb_nbr(s), then through a = q c / |q|
+#pragma omp parallel for schedule(static) num_threads(threads)
             for (int i = 0; i < nsim; ++i) {
                 const int o = lOff[i];
                 T q[3] = {0, 0, 0}, a[3] = {0, 0, 0};
@@ -1720,6 +1740,7 @@ struct Sim {
                 for (int k = 0; k < 3; ++k) qb[3 * (size_t)i + k] = a[k];
             }
             // positions: transposed LBO gather of qb, spring projections; strain weights
+#pragma omp parallel for schedule(static) num_threads(threads)
             for (int m = 0; m < nsim; ++m) {
                 const int o = lOff[m];
                 T acc[3];
@@ -1780,6 +1801,7 @@ struct Sim {
         std::vector<T> aq, da(n3), dr(n3);
         auto S = [&](const std::vector<T>& z, const std::vector<T>& dz, std::vector<T>& y, std::vector<T>& dy) {
             jsweep(z, y, w, invD);
+#pragma omp parallel for schedule(static) num_threads(threads)
             for (int i = 0; i < nsim; ++i) {
                 const int o = lOff[i];
                 for (int k = 0; k < 3; ++k) {
@@ -1796,6 +1818,7 @@ struct Sim {
         };
         for (int lg = 0; lg < prm.lg_iterations; ++lg) {
             // tangent of the curvature vectors and of the rhs at X
+#pragma omp parallel for schedule(static) num_threads(threads)
             for (int i = 0; i < nsim; ++i) {
                 const int o = lOff[i];
                 T q[3] = {0, 0, 0}, dq[3] = {0, 0, 0};
@@ -1814,6 +1837,7 @@ struct Sim {
                 }
                 for (int k = 0; k < 3; ++k) da[3 * (size_t)i + k] = dq[k];
             }
+#pragma omp parallel for schedule(static) num_threads(threads)
             for (int i = 0; i < nsim; ++i) {
                 const int o = lOff[i];
                 T r[3];
