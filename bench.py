@@ -15,7 +15,12 @@ not shard: "replicas only"); the value is all replicas' steps over the slowest
 rank's time.
 
 --impl reference times the CPU restatement of the reference algorithm (the
-reference has no CPU path and cannot be built here) on the host cores.
+reference has no CPU path and cannot be built here) on every host core: whole
+steps 0..K-1 of the same workload with the reference's stopping rule, in the
+R2-operator form and FP64 (in the reference's FP32 the stopping rule never
+fires at 512x512, so FP64 is the CPU's fastest convergent arithmetic and runs
+the same outer-iteration counts as the GPU's mixed mode); steps that would
+start after --ref-budget-s are not run and `steps` says how many ran.
 """
 from __future__ import annotations
 
@@ -186,26 +191,63 @@ def profiled_traffic(prec: str):
     return None
 
 
-def cpu_reference_sample(scene, prec: str, outer_sample: int, outer_per_step: float, threads: int):
-    """Oracle (the reference's R2 algorithm restated on the CPU) on a bounded
-    sample: one step limited to `outer_sample` outer iterations, scaled to the
-    outer iterations a full step runs."""
+def oracle_whole_steps(scene, prec: str, threads: int, max_steps: int, budget_s: float, warmup: int = 0):
+    """The oracle (the reference's algorithm restated on the CPU, its R2-operator
+    form) stepping the workload from its initial state with the reference's
+    stopping rule: whole steps, timed one by one, until `max_steps` steps or
+    `budget_s` seconds.  Nothing is extrapolated: the figures cover the steps
+    that ran."""
     from oracle.oracle import FORM_R2, Oracle
     t0 = time.perf_counter()
-    orc = Oracle(scene, prec, FORM_R2, threads=threads, fixed_outer=outer_sample)
+    orc = Oracle(scene, prec, FORM_R2, threads=threads)
     t_init = time.perf_counter() - t0
+    x0, v0 = scene.initial_positions(), np.zeros((scene.n_sim, 3))
+    for _ in range(warmup):
+        orc.step(1)
+    if warmup:
+        orc.set_state(x0, v0)
+    times, outers = [], []
+    while len(times) < max_steps and sum(times) < budget_s:
+        t0 = time.perf_counter()
+        orc.step(1)
+        times.append(time.perf_counter() - t0)
+        outers.append(int(orc.stats()["last_outer_iters"]))
+    orc.close()
+    n, total = len(times), float(sum(times))
+    return {"steps": n, "seconds": total, "init_s": t_init, "outers": outers,
+            "steps_per_s": n / total, "s_per_outer_iteration": total / max(sum(outers), 1)}
+
+
+def oracle_fp32_outer(scene, threads: int):
+    """Seconds per outer iteration of the oracle in the reference's own FP32
+    arithmetic (R2-operator form): one outer iteration of step 0.  At this size
+    the reference's absolute stopping rule never fires in FP32, so its steps run
+    the 30-iteration cap; this figure prices one iteration of that."""
+    from oracle.oracle import FORM_R2, Oracle
+    orc = Oracle(scene, "fp32", FORM_R2, threads=threads, fixed_outer=1)
     t0 = time.perf_counter()
     orc.step(1)
-    t_step = time.perf_counter() - t0
-    st = orc.stats()
-    per_outer = t_step / outer_sample
-    sec_per_step = per_outer * outer_per_step
-    return {"value": 1.0 / sec_per_step, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": (f"step 0 of the same workload with {outer_sample} outer iterations "
-                       f"({t_step:.1f} s, residual after them {st['last_residual']:.2e} > tol), scaled to "
-                       f"{outer_per_step:.1f} outer iterations per step as run by the GPU; "
-                       f"reference R2-operator form, {prec}, {threads} threads; init {t_init:.1f} s untimed"),
-            "seconds_per_outer_iteration": per_outer}
+    dt = time.perf_counter() - t0
+    orc.close()
+    return dt
+
+
+def cpu_reference_sample(scene, threads: int, max_steps: int = 3, budget_s: float = 20.0):
+    """cpu_baseline of the GPU arm: the first whole steps of the same workload on
+    the host cores (FP64 R2-operator form of the oracle, the reference's stopping
+    rule), plus the price of one FP32 outer iteration."""
+    r = oracle_whole_steps(scene, "fp64", threads, max_steps, budget_s)
+    fp32_outer = oracle_fp32_outer(scene, threads)
+    return {"value": r["steps_per_s"], "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"steps 0..{r['steps'] - 1} of the same workload run in full ({r['seconds']:.1f} s; outer "
+                       f"iterations {r['outers']}, the reference's stopping rule), the reference's R2-operator "
+                       f"algorithm restated on the CPU in FP64, {threads} threads, init {r['init_s']:.1f} s "
+                       f"untimed. FP64 is the CPU's fastest convergent arithmetic here: in the reference's FP32 "
+                       f"the absolute rule |dx|^2 < 1e-5 never fires at 512x512 and every step runs the "
+                       f"30-iteration cap at {fp32_outer:.2f} s per outer iteration"),
+            "s_per_outer_iteration": r["s_per_outer_iteration"],
+            "outer_iterations_per_step": float(np.mean(r["outers"])),
+            "fp32_s_per_outer_iteration": fp32_outer}
 
 
 # ---------------------------------------------------------------------------- arms
@@ -263,6 +305,35 @@ def run_ours(args):
     st_end = sim.stats()
     x_end = out.copy()
 
+    # the contact phase of the same run: advance untimed to step
+    # `contact_start`, then time `contact_steps` steps the same way
+    contact = None
+    if args.contact_steps > 0 and not args.scene:
+        done = args.steps
+        if done < args.contact_start:
+            sim.step(args.contact_start - done)
+            done = args.contact_start
+        c_ms, c_outers, c_pd, c_ccd, c_ct = 0.0, [], 0.0, 0.0, 0.0
+        for _ in range(args.contact_steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            sim.step(1)
+            st = sim.stats()
+            c_ms += st["device_ms"]
+            c_outers.append(st["last_outer_iters"])
+            c_pd += st["pd_solve_ms"]
+            c_ccd += st["ccd_ms"]
+            c_ct += st["contact_ms"]
+        k = args.contact_steps
+        contact = {"steps_timed": f"{done}..{done + k - 1} (after {done} steps from the initial state)",
+                   "value": round(k / (c_ms * 1e-3), 4), "unit": UNIT, "ms_per_step": round(c_ms / k, 3),
+                   "outer_iterations_per_step": float(np.mean(c_outers)),
+                   "ms_per_outer_iteration": round(c_ms / max(sum(c_outers), 1), 4),
+                   "active_contacts_last": int(sim.stats()["active_contacts"]),
+                   "step_breakdown_ms": {"pd_solve": round(c_pd / k, 3), "ccd": round(c_ccd / k, 3),
+                                         "contact": round(c_ct / k, 3),
+                                         "rest": round((c_ms - c_pd - c_ccd - c_ct) / k, 3)}}
+
     # plain FP64 GPU form over the same steps: its speed, the position error of
     # this run after them, and the one-step error of this mode started from the
     # FP64 run's own state every 10 steps
@@ -301,6 +372,29 @@ def run_ours(args):
         ref.close()
         del ref
 
+    # the reference's own arithmetic on the GPU over the same steps: FP32 in
+    # every kernel, the reference's stopping rule (which never fires at this
+    # size in FP32, so its steps run the outer-iteration cap)
+    fp32 = None
+    if args.precision != "fp32" and args.fp32_steps > 0:
+        k32 = min(args.fp32_steps, args.steps)
+        g32 = pdipc.Simulator(sc, "fp32", device=local)
+        g32.step(args.warmup)
+        g32.reset()
+        ms32, outers32 = 0.0, []
+        for _ in range(k32):
+            flush.zero_()
+            torch.cuda.synchronize()
+            g32.step(1)
+            ms32 += g32.stats()["device_ms"]
+            outers32.append(g32.stats()["last_outer_iters"])
+        fp32 = {"value": round(k32 / (ms32 * 1e-3), 4), "unit": UNIT, "steps": k32,
+                "ms_per_step": round(ms32 / k32, 3),
+                "outer_iterations_per_step": {"mean": float(np.mean(outers32)), "max": int(max(outers32))},
+                "ms_per_outer_iteration": round(ms32 / max(sum(outers32), 1), 4)}
+        g32.close()
+        del g32
+
     # roofline of the dominant kernel: the PD solve of an outer iteration (one
     # persistent launch), timed by the library's events around each solve over
     # the timed steps; and one J sweep launched alone, for comparison
@@ -333,14 +427,13 @@ def run_ours(args):
         "dtype": {"fp32": "f32", "fp64": "f64",
                   "mixed": "f32 (local step, residual terms, sweeps) + f64 (state, CCD/contact refinement)"}[
             args.precision], "data": "synthetic (seeded generator; no public dataset for this path)",
-        "config": {"workload": workload_desc(sc, args.precision), "steps_timed": f"0..{args.steps - 1}",
-                   "parallelism": "replicas only" if ws > 1 else "single GPU",
-                   "l2": "flushed between timed steps (256 MB write)",
-                   "outer_iterations_per_step": {"mean": mean_outer, "min": int(min(outers)),
-                                                 "max": int(max(outers))},
-                   "vertices_sim": sim.n_sim, "vertices_total": sim.n_total,
-                   "patch_pairs": st_end["patch_pairs"], "pt_candidates": st_end["pt_candidates"],
-                   "ee_candidates": st_end["ee_candidates"], "device_bytes": st_end["device_bytes"]},
+        "config": run_config(sc, args, ws),
+        "run": {"outer_iterations_per_step": {"mean": mean_outer, "min": int(min(outers)), "max": int(max(outers))},
+                "ms_per_outer_iteration": round(dev_ms_max / max(sum(outers), 1), 4),
+                "vertices_sim": sim.n_sim, "vertices_total": sim.n_total,
+                "patch_pairs": st_end["patch_pairs"], "pt_candidates": st_end["pt_candidates"],
+                "ee_candidates": st_end["ee_candidates"], "device_bytes": st_end["device_bytes"],
+                "l2_flush": "256 MB written between timed steps"},
         "element_updates_per_s": round(sim.n_sim * sc.lg_iterations * float(np.sum(outers)) / (dev_ms / 1e3), 1),
         "gpu_launches": int(launches),
         "step_breakdown_ms": {"pd_solve": round(pd_ms / args.steps, 3), "ccd": round(ccd_ms / args.steps, 3),
@@ -368,45 +461,62 @@ def run_ours(args):
     }
     if fp64 is not None:
         res["fp64_gpu"] = fp64
+    if fp32 is not None:
+        res["fp32_gpu"] = fp32
+    if contact is not None:
+        res["contact_phase"] = contact
     if not args.no_cpu_baseline:
-        res["cpu_baseline"] = cpu_reference_sample(sc, "fp32", args.cpu_outer_sample, args.ref_outer_per_step,
-                                                   os.cpu_count() or 1)
+        res["cpu_baseline"] = cpu_reference_sample(sc, os.cpu_count() or 1, args.cpu_steps, args.cpu_budget_s)
+        cb = res["cpu_baseline"]
+        res["per_outer_iteration"] = {
+            "gpu_ms": res["run"]["ms_per_outer_iteration"],
+            "cpu_fp64_r2_ms": round(cb["s_per_outer_iteration"] * 1e3, 2),
+            "gpu_fp32_ms": fp32["ms_per_outer_iteration"] if fp32 else None,
+            "cpu_fp32_r2_ms": round(cb["fp32_s_per_outer_iteration"] * 1e3, 2),
+            "note": "the same outer iteration (20 local-global iterations of 15 Chebyshev R2 steps, CCD, "
+                    "contact) priced on each side; the GPU mixed mode and the CPU FP64 run stop after the same "
+                    "outer-iteration counts (equal to the FP64 oracle's step for step)"}
     print(json.dumps(res), flush=True)
     if dist is not None:
         dist.destroy_process_group()
 
 
+def run_config(sc, args, ws: int) -> dict:
+    """The `config` object, identical in both arms for the same arguments."""
+    return {"workload": workload_desc(sc, args.precision), "steps_timed": f"0..{args.steps - 1}",
+            "parallelism": "replicas only" if ws > 1 else "single GPU",
+            "l2": "working set above L2 (about 1 GB at 512x512, more than any cache on either side); the GPU "
+                  "arm also writes 256 MB between timed steps"}
+
+
 def run_reference(args):
+    """The reference arm: the oracle (the reference's algorithm, R2-operator
+    form, restated on the CPU) on every host thread, stepping the same workload
+    from the same initial state with the reference's stopping rule.  Whole
+    steps, timed one by one; steps past the time budget are not run, and
+    `steps` reports how many were."""
     ws, rank, local = dist_env()
     if rank != 0:
         return
-    from oracle.oracle import FORM_R2, Oracle
     sc = workload(args.config, args.scene)
     threads = os.cpu_count() or 1
-    sample_outer = args.cpu_outer_sample
-    orc = Oracle(sc, "fp32", FORM_R2, threads=threads, fixed_outer=sample_outer)
-    for _ in range(min(args.warmup, 1)):
-        orc.step(1)
-    orc.set_state(sc.initial_positions(),
-                  np.zeros((sc.n_sim, 3)))
-    budget, t_used, n = args.ref_budget_s, 0.0, 0
-    while n < args.steps and t_used < budget:
-        t0 = time.perf_counter()
-        orc.step(1)
-        t_used += time.perf_counter() - t0
-        n += 1
-    per_outer = t_used / (n * sample_outer)
-    outer_per_step = args.ref_outer_per_step
-    value = 1.0 / (per_outer * outer_per_step)
-    resid = orc.stats()["last_residual"]
-    sample = (f"{n} steps from step 0, each with {sample_outer} outer iterations, scaled to {outer_per_step} "
-              f"outer iterations per step: the reference's stopping rule (|dx|^2 < 1e-5) never fires at this size "
-              f"in its FP32 arithmetic (residual after the sampled iterations {resid:.2e}); reference R2-operator "
-              f"form and FP32 arithmetic restated on the CPU, {threads} threads")
+    r = oracle_whole_steps(sc, "fp64", threads, args.steps, args.ref_budget_s, warmup=min(args.warmup, 1))
+    n = r["steps"]
+    value = r["steps_per_s"]
+    sample = (f"steps 0..{n - 1} of {args.steps} run in full ({r['seconds']:.1f} s; outer iterations per step "
+              f"{r['outers']}, the reference's stopping rule |dx|^2 < 1e-5, cap 30), the reference's R2-operator "
+              f"algorithm restated on the CPU in FP64 (at 512x512 the rule never fires in FP32, so FP64 is the "
+              f"CPU's fastest convergent arithmetic), {threads} threads; init {r['init_s']:.1f} s and "
+              f"{min(args.warmup, 1)} warm-up step untimed")
     res = {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": ws,
            "steps": n, "warmup": args.warmup, "ms_per_step": round(1e3 / value, 3), "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic", "config": {"workload": workload_desc(sc, args.precision)},
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded generator; no public dataset for this path)",
+           "config": run_config(sc, args, ws),
+           "run": {"outer_iterations_per_step": {"mean": float(np.mean(r["outers"])), "min": int(min(r["outers"])),
+                                                 "max": int(max(r["outers"]))},
+                   "s_per_outer_iteration": round(r["s_per_outer_iteration"], 4),
+                   "steps_requested": args.steps},
            "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": threads, "kind": "port",
                             "sample": sample},
            "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -456,10 +566,16 @@ def main(argv=None):
                     help="c1 is the benchmark workload; the others are for reference measurements")
     ap.add_argument("--scene", default=None,
                     help="a reference-format config.xml to run instead of --config (reference measurement)")
+    ap.add_argument("--fp32-steps", type=int, default=100,
+                    help="steps of the FP32 GPU form (the reference's arithmetic) timed beside the headline")
+    ap.add_argument("--contact-start", type=int, default=50,
+                    help="first step of the contact-phase window timed after the headline run")
+    ap.add_argument("--contact-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-outer-sample", type=int, default=2)
-    ap.add_argument("--ref-outer-per-step", type=float, default=30.0)
-    ap.add_argument("--ref-budget-s", type=float, default=60.0)
+    ap.add_argument("--cpu-steps", type=int, default=3, help="whole steps in the GPU arm's cpu_baseline sample")
+    ap.add_argument("--cpu-budget-s", type=float, default=20.0)
+    ap.add_argument("--ref-budget-s", type=float, default=300.0,
+                    help="the reference arm stops starting new steps after this many seconds of stepping")
     ap.add_argument("--accuracy-study", action="store_true",
                     help="print the error-vs-FP64 table of the precision mode instead of the bench line")
     args = ap.parse_args(argv)

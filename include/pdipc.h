@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PDIPC_ABI_VERSION 6
+#define PDIPC_ABI_VERSION 7
 
 typedef struct pdipc_ctx pdipc_ctx;
 
@@ -89,7 +89,13 @@ typedef struct {
                                 (else, and in FP32, gathers through L1); 2 neighbour waits, L2-only
                                 gathers; 3 grid-wide barriers, gathers through L1; 4 neighbour waits,
                                 gathers through L1 (no band); 0 one launch per sweep */
-    int reserved[6];
+    int wait_limit_us;       /* limit of every device-side wait of the persistent solve (neighbour flags,
+                                grid barrier, halo copies), in microseconds at the maximum SM clock; past
+                                it the launch ends and the step returns PDIPC_ERR_CUDA; 0 = 2 s.  The
+                                reference has no device-side waits (one launch per kernel). */
+    int autotune;            /* 1: choose launch shapes by timing candidates on the first step (see
+                                pdipc_get_tuning); 0: the built-in defaults */
+    int reserved[4];
 } pdipc_params;
 
 /* Per-context statistics of the most recent pdipc_step call. */
@@ -217,6 +223,13 @@ pdipc_status pdipc_initialize(pdipc_ctx* ctx);
 /* nsteps x PdIpcSimulator::run(frame) (cpp:18-21 -> doTime cpp:1538 -> advance cpp:1683-1796).
  * The state stays on the device. */
 pdipc_status pdipc_step(pdipc_ctx* ctx, int nsteps);
+
+/* Change pdipc_params.wait_limit_us of an initialised context (no counterpart in
+ * the reference, whose kernels never wait on one another).  A launch whose wait
+ * runs past the limit ends early, the step returns PDIPC_ERR_CUDA with the state
+ * of a partial step, and the context stays usable: set the state again
+ * (pdipc_set_state / pdipc_load / pdipc_reset) and step on. */
+pdipc_status pdipc_set_wait_limit(pdipc_ctx* ctx, int wait_limit_us);
 
 /* BaseSimulator::animate(frame) = run(frame); postRun() (BaseSimulator.h:73-76):
  * one step, then copy every vertex position to out (3*n_total float64) —

@@ -46,9 +46,16 @@ pdipc_status guarded(pdipc_ctx* c, F&& f) {
     }
 }
 
+// Every call on an initialised context runs on the context's device: two
+// contexts on different devices can share one host thread, and device-keyed
+// state (the no-allocation stage's scratch address) follows the current device.
 pdipc_status need_init(pdipc_ctx* c) {
     if (!c) return PDIPC_ERR_ARG;
     if (!c->initialized || !c->solver) return fail(c, PDIPC_ERR_STATE, "call pdipc_initialize first");
+    if (cudaSetDevice(c->prm.device) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, PDIPC_ERR_CUDA, "cudaSetDevice failed");
+    }
     return PDIPC_OK;
 }
 
@@ -251,8 +258,16 @@ pdipc_status pdipc_initialize(pdipc_ctx* ctx) {
 pdipc_status pdipc_step(pdipc_ctx* ctx, int nsteps) {
     pdipc_status s = need_init(ctx);
     if (s != PDIPC_OK) return s;
-    cudaSetDevice(ctx->prm.device);
     return guarded(ctx, [&]() { return ctx->solver->step(nsteps, ctx->err); });
+}
+
+pdipc_status pdipc_set_wait_limit(pdipc_ctx* ctx, int wait_limit_us) {
+    pdipc_status s = need_init(ctx);
+    if (s != PDIPC_OK) return s;
+    if (wait_limit_us < 0) return fail(ctx, PDIPC_ERR_ARG, "wait_limit_us must not be negative");
+    ctx->prm.wait_limit_us = wait_limit_us;
+    ctx->solver->set_wait_limit(wait_limit_us);
+    return PDIPC_OK;
 }
 
 pdipc_status pdipc_get_positions(pdipc_ctx* ctx, double* out) {

@@ -354,12 +354,16 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     const unsigned ncomp = blockDim.x - 32u;
     unsigned mphase = 0;
     // sync warp: optionally wait until the neighbours have published phase
-    // `epoch`, then copy the halo of src
+    // `epoch`, then copy the halo of src.  The whole poll has one deadline (a
+    // lane that polls several neighbours does not restart its clock), so the
+    // warp has either issued the copies or arrived without them within
+    // a.timeout of entering; the compute warps start waiting later than that
+    // and give up only after 2 * a.timeout.
     auto issue_halo = [&](const V4<T>* src, bool poll) -> bool {
         int ok = (ld_acquire_gpu(a.err) & kErrBarrier) ? 0 : 1;
+        const long long t0 = clock64();
         for (int n = nrange.x + lane; poll && ok && n <= nrange.y; n += 32) {
             if (n == cta) continue;
-            const long long t0 = clock64();
             while ((int)(ld_acquire_gpu(a.flags + n) - epoch) < 0) {
                 if (clock64() - t0 > a.timeout || (ld_acquire_gpu(a.err) & kErrBarrier)) {
                     atomicOr(a.err, (unsigned)kErrBarrier);
@@ -387,14 +391,25 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
         __syncwarp();
         return ok != 0;
     };
-    // compute warps: wait for the halo copy; false when the launch is ending
+    // compute warps: wait for the halo copy; false when the launch is ending.
+    // The phase completes either when the copies land or when the sync warp
+    // gives up and arrives without copies (abort_s set first).  Past the
+    // limit, the error bit makes the sync warp's poll give up at once, and
+    // the warps keep waiting (bounded) for the phase: leaving earlier could
+    // end the CTA while a bulk copy still writes its shared memory.  When the
+    // copies did land, the sweep finishes normally and the launch ends at the
+    // sync warp's next poll, which sees the error bit; so no warp returns
+    // while another waits for it at a CTA barrier.
     auto halo_ready = [&]() -> bool {
         const long long t0 = clock64();
+        bool raised = false;
         while (!mbar_try_wait(mbar, mphase)) {
-            if (clock64() - t0 > 2 * a.timeout) {  // longer than the sync warp's own waits
+            const long long dt = clock64() - t0;
+            if (!raised && dt > 2 * a.timeout) {
                 atomicOr(a.err, (unsigned)kErrBarrier);
-                return false;
+                raised = true;
             }
+            if (dt > 4 * a.timeout) return false;  // the sync warp stopped too: nothing is in flight
         }
         mphase ^= 1u;
         return *((volatile int*)&abort_s) == 0;

@@ -69,6 +69,14 @@ public:
     int n_sim() const override { return d_.nsim; }
     int n_total() const override { return d_.ntot; }
 
+    // Device-side wait limit of the persistent solve, converted to SM clock
+    // cycles at the device's maximum clock (clock64 counts cycles); 0 = 2 s.
+    void set_wait_limit(int us) override {
+        const long long u = us > 0 ? (long long)us : 2000000ll;
+        wait_cycles_ = std::max(1ll, u * (long long)clock_khz_ / 1000ll);
+        if constexpr (std::is_same<T, float>::value) pargs_.timeout = wait_cycles_;
+    }
+
     pdipc_status init(const HostTables& H, const pdipc_params& p, std::string& err) override {
         prm_ = p;
         c_.dt = p.time_step;
@@ -89,6 +97,16 @@ public:
             err = "lg_iterations, cheby_iterations, max_outer and time_step must be positive";
             return PDIPC_ERR_ARG;
         }
+        if (p.wait_limit_us < 0) {
+            err = "wait_limit_us must not be negative";
+            return PDIPC_ERR_ARG;
+        }
+        {
+            int khz = 0;
+            PD_CK(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, p.device));
+            clock_khz_ = khz > 0 ? khz : 2000000;
+        }
+        set_wait_limit(p.wait_limit_us);
         PD_CK(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
         PD_CK(cudaEventCreate(&ev0_));
         PD_CK(cudaEventCreate(&ev1_));
@@ -306,11 +324,23 @@ public:
         for (int k = 0; k < n; ++k) {
             if (adj_every_ > 0) {
                 pdipc_status r = adjoint_checkpoint(err);
-                if (r != PDIPC_OK) return r;
+                if (r != PDIPC_OK) {
+                    adjoint_clear();
+                    return r;
+                }
             }
             PD_CK(cudaEventRecord(ev0_, s_));
             pdipc_status r = step_once(err);
-            if (r != PDIPC_OK) return r;
+            if (r != PDIPC_OK) {
+                // a failed step has no well-defined end state to differentiate:
+                // the recording ends here rather than count a step that never finished
+                if (adj_every_ > 0) {
+                    adjoint_clear();
+                    err += " (the adjoint recording was dropped)";
+                }
+                return r;
+            }
+            if (adj_every_ > 0) ++adj_steps_;
             PD_CK(cudaEventRecord(ev1_, s_));
             PD_CK(cudaEventSynchronize(ev1_));
             float ms = 0.f;
@@ -350,6 +380,10 @@ public:
     }
     pdipc_status set_state(const double* X, const double* V, std::string& err) override {
         adjoint_clear();  // the recorded trajectory no longer leads here
+        return put_state(X, V, err);
+    }
+    // positions (and velocities) to the device without touching a recording
+    pdipc_status put_state(const double* X, const double* V, std::string& err) {
         pdipc_status r = upload_vec(d_.P, X, d_.ntot, err);
         if (r != PDIPC_OK) return r;
         launch_split(d_, d_.P, d_.Ph, d_.Pl, d_.ntot, s_);
@@ -460,6 +494,14 @@ public:
                 return PDIPC_ERR_OVERFLOW;
             }
             std::lock_guard<std::mutex> hold(*sc.lock);
+            // Declared after the lock, so destroyed before it: on every return
+            // path, including the error returns of PD_CK below, the stream
+            // has drained (no kernel or copy still uses the shared array)
+            // before another context may take the lock.
+            struct Drain {
+                cudaStream_t s;
+                ~Drain() { cudaStreamSynchronize(s); }
+            } drain{s_};
             pdipc_status r = upload_vec(d_.Pold, x0, d_.ntot, err);
             if (r == PDIPC_OK) r = upload_vec(scratch_, x1, d_.ntot, err);
             if (r != PDIPC_OK) return r;
@@ -508,14 +550,16 @@ public:
         std::vector<double> saveX(3 * (size_t)d_.ntot), saveV(3 * (size_t)d_.nsim);
         pdipc_status r = get_positions(saveX.data(), err);
         if (r == PDIPC_OK) r = get_velocities(saveV.data(), err);
-        if (r == PDIPC_OK) r = set_state(X, V, err);
+        // put_state, not set_state: the state is restored below, so a
+        // recording in progress stays valid across this diagnostic call
+        if (r == PDIPC_OK) r = put_state(X, V, err);
         if (r != PDIPC_OK) return r;
         launch_predict(d_, (TC)c_.dt, s_);
         if (plan_.enabled) PD_CK(launch_persistent());
         else enqueue_pd();
         r = get_positions(out, err);
-        if (r == PDIPC_OK) r = set_state(saveX.data(), saveV.data(), err);
-        return r;
+        pdipc_status r2 = put_state(saveX.data(), saveV.data(), err);
+        return r != PDIPC_OK ? r : r2;
     }
 
     // ---------------- penalty / discrete-collision stages ----------------
@@ -644,8 +688,7 @@ private:
             PD_CK(cudaMemcpyAsync(c, d_.P, sizeof(V4<TC>) * d_.nsim, cudaMemcpyDeviceToDevice, s_));
             PD_CK(cudaMemcpyAsync(c + d_.nsim, d_.Vel, sizeof(V4<TC>) * d_.nsim, cudaMemcpyDeviceToDevice, s_));
         }
-        ++adj_steps_;
-        return PDIPC_OK;
+        return PDIPC_OK;  // step() counts the step once it has completed
     }
 
     pdipc_status adjoint_record(int every, std::string& err) override {
@@ -1172,7 +1215,7 @@ private:
                 a.omega[it] = om;
                 om = omega_next(rho2, om);
             }
-            a.timeout = 4000000000ll;  // ~2 s at 2 GHz
+            a.timeout = wait_cycles_;
             a.P = d.P;
             a.Ph = d.Ph;
             a.Pl = d.Pl;
@@ -1625,6 +1668,8 @@ private:
     Pinned* pin_ = nullptr;
     // discrete adjoint: checkpoints, tape and work vectors (FP64 form)
     int adj_every_ = 0, adj_steps_ = 0;
+    int clock_khz_ = 2000000;
+    long long wait_cycles_ = 4000000000ll;
     std::vector<V4<TC>*> adj_ckpt_, adj_seg_;
     V4<TC>* adj_tape_ = nullptr;
     int adj_tape_cap_ = 0, adj_tape_n_ = 0;

@@ -42,6 +42,8 @@ public:
     virtual pdipc_status adjoint_record(int every, std::string& err) = 0;
     virtual pdipc_status adjoint_backward(const double* gx, const double* gv, double* gx0, double* gv0, double* gk,
                                           std::string& err) = 0;
+    // limit of the persistent solve's device-side waits, microseconds (0 = 2 s)
+    virtual void set_wait_limit(int us) = 0;
     virtual int n_sim() const = 0;
     virtual int n_total() const = 0;
 };

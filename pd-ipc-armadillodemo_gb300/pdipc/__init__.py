@@ -37,10 +37,11 @@ EXPORTS = [
     "pdipc_scene_load", "pdipc_scene_model_count", "pdipc_scene_get_model", "pdipc_scene_apply_params",
     "pdipc_scene_add_models", "pdipc_scene_free", "pdipc_stage_penalty_predict", "pdipc_stage_penalty_ccd",
     "pdipc_stage_penalty_floor", "pdipc_stage_penalty_dcd", "pdipc_adjoint_record", "pdipc_adjoint_backward",
+    "pdipc_set_wait_limit",
 ]
 
 
-ABI_VERSION = 6  # PDIPC_ABI_VERSION of include/pdipc.h
+ABI_VERSION = 7  # PDIPC_ABI_VERSION of include/pdipc.h
 
 
 class PdipcError(RuntimeError):
@@ -81,6 +82,7 @@ def load_library(path: str | None = None):
                                        C.c_int, C.c_double, C.c_int]
     L.pdipc_initialize.argtypes = [vp]
     L.pdipc_step.argtypes = [vp, C.c_int]
+    L.pdipc_set_wait_limit.argtypes = [vp, C.c_int]
     L.pdipc_animate.argtypes = [vp, _dp]
     L.pdipc_get_positions.argtypes = [vp, _dp]
     L.pdipc_get_velocities.argtypes = [vp, _dp]
@@ -194,6 +196,10 @@ class Simulator:
         self._check(load_library().pdipc_step(self.h, int(nsteps)), "pdipc_step")
 
     step = run
+
+    def set_wait_limit(self, us: int):
+        """Limit of the persistent solve's device-side waits in microseconds (0 = 2 s)."""
+        self._check(load_library().pdipc_set_wait_limit(self.h, int(us)), "pdipc_set_wait_limit")
 
     def animate(self, out: np.ndarray | None = None) -> np.ndarray:
         """run(frame); postRun(): one step and the positions copied to the host."""

@@ -51,7 +51,9 @@ class Params(C.Structure):
         ("device", C.c_int),
         ("rebuild_bvh", C.c_int),
         ("persistent", C.c_int),
-        ("reserved", C.c_int * 6),
+        ("wait_limit_us", C.c_int),
+        ("autotune", C.c_int),
+        ("reserved", C.c_int * 4),
     ]
 
 
