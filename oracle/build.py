@@ -2,8 +2,10 @@
 
 Compiles oracle/pdipc_oracle.cpp into oracle/liborc.so with g++ and OpenMP.
 -ffp-contract=off keeps the arithmetic identical on x86 and Arm hosts.
-The reference itself cannot be compiled here (MSVC project; Eigen, Qt, oneTBB
-and BVH_lib are absent), so there is no oracle/_ref build.
+The reference's project cannot be built here (MSVC; Eigen, Qt, oneTBB and
+BVH_lib are absent), but its PD-IPC kernels can: oracle/build_ref.py compiles
+them for the host into oracle/_ref, and they pin this restatement
+(tests/golden/ref_kernels.npz).
 """
 import os
 import subprocess

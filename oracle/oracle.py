@@ -54,6 +54,8 @@ def lib():
         L.orc_morton.argtypes = [C.c_void_p, C.POINTER(C.c_ulonglong), _ip, C.c_int]
         L.orc_toi.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
         L.orc_contact.argtypes = [C.c_void_p, _dp, _dp, _dp, _i64p]
+        L.orc_table.restype = C.c_longlong
+        L.orc_table.argtypes = [C.c_void_p, C.c_char_p, _dp, _ip, C.c_longlong]
         L.orc_stage_pd.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.orc_adjoint_rollout.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.orc_tangent_rollout.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
@@ -176,6 +178,22 @@ class Oracle:
         _check(lib().orc_morton(self.h, codes.ctypes.data_as(C.POINTER(C.c_ulonglong)), _i(order), npatch),
                "morton")
         return codes, order
+
+    _INT_TABLES = {"lOff", "lNum", "lNbr", "pinFlag", "nPtr", "nCol", "r2Ptr", "r2Col", "r2Const", "r2First",
+                   "pathPtr", "pathK"}
+
+    def table(self, name):
+        """One initialised table (orc_table): int32 for index tables, float64 otherwise."""
+        n = lib().orc_table(self.h, name.encode(), None, None, 0)
+        if n < 0:
+            raise OracleError(f"unknown table {name}")
+        if name in self._INT_TABLES:
+            out = np.empty(max(n, 1), np.int32)
+            lib().orc_table(self.h, name.encode(), None, _i(out), n)
+        else:
+            out = np.empty(max(n, 1), np.float64)
+            lib().orc_table(self.h, name.encode(), _d(out), None, n)
+        return out[:n]
 
     def toi(self, x0, x1, npt, nee):
         x0 = np.ascontiguousarray(x0, dtype=np.float64)

@@ -2397,6 +2397,55 @@ int orc_contact(void* h, const double* x, double* diag, double* rhs, long long* 
     });
 }
 
+// One of the initialised tables by name, for the harness that runs the
+// reference's own kernels on the same inputs (oracle/ref_harness.cpp): integer
+// tables go to iout, real ones to dout (either may be NULL to ask for the
+// size).  Returns the entry count, or -1 for an unknown name.
+long long orc_table(void* h, const char* name, double* dout, int* iout, long long cap) {
+    long long n = -1;
+    orc::dispatch((Ctx*)h, [&](auto& s) {
+        if (!s.initialized || !name) return (int)PDIPC_ERR_STATE;
+        const std::string k(name);
+        auto ints = [&](const std::vector<int>& v) {
+            n = (long long)v.size();
+            if (iout && n <= cap) std::copy(v.begin(), v.end(), iout);
+        };
+        auto reals = [&](const auto& v) {
+            n = (long long)v.size();
+            if (dout && n <= cap)
+                for (long long q = 0; q < n; ++q) dout[q] = (double)v[q];
+        };
+        if (k == "lOff") ints(s.lOff);
+        else if (k == "lNum") ints(s.lNum);
+        else if (k == "lNbr") ints(s.lNbr);
+        else if (k == "pinFlag") ints(s.pinFlag);
+        else if (k == "nPtr") ints(s.nPtr);
+        else if (k == "nCol") ints(s.nCol);
+        else if (k == "r2Ptr") ints(s.r2Ptr);
+        else if (k == "r2Col") ints(s.r2Col);
+        else if (k == "r2Const") ints(s.r2Const);
+        else if (k == "r2First") ints(s.r2First);
+        else if (k == "pathPtr") ints(s.pathPtr);
+        else if (k == "pathK") ints(s.pathK);
+        else if (k == "lStrain") reals(s.lStrain);
+        else if (k == "lRest") reals(s.lRest);
+        else if (k == "lLbo") reals(s.lLbo);
+        else if (k == "lBend") reals(s.lBend);
+        else if (k == "lBendT") reals(s.lBendT);
+        else if (k == "curvNorm") reals(s.curvNorm);
+        else if (k == "invMass") reals(s.invMass);
+        else if (k == "grav") reals(s.grav);
+        else if (k == "pinStiff") reals(s.pinStiff);
+        else if (k == "Delastic") reals(s.Delastic);
+        else if (k == "nVal") reals(s.nVal);
+        else if (k == "pathA") reals(s.pathA);
+        else if (k == "collMass") reals(s.collMass);
+        else if (k == "Xrest") reals(s.Xrest_all);
+        return (int)PDIPC_OK;
+    });
+    return n;
+}
+
 int orc_penalty_predict(void* h, const double* X, double* V, double* sn) {
     return orc::dispatch((Ctx*)h, [&](auto& s) {
         if (!s.initialized) return (int)PDIPC_ERR_STATE;
