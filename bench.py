@@ -405,6 +405,8 @@ def run_ours(args):
     sim.set_state(x_end)
     sweep_ms, sweep_bytes = sim.sweep_timing(400)
     sweep_gbs = sweep_bytes / (sweep_ms * 1e-3) / 1e9
+    local_ms, local_bytes = sim.local_timing(400)
+    local_gbs = local_bytes / (local_ms * 1e-3) / 1e9
     pd_kernel = {3: "k_pd_persistent (cooperative, matrix values and the iterate's band in shared memory, "
                     "halo by bulk copies)",
                  2: "k_pd_persistent (cooperative, matrix values in shared memory)",
@@ -456,7 +458,13 @@ def run_ours(args):
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)",
                      "sweep_alone": {"kernel": "one weighted-Jacobi sweep launch (SELL-32) timed alone",
                                      "bytes_per_launch": int(sweep_bytes), "ms_per_launch": round(sweep_ms, 6),
-                                     "achieved": round(sweep_gbs, 1), "frac": round(sweep_gbs / peak, 4)}},
+                                     "achieved": round(sweep_gbs, 1), "frac": round(sweep_gbs / peak, 4)},
+                     "local_alone": {"kernel": "the local step alone: curvature kernel + right-hand-side kernel "
+                                               "with the first sweep fused (k_local_aq_rel + k_local_residual in "
+                                               "the mixed mode), 400 back to back",
+                                     "bytes_per_launch": int(local_bytes), "ms_per_launch": round(local_ms, 6),
+                                     "achieved": round(local_gbs, 1), "frac": round(local_gbs / peak, 4),
+                                     "bytes_rule": "per vertex: 16 d + 68 (local step) + 8 n + 28 (fused sweep)"}},
         "clocks": clk.summary(),
     }
     if fp64 is not None:

@@ -340,6 +340,18 @@ pdipc_status pdipc_stage_pd(pdipc_ctx* ctx, const double* X, const double* V, do
  * inverse diagonal; FP32 sizes, double value sizes in FP64 mode). */
 pdipc_status pdipc_stage_sweep_timing(pdipc_ctx* ctx, int launches, double* avg_ms, double* bytes);
 
+/* Times the local step (solveClothPointsStrainAndBendingConstraintKernel +
+ * solvePointsConstraintKernel, PdIpcGpuFunc.cu:627-790, with the right-hand
+ * side's first Jacobi sweep fused as the per-sweep solve runs it) launched on
+ * its own: the curvature kernel and the right-hand-side kernel, `launches`
+ * times back to back between two CUDA events on the context's stream, at the
+ * current positions (which stay untouched).  *avg_ms = mean duration of one
+ * local step (two launches); *bytes = its algorithmic bytes: per vertex i,
+ * 16 d_i + 68 for the local step (d_i stencil neighbours) plus 8 n_i + 28 for
+ * the fused sweep (n_i matrix off-diagonals; FP32 sizes, double value sizes
+ * in FP64 mode). */
+pdipc_status pdipc_stage_local_timing(pdipc_ctx* ctx, int launches, double* avg_ms, double* bytes);
+
 /* The reference's penalty / discrete-collision contact path
  * (Simulator/PD-IPC/PdIpcGpuFunc.cu:2933-3740).  The reference declares these
  * kernels beside the IPC path, but its step never calls them (PdIpcSimulator.cpp

@@ -411,6 +411,13 @@ pdipc_status pdipc_stage_sweep_timing(pdipc_ctx* ctx, int launches, double* avg_
     return guarded(ctx, [&]() { return ctx->solver->sweep_timing(launches, avg_ms, bytes, ctx->err); });
 }
 
+pdipc_status pdipc_stage_local_timing(pdipc_ctx* ctx, int launches, double* avg_ms, double* bytes) {
+    pdipc_status s = need_init(ctx);
+    if (s != PDIPC_OK) return s;
+    if (!avg_ms || !bytes || launches <= 0) return fail(ctx, PDIPC_ERR_ARG, "bad argument");
+    return guarded(ctx, [&]() { return ctx->solver->local_timing(launches, avg_ms, bytes, ctx->err); });
+}
+
 pdipc_status pdipc_stage_penalty_predict(pdipc_ctx* ctx, const double* X, double* V, double* sn) {
     pdipc_status s = need_init(ctx);
     if (s != PDIPC_OK) return s;

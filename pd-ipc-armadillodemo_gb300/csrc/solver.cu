@@ -233,15 +233,17 @@ public:
         sell_entries_ = (int64_t)H.nPtr[ns];
         {   // algorithmic bytes of one PD solve (the stats field pd_solve_bytes)
             const double V = sizeof(T);
-            double b = 0.0;
+            double b = 0.0, lb = 0.0;
             for (int i = 0; i < ns; ++i) {
                 const double d1 = H.lPtr[i + 1] - H.lPtr[i];  // self + stencil neighbours
                 const double n = H.nPtr[i + 1] - H.nPtr[i];   // matrix off-diagonals
                 const double local = d1 * (4.0 + 3.0 * V) + 2.0 * V + 8.0 + 9.0 * V;
                 const double sweep = n * (4.0 + V) + 7.0 * V;
                 b += local + 2.0 * c_.cheby * sweep + (c_.cheby - 1) * 3.0 * V;
+                lb += local + sweep;
             }
             pd_bytes_ = b * c_.lg;
+            local_bytes_ = lb;
         }
         sell_padded_ = (int64_t)soff[d.nslice];
         PD_CK(up(d.sOff, soff));
@@ -654,6 +656,30 @@ public:
         *avg_ms = (double)ms / launches;
         const double vec = 3.0 * sizeof(T);
         *bytes = (double)sell_entries_ * (sizeof(int) + sizeof(T)) + (double)d_.nsim * (3.0 * vec + sizeof(T));
+        return PDIPC_OK;
+    }
+
+    // The local step of the per-sweep path timed alone: the curvature kernel
+    // and the right-hand-side kernel (residual in the correction form) with
+    // the first Jacobi sweep fused, `launches` times back to back.  Positions
+    // are read, never written.
+    pdipc_status local_timing(int launches, double* avg_ms, double* bytes, std::string& err) override {
+        const T w = (T)c_.relax;
+        auto once = [&]() {
+            launch_local_aq(d_, s_);
+            if constexpr (kCorrection) launch_local_residual(d_, w, s_);
+            else launch_local_rhs_sweep(d_, w, s_);
+        };
+        launch_diag(d_, s_);
+        once();  // warm
+        PD_CK(cudaEventRecord(ev0_, s_));
+        for (int k = 0; k < launches; ++k) once();
+        PD_CK(cudaEventRecord(ev1_, s_));
+        PD_CK(cudaEventSynchronize(ev1_));
+        float ms = 0.f;
+        PD_CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
+        *avg_ms = (double)ms / launches;
+        *bytes = local_bytes_;
         return PDIPC_OK;
     }
 
@@ -1640,7 +1666,7 @@ private:
     OuterGate* gate_ = nullptr;  // the device's stopping test of the outer loop
     double ccd_ms_ = 0.0, contact_ms_ = 0.0;
     double device_ms_ = 0.0;
-    double pd_ms_ = 0.0, pd_bytes_ = 0.0;
+    double pd_ms_ = 0.0, pd_bytes_ = 0.0, local_bytes_ = 0.0;
     int64_t pd_solves_ = 0;
     std::vector<std::pair<void*, size_t>> ptrs_;
     int64_t bytes_ = 0;

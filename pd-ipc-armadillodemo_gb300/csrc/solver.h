@@ -32,6 +32,7 @@ public:
                                        std::string& err) = 0;
     virtual pdipc_status stage_pd(const double* X, const double* V, double* out, std::string& err) = 0;
     virtual pdipc_status sweep_timing(int launches, double* avg_ms, double* bytes, std::string& err) = 0;
+    virtual pdipc_status local_timing(int launches, double* avg_ms, double* bytes, std::string& err) = 0;
     // penalty / discrete-collision stages; kind: 0 CCD candidates, 1 floor, 2 face pairs
     virtual pdipc_status stage_penalty_predict(const double* X, double* V, double* sn, std::string& err) = 0;
     virtual pdipc_status stage_penalty(int kind, const double* x, const double* dir, const int* face_pairs,

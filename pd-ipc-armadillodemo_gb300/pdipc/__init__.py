@@ -37,7 +37,7 @@ EXPORTS = [
     "pdipc_scene_load", "pdipc_scene_model_count", "pdipc_scene_get_model", "pdipc_scene_apply_params",
     "pdipc_scene_add_models", "pdipc_scene_free", "pdipc_stage_penalty_predict", "pdipc_stage_penalty_ccd",
     "pdipc_stage_penalty_floor", "pdipc_stage_penalty_dcd", "pdipc_adjoint_record", "pdipc_adjoint_backward",
-    "pdipc_set_wait_limit",
+    "pdipc_set_wait_limit", "pdipc_stage_local_timing",
 ]
 
 
@@ -113,6 +113,7 @@ def load_library(path: str | None = None):
     L.pdipc_stage_contact.argtypes = [vp, _dp, _dp, _dp, _i64p]
     L.pdipc_stage_pd.argtypes = [vp, _dp, _dp, _dp]
     L.pdipc_stage_sweep_timing.argtypes = [vp, C.c_int, _dp, _dp]
+    L.pdipc_stage_local_timing.argtypes = [vp, C.c_int, _dp, _dp]
     L.pdipc_mesh_topology.argtypes = [_dp, C.c_int, _ip, C.c_int, C.c_int, _ip, C.c_int, _ip, _ip, C.c_int, _ip,
                                       C.c_int, _ip, _ip, _ip]
     if L.pdipc_abi_version() != ABI_VERSION:
@@ -382,6 +383,13 @@ class Simulator:
         ms, b = C.c_double(), C.c_double()
         self._check(load_library().pdipc_stage_sweep_timing(self.h, int(launches), C.byref(ms), C.byref(b)),
                     "pdipc_stage_sweep_timing")
+        return ms.value, b.value
+
+    def local_timing(self, launches=200):
+        """(mean ms, algorithmic bytes) of one local step of the per-sweep path."""
+        ms, b = C.c_double(), C.c_double()
+        self._check(load_library().pdipc_stage_local_timing(self.h, int(launches), C.byref(ms), C.byref(b)),
+                    "pdipc_stage_local_timing")
         return ms.value, b.value
 
     def stage_pd(self, X, V):
