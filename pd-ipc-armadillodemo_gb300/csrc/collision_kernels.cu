@@ -7,9 +7,10 @@
 //                                                      radix sort, k_karras (GPU LBVH build)
 //   updateBvhsBboxesKernel :1506-1561 (1 block)     -> k_refit (bottom-up, atomic arrival flags)
 //   findPatchsICPairsKernel :1699-1732 + thrust scan
-//   + fillCompactPotentialPatchPairListKernel       -> k_traverse (count, scan, write)
-//   computeCcdPatchICPairsVfeeNumKernel :1811 + scan
-//   + getCcdPotentialICPairsListKernel :1838-1948   -> k_pair_counts, k_expand
+//   + fillCompactPotentialPatchPairListKernel
+//   + computeCcdPatchICPairsVfeeNumKernel :1811      -> k_traverse (one stackless pass over escape
+//                                                      links, warp-ballot compaction, record counts)
+//   getCcdPotentialICPairsListKernel :1838-1948     -> k_expand (one warp per 32 pairs)
 //   getImpactOfTimeKernel :2610-2704 + cublasIsamin -> k_toi_* (atomic min, no host copy)
 //   setCollisionConstraintsKernel :2756-2892        -> k_contact_*
 //
@@ -258,6 +259,27 @@ __global__ void k_karras(int n, const unsigned long long* __restrict__ c, int2* 
     parent[right] = i;
 }
 
+// Escape links of the stackless traversal: the node to visit once node c's
+// subtree is done or skipped.  For a left child that is its sibling, else the
+// parent's link; -1 past the root.  Computed once per tree build (refits keep
+// the topology); the walk up is bounded by the tree's depth.
+__global__ void k_escape(int nnodes, const int2* __restrict__ child, const int* __restrict__ parent,
+                         int* __restrict__ escape) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nnodes) return;
+    int x = c, e = -1;
+    for (int up = 0; x > 0 && up < nnodes; ++up) {  // a tree's depth is below its node count
+        const int p = parent[x];
+        const int2 ch = child[p];
+        if (ch.x == x) {
+            e = ch.y;
+            break;
+        }
+        x = p;
+    }
+    escape[c] = e;
+}
+
 template <typename T>
 __device__ __forceinline__ Box6<T> load_box_cg(const Box6<T>* p) {
     Box6<T> b;
@@ -305,96 +327,173 @@ __device__ __forceinline__ bool overlap(const Box6<T>& a, const Box6<T>& b) {
     return true;
 }
 
-constexpr int kStack = 64;
-
-// Per query patch q: every patch p > q whose box overlaps q's, skipping pairs
-// of two static patches (they cannot move or receive contact forces).
+// Stackless traversal, one query patch q per thread: every patch p > q whose
+// box overlaps q's, skipping pairs of two static patches (they cannot move or
+// receive contact forces).  Depth first, left child first, along the escape
+// links.  Each warp appends its lanes' finds by ballot: one atomicAdd per
+// warp and round reserves a contiguous run, so the pair stores coalesce.
+// With each pair it writes the pair's record counts (points(q) x faces(p) +
+// points(p) x faces(q) point-triangle, edges(q) x edges(p) edge-edge,
+// computeCcdPatchICPairsVfeeNumKernel cu:1811-1836).  Finds past `cap` are
+// counted, not written: the caller grows the buffers and runs the pass again.
+// The pair order varies between runs (the order warps reserve their runs);
+// every consumer of the list is order-free or sums with atomics anyway.
 template <typename T>
-__global__ void k_traverse(int n, const Box6<T>* __restrict__ patchBox, const Box6<T>* __restrict__ nodeBox,
-                           const int2* __restrict__ child, const int* __restrict__ leafPatch,
-                           const uint8_t* __restrict__ pStatic, int* __restrict__ counts,
-                           const int* __restrict__ offsets, int2* __restrict__ out, unsigned int* __restrict__ err) {
+__global__ void __launch_bounds__(128) k_traverse(int n, const Box6<T>* __restrict__ patchBox,
+                                                  const Box6<T>* __restrict__ nodeBox,
+                                                  const int2* __restrict__ child, const int* __restrict__ escape,
+                                                  const int* __restrict__ leafPatch,
+                                                  const uint8_t* __restrict__ pStatic, const int* __restrict__ pfPtr,
+                                                  const int* __restrict__ ppPtr, const int* __restrict__ pePtr,
+                                                  int2* __restrict__ out, int64_t* __restrict__ cpt,
+                                                  int64_t* __restrict__ cee, int64_t cap,
+                                                  unsigned long long* __restrict__ count,
+                                                  unsigned int* __restrict__ err) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    int cnt = 0;
-    if (n > 1) {
-        const Box6<T> qb = patchBox[q];
-        const bool qs = pStatic[q] != 0;
-        const int base = out ? offsets[q] : 0;
-        int stack[kStack];
-        int sp = 0;
-        stack[sp++] = 0;
-        while (sp > 0) {
-            const int node = stack[--sp];
-            const int2 ch = child[node];
-            const int cc[2] = {ch.x, ch.y};
-            for (int h = 0; h < 2; ++h) {
-                const int c = cc[h];
-                if (!overlap(qb, nodeBox[c])) continue;
-                if (c >= n - 1) {
-                    const int p = leafPatch[c - (n - 1)];
-                    if (q < p && !(qs && pStatic[p])) {
-                        if (out) out[base + cnt] = make_int2(q, p);
-                        ++cnt;
-                    }
-                } else if (sp < kStack) {
-                    stack[sp++] = c;
+    const unsigned lane = threadIdx.x & 31u;
+    bool active = q < n && n > 1;
+    // a depth-first walk visits each of the 2n-1 nodes at most once
+    int budget = 2 * n;
+    Box6<T> qb{};
+    bool qs = false;
+    int fa = 0, va = 0, ea = 0;
+    if (active) {
+        qb = patchBox[q];
+        qs = pStatic[q] != 0;
+        fa = pfPtr[q + 1] - pfPtr[q];
+        va = ppPtr[q + 1] - ppPtr[q];
+        ea = pePtr[q + 1] - pePtr[q];
+    }
+    int node = 0;
+    while (__any_sync(0xffffffffu, active)) {
+        int found = -1;
+        while (active) {  // to this lane's next find, or to the end of its traversal
+            int next;
+            if (overlap(qb, nodeBox[node])) {
+                if (node >= n - 1) {
+                    const int p = leafPatch[node - (n - 1)];
+                    if (q < p && !(qs && pStatic[p])) found = p;
+                    next = escape[node];
                 } else {
-                    atomicOr(err, (unsigned int)kErrTraversalStack);
+                    next = child[node].x;
                 }
+            } else {
+                next = escape[node];
+            }
+            node = next;
+            if (node < 0) active = false;
+            if (--budget < 0 && active) {  // only a malformed tree gets here
+                atomicOr(err, (unsigned int)kErrTraversal);
+                active = false;
+            }
+            if (found >= 0) break;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, found >= 0);
+        if (m == 0u) continue;
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (found >= 0) {
+            const unsigned long long pos = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
+            if (pos < (unsigned long long)cap) {
+                const int p = found;
+                const int64_t fb = pfPtr[p + 1] - pfPtr[p], vb = ppPtr[p + 1] - ppPtr[p],
+                              eb = pePtr[p + 1] - pePtr[p];
+                out[pos] = make_int2(q, p);
+                cpt[pos] = (int64_t)va * fb + vb * (int64_t)fa;
+                cee[pos] = (int64_t)ea * eb;
             }
         }
     }
-    if (!out) counts[q] = cnt;
 }
 
-__global__ void k_pair_counts(int64_t npairs, const int2* __restrict__ pairs, const int* __restrict__ pfPtr,
-                              const int* __restrict__ ppPtr, const int* __restrict__ pePtr, int64_t* __restrict__ cpt,
-                              int64_t* __restrict__ cee) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= npairs) return;
-    const int2 pr = pairs[t];
-    const int64_t fa = pfPtr[pr.x + 1] - pfPtr[pr.x], fb = pfPtr[pr.y + 1] - pfPtr[pr.y];
-    const int64_t va = ppPtr[pr.x + 1] - ppPtr[pr.x], vb = ppPtr[pr.y + 1] - ppPtr[pr.y];
-    const int64_t ea = pePtr[pr.x + 1] - pePtr[pr.x], eb = pePtr[pr.y + 1] - pePtr[pr.y];
-    cpt[t] = va * fb + vb * fa;
-    cee[t] = ea * eb;
-}
-
-// Expansion of one patch pair (A,B) per warp into point-triangle records
-// (points of A x faces of B, then points of B x faces of A) and edge-edge
-// records (edges of A x edges of B), point-major as in cu:1900-1945.
-__global__ void k_expand(int64_t npairs, const int2* __restrict__ pairs, const int* __restrict__ pfPtr,
-                         const int* __restrict__ pfIdx, const int* __restrict__ ppPtr, const int* __restrict__ ppIdx,
-                         const int* __restrict__ pePtr, const int* __restrict__ peIdx, const int4* __restrict__ Faces,
-                         const int2* __restrict__ Edges, const int64_t* __restrict__ opt,
-                         const int64_t* __restrict__ oee, int4* __restrict__ PT, int4* __restrict__ EE) {
-    const int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Expansion of the patch pairs into point-triangle records (points of A x
+// faces of B, then points of B x faces of A, point-major) and edge-edge
+// records (edges of A x edges of B), as getCcdPotentialICPairsListKernel
+// (cu:1838-1948) lays them out.  A warp takes 32 consecutive pairs, whose
+// records form one contiguous run of each list, and writes the run lane by
+// lane (16-byte records, 512 bytes per warp store); a record finds its pair by
+// a binary search over the lanes' run offsets (shuffles) and the pair's
+// tables by shuffles from the owning lane.
+__global__ void __launch_bounds__(kBlock) k_expand(int64_t npairs, const int2* __restrict__ pairs,
+                                                   const int* __restrict__ pfPtr, const int* __restrict__ pfIdx,
+                                                   const int* __restrict__ ppPtr, const int* __restrict__ ppIdx,
+                                                   const int* __restrict__ pePtr, const int* __restrict__ peIdx,
+                                                   const int4* __restrict__ Faces, const int2* __restrict__ Edges,
+                                                   const int64_t* __restrict__ opt, const int64_t* __restrict__ oee,
+                                                   int4* __restrict__ PT, int4* __restrict__ EE) {
+    constexpr unsigned kAll = 0xffffffffu;
+    const int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) << 5;
     const int lane = threadIdx.x & 31;
-    if (t >= npairs) return;
-    const int2 pr = pairs[t];
-    const int A = pr.x, B = pr.y;
-    const int fa0 = pfPtr[A], fa = pfPtr[A + 1] - fa0, fb0 = pfPtr[B], fb = pfPtr[B + 1] - fb0;
-    const int va0 = ppPtr[A], va = ppPtr[A + 1] - va0, vb0 = ppPtr[B], vb = ppPtr[B + 1] - vb0;
-    const int ea0 = pePtr[A], ea = pePtr[A + 1] - ea0, eb0 = pePtr[B], eb = pePtr[B + 1] - eb0;
-    const int64_t bp = opt[t], be = oee[t];
-    const int nab = va * fb, nba = vb * fa;
-    for (int id = lane; id < nab + nba; id += 32) {
-        int v, f;
-        if (id < nab) {
-            v = ppIdx[va0 + id / fb];
-            f = pfIdx[fb0 + id % fb];
-        } else {
-            const int id2 = id - nab;
-            v = ppIdx[vb0 + id2 / fa];
-            f = pfIdx[fa0 + id2 % fa];
-        }
-        const int4 F = Faces[f];
-        PT[bp + id] = make_int4(v, F.x, F.y, F.z);
+    if (w0 >= npairs) return;  // whole warps only
+    const int64_t t = w0 + lane;
+    const int last = (npairs - w0 < 32 ? (int)(npairs - w0) : 32) - 1;
+    int fa0 = 0, fa = 0, fb0 = 0, fb = 0, va0 = 0, va = 0, vb0 = 0, vb = 0, ea0 = 0, ea = 0, eb0 = 0, eb = 0;
+    int64_t bp = INT64_MAX, be = INT64_MAX;
+    if (lane <= last) {
+        const int2 pr = pairs[t];
+        fa0 = pfPtr[pr.x];
+        fa = pfPtr[pr.x + 1] - fa0;
+        fb0 = pfPtr[pr.y];
+        fb = pfPtr[pr.y + 1] - fb0;
+        va0 = ppPtr[pr.x];
+        va = ppPtr[pr.x + 1] - va0;
+        vb0 = ppPtr[pr.y];
+        vb = ppPtr[pr.y + 1] - vb0;
+        ea0 = pePtr[pr.x];
+        ea = pePtr[pr.x + 1] - ea0;
+        eb0 = pePtr[pr.y];
+        eb = pePtr[pr.y + 1] - eb0;
+        bp = opt[t];
+        be = oee[t];
     }
-    for (int id = lane; id < ea * eb; id += 32) {
-        const int2 a = Edges[peIdx[ea0 + id / eb]], b = Edges[peIdx[eb0 + id % eb]];
-        EE[be + id] = make_int4(a.x, a.y, b.x, b.y);
+    // the owning lane of record r: the largest lane j <= last with start_j <= r
+    auto owner = [&](int64_t start, int64_t r) {
+        int j = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int c = j + step;
+            const int64_t v = __shfl_sync(kAll, start, c & 31);
+            if (c <= last && v <= r) j = c;
+        }
+        return j;
+    };
+    const int nab = va * fb;
+    const int64_t ptBeg = __shfl_sync(kAll, bp, 0);
+    const int64_t ptEnd = __shfl_sync(kAll, bp + (int64_t)nab + (int64_t)vb * fa, last);
+    for (int64_t r0 = ptBeg; r0 < ptEnd; r0 += 32) {
+        const int64_t r = r0 + lane;
+        const int j = owner(bp, r);
+        const int64_t id = r - __shfl_sync(kAll, bp, j);
+        const int jnab = __shfl_sync(kAll, nab, j), jfa = __shfl_sync(kAll, fa, j), jfb = __shfl_sync(kAll, fb, j);
+        const int jfa0 = __shfl_sync(kAll, fa0, j), jfb0 = __shfl_sync(kAll, fb0, j);
+        const int jva0 = __shfl_sync(kAll, va0, j), jvb0 = __shfl_sync(kAll, vb0, j);
+        if (r < ptEnd) {
+            int v, f;
+            if (id < jnab) {
+                v = ppIdx[jva0 + (int)(id / jfb)];
+                f = pfIdx[jfb0 + (int)(id % jfb)];
+            } else {
+                const int id2 = (int)(id - jnab);
+                v = ppIdx[jvb0 + id2 / jfa];
+                f = pfIdx[jfa0 + id2 % jfa];
+            }
+            const int4 F = Faces[f];
+            PT[r] = make_int4(v, F.x, F.y, F.z);
+        }
+    }
+    const int64_t eeBeg = __shfl_sync(kAll, be, 0);
+    const int64_t eeEnd = __shfl_sync(kAll, be + (int64_t)ea * eb, last);
+    for (int64_t r0 = eeBeg; r0 < eeEnd; r0 += 32) {
+        const int64_t r = r0 + lane;
+        const int j = owner(be, r);
+        const int64_t id = r - __shfl_sync(kAll, be, j);
+        const int jeb = __shfl_sync(kAll, eb, j), jea0 = __shfl_sync(kAll, ea0, j),
+                  jeb0 = __shfl_sync(kAll, eb0, j);
+        if (r < eeEnd) {
+            const int2 a = Edges[peIdx[jea0 + (int)(id / jeb)]], b = Edges[peIdx[jeb0 + (int)(id % jeb)]];
+            EE[r] = make_int4(a.x, a.y, b.x, b.y);
+        }
     }
 }
 
@@ -858,6 +957,8 @@ template <typename T, typename TC>
 void launch_karras(const Dev<T, TC>& d, const unsigned long long* sorted, cudaStream_t s) {
     if (d.npatch == 0) return;
     k_karras<<<blocks_for(d.npatch), kBlock, 0, s>>>(d.npatch, sorted, d.NodeChild, d.NodeParent);
+    k_escape<<<blocks_for(2 * (int64_t)d.npatch - 1), kBlock, 0, s>>>(2 * d.npatch - 1, d.NodeChild, d.NodeParent,
+                                                                     d.NodeEscape);
 }
 template <typename T, typename TC>
 void launch_refit(const Dev<T, TC>& d, cudaStream_t s) {
@@ -867,16 +968,12 @@ void launch_refit(const Dev<T, TC>& d, cudaStream_t s) {
                                                        d.NodeParent, d.RefitFlag);
 }
 template <typename T, typename TC>
-void launch_traverse(const Dev<T, TC>& d, int* counts, const int* offsets, int2* out, cudaStream_t s) {
+void launch_traverse(const Dev<T, TC>& d, int64_t* cpt, int64_t* cee, int64_t cap, unsigned long long* count,
+                     cudaStream_t s) {
     if (d.npatch == 0) return;
     k_traverse<T><<<blocks_for(d.npatch, 128), 128, 0, s>>>(d.npatch, d.PatchBox, d.NodeBox, d.NodeChild,
-                                                            d.LeafPatch, d.pStatic, counts, offsets, out,
-                                                            d.ErrFlags);
-}
-template <typename T, typename TC>
-void launch_pair_counts(const Dev<T, TC>& d, int64_t* cpt, int64_t* cee, cudaStream_t s) {
-    if (d.nPairs == 0) return;
-    k_pair_counts<<<blocks_for(d.nPairs), kBlock, 0, s>>>(d.nPairs, d.Pairs, d.pfPtr, d.ppPtr, d.pePtr, cpt, cee);
+                                                            d.NodeEscape, d.LeafPatch, d.pStatic, d.pfPtr, d.ppPtr,
+                                                            d.pePtr, d.Pairs, cpt, cee, cap, count, d.ErrFlags);
 }
 template <typename T, typename TC>
 void launch_expand(const Dev<T, TC>& d, const int64_t* opt, const int64_t* oee, cudaStream_t s) {
@@ -956,8 +1053,8 @@ cudaError_t toi_scratch(ToiScratch* out) {
     template void launch_morton<T, TC>(const Dev<T, TC>&, T*, unsigned long long*, int*, cudaStream_t);     \
     template void launch_karras<T, TC>(const Dev<T, TC>&, const unsigned long long*, cudaStream_t);           \
     template void launch_refit<T, TC>(const Dev<T, TC>&, cudaStream_t);                                       \
-    template void launch_traverse<T, TC>(const Dev<T, TC>&, int*, const int*, int2*, cudaStream_t);           \
-    template void launch_pair_counts<T, TC>(const Dev<T, TC>&, int64_t*, int64_t*, cudaStream_t);             \
+    template void launch_traverse<T, TC>(const Dev<T, TC>&, int64_t*, int64_t*, int64_t, unsigned long long*,  \
+                                         cudaStream_t);                                                        \
     template void launch_expand<T, TC>(const Dev<T, TC>&, const int64_t*, const int64_t*, cudaStream_t);      \
     template void launch_toi<T, TC>(const Dev<T, TC>&, Pos<T, TC>, Pos<T, TC>, const SolverConsts&, TC*,      \
                                     TC*, cudaStream_t);                                                       \

@@ -149,7 +149,7 @@ __device__ __forceinline__ float diff_ff(float hj, float lj, float hi, float li)
 // Device-side error flags (bit mask), read back by the host after a step.
 enum ErrFlag : unsigned int {
     kErrNonFinite = 1u,
-    kErrTraversalStack = 2u,
+    kErrTraversal = 2u,
     kErrPairOverflow = 4u,
     kErrCandidateOverflow = 8u,
     kErrBarrier = 16u,  // a grid barrier of the persistent solve timed out

@@ -102,6 +102,7 @@ struct Dev {
     Box6<T>* NodeBox = nullptr;    // [2 npatch - 1]
     int2* NodeChild = nullptr;     // [npatch - 1]
     int* NodeParent = nullptr;     // [2 npatch - 1]
+    int* NodeEscape = nullptr;     // [2 npatch - 1] next node once this subtree is done (-1: end)
     int* LeafPatch = nullptr;      // [npatch] sorted order: leaf k -> patch id
     int* RefitFlag = nullptr;      // [npatch - 1]
     unsigned long long* Morton = nullptr;  // [npatch] codes by patch id
@@ -109,6 +110,7 @@ struct Dev {
     // candidates of the current step
     int2* Pairs = nullptr;
     int64_t capPairs = 0;
+    unsigned long long* PairCount = nullptr;  // pairs found by the last traversal
     int4* PT = nullptr;
     int64_t capPT = 0;
     int4* EE = nullptr;
@@ -202,11 +204,11 @@ template <typename T, typename TC>
 void launch_karras(const Dev<T, TC>& d, const unsigned long long* sorted_codes, cudaStream_t s);
 template <typename T, typename TC>
 void launch_refit(const Dev<T, TC>& d, cudaStream_t s);
-// count (out_pairs == null) or write overlapping patch pairs
+// overlapping patch pairs into d.Pairs[0, cap) with their point-triangle and
+// edge-edge record counts; *count (zeroed by the caller) gets the full number
 template <typename T, typename TC>
-void launch_traverse(const Dev<T, TC>& d, int* counts, const int* offsets, int2* out_pairs, cudaStream_t s);
-template <typename T, typename TC>
-void launch_pair_counts(const Dev<T, TC>& d, int64_t* cnt_pt, int64_t* cnt_ee, cudaStream_t s);
+void launch_traverse(const Dev<T, TC>& d, int64_t* cnt_pt, int64_t* cnt_ee, int64_t cap, unsigned long long* count,
+                     cudaStream_t s);
 template <typename T, typename TC>
 void launch_expand(const Dev<T, TC>& d, const int64_t* off_pt, const int64_t* off_ee, cudaStream_t s);
 template <typename T, typename TC>

@@ -274,11 +274,11 @@ public:
         PD_CK(zeros(d.NodeBox, 2 * np));
         PD_CK(zeros(d.NodeChild, np));
         PD_CK(zeros(d.NodeParent, 2 * np));
+        PD_CK(zeros(d.NodeEscape, 2 * np));
+        PD_CK(zeros(d.PairCount, 1));
         PD_CK(zeros(d.LeafPatch, np));
         PD_CK(zeros(d.RefitFlag, np));
         PD_CK(zeros(d.Morton, np));
-        PD_CK(zeros(cnt_, np + 1));
-        PD_CK(zeros(off_, np + 1));
 
         // ---- scalars ----
         PD_CK(zeros(d.ToiMin, 1));
@@ -1384,37 +1384,40 @@ private:
             if (r != PDIPC_OK) return r;
         }
         launch_refit(d, s_);
-        launch_traverse(d, cnt_, nullptr, nullptr, s_);
-        launches_ += 2;
-        pdipc_status r = ensure_scan_tmp(d.npatch + 1, err);
-        if (r != PDIPC_OK) return r;
-        scan_exclusive_i32(cnt_, off_, d.npatch, &off_[d.npatch], (int*)scan_tmp_, s_);
-        launches_ += 2;
-        PD_CK(cudaMemcpyAsync(&pin_->n_pair_total_i32, &off_[d.npatch], sizeof(int), cudaMemcpyDeviceToHost, s_));
-        PD_CK(cudaStreamSynchronize(s_));
-        d.nPairs = pin_->n_pair_total_i32;
-        if (d.nPairs == 0) return PDIPC_OK;
-        const int64_t capBefore = d.capPairs;
-        PD_CK(grow(d.Pairs, d.capPairs, d.nPairs));
-        if (d.capPairs != capBefore || !cpt_) {
-            int64_t c1 = 0, c2 = 0, c3 = 0, c4 = 0;
-            if (cpt_) { dfree(cpt_); dfree(cee_); dfree(opt_); dfree(oee_); }
-            PD_CK(grow(cpt_, c1, d.capPairs));
-            PD_CK(grow(cee_, c2, d.capPairs));
-            PD_CK(grow(opt_, c3, d.capPairs + 1));
-            PD_CK(grow(oee_, c4, d.capPairs + 1));
+        ++launches_;
+        // One traversal writes the pairs and their record counts; the counts
+        // are scanned over the whole buffer (entries past the pairs found stay
+        // zero), so one read gives the pair and record totals.  When the pairs
+        // overflow the buffer it grows and the traversal runs again.
+        if (d.capPairs < 1) PD_CK(grow(d.Pairs, d.capPairs, 8 * (int64_t)d.npatch));
+        for (;;) {
+            if (!cpt_ || cptCap_ != d.capPairs) {
+                if (cpt_) { dfree(cpt_); dfree(cee_); dfree(opt_); dfree(oee_); }
+                int64_t c1 = 0, c2 = 0, c3 = 0, c4 = 0;
+                PD_CK(grow(cpt_, c1, d.capPairs));
+                PD_CK(grow(cee_, c2, d.capPairs));
+                PD_CK(grow(opt_, c3, d.capPairs + 1));
+                PD_CK(grow(oee_, c4, d.capPairs + 1));
+                cptCap_ = d.capPairs;
+            }
+            pdipc_status r = ensure_scan_tmp(d.capPairs + 1, err);
+            if (r != PDIPC_OK) return r;
+            PD_CK(cudaMemsetAsync(d.PairCount, 0, sizeof(unsigned long long), s_));
+            PD_CK(cudaMemsetAsync(cpt_, 0, sizeof(int64_t) * d.capPairs, s_));
+            PD_CK(cudaMemsetAsync(cee_, 0, sizeof(int64_t) * d.capPairs, s_));
+            launch_traverse(d, cpt_, cee_, d.capPairs, d.PairCount, s_);
+            scan_exclusive_i64(cpt_, opt_, d.capPairs, opt_ + d.capPairs, scan_tmp_, s_);
+            scan_exclusive_i64(cee_, oee_, d.capPairs, oee_ + d.capPairs, scan_tmp_, s_);
+            launches_ += 5;
+            PD_CK(cudaMemcpyAsync(&pin_->n_pairs, d.PairCount, sizeof(int64_t), cudaMemcpyDeviceToHost, s_));
+            PD_CK(cudaMemcpyAsync(&pin_->n_pt, opt_ + d.capPairs, sizeof(int64_t), cudaMemcpyDeviceToHost, s_));
+            PD_CK(cudaMemcpyAsync(&pin_->n_ee, oee_ + d.capPairs, sizeof(int64_t), cudaMemcpyDeviceToHost, s_));
+            PD_CK(cudaStreamSynchronize(s_));
+            d.nPairs = pin_->n_pairs;
+            if (d.nPairs <= d.capPairs) break;
+            PD_CK(grow(d.Pairs, d.capPairs, d.nPairs + d.nPairs / 4));
         }
-        launch_traverse(d, nullptr, off_, d.Pairs, s_);
-        launch_pair_counts(d, cpt_, cee_, s_);
-        launches_ += 2;
-        r = ensure_scan_tmp(d.nPairs + 1, err);
-        if (r != PDIPC_OK) return r;
-        scan_exclusive_i64(cpt_, opt_, d.nPairs, opt_ + d.nPairs, scan_tmp_, s_);
-        scan_exclusive_i64(cee_, oee_, d.nPairs, oee_ + d.nPairs, scan_tmp_, s_);
-        launches_ += 4;
-        PD_CK(cudaMemcpyAsync(&pin_->n_pt, opt_ + d.nPairs, sizeof(int64_t), cudaMemcpyDeviceToHost, s_));
-        PD_CK(cudaMemcpyAsync(&pin_->n_ee, oee_ + d.nPairs, sizeof(int64_t), cudaMemcpyDeviceToHost, s_));
-        PD_CK(cudaStreamSynchronize(s_));
+        if (d.nPairs == 0) return PDIPC_OK;
         d.nPT = pin_->n_pt;
         d.nEE = pin_->n_ee;
         PD_CK(grow(d.PT, d.capPT, d.nPT));
@@ -1648,7 +1651,7 @@ private:
                 err = "non-finite position after the step";
                 return PDIPC_ERR_NONFINITE;
             }
-            err = "broad-phase traversal stack overflow";
+            err = "broad-phase traversal ran past its node budget (malformed patch tree)";
             return PDIPC_ERR_OVERFLOW;
         }
         return PDIPC_OK;
@@ -1683,8 +1686,7 @@ private:
     int* vModel_ = nullptr;
     V4<T>* sh_ = nullptr;  // float-float mirror of scratch_ (correction form)
     V4<T>* sl_ = nullptr;
-    int* cnt_ = nullptr;
-    int* off_ = nullptr;
+    int64_t cptCap_ = 0;  // pair capacity the record-count buffers below were sized for
     int64_t* cpt_ = nullptr;
     int64_t* cee_ = nullptr;
     int64_t* opt_ = nullptr;
