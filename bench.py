@@ -260,7 +260,10 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     dist = init_dist(ws, "nccl")
     sc = workload(args.config, args.scene)
-    sim = pdipc.Simulator(sc, args.precision, device=local)
+    # the launch configuration is chosen by the library's autotuner at
+    # initialize (untimed), unless --no-autotune
+    sim = pdipc.Simulator(sc, args.precision, device=local, autotune=0 if args.no_autotune else 1)
+    tuning = sim.tuning()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     sim.step(args.warmup)                    # captures the graph, grows candidate buffers
@@ -467,6 +470,7 @@ def run_ours(args):
                                      "bytes_rule": "per vertex: 16 d + 68 (local step) + 8 n + 28 (fused sweep)"}},
         "clocks": clk.summary(),
     }
+    res["tuning"] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in tuning.items()}
     if fp64 is not None:
         res["fp64_gpu"] = fp64
     if fp32 is not None:
@@ -580,6 +584,7 @@ def main(argv=None):
                     help="first step of the contact-phase window timed after the headline run")
     ap.add_argument("--contact-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="run the built-in launch configuration")
     ap.add_argument("--cpu-steps", type=int, default=3, help="whole steps in the GPU arm's cpu_baseline sample")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--ref-budget-s", type=float, default=300.0,

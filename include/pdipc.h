@@ -134,6 +134,30 @@ typedef struct {
     double contact_ms;           /* device time of the contact-constraint passes of the last call */
 } pdipc_stats;
 
+/* Launch configuration a context runs with, and how it was chosen (no
+ * counterpart in the reference, whose launch shapes are fixed macros:
+ * PdIpcGpuFunc.cuh:133-134, PdIpcSimulator.cpp:418-431, 1121-1137). */
+typedef struct {
+    int32_t autotuned;          /* 1: chosen by timing candidates at pdipc_initialize (params.autotune) */
+    int32_t from_cache;         /* 1: taken from an earlier context of the same shape in this process */
+    int32_t pd_rows_per_thread; /* persistent PD solve: rows per thread (slices per warp); 0: one launch
+                                   per sweep */
+    int32_t pd_ctas;            /* CTAs of the persistent solve */
+    int32_t pd_band;            /* 1: the iterate's column band in shared memory */
+    int32_t pd_l1_gather;       /* 1: gathers through L1 */
+    int32_t pd_local_sync;      /* 1: neighbour waits, 0: grid barriers */
+    int32_t cand_grid;          /* blocks of the time-of-impact and contact kernels (grid-stride) */
+    int32_t traverse_block;     /* threads per block of the broad-phase traversal */
+    int32_t expand_block;       /* threads per block of the candidate expansion */
+    int32_t candidates_timed;   /* configurations the autotuner timed */
+    int32_t reserved0;
+    double pd_solve_ms;         /* one outer iteration's PD solve, chosen configuration (0: not timed) */
+    double pd_default_ms;       /* the same with the default configuration */
+    double collision_ms;        /* broad phase + time of impact + contact, chosen shapes */
+    double collision_default_ms;/* the same with the default shapes */
+    int32_t reserved[8];
+} pdipc_tuning;
+
 /* Fill *p with the reference defaults listed beside each field. */
 void pdipc_default_params(pdipc_params* p);
 
@@ -149,6 +173,39 @@ pdipc_status pdipc_create(const pdipc_params* p, pdipc_ctx** out);
 pdipc_status pdipc_add_cloth(pdipc_ctx* ctx, const double* X, int nv, const int* F, int nf,
                              double density, double k_stretch, double k_bend,
                              const int* pins, int npins, double k_pin, int patch_dim);
+
+/* Options of pdipc_add_cloth_ex beyond pdipc_add_cloth's. */
+typedef struct {
+    /* nf per-triangle stretch stiffnesses, or NULL for k_stretch everywhere.  The
+     * reference weighs a vertex's springs by one per-vertex stiffness
+     * (devStrainStiffness[offset], PdIpcGpuFunc.cu:673), so a vertex takes the mean
+     * over its triangles. */
+    const double* per_tri_stretch;
+    /* Triangle strain limit: each triangle (where the stiffness is > 0) gets the
+     * strain constraint of solveVolumetricStrainConstraintKernel (PdIpcGpuFunc.cu:
+     * 439-599) on its 3 x 2 deformation gradient F = Ds Dm^-1: a 3 x 3 SVD (F with
+     * the deformed unit normal as third column), singular values clamped to
+     * [0.999, 1.001], weight = stiffness x rest area.  k_tri_strain applies to
+     * every triangle, per_tri_strain (nf values, or NULL) overrides it.  The
+     * reference applies this constraint to tets only. */
+    double k_tri_strain;
+    const double* per_tri_strain;
+    int32_t reserved[8];
+} pdipc_cloth_options;
+
+/* pdipc_add_cloth with the options above (opt may be NULL: pdipc_add_cloth). */
+pdipc_status pdipc_add_cloth_ex(pdipc_ctx* ctx, const double* X, int nv, const int* F, int nf, double density,
+                                double k_stretch, double k_bend, const int* pins, int npins, double k_pin,
+                                int patch_dim, const pdipc_cloth_options* opt);
+
+/* Chain rule of the per-triangle stretch mapping, on the host: given the
+ * gradient of a loss with respect to every simulated vertex's stretch stiffness
+ * (dl_dvertex, n_sim, as pdipc_adjoint_backward returns it), the gradient with
+ * respect to the per-triangle stretch stiffnesses of the cloth added
+ * `cloth_index`-th (0-based among cloths): dl/dk_t = sum over t's vertices i of
+ * dl/dk_i / (triangles at i).  dl_dtri: nf of that cloth. */
+pdipc_status pdipc_stretch_gradient_per_triangle(pdipc_ctx* ctx, int cloth_index, const double* dl_dvertex,
+                                                 double* dl_dtri);
 
 /* Add a simulated tetrahedral (volumetric) model: PdIpcSimulator::addModelFromConfigFile
  * with <type> 1 k_strain k_volume k_pin, <density>, <patchDim> (PdIpcSimulator.h:462-534,
@@ -250,6 +307,9 @@ pdipc_status pdipc_set_state(pdipc_ctx* ctx, const double* X, const double* V);
 pdipc_status pdipc_reset(pdipc_ctx* ctx);
 
 pdipc_status pdipc_get_stats(pdipc_ctx* ctx, pdipc_stats* out);
+
+/* The launch configuration of an initialised context (see pdipc_tuning). */
+pdipc_status pdipc_get_tuning(pdipc_ctx* ctx, pdipc_tuning* out);
 
 /* PdIpcSimulator::saveSimulator(frame) (PdIpcSimulator.h:879-916): writes the
  * EigenMatrixIO::write_binary layout (int64 rows=3, int64 cols=n_total, float32

@@ -37,10 +37,13 @@ def lib():
         L.orc_destroy.argtypes = [C.c_void_p]
         L.orc_add_cloth.argtypes = [C.c_void_p, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double,
                                     C.c_double, _ip, C.c_int, C.c_double, C.c_int]
+        L.orc_add_cloth_ex.argtypes = [C.c_void_p, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double,
+                                       C.c_double, _ip, C.c_int, C.c_double, C.c_int, _dp, C.c_double, _dp]
         L.orc_add_static.argtypes = [C.c_void_p, _dp, C.c_int, _ip, C.c_int, C.c_int]
         L.orc_add_volumetric.argtypes = [C.c_void_p, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double, _ip,
                                          C.c_int, C.c_double, C.c_int]
         L.orc_tet_project.argtypes = [C.c_int, _dp, _dp, _dp, _dp]
+        L.orc_tri_project.argtypes = [C.c_int, _dp, _dp, _dp, _dp]
         L.orc_svd3.argtypes = [_dp, _dp, _dp, _dp]
         L.orc_tet_surface.argtypes = [_dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip]
         L.orc_initialize.argtypes = [C.c_void_p]
@@ -102,8 +105,14 @@ class Oracle:
             X = np.ascontiguousarray(c.X, dtype=np.float64)
             F = np.ascontiguousarray(c.F, dtype=np.int32)
             P = np.ascontiguousarray(c.pins, dtype=np.int32)
-            _check(L.orc_add_cloth(self.h, _d(X), X.shape[0], _i(F), F.shape[0], c.density, c.k_stretch,
-                                   c.k_bend, _i(P), P.shape[0], c.k_pin, c.patch_dim), "add_cloth")
+            ts, tk = getattr(c, "tri_stretch", None), getattr(c, "tri_strain", None)
+            ts = None if ts is None else np.ascontiguousarray(ts, dtype=np.float64)
+            tk = None if tk is None else np.ascontiguousarray(tk, dtype=np.float64)
+            self._keep += [a for a in (ts, tk) if a is not None]
+            _check(L.orc_add_cloth_ex(self.h, _d(X), X.shape[0], _i(F), F.shape[0], c.density, c.k_stretch,
+                                      c.k_bend, _i(P), P.shape[0], c.k_pin, c.patch_dim,
+                                      None if ts is None else _d(ts), float(getattr(c, "k_tri_strain", 0.0)),
+                                      None if tk is None else _d(tk)), "add_cloth")
         for v in getattr(scene, "solids", []):
             X = np.ascontiguousarray(v.X, dtype=np.float64)
             T = np.ascontiguousarray(v.T, dtype=np.int32)
@@ -309,6 +318,17 @@ def tet_project(x, idm, w):
     w = np.ascontiguousarray(w, dtype=np.float64)
     out = np.empty((x.shape[0], 4, 3), np.float64)
     _check(lib().orc_tet_project(x.shape[0], _d(x), _d(idm), _d(w), _d(out)), "tet_project")
+    return out
+
+
+def tri_project(x, idm, w):
+    """The oracle's triangle strain projection on its own: x (n, 3, 3) vertex
+    positions, idm (n, 2, 2) row-major Dm^-1, w (n,) -> (n, 3, 3) = w P G per vertex."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    idm = np.ascontiguousarray(idm, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    out = np.empty((x.shape[0], 3, 3), np.float64)
+    _check(lib().orc_tri_project(x.shape[0], _d(x), _d(idm), _d(w), _d(out)), "tri_project")
     return out
 
 

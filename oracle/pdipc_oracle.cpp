@@ -276,6 +276,10 @@ struct ModelIn {
     bool is_static = false;
     bool is_volumetric = false;
     double density = 0, k_stretch = 0, k_bend = 0, k_pin = 0, k_strain = 0;
+    // cloth: per-triangle stretch (a vertex takes the mean over its triangles)
+    // and per-triangle strain limits (the tet constraint on a triangle)
+    std::vector<double> tri_stretch, tri_strain;
+    double k_tri_strain = 0;
     std::vector<int> pins;
     int patch_dim = 10;
 };
@@ -396,6 +400,44 @@ static void tet_project(const R* x0, const R* x1, const R* x2, const R* x3, cons
     }
     for (int c = 0; c < 4; ++c)
         for (int r = 0; r < 3; ++r) out[c][r] = w * (Rm[3 * r] * G[0][c] + Rm[3 * r + 1] * G[1][c] + Rm[3 * r + 2] * G[2][c]);
+}
+
+// The same strain limit on a cloth triangle (no reference counterpart: the
+// reference applies it to tets): F = Ds Dm^-1 (3 x 2, Dm the rest edges in the
+// rest triangle's orthonormal frame, idm row-major 2 x 2) with the deformed
+// unit normal appended as a third column, so F has singular values
+// (s0, s1, 1) and a positive determinant (the AutoFlipSVD convention needs no
+// flip, AutoFlipSVD.h:253-309); clamped to [0.999, 1.001]; the first two
+// columns P of U S' V^T are the projection; out[c] = w P G[c], G = S Dm^-1
+// with S the edge-selection rows (-1, -1), (1, 0), (0, 1).
+template <typename R>
+static void tri_project(const R* x0, const R* x1, const R* x2, const R* idm, R w, R out[4][3]) {
+    R F[9];
+    for (int k = 0; k < 3; ++k) {
+        const R a = x1[k] - x0[k], b = x2[k] - x0[k];
+        F[3 * k + 0] = a * idm[0] + b * idm[2];
+        F[3 * k + 1] = a * idm[1] + b * idm[3];
+    }
+    R n[3] = {F[3] * F[7] - F[6] * F[4], F[6] * F[1] - F[0] * F[7], F[0] * F[4] - F[3] * F[1]};
+    const R nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int k = 0; k < 3; ++k) F[3 * k + 2] = nn > R(0) ? n[k] / nn : R(0);
+    R U[9], sv[3], V[9];
+    svd3_onesided(F, U, sv, V);
+    R sc[3];
+    for (int k = 0; k < 3; ++k) {
+        const R a = sv[k] < R(0) ? -sv[k] : sv[k];
+        R r = a < R(1.001) ? a : R(1.001);
+        sc[k] = r < R(0.999) ? R(0.999) : r;
+        if (sv[k] < R(0)) sc[k] = -sc[k];
+    }
+    R P[3][2];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 2; ++j)
+            P[i][j] = U[3 * i] * sc[0] * V[3 * j] + U[3 * i + 1] * sc[1] * V[3 * j + 1] + U[3 * i + 2] * sc[2] * V[3 * j + 2];
+    const R G[3][2] = {{-(idm[0] + idm[2]), -(idm[1] + idm[3])}, {idm[0], idm[1]}, {idm[2], idm[3]}};
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) out[c][r] = w * (P[r][0] * G[c][0] + P[r][1] * G[c][1]);
+    out[3][0] = out[3][1] = out[3][2] = R(0);
 }
 
 // Morton code of a quantised, centred patch centre.  The reference calls the
@@ -643,12 +685,55 @@ struct Sim {
                     cotw[e] += -0.5 * (1.0 / std::tan(th));
                 }
             }
+            // per-vertex stretch weight: k_stretch, or the mean of the vertex's
+            // triangles' stiffnesses (the reference's weight is per vertex,
+            // PdIpcGpuFunc.cu:673)
+            std::vector<double> kv(m.nv, m.k_stretch);
+            if (!m.tri_stretch.empty()) {
+                std::vector<int> nt(m.nv, 0);
+                std::fill(kv.begin(), kv.end(), 0.0);
+                for (int f = 0; f < m.nf; ++f)
+                    for (int k = 0; k < 3; ++k) {
+                        kv[t.faces[f][k]] += m.tri_stretch[f];
+                        ++nt[t.faces[f][k]];
+                    }
+                for (int i = 0; i < m.nv; ++i) kv[i] = nt[i] ? kv[i] / nt[i] : m.k_stretch;
+            }
             for (int i = 0; i < m.nv; ++i) {
                 int g = o + i;
                 massD[g] = area[i] * m.density;
                 invMass[g] = (T)(1.0 / massD[g]);
                 bendArea[g] = area[i] * m.k_bend;
-                strainD[g] = m.k_stretch;
+                strainD[g] = kv[i];
+            }
+            // triangle strain limits: element (v0, v1, v2, -1), Dm^-1 (2 x 2) of the
+            // rest edges in the rest triangle's orthonormal frame, weight k x area
+            if (m.k_tri_strain > 0.0 || !m.tri_strain.empty()) {
+                for (int f = 0; f < m.nf; ++f) {
+                    const double kf = m.tri_strain.empty() ? m.k_tri_strain : m.tri_strain[f];
+                    if (!(kf > 0.0)) continue;
+                    const auto& F = t.faces[f];
+                    double a[3], b[3];
+                    for (int k = 0; k < 3; ++k) { a[k] = P(F[1], k) - P(F[0], k); b[k] = P(F[2], k) - P(F[0], k); }
+                    const double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+                    const double la = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+                    const double ln = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+                    if (!(la > 0.0) || !(ln > 0.0)) return PDIPC_ERR_ARG;
+                    double e1[3], e2[3];
+                    for (int k = 0; k < 3; ++k) e1[k] = a[k] / la;
+                    e2[0] = (n[1] * e1[2] - n[2] * e1[1]) / ln;
+                    e2[1] = (n[2] * e1[0] - n[0] * e1[2]) / ln;
+                    e2[2] = (n[0] * e1[1] - n[1] * e1[0]) / ln;
+                    const double d00 = a[0] * e1[0] + a[1] * e1[1] + a[2] * e1[2];
+                    const double d01 = b[0] * e1[0] + b[1] * e1[1] + b[2] * e1[2];
+                    const double d10 = a[0] * e2[0] + a[1] * e2[1] + a[2] * e2[2];
+                    const double d11 = b[0] * e2[0] + b[1] * e2[1] + b[2] * e2[2];
+                    const double det = d00 * d11 - d01 * d10;
+                    const double idm[9] = {d11 / det, -d01 / det, -d10 / det, d00 / det, 0, 0, 0, 0, 0};
+                    for (double v : idm) tetIdmD.push_back(v);
+                    tets.push_back({o + F[0], o + F[1], o + F[2], -1});
+                    tetWD.push_back(kf * 0.5 * ln);
+                }
             }
             for (int i = 0; i < m.nv; ++i) {
                 int g = o + i;
@@ -680,7 +765,7 @@ struct Sim {
                 curvNorm[g] = (T)std::sqrt(cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2]);
                 for (int k = 0; k < deg + 1; ++k) {
                     lNbr.push_back(nb[k]);
-                    lStrain.push_back((T)m.k_stretch);
+                    lStrain.push_back((T)kv[i]);
                     lRest.push_back((T)rl[k]);
                     lLbo.push_back((T)lbo[k]);
                     lBend.push_back((T)(lbo[k] * m.k_bend * area[i]));
@@ -736,13 +821,22 @@ struct Sim {
         ntet = (int)tets.size();
         for (int e = 0; e < ntet; ++e) {
             const double* idm = &tetIdmD[9 * (size_t)e];
-            double G[3][4];
-            for (int i = 0; i < 3; ++i) {
-                G[i][1] = idm[i]; G[i][2] = idm[3 + i]; G[i][3] = idm[6 + i];
-                G[i][0] = -(G[i][1] + G[i][2] + G[i][3]);
+            const bool tri = tets[e][3] < 0;  // triangle element: G^T = S Dm^-1 (3 x 2)
+            double G[3][4] = {};
+            if (tri) {
+                for (int j = 0; j < 2; ++j) {
+                    G[j][1] = idm[j]; G[j][2] = idm[2 + j];
+                    G[j][0] = -(G[j][1] + G[j][2]);
+                }
+            } else {
+                for (int i = 0; i < 3; ++i) {
+                    G[i][1] = idm[i]; G[i][2] = idm[3 + i]; G[i][3] = idm[6 + i];
+                    G[i][0] = -(G[i][1] + G[i][2] + G[i][3]);
+                }
             }
-            for (int r = 0; r < 4; ++r)
-                for (int c = 0; c < 4; ++c) {
+            const int nvert = tri ? 3 : 4;
+            for (int r = 0; r < nvert; ++r)
+                for (int c = 0; c < nvert; ++c) {
                     double v = 0.0;
                     for (int k = 0; k < 3; ++k) v += G[k][r] * G[k][c];
                     v *= tetWD[e];
@@ -754,12 +848,14 @@ struct Sim {
         tetIdm.assign(tetIdmD.begin(), tetIdmD.end());
         tetW.assign(tetWD.begin(), tetWD.end());
         vtPtr.assign(nsim + 1, 0);
-        for (auto& q : tets) for (int k = 0; k < 4; ++k) ++vtPtr[q[k] + 1];
+        for (auto& q : tets) for (int k = 0; k < 4; ++k) if (q[k] >= 0) ++vtPtr[q[k] + 1];
         for (int i = 0; i < nsim; ++i) vtPtr[i + 1] += vtPtr[i];
         vtIdx.assign(vtPtr[nsim], 0);
         {
             std::vector<int> fill(vtPtr.begin(), vtPtr.end() - 1);
-            for (int e = 0; e < ntet; ++e) for (int k = 0; k < 4; ++k) vtIdx[fill[tets[e][k]]++] = 4 * e + k;
+            for (int e = 0; e < ntet; ++e)
+                for (int k = 0; k < 4; ++k)
+                    if (tets[e][k] >= 0) vtIdx[fill[tets[e][k]]++] = 4 * e + k;
         }
         tetOut.assign(12 * (size_t)ntet, T(0));
         Delastic.assign(nsim, T(0));
@@ -1366,10 +1462,14 @@ struct Sim {
         }
 #pragma omp parallel for schedule(static) num_threads(threads)
         for (int e = 0; e < ntet; ++e) {
-            T out[4][3];
+            T out[4][3] = {};
             const auto& q = tets[e];
-            tet_project<T>(&X[3 * (size_t)q[0]], &X[3 * (size_t)q[1]], &X[3 * (size_t)q[2]], &X[3 * (size_t)q[3]],
-                           &tetIdm[9 * (size_t)e], tetW[e], out);
+            if (q[3] < 0)
+                tri_project<T>(&X[3 * (size_t)q[0]], &X[3 * (size_t)q[1]], &X[3 * (size_t)q[2]], &tetIdm[9 * (size_t)e],
+                               tetW[e], out);
+            else
+                tet_project<T>(&X[3 * (size_t)q[0]], &X[3 * (size_t)q[1]], &X[3 * (size_t)q[2]],
+                               &X[3 * (size_t)q[3]], &tetIdm[9 * (size_t)e], tetW[e], out);
             for (int c = 0; c < 4; ++c)
                 for (int k = 0; k < 3; ++k) tetOut[12 * (size_t)e + 3 * c + k] = out[c][k];
         }
@@ -2283,6 +2383,19 @@ int orc_tet_project(int n, const double* x, const double* idm, const double* w, 
     return PDIPC_OK;
 }
 
+// The triangle strain projection for n triangles: x (9 per triangle: the three
+// vertices), idm (4 per triangle, row-major Dm^-1), w (n); out (9 per triangle:
+// the three vertices' contributions), FP64.
+int orc_tri_project(int n, const double* x, const double* idm, const double* w, double* out) {
+    for (int e = 0; e < n; ++e) {
+        double o[4][3];
+        orc::tri_project<double>(x + 9 * (size_t)e, x + 9 * (size_t)e + 3, x + 9 * (size_t)e + 6, idm + 4 * (size_t)e,
+                                 w[e], o);
+        for (int c = 0; c < 3; ++c)
+            for (int k = 0; k < 3; ++k) out[9 * (size_t)e + 3 * c + k] = o[c][k];
+    }
+    return PDIPC_OK;
+}
 int orc_tet_surface(const double* X, int nv, const int* T, int nt, int* faces, int cap, int* nf) {
     std::vector<double> x(X, X + 3 * (size_t)nv);
     std::vector<int> t(T, T + 4 * (size_t)nt);
@@ -2302,6 +2415,20 @@ int orc_svd3(const double* F, double* U, double* s, double* V) {
 int orc_add_cloth(void* h, const double* X, int nv, const int* F, int nf, double density, double ks, double kb,
                   const int* pins, int npins, double kp, int pd) {
     return add_model((Ctx*)h, X, nv, F, nf, false, density, ks, kb, pins, npins, kp, pd);
+}
+// orc_add_cloth with the per-triangle options of pdipc_add_cloth_ex (each array nf values or NULL)
+int orc_add_cloth_ex(void* h, const double* X, int nv, const int* F, int nf, double density, double ks, double kb,
+                     const int* pins, int npins, double kp, int pd, const double* tri_stretch, double k_tri_strain,
+                     const double* tri_strain) {
+    int r = add_model((Ctx*)h, X, nv, F, nf, false, density, ks, kb, pins, npins, kp, pd);
+    if (r != PDIPC_OK) return r;
+    return orc::dispatch((Ctx*)h, [&](auto& s) {
+        orc::ModelIn& m = s.models.back();
+        if (tri_stretch) m.tri_stretch.assign(tri_stretch, tri_stretch + nf);
+        if (tri_strain) m.tri_strain.assign(tri_strain, tri_strain + nf);
+        m.k_tri_strain = k_tri_strain;
+        return (int)PDIPC_OK;
+    });
 }
 int orc_add_static(void* h, const double* X, int nv, const int* F, int nf, int pd) {
     return add_model((Ctx*)h, X, nv, F, nf, true, 0, 0, 0, nullptr, 0, 0, pd);

@@ -5,6 +5,7 @@
 // postRun(), saveSimulator(frame).  No exception crosses the boundary.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
@@ -24,6 +25,14 @@ struct pdipc_ctx {
     std::unique_ptr<pdipc::SolverBase> solver;
     std::string err;
     bool initialized = false;
+    // per cloth model, kept past initialize for pdipc_stretch_gradient_per_triangle:
+    // its first simulated vertex, its faces and each vertex's triangle count
+    struct Cloth {
+        int first = 0;
+        std::vector<int> F;
+        std::vector<int> ntri;
+    };
+    std::vector<Cloth> cloths;
 };
 
 namespace {
@@ -180,7 +189,59 @@ pdipc_status pdipc_create(const pdipc_params* p, pdipc_ctx** out) {
 pdipc_status pdipc_add_cloth(pdipc_ctx* ctx, const double* X, int nv, const int* F, int nf, double density,
                              double k_stretch, double k_bend, const int* pins, int npins, double k_pin,
                              int patch_dim) {
-    return add_model(ctx, X, nv, F, nf, false, density, k_stretch, k_bend, pins, npins, k_pin, patch_dim);
+    return pdipc_add_cloth_ex(ctx, X, nv, F, nf, density, k_stretch, k_bend, pins, npins, k_pin, patch_dim, nullptr);
+}
+
+pdipc_status pdipc_add_cloth_ex(pdipc_ctx* ctx, const double* X, int nv, const int* F, int nf, double density,
+                                double k_stretch, double k_bend, const int* pins, int npins, double k_pin,
+                                int patch_dim, const pdipc_cloth_options* opt) {
+    if (opt) {
+        if (!ctx) return PDIPC_ERR_ARG;
+        if (!(opt->k_tri_strain >= 0.0) || !std::isfinite(opt->k_tri_strain))
+            return fail(ctx, PDIPC_ERR_ARG, "k_tri_strain must be a finite value >= 0");
+        for (const double* a : {opt->per_tri_stretch, opt->per_tri_strain})
+            if (a && F && nf > 0)
+                for (int f = 0; f < nf; ++f)
+                    if (!(a[f] >= 0.0) || !std::isfinite(a[f]))
+                        return fail(ctx, PDIPC_ERR_ARG, "per-triangle stiffness must be finite and >= 0");
+    }
+    pdipc_status s = add_model(ctx, X, nv, F, nf, false, density, k_stretch, k_bend, pins, npins, k_pin, patch_dim);
+    if (s != PDIPC_OK) return s;
+    return guarded(ctx, [&]() {
+        pdipc::ModelInput& m = ctx->models.back();
+        if (opt) {
+            if (opt->per_tri_stretch) m.tri_stretch.assign(opt->per_tri_stretch, opt->per_tri_stretch + nf);
+            m.k_tri_strain = opt->k_tri_strain;
+            if (opt->per_tri_strain) m.tri_strain.assign(opt->per_tri_strain, opt->per_tri_strain + nf);
+        }
+        pdipc_ctx::Cloth c;  // simulated models come first, in add order
+        for (size_t q = 0; q + 1 < ctx->models.size(); ++q)
+            if (!ctx->models[q].is_static) c.first += ctx->models[q].nv;
+        c.F.assign(F, F + 3 * (size_t)nf);
+        c.ntri.assign(nv, 0);
+        for (int q = 0; q < 3 * nf; ++q) ++c.ntri[F[q]];
+        ctx->cloths.push_back(std::move(c));
+        return PDIPC_OK;
+    });
+}
+
+pdipc_status pdipc_stretch_gradient_per_triangle(pdipc_ctx* ctx, int cloth_index, const double* dl_dvertex,
+                                                 double* dl_dtri) {
+    if (!ctx) return PDIPC_ERR_ARG;
+    if (!dl_dvertex || !dl_dtri) return fail(ctx, PDIPC_ERR_ARG, "null argument");
+    if (cloth_index < 0 || cloth_index >= (int)ctx->cloths.size())
+        return fail(ctx, PDIPC_ERR_ARG, "no cloth with that index");
+    const pdipc_ctx::Cloth& c = ctx->cloths[cloth_index];
+    const int nf = (int)c.F.size() / 3;
+    for (int f = 0; f < nf; ++f) {
+        double g = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            const int v = c.F[3 * f + k];
+            g += dl_dvertex[c.first + v] / (double)c.ntri[v];
+        }
+        dl_dtri[f] = g;
+    }
+    return PDIPC_OK;
 }
 
 pdipc_status pdipc_add_volumetric(pdipc_ctx* ctx, const double* X, int nv, const int* T, int nt, double density,
@@ -308,6 +369,14 @@ pdipc_status pdipc_get_stats(pdipc_ctx* ctx, pdipc_stats* out) {
     if (s != PDIPC_OK) return s;
     if (!out) return fail(ctx, PDIPC_ERR_ARG, "null output");
     ctx->solver->stats(out);
+    return PDIPC_OK;
+}
+
+pdipc_status pdipc_get_tuning(pdipc_ctx* ctx, pdipc_tuning* out) {
+    pdipc_status s = need_init(ctx);
+    if (s != PDIPC_OK) return s;
+    if (!out) return fail(ctx, PDIPC_ERR_ARG, "null output");
+    ctx->solver->tuning(out);
     return PDIPC_OK;
 }
 

@@ -969,28 +969,32 @@ void launch_refit(const Dev<T, TC>& d, cudaStream_t s) {
 }
 template <typename T, typename TC>
 void launch_traverse(const Dev<T, TC>& d, int64_t* cpt, int64_t* cee, int64_t cap, unsigned long long* count,
-                     cudaStream_t s) {
+                     const SolverConsts& c, cudaStream_t s) {
     if (d.npatch == 0) return;
-    k_traverse<T><<<blocks_for(d.npatch, 128), 128, 0, s>>>(d.npatch, d.PatchBox, d.NodeBox, d.NodeChild,
-                                                            d.NodeEscape, d.LeafPatch, d.pStatic, d.pfPtr, d.ppPtr,
-                                                            d.pePtr, d.Pairs, cpt, cee, cap, count, d.ErrFlags);
+    const int b = c.trav_block == 64 ? 64 : 128;  // within the kernel's launch bound, whole warps
+    k_traverse<T><<<blocks_for(d.npatch, b), b, 0, s>>>(d.npatch, d.PatchBox, d.NodeBox, d.NodeChild, d.NodeEscape,
+                                                        d.LeafPatch, d.pStatic, d.pfPtr, d.ppPtr, d.pePtr, d.Pairs,
+                                                        cpt, cee, cap, count, d.ErrFlags);
 }
 template <typename T, typename TC>
-void launch_expand(const Dev<T, TC>& d, const int64_t* opt, const int64_t* oee, cudaStream_t s) {
+void launch_expand(const Dev<T, TC>& d, const int64_t* opt, const int64_t* oee, const SolverConsts& c,
+                   cudaStream_t s) {
     if (d.nPairs == 0) return;
-    k_expand<<<blocks_for(d.nPairs * 32), kBlock, 0, s>>>(d.nPairs, d.Pairs, d.pfPtr, d.pfIdx, d.ppPtr, d.ppIdx,
-                                                          d.pePtr, d.peIdx, d.Faces, d.Edges, opt, oee, d.PT, d.EE);
+    const int b = c.expand_block == 128 ? 128 : kBlock;
+    // one thread per pair: each warp expands 32 consecutive pairs
+    k_expand<<<blocks_for(d.nPairs, b), b, 0, s>>>(d.nPairs, d.Pairs, d.pfPtr, d.pfIdx, d.ppPtr, d.ppIdx, d.pePtr,
+                                                   d.peIdx, d.Faces, d.Edges, opt, oee, d.PT, d.EE);
 }
 template <typename T, typename TC>
 void launch_toi(const Dev<T, TC>& d, Pos<T, TC> X0, Pos<T, TC> X1, const SolverConsts& c, TC* per_pt,
                 TC* per_ee, cudaStream_t s) {
     constexpr bool kRel = sizeof(T) == 4 && sizeof(TC) == 8;
     if (d.nPT > 0)
-        k_toi<T, TC, true, kRel><<<grid_cap(d.nPT), kBlock, 0, s>>>(
+        k_toi<T, TC, true, kRel><<<grid_cap(d.nPT, kBlock, c.cand_grid), kBlock, 0, s>>>(
             d.nPT, d.PT, X0.x, X1.x, X0.hi, X0.lo, X1.hi, X1.lo, (TC)c.ccd_slack, (TC)c.ccd_eta, c.ccd_max_iter,
             per_pt, d.ToiMin, d.Gate);
     if (d.nEE > 0)
-        k_toi<T, TC, false, kRel><<<grid_cap(d.nEE), kBlock, 0, s>>>(
+        k_toi<T, TC, false, kRel><<<grid_cap(d.nEE, kBlock, c.cand_grid), kBlock, 0, s>>>(
             d.nEE, d.EE, X0.x, X1.x, X0.hi, X0.lo, X1.hi, X1.lo, (TC)c.ccd_slack, (TC)c.ccd_eta, c.ccd_max_iter,
             per_ee, d.ToiMin, d.Gate);
 }
@@ -1009,11 +1013,11 @@ void launch_contact(const Dev<T, TC>& d, Pos<T, TC> X, const SolverConsts& c, cu
     cc.dt = (TC)(T)c.dt;
     constexpr bool kRel = sizeof(T) == 4 && sizeof(TC) == 8;
     if (d.nPT > 0)
-        k_contact<T, TC, true, kRel><<<grid_cap(d.nPT), kBlock, 0, s>>>(d.nPT, d.PT, X.x, X.hi, X.lo, d.CollMass,
+        k_contact<T, TC, true, kRel><<<grid_cap(d.nPT, kBlock, c.cand_grid), kBlock, 0, s>>>(d.nPT, d.PT, X.x, X.hi, X.lo, d.CollMass,
                                                                          cc, d.CollDiag, d.CollRhs, d.ActiveCount,
                                                                          d.Gate);
     if (d.nEE > 0)
-        k_contact<T, TC, false, kRel><<<grid_cap(d.nEE), kBlock, 0, s>>>(d.nEE, d.EE, X.x, X.hi, X.lo,
+        k_contact<T, TC, false, kRel><<<grid_cap(d.nEE, kBlock, c.cand_grid), kBlock, 0, s>>>(d.nEE, d.EE, X.x, X.hi, X.lo,
                                                                           d.CollMass, cc, d.CollDiag, d.CollRhs,
                                                                           d.ActiveCount, d.Gate);
 }
@@ -1054,8 +1058,9 @@ cudaError_t toi_scratch(ToiScratch* out) {
     template void launch_karras<T, TC>(const Dev<T, TC>&, const unsigned long long*, cudaStream_t);           \
     template void launch_refit<T, TC>(const Dev<T, TC>&, cudaStream_t);                                       \
     template void launch_traverse<T, TC>(const Dev<T, TC>&, int64_t*, int64_t*, int64_t, unsigned long long*,  \
-                                         cudaStream_t);                                                        \
-    template void launch_expand<T, TC>(const Dev<T, TC>&, const int64_t*, const int64_t*, cudaStream_t);      \
+                                         const SolverConsts&, cudaStream_t);                                   \
+    template void launch_expand<T, TC>(const Dev<T, TC>&, const int64_t*, const int64_t*, const SolverConsts&, \
+                                       cudaStream_t);                                                          \
     template void launch_toi<T, TC>(const Dev<T, TC>&, Pos<T, TC>, Pos<T, TC>, const SolverConsts&, TC*,      \
                                     TC*, cudaStream_t);                                                       \
     template void launch_toi_finalize<T, TC>(const Dev<T, TC>&, const SolverConsts&, cudaStream_t);           \

@@ -347,13 +347,64 @@ std::string build_host_tables(const std::vector<ModelInput>& models, double grav
             double ar = 0.5 * std::fabs(std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
             for (int k = 0; k < 3; ++k) area[Fv[k]] += ar / 3.0;
         }
+        // per-triangle stretch stiffness: a vertex's spring weight is the mean
+        // over its triangles (the reference's weight is per vertex,
+        // PdIpcGpuFunc.cu:673, set from one k per model, PdIpcClothModel.h:282,300)
+        std::vector<double> kv;
+        if (!m.tri_stretch.empty()) {
+            kv.assign(m.nv, 0.0);
+            std::vector<int> nt(m.nv, 0);
+            for (int f = 0; f < m.nf; ++f)
+                for (int k = 0; k < 3; ++k) {
+                    kv[m.F[3 * f + k]] += m.tri_stretch[f];
+                    ++nt[m.F[3 * f + k]];
+                }
+            for (int i = 0; i < m.nv; ++i) kv[i] = nt[i] ? kv[i] / nt[i] : m.k_stretch;
+        }
         for (int i = 0; i < m.nv; ++i) {
             const int g = o + i;
             H.mass[g] = area[i] * m.density;
             bendArea[g] = area[i] * m.k_bend;
-            H.strain[g] = m.k_stretch;
+            H.strain[g] = kv.empty() ? m.k_stretch : kv[i];
             const int deg = (int)t.point_edges[i].size();
             H.lPtr[g + 1] = deg + 1;  // counts for now
+        }
+        // Triangle strain limits: the tet constraint of
+        // solveVolumetricStrainConstraintKernel (PdIpcGpuFunc.cu:439-599) for a
+        // triangle, F = Ds Dm^-1 (3 x 2), with Dm the rest edges in the rest
+        // triangle's orthonormal frame (e1 along the first edge, e2 in the plane)
+        // and weight k x rest area.  An element with fourth vertex -1.
+        if (m.k_tri_strain > 0.0 || !m.tri_strain.empty()) {
+            auto P = [&](int i, int k) { return m.X[3 * i + k]; };
+            for (int f = 0; f < m.nf; ++f) {
+                const double kf = m.tri_strain.empty() ? m.k_tri_strain : m.tri_strain[f];
+                if (!(kf > 0.0)) continue;
+                const int* Fv = &m.F[3 * f];
+                double a[3], b[3];
+                for (int k = 0; k < 3; ++k) {
+                    a[k] = P(Fv[1], k) - P(Fv[0], k);
+                    b[k] = P(Fv[2], k) - P(Fv[0], k);
+                }
+                const double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+                const double la = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+                const double ln = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+                if (!(la > 0.0) || !(ln > 0.0)) return "degenerate cloth triangle under a strain limit";
+                double e1[3], e2[3];
+                for (int k = 0; k < 3; ++k) e1[k] = a[k] / la;
+                // e2 = (n x e1) / |n|: in the plane, perpendicular to e1
+                e2[0] = (n[1] * e1[2] - n[2] * e1[1]) / ln;
+                e2[1] = (n[2] * e1[0] - n[0] * e1[2]) / ln;
+                e2[2] = (n[0] * e1[1] - n[1] * e1[0]) / ln;
+                auto dot = [](const double* u, const double* v) { return u[0] * v[0] + u[1] * v[1] + u[2] * v[2]; };
+                // Dm columns: the rest edges in (e1, e2)
+                const double d00 = dot(a, e1), d01 = dot(b, e1), d10 = dot(a, e2), d11 = dot(b, e2);
+                const double det = d00 * d11 - d01 * d10;
+                const double idm[9] = {d11 / det, -d01 / det, -d10 / det, d00 / det, 0, 0, 0, 0, 0};
+                for (double v : idm) H.tetIdm.push_back(v);
+                for (int k = 0; k < 3; ++k) H.tets.push_back(o + Fv[k]);
+                H.tets.push_back(-1);
+                H.tetW.push_back(kf * 0.5 * ln);
+            }
         }
     }
     // prefix the stencil sizes, then fill the stencils
@@ -504,19 +555,33 @@ std::string build_host_tables(const std::vector<ModelInput>& models, double grav
                 else rows[a].push_back({b, v});
             }
     }
-    // tet strain terms: w G^T G with G = [-sum_k Dm^-T(:,k) | Dm^-T] (3 x 4)
+    // tet strain terms: w G^T G with G = [-sum_k Dm^-T(:,k) | Dm^-T] (3 x 4);
+    // a triangle element (fourth vertex -1): G^T = S Dm^-1 (3 x 2), S the rows
+    // (-1, -1), (1, 0), (0, 1), the third row of G zero
     H.ntet = (int)H.tetW.size();
     for (int e = 0; e < H.ntet; ++e) {
         const double* idm = &H.tetIdm[9 * (size_t)e];
+        const bool tri = H.tets[4 * (size_t)e + 3] < 0;
         double G[3][4];
-        for (int i = 0; i < 3; ++i) {
-            G[i][1] = idm[i];
-            G[i][2] = idm[3 + i];
-            G[i][3] = idm[6 + i];
-            G[i][0] = -(G[i][1] + G[i][2] + G[i][3]);
+        if (tri) {
+            for (int j = 0; j < 2; ++j) {
+                G[j][1] = idm[j];
+                G[j][2] = idm[2 + j];
+                G[j][0] = -(G[j][1] + G[j][2]);
+                G[j][3] = 0.0;
+            }
+            for (int c = 0; c < 4; ++c) G[2][c] = 0.0;
+        } else {
+            for (int i = 0; i < 3; ++i) {
+                G[i][1] = idm[i];
+                G[i][2] = idm[3 + i];
+                G[i][3] = idm[6 + i];
+                G[i][0] = -(G[i][1] + G[i][2] + G[i][3]);
+            }
         }
-        for (int r = 0; r < 4; ++r)
-            for (int c = 0; c < 4; ++c) {
+        const int nvert = tri ? 3 : 4;
+        for (int r = 0; r < nvert; ++r)
+            for (int c = 0; c < nvert; ++c) {
                 double v = 0.0;
                 for (int k = 0; k < 3; ++k) v += G[k][r] * G[k][c];
                 v *= H.tetW[e];
@@ -528,13 +593,15 @@ std::string build_host_tables(const std::vector<ModelInput>& models, double grav
     // vertex -> (tet, slot) incidence, ascending tet
     H.vtPtr.assign(nsim + 1, 0);
     for (int e = 0; e < H.ntet; ++e)
-        for (int k = 0; k < 4; ++k) ++H.vtPtr[H.tets[4 * (size_t)e + k] + 1];
+        for (int k = 0; k < 4; ++k)
+            if (H.tets[4 * (size_t)e + k] >= 0) ++H.vtPtr[H.tets[4 * (size_t)e + k] + 1];
     for (int i = 0; i < nsim; ++i) H.vtPtr[i + 1] += H.vtPtr[i];
     H.vtIdx.assign(H.vtPtr[nsim], 0);
     {
         std::vector<int> fill(H.vtPtr.begin(), H.vtPtr.end() - 1);
         for (int e = 0; e < H.ntet; ++e)
-            for (int k = 0; k < 4; ++k) H.vtIdx[fill[H.tets[4 * (size_t)e + k]]++] = (e << 2) | k;
+            for (int k = 0; k < 4; ++k)
+                if (H.tets[4 * (size_t)e + k] >= 0) H.vtIdx[fill[H.tets[4 * (size_t)e + k]]++] = (e << 2) | k;
     }
     H.nPtr.assign(nsim + 1, 0);
     for (int i = 0; i < nsim; ++i) {

@@ -17,6 +17,13 @@ struct ModelInput {
     bool is_volumetric = false;
     double density = 0, k_stretch = 0, k_bend = 0, k_pin = 0;
     double k_strain = 0, k_volume = 0;  // volumetric: strain and (unused by the reference) volume stiffness
+    // cloth: per-triangle stretch stiffness (nf, or empty: k_stretch), mapped to
+    // the per-vertex spring weight as the mean over a vertex's triangles
+    std::vector<double> tri_stretch;
+    // cloth: per-triangle strain-limit weight per unit rest area (nf, or empty:
+    // k_tri_strain everywhere; no constraint where it is 0)
+    double k_tri_strain = 0;
+    std::vector<double> tri_strain;
     std::vector<int> pins;
     int patch_dim = 10;
 };

@@ -141,6 +141,12 @@ struct Pos {
 struct SolverConsts {
     double dt, gravity, dhat, kappa, infl, relax, rho, toi_scale, ccd_slack, ccd_eta, static_mass;
     int lg, cheby, ccd_max_iter;
+    // launch shapes the autotuner may change: blocks of the grid-stride
+    // candidate kernels (time of impact, contact), threads per block of the
+    // broad phase's traversal and expansion
+    int cand_grid = 152 * 16;
+    int trav_block = 128;
+    int expand_block = 256;
 };
 
 // ---------------- PD kernels (pd_kernels.cu) ----------------
@@ -208,9 +214,10 @@ void launch_refit(const Dev<T, TC>& d, cudaStream_t s);
 // edge-edge record counts; *count (zeroed by the caller) gets the full number
 template <typename T, typename TC>
 void launch_traverse(const Dev<T, TC>& d, int64_t* cnt_pt, int64_t* cnt_ee, int64_t cap, unsigned long long* count,
-                     cudaStream_t s);
+                     const SolverConsts& c, cudaStream_t s);
 template <typename T, typename TC>
-void launch_expand(const Dev<T, TC>& d, const int64_t* off_pt, const int64_t* off_ee, cudaStream_t s);
+void launch_expand(const Dev<T, TC>& d, const int64_t* off_pt, const int64_t* off_ee, const SolverConsts& c,
+                   cudaStream_t s);
 template <typename T, typename TC>
 void launch_toi(const Dev<T, TC>& d, Pos<T, TC> X0, Pos<T, TC> X1, const SolverConsts& c, TC* per_pt,
                 TC* per_ee, cudaStream_t s);

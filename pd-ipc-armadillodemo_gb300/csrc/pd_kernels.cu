@@ -103,7 +103,10 @@ __global__ void k_tet_project(int ntet, const int4* __restrict__ Tets, const T* 
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ntet) return;
     const int4 q = Tets[e];
-    const int id[4] = {q.x, q.y, q.z, q.w};
+    // a cloth triangle's strain element has no fourth vertex (-1): its first
+    // vertex stands in, so the third edge is zero and unused
+    const bool tri = q.w < 0;
+    const int id[4] = {q.x, q.y, q.z, tri ? q.x : q.w};
     T Ds[3][3];
     if constexpr (kMirror<T, S>) {
         const V4<T> h0 = ld4(Ph, id[0]), l0 = ld4(Pl, id[0]);
@@ -128,7 +131,18 @@ __global__ void k_tet_project(int ntet, const int4* __restrict__ Tets, const T* 
 #pragma unroll
     for (int k = 0; k < 9; ++k) idm[k] = __ldg(Idm + 9 * (size_t)e + k);
     T out[4][3];
-    svd::tet_project<T>(Ds, idm, __ldg(W + e), out);
+    if (tri) {
+        const T D2[3][2] = {{Ds[0][0], Ds[0][1]}, {Ds[1][0], Ds[1][1]}, {Ds[2][0], Ds[2][1]}};
+        T o3[3][3];
+        svd::tri_project<T>(D2, idm, __ldg(W + e), o3);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) out[c][r] = o3[c][r];
+        out[3][0] = out[3][1] = out[3][2] = T(0);
+    } else {
+        svd::tet_project<T>(Ds, idm, __ldg(W + e), out);
+    }
 #pragma unroll
     for (int c = 0; c < 4; ++c) Out[4 * (size_t)e + c] = V4<T>{out[c][0], out[c][1], out[c][2], T(0)};
 }

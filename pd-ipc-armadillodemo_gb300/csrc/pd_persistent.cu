@@ -221,7 +221,8 @@ __device__ __noinline__ void tet_project_one(int e, const int4* __restrict__ Tet
                                              const V4<float>* __restrict__ Ph, const V4<float>* __restrict__ Pl,
                                              V4<float>* __restrict__ Out) {
     const int4 q = Tets[e];
-    const int id[4] = {q.x, q.y, q.z, q.w};
+    const bool tri = q.w < 0;  // a cloth triangle's strain element: no fourth vertex
+    const int id[4] = {q.x, q.y, q.z, tri ? q.x : q.w};
     float Ds[3][3];
     if constexpr (kCorr) {
         const V4<float> h0 = ldcg4(Ph, id[0]), l0 = ldcg4(Pl, id[0]);
@@ -243,7 +244,16 @@ __device__ __noinline__ void tet_project_one(int e, const int4* __restrict__ Tet
     float idm[9];
     for (int k = 0; k < 9; ++k) idm[k] = __ldg(Idm + 9 * (size_t)e + k);
     float out[4][3];
-    svd::tet_project<float>(Ds, idm, __ldg(W + e), out);
+    if (tri) {
+        const float D2[3][2] = {{Ds[0][0], Ds[0][1]}, {Ds[1][0], Ds[1][1]}, {Ds[2][0], Ds[2][1]}};
+        float o3[3][3];
+        svd::tri_project<float>(D2, idm, __ldg(W + e), o3);
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) out[c][r] = o3[c][r];
+        out[3][0] = out[3][1] = out[3][2] = 0.f;
+    } else {
+        svd::tet_project<float>(Ds, idm, __ldg(W + e), out);
+    }
     for (int c = 0; c < 4; ++c) __stcg(reinterpret_cast<float4*>(Out) + 4 * (size_t)e + c, make_float4(out[c][0], out[c][1], out[c][2], 0.f));
 }
 

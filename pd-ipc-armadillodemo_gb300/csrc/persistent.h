@@ -17,6 +17,14 @@ constexpr int kMaxPersistWarps = 28;
 // (read through the constant cache, off the shared-memory pipe)
 constexpr int kParamPatterns = 4096;
 
+// One configuration of the persistent solve, as the autotuner names it.
+struct PlanChoice {
+    int rows_per_thread = 0;  // R, slices per warp; 0: one launch per sweep instead
+    bool band = false;        // the iterate's column band in shared memory (correction form)
+    bool l1_gather = true;
+    bool local_sync = true;
+};
+
 struct PersistPlan {
     bool enabled = false;
     bool matrix_in_smem = false;  // values in shared memory, columns from the pattern table

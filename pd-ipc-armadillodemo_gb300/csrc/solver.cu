@@ -16,6 +16,8 @@
 #include <vector>
 
 #include <map>
+#include <mutex>
+#include <string>
 #include <type_traits>
 
 #include "kernels.cuh"
@@ -302,9 +304,253 @@ public:
         pdipc_status r = build_tree(true, err);
         if (r != PDIPC_OK) return r;
         PD_CK(cudaStreamSynchronize(s_));
+        fill_tuning_record();
+        if (prm_.autotune) {
+            r = autotune(H, err);
+            if (r != PDIPC_OK) return r;
+        }
         inited_ = true;
         return PDIPC_OK;
     }
+
+    void tuning(pdipc_tuning* out) override { *out = tuning_; }
+
+private:
+    // ---------------- autotuner ----------------
+    struct Tuned {
+        PlanChoice pd;
+        int cand_grid, trav_block, expand_block;
+    };
+
+    void fill_tuning_record() {
+        tuning_.pd_rows_per_thread = plan_.enabled ? plan_.rows_per_thread : 0;
+        tuning_.pd_ctas = plan_.enabled ? plan_.ctas : 0;
+        tuning_.pd_band = plan_.enabled && plan_.own_max > 0;
+        tuning_.pd_l1_gather = plan_.enabled && plan_.l1_gather;
+        tuning_.pd_local_sync = plan_.enabled && plan_.local_sync;
+        tuning_.cand_grid = c_.cand_grid;
+        tuning_.traverse_block = c_.trav_block;
+        tuning_.expand_block = c_.expand_block;
+    }
+
+    PlanChoice current_choice() const {
+        PlanChoice ch;
+        if (!plan_.enabled) return ch;
+        ch.rows_per_thread = plan_.rows_per_thread;
+        ch.band = plan_.own_max > 0;
+        ch.l1_gather = plan_.l1_gather;
+        ch.local_sync = plan_.local_sync;
+        return ch;
+    }
+
+    // One outer iteration's PD solve from the predicted state in `start`
+    // (positions and, in the correction form, their float-float mirror), timed
+    // with CUDA events on the context's stream; mean of `reps` after one warm-up.
+    pdipc_status time_pd_solve(const V4<TC>* start, const V4<T>* sh, const V4<T>* sl, int reps, float* ms_out,
+                               std::string& err) {
+        auto restore = [&]() -> cudaError_t {
+            cudaError_t e = cudaMemcpyAsync(d_.P, start, sizeof(V4<TC>) * d_.nsim, cudaMemcpyDeviceToDevice, s_);
+            if (e == cudaSuccess && sh)
+                e = cudaMemcpyAsync(d_.Ph, sh, sizeof(V4<T>) * d_.nsim, cudaMemcpyDeviceToDevice, s_);
+            if (e == cudaSuccess && sl)
+                e = cudaMemcpyAsync(d_.Pl, sl, sizeof(V4<T>) * d_.nsim, cudaMemcpyDeviceToDevice, s_);
+            return e;
+        };
+        auto solve = [&]() -> cudaError_t {
+            if (plan_.enabled) return launch_persistent();
+            enqueue_pd();
+            return cudaGetLastError();
+        };
+        float total = 0.f;
+        for (int k = -1; k < reps; ++k) {
+            PD_CK(restore());
+            PD_CK(cudaEventRecord(ev0_, s_));
+            PD_CK(solve());
+            PD_CK(cudaEventRecord(ev1_, s_));
+            PD_CK(cudaEventSynchronize(ev1_));
+            float ms = 0.f;
+            PD_CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
+            if (k >= 0) total += ms;
+        }
+        pin_->err = 0;
+        PD_CK(cudaMemcpyAsync(&pin_->err, d_.ErrFlags, sizeof(unsigned int), cudaMemcpyDeviceToHost, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        if (pin_->err) {  // a device wait gave up: this configuration is not usable here
+            PD_CK(cudaMemsetAsync(d_.ErrFlags, 0, sizeof(unsigned int), s_));
+            PD_CK(cudaMemsetAsync(pBar_ + 1, 0, sizeof(unsigned), s_));
+            *ms_out = -1.f;
+            return PDIPC_OK;
+        }
+        *ms_out = total / (float)reps;
+        return PDIPC_OK;
+    }
+
+    // The broad phase, the time-of-impact pass and the contact pass over the
+    // candidates of the current positions, timed with CUDA events.
+    pdipc_status time_collision(int reps, float* ms_out, std::string& err) {
+        float total = 0.f;
+        for (int k = -1; k < reps; ++k) {
+            PD_CK(cudaEventRecord(ev0_, s_));
+            pdipc_status r = broadphase(err);
+            if (r != PDIPC_OK) return r;
+            launch_toi(d_, pos_old(), pos(), c_, (TC*)nullptr, (TC*)nullptr, s_);
+            launch_toi_finalize(d_, c_, s_);
+            launch_contact(d_, pos(), c_, s_);
+            PD_CK(cudaEventRecord(ev1_, s_));
+            PD_CK(cudaEventSynchronize(ev1_));
+            float ms = 0.f;
+            PD_CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
+            if (k >= 0) total += ms;
+        }
+        *ms_out = total / (float)reps;
+        return PDIPC_OK;
+    }
+
+    // Chooses, per mesh and precision, the persistent solve's configuration
+    // (rows per thread and so CTA count, band, gathers, synchronisation, or
+    // one launch per sweep) and the collision kernels' launch shapes (grid of
+    // the candidate kernels, block sizes of the traversal and the expansion)
+    // by timing every candidate with CUDA events at initialize, on the
+    // predicted first step of the current state (restored afterwards).  The
+    // choice is cached by shape for the process: later contexts of the same
+    // shape take it without timing.  Every candidate computes the same
+    // iteration; they differ in launch shape and, on the band path, in where a
+    // row's sum splits between own and halo entries.
+    pdipc_status autotune(const HostTables& H, std::string& err) {
+        static std::mutex mu;
+        static std::map<std::string, Tuned> cache;
+        const std::string key = std::to_string(sizeof(T)) + "/" + std::to_string(sizeof(TC)) + "/" +
+                                std::to_string(d_.nsim) + "/" + std::to_string(d_.ntot) + "/" +
+                                std::to_string(d_.npatch) + "/" + std::to_string(sell_entries_) + "/" +
+                                std::to_string(c_.lg) + "/" + std::to_string(c_.cheby) + "/" +
+                                std::to_string(prm_.persistent) + "/" + std::to_string(d_.ntet);
+        Tuned best{current_choice(), c_.cand_grid, c_.trav_block, c_.expand_block};
+        bool cached = false;
+        {
+            std::lock_guard<std::mutex> g(mu);
+            auto it = cache.find(key);
+            if (it != cache.end()) {
+                best = it->second;
+                cached = true;
+            }
+        }
+        if (cached) {
+            pdipc_status r = plan_persistent(H, sliceOffH_, sliceLenH_, err, best.pd.rows_per_thread ? &best.pd : nullptr);
+            if (r != PDIPC_OK) return r;
+            if (best.pd.rows_per_thread == 0) plan_ = PersistPlan();
+            c_.cand_grid = best.cand_grid;
+            c_.trav_block = best.trav_block;
+            c_.expand_block = best.expand_block;
+            fill_tuning_record();
+            tuning_.autotuned = 1;
+            tuning_.from_cache = 1;
+            return PDIPC_OK;
+        }
+        // ---- the PD solve: every configuration that fits, and one launch per sweep ----
+        const int ns = d_.nsim;
+        V4<TC>*saveP = nullptr, *saveV = nullptr, *start = nullptr;
+        V4<T>*saveH = nullptr, *saveL = nullptr, *startH = nullptr, *startL = nullptr;
+        PD_CK(alloc(saveP, ns));
+        PD_CK(alloc(saveV, ns));
+        PD_CK(alloc(start, ns));
+        PD_CK(cudaMemcpyAsync(saveP, d_.P, sizeof(V4<TC>) * ns, cudaMemcpyDeviceToDevice, s_));
+        PD_CK(cudaMemcpyAsync(saveV, d_.Vel, sizeof(V4<TC>) * ns, cudaMemcpyDeviceToDevice, s_));
+        if (d_.Ph) {
+            PD_CK(alloc(saveH, ns));
+            PD_CK(alloc(saveL, ns));
+            PD_CK(alloc(startH, ns));
+            PD_CK(alloc(startL, ns));
+            PD_CK(cudaMemcpyAsync(saveH, d_.Ph, sizeof(V4<T>) * ns, cudaMemcpyDeviceToDevice, s_));
+            PD_CK(cudaMemcpyAsync(saveL, d_.Pl, sizeof(V4<T>) * ns, cudaMemcpyDeviceToDevice, s_));
+        }
+        launch_predict(d_, (TC)c_.dt, s_);
+        PD_CK(cudaMemcpyAsync(start, d_.P, sizeof(V4<TC>) * ns, cudaMemcpyDeviceToDevice, s_));
+        if (d_.Ph) {
+            PD_CK(cudaMemcpyAsync(startH, d_.Ph, sizeof(V4<T>) * ns, cudaMemcpyDeviceToDevice, s_));
+            PD_CK(cudaMemcpyAsync(startL, d_.Pl, sizeof(V4<T>) * ns, cudaMemcpyDeviceToDevice, s_));
+        }
+        std::vector<PlanChoice> pds;
+        pds.push_back(current_choice());  // the default first
+        for (const PlanChoice& c : plan_choices_)
+            if (!(c.rows_per_thread == pds[0].rows_per_thread && c.band == pds[0].band &&
+                  c.l1_gather == pds[0].l1_gather && c.local_sync == pds[0].local_sync))
+                pds.push_back(c);
+        if (pds[0].rows_per_thread != 0) pds.push_back(PlanChoice{});  // one launch per sweep
+        float bestMs = -1.f;
+        for (size_t k = 0; k < pds.size(); ++k) {
+            pdipc_status r = plan_persistent(H, sliceOffH_, sliceLenH_, err, pds[k].rows_per_thread ? &pds[k] : nullptr);
+            if (r != PDIPC_OK) return r;
+            if (pds[k].rows_per_thread == 0) plan_ = PersistPlan();
+            else if (!plan_.enabled) continue;
+            float ms = -1.f;
+            r = time_pd_solve(start, startH, startL, 3, &ms, err);
+            if (r != PDIPC_OK) return r;
+            ++tuning_.candidates_timed;
+            if (k == 0) tuning_.pd_default_ms = ms;
+            if (ms > 0.f && (bestMs < 0.f || ms < bestMs)) {
+                bestMs = ms;
+                best.pd = pds[k];
+            }
+        }
+        pdipc_status r = plan_persistent(H, sliceOffH_, sliceLenH_, err, best.pd.rows_per_thread ? &best.pd : nullptr);
+        if (r != PDIPC_OK) return r;
+        if (best.pd.rows_per_thread == 0) plan_ = PersistPlan();
+        tuning_.pd_solve_ms = bestMs;
+        // ---- the collision kernels' launch shapes, over the current candidates ----
+        PD_CK(cudaMemcpyAsync(d_.P, saveP, sizeof(V4<TC>) * ns, cudaMemcpyDeviceToDevice, s_));
+        if (d_.Ph) {
+            PD_CK(cudaMemcpyAsync(d_.Ph, saveH, sizeof(V4<T>) * ns, cudaMemcpyDeviceToDevice, s_));
+            PD_CK(cudaMemcpyAsync(d_.Pl, saveL, sizeof(V4<T>) * ns, cudaMemcpyDeviceToDevice, s_));
+        }
+        float collBest = -1.f;
+        const int grids[] = {152 * 16, 152 * 4, 152 * 8, 152 * 32};
+        const int tblocks[] = {128, 64};
+        const int eblocks[] = {256, 128};
+        for (int g : grids)
+            for (int tb : tblocks)
+                for (int eb : eblocks) {
+                    c_.cand_grid = g;
+                    c_.trav_block = tb;
+                    c_.expand_block = eb;
+                    float ms = 0.f;
+                    r = time_collision(2, &ms, err);
+                    if (r != PDIPC_OK) return r;
+                    ++tuning_.candidates_timed;
+                    if (g == grids[0] && tb == tblocks[0] && eb == eblocks[0]) tuning_.collision_default_ms = ms;
+                    if (collBest < 0.f || ms < collBest) {
+                        collBest = ms;
+                        best.cand_grid = g;
+                        best.trav_block = tb;
+                        best.expand_block = eb;
+                    }
+                }
+        c_.cand_grid = best.cand_grid;
+        c_.trav_block = best.trav_block;
+        c_.expand_block = best.expand_block;
+        tuning_.collision_ms = collBest;
+        // ---- the state as it was ----
+        PD_CK(cudaMemcpyAsync(d_.P, saveP, sizeof(V4<TC>) * ns, cudaMemcpyDeviceToDevice, s_));
+        PD_CK(cudaMemcpyAsync(d_.Vel, saveV, sizeof(V4<TC>) * ns, cudaMemcpyDeviceToDevice, s_));
+        if (d_.Ph) {
+            PD_CK(cudaMemcpyAsync(d_.Ph, saveH, sizeof(V4<T>) * ns, cudaMemcpyDeviceToDevice, s_));
+            PD_CK(cudaMemcpyAsync(d_.Pl, saveL, sizeof(V4<T>) * ns, cudaMemcpyDeviceToDevice, s_));
+        }
+        PD_CK(cudaMemsetAsync(d_.CollDiag, 0, sizeof(T) * d_.ntot, s_));
+        PD_CK(cudaMemsetAsync(d_.CollRhs, 0, sizeof(V4<T>) * d_.ntot, s_));
+        PD_CK(cudaStreamSynchronize(s_));
+        for (V4<TC>* p : {saveP, saveV, start}) dfree(p);
+        for (V4<T>* p : {saveH, saveL, startH, startL}) dfree(p);
+        launches_ = 0;
+        fill_tuning_record();
+        tuning_.autotuned = 1;
+        {
+            std::lock_guard<std::mutex> g(mu);
+            cache[key] = best;
+        }
+        return PDIPC_OK;
+    }
+
+public:
 
     pdipc_status step(int n, std::string& err) override {
         if (!inited_) {
@@ -1025,9 +1271,22 @@ private:
     // ---------------- persistent PD solve ----------------
     // Partition of the SELL slices over co-resident CTAs (one per SM), with the
     // matrix values in shared memory when they fit, and the argument block.
+    // The launch plan of the persistent solve: the default configuration, or
+    // `force` when given (disabled if that configuration does not fit).  May
+    // run again (the autotuner): the previous plan's tables are freed first.
     pdipc_status plan_persistent(const HostTables& H, const std::vector<int>& soff, const std::vector<int>& slen,
-                                 std::string& err) {
+                                 std::string& err, const PlanChoice* force = nullptr) {
         plan_ = PersistPlan();
+        dfree(pNbr_);
+        dfree(pCtaTetPtr_);
+        dfree(pCtaTetIdx_);
+        dfree(pBand_);
+        dfree(pFlags_);
+        dfree(pCtaSlice_);
+        dfree(pCtaEntry_);
+        dfree(pRowPat_);
+        dfree(pPatOff_);
+        dfree(pBar_);
         // the persistent solve covers cloth stencils only: tet models take the per-sweep path
         if (!std::is_same<T, float>::value || !prm_.persistent || c_.cheby >= kMaxCheby)
             return PDIPC_OK;
@@ -1097,61 +1356,94 @@ private:
             }
             return mx;
         };
-        std::vector<int2> bandRange;
         const size_t limit = (size_t)smem_optin - 1024;
-        for (int pass = 0; pass < 2 && !plan_.enabled; ++pass) {
+        // Every configuration that fits: rows per thread R (slices per warp),
+        // the band of the iterate in shared memory (correction form: own rows
+        // planar, halo as 16-byte vertices, the copies' mbarrier, one more warp
+        // without rows for the neighbour flags and the copies), L1 or L2-only
+        // gathers, neighbour waits or grid barriers.  The direct form keeps the
+        // reference's summation order (gathers, no band).  The default is the
+        // first R that fits, with the band when it fits, and the gathers and
+        // synchronisation `persistent` names; with persistent = 1 the others
+        // are listed in plan_choices_ for the autotuner.
+        struct Cand {
+            PlanChoice ch;
+            bool smem_mat;
+            int spc, ctas, threads;
+            size_t sm;
+            int ownMax, haloMax;
+            std::vector<int2> band;
+        };
+        std::vector<Cand> cands;
+        const bool dflt_l1 = prm_.persistent != 2, dflt_ls = prm_.persistent != 3;
+        for (int pass = 0; pass < 2; ++pass) {
             const bool smem_mat = pass == 0 && fits16;
             if (pass == 0 && !fits16) continue;
+            if (pass == 1 && !cands.empty()) break;  // the L2-streamed matrix only when no slice fits
             for (int R = 1; R <= 4; ++R) {
                 const int W = std::max(1, (nsl + nsm * R - 1) / (nsm * R));
                 if (W > kMaxPersistWarps) continue;
                 const int spc = W * R;
                 const int ctas = (nsl + spc - 1) / spc;
-                size_t sm = cta_smem(spc, smem_mat, 0);
-                if (sm > limit) continue;
-                int ownMax = 0, haloMax = 0;
-                if (kCorrection && smem_mat && prm_.persistent == 1 &&
-                    W + 1 <= kMaxPersistWarps && pats.size() * (size_t)patW <= (size_t)kParamPatterns) {
-                    // correction form: own rows planar, halo as 16-byte vertices, the
-                    // copies' mbarrier; one more warp (no rows) for the neighbour
-                    // flags and the copies.  The direct form keeps the reference's
-                    // summation order (gathers through L1).
+                const size_t sm0 = cta_smem(spc, smem_mat, 0);
+                if (sm0 > limit) continue;
+                std::vector<Cand> vs;
+                if (kCorrection && smem_mat && prm_.persistent == 1 && W + 1 <= kMaxPersistWarps &&
+                    pats.size() * (size_t)patW <= (size_t)kParamPatterns) {
                     std::vector<int2> rg;
                     const int hx = col_ranges(spc, rg);
                     const int om = spc * kSlice;
                     const size_t smb =
                         cta_smem(spc, smem_mat, a16(3 * (size_t)om * sizeof(T)) + (size_t)hx * sizeof(V4<T>) + 16);
-                    if (smb <= limit) {
-                        sm = smb;
-                        ownMax = om;
-                        haloMax = hx;
-                        bandRange.swap(rg);
-                    }
+                    if (smb <= limit)
+                        vs.push_back(Cand{PlanChoice{R, true, true, true}, smem_mat, spc, ctas, (W + 1) * 32, smb, om,
+                                          hx, std::move(rg)});
                 }
-                const int threads = (W + (ownMax > 0 ? 1 : 0)) * 32;
-                const void* f = persistent_kernel(kCorrection, smem_mat, ownMax > 0, prm_.persistent != 2, R, H.ntet > 0);
-                if (!f) continue;
-                PD_CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
-                int per_sm = 0;
-                PD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, threads, sm));
-                if (per_sm < 1 || ctas > per_sm * nsm) continue;
-                plan_.enabled = true;
-                plan_.matrix_in_smem = smem_mat;
-                plan_.l1_gather = prm_.persistent != 2;
-                plan_.local_sync = prm_.persistent != 3;
-                plan_.ctas = ctas;
-                plan_.threads = threads;
-                plan_.rows_per_thread = R;
-                plan_.slices_per_cta = spc;
-                plan_.smem_bytes = sm;
-                plan_.patterns = smem_mat ? (int)pats.size() : 0;
-                plan_.pattern_width = patW;
-                plan_.own_max = ownMax;
-                plan_.halo_max = haloMax;
+                for (int v = 0; v < 4 && (v == 0 || prm_.persistent == 1); ++v) {
+                    const bool l1 = (v & 1) ? !dflt_l1 : dflt_l1, ls = (v & 2) ? !dflt_ls : dflt_ls;
+                    vs.push_back(Cand{PlanChoice{R, false, l1, ls}, smem_mat, spc, ctas, W * 32, sm0, 0, 0, {}});
+                }
+                for (Cand& c : vs) {
+                    const void* f = persistent_kernel(kCorrection, smem_mat, c.ch.band, c.ch.l1_gather, R, H.ntet > 0);
+                    if (!f) continue;
+                    PD_CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)std::max<size_t>(c.sm, 1)));
+                    int per_sm = 0;
+                    PD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, c.threads, c.sm));
+                    if (per_sm < 1 || ctas > per_sm * nsm) continue;
+                    cands.push_back(std::move(c));
+                }
+            }
+        }
+        if (!force) {
+            plan_choices_.clear();
+            for (const Cand& c : cands) plan_choices_.push_back(c.ch);
+        }
+        const Cand* pick = nullptr;
+        for (const Cand& c : cands) {
+            const bool match = force ? (c.ch.rows_per_thread == force->rows_per_thread && c.ch.band == force->band &&
+                                        c.ch.l1_gather == force->l1_gather && c.ch.local_sync == force->local_sync)
+                                     : (c.ch.l1_gather == dflt_l1 && c.ch.local_sync == dflt_ls);
+            if (match) {
+                pick = &c;
                 break;
             }
         }
-        if (!plan_.enabled) return PDIPC_OK;
+        if (!pick) return PDIPC_OK;
+        plan_.enabled = true;
+        plan_.matrix_in_smem = pick->smem_mat;
+        plan_.l1_gather = pick->ch.l1_gather;
+        plan_.local_sync = pick->ch.local_sync;
+        plan_.ctas = pick->ctas;
+        plan_.threads = pick->threads;
+        plan_.rows_per_thread = pick->ch.rows_per_thread;
+        plan_.slices_per_cta = pick->spc;
+        plan_.smem_bytes = pick->sm;
+        plan_.patterns = pick->smem_mat ? (int)pats.size() : 0;
+        plan_.pattern_width = patW;
+        plan_.own_max = pick->ownMax;
+        plan_.halo_max = pick->haloMax;
+        const std::vector<int2> bandRange = pick->band;
         std::vector<int> ctaSlice(plan_.ctas + 1), ctaEntry(plan_.ctas + 1);
         for (int c = 0; c <= plan_.ctas; ++c) {
             ctaSlice[c] = std::min(nsl, c * plan_.slices_per_cta);
@@ -1190,6 +1482,7 @@ private:
                 owner[e] = c;
                 ++ctaTetPtr[c + 1];
                 for (int k = 0; k < 4; ++k) {
+                    if (H.tets[4 * (size_t)e + k] < 0) continue;  // a triangle element has three vertices
                     const int c2 = ctaOfRow[H.tets[4 * (size_t)e + k]];
                     rng[c].x = std::min(rng[c].x, c2);
                     rng[c].y = std::max(rng[c].y, c2);
@@ -1405,7 +1698,7 @@ private:
             PD_CK(cudaMemsetAsync(d.PairCount, 0, sizeof(unsigned long long), s_));
             PD_CK(cudaMemsetAsync(cpt_, 0, sizeof(int64_t) * d.capPairs, s_));
             PD_CK(cudaMemsetAsync(cee_, 0, sizeof(int64_t) * d.capPairs, s_));
-            launch_traverse(d, cpt_, cee_, d.capPairs, d.PairCount, s_);
+            launch_traverse(d, cpt_, cee_, d.capPairs, d.PairCount, c_, s_);
             scan_exclusive_i64(cpt_, opt_, d.capPairs, opt_ + d.capPairs, scan_tmp_, s_);
             scan_exclusive_i64(cee_, oee_, d.capPairs, oee_ + d.capPairs, scan_tmp_, s_);
             launches_ += 5;
@@ -1422,7 +1715,7 @@ private:
         d.nEE = pin_->n_ee;
         PD_CK(grow(d.PT, d.capPT, d.nPT));
         PD_CK(grow(d.EE, d.capEE, d.nEE));
-        launch_expand(d, opt_, oee_, s_);
+        launch_expand(d, opt_, oee_, c_, s_);
         ++launches_;
         st_.patch_pairs = d.nPairs;
         st_.pt_candidates = d.nPT;
@@ -1710,6 +2003,8 @@ private:
            *adj_u_ = nullptr, *adj_rho_ = nullptr;
     std::vector<V4<TC>*> adj_xb_, adj_xs_, adj_ys_;
     PersistPlan plan_;
+    std::vector<PlanChoice> plan_choices_;  // every persistent configuration that fits (default planning)
+    pdipc_tuning tuning_{};
     std::vector<int> sliceOffH_, sliceLenH_;
     PersistArgs<float, TC> pargs_{};
     int* pCtaSlice_ = nullptr;

@@ -45,6 +45,7 @@ public:
                                           std::string& err) = 0;
     // limit of the persistent solve's device-side waits, microseconds (0 = 2 s)
     virtual void set_wait_limit(int us) = 0;
+    virtual void tuning(pdipc_tuning* out) = 0;
     virtual int n_sim() const = 0;
     virtual int n_total() const = 0;
 };

@@ -180,5 +180,52 @@ __device__ __forceinline__ void tet_project(const R (&Ds)[3][3], const R* idm, R
         for (int r = 0; r < 3; ++r) out[c][r] = w * (Rm[r][0] * G[0][c] + Rm[r][1] * G[1][c] + Rm[r][2] * G[2][c]);
 }
 
+// The same strain limit for a cloth triangle (an element with three
+// vertices): F = Ds Dm^-1 (3 x 2: the deformed edges x1 - x0, x2 - x0 over the
+// rest edges in the rest triangle's own orthonormal frame, idm = Dm^-1
+// row-major 2 x 2).  F takes the deformed unit normal as a third column, so the
+// 3 x 3 F has singular values (s0, s1, 1) and det F > 0 (no flip); its SVD,
+// clamped to [0.999, 1.001] as above, gives R = U S' V^T, whose first two
+// columns P are the projection of F.  out[c] = w P G[c] with G = S Dm^-1, S
+// the edge-selection rows (-1, -1), (1, 0), (0, 1).  A triangle folded flat
+// (zero normal) keeps the third column zero and still projects its two
+// in-plane directions.
+template <typename R>
+__device__ __forceinline__ void tri_project(const R (&Ds)[3][2], const R* idm, R w, R (&out)[3][3]) {
+    R F[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        F[i][0] = Ds[i][0] * idm[0] + Ds[i][1] * idm[2];
+        F[i][1] = Ds[i][0] * idm[1] + Ds[i][1] * idm[3];
+    }
+    R n[3] = {F[1][0] * F[2][1] - F[2][0] * F[1][1], F[2][0] * F[0][1] - F[0][0] * F[2][1],
+              F[0][0] * F[1][1] - F[1][0] * F[0][1]};
+    const R nn = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+    const R inv = nn > R(0) ? R(1) / dsqrt(nn) : R(0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) F[i][2] = n[i] * inv;
+    R U[3][3], s[3], V[3][3];
+    svd3(F, U, s, V);
+    R sc[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const R a = s[k] < R(0) ? -s[k] : s[k];
+        R v = a < R(1.001) ? a : R(1.001);
+        sc[k] = v < R(0.999) ? R(0.999) : v;
+        if (s[k] < R(0)) sc[k] = -sc[k];  // rank-deficient F only: keep U S V^T's orientation
+    }
+    R P[3][2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+            P[i][j] = U[i][0] * sc[0] * V[j][0] + U[i][1] * sc[1] * V[j][1] + U[i][2] * sc[2] * V[j][2];
+    const R G[3][2] = {{-(idm[0] + idm[2]), -(idm[1] + idm[3])}, {idm[0], idm[1]}, {idm[2], idm[3]}};
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) out[c][r] = w * (P[r][0] * G[c][0] + P[r][1] * G[c][1]);
+}
+
 }  // namespace svd
 }  // namespace pdipc

@@ -14,8 +14,8 @@ import os
 
 import numpy as np
 
-from .abi import (PDIPC_ERR_CUDA, PDIPC_ERR_OVERFLOW, PDIPC_OK, PRECISIONS, STATUS_NAMES, Params,  # noqa: F401
-                  SceneModel, Stats, default_params, params_for_scene)
+from .abi import (PDIPC_ERR_CUDA, PDIPC_ERR_OVERFLOW, PDIPC_OK, PRECISIONS, STATUS_NAMES, ClothOptions,  # noqa: F401
+                  Params, SceneModel, Stats, Tuning, default_params, params_for_scene)
 from . import scenes  # noqa: F401
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -37,7 +37,8 @@ EXPORTS = [
     "pdipc_scene_load", "pdipc_scene_model_count", "pdipc_scene_get_model", "pdipc_scene_apply_params",
     "pdipc_scene_add_models", "pdipc_scene_free", "pdipc_stage_penalty_predict", "pdipc_stage_penalty_ccd",
     "pdipc_stage_penalty_floor", "pdipc_stage_penalty_dcd", "pdipc_adjoint_record", "pdipc_adjoint_backward",
-    "pdipc_set_wait_limit", "pdipc_stage_local_timing",
+    "pdipc_set_wait_limit", "pdipc_stage_local_timing", "pdipc_get_tuning", "pdipc_add_cloth_ex",
+    "pdipc_stretch_gradient_per_triangle",
 ]
 
 
@@ -68,6 +69,9 @@ def load_library(path: str | None = None):
     L.pdipc_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
     L.pdipc_add_cloth.argtypes = [vp, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double, C.c_double, _ip,
                                   C.c_int, C.c_double, C.c_int]
+    L.pdipc_add_cloth_ex.argtypes = [vp, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double, C.c_double, _ip,
+                                     C.c_int, C.c_double, C.c_int, C.POINTER(ClothOptions)]
+    L.pdipc_stretch_gradient_per_triangle.argtypes = [vp, C.c_int, _dp, _dp]
     L.pdipc_add_static.argtypes = [vp, _dp, C.c_int, _ip, C.c_int, C.c_int]
     L.pdipc_tet_surface.argtypes = [_dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip]
     L.pdipc_scene_load.argtypes = [C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_int]
@@ -89,6 +93,7 @@ def load_library(path: str | None = None):
     L.pdipc_set_state.argtypes = [vp, _dp, _dp]
     L.pdipc_reset.argtypes = [vp]
     L.pdipc_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    L.pdipc_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.pdipc_save.argtypes = [vp, C.c_char_p]
     L.pdipc_load.argtypes = [vp, C.c_char_p]
     L.pdipc_destroy.argtypes = [vp]
@@ -146,9 +151,12 @@ class Simulator:
             raise PdipcError(rc, "pdipc_create", "no usable GB300 (sm_103) device" if rc == PDIPC_ERR_CUDA else "")
         self.n_sim = 0
         self.n_total = 0
+        self.cloth_faces = []
         if scene is not None:
             for c in scene.cloths:
-                self.add_cloth(c.X, c.F, c.pins, c.density, c.k_stretch, c.k_bend, c.k_pin, c.patch_dim)
+                self.add_cloth(c.X, c.F, c.pins, c.density, c.k_stretch, c.k_bend, c.k_pin, c.patch_dim,
+                               tri_stretch=getattr(c, "tri_stretch", None), k_tri_strain=getattr(c, "k_tri_strain", 0.0),
+                               tri_strain=getattr(c, "tri_strain", None))
             for v in getattr(scene, "solids", []):
                 self.add_volumetric(v.X, v.T, v.pins, v.density, v.k_strain, v.k_volume, v.k_pin, v.patch_dim)
             for s in scene.statics:
@@ -162,15 +170,40 @@ class Simulator:
             detail = load_library().pdipc_last_error(self.h).decode(errors="replace") if self.h else ""
             raise PdipcError(rc, what, detail)
 
-    def add_cloth(self, X, F, pins=(), density=0.1, k_stretch=1e4, k_bend=1e-3, k_pin=1e6, patch_dim=10):
+    def add_cloth(self, X, F, pins=(), density=0.1, k_stretch=1e4, k_bend=1e-3, k_pin=1e6, patch_dim=10,
+                  tri_stretch=None, k_tri_strain=0.0, tri_strain=None):
+        """pdipc_add_cloth_ex: optional per-triangle stretch stiffness (nf), and a
+        triangle strain limit (weight k_tri_strain, or per-triangle tri_strain,
+        times rest area)."""
         X = np.ascontiguousarray(X, dtype=np.float64)
         F = np.ascontiguousarray(F, dtype=np.int32)
         P = np.ascontiguousarray(pins, dtype=np.int32)
-        self._check(load_library().pdipc_add_cloth(self.h, _d(X), X.shape[0], _i(F), F.shape[0], density,
-                                                   k_stretch, k_bend, _i(P), P.shape[0], k_pin, patch_dim),
-                    "pdipc_add_cloth")
+        opt = ClothOptions()
+        keep = []
+        if tri_stretch is not None:
+            ts = np.ascontiguousarray(tri_stretch, dtype=np.float64).reshape(F.shape[0])
+            keep.append(ts)
+            opt.per_tri_stretch = _d(ts)
+        opt.k_tri_strain = float(k_tri_strain)
+        if tri_strain is not None:
+            tk = np.ascontiguousarray(tri_strain, dtype=np.float64).reshape(F.shape[0])
+            keep.append(tk)
+            opt.per_tri_strain = _d(tk)
+        self._check(load_library().pdipc_add_cloth_ex(self.h, _d(X), X.shape[0], _i(F), F.shape[0], density,
+                                                      k_stretch, k_bend, _i(P), P.shape[0], k_pin, patch_dim,
+                                                      C.byref(opt)), "pdipc_add_cloth_ex")
+        self.cloth_faces.append(F.shape[0])
         self.n_sim += X.shape[0]
         self.n_total += X.shape[0]
+
+    def stretch_gradient_per_triangle(self, dl_dvertex, cloth_index=0):
+        """dL/d(per-triangle stretch stiffness) of one cloth from dL/d(per-vertex
+        stretch stiffness) (pdipc_stretch_gradient_per_triangle)."""
+        g = np.ascontiguousarray(dl_dvertex, dtype=np.float64).reshape(self.n_sim)
+        out = np.empty(self.cloth_faces[cloth_index], np.float64)
+        self._check(load_library().pdipc_stretch_gradient_per_triangle(self.h, int(cloth_index), _d(g), _d(out)),
+                    "pdipc_stretch_gradient_per_triangle")
+        return out
 
     def add_volumetric(self, X, T, pins=(), density=1000.0, k_strain=1e6, k_volume=1e3, k_pin=1e12, patch_dim=10):
         X = np.ascontiguousarray(X, dtype=np.float64)
@@ -241,6 +274,13 @@ class Simulator:
         s = Stats()
         self._check(load_library().pdipc_get_stats(self.h, C.byref(s)), "pdipc_get_stats")
         return s.as_dict()
+
+    def tuning(self) -> dict:
+        """The launch configuration (pdipc_get_tuning): chosen by the autotuner
+        when the context was created with autotune=1."""
+        t = Tuning()
+        self._check(load_library().pdipc_get_tuning(self.h, C.byref(t)), "pdipc_get_tuning")
+        return t.as_dict()
 
     def save(self, path: str):
         self._check(load_library().pdipc_save(self.h, path.encode()), "pdipc_save")

@@ -98,6 +98,16 @@ def params_for_scene(scene, precision="fp32", **overrides) -> Params:
     return p
 
 
+class ClothOptions(C.Structure):
+    """pdipc_cloth_options of pdipc_add_cloth_ex."""
+    _fields_ = [
+        ("per_tri_stretch", C.POINTER(C.c_double)),
+        ("k_tri_strain", C.c_double),
+        ("per_tri_strain", C.POINTER(C.c_double)),
+        ("reserved", C.c_int32 * 8),
+    ]
+
+
 class SceneModel(C.Structure):
     _fields_ = [
         ("name", C.c_char_p),
@@ -146,3 +156,29 @@ class Stats(C.Structure):
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    """pdipc_tuning: the launch configuration of a context and how it was chosen."""
+    _fields_ = [
+        ("autotuned", C.c_int32),
+        ("from_cache", C.c_int32),
+        ("pd_rows_per_thread", C.c_int32),
+        ("pd_ctas", C.c_int32),
+        ("pd_band", C.c_int32),
+        ("pd_l1_gather", C.c_int32),
+        ("pd_local_sync", C.c_int32),
+        ("cand_grid", C.c_int32),
+        ("traverse_block", C.c_int32),
+        ("expand_block", C.c_int32),
+        ("candidates_timed", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("pd_solve_ms", C.c_double),
+        ("pd_default_ms", C.c_double),
+        ("collision_ms", C.c_double),
+        ("collision_default_ms", C.c_double),
+        ("reserved", C.c_int32 * 8),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if not name.startswith("reserved")}

@@ -138,6 +138,12 @@ class ClothSpec:
     k_bend: float = 1e-3
     k_pin: float = 1e6
     patch_dim: int = 10
+    # optional (pdipc_add_cloth_ex): per-triangle stretch stiffness (nf values),
+    # and a triangle strain limit of weight k_tri_strain (or per-triangle
+    # tri_strain) times rest area
+    tri_stretch: np.ndarray | None = None
+    k_tri_strain: float = 0.0
+    tri_strain: np.ndarray | None = None
 
 
 @dataclasses.dataclass
