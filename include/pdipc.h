@@ -198,6 +198,16 @@ pdipc_status pdipc_add_cloth_ex(pdipc_ctx* ctx, const double* X, int nv, const i
                                 double k_stretch, double k_bend, const int* pins, int npins, double k_pin,
                                 int patch_dim, const pdipc_cloth_options* opt);
 
+/* Partition of a batch of independent instances (each cloth with its own
+ * obstacles, nothing shared between instances) over `ranks` processes, one GPU
+ * each, on the host: instance i has sizes[i] simulated vertices; rank r takes
+ * instances [first[r], first[r + 1]) (first: ranks + 1 ints), contiguous runs
+ * whose cumulative vertex counts split the total as evenly as whole instances
+ * allow (the boundary after rank r is the instance boundary nearest to r + 1
+ * shares of the total).  The step needs no exchange between ranks.  No
+ * counterpart in the reference (one process, one GPU). */
+pdipc_status pdipc_partition_instances(const int64_t* sizes, int n, int ranks, int* first);
+
 /* Chain rule of the per-triangle stretch mapping, on the host: given the
  * gradient of a loss with respect to every simulated vertex's stretch stiffness
  * (dl_dvertex, n_sim, as pdipc_adjoint_backward returns it), the gradient with

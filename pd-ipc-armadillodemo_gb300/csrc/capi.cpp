@@ -225,6 +225,30 @@ pdipc_status pdipc_add_cloth_ex(pdipc_ctx* ctx, const double* X, int nv, const i
     });
 }
 
+pdipc_status pdipc_partition_instances(const int64_t* sizes, int n, int ranks, int* first) {
+    if (!sizes || !first || n < 0 || ranks < 1) return PDIPC_ERR_ARG;
+    int64_t total = 0;
+    for (int i = 0; i < n; ++i) {
+        if (sizes[i] < 0) return PDIPC_ERR_ARG;
+        total += sizes[i];
+    }
+    // rank r ends after the first instance whose running count reaches
+    // (r + 1) / ranks of the total, rounding the boundary to the nearer side
+    first[0] = 0;
+    int i = 0;
+    int64_t run = 0;
+    for (int r = 0; r < ranks; ++r) {
+        const double goal = (double)total * (double)(r + 1) / (double)ranks;
+        while (i < n && (double)(run + sizes[i]) <= goal) run += sizes[i++];
+        if (i < n && r + 1 < ranks) {  // the instance that crosses the goal: to whichever side is nearer
+            const double over = (double)(run + sizes[i]) - goal, under = goal - (double)run;
+            if (over < under) run += sizes[i++];
+        }
+        first[r + 1] = (r + 1 == ranks) ? n : i;
+    }
+    return PDIPC_OK;
+}
+
 pdipc_status pdipc_stretch_gradient_per_triangle(pdipc_ctx* ctx, int cloth_index, const double* dl_dvertex,
                                                  double* dl_dtri) {
     if (!ctx) return PDIPC_ERR_ARG;

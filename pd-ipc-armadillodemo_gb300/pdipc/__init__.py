@@ -38,7 +38,7 @@ EXPORTS = [
     "pdipc_scene_add_models", "pdipc_scene_free", "pdipc_stage_penalty_predict", "pdipc_stage_penalty_ccd",
     "pdipc_stage_penalty_floor", "pdipc_stage_penalty_dcd", "pdipc_adjoint_record", "pdipc_adjoint_backward",
     "pdipc_set_wait_limit", "pdipc_stage_local_timing", "pdipc_get_tuning", "pdipc_add_cloth_ex",
-    "pdipc_stretch_gradient_per_triangle",
+    "pdipc_stretch_gradient_per_triangle", "pdipc_partition_instances",
 ]
 
 
@@ -72,6 +72,7 @@ def load_library(path: str | None = None):
     L.pdipc_add_cloth_ex.argtypes = [vp, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double, C.c_double, _ip,
                                      C.c_int, C.c_double, C.c_int, C.POINTER(ClothOptions)]
     L.pdipc_stretch_gradient_per_triangle.argtypes = [vp, C.c_int, _dp, _dp]
+    L.pdipc_partition_instances.argtypes = [_i64p, C.c_int, C.c_int, _ip]
     L.pdipc_add_static.argtypes = [vp, _dp, C.c_int, _ip, C.c_int, C.c_int]
     L.pdipc_tet_surface.argtypes = [_dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip]
     L.pdipc_scene_load.argtypes = [C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_int]
@@ -459,6 +460,17 @@ def mesh_topology(X, F, patch_dim):
     n_e, n_p = ne.value, npch.value
     patches = [pf[poff[p]:poff[p + 1]].copy() for p in range(n_p)]
     return edges[:n_e].copy(), patches, own_p, own_e[:n_e].copy()
+
+
+def partition_instances(sizes, ranks: int) -> np.ndarray:
+    """pdipc_partition_instances (host only): instance ranges [first[r], first[r+1])
+    of `ranks` processes balancing the cumulative simulated-vertex counts."""
+    s = np.ascontiguousarray(sizes, dtype=np.int64)
+    first = np.empty(ranks + 1, np.int32)
+    rc = load_library().pdipc_partition_instances(s.ctypes.data_as(_i64p), int(s.shape[0]), int(ranks), _i(first))
+    if rc != PDIPC_OK:
+        raise PdipcError(rc, "pdipc_partition_instances")
+    return first
 
 
 def create_simulator(sim_name: str, scene=None, **kw):

@@ -278,6 +278,14 @@ def batched(count: int = 256, nmin: int = 16, nmax: int = 128, seed: int = 0,
     return Scene(f"batched{count}_{nmin}to{nmax}", cloths, statics, lg_iterations=lg, steps=steps)
 
 
+def instance_slice(scene: Scene, first: int, last: int) -> Scene:
+    """Instances [first, last) of a batched scene (cloth k with its obstacle k),
+    as their own scene: what one rank steps when the batch is partitioned."""
+    return Scene(f"{scene.name}[{first}:{last}]", scene.cloths[first:last], scene.statics[first:last],
+                 dt=scene.dt, gravity=scene.gravity, dhat=scene.dhat, kappa=scene.kappa,
+                 lg_iterations=scene.lg_iterations, steps=scene.steps)
+
+
 def config2(seed: int = 0) -> Scene:
     """256 independent drops, cloth sides U{16..128}, in one context, 100 steps."""
     sc = batched(256, 16, 128, seed=seed, lg=10, steps=100)
