@@ -90,4 +90,8 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # the reference tree: the first argument, else $PDIPC_REFERENCE_DIR
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PDIPC_REFERENCE_DIR")
+    if not ref:
+        raise SystemExit("usage: make_example_fixtures.py <reference tree> (or set PDIPC_REFERENCE_DIR)")
+    main(ref)

@@ -1,18 +1,20 @@
 """The scene reader (pdipc_scene_load): a reference-format config.xml with its
 OBJ, tetgen and fixed_points.txt files, written here from the seeded
 generators; placement (origin, uniform, scale, translation) checked against
-the same transforms in numpy; and, when the reference example is present on
-this machine, its ClothArmadillo scene."""
+the same transforms in numpy; and, when the reference tree is given
+($PDIPC_REFERENCE_DIR), its ClothArmadillo example scene."""
 import os
 
 import numpy as np
 import pytest
 
 import pdipc
+from oracle import build_ref
 from oracle.oracle import FORM_JJ, Oracle
 from pdipc import scenes
 
-EXAMPLE = "/root/reference/example/ClothArmadillo/config.xml"
+_REF = build_ref.reference_dir()
+EXAMPLE = os.path.join(_REF, "example", "ClothArmadillo", "config.xml") if _REF else ""
 
 
 def write_obj(path, X, F):
@@ -112,7 +114,7 @@ def test_reader_reports_missing_files(tmp_path, built_lib):
     assert "nothing.obj" in str(e.value)
 
 
-@pytest.mark.skipif(not os.path.exists(EXAMPLE), reason="reference example not on this machine")
+@pytest.mark.skipif(not EXAMPLE or not os.path.exists(EXAMPLE), reason="reference tree not given")
 def test_reads_the_reference_cloth_armadillo_example(built_lib):
     sc = pdipc.read_scene(EXAMPLE)
     assert (sc.dt, sc.gravity, sc.dhat, sc.kappa) == (0.01, -9.8, 5e-3, 5e7)
