@@ -93,9 +93,15 @@ typedef struct {
                                 grid barrier, halo copies), in microseconds at the maximum SM clock; past
                                 it the launch ends and the step returns PDIPC_ERR_CUDA; 0 = 2 s.  The
                                 reference has no device-side waits (one launch per kernel). */
-    int autotune;            /* 1: choose launch shapes by timing candidates on the first step (see
+    int autotune;            /* 1: choose launch shapes by timing candidates at pdipc_initialize (see
                                 pdipc_get_tuning); 0: the built-in defaults */
-    int reserved[4];
+    int ccd_mode;            /* 0: the reference's additive CCD (PdIpcGpuFunc.cu:2460-2607); 1: plus an FP64
+                                coplanarity-cubic root solve per candidate (the PolynomialSolver path the
+                                reference compiles but never calls, Commom/PolynomialSolver.h:10-60), which
+                                can only lower a candidate's time of impact; 2: the FP64 cubic alone, the
+                                exact first-contact time of every candidate (the step then stops at
+                                toi_scale of the first contact instead of the additive CCD's gap) */
+    int reserved[3];
 } pdipc_params;
 
 /* Per-context statistics of the most recent pdipc_step call. */

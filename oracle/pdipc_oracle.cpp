@@ -440,6 +440,130 @@ static void tri_project(const R* x0, const R* x1, const R* x2, const R* idm, R w
     out[3][0] = out[3][1] = out[3][2] = R(0);
 }
 
+// FP64 coplanarity-cubic CCD of one candidate (pdipc_params.ccd_mode 1; no
+// reference kernel: the reference compiles Commom/PolynomialSolver.h:10-60 and
+// never calls it).  Four points moving linearly are coplanar where
+// f(t) = u1 . (u2 x u3) = 0, u_k(t) = (x_k - x_0) + t (d_k - d_0), a cubic; its
+// roots in [0, 1] come from bisecting the monotone pieces between the roots of
+// f'; the first root where the primitives touch (point inside the triangle,
+// edges crossing; relative tolerance 1e-6 toward contact) is the time of
+// impact, else 1.  PT: x_0 the point; EE: edges (x_0, x_1), (x_2, x_3).
+static double cubic_eval(const double c[4], double t) { return ((c[3] * t + c[2]) * t + c[1]) * t + c[0]; }
+static double dot3d(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static void cross3d(const double* a, const double* b, double* r) {
+    r[0] = a[1] * b[2] - a[2] * b[1];
+    r[1] = a[2] * b[0] - a[0] * b[2];
+    r[2] = a[0] * b[1] - a[1] * b[0];
+}
+template <bool kPT>
+static bool touching_at(const double (*x)[3], const double (*d)[3], double t, double tol) {
+    double p[4][3];
+    for (int j = 0; j < 4; ++j)
+        for (int k = 0; k < 3; ++k) p[j][k] = x[j][k] + t * d[j][k];
+    auto sub = [](const double* a, const double* b, double* r) {
+        for (int k = 0; k < 3; ++k) r[k] = a[k] - b[k];
+    };
+    if (kPT) {
+        double e1[3], e2[3], n[3], a[3], b[3], c[3], q[3];
+        sub(p[2], p[1], e1);
+        sub(p[3], p[1], e2);
+        cross3d(e1, e2, n);
+        const double nn = dot3d(n, n);
+        if (!(nn > 0.0)) return false;
+        sub(p[1], p[0], a);
+        sub(p[2], p[0], b);
+        sub(p[3], p[0], c);
+        cross3d(b, c, q);
+        const double wa = dot3d(q, n) / nn;
+        cross3d(c, a, q);
+        const double wb = dot3d(q, n) / nn;
+        cross3d(a, b, q);
+        const double wc = dot3d(q, n) / nn;
+        return wa >= -tol && wb >= -tol && wc >= -tol;
+    }
+    double ea[3], eb[3], w[3];
+    sub(p[1], p[0], ea);
+    sub(p[3], p[2], eb);
+    sub(p[0], p[2], w);
+    const double aa = dot3d(ea, ea), bb = dot3d(eb, eb), ab = dot3d(ea, eb);
+    const double den = aa * bb - ab * ab;
+    if (!(den > 1e-24 * aa * bb)) return false;
+    const double wa = dot3d(w, ea), wb = dot3d(w, eb);
+    const double s = (ab * wb - bb * wa) / den, u = (aa * wb - ab * wa) / den;
+    return s >= -tol && s <= 1.0 + tol && u >= -tol && u <= 1.0 + tol;
+}
+template <bool kPT>
+static double ccd_cubic(const double (*x)[3], const double (*d)[3]) {
+    double u0[3][3], u1[3][3];
+    for (int k = 0; k < 3; ++k)
+        for (int a = 0; a < 3; ++a) {
+            u0[k][a] = x[k + 1][a] - x[0][a];
+            u1[k][a] = d[k + 1][a] - d[0][a];
+        }
+    double c[4], bc[3], t1[3], t2[3], t3[3];
+    cross3d(u0[1], u0[2], bc);
+    c[0] = dot3d(u0[0], bc);
+    cross3d(u1[1], u0[2], t1);
+    cross3d(u0[1], u1[2], t2);
+    c[1] = dot3d(u1[0], bc) + dot3d(u0[0], t1) + dot3d(u0[0], t2);
+    cross3d(u1[1], u1[2], t3);
+    c[2] = dot3d(u1[0], t1) + dot3d(u1[0], t2) + dot3d(u0[0], t3);
+    c[3] = dot3d(u1[0], t3);
+    double scale = 0.0;
+    for (int k = 0; k < 3; ++k)
+        scale = std::max(scale, std::max(std::sqrt(dot3d(u0[k], u0[k])), std::sqrt(dot3d(u1[k], u1[k]))));
+    const double s3 = scale * scale * scale;
+    if (!(s3 > 0.0) || !(std::fabs(c[0]) + std::fabs(c[1]) + std::fabs(c[2]) + std::fabs(c[3]) > 1e-14 * s3))
+        return 1.0;
+    double br[4] = {0.0, 1.0, 1.0, 1.0};
+    int nb = 1;
+    {
+        const double A = 3.0 * c[3], B = 2.0 * c[2], C = c[1];
+        double r0 = 2.0, r1 = 2.0;
+        if (std::fabs(A) > 1e-300) {
+            const double disc = B * B - 4.0 * A * C;
+            if (disc >= 0.0) {
+                const double q = -0.5 * (B + std::copysign(std::sqrt(disc), B));
+                r0 = q / A;
+                r1 = q != 0.0 ? C / q : r0;
+            }
+        } else if (std::fabs(B) > 1e-300) {
+            r0 = -C / B;
+        }
+        if (r0 > r1) std::swap(r0, r1);
+        if (r0 > 0.0 && r0 < 1.0) br[nb++] = r0;
+        if (r1 > 0.0 && r1 < 1.0 && r1 != r0) br[nb++] = r1;
+        br[nb] = 1.0;
+    }
+    const double tol = 1e-6;
+    for (int s = 0; s < nb; ++s) {
+        double lo = br[s], hi = br[s + 1];
+        double flo = cubic_eval(c, lo);
+        const double fhi = cubic_eval(c, hi);
+        double root;
+        if (flo == 0.0) {
+            root = lo;
+        } else if ((flo < 0.0) != (fhi < 0.0) || fhi == 0.0) {
+            for (int it = 0; it < 64 && hi - lo > 0.0; ++it) {
+                const double mid = 0.5 * (lo + hi);
+                if (mid <= lo || mid >= hi) break;
+                const double fm = cubic_eval(c, mid);
+                if ((fm < 0.0) == (flo < 0.0) && fm != 0.0) {
+                    lo = mid;
+                    flo = fm;
+                } else {
+                    hi = mid;
+                }
+            }
+            root = lo;
+        } else {
+            continue;
+        }
+        if (touching_at<kPT>(x, d, root, tol) || touching_at<kPT>(x, d, hi, tol)) return root;
+    }
+    return 1.0;
+}
+
 // Morton code of a quantised, centred patch centre.  The reference calls the
 // un-vendored Resorting::MortonCode64(int,int,int) (AipcBvhs.cpp:181); this is
 // the 63-bit interleave used by the library: each coordinate offset by 2^20,
@@ -1188,27 +1312,31 @@ struct Sim {
     }
     static TC mn3(TC a, TC b, TC c) { return std::min(std::min(a, b), c); }
     static TC mx3(TC a, TC b, TC c) { return std::max(std::max(a, b), c); }
-    static bool pt_ccd_broad(const TC* p, const TC* t0, const TC* t1, const TC* t2, const TC* dp, const TC* d0,
-                             const TC* d1, const TC* d2, TC dist) {
+    template <typename R>
+    static bool pt_ccd_broad(const R* p, const R* t0, const R* t1, const R* t2, const R* dp, const R* d0,
+                             const R* d1, const R* d2, R dist) {
+        auto lo3 = [](R a, R b, R c) { return std::min(std::min(a, b), c); };
+        auto hi3 = [](R a, R b, R c) { return std::max(std::max(a, b), c); };
         for (int k = 0; k < 3; ++k) {
-            TC tmin = mn3(t0[k], t1[k], t2[k]);
-            tmin = mn3(tmin, t0[k] + d0[k], t1[k] + d1[k]);
+            R tmin = lo3(t0[k], t1[k], t2[k]);
+            tmin = lo3(tmin, t0[k] + d0[k], t1[k] + d1[k]);
             tmin = std::min(tmin, t2[k] + d2[k]);
-            TC tmax = mx3(t0[k], t1[k], t2[k]);
-            tmax = mx3(tmax, t0[k] + d0[k], t1[k] + d1[k]);
+            R tmax = hi3(t0[k], t1[k], t2[k]);
+            tmax = hi3(tmax, t0[k] + d0[k], t1[k] + d1[k]);
             tmax = std::max(tmax, t2[k] + d2[k]);
-            TC pmin = std::min(p[k], p[k] + dp[k]), pmax = std::max(p[k], p[k] + dp[k]);
+            R pmin = std::min(p[k], p[k] + dp[k]), pmax = std::max(p[k], p[k] + dp[k]);
             if ((pmin - tmax) > dist || (tmin - pmax) > dist) return false;
         }
         return true;
     }
-    static bool ee_ccd_broad(const TC* a0, const TC* a1, const TC* b0, const TC* b1, const TC* da0, const TC* da1,
-                             const TC* db0, const TC* db1, TC dist) {
+    template <typename R>
+    static bool ee_ccd_broad(const R* a0, const R* a1, const R* b0, const R* b1, const R* da0, const R* da1,
+                             const R* db0, const R* db1, R dist) {
         for (int k = 0; k < 3; ++k) {
-            TC mina = std::min(a0[k], a0[k] + da0[k]); mina = std::min(mina, a1[k]); mina = std::min(mina, a1[k] + da1[k]);
-            TC maxa = std::max(a0[k], a0[k] + da0[k]); maxa = std::max(maxa, a1[k]); maxa = std::max(maxa, a1[k] + da1[k]);
-            TC minb = std::min(b0[k], b0[k] + db0[k]); minb = std::min(minb, b1[k]); minb = std::min(minb, b1[k] + db1[k]);
-            TC maxb = std::max(b0[k], b0[k] + db0[k]); maxb = std::max(maxb, b1[k]); maxb = std::max(maxb, b1[k] + db1[k]);
+            R mina = std::min(a0[k], a0[k] + da0[k]); mina = std::min(mina, a1[k]); mina = std::min(mina, a1[k] + da1[k]);
+            R maxa = std::max(a0[k], a0[k] + da0[k]); maxa = std::max(maxa, a1[k]); maxa = std::max(maxa, a1[k] + da1[k]);
+            R minb = std::min(b0[k], b0[k] + db0[k]); minb = std::min(minb, b1[k]); minb = std::min(minb, b1[k] + db1[k]);
+            R maxb = std::max(b0[k], b0[k] + db0[k]); maxb = std::max(maxb, b1[k]); maxb = std::max(maxb, b1[k] + db1[k]);
             if ((mina - maxb) > dist || (minb - maxa) > dist) return false;
         }
         return true;
@@ -1288,8 +1416,12 @@ struct Sim {
         load4(xa, c, p);
         load4(xb, c, q);
         for (int j = 0; j < 4; ++j) for (int k = 0; k < 3; ++k) d[j][k] = q[j][k] - p[j][k];
-        if (!pt_ccd_broad(p[0], p[1], p[2], p[3], d[0], d[1], d[2], d[3], (TC)prm.ccd_slack)) return 1;
-        return ccd_pt(p[0], d[0], p[1], d[1], p[2], d[2], p[3], d[3]);
+        if (prm.ccd_mode == 2) return (TC)cubic_toi<true>(c, xa, xb);
+        TC t = 1;
+        if (pt_ccd_broad(p[0], p[1], p[2], p[3], d[0], d[1], d[2], d[3], (TC)prm.ccd_slack))
+            t = ccd_pt(p[0], d[0], p[1], d[1], p[2], d[2], p[3], d[3]);
+        if (prm.ccd_mode == 1) t = std::min(t, (TC)cubic_toi<true>(c, xa, xb));
+        return t;
     }
     TC toi_ee_one(const std::array<int, 4>& c, const std::vector<T>& xa, const std::vector<T>& xb) const {
         if (c[0] == c[2] || c[0] == c[3] || c[1] == c[2] || c[1] == c[3]) return 1;
@@ -1297,8 +1429,31 @@ struct Sim {
         load4(xa, c, p);
         load4(xb, c, q);
         for (int j = 0; j < 4; ++j) for (int k = 0; k < 3; ++k) d[j][k] = q[j][k] - p[j][k];
-        if (!ee_ccd_broad(p[0], p[1], p[2], p[3], d[0], d[1], d[2], d[3], (TC)prm.ccd_slack)) return 1;
-        return ccd_ee(p[0], d[0], p[1], d[1], p[2], d[2], p[3], d[3]);
+        if (prm.ccd_mode == 2) return (TC)cubic_toi<false>(c, xa, xb);
+        TC t = 1;
+        if (ee_ccd_broad(p[0], p[1], p[2], p[3], d[0], d[1], d[2], d[3], (TC)prm.ccd_slack))
+            t = ccd_ee(p[0], d[0], p[1], d[1], p[2], d[2], p[3], d[3]);
+        if (prm.ccd_mode == 1) t = std::min(t, (TC)cubic_toi<false>(c, xa, xb));
+        return t;
+    }
+    // ccd_mode 1: the FP64 coplanarity-cubic time of impact of one candidate
+    // (the swept-box test in FP64, then orc::ccd_cubic on coordinates relative
+    // to the first point); 1 when it finds no contact.
+    template <bool kPT>
+    double cubic_toi(const std::array<int, 4>& c, const std::vector<T>& xa, const std::vector<T>& xb) const {
+        double p[4][3], d[4][3];
+        for (int j = 0; j < 4; ++j)
+            for (int k = 0; k < 3; ++k) {
+                p[j][k] = (double)(TC)xa[3 * (size_t)c[j] + k];
+                d[j][k] = (double)(TC)xb[3 * (size_t)c[j] + k] - p[j][k];
+            }
+        const double sl = prm.ccd_slack;
+        const bool near = kPT ? pt_ccd_broad(p[0], p[1], p[2], p[3], d[0], d[1], d[2], d[3], sl)
+                              : ee_ccd_broad(p[0], p[1], p[2], p[3], d[0], d[1], d[2], d[3], sl);
+        if (!near) return 1.0;
+        for (int j = 3; j >= 0; --j)
+            for (int k = 0; k < 3; ++k) p[j][k] -= p[0][k];
+        return ccd_cubic<kPT>(p, d);
     }
     // global toi: min over candidates (NaN results never win, as in the
     // reference's `toi < toiList` test), then times 0.98 if below 1.

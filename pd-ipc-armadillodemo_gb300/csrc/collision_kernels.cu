@@ -700,6 +700,48 @@ __global__ void __launch_bounds__(kBlock, kCandBlocks<T>) k_toi(int64_t n, const
     block_min_to(local, toi_min);
 }
 
+// ccd_mode 1: the FP64 coplanarity-cubic pass over the same candidates, after
+// k_toi.  Candidates that pass the shared-vertex and swept-box tests (in
+// FP64) get geo::ccd_cubic; a result below the additive CCD's lowers the
+// candidate's time of impact and the running minimum.  FP64 on the GPU is
+// kept to this root solve and the few candidates that reach it.
+// kAlone (ccd_mode 2): no additive CCD ran, so every candidate's entry is
+// written here (1 where the cubic finds no contact).
+template <typename TC, bool kPT, bool kAlone>
+__global__ void __launch_bounds__(kBlock) k_toi_cubic(int64_t n, const int4* __restrict__ cand,
+                                                      const V4<TC>* __restrict__ X0, const V4<TC>* __restrict__ X1,
+                                                      double slack, TC* __restrict__ per, TC* __restrict__ toi_min,
+                                                      const OuterGate* __restrict__ gate) {
+    if (outer_stopped(gate)) return;
+    TC local = TC(1);
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int4 c = cand[t];
+        if (kAlone && per) per[t] = TC(1);
+        if (kPT ? (c.x == c.y || c.x == c.z || c.x == c.w) : (c.x == c.z || c.x == c.w || c.y == c.z || c.y == c.w))
+            continue;
+        const int ids[4] = {c.x, c.y, c.z, c.w};
+        double x[4][3], d[4][3];
+        gather4<TC, double>(X0, ids, x);
+        gather4<TC, double>(X1, ids, d);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) d[j][k] -= x[j][k];
+        if (!(kPT ? geo::pt_ccd_broad<double>(x, d, slack) : geo::ee_ccd_broad<double>(x, d, slack))) continue;
+        // relative to the first point: the cubic's coefficients lose nothing to large coordinates
+#pragma unroll
+        for (int j = 3; j >= 0; --j)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) x[j][k] -= x[0][k];
+        const TC tc = (TC)geo::ccd_cubic<kPT>(x, d);
+        if (tc < TC(1)) {
+            if (per && tc < per[t]) per[t] = tc;
+            if (tc < local) local = tc;
+        }
+    }
+    block_min_to(local, toi_min);
+}
+
 template <typename TC>
 __global__ void k_toi_finalize(TC* __restrict__ toi_min, TC* __restrict__ toi, double scale,
                                const OuterGate* __restrict__ gate) {
@@ -989,14 +1031,31 @@ template <typename T, typename TC>
 void launch_toi(const Dev<T, TC>& d, Pos<T, TC> X0, Pos<T, TC> X1, const SolverConsts& c, TC* per_pt,
                 TC* per_ee, cudaStream_t s) {
     constexpr bool kRel = sizeof(T) == 4 && sizeof(TC) == 8;
-    if (d.nPT > 0)
-        k_toi<T, TC, true, kRel><<<grid_cap(d.nPT, kBlock, c.cand_grid), kBlock, 0, s>>>(
-            d.nPT, d.PT, X0.x, X1.x, X0.hi, X0.lo, X1.hi, X1.lo, (TC)c.ccd_slack, (TC)c.ccd_eta, c.ccd_max_iter,
-            per_pt, d.ToiMin, d.Gate);
-    if (d.nEE > 0)
-        k_toi<T, TC, false, kRel><<<grid_cap(d.nEE, kBlock, c.cand_grid), kBlock, 0, s>>>(
-            d.nEE, d.EE, X0.x, X1.x, X0.hi, X0.lo, X1.hi, X1.lo, (TC)c.ccd_slack, (TC)c.ccd_eta, c.ccd_max_iter,
-            per_ee, d.ToiMin, d.Gate);
+    if (c.ccd_mode != 2) {  // the reference's additive CCD
+        if (d.nPT > 0)
+            k_toi<T, TC, true, kRel><<<grid_cap(d.nPT, kBlock, c.cand_grid), kBlock, 0, s>>>(
+                d.nPT, d.PT, X0.x, X1.x, X0.hi, X0.lo, X1.hi, X1.lo, (TC)c.ccd_slack, (TC)c.ccd_eta,
+                c.ccd_max_iter, per_pt, d.ToiMin, d.Gate);
+        if (d.nEE > 0)
+            k_toi<T, TC, false, kRel><<<grid_cap(d.nEE, kBlock, c.cand_grid), kBlock, 0, s>>>(
+                d.nEE, d.EE, X0.x, X1.x, X0.hi, X0.lo, X1.hi, X1.lo, (TC)c.ccd_slack, (TC)c.ccd_eta,
+                c.ccd_max_iter, per_ee, d.ToiMin, d.Gate);
+    }
+    if (c.ccd_mode == 1) {  // the FP64 cubic may lower it
+        if (d.nPT > 0)
+            k_toi_cubic<TC, true, false><<<grid_cap(d.nPT, kBlock, c.cand_grid), kBlock, 0, s>>>(
+                d.nPT, d.PT, X0.x, X1.x, c.ccd_slack, per_pt, d.ToiMin, d.Gate);
+        if (d.nEE > 0)
+            k_toi_cubic<TC, false, false><<<grid_cap(d.nEE, kBlock, c.cand_grid), kBlock, 0, s>>>(
+                d.nEE, d.EE, X0.x, X1.x, c.ccd_slack, per_ee, d.ToiMin, d.Gate);
+    } else if (c.ccd_mode == 2) {  // the FP64 cubic alone: exact first-contact times
+        if (d.nPT > 0)
+            k_toi_cubic<TC, true, true><<<grid_cap(d.nPT, kBlock, c.cand_grid), kBlock, 0, s>>>(
+                d.nPT, d.PT, X0.x, X1.x, c.ccd_slack, per_pt, d.ToiMin, d.Gate);
+        if (d.nEE > 0)
+            k_toi_cubic<TC, false, true><<<grid_cap(d.nEE, kBlock, c.cand_grid), kBlock, 0, s>>>(
+                d.nEE, d.EE, X0.x, X1.x, c.ccd_slack, per_ee, d.ToiMin, d.Gate);
+    }
 }
 template <typename T, typename TC>
 void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s) {

@@ -321,5 +321,143 @@ __device__ R ccd_ee(R (*x)[3], R (*dx)[3], R eta, int max_iter) {
     return toc;
 }
 
+// ---------------- FP64 coplanarity-cubic CCD (optional, ccd_mode 1) ----------------
+// Four points moving linearly over the step are coplanar where
+// f(t) = u1(t) . (u2(t) x u3(t)) = 0, u_k(t) = (x_k - x_0) + t (d_k - d_0): a
+// cubic in t (Provot's vertex-face / edge-edge coplanarity test).  Its roots
+// in [0, 1] are found by splitting [0, 1] at the roots of f' (monotone pieces)
+// and bisecting every piece that changes sign to full precision; at each root,
+// in increasing order, the primitives are tested for actual contact (the
+// point inside the triangle, the two edges crossing), with a relative
+// tolerance that errs toward contact.  The first root that passes is the time
+// of impact, else 1.  It can only lower the additive CCD's result, which
+// stops after a fixed number of iterations.  x: positions relative to x_0,
+// d: displacements; PT: x_0 the point, x_1..3 the triangle; EE: edges
+// (x_0, x_1) and (x_2, x_3).
+__device__ __forceinline__ double cubic_eval(const double (&c)[4], double t) {
+    return ((c[3] * t + c[2]) * t + c[1]) * t + c[0];
+}
+
+template <bool kPT>
+__device__ __forceinline__ bool touching_at(const double (*x)[3], const double (*d)[3], double t, double tol) {
+    double p[4][3];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) p[j][k] = x[j][k] + t * d[j][k];
+    if (kPT) {
+        double e1[3], e2[3], n[3];
+        sub3(p[2], p[1], e1);
+        sub3(p[3], p[1], e2);
+        cross3(e1, e2, n);
+        const double nn = dot3(n, n);
+        if (!(nn > 0.0)) return false;
+        double a[3], b[3], c[3], q[3];
+        sub3(p[1], p[0], a);
+        sub3(p[2], p[0], b);
+        sub3(p[3], p[0], c);
+        cross3(b, c, q);
+        const double wa = dot3(q, n) / nn;
+        cross3(c, a, q);
+        const double wb = dot3(q, n) / nn;
+        cross3(a, b, q);
+        const double wc = dot3(q, n) / nn;
+        return wa >= -tol && wb >= -tol && wc >= -tol;
+    } else {
+        double ea[3], eb[3], w[3];
+        sub3(p[1], p[0], ea);
+        sub3(p[3], p[2], eb);
+        sub3(p[0], p[2], w);
+        const double aa = dot3(ea, ea), bb = dot3(eb, eb), ab = dot3(ea, eb);
+        const double den = aa * bb - ab * ab;
+        if (!(den > 1e-24 * aa * bb)) return false;  // parallel edges: left to the additive CCD
+        const double wa = dot3(w, ea), wb = dot3(w, eb);
+        const double s = (ab * wb - bb * wa) / den, u = (aa * wb - ab * wa) / den;
+        return s >= -tol && s <= 1.0 + tol && u >= -tol && u <= 1.0 + tol;
+    }
+}
+
+template <bool kPT>
+__device__ double ccd_cubic(const double (*x)[3], const double (*d)[3]) {
+    double u0[3][3], u1[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            u0[k][a] = x[k + 1][a] - x[0][a];
+            u1[k][a] = d[k + 1][a] - d[0][a];
+        }
+    double c[4];
+    {
+        double bc[3], t1[3], t2[3], t3[3];
+        cross3(u0[1], u0[2], bc);
+        c[0] = dot3(u0[0], bc);
+        cross3(u1[1], u0[2], t1);
+        cross3(u0[1], u1[2], t2);
+        c[1] = dot3(u1[0], bc) + dot3(u0[0], t1) + dot3(u0[0], t2);
+        cross3(u1[1], u1[2], t3);
+        c[2] = dot3(u1[0], t1) + dot3(u1[0], t2) + dot3(u0[0], t3);
+        c[3] = dot3(u1[0], t3);
+    }
+    double scale = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        scale = fmax(scale, fmax(sqrt(dot3(u0[k], u0[k])), sqrt(dot3(u1[k], u1[k]))));
+    const double s3 = scale * scale * scale;
+    if (!(s3 > 0.0) || !(fabs(c[0]) + fabs(c[1]) + fabs(c[2]) + fabs(c[3]) > 1e-14 * s3))
+        return 1.0;  // no motion, or coplanar throughout: left to the additive CCD
+    // split points: 0, the roots of f' = 3 c3 t^2 + 2 c2 t + c1 inside (0, 1), 1
+    double br[4] = {0.0, 1.0, 1.0, 1.0};
+    int nb = 1;
+    {
+        const double A = 3.0 * c[3], B = 2.0 * c[2], C = c[1];
+        double r0 = 2.0, r1 = 2.0;
+        if (fabs(A) > 1e-300) {
+            const double disc = B * B - 4.0 * A * C;
+            if (disc >= 0.0) {
+                const double q = -0.5 * (B + copysign(sqrt(disc), B));
+                r0 = q / A;
+                r1 = q != 0.0 ? C / q : r0;
+            }
+        } else if (fabs(B) > 1e-300) {
+            r0 = -C / B;
+        }
+        if (r0 > r1) {
+            const double tt = r0;
+            r0 = r1;
+            r1 = tt;
+        }
+        if (r0 > 0.0 && r0 < 1.0) br[nb++] = r0;
+        if (r1 > 0.0 && r1 < 1.0 && r1 != r0) br[nb++] = r1;
+        br[nb] = 1.0;
+    }
+    const double tol = 1e-6;
+    for (int s = 0; s < nb; ++s) {
+        double lo = br[s], hi = br[s + 1];
+        double flo = cubic_eval(c, lo), fhi = cubic_eval(c, hi);
+        double root;
+        if (flo == 0.0) {
+            root = lo;
+        } else if ((flo < 0.0) != (fhi < 0.0) || fhi == 0.0) {
+            for (int it = 0; it < 64 && hi - lo > 0.0; ++it) {  // to the last bit of [lo, hi]
+                const double mid = 0.5 * (lo + hi);
+                if (mid <= lo || mid >= hi) break;
+                const double fm = cubic_eval(c, mid);
+                if ((fm < 0.0) == (flo < 0.0) && fm != 0.0) {
+                    lo = mid;
+                    flo = fm;
+                } else {
+                    hi = mid;
+                }
+            }
+            root = lo;  // the side before the crossing
+        } else {
+            continue;
+        }
+        if (touching_at<kPT>(x, d, root, tol) || touching_at<kPT>(x, d, hi, tol)) return root;
+    }
+    return 1.0;
+}
+
 }  // namespace geo
 }  // namespace pdipc

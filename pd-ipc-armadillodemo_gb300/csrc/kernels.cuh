@@ -147,6 +147,8 @@ struct SolverConsts {
     int cand_grid = 152 * 16;
     int trav_block = 128;
     int expand_block = 256;
+    // 1: after the additive CCD, the FP64 coplanarity-cubic pass (pdipc_params.ccd_mode)
+    int ccd_mode = 0;
 };
 
 // ---------------- PD kernels (pd_kernels.cu) ----------------

@@ -103,6 +103,11 @@ public:
             err = "wait_limit_us must not be negative";
             return PDIPC_ERR_ARG;
         }
+        if (p.ccd_mode < 0 || p.ccd_mode > 2) {
+            err = "ccd_mode must be 0 (additive CCD), 1 (plus the FP64 coplanarity cubic) or 2 (the cubic alone)";
+            return PDIPC_ERR_ARG;
+        }
+        c_.ccd_mode = p.ccd_mode;
         {
             int khz = 0;
             PD_CK(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, p.device));

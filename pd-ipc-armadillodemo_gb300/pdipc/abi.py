@@ -53,7 +53,8 @@ class Params(C.Structure):
         ("persistent", C.c_int),
         ("wait_limit_us", C.c_int),
         ("autotune", C.c_int),
-        ("reserved", C.c_int * 4),
+        ("ccd_mode", C.c_int),
+        ("reserved", C.c_int * 3),
     ]
 
 
