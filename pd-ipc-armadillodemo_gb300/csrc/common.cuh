@@ -153,6 +153,7 @@ enum ErrFlag : unsigned int {
     kErrPairOverflow = 4u,
     kErrCandidateOverflow = 8u,
     kErrBarrier = 16u,  // a grid barrier of the persistent solve timed out
+    kErrSort = 32u,     // a look-back wait of the radix sort timed out
 };
 
 // Stopping test of the outer loop, made on the device.  k_outer_gate writes it

@@ -285,7 +285,8 @@ void scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, int64_t* tot
 void scan_exclusive_i32(const int* in, int* out, int n, int* total, void* tmp, cudaStream_t s);
 // Stable LSD radix sort of 64-bit keys with int values (keys use the low 63 bits).
 size_t sort_tmp_bytes(int n);
-void radix_sort_u64(unsigned long long* keys, int* vals, int n, void* tmp, cudaStream_t s);
+// stable onesweep sort by key; a timed-out look-back wait sets kErrSort in *err
+void radix_sort_u64(unsigned long long* keys, int* vals, int n, void* tmp, unsigned* err, cudaStream_t s);
 void launch_reduce_sum_f64(const double* part, int n, double* out, cudaStream_t s);
 
 }  // namespace pdipc

@@ -100,52 +100,146 @@ void scan_rec(const I* in, I* out, int64_t n, I* total, I* tmp, cudaStream_t s) 
     k_scan_add<I><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n, sums);
 }
 
-// ---------------- radix sort ----------------
-constexpr int kSortTile = 4096;
-constexpr int kSortThreads = 256;
+// ---------------- onesweep radix sort (64-bit keys, 8 digits of 8 bits) ----------------
+// One read of the keys builds all eight digit histograms; then each digit
+// pass is one kernel.  A CTA takes the next partition of 2048 keys by an
+// atomic ticket (so partitions start in order), ranks its keys stably (rounds
+// in index order, warps by __match_any_sync), publishes its per-digit counts,
+// and looks back through the earlier partitions' published values for its
+// exclusive prefix (decoupled look-back: an earlier partition publishes its
+// aggregate before it looks back itself, so the chain always advances), then
+// scatters.  Waits are bounded: past the limit the pass records kErrSort.
+constexpr int kOsThreads = 256;
+constexpr int kOsRounds = 8;
+constexpr int kOsTile = kOsThreads * kOsRounds;
+constexpr unsigned kOsAggregate = 1u << 30, kOsPrefix = 2u << 30, kOsValue = (1u << 30) - 1u;
+constexpr long long kOsMaxSpins = 1ll << 22;
 
-__global__ void k_hist(const unsigned long long* __restrict__ keys, int n, int shift, int nblk,
-                       int* __restrict__ hist) {
-    __shared__ int h[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
-    __syncthreads();
-    const int base = blockIdx.x * kSortTile;
-    for (int i = threadIdx.x; i < kSortTile; i += blockDim.x) {
-        const int g = base + i;
-        if (g < n) atomicAdd(&h[(keys[g] >> shift) & 0xff], 1);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i * nblk + blockIdx.x] = h[i];
+__device__ __forceinline__ unsigned os_ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void os_st_release(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// One warp per tile, in order, so equal digits keep their input order.
-__global__ void k_scatter(const unsigned long long* __restrict__ kin, const int* __restrict__ vin,
-                          unsigned long long* __restrict__ kout, int* __restrict__ vout, int n, int shift, int nblk,
-                          const int* __restrict__ off) {
-    __shared__ int cnt[256];
-    const int lane = threadIdx.x;
-    for (int i = lane; i < 256; i += 32) cnt[i] = off[i * nblk + blockIdx.x];
-    __syncwarp();
-    const int base = blockIdx.x * kSortTile;
+__global__ void __launch_bounds__(kOsThreads) k_os_hist(const unsigned long long* __restrict__ keys, int n,
+                                                        unsigned* __restrict__ hist) {
+    __shared__ unsigned h[8][256];
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&h[0][0])[i] = 0u;
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned long long k = keys[i];
+#pragma unroll
+        for (int p = 0; p < 8; ++p) atomicAdd(&h[p][(k >> (8 * p)) & 0xffull], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) {
+        const unsigned c = (&h[0][0])[i];
+        if (c) atomicAdd(hist + i, c);
+    }
+}
+
+// exclusive scan of each pass's 256 digit counts: block p, thread d
+__global__ void __launch_bounds__(256) k_os_offsets(const unsigned* __restrict__ hist, unsigned* __restrict__ off) {
+    __shared__ unsigned s[256];
+    const int p = blockIdx.x, d = threadIdx.x;
+    const unsigned own = hist[p * 256 + d];
+    s[d] = own;
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1) {  // inclusive Hillis-Steele scan
+        const unsigned v = d >= o ? s[d - o] : 0u;
+        __syncthreads();
+        s[d] += v;
+        __syncthreads();
+    }
+    off[p * 256 + d] = s[d] - own;
+}
+
+__global__ void __launch_bounds__(kOsThreads) k_onesweep(const unsigned long long* __restrict__ kin,
+                                                         const int* __restrict__ vin,
+                                                         unsigned long long* __restrict__ kout,
+                                                         int* __restrict__ vout, int n, int shift,
+                                                         const unsigned* __restrict__ digitOff,
+                                                         unsigned* __restrict__ status, unsigned* __restrict__ ticket,
+                                                         unsigned* __restrict__ err) {
+    __shared__ int part_s;
+    __shared__ unsigned cnt[256];
+    __shared__ unsigned wcnt[kOsThreads / 32][256];
+    __shared__ unsigned base_s[256];
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    if (tid == 0) part_s = (int)atomicAdd(ticket, 1u);
+    cnt[tid] = 0u;
+    __syncthreads();
+    const int part = part_s;
+    const int tile = part * kOsTile;
     const unsigned lt = (1u << lane) - 1u;
-    for (int c = 0; c < kSortTile; c += 32) {
-        const int g = base + c + lane;
-        const bool ok = g < n;
-        unsigned long long k = ok ? kin[g] : 0ull;
-        const int v = ok ? vin[g] : 0;
-        const int d = ok ? (int)((k >> shift) & 0xff) : 256 + lane;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        const int rank = __popc(peers & lt);
-        int pos = 0;
-        if (ok) pos = cnt[d] + rank;
+    unsigned long long key[kOsRounds];
+    int val[kOsRounds], dig[kOsRounds];
+    unsigned rank[kOsRounds];
+#pragma unroll
+    for (int r = 0; r < kOsRounds; ++r) {
+        const int i = tile + r * kOsThreads + tid;
+        const bool ok = i < n;
+        key[r] = ok ? kin[i] : 0ull;
+        val[r] = ok ? vin[i] : 0;
+        dig[r] = ok ? (int)((key[r] >> shift) & 0xffull) : 256 + lane;  // past the end: no peers
+        const unsigned peers = __match_any_sync(0xffffffffu, dig[r]);
+        for (int j = lane; j < 256; j += 32) wcnt[w][j] = 0u;
         __syncwarp();
-        if (ok) {
-            kout[pos] = k;
-            vout[pos] = v;
-            if (rank == 0) cnt[d] += __popc(peers);
+        if (ok && __popc(peers & lt) == 0) wcnt[w][dig[r]] = (unsigned)__popc(peers);
+        __syncthreads();
+        // thread tid owns digit tid: exclusive prefix over the warps of this round,
+        // on top of the tile's count so far
+        unsigned run = cnt[tid];
+#pragma unroll
+        for (int ww = 0; ww < kOsThreads / 32; ++ww) {
+            const unsigned c = wcnt[ww][tid];
+            wcnt[ww][tid] = run;
+            run += c;
         }
-        __syncwarp();
-        if (base + c + 32 >= n) break;
+        __syncthreads();
+        rank[r] = ok ? wcnt[w][dig[r]] + (unsigned)__popc(peers & lt) : 0u;
+        __syncthreads();
+        cnt[tid] = run;
+        __syncthreads();
+    }
+    // publish this partition's count of digit tid, look back for the prefix
+    const unsigned local = cnt[tid];
+    unsigned* st = status + (size_t)part * 256 + tid;
+    unsigned before = 0u;
+    if (part == 0) {
+        os_st_release(st, kOsPrefix | local);
+    } else {
+        os_st_release(st, kOsAggregate | local);
+        long long spins = 0;
+        for (int j = part - 1; j >= 0;) {
+            const unsigned s = os_ld_acquire(status + (size_t)j * 256 + tid);
+            const unsigned f = s & ~kOsValue;
+            if (f == 0u) {
+                if (++spins > kOsMaxSpins) {
+                    atomicOr(err, (unsigned)kErrSort);
+                    break;
+                }
+                __nanosleep(32);
+                continue;
+            }
+            before += s & kOsValue;
+            if (f == kOsPrefix) break;
+            --j;
+        }
+        os_st_release(st, kOsPrefix | (before + local));
+    }
+    base_s[tid] = digitOff[tid] + before;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kOsRounds; ++r) {
+        if (tile + r * kOsThreads + tid < n) {
+            const unsigned pos = base_s[dig[r]] + rank[r];
+            kout[pos] = key[r];
+            vout[pos] = val[r];
+        }
     }
 }
 
@@ -174,38 +268,37 @@ void scan_exclusive_i32(const int* in, int* out, int n, int* total, void* tmp, c
     scan_rec<int>(in, out, n, total, static_cast<int*>(tmp), s);
 }
 
+// scratch: alternate keys and values, then (256-aligned) the histograms and
+// offsets of the 8 passes, the 8 passes' look-back status words and tickets
 size_t sort_tmp_bytes(int n) {
-    const int nblk = std::max(1, (n + kSortTile - 1) / kSortTile);
-    size_t b = 0;
-    b += (size_t)n * sizeof(unsigned long long);        // alternate keys
-    b += (size_t)n * sizeof(int);                       // alternate values
+    const size_t parts = (size_t)std::max(1, (n + kOsTile - 1) / kOsTile);
+    size_t b = (size_t)n * (sizeof(unsigned long long) + sizeof(int));
     b = (b + 255) & ~(size_t)255;
-    b += (size_t)256 * nblk * sizeof(int);              // histograms / offsets
-    b = (b + 255) & ~(size_t)255;
-    b += scan_tmp_bytes((int64_t)256 * nblk);
+    b += (2 * 8 * 256 + 8 * parts * 256 + 8) * sizeof(unsigned);
     return b + 256;
 }
 
-void radix_sort_u64(unsigned long long* keys, int* vals, int n, void* tmp, cudaStream_t s) {
+void radix_sort_u64(unsigned long long* keys, int* vals, int n, void* tmp, unsigned* err, cudaStream_t s) {
     if (n <= 1) return;
-    const int nblk = (n + kSortTile - 1) / kSortTile;
+    const int parts = (n + kOsTile - 1) / kOsTile;
     char* t = static_cast<char*>(tmp);
     auto* k2 = reinterpret_cast<unsigned long long*>(t);
     t += (size_t)n * sizeof(unsigned long long);
     auto* v2 = reinterpret_cast<int*>(t);
     t += (size_t)n * sizeof(int);
     t = reinterpret_cast<char*>(((uintptr_t)t + 255) & ~(uintptr_t)255);
-    int* hist = reinterpret_cast<int*>(t);
-    t += (size_t)256 * nblk * sizeof(int);
-    t = reinterpret_cast<char*>(((uintptr_t)t + 255) & ~(uintptr_t)255);
-    void* stmp = t;
+    unsigned* hist = reinterpret_cast<unsigned*>(t);
+    unsigned* off = hist + 8 * 256;
+    unsigned* status = off + 8 * 256;
+    unsigned* tickets = status + (size_t)8 * parts * 256;
+    cudaMemsetAsync(hist, 0, (2 * 8 * 256 + (size_t)8 * parts * 256 + 8) * sizeof(unsigned), s);
+    k_os_hist<<<std::min(parts, 152 * 4), kOsThreads, 0, s>>>(keys, n, hist);
+    k_os_offsets<<<8, 256, 0, s>>>(hist, off);
     unsigned long long *ka = keys, *kb = k2;
     int *va = vals, *vb = v2;
     for (int pass = 0; pass < 8; ++pass) {
-        const int shift = 8 * pass;
-        k_hist<<<nblk, kSortThreads, 0, s>>>(ka, n, shift, nblk, hist);
-        scan_exclusive_i32(hist, hist, 256 * nblk, nullptr, stmp, s);
-        k_scatter<<<nblk, 32, 0, s>>>(ka, va, kb, vb, n, shift, nblk, hist);
+        k_onesweep<<<parts, kOsThreads, 0, s>>>(ka, va, kb, vb, n, 8 * pass, off + 256 * pass,
+                                               status + (size_t)pass * parts * 256, tickets + pass, err);
         std::swap(ka, kb);
         std::swap(va, vb);
     }

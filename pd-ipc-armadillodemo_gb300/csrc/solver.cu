@@ -1647,16 +1647,23 @@ private:
         PD_CK(cudaMalloc(&vals, sizeof(int) * d.npatch));
         PD_CK(cudaMalloc(&tmp, sort_tmp_bytes(d.npatch)));
         launch_morton(d, cs, keys, vals, s_);
-        radix_sort_u64(keys, vals, d.npatch, tmp, s_);
+        radix_sort_u64(keys, vals, d.npatch, tmp, d.ErrFlags, s_);
         PD_CK(cudaMemcpyAsync(d.LeafPatch, vals, sizeof(int) * d.npatch, cudaMemcpyDeviceToDevice, s_));
         launch_karras(d, keys, s_);
-        launches_ += 3 + 8 * 3;
+        launches_ += 3 + 2 + 8 + 1;
+        pin_->err = 0;
+        PD_CK(cudaMemcpyAsync(&pin_->err, d.ErrFlags, sizeof(unsigned int), cudaMemcpyDeviceToHost, s_));
         PD_CK(cudaStreamSynchronize(s_));
         cudaFree(cs);
         cudaFree(keys);
         cudaFree(vals);
         cudaFree(tmp);
         PD_CK(cudaGetLastError());
+        if (pin_->err & kErrSort) {
+            PD_CK(cudaMemsetAsync(d.ErrFlags, 0, sizeof(unsigned int), s_));
+            err = "patch tree: a look-back wait of the radix sort timed out";
+            return PDIPC_ERR_CUDA;
+        }
         return PDIPC_OK;
     }
 

@@ -44,6 +44,19 @@ def sort_rows(a):
     return a[np.lexsort(a.T[::-1])] if a.size else a
 
 
+@pytest.mark.parametrize("config", ["c1", "c2"])
+def test_patch_order_is_a_stable_sort_at_full_size(config, built_lib):
+    """The onesweep radix sort over many partitions (c1: about 303 k patches, c2:
+    several hundred thousand over 512 meshes): the patch order equals a stable
+    sort of the Morton codes, ties in patch order."""
+    sc = scenes.config1() if config == "c1" else scenes.config2()
+    sim = pdipc.Simulator(sc, "mixed")
+    npatch = sim.stats()["n_patches"]
+    assert npatch > 100000
+    codes, order = sim.stage_morton(npatch)
+    assert np.array_equal(order, np.argsort(codes, kind="stable"))
+
+
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
 def test_morton_codes_and_order_bitexact(prec, built_lib):
     sc = small_scene()
