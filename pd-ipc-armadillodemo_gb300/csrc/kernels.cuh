@@ -64,6 +64,17 @@ struct Dev {
     T* lBendT = nullptr;
     T* Strain = nullptr;     // per vertex
     T* CurvNorm = nullptr;   // per vertex
+    // the same stencils in SELL-32 order for the per-vertex kernels: neighbour
+    // k of row i (self excluded, k < lPtr[i+1] - lPtr[i] - 1, ascending as in
+    // the CSR) at tOff[i >> 5] + 32 k + (i & 31), so that a warp's k-th loads
+    // are one 128-byte line; tBend0 / tLbo0 the self weights per row
+    int* tOff = nullptr;
+    int* tNbr = nullptr;
+    T* tRest = nullptr;
+    T* tLbo = nullptr;
+    T* tBendT = nullptr;
+    T* tBend0 = nullptr;
+    T* tLbo0 = nullptr;
 
     // tetrahedral strain constraints: vertices, row-major Dm^-1 (9 per tet),
     // weights; per-tet projections w R G (4 per tet, vertex-major), gathered
@@ -129,6 +140,12 @@ struct Dev {
     // once Gate->stop is set; null everywhere else (stage entry points)
     OuterGate* Gate = nullptr;
 };
+
+// Row i's stencil in the SELL-32 copy: (slot of neighbour 0, neighbour count);
+// neighbour k sits at .x + 32 k.
+__device__ __forceinline__ int2 stencil_of(int i, const int* __restrict__ lPtr, const int* __restrict__ tOff) {
+    return make_int2(__ldg(tOff + (i >> 5)) + (i & 31), __ldg(lPtr + i + 1) - __ldg(lPtr + i) - 1);
+}
 
 // A position array and its float-float mirror (null outside the correction form).
 template <typename T, typename TC>

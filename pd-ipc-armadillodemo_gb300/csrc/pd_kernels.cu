@@ -151,17 +151,19 @@ __global__ void k_tet_project(int ntet, const int4* __restrict__ Tets, const T* 
 // (PdIpcGpuFunc.cu:664-699).
 template <typename T>
 __global__ void k_local_aq(int nsim, const V4<T>* __restrict__ P, const int* __restrict__ lPtr,
-                           const int* __restrict__ lNbr, const T* __restrict__ lLbo, const T* __restrict__ CurvNorm,
+                           const int* __restrict__ tOff, const int* __restrict__ tNbr, const T* __restrict__ tLbo,
+                           const T* __restrict__ tLbo0, const T* __restrict__ CurvNorm,
                            V4<T>* __restrict__ Aq) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
-    const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
+    const int2 st = stencil_of(i, lPtr, tOff);
     const V4<T> x = ld4(P, i);
-    const T l0 = __ldg(lLbo + b);
+    const T l0 = __ldg(tLbo0 + i);
     T a0 = x.x * l0, a1 = x.y * l0, a2 = x.z * l0;
-    for (int s = b + 1; s < e; ++s) {
-        const V4<T> xj = ld4(P, __ldg(lNbr + s));
-        const T l = __ldg(lLbo + s);
+    for (int k = 0; k < st.y; ++k) {
+        const int s = st.x + kSlice * k;
+        const V4<T> xj = ld4(P, __ldg(tNbr + s));
+        const T l = __ldg(tLbo + s);
         a0 += xj.x * l;
         a1 += xj.y * l;
         a2 += xj.z * l;
@@ -201,8 +203,9 @@ __device__ __forceinline__ void sell_row(int i, const int* __restrict__ sOff, co
 // then the first weighted-Jacobi sweep Y = (1-w) x + w D^-1 (N x + rhs).
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_local_rhs_sweep(
-    int nsim, T relax, const V4<T>* __restrict__ P, const int* __restrict__ lPtr, const int* __restrict__ lNbr,
-    const T* __restrict__ lRest, const T* __restrict__ lBend, const T* __restrict__ lBendT,
+    int nsim, T relax, const V4<T>* __restrict__ P, const int* __restrict__ lPtr, const int* __restrict__ tOff,
+    const int* __restrict__ tNbr, const T* __restrict__ tRest, const T* __restrict__ tBend0,
+    const T* __restrict__ tBendT,
     const T* __restrict__ Strain, const V4<T>* __restrict__ Aq, const V4<T>* __restrict__ Rhs0,
     const V4<T>* __restrict__ CollRhs, const V4<T>* __restrict__ PinRhs, const T* __restrict__ InvD,
     const int* __restrict__ sOff, const int* __restrict__ sLen, const int* __restrict__ sCol,
@@ -210,29 +213,31 @@ __global__ void __launch_bounds__(kBlock) k_local_rhs_sweep(
     const V4<T>* __restrict__ TetOut, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
-    const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
+    const int2 st = stencil_of(i, lPtr, tOff);
     const V4<T> x = ld4(P, i);
     const T strain = __ldg(Strain + i);
     T t0 = T(0), t1 = T(0), t2 = T(0);
-    for (int s = b + 1; s < e; ++s) {  // mass-spring projections (cu:670-690)
-        const V4<T> xj = ld4(P, __ldg(lNbr + s));
+    for (int k = 0; k < st.y; ++k) {  // mass-spring projections (cu:670-690)
+        const int s = st.x + kSlice * k;
+        const V4<T> xj = ld4(P, __ldg(tNbr + s));
         const T d0 = x.x - xj.x, d1 = x.y - xj.y, d2 = x.z - xj.z;
         const T cl = dsqrt(d0 * d0 + d1 * d1 + d2 * d2);
-        const T rc = strain * (__ldg(lRest + s) / cl);
+        const T rc = strain * (__ldg(tRest + s) / cl);
         t0 += rc * d0;
         t1 += rc * d1;
         t2 += rc * d2;
     }
     const V4<T> ai = ld4(Aq, i);
-    const T b0 = __ldg(lBend + b);
+    const T b0 = __ldg(tBend0 + i);
     t0 += b0 * ai.x;
     t1 += b0 * ai.y;
     t2 += b0 * ai.z;
     const V4<T> r0 = ld4(Rhs0, i);
     T r_0 = r0.x + t0, r_1 = r0.y + t1, r_2 = r0.z + t2;
-    for (int s = b + 1; s < e; ++s) {  // bending terms the neighbours' stencils put on i
-        const V4<T> ak = ld4(Aq, __ldg(lNbr + s));
-        const T bt = __ldg(lBendT + s);
+    for (int k = 0; k < st.y; ++k) {  // bending terms the neighbours' stencils put on i
+        const int s = st.x + kSlice * k;
+        const V4<T> ak = ld4(Aq, __ldg(tNbr + s));
+        const T bt = __ldg(tBendT + s);
         r_0 += bt * ak.x;
         r_1 += bt * ak.y;
         r_2 += bt * ak.z;
@@ -308,8 +313,9 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
     const V4<S>* __restrict__ Pold, const V4<S>* __restrict__ Xrest,
     const V4<S>* __restrict__ Ypred, const T* __restrict__ Dinert, const T* __restrict__ CollDiag,
     const V4<T>* __restrict__ CollRes, const int* __restrict__ PinFlag, const T* __restrict__ PinK,
-    const int* __restrict__ lPtr, const int* __restrict__ lNbr, const T* __restrict__ lRest,
-    const T* __restrict__ lBend, const T* __restrict__ lBendT, const T* __restrict__ Strain,
+    const int* __restrict__ lPtr, const int* __restrict__ tOff, const int* __restrict__ tNbr,
+    const T* __restrict__ tRest, const T* __restrict__ tBend0, const T* __restrict__ tBendT,
+    const T* __restrict__ Strain,
     const V4<T>* __restrict__ Aq, const T* __restrict__ InvD,
     const int* __restrict__ sOff, const int* __restrict__ sLen, const int* __restrict__ sCol,
     const T* __restrict__ sVal, const int* __restrict__ vtPtr, const int* __restrict__ vtIdx,
@@ -344,29 +350,31 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
         r2.add(c.z);
         r2.add(dc * (T)(xo.z - x.z));
     }
-    const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
+    const int2 st = stencil_of(i, lPtr, tOff);
     const T strain = __ldg(Strain + i);
     const V4<T> h = ld4(Ph, i), l = ld4(Pl, i);
-    for (int s = b + 1; s < e; ++s) {  // mass-spring projections
-        const int j = __ldg(lNbr + s);
+    for (int k = 0; k < st.y; ++k) {  // mass-spring projections
+        const int s = st.x + kSlice * k;
+        const int j = __ldg(tNbr + s);
         const V4<T> hj = ld4(Ph, j), lj = ld4(Pl, j);
         const T d0 = diff_ff(h.x, l.x, hj.x, lj.x), d1 = diff_ff(h.y, l.y, hj.y, lj.y),
                 d2 = diff_ff(h.z, l.z, hj.z, lj.z);
         const T cl = dsqrt(d0 * d0 + d1 * d1 + d2 * d2);
-        const T rc = strain * (__ldg(lRest + s) / cl);
+        const T rc = strain * (__ldg(tRest + s) / cl);
         r0.add(rc * d0);
         r1.add(rc * d1);
         r2.add(rc * d2);
     }
     {   // bending: own stencil and the neighbours' stencils
         const V4<T> ai = ld4(Aq, i);
-        const T b0 = __ldg(lBend + b);
+        const T b0 = __ldg(tBend0 + i);
         r0.add(b0 * ai.x);
         r1.add(b0 * ai.y);
         r2.add(b0 * ai.z);
-        for (int s = b + 1; s < e; ++s) {
-            const V4<T> ak = ld4(Aq, __ldg(lNbr + s));
-            const T bt = __ldg(lBendT + s);
+        for (int k = 0; k < st.y; ++k) {
+            const int s = st.x + kSlice * k;
+            const V4<T> ak = ld4(Aq, __ldg(tNbr + s));
+            const T bt = __ldg(tBendT + s);
             r0.add(bt * ak.x);
             r1.add(bt * ak.y);
             r2.add(bt * ak.z);
@@ -448,19 +456,21 @@ __global__ void __launch_bounds__(kBlock) k_sweep_delta(int nsim, T relax, T ome
 // aq = sum_{k>0} lbo_k (x_k - x_i), using that the LBO weights of a stencil sum
 // to zero.
 __global__ void k_local_aq_rel(int nsim, const V4<float>* __restrict__ Ph, const V4<float>* __restrict__ Pl,
-                               const int* __restrict__ lPtr, const int* __restrict__ lNbr,
-                               const float* __restrict__ lLbo, const float* __restrict__ CurvNorm,
+                               const int* __restrict__ lPtr, const int* __restrict__ tOff,
+                               const int* __restrict__ tNbr, const float* __restrict__ tLbo,
+                               const float* __restrict__ CurvNorm,
                                V4<float>* __restrict__ Aq) {
     using T = float;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
-    const int b = __ldg(lPtr + i), e = __ldg(lPtr + i + 1);
+    const int2 st = stencil_of(i, lPtr, tOff);
     const V4<T> h = ld4(Ph, i), l = ld4(Pl, i);
     T a0 = T(0), a1 = T(0), a2 = T(0);
-    for (int s = b + 1; s < e; ++s) {
-        const int j = __ldg(lNbr + s);
+    for (int k = 0; k < st.y; ++k) {
+        const int s = st.x + kSlice * k;
+        const int j = __ldg(tNbr + s);
         const V4<T> hj = ld4(Ph, j), lj = ld4(Pl, j);
-        const T w = __ldg(lLbo + s);
+        const T w = __ldg(tLbo + s);
         a0 += w * diff_ff(hj.x, lj.x, h.x, l.x);
         a1 += w * diff_ff(hj.y, lj.y, h.y, l.y);
         a2 += w * diff_ff(hj.z, lj.z, h.z, l.z);
@@ -590,17 +600,18 @@ void launch_tet_project(const Dev<T, TC>& d, cudaStream_t s) {
 template <typename T, typename TC>
 void launch_local_aq(const Dev<T, TC>& d, cudaStream_t s) {
     if constexpr (correction_form<T, TC>())
-        k_local_aq_rel<<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Ph, d.Pl, d.lPtr, d.lNbr, d.lLbo,
+        k_local_aq_rel<<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Ph, d.Pl, d.lPtr, d.tOff, d.tNbr, d.tLbo,
                                                               d.CurvNorm, d.Aq);
     else
-        k_local_aq<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.lNbr, d.lLbo, d.CurvNorm, d.Aq);
+        k_local_aq<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.tOff, d.tNbr, d.tLbo, d.tLbo0,
+                                                            d.CurvNorm, d.Aq);
 }
 template <typename T, typename TC>
 void launch_local_residual(const Dev<T, TC>& d, T relax, cudaStream_t s) {
     if constexpr (kMirror<T, TC>) {
         k_local_residual<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(
             d.nsim, relax, d.P, d.Ph, d.Pl, d.Pold, d.Xrest, d.Rhs0, d.Dinert, d.CollDiag, d.CollRhs, d.PinFlag,
-            d.PinK, d.lPtr, d.lNbr, d.lRest, d.lBend, d.lBendT, d.Strain, d.Aq, d.InvD, d.sOff, d.sLen, d.sCol,
+            d.PinK, d.lPtr, d.tOff, d.tNbr, d.tRest, d.tBend0, d.tBendT, d.Strain, d.Aq, d.InvD, d.sOff, d.sLen, d.sCol,
             d.sVal, d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs, d.Y);
     }
 }
@@ -629,7 +640,7 @@ template <typename T, typename TC>
 void launch_local_rhs_sweep(const Dev<T, TC>& d, T relax, cudaStream_t s) {
     if constexpr (std::is_same<T, TC>::value)
         k_local_rhs_sweep<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(
-            d.nsim, relax, d.P, d.lPtr, d.lNbr, d.lRest, d.lBend, d.lBendT, d.Strain, d.Aq, d.Rhs0, d.CollRhs,
+            d.nsim, relax, d.P, d.lPtr, d.tOff, d.tNbr, d.tRest, d.tBend0, d.tBendT, d.Strain, d.Aq, d.Rhs0, d.CollRhs,
             d.PinRhs, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal, d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs,
             d.Y);
 }

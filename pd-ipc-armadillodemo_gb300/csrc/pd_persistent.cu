@@ -305,10 +305,12 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     // ---- rows owned by this thread: one per slice, the warp's R slices
     // consecutive; the band path's last warp has no rows ----
     // pk[r] packs the row's entry count (bits 0-9) and, on the band path, the
-    // bounds of its entries on own rows (bits 10-19, 20-29)
+    // bounds of its entries on own rows (bits 10-19, 20-29).  slotof(r) is the
+    // row's slot (iterates, band), rowof(r) the row itself (state arrays).
     const int nrw = (int)(blockDim.x >> 5) - (band ? 1 : 0);
-    const int row0 = (a.ctaSlice[cta] + warp * R) * 32 + lane;
-    auto rowof = [&](int r) { return row0 + 32 * r; };
+    const int slot0 = (a.ctaSlice[cta] + warp * R) * 32 + lane;
+    auto slotof = [&](int r) { return slot0 + 32 * r; };
+    auto rowof = [&](int r) { return row_of(slot0 + 32 * r); };
     int gb[R], pk[R], pid[R];
     bool val[R];
 #pragma unroll
@@ -321,7 +323,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
         pid[r] = (kSmem && val[r]) ? a.rowPattern[rowof(r)] * a.patW : 0;
     }
     auto slen = [&](int r) { return pk[r] & 1023; };
-    // entry k of owned row r: value and gathered row
+    // entry k of owned row r: value and gathered row (a row, not a slot)
     auto entry = [&](int r, int k, T& v, int& j) {
         if (kSmem) {
             v = sval[gb[r] - eb + 32 * k];
@@ -348,11 +350,12 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
         id[r] = val[r] ? T(1) / ((a.Delastic[rowof(r)] + a.Dinert[rowof(r)]) + a.CollDiag[rowof(r)]) : T(0);
 
     // ---- the band: this CTA's own rows and the halo its matrix rows reach ----
-    // Own rows [own0, own1) live in the planar arrays; between sweeps each
-    // thread writes its rows' new values there.  The halo, columns
+    // Own slots [own0, own1) live in the planar arrays; between sweeps each
+    // thread writes its rows' new values there.  The halo, slots
     // [brange.x, own0) and [own1, brange.y), is copied from global memory in
-    // two bulk copies once the neighbours have published it.
-    const int own0 = a.ctaSlice[cta] * 32, own1 = min(a.ctaSlice[cta + 1] * 32, a.nsim);
+    // two bulk copies once the neighbours have published it.  A CTA owns whole
+    // 64-row windows, so a row j is one of its own exactly when slot_of(j) is.
+    const int own0 = a.ctaSlice[cta] * 32, own1 = min(a.ctaSlice[cta + 1] * 32, a.nslot);
     const int nlo = band ? own0 - brange.x : 0, nhi = band ? brange.y - own1 : 0;
     const int hiBase = own1 - nlo;  // halo slot of column j >= own1: j - hiBase
     // The band path runs one extra warp, the last, with no rows: it publishes
@@ -460,7 +463,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
             T v;
             int j;
             entry(r, k, v, j);
-            const int q = j - own0;
+            const int q = slot_of(j) - own0;
             s0 += v * ox[q];
             s1 += v * oy[q];
             s2 += v * oz[q];
@@ -472,7 +475,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
             T v;
             int j;
             entry(r, k, v, j);
-            const V4<T> h = hv[j - base];
+            const V4<T> h = hv[slot_of(j) - base];
             s0 += v * h.x;
             s1 += v * h.y;
             s2 += v * h.z;
@@ -483,8 +486,9 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
         halo_range(r, pk[r] >> 20, slen(r), hiBase, s0, s1, s2);
     };
     // sum_k N_ik src_k for the owned rows (paths without the band): matrix
-    // from shared memory or L2, src gathered from global memory
-    auto gather = [&](const V4<T>* src, int r, T& s0, T& s1, T& s2) {
+    // from shared memory or L2, src gathered from global memory, in slot order
+    // (iterates) or row order (slots == false: the positions)
+    auto gather = [&](const V4<T>* src, bool slots, int r, T& s0, T& s1, T& s2) {
         s0 = T(0);
         s1 = T(0);
         s2 = T(0);
@@ -493,7 +497,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
             T v;
             int j;
             entry(r, k, v, j);
-            const V4<T> xj = ldv<kL1>(src, j);
+            const V4<T> xj = ldv<kL1>(src, slots ? slot_of(j) : j);
             s0 += v * xj.x;
             s1 += v * xj.y;
             s2 += v * xj.z;
@@ -506,28 +510,30 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
         for (int r = 0; r < R; ++r) {
             if (!val[r]) continue;
             const int i = rowof(r);
-            const int b = a.lPtr[i], e = a.lPtr[i + 1];
+            const int2 st = stencil_of(i, a.lPtr, a.tOff);
             T a0, a1, a2;
             if constexpr (kCorr) {
                 const V4<T> h = ldv<kL1>(a.Ph, i), l = ldv<kL1>(a.Pl, i);
                 a0 = a1 = a2 = T(0);
-                for (int s = b + 1; s < e; ++s) {
-                    const int j = a.lNbr[s];
+                for (int k = 0; k < st.y; ++k) {
+                    const int s = st.x + kSlice * k;
+                    const int j = __ldg(a.tNbr + s);
                     const V4<T> hj = ldv<kL1>(a.Ph, j), lj = ldv<kL1>(a.Pl, j);
-                    const T wl = a.lLbo[s];
+                    const T wl = __ldg(a.tLbo + s);
                     a0 += wl * diff_ff(hj.x, lj.x, h.x, l.x);
                     a1 += wl * diff_ff(hj.y, lj.y, h.y, l.y);
                     a2 += wl * diff_ff(hj.z, lj.z, h.z, l.z);
                 }
             } else {
                 const V4<S> x = ldv<kL1>(a.P, i);
-                const T l0 = a.lLbo[b];
+                const T l0 = __ldg(a.tLbo0 + i);
                 a0 = x.x * l0;
                 a1 = x.y * l0;
                 a2 = x.z * l0;
-                for (int s = b + 1; s < e; ++s) {
-                    const V4<T> xj = ldv<kL1>(a.P, a.lNbr[s]);
-                    const T l = a.lLbo[s];
+                for (int k = 0; k < st.y; ++k) {
+                    const int s = st.x + kSlice * k;
+                    const V4<T> xj = ldv<kL1>(a.P, __ldg(a.tNbr + s));
+                    const T l = __ldg(a.tLbo + s);
                     a0 += xj.x * l;
                     a1 += xj.y * l;
                     a2 += xj.z * l;
@@ -556,7 +562,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
             rh[r][0] = rh[r][1] = rh[r][2] = T(0);
             if (!val[r]) continue;
             const int i = rowof(r);
-            const int b = a.lPtr[i], e = a.lPtr[i + 1];
+            const int2 st = stencil_of(i, a.lPtr, a.tOff);
             const V4<S> x = ldv<kL1>(a.P, i);
             const T strain = a.Strain[i];
             if constexpr (kCorr) {
@@ -588,25 +594,27 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     r2.add(dc * (T)(xo.z - x.z));
                 }
                 const V4<T> h = ldv<kL1>(a.Ph, i), l = ldv<kL1>(a.Pl, i);
-                for (int s = b + 1; s < e; ++s) {
-                    const int j = a.lNbr[s];
+                for (int k = 0; k < st.y; ++k) {
+                    const int s = st.x + kSlice * k;
+                    const int j = __ldg(a.tNbr + s);
                     const V4<T> hj = ldv<kL1>(a.Ph, j), lj = ldv<kL1>(a.Pl, j);
                     const T d0 = diff_ff(h.x, l.x, hj.x, lj.x), d1 = diff_ff(h.y, l.y, hj.y, lj.y),
                             d2 = diff_ff(h.z, l.z, hj.z, lj.z);
                     const T cl = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
-                    const T rc = strain * (a.lRest[s] / cl);
+                    const T rc = strain * (__ldg(a.tRest + s) / cl);
                     r0.add(rc * d0);
                     r1.add(rc * d1);
                     r2.add(rc * d2);
                 }
                 const V4<T> ai = ldv<kL1>(a.Aq, i);
-                const T b0 = a.lBend[b];
+                const T b0 = __ldg(a.tBend0 + i);
                 r0.add(b0 * ai.x);
                 r1.add(b0 * ai.y);
                 r2.add(b0 * ai.z);
-                for (int s = b + 1; s < e; ++s) {
-                    const V4<T> ak = ldv<kL1>(a.Aq, a.lNbr[s]);
-                    const T bt = a.lBendT[s];
+                for (int k = 0; k < st.y; ++k) {
+                    const int s = st.x + kSlice * k;
+                    const V4<T> ak = ldv<kL1>(a.Aq, __ldg(a.tNbr + s));
+                    const T bt = __ldg(a.tBendT + s);
                     r0.add(bt * ak.x);
                     r1.add(bt * ak.y);
                     r2.add(bt * ak.z);
@@ -635,25 +643,27 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                 x0[r][1] = x.y;
                 x0[r][2] = x.z;
                 T t0 = T(0), t1 = T(0), t2 = T(0);
-                for (int s = b + 1; s < e; ++s) {
-                    const V4<T> xj = ldv<kL1>(a.P, a.lNbr[s]);
+                for (int k = 0; k < st.y; ++k) {
+                    const int s = st.x + kSlice * k;
+                    const V4<T> xj = ldv<kL1>(a.P, __ldg(a.tNbr + s));
                     const T d0 = x.x - xj.x, d1 = x.y - xj.y, d2 = x.z - xj.z;
                     const T cl = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
-                    const T rc = strain * (a.lRest[s] / cl);
+                    const T rc = strain * (__ldg(a.tRest + s) / cl);
                     t0 += rc * d0;
                     t1 += rc * d1;
                     t2 += rc * d2;
                 }
                 const V4<T> ai = ldv<kL1>(a.Aq, i);
-                const T b0 = a.lBend[b];
+                const T b0 = __ldg(a.tBend0 + i);
                 t0 += b0 * ai.x;
                 t1 += b0 * ai.y;
                 t2 += b0 * ai.z;
                 const V4<T> q0 = ldcg4(a.Rhs0, i);
                 T u0 = q0.x + t0, u1 = q0.y + t1, u2 = q0.z + t2;
-                for (int s = b + 1; s < e; ++s) {
-                    const V4<T> ak = ldv<kL1>(a.Aq, a.lNbr[s]);
-                    const T bt = a.lBendT[s];
+                for (int k = 0; k < st.y; ++k) {
+                    const int s = st.x + kSlice * k;
+                    const V4<T> ak = ldv<kL1>(a.Aq, __ldg(a.tNbr + s));
+                    const T bt = __ldg(a.tBendT + s);
                     u0 += bt * ak.x;
                     u1 += bt * ak.y;
                     u2 += bt * ak.z;
@@ -687,7 +697,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
             y[0] = om1 * c[0] + w * ((s0 + rh[r][0]) * id[r]);
             y[1] = om1 * c[1] + w * ((s1 + rh[r][1]) * id[r]);
             y[2] = om1 * c[2] + w * ((s2 + rh[r][2]) * id[r]);
-            if (val[r]) stcg4(a.GY, rowof(r), y[0], y[1], y[2]);
+            if (val[r]) stcg4(a.GY, slotof(r), y[0], y[1], y[2]);
         };
         // second sweep of step it: S(y), Chebyshev-combined with the previous
         // second-sweep iterate p except for the first step; the last one
@@ -719,7 +729,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     stcg4(a.P, rowof(r), n[0], n[1], n[2]);
                 }
             } else {
-                stcg4(xout, rowof(r), n[0], n[1], n[2]);
+                stcg4(xout, slotof(r), n[0], n[1], n[2]);
             }
         };
         const int nsteps = a.cheby;
@@ -742,7 +752,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                 }
             };
             auto own_slot = [&](int r, T (&c)[3]) {
-                const int q = val[r] ? rowof(r) - own0 : 0;
+                const int q = val[r] ? slotof(r) - own0 : 0;
                 c[0] = ox[q];
                 c[1] = oy[q];
                 c[2] = oz[q];
@@ -751,7 +761,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
 #pragma unroll
                 for (int r = 0; r < R; ++r)
                     if (val[r]) {
-                        const int q = rowof(r) - own0;
+                        const int q = slotof(r) - own0;
                         ox[q] = nv[r][0];
                         oy[q] = nv[r][1];
                         oz[q] = nv[r][2];
@@ -793,7 +803,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                 const T zero[3] = {T(0), T(0), T(0)};
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    if (val[r]) stcg4(a.GX2, rowof(r), T(0), T(0), T(0));
+                    if (val[r]) stcg4(a.GX2, slotof(r), T(0), T(0), T(0));
                     finish_y(r, T(0), T(0), T(0), zero, nv[r]);
                 }
             }
@@ -810,7 +820,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     for (int r = 0; r < R; ++r) {
                         p[r][0] = p[r][1] = p[r][2] = T(0);
                         if (it > 0 && val[r]) {
-                            const V4<T> g = ldcg4(xb, rowof(r));
+                            const V4<T> g = ldcg4(xb, slotof(r));
                             p[r][0] = g.x;
                             p[r][1] = g.y;
                             p[r][2] = g.z;
@@ -854,7 +864,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     cx[r][0] = x0[r][0];
                     cx[r][1] = x0[r][1];
                     cx[r][2] = x0[r][2];
-                    if (val[r]) gather(a.P, r, s0, s1, s2);
+                    if (val[r]) gather(a.P, false, r, s0, s1, s2);
                 }
                 finish_y(r, s0, s1, s2, cx[r], yv[r]);
             }
@@ -864,7 +874,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     T s0 = T(0), s1 = T(0), s2 = T(0), n[3];
-                    if (val[r]) gather(a.GY, r, s0, s1, s2);
+                    if (val[r]) gather(a.GY, true, r, s0, s1, s2);
                     finish_x(r, s0, s1, s2, yv[r], px[r], it, last, a.GX, n);
                     px[r][0] = cx[r][0];
                     px[r][1] = cx[r][1];
@@ -878,7 +888,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     T s0 = T(0), s1 = T(0), s2 = T(0);
-                    if (val[r]) gather(a.GX, r, s0, s1, s2);
+                    if (val[r]) gather(a.GX, true, r, s0, s1, s2);
                     finish_y(r, s0, s1, s2, cx[r], yv[r]);
                 }
                 if (!sync()) return;

@@ -17,6 +17,19 @@ constexpr int kMaxPersistWarps = 28;
 // (read through the constant cache, off the shared-memory pipe)
 constexpr int kParamPatterns = 4096;
 
+// Slot order of the persistent solve: in every window of 64 rows, its 32 even
+// rows, then its 32 odd rows (a fixed bijection of [0, 64 ceil(n / 64))).  The
+// iterates, the matrix slices and the band in shared memory are kept in slot
+// order; the state arrays stay in row (vertex) order.  A structured triangle
+// mesh whose quads alternate their diagonal has two stencil shapes that
+// alternate with the row parity: in slot order the 32 rows of a warp share one
+// shape, so a warp's k-th entries read 32 consecutive slots (no shared-memory
+// bank conflicts) and its column offsets are one constant-cache address.
+__host__ __device__ __forceinline__ int slot_of(int row) { return (row & ~63) | ((row & 1) << 5) | ((row >> 1) & 31); }
+__host__ __device__ __forceinline__ int row_of(int slot) {
+    return (slot & ~63) | ((slot >> 5) & 1) | ((slot & 31) << 1);
+}
+
 // One configuration of the persistent solve, as the autotuner names it.
 struct PlanChoice {
     int rows_per_thread = 0;  // R, slices per warp; 0: one launch per sweep instead
@@ -46,6 +59,7 @@ struct PersistPlan {
 template <typename T, typename S>
 struct PersistArgs {
     int nsim;
+    int nslot;  // 64 ceil(nsim / 64): slots of the iterates
     int lg;
     int cheby;
     T relax;
@@ -61,21 +75,25 @@ struct PersistArgs {
     const V4<T>* CollRhs;
     const V4<T>* PinRhs;
     V4<T>* Aq;
-    V4<T>* GX;   // second-sweep iterates (odd steps in GX2 on the band path)
+    V4<T>* GX;   // second-sweep iterates (odd steps in GX2 on the band path), slot order [nslot]
     V4<T>* GX2;
-    V4<T>* GY;   // first-sweep iterates
+    V4<T>* GY;   // first-sweep iterates, slot order [nslot]
     const T* Delastic;
     const T* Dinert;
     const T* CollDiag;
     const int* PinFlag;
     const T* PinK;
-    // local step stencils
+    // local step stencils: counts from the CSR row pointer, neighbours and
+    // weights from the SELL-32 copy (neighbour k of row i at tOff[i >> 5] +
+    // 32 k + (i & 31)), self weights per row
     const int* lPtr;
-    const int* lNbr;
-    const T* lRest;
-    const T* lLbo;
-    const T* lBend;
-    const T* lBendT;
+    const int* tOff;
+    const int* tNbr;
+    const T* tRest;
+    const T* tLbo;
+    const T* tBendT;
+    const T* tBend0;
+    const T* tLbo0;
     const T* Strain;
     const T* CurvNorm;
     // tetrahedral strain constraints: CTA c projects tets ctaTetIdx[ctaTetPtr[c] ..
@@ -90,15 +108,15 @@ struct PersistArgs {
     const int* vtIdx;
     const int* ctaTetPtr;
     const int* ctaTetIdx;
-    // matrix
+    // matrix, SELL-32 over slots: slice s holds the rows of slots [32 s, 32 s + 32)
     const int* sliceEntry;  // SELL entry offset of every slice
     const int* sliceLen;
-    const int* sCol;        // absolute columns (matrix streamed from global)
+    const int* sCol;        // absolute columns, row order (matrix streamed from global)
     const T* sVal;
-    const int* ctaSlice;    // first slice of each CTA (ctas + 1)
+    const int* ctaSlice;    // first slice of each CTA (ctas + 1; even: CTAs own whole 64-row windows)
     const int* ctaEntry;    // first SELL entry of each CTA (ctas + 1)
     const int* rowPattern;  // pattern id of every row (matrix in shared memory)
-    const int16_t* patOff;  // [patterns x pattern_width] column offsets
+    const int16_t* patOff;  // [patterns x pattern_width] column offsets in row order
     int16_t patc[kParamPatterns];  // band path: the same table (patterns x pattern_width <= kParamPatterns)
     int patterns;
     int patW;
@@ -115,8 +133,8 @@ struct PersistArgs {
     const int2* nbr;
     unsigned epoch0;
     // band of the iterate in shared memory (band != null, matrix in shared
-    // memory, neighbour synchronisation): CTA c's matrix rows read columns
-    // [band[c].x, band[c].y).  Its own rows stay in three planar arrays of
+    // memory, neighbour synchronisation): CTA c's matrix rows read the slots
+    // [band[c].x, band[c].y) (whole 64-row windows).  Its own rows stay in three planar arrays of
     // ownMax floats that its threads update after every sweep; the halo (the
     // columns outside its own rows, at most haloMax vertices) is copied from
     // global memory in two bulk copies per sweep

@@ -147,8 +147,11 @@ public:
         PD_CK(zeros(d.X0, ns));
         PD_CK(zeros(d.Vel, ns));
         PD_CK(zeros(d.Dir, nt));
-        PD_CK(zeros(d.Y, ns));
-        PD_CK(zeros(d.B, ns));
+        // iterates: row order on the per-sweep path, slot order (a multiple of
+        // 64 slots) on the persistent one
+        const int nslot = (ns + 63) / 64 * 64;
+        PD_CK(zeros(d.Y, nslot));
+        PD_CK(zeros(d.B, nslot));
         PD_CK(zeros(d.Aq, ns));
         PD_CK(zeros(d.Rhs, ns));
         PD_CK(zeros(d.Rhs0, ns));
@@ -184,7 +187,7 @@ public:
         PD_CK(up(d.Strain, st));
         PD_CK(up(d.PinFlag, pinf));
         PD_CK(up(d.PinK, conv(H.pinK)));
-        PD_CK(zeros(d.C, ns));
+        PD_CK(zeros(d.C, nslot));
         std::vector<TC> cm(nt, (TC)p.static_mass);
         for (int i = 0; i < ns; ++i) cm[i] = (TC)(T)H.collMassSim[i];
         PD_CK(up(d.CollMass, cm));
@@ -210,6 +213,41 @@ public:
         PD_CK(up(d.lLbo, conv(H.lLbo)));
         PD_CK(up(d.lBend, conv(H.lBend)));
         PD_CK(up(d.lBendT, conv(H.lBendT)));
+        {   // and in SELL-32 order (padding: the row itself, zero weights, never read)
+            const int nsl = (ns + kSlice - 1) / kSlice;
+            std::vector<int> toff(nsl + 1, 0);
+            for (int sl = 0; sl < nsl; ++sl) {
+                int w = 0;
+                for (int r = sl * kSlice; r < std::min(ns, (sl + 1) * kSlice); ++r)
+                    w = std::max(w, H.lPtr[r + 1] - H.lPtr[r] - 1);
+                toff[sl + 1] = toff[sl] + kSlice * w;
+            }
+            const size_t tsz = (size_t)std::max(toff[nsl], 1);
+            std::vector<int> tn(tsz, 0);
+            std::vector<T> tr(tsz, T(0)), tl(tsz, T(0)), tb(tsz, T(0)), b0(ns), l0(ns);
+            for (int r = 0; r < ns; ++r) {
+                const int sl = r / kSlice, b = H.lPtr[r], e = H.lPtr[r + 1], at = toff[sl] + r % kSlice;
+                const int w = (toff[sl + 1] - toff[sl]) / kSlice;
+                b0[r] = (T)H.lBend[b];
+                l0[r] = (T)H.lLbo[b];
+                for (int k = 0; k < w; ++k) {
+                    const size_t q = (size_t)at + (size_t)kSlice * k;
+                    const int s = b + 1 + k;
+                    const bool live = s < e;
+                    tn[q] = live ? H.lNbr[s] : r;
+                    tr[q] = live ? (T)H.lRest[s] : T(0);
+                    tl[q] = live ? (T)H.lLbo[s] : T(0);
+                    tb[q] = live ? (T)H.lBendT[s] : T(0);
+                }
+            }
+            PD_CK(up(d.tOff, toff));
+            PD_CK(up(d.tNbr, tn));
+            PD_CK(up(d.tRest, tr));
+            PD_CK(up(d.tLbo, tl));
+            PD_CK(up(d.tBendT, tb));
+            PD_CK(up(d.tBend0, b0));
+            PD_CK(up(d.tLbo0, l0));
+        }
 
         // ---- system matrix in SELL-32 ----
         d.nslice = (ns + kSlice - 1) / kSlice;
@@ -257,8 +295,6 @@ public:
         PD_CK(up(d.sLen, slen));
         PD_CK(up(d.sCol, scol));
         PD_CK(up(d.sVal, sval));
-        sliceOffH_ = soff;
-        sliceLenH_ = slen;
 
         // ---- collision topology ----
         std::vector<int4> faces(d.nface);
@@ -302,7 +338,7 @@ public:
         PD_CK(cudaMallocHost(&stage_, sizeof(V4<TC>) * (size_t)std::max(nt, 1)));
 
         // ---- persistent PD solve plan (needs every buffer above) ----
-        pdipc_status pr = plan_persistent(H, sliceOffH_, sliceLenH_, err);
+        pdipc_status pr = plan_persistent(H, err);
         if (pr != PDIPC_OK) return pr;
 
         // ---- patch tree at the rest positions (AipcBvhs::init at initialization) ----
@@ -440,7 +476,7 @@ private:
             }
         }
         if (cached) {
-            pdipc_status r = plan_persistent(H, sliceOffH_, sliceLenH_, err, best.pd.rows_per_thread ? &best.pd : nullptr);
+            pdipc_status r = plan_persistent(H, err, best.pd.rows_per_thread ? &best.pd : nullptr);
             if (r != PDIPC_OK) return r;
             if (best.pd.rows_per_thread == 0) plan_ = PersistPlan();
             c_.cand_grid = best.cand_grid;
@@ -483,7 +519,7 @@ private:
         if (pds[0].rows_per_thread != 0) pds.push_back(PlanChoice{});  // one launch per sweep
         float bestMs = -1.f;
         for (size_t k = 0; k < pds.size(); ++k) {
-            pdipc_status r = plan_persistent(H, sliceOffH_, sliceLenH_, err, pds[k].rows_per_thread ? &pds[k] : nullptr);
+            pdipc_status r = plan_persistent(H, err, pds[k].rows_per_thread ? &pds[k] : nullptr);
             if (r != PDIPC_OK) return r;
             if (pds[k].rows_per_thread == 0) plan_ = PersistPlan();
             else if (!plan_.enabled) continue;
@@ -497,7 +533,7 @@ private:
                 best.pd = pds[k];
             }
         }
-        pdipc_status r = plan_persistent(H, sliceOffH_, sliceLenH_, err, best.pd.rows_per_thread ? &best.pd : nullptr);
+        pdipc_status r = plan_persistent(H, err, best.pd.rows_per_thread ? &best.pd : nullptr);
         if (r != PDIPC_OK) return r;
         if (best.pd.rows_per_thread == 0) plan_ = PersistPlan();
         tuning_.pd_solve_ms = bestMs;
@@ -1279,8 +1315,7 @@ private:
     // The launch plan of the persistent solve: the default configuration, or
     // `force` when given (disabled if that configuration does not fit).  May
     // run again (the autotuner): the previous plan's tables are freed first.
-    pdipc_status plan_persistent(const HostTables& H, const std::vector<int>& soff, const std::vector<int>& slen,
-                                 std::string& err, const PlanChoice* force = nullptr) {
+    pdipc_status plan_persistent(const HostTables& H, std::string& err, const PlanChoice* force = nullptr) {
         plan_ = PersistPlan();
         dfree(pNbr_);
         dfree(pCtaTetPtr_);
@@ -1292,17 +1327,50 @@ private:
         dfree(pRowPat_);
         dfree(pPatOff_);
         dfree(pBar_);
+        dfree(pSOff_);
+        dfree(pSLen_);
+        dfree(pSCol_);
+        dfree(pSVal_);
         // the persistent solve covers cloth stencils only: tet models take the per-sweep path
         if (!std::is_same<T, float>::value || !prm_.persistent || c_.cheby >= kMaxCheby)
             return PDIPC_OK;
         Dev<T, TC>& d = d_;
-        const int ns = d.nsim, nsl = d.nslice;
+        const int ns = d.nsim;
         int dev = 0, nsm = 0, smem_optin = 0, coop = 0;
         PD_CK(cudaGetDevice(&dev));
         PD_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
         PD_CK(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
         PD_CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-        if (!coop || nsl == 0) return PDIPC_OK;
+        if (!coop || ns == 0) return PDIPC_OK;
+        // the matrix in SELL-32 over slots (slot_of: in every 64-row window the
+        // even rows, then the odd ones); columns stay rows, padding repeats a
+        // row's last column with value 0 (so its columns stay in order: low
+        // halo, own rows, high halo)
+        const int nslot = (ns + 63) / 64 * 64, nsl = nslot / kSlice;
+        std::vector<int> soff(nsl + 1, 0), slen(nsl, 0);
+        auto row_len = [&](int r) { return r < ns ? H.nPtr[r + 1] - H.nPtr[r] : 0; };
+        for (int sl = 0; sl < nsl; ++sl) {
+            for (int lane = 0; lane < kSlice; ++lane) slen[sl] = std::max(slen[sl], row_len(row_of(sl * kSlice + lane)));
+            soff[sl + 1] = soff[sl] + kSlice * slen[sl];
+        }
+        {
+            std::vector<int> pcol((size_t)std::max(soff[nsl], 1), 0);
+            std::vector<T> pval((size_t)std::max(soff[nsl], 1), T(0));
+            for (int sl = 0; sl < nsl; ++sl)
+                for (int lane = 0; lane < kSlice; ++lane) {
+                    const int r = row_of(sl * kSlice + lane), len = row_len(r);
+                    for (int k = 0; k < slen[sl]; ++k) {
+                        const size_t at = (size_t)soff[sl] + (size_t)kSlice * k + lane;
+                        const int e = r < ns ? H.nPtr[r] + std::min(k, std::max(len - 1, 0)) : 0;
+                        pcol[at] = len > 0 ? H.nCol[e] : std::min(r, ns - 1);
+                        pval[at] = k < len ? (T)H.nVal[e] : T(0);
+                    }
+                }
+            PD_CK(up(pSOff_, soff));
+            PD_CK(up(pSLen_, slen));
+            PD_CK(up(pSCol_, pcol));
+            PD_CK(up(pSVal_, pval));
+        }
         // distinct column-offset patterns of the rows
         int patW = 0;
         for (int w : slen) patW = std::max(patW, w);
@@ -1349,15 +1417,18 @@ private:
             rg.assign(ctas, make_int2(0, 0));
             int mx = 0;
             for (int c = 0; c < ctas; ++c) {
-                const int r0 = c * spc * kSlice, r1 = std::min(ns, (c + 1) * spc * kSlice);
-                int lo = r0, hi = std::max(r0, r1 - 1);
-                for (int r = r0; r < r1; ++r)
+                // own slots [r0, r1): the rows of whole 64-row windows
+                const int r0 = c * spc * kSlice, r1 = std::min(nslot, (c + 1) * spc * kSlice);
+                int lo = r0, hi = r1 - 1;
+                for (int r = r0; r < std::min(ns, r1); ++r)
                     for (int e = H.nPtr[r]; e < H.nPtr[r + 1]; ++e) {
                         lo = std::min(lo, H.nCol[e]);
                         hi = std::max(hi, H.nCol[e]);
                     }
-                rg[c] = make_int2(lo, hi + 1);
-                mx = std::max(mx, (r0 - lo) + (hi + 1 - r1));
+                lo &= ~63;                                    // whole windows of slots
+                const int hs = std::min(nslot, (hi + 64) & ~63);
+                rg[c] = make_int2(lo, hs);
+                mx = std::max(mx, (r0 - lo) + (hs - r1));
             }
             return mx;
         };
@@ -1386,7 +1457,8 @@ private:
             if (pass == 0 && !fits16) continue;
             if (pass == 1 && !cands.empty()) break;  // the L2-streamed matrix only when no slice fits
             for (int R = 1; R <= 4; ++R) {
-                const int W = std::max(1, (nsl + nsm * R - 1) / (nsm * R));
+                int W = std::max(1, (nsl + nsm * R - 1) / (nsm * R));
+                if ((W * R) & 1) ++W;  // CTAs own whole windows (pairs of slices)
                 if (W > kMaxPersistWarps) continue;
                 const int spc = W * R;
                 const int ctas = (nsl + spc - 1) / spc;
@@ -1458,6 +1530,7 @@ private:
         for (auto& kv : pats) std::copy(kv.first.begin(), kv.first.end(), patOff.begin() + (size_t)kv.second * patW);
         // CTAs each CTA exchanges rows with: the CTAs owning the columns of its
         // matrix rows and stencils, closed under "is read by", as one range
+        // (a CTA's slots are the rows of whole windows: the same range of rows)
         std::vector<int> ctaOfRow(ns, 0);
         for (int c = 0; c < plan_.ctas; ++c)
             for (int r = ctaSlice[c] * kSlice; r < std::min(ns, ctaSlice[c + 1] * kSlice); ++r) ctaOfRow[r] = c;
@@ -1528,6 +1601,7 @@ private:
         if constexpr (std::is_same<T, float>::value) {
             PersistArgs<float, TC>& a = pargs_;
             a.nsim = ns;
+            a.nslot = nslot;
             a.lg = c_.lg;
             a.cheby = c_.cheby;
             a.relax = (T)c_.relax;
@@ -1558,11 +1632,13 @@ private:
             a.PinFlag = d.PinFlag;
             a.PinK = d.PinK;
             a.lPtr = d.lPtr;
-            a.lNbr = d.lNbr;
-            a.lRest = d.lRest;
-            a.lLbo = d.lLbo;
-            a.lBend = d.lBend;
-            a.lBendT = d.lBendT;
+            a.tOff = d.tOff;
+            a.tNbr = d.tNbr;
+            a.tRest = d.tRest;
+            a.tLbo = d.tLbo;
+            a.tBendT = d.tBendT;
+            a.tBend0 = d.tBend0;
+            a.tLbo0 = d.tLbo0;
             a.Strain = d.Strain;
             a.CurvNorm = d.CurvNorm;
             a.ntet = d.ntet;
@@ -1574,10 +1650,10 @@ private:
             a.vtIdx = d.vtIdx;
             a.ctaTetPtr = pCtaTetPtr_;
             a.ctaTetIdx = pCtaTetIdx_;
-            a.sliceEntry = d.sOff;
-            a.sliceLen = d.sLen;
-            a.sCol = d.sCol;
-            a.sVal = d.sVal;
+            a.sliceEntry = pSOff_;
+            a.sliceLen = pSLen_;
+            a.sCol = pSCol_;
+            a.sVal = pSVal_;
             a.ctaSlice = pCtaSlice_;
             a.ctaEntry = pCtaEntry_;
             a.rowPattern = pRowPat_;
@@ -1595,8 +1671,8 @@ private:
             a.haloMax = plan_.halo_max;
             a.epoch0 = 0;
             const void* ptrs[] = {a.P, a.Pold, a.Xrest, a.Rhs0, a.CollRhs, a.PinRhs, a.Aq, a.GX, a.GX2, a.GY, a.Delastic,
-                                  a.Dinert, a.CollDiag, a.PinFlag, a.PinK, a.lPtr, a.lNbr, a.lRest, a.lLbo,
-                                  a.lBend, a.lBendT, a.Strain, a.CurvNorm, a.sliceEntry, a.sliceLen, a.sCol,
+                                  a.Dinert, a.CollDiag, a.PinFlag, a.PinK, a.lPtr, a.tOff, a.tNbr, a.tRest,
+                                  a.tLbo, a.tBendT, a.tBend0, a.tLbo0, a.Strain, a.CurvNorm, a.sliceEntry, a.sliceLen, a.sCol,
                                   a.sVal, a.ctaSlice, a.ctaEntry, a.rowPattern, a.patOff, a.bar, a.err};
             if (a.ntet > 0 && (!a.Tets || !a.TetIdm || !a.TetW || !a.TetOut || !a.vtPtr || !a.vtIdx)) {
                 plan_.enabled = false;
@@ -2017,8 +2093,12 @@ private:
     PersistPlan plan_;
     std::vector<PlanChoice> plan_choices_;  // every persistent configuration that fits (default planning)
     pdipc_tuning tuning_{};
-    std::vector<int> sliceOffH_, sliceLenH_;
     PersistArgs<float, TC> pargs_{};
+    // the matrix in SELL-32 over slots (slot_of) for the persistent solve
+    int* pSOff_ = nullptr;
+    int* pSLen_ = nullptr;
+    int* pSCol_ = nullptr;
+    T* pSVal_ = nullptr;
     int* pCtaSlice_ = nullptr;
     int* pCtaEntry_ = nullptr;
     int* pRowPat_ = nullptr;
@@ -2026,7 +2106,7 @@ private:
     unsigned* pBar_ = nullptr;
     unsigned* pFlags_ = nullptr;  // per-CTA phase counts of the neighbour synchronisation
     int2* pNbr_ = nullptr;        // per-CTA range of CTAs to wait for
-    int2* pBand_ = nullptr;       // per-CTA [first, last + 1) column of its rows (band path)
+    int2* pBand_ = nullptr;       // per-CTA [first, last + 1) slot its rows read (band path)
     int* pCtaTetPtr_ = nullptr;   // per-CTA range of the tets it projects
     int* pCtaTetIdx_ = nullptr;
     unsigned epoch_ = 1;

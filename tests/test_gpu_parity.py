@@ -214,13 +214,14 @@ def test_fp32_steps_match_oracle_short_horizon(built_lib):
 
 
 @pytest.mark.parametrize("prec,atol", [("fp32", 2e-5), ("mixed", 1e-6)])
-@pytest.mark.parametrize("n", [16, 48, 160])
+@pytest.mark.parametrize("n", [16, 37, 48, 160])
 @pytest.mark.parametrize("variant", [1, 2, 3, 4])
 def test_persistent_solve_matches_per_sweep_launches(prec, atol, n, variant, built_lib):
     """One cooperative launch per outer iteration (neighbour synchronisation or
     grid barriers; sweeps gathering from the shared-memory band, through L1 or
     L2 only) gives the same PD solve as one launch per sweep.  At 48 and 160 a
-    CTA's rows reach several CTAs on each side."""
+    CTA's rows reach several CTAs on each side; 37 x 37 = 1369 rows end in a
+    partial 64-row window of the solve's slot order."""
     sc = small_scene(n, 2)
     a = pdipc.Simulator(sc, prec, persistent=variant)
     b = pdipc.Simulator(sc, prec, persistent=0)
