@@ -53,19 +53,21 @@ __device__ __forceinline__ void warp_box_reduce(T lo[3], T hi[3]) {
 // vertices, minus/plus the inflation radius (getFaceBbox, cu:1350-1375), then
 // reduced over the patch's faces.  Boxes are in T: FP64 state (S) is rounded
 // to T first (read from the T-rounded copies Xh, Dh when given), so the mixed
-// form's boxes are the FP32 form's.
+// form's boxes are the FP32 form's.  One thread per patch: a grid patch holds
+// a few faces (about two on a cloth whose patch grid matches its vertex grid),
+// and min/max give the same box in any order.
 template <typename T, typename S>
 __global__ void k_patch_boxes(int npatch, const int* __restrict__ pfPtr, const int* __restrict__ pfIdx,
                               const int4* __restrict__ Faces, const V4<S>* __restrict__ X,
                               const V4<S>* __restrict__ D, const V4<T>* __restrict__ Xh,
                               const V4<T>* __restrict__ Dh, T infl, Box6<T>* __restrict__ out) {
-    const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npatch) return;
     T lo[3] = {tmax_val<T>(), tmax_val<T>(), tmax_val<T>()};
     T hi[3] = {-tmax_val<T>(), -tmax_val<T>(), -tmax_val<T>()};
-    const int b = pfPtr[p], e = pfPtr[p + 1];
-    for (int q = b + lane; q < e; q += 32) {
+    const int b = __ldg(pfPtr + p), e = __ldg(pfPtr + p + 1);
+#pragma unroll 2
+    for (int q = b; q < e; ++q) {
         const int4 f = Faces[pfIdx[q]];
         const int vv[3] = {f.x, f.y, f.z};
         T a[3][3], c[3][3];
@@ -104,15 +106,12 @@ __global__ void k_patch_boxes(int npatch, const int* __restrict__ pfPtr, const i
             hi[k] = dmax(hi[k], mx);
         }
     }
-    warp_box_reduce(lo, hi);
-    if (lane == 0) {
-        Box6<T> bx;
-        for (int k = 0; k < 3; ++k) {
-            bx.lo[k] = lo[k];
-            bx.hi[k] = hi[k];
-        }
-        out[p] = bx;
+    Box6<T> bx;
+    for (int k = 0; k < 3; ++k) {
+        bx.lo[k] = lo[k];
+        bx.hi[k] = hi[k];
     }
+    out[p] = bx;
 }
 
 // Init-time patch boxes over every vertex of the patch's faces, inflated
@@ -980,8 +979,8 @@ template <typename T, typename TC>
 void launch_patch_boxes(const Dev<T, TC>& d, const V4<TC>* X, const V4<TC>* D, const V4<T>* Xh, const V4<T>* Dh,
                         T infl, cudaStream_t s) {
     if (d.npatch == 0) return;
-    k_patch_boxes<T, TC><<<blocks_for((int64_t)d.npatch * 32), kBlock, 0, s>>>(d.npatch, d.pfPtr, d.pfIdx, d.Faces, X,
-                                                                              D, Xh, Dh, infl, d.PatchBox);
+    k_patch_boxes<T, TC><<<blocks_for(d.npatch, 128), 128, 0, s>>>(d.npatch, d.pfPtr, d.pfIdx, d.Faces, X, D, Xh, Dh,
+                                                                  infl, d.PatchBox);
 }
 template <typename T, typename TC>
 void launch_patch_init_boxes(const Dev<T, TC>& d, T infl, cudaStream_t s) {
