@@ -201,3 +201,32 @@ def test_adjoint_matches_the_oracle_restatement(built_lib):
     ref = orc.adjoint_rollout(T, x0, v0, gx, gv)
     for name, a, b in zip(("x0", "v0", "k"), ours, ref):
         assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b), (name, np.linalg.norm(a - b), np.linalg.norm(b))
+
+
+def test_adjoint_matches_the_oracle_on_the_128_cloth_50_steps(built_lib):
+    """Config 3's rollout shape (128x128 cloth, 50 steps, checkpoints every 10,
+    10 local-global iterations x 15 Chebyshev steps x 3 outer iterations): the
+    GPU adjoint against the oracle's sequential restatement of the same reverse
+    pass, every gradient within 1e-5 of the oracle's, norm-relative.  The
+    oracle's adjoint is itself tied to its forward-mode tangent (the transpose
+    identity to round-off, tests/test_adjoint_cpu.py), which is the check that
+    holds at this length where central differences of the forward do not."""
+    import os
+
+    from oracle.oracle import FORM_JJ, Oracle
+
+    sc = free_cloth(128)
+    kw = dict(fixed_outer=3)
+    sim = make(sc, **kw)
+    orc = Oracle(sc, "fp64", FORM_JJ, threads=os.cpu_count() or 8, **kw)
+    rng = np.random.default_rng(8)
+    n, T = sc.n_sim, 50
+    x0 = sc.initial_positions()
+    v0 = rng.uniform(-0.1, 0.1, (n, 3))
+    gx, gv = rng.normal(size=(n, 3)), rng.normal(size=(n, 3))
+    rollout(sim, x0, v0, T, every=10)
+    ours = sim.adjoint_backward(gx, gv)
+    ref = orc.adjoint_rollout(T, x0, v0, gx, gv)
+    for name, a, b in zip(("x0", "v0", "k"), ours, ref):
+        assert np.all(np.isfinite(a)) and np.linalg.norm(b) > 0
+        assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b), (name, np.linalg.norm(a - b), np.linalg.norm(b))
