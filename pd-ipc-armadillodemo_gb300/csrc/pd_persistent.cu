@@ -323,16 +323,18 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
         pid[r] = (kSmem && val[r]) ? a.rowPattern[rowof(r)] * a.patW : 0;
     }
     auto slen = [&](int r) { return pk[r] & 1023; };
-    // entry k of owned row r: value and gathered row (a row, not a slot)
-    auto entry = [&](int r, int k, T& v, int& j) {
+    // entry k of the row `row` whose SELL entries start at g (pattern p):
+    // value and gathered row (a row, not a slot); entry(r, ...) for owned row r
+    auto entry_at = [&](int g, int p, int row, int k, T& v, int& j) {
         if (kSmem) {
-            v = sval[gb[r] - eb + 32 * k];
-            j = rowof(r) + (int)(band ? a.patc[pid[r] + k] : spat[pid[r] + k]);
+            v = sval[g - eb + 32 * k];
+            j = row + (int)(band ? a.patc[p + k] : spat[p + k]);
         } else {
-            v = __ldg(a.sVal + gb[r] + 32 * k);
-            j = __ldg(a.sCol + gb[r] + 32 * k);
+            v = __ldg(a.sVal + g + 32 * k);
+            j = __ldg(a.sCol + g + 32 * k);
         }
     };
+    auto entry = [&](int r, int k, T& v, int& j) { entry_at(gb[r], pid[r], rowof(r), k, v, j); };
     __syncthreads();
     unsigned my_gen = 0;
     if (threadIdx.x == 0) my_gen = ld_acquire_gpu(a.bar);
@@ -356,6 +358,10 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     // two bulk copies once the neighbours have published it.  A CTA owns whole
     // 64-row windows, so a row j is one of its own exactly when slot_of(j) is.
     const int own0 = a.ctaSlice[cta] * 32, own1 = min(a.ctaSlice[cta + 1] * 32, a.nslot);
+    // The curvature and residual phases take the CTA's rows in row order:
+    // thread t of the nct compute threads takes rows own0 + t + k nct
+    // (k < R), which cover [own0, ownEnd).
+    const int nct = nrw * 32, ownEnd = min(a.ctaSlice[cta + 1] * 32, a.nsim);
     const int nlo = band ? own0 - brange.x : 0, nhi = band ? brange.y - own1 : 0;
     const int hiBase = own1 - nlo;  // halo slot of column j >= own1: j - hiBase
     // The band path runs one extra warp, the last, with no rows: it publishes
@@ -365,6 +371,8 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     // when a neighbour wait has failed.
     const bool syncw = band && warp == (int)(blockDim.x >> 5) - 1;
     const unsigned ncomp = blockDim.x - 32u;
+    // barrier of the compute warps alone (band path: the sync warp does not take part)
+    auto comp_bar = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(ncomp) : "memory"); };
     unsigned mphase = 0;
     // sync warp: optionally wait until the neighbours have published phase
     // `epoch`, then copy the halo of src.  The whole poll has one deadline (a
@@ -505,11 +513,11 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     };
 
     for (int lg = 0; lg < a.lg; ++lg) {
-        // ---- curvature vectors of the owned rows ----
+        // ---- curvature vectors of the owned rows, in row order ----
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            if (!val[r]) continue;
-            const int i = rowof(r);
+            const int i = own0 + (int)threadIdx.x + r * nct;
+            if ((int)threadIdx.x >= nct || i >= ownEnd) continue;
             const int2 st = stencil_of(i, a.lPtr, a.tOff);
             T a0, a1, a2;
             if constexpr (kCorr) {
@@ -555,13 +563,11 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
         if (!sync()) return;
 
         // ---- right-hand side (direct) or residual (correction) of the owned rows ----
-        T x0[R][3], rh[R][3];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            x0[r][0] = x0[r][1] = x0[r][2] = T(0);
-            rh[r][0] = rh[r][1] = rh[r][2] = T(0);
-            if (!val[r]) continue;
-            const int i = rowof(r);
+        // row i, whose SELL entries start at gbi (leni of them, pattern pidi):
+        // its right-hand side (direct form, with its positions in xx) or its
+        // residual (correction form) in rr
+        auto rhs_row = [&](int i, int gbi, int leni, int pidi, T (&rr)[3], T (&xx)[3]) {
+            xx[0] = xx[1] = xx[2] = T(0);
             const int2 st = stencil_of(i, a.lPtr, a.tOff);
             const V4<S> x = ldv<kL1>(a.P, i);
             const T strain = a.Strain[i];
@@ -619,29 +625,30 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     r1.add(bt * ak.y);
                     r2.add(bt * ak.z);
                 }
-                if constexpr (kTets)
+                if constexpr (kTets) {
                     for (int q = a.vtPtr[i]; q < a.vtPtr[i + 1]; ++q) {  // tet projections w R G, ascending tet
                         const V4<T> t = ldcg4(a.TetOut, a.vtIdx[q]);
                         r0.add(t.x);
                         r1.add(t.y);
                         r2.add(t.z);
                     }
-                for (int k = 0; k < slen(r); ++k) {
+                }
+                for (int k = 0; k < leni; ++k) {
                     T v;
                     int j;
-                    entry(r, k, v, j);
+                    entry_at(gbi, pidi, i, k, v, j);
                     const V4<T> hj = ldv<kL1>(a.Ph, j), lj = ldv<kL1>(a.Pl, j);
                     r0.add(v * diff_ff(hj.x, lj.x, h.x, l.x));
                     r1.add(v * diff_ff(hj.y, lj.y, h.y, l.y));
                     r2.add(v * diff_ff(hj.z, lj.z, h.z, l.z));
                 }
-                rh[r][0] = r0.value();
-                rh[r][1] = r1.value();
-                rh[r][2] = r2.value();
+                rr[0] = r0.value();
+                rr[1] = r1.value();
+                rr[2] = r2.value();
             } else {
-                x0[r][0] = x.x;
-                x0[r][1] = x.y;
-                x0[r][2] = x.z;
+                xx[0] = x.x;
+                xx[1] = x.y;
+                xx[2] = x.z;
                 T t0 = T(0), t1 = T(0), t2 = T(0);
                 for (int k = 0; k < st.y; ++k) {
                     const int s = st.x + kSlice * k;
@@ -668,24 +675,61 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     u1 += bt * ak.y;
                     u2 += bt * ak.z;
                 }
-                if constexpr (kTets)
+                if constexpr (kTets) {
                     for (int q = a.vtPtr[i]; q < a.vtPtr[i + 1]; ++q) {  // tet projections, ascending tet
                         const V4<T> t = ldcg4(a.TetOut, a.vtIdx[q]);
                         u0 += t.x;
                         u1 += t.y;
                         u2 += t.z;
                     }
-                const V4<T> c = ldcg4(a.CollRhs, i);
-                u0 += c.x;
-                u1 += c.y;
-                u2 += c.z;
+                }
+                const V4<T> cr = ldcg4(a.CollRhs, i);
+                u0 += cr.x;
+                u1 += cr.y;
+                u2 += cr.z;
                 const V4<T> pn = ldcg4(a.PinRhs, i);
                 u0 += pn.x;
                 u1 += pn.y;
                 u2 += pn.z;
-                rh[r][0] = u0;
-                rh[r][1] = u1;
-                rh[r][2] = u2;
+                rr[0] = u0;
+                rr[1] = u1;
+                rr[2] = u2;
+            }
+        };
+        T x0[R][3], rh[R][3];
+        if constexpr (band) {
+            // Row order: the per-row state of consecutive threads' rows sits at
+            // consecutive addresses.  The residuals go to the own-row arrays
+            // (free until the first sweep of this iteration writes them) at the
+            // rows' slots, where every thread picks up those of its own rows.
+            if (!syncw) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int i = own0 + (int)threadIdx.x + r * nct;
+                    if (i >= ownEnd) continue;
+                    const int q = slot_of(i), sl = q >> 5;
+                    T rr[3], xx[3];
+                    rhs_row(i, a.sliceEntry[sl] + (q & 31), a.sliceLen[sl], a.rowPattern[i] * a.patW, rr, xx);
+                    ox[q - own0] = rr[0];
+                    oy[q - own0] = rr[1];
+                    oz[q - own0] = rr[2];
+                }
+                comp_bar();
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    x0[r][0] = x0[r][1] = x0[r][2] = T(0);
+                    const int q = val[r] ? slotof(r) - own0 : 0;
+                    rh[r][0] = val[r] ? ox[q] : T(0);
+                    rh[r][1] = val[r] ? oy[q] : T(0);
+                    rh[r][2] = val[r] ? oz[q] : T(0);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                x0[r][0] = x0[r][1] = x0[r][2] = T(0);
+                rh[r][0] = rh[r][1] = rh[r][2] = T(0);
+                if (val[r]) rhs_row(rowof(r), gb[r], slen(r), pid[r], rh[r], x0[r]);
             }
         }
 
@@ -767,7 +811,6 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                         oz[q] = nv[r][2];
                     }
             };
-            auto comp_bar = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(ncomp) : "memory"); };
             // end of a sweep: every row's global stores are issued and nobody
             // reads the band; the sync warp publishes the phase while the
             // compute warps move their new iterate into the own slots
