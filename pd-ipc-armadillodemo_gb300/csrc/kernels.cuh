@@ -36,13 +36,15 @@ struct Dev {
     V4<T>* Dh = nullptr;      // (float) Dir [ntot]
 
     // solver work
-    V4<T>* Y = nullptr;      // first half of a two-sweep step [nsim]
-    V4<T>* B = nullptr;      // odd Chebyshev iterates [nsim]
+    // Y, B, C: [64 ceil(nsim / 64)]; row order on the per-sweep path, slot
+    // order on the persistent one (three planes of floats on its band path)
+    V4<T>* Y = nullptr;      // first half of a two-sweep step
+    V4<T>* B = nullptr;      // odd Chebyshev iterates
     V4<T>* Aq = nullptr;     // rescaled curvature vector per vertex [nsim]
     V4<T>* Rhs = nullptr;    // right-hand side of the current local-global iteration [nsim]
     V4<TC>* Rhs0 = nullptr;  // inertial right-hand side (m/dt^2) y [nsim]; the predicted y itself in
                              // the correction (mixed) form
-    V4<T>* C = nullptr;      // even correction iterates of the correction form [nsim]
+    V4<T>* C = nullptr;      // even correction iterates of the correction form
     V4<T>* Grav = nullptr;   // (0, g m, 0) [nsim]
     V4<T>* PinRhs = nullptr; // k_pin * X_rest for pinned vertices, else 0 [nsim]
     T* InvMass = nullptr;    // [nsim]
@@ -94,6 +96,13 @@ struct Dev {
     int* sLen = nullptr;
     int* sCol = nullptr;
     T* sVal = nullptr;
+    // when rows share a few column-offset lists (a structured mesh has a few
+    // dozen per cloth): row i's columns are i + patOff[rowPat[i] * patW + k]
+    // (int16, padded with 0: the row itself, as sCol's padding), read through
+    // L1 instead of streaming sCol; null otherwise
+    int* rowPat = nullptr;
+    int16_t* patOff = nullptr;
+    int patW = 0;
 
     // collision topology
     int4* Faces = nullptr;   // (v0, v1, v2, -)
@@ -140,6 +149,22 @@ struct Dev {
     // once Gate->stop is set; null everywhere else (stage entry points)
     OuterGate* Gate = nullptr;
 };
+
+// The matrix N as the per-row kernels read it.
+template <typename T>
+struct Sell {
+    const int* off;
+    const int* len;
+    const int* col;
+    const T* val;
+    const int* rowPat;      // null: columns from col
+    const int16_t* patOff;
+    int patW;
+};
+template <typename T, typename TC>
+inline Sell<T> sell_of(const Dev<T, TC>& d) {
+    return Sell<T>{d.sOff, d.sLen, d.sCol, d.sVal, d.rowPat, d.patOff, d.patW};
+}
 
 // Row i's stencil in the SELL-32 copy: (slot of neighbour 0, neighbour count);
 // neighbour k sits at .x + 32 k.

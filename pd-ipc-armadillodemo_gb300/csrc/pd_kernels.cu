@@ -179,19 +179,18 @@ __global__ void k_local_aq(int nsim, const V4<T>* __restrict__ P, const int* __r
 }
 
 template <typename T>
-__device__ __forceinline__ void sell_row(int i, const int* __restrict__ sOff, const int* __restrict__ sLen,
-                                         const int* __restrict__ sCol, const T* __restrict__ sVal,
-                                         const V4<T>* __restrict__ X, T& s0, T& s1, T& s2) {
+__device__ __forceinline__ void sell_row(int i, const Sell<T> M, const V4<T>* __restrict__ X, T& s0, T& s1, T& s2) {
     const int sl = i >> 5, lane = i & 31;
-    const int base = __ldg(sOff + sl) + lane;
-    const int len = __ldg(sLen + sl);
+    const int base = __ldg(M.off + sl) + lane;
+    const int len = __ldg(M.len + sl);
+    const int16_t* po = M.rowPat ? M.patOff + (size_t)__ldg(M.rowPat + i) * M.patW : nullptr;
     s0 = T(0);
     s1 = T(0);
     s2 = T(0);
 #pragma unroll 4
     for (int k = 0; k < len; ++k) {
-        const int j = __ldg(sCol + base + 32 * k);
-        const T v = __ldg(sVal + base + 32 * k);
+        const int j = po ? i + (int)__ldg(po + k) : __ldg(M.col + base + 32 * k);
+        const T v = __ldg(M.val + base + 32 * k);
         const V4<T> xj = ld4(X, j);
         s0 += v * xj.x;
         s1 += v * xj.y;
@@ -208,8 +207,7 @@ __global__ void __launch_bounds__(kBlock) k_local_rhs_sweep(
     const T* __restrict__ tBendT,
     const T* __restrict__ Strain, const V4<T>* __restrict__ Aq, const V4<T>* __restrict__ Rhs0,
     const V4<T>* __restrict__ CollRhs, const V4<T>* __restrict__ PinRhs, const T* __restrict__ InvD,
-    const int* __restrict__ sOff, const int* __restrict__ sLen, const int* __restrict__ sCol,
-    const T* __restrict__ sVal, const int* __restrict__ vtPtr, const int* __restrict__ vtIdx,
+    const Sell<T> M, const int* __restrict__ vtPtr, const int* __restrict__ vtIdx,
     const V4<T>* __restrict__ TetOut, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
@@ -259,7 +257,7 @@ __global__ void __launch_bounds__(kBlock) k_local_rhs_sweep(
     r_2 += pn.z;
     Rhs[i] = V4<T>{r_0, r_1, r_2, T(0)};
     T s0, s1, s2;
-    sell_row(i, sOff, sLen, sCol, sVal, P, s0, s1, s2);
+    sell_row(i, M, P, s0, s1, s2);
     const T id = __ldg(InvD + i);
     const T om = T(1) - relax;
     Y[i] = V4<T>{om * x.x + relax * ((s0 + r_0) * id), om * x.y + relax * ((s1 + r_1) * id),
@@ -272,12 +270,11 @@ template <typename T, bool kCheby>
 __global__ void __launch_bounds__(kBlock) k_sweep(int nsim, T relax, T omega, const V4<T>* __restrict__ src,
                                                   const V4<T>* __restrict__ prev, V4<T>* __restrict__ out,
                                                   const V4<T>* __restrict__ Rhs, const T* __restrict__ InvD,
-                                                  const int* __restrict__ sOff, const int* __restrict__ sLen,
-                                                  const int* __restrict__ sCol, const T* __restrict__ sVal) {
+                                                  const Sell<T> M) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
     T s0, s1, s2;
-    sell_row(i, sOff, sLen, sCol, sVal, src, s0, s1, s2);
+    sell_row(i, M, src, s0, s1, s2);
     const V4<T> x = ld4(src, i);
     const V4<T> r = ld4(Rhs, i);
     const T id = __ldg(InvD + i);
@@ -317,8 +314,7 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
     const T* __restrict__ tRest, const T* __restrict__ tBend0, const T* __restrict__ tBendT,
     const T* __restrict__ Strain,
     const V4<T>* __restrict__ Aq, const T* __restrict__ InvD,
-    const int* __restrict__ sOff, const int* __restrict__ sLen, const int* __restrict__ sCol,
-    const T* __restrict__ sVal, const int* __restrict__ vtPtr, const int* __restrict__ vtIdx,
+    const Sell<T> M, const int* __restrict__ vtPtr, const int* __restrict__ vtIdx,
     const V4<T>* __restrict__ TetOut, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
@@ -389,12 +385,13 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
         }
     {   // sum_j N_ij (x_j - x_i)
         const int sl = i >> 5, lane = i & 31;
-        const int base = __ldg(sOff + sl) + lane;
-        const int len = __ldg(sLen + sl);
+        const int base = __ldg(M.off + sl) + lane;
+        const int len = __ldg(M.len + sl);
+        const int16_t* po = M.rowPat ? M.patOff + (size_t)__ldg(M.rowPat + i) * M.patW : nullptr;
 #pragma unroll 4
         for (int k = 0; k < len; ++k) {
-            const int j = __ldg(sCol + base + 32 * k);
-            const T v = __ldg(sVal + base + 32 * k);
+            const int j = po ? i + (int)__ldg(po + k) : __ldg(M.col + base + 32 * k);
+            const T v = __ldg(M.val + base + 32 * k);
             const V4<T> hj = ld4(Ph, j), lj = ld4(Pl, j);
             r0.add(v * diff_ff(hj.x, lj.x, h.x, l.x));
             r1.add(v * diff_ff(hj.y, lj.y, h.y, l.y));
@@ -417,12 +414,11 @@ __global__ void __launch_bounds__(kBlock) k_sweep_delta(int nsim, T relax, T ome
                                                         V4<S>* __restrict__ P, V4<T>* __restrict__ Ph,
                                                         V4<T>* __restrict__ Pl,
                                                         const V4<T>* __restrict__ Rhs, const T* __restrict__ InvD,
-                                                        const int* __restrict__ sOff, const int* __restrict__ sLen,
-                                                        const int* __restrict__ sCol, const T* __restrict__ sVal) {
+                                                        const Sell<T> M) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim) return;
     T s0, s1, s2;
-    sell_row(i, sOff, sLen, sCol, sVal, src, s0, s1, s2);
+    sell_row(i, M, src, s0, s1, s2);
     const V4<T> x = ld4(src, i);
     const V4<T> r = ld4(Rhs, i);
     const T id = __ldg(InvD + i);
@@ -611,8 +607,7 @@ void launch_local_residual(const Dev<T, TC>& d, T relax, cudaStream_t s) {
     if constexpr (kMirror<T, TC>) {
         k_local_residual<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(
             d.nsim, relax, d.P, d.Ph, d.Pl, d.Pold, d.Xrest, d.Rhs0, d.Dinert, d.CollDiag, d.CollRhs, d.PinFlag,
-            d.PinK, d.lPtr, d.tOff, d.tNbr, d.tRest, d.tBend0, d.tBendT, d.Strain, d.Aq, d.InvD, d.sOff, d.sLen, d.sCol,
-            d.sVal, d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs, d.Y);
+            d.PinK, d.lPtr, d.tOff, d.tNbr, d.tRest, d.tBend0, d.tBendT, d.Strain, d.Aq, d.InvD, sell_of(d), d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs, d.Y);
     }
 }
 template <typename T, typename TC>
@@ -622,7 +617,7 @@ void launch_sweep_delta(const Dev<T, TC>& d, int mode, const V4<T>* src, const V
 #define PDIPC_SWEEP_DELTA(M)                                                                                   \
     case M:                                                                                                    \
         k_sweep_delta<T, TC, M><<<nb, kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.P, d.Ph, d.Pl,  \
-                                                      d.Rhs, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal);          \
+                                                      d.Rhs, d.InvD, sell_of(d));          \
         break;
     switch (mode) {
         PDIPC_SWEEP_DELTA(0)
@@ -641,7 +636,7 @@ void launch_local_rhs_sweep(const Dev<T, TC>& d, T relax, cudaStream_t s) {
     if constexpr (std::is_same<T, TC>::value)
         k_local_rhs_sweep<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(
             d.nsim, relax, d.P, d.lPtr, d.tOff, d.tNbr, d.tRest, d.tBend0, d.tBendT, d.Strain, d.Aq, d.Rhs0, d.CollRhs,
-            d.PinRhs, d.InvD, d.sOff, d.sLen, d.sCol, d.sVal, d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs,
+            d.PinRhs, d.InvD, sell_of(d), d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs,
             d.Y);
 }
 template <typename T, typename TC>
@@ -649,10 +644,10 @@ void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T
                   cudaStream_t s) {
     if (prev)
         k_sweep<T, true><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.Rhs, d.InvD,
-                                                              d.sOff, d.sLen, d.sCol, d.sVal);
+                                                              sell_of(d));
     else
         k_sweep<T, false><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.Rhs,
-                                                               d.InvD, d.sOff, d.sLen, d.sCol, d.sVal);
+                                                               d.InvD, sell_of(d));
 }
 template <typename T, typename TC>
 void launch_direction(const Dev<T, TC>& d, cudaStream_t s) {

@@ -16,8 +16,9 @@
 //     CTAs it exchanges rows with) or, optionally, a grid barrier (a
 //     counter/generation pair);
 //   * band path (mixed precision, kMode 2): the iterate's band of the CTA stays
-//     in shared memory (own rows as planar floats, the halo as 16-byte vertices
-//     filled by cp.async.bulk copies on an mbarrier), the offset patterns come
+//     in shared memory as three planar float arrays (own rows written by the
+//     CTA's threads, the halo filled by cp.async.bulk copies from the planar
+//     global iterate on an mbarrier), the offset patterns come
 //     from parameter space, and one extra warp without rows publishes each
 //     sweep, polls the neighbours and issues the copies while the row warps sum
 //     their entries on own rows; other paths gather the iterate from global
@@ -284,14 +285,16 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     int16_t* spat = reinterpret_cast<int16_t*>(smem + ((size_t)E * sizeof(T) + 15) / 16 * 16);
     // (the band path reads the patterns from parameter space)
     const size_t patBytes = band ? 0 : ((size_t)a.patterns * a.patW * sizeof(int16_t) + 15) / 16 * 16;
-    // the band of the iterate: own rows as three planar arrays, the halo as
-    // 16-byte vertices (copied in bulk), then the copies' mbarrier
+    // the band of the iterate, slots [brange.x, brange.y), as three planar
+    // arrays of bandW floats (the own rows written by this CTA's threads after
+    // every sweep, the halo on each side copied in bulk from the planar global
+    // iterate), then the copies' mbarrier
     unsigned char* bandp = smem + ((size_t)E * sizeof(T) + 15) / 16 * 16 + patBytes;
-    T* ox = reinterpret_cast<T*>(bandp);
-    T* oy = ox + a.ownMax;
-    T* oz = oy + a.ownMax;
-    V4<T>* hv = reinterpret_cast<V4<T>*>(bandp + (3 * (size_t)a.ownMax * sizeof(T) + 15) / 16 * 16);
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(hv + a.haloMax);
+    const int bandW = a.ownMax + a.haloMax;  // a multiple of 64 (whole windows)
+    T* bx = reinterpret_cast<T*>(bandp);
+    T* by = bx + bandW;
+    T* bz = by + bandW;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(bandp + (3 * (size_t)bandW * sizeof(T) + 15) / 16 * 16);
     const int2 brange = band ? a.band[cta] : make_int2(0, 0);
     if (kSmem) {
         for (int q = threadIdx.x; q < E; q += blockDim.x) sval[q] = __ldg(a.sVal + eb + q);
@@ -358,12 +361,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     // two bulk copies once the neighbours have published it.  A CTA owns whole
     // 64-row windows, so a row j is one of its own exactly when slot_of(j) is.
     const int own0 = a.ctaSlice[cta] * 32, own1 = min(a.ctaSlice[cta + 1] * 32, a.nslot);
-    // The curvature and residual phases take the CTA's rows in row order:
-    // thread t of the nct compute threads takes rows own0 + t + k nct
-    // (k < R), which cover [own0, ownEnd).
-    const int nct = nrw * 32, ownEnd = min(a.ctaSlice[cta + 1] * 32, a.nsim);
     const int nlo = band ? own0 - brange.x : 0, nhi = band ? brange.y - own1 : 0;
-    const int hiBase = own1 - nlo;  // halo slot of column j >= own1: j - hiBase
     // The band path runs one extra warp, the last, with no rows: it publishes
     // each sweep, polls the neighbours' flags and issues the halo copies, so
     // the compute warps never wait on a flag.  Compute warps wait for a copy
@@ -401,9 +399,17 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                 // earlier reads of the halo area come before the async-proxy copy
                 asm volatile("fence.proxy.async.global;" ::: "memory");
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_arrive_expect(mbar, (unsigned)(nlo + nhi) * (unsigned)sizeof(V4<T>));
-                if (nlo > 0) bulk_load(hv, src + brange.x, (unsigned)nlo * (unsigned)sizeof(V4<T>), mbar);
-                if (nhi > 0) bulk_load(hv + nlo, src + own1, (unsigned)nhi * (unsigned)sizeof(V4<T>), mbar);
+                // per plane: slots [brange.x, own0) and [own1, brange.y), all
+                // offsets and sizes multiples of 64 floats (whole windows)
+                mbar_arrive_expect(mbar, (unsigned)(nlo + nhi) * 3u * (unsigned)sizeof(T));
+                const T* sp = reinterpret_cast<const T*>(src);
+                for (int pl = 0; pl < 3; ++pl) {
+                    const T* plane = sp + (size_t)pl * a.nslot;
+                    T* dst = bx + (size_t)pl * bandW;
+                    if (nlo > 0) bulk_load(dst, plane + brange.x, (unsigned)nlo * (unsigned)sizeof(T), mbar);
+                    if (nhi > 0)
+                        bulk_load(dst + (own1 - brange.x), plane + own1, (unsigned)nhi * (unsigned)sizeof(T), mbar);
+                }
             } else {
                 abort_s = 1;
                 mbar_arrive(mbar);
@@ -464,34 +470,44 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
         }
         pk[r] |= (b << 10) | (e << 20);
     }
-    auto own_sum = [&](int r, T& s0, T& s1, T& s2) {
-        const int k1 = pk[r] >> 20;
-#pragma unroll 8
-        for (int k = (pk[r] >> 10) & 1023; k < k1; ++k) {
-            T v;
-            int j;
-            entry(r, k, v, j);
-            const int q = slot_of(j) - own0;
-            s0 += v * ox[q];
-            s1 += v * oy[q];
-            s2 += v * oz[q];
-        }
-    };
-    auto halo_range = [&](int r, int k0, int k1, int base, T& s0, T& s1, T& s2) {
+    // entries [k0, k1) of owned row r against the band
+    auto band_sum = [&](int r, int k0, int k1, T& s0, T& s1, T& s2) {
 #pragma unroll 8
         for (int k = k0; k < k1; ++k) {
             T v;
             int j;
             entry(r, k, v, j);
-            const V4<T> h = hv[slot_of(j) - base];
-            s0 += v * h.x;
-            s1 += v * h.y;
-            s2 += v * h.z;
+            const int q = slot_of(j) - brange.x;
+            s0 += v * bx[q];
+            s1 += v * by[q];
+            s2 += v * bz[q];
         }
     };
+    auto own_sum = [&](int r, T& s0, T& s1, T& s2) { band_sum(r, (pk[r] >> 10) & 1023, pk[r] >> 20, s0, s1, s2); };
     auto halo_part = [&](int r, T& s0, T& s1, T& s2) {
-        halo_range(r, 0, (pk[r] >> 10) & 1023, brange.x, s0, s1, s2);
-        halo_range(r, pk[r] >> 20, slen(r), hiBase, s0, s1, s2);
+        band_sum(r, 0, (pk[r] >> 10) & 1023, s0, s1, s2);
+        band_sum(r, pk[r] >> 20, slen(r), s0, s1, s2);
+    };
+    // the iterates in global memory: three planes of nslot floats on the band
+    // path (the halo copies take one contiguous run per plane), 4-vectors
+    // elsewhere (gathered per entry)
+    auto st_it = [&](V4<T>* buf, int q, T x, T y, T z) {
+        if constexpr (band) {
+            T* p = reinterpret_cast<T*>(buf);
+            __stcg(p + q, x);
+            __stcg(p + a.nslot + q, y);
+            __stcg(p + 2 * (size_t)a.nslot + q, z);
+        } else {
+            stcg4(buf, q, x, y, z);
+        }
+    };
+    auto ld_it = [&](const V4<T>* buf, int q) -> V4<T> {
+        if constexpr (band) {
+            const T* p = reinterpret_cast<const T*>(buf);
+            return V4<T>{__ldcg(p + q), __ldcg(p + a.nslot + q), __ldcg(p + 2 * (size_t)a.nslot + q), T(0)};
+        } else {
+            return ldcg4(buf, q);
+        }
     };
     // sum_k N_ik src_k for the owned rows (paths without the band): matrix
     // from shared memory or L2, src gathered from global memory, in slot order
@@ -513,11 +529,11 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     };
 
     for (int lg = 0; lg < a.lg; ++lg) {
-        // ---- curvature vectors of the owned rows, in row order ----
+        // ---- curvature vectors of the owned rows ----
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const int i = own0 + (int)threadIdx.x + r * nct;
-            if ((int)threadIdx.x >= nct || i >= ownEnd) continue;
+            if (!val[r]) continue;
+            const int i = rowof(r);
             const int2 st = stencil_of(i, a.lPtr, a.tOff);
             T a0, a1, a2;
             if constexpr (kCorr) {
@@ -697,40 +713,11 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
             }
         };
         T x0[R][3], rh[R][3];
-        if constexpr (band) {
-            // Row order: the per-row state of consecutive threads' rows sits at
-            // consecutive addresses.  The residuals go to the own-row arrays
-            // (free until the first sweep of this iteration writes them) at the
-            // rows' slots, where every thread picks up those of its own rows.
-            if (!syncw) {
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const int i = own0 + (int)threadIdx.x + r * nct;
-                    if (i >= ownEnd) continue;
-                    const int q = slot_of(i), sl = q >> 5;
-                    T rr[3], xx[3];
-                    rhs_row(i, a.sliceEntry[sl] + (q & 31), a.sliceLen[sl], a.rowPattern[i] * a.patW, rr, xx);
-                    ox[q - own0] = rr[0];
-                    oy[q - own0] = rr[1];
-                    oz[q - own0] = rr[2];
-                }
-                comp_bar();
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    x0[r][0] = x0[r][1] = x0[r][2] = T(0);
-                    const int q = val[r] ? slotof(r) - own0 : 0;
-                    rh[r][0] = val[r] ? ox[q] : T(0);
-                    rh[r][1] = val[r] ? oy[q] : T(0);
-                    rh[r][2] = val[r] ? oz[q] : T(0);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                x0[r][0] = x0[r][1] = x0[r][2] = T(0);
-                rh[r][0] = rh[r][1] = rh[r][2] = T(0);
-                if (val[r]) rhs_row(rowof(r), gb[r], slen(r), pid[r], rh[r], x0[r]);
-            }
+        for (int r = 0; r < R; ++r) {
+            x0[r][0] = x0[r][1] = x0[r][2] = T(0);
+            rh[r][0] = rh[r][1] = rh[r][2] = T(0);
+            if (val[r]) rhs_row(rowof(r), gb[r], slen(r), pid[r], rh[r], x0[r]);
         }
 
         // ---- Chebyshev-accelerated R2 iteration as two J sweeps per step ----
@@ -741,7 +728,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
             y[0] = om1 * c[0] + w * ((s0 + rh[r][0]) * id[r]);
             y[1] = om1 * c[1] + w * ((s1 + rh[r][1]) * id[r]);
             y[2] = om1 * c[2] + w * ((s2 + rh[r][2]) * id[r]);
-            if (val[r]) stcg4(a.GY, slotof(r), y[0], y[1], y[2]);
+            if (val[r]) st_it(a.GY, slotof(r), y[0], y[1], y[2]);
         };
         // second sweep of step it: S(y), Chebyshev-combined with the previous
         // second-sweep iterate p except for the first step; the last one
@@ -773,7 +760,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     stcg4(a.P, rowof(r), n[0], n[1], n[2]);
                 }
             } else {
-                stcg4(xout, slotof(r), n[0], n[1], n[2]);
+                st_it(xout, slotof(r), n[0], n[1], n[2]);
             }
         };
         const int nsteps = a.cheby;
@@ -796,19 +783,19 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                 }
             };
             auto own_slot = [&](int r, T (&c)[3]) {
-                const int q = val[r] ? slotof(r) - own0 : 0;
-                c[0] = ox[q];
-                c[1] = oy[q];
-                c[2] = oz[q];
+                const int q = val[r] ? slotof(r) - brange.x : 0;
+                c[0] = bx[q];
+                c[1] = by[q];
+                c[2] = bz[q];
             };
             auto write_own = [&]() {
 #pragma unroll
                 for (int r = 0; r < R; ++r)
                     if (val[r]) {
-                        const int q = slotof(r) - own0;
-                        ox[q] = nv[r][0];
-                        oy[q] = nv[r][1];
-                        oz[q] = nv[r][2];
+                        const int q = slotof(r) - brange.x;
+                        bx[q] = nv[r][0];
+                        by[q] = nv[r][1];
+                        bz[q] = nv[r][2];
                     }
             };
             // end of a sweep: every row's global stores are issued and nobody
@@ -846,7 +833,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                 const T zero[3] = {T(0), T(0), T(0)};
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    if (val[r]) stcg4(a.GX2, slotof(r), T(0), T(0), T(0));
+                    if (val[r]) st_it(a.GX2, slotof(r), T(0), T(0), T(0));
                     finish_y(r, T(0), T(0), T(0), zero, nv[r]);
                 }
             }
@@ -863,7 +850,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     for (int r = 0; r < R; ++r) {
                         p[r][0] = p[r][1] = p[r][2] = T(0);
                         if (it > 0 && val[r]) {
-                            const V4<T> g = ldcg4(xb, slotof(r));
+                            const V4<T> g = ld_it(xb, slotof(r));
                             p[r][0] = g.x;
                             p[r][1] = g.y;
                             p[r][2] = g.z;

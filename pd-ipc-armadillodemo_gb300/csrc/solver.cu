@@ -295,6 +295,35 @@ public:
         PD_CK(up(d.sLen, slen));
         PD_CK(up(d.sCol, scol));
         PD_CK(up(d.sVal, sval));
+        {   // column-offset patterns for the per-row kernels, kept only when
+            // rows share them (a table at most an eighth of the rows' count)
+            int patW = 0;
+            for (int w : slen) patW = std::max(patW, w);
+            std::map<std::vector<int16_t>, int> pats;
+            std::vector<int> rp(std::max(ns, 1), 0);
+            bool share = patW > 0;
+            std::vector<int16_t> o(patW);
+            for (int i = 0; i < ns && share; ++i) {
+                std::fill(o.begin(), o.end(), (int16_t)0);
+                for (int e = H.nPtr[i]; e < H.nPtr[i + 1]; ++e) {
+                    const int off = H.nCol[e] - i;
+                    if (off < -32768 || off > 32767) {
+                        share = false;
+                        break;
+                    }
+                    o[e - H.nPtr[i]] = (int16_t)off;
+                }
+                rp[i] = pats.emplace(o, (int)pats.size()).first->second;
+                if ((int64_t)pats.size() * 8 > (int64_t)ns + 64) share = false;
+            }
+            if (share) {
+                std::vector<int16_t> tab(pats.size() * (size_t)patW);
+                for (auto& kv : pats) std::copy(kv.first.begin(), kv.first.end(), tab.begin() + (size_t)kv.second * patW);
+                PD_CK(up(d.rowPat, rp));
+                PD_CK(up(d.patOff, tab));
+                d.patW = patW;
+            }
+        }
 
         // ---- collision topology ----
         std::vector<int4> faces(d.nface);
@@ -1435,7 +1464,7 @@ private:
         const size_t limit = (size_t)smem_optin - 1024;
         // Every configuration that fits: rows per thread R (slices per warp),
         // the band of the iterate in shared memory (correction form: own rows
-        // planar, halo as 16-byte vertices, the copies' mbarrier, one more warp
+        // and halo as three planar float arrays, the copies' mbarrier, one more warp
         // without rows for the neighbour flags and the copies), L1 or L2-only
         // gathers, neighbour waits or grid barriers.  The direct form keeps the
         // reference's summation order (gathers, no band).  The default is the
@@ -1471,7 +1500,7 @@ private:
                     const int hx = col_ranges(spc, rg);
                     const int om = spc * kSlice;
                     const size_t smb =
-                        cta_smem(spc, smem_mat, a16(3 * (size_t)om * sizeof(T)) + (size_t)hx * sizeof(V4<T>) + 16);
+                        cta_smem(spc, smem_mat, a16(3 * (size_t)(om + hx) * sizeof(T)) + 16);
                     if (smb <= limit)
                         vs.push_back(Cand{PlanChoice{R, true, true, true}, smem_mat, spc, ctas, (W + 1) * 32, smb, om,
                                           hx, std::move(rg)});
