@@ -104,6 +104,28 @@ def aggregate_steps_per_s(world_size: int, steps: int, max_ms: float) -> float:
     return world_size * steps / (max_ms * 1e-3)
 
 
+def cloth_energy(sc, X, V) -> float:
+    """Energy of the simulated cloths in a state (J): kinetic (lumped masses,
+    density x one third of the adjacent triangles' rest area), gravitational
+    potential along y, and the stretch energy 1/2 k_stretch (l - l0)^2 over the
+    mesh edges (rest lengths from the cloth's initial positions)."""
+    e, off = 0.0, 0
+    for c in sc.cloths:
+        n = c.X.shape[0]
+        x, v = X[off:off + n], V[off:off + n]
+        a = np.linalg.norm(np.cross(c.X[c.F[:, 1]] - c.X[c.F[:, 0]], c.X[c.F[:, 2]] - c.X[c.F[:, 0]]), axis=1) / 2
+        m = np.zeros(n)
+        for k in range(3):
+            np.add.at(m, c.F[:, k], c.density * a / 3.0)
+        ed = np.unique(np.sort(np.concatenate([c.F[:, [0, 1]], c.F[:, [1, 2]], c.F[:, [2, 0]]]), axis=1), axis=0)
+        l0 = np.linalg.norm(c.X[ed[:, 0]] - c.X[ed[:, 1]], axis=1)
+        ln = np.linalg.norm(x[ed[:, 0]] - x[ed[:, 1]], axis=1)
+        e += 0.5 * float(np.sum(m[:, None] * v * v)) - sc.gravity * float(np.sum(m * x[:, 1]))
+        e += 0.5 * c.k_stretch * float(np.sum((ln - l0) ** 2))
+        off += n
+    return e
+
+
 def nvtx_push(name: str):
     """Open an NVTX push/pop range on this thread (`ncu --nvtx --nvtx-include
     "<name>/"` then profiles only launches inside it); returns its pop."""
@@ -330,6 +352,7 @@ def run_ours(args):
     e2e_max = max_over_ranks(dist, e2e_wall, dev)
     st_end = sim.stats()
     x_end = out.copy()
+    v_end = sim.velocities().copy()
 
     # the contact phase of the same run: advance untimed to step
     # `contact_start`, then time `contact_steps` steps the same way
@@ -384,10 +407,19 @@ def run_ours(args):
             if probe:
                 one_step.append((k, float(np.abs(x_probe - ref.positions()).max())))
         err = float(np.abs(x_end - ref.positions()).max()) if k64 == args.steps else None
+        energy = None
+        if k64 == args.steps and not args.scene:
+            e_mine = cloth_energy(sc, x_end[:sc.n_sim], v_end)
+            e_ref = cloth_energy(sc, ref.positions()[:sc.n_sim], ref.velocities())
+            energy = {"this_mode_J": e_mine, "fp64_J": e_ref, "abs_err_J": abs(e_mine - e_ref),
+                      "rel_err": abs(e_mine - e_ref) / max(abs(e_ref), 1e-300),
+                      "definition": "kinetic + gravitational potential + 1/2 k_stretch (l - l0)^2 over mesh edges "
+                                    "of the simulated cloths after the timed steps"}
         fp64 = {"value": round(k64 / (ms64 * 1e-3), 4), "unit": UNIT, "steps": k64,
                 "ms_per_step": round(ms64 / k64, 3),
                 "outer_iterations_per_step": {"mean": float(np.mean(outers64)), "max": int(max(outers64))},
                 "max_position_err_m_after_steps": err,
+                "energy_after_steps": energy,
                 "one_step_err_m_from_fp64_state": {"max": max(e for _, e in one_step),
                                                    "at_steps": [k for k, _ in one_step],
                                                    "values": [float("%.3g" % e) for _, e in one_step]},
