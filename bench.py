@@ -305,7 +305,8 @@ def run_ours(args):
         sc = _sc.instance_slice(sc, int(first[rank]), int(first[rank + 1]))
     # the launch configuration is chosen by the library's autotuner at
     # initialize (untimed), unless --no-autotune
-    sim = pdipc.Simulator(sc, args.precision, device=local, autotune=0 if args.no_autotune else 1)
+    sim = pdipc.Simulator(sc, args.precision, device=local, autotune=0 if args.no_autotune else 1,
+                          instance_stop=instance_stop(args))
     tuning = sim.tuning()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -389,7 +390,7 @@ def run_ours(args):
     fp64 = None
     if args.precision != "fp64" and args.fp64_steps > 0:
         k64 = min(args.fp64_steps, args.steps)
-        ref = pdipc.Simulator(sc, "fp64", device=local)
+        ref = pdipc.Simulator(sc, "fp64", device=local, instance_stop=instance_stop(args))
         ref.step(args.warmup)
         ref.reset()
         ms64, outers64, one_step = 0.0, [], []
@@ -436,7 +437,7 @@ def run_ours(args):
     fp32 = None
     if args.precision != "fp32" and args.fp32_steps > 0:
         k32 = min(args.fp32_steps, args.steps)
-        g32 = pdipc.Simulator(sc, "fp32", device=local)
+        g32 = pdipc.Simulator(sc, "fp32", device=local, instance_stop=instance_stop(args))
         g32.step(args.warmup)
         g32.reset()
         ms32, outers32 = 0.0, []
@@ -550,9 +551,19 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def instance_stop(args) -> int:
+    """1 when the run uses per-instance stopping (each independent instance of
+    a batch takes the reference's stopping rule on its own vertices)."""
+    if args.instance_stop == "auto":
+        return int(args.config == "c2" and not args.scene)
+    return int(args.instance_stop == "on")
+
+
 def run_config(sc, args, ws: int) -> dict:
     """The `config` object, identical in both arms for the same arguments."""
     return {"workload": workload_desc(sc, args.precision), "steps_timed": f"0..{args.steps - 1}",
+            "stopping_rule": ("per instance (each model's own |dx|^2 < 1e-5)" if instance_stop(args)
+                              else "the reference's: one test over the scene's vertices (|dx|^2 < 1e-5)"),
             "parallelism": ((f"instance table partitioned over {ws} ranks by cumulative vertex count"
                              if args.config == "c2" and not args.scene else "replicas only")
                             if ws > 1 else "single GPU"),
@@ -644,6 +655,9 @@ def main(argv=None):
     ap.add_argument("--contact-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="run the built-in launch configuration")
+    ap.add_argument("--instance-stop", choices=["auto", "on", "off"], default="auto",
+                    help="per-instance stopping rule (pdipc_params.instance_stop); auto: on for the batch of "
+                         "independent drops (config c2), off otherwise")
     ap.add_argument("--cpu-steps", type=int, default=3, help="whole steps in the GPU arm's cpu_baseline sample")
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--ref-budget-s", type=float, default=300.0,

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PDIPC_ABI_VERSION 7
+#define PDIPC_ABI_VERSION 8
 
 typedef struct pdipc_ctx pdipc_ctx;
 
@@ -101,7 +101,13 @@ typedef struct {
                                 can only lower a candidate's time of impact; 2: the FP64 cubic alone, the
                                 exact first-contact time of every candidate (the step then stops at
                                 toi_scale of the first contact instead of the additive CCD's gap) */
-    int reserved[3];
+    int instance_stop;       /* 0: the reference's stopping rule, one test over all vertices of the scene
+                                (cpp:1776); 1: for batches of independent instances, the same rule per
+                                simulated model: each model stops on its own |dx|^2 < outer_tol and clamps
+                                its step by its own time of impact, and the step ends when every model has
+                                stopped (or at max_outer).  A model that has stopped skips its sweeps.  Models
+                                that touch one another should keep 0.  Runs the per-sweep PD solve. */
+    int reserved[2];
 } pdipc_params;
 
 /* Per-context statistics of the most recent pdipc_step call. */
@@ -138,6 +144,11 @@ typedef struct {
                                     candidates, global minimum) of the last call, CUDA events per outer
                                     iteration */
     double contact_ms;           /* device time of the contact-constraint passes of the last call */
+    int32_t instances;           /* simulated models (the instances of params.instance_stop) */
+    int32_t reserved_i;
+    int64_t instance_outer_iters; /* sum over the steps of the last call and over the models of the outer
+                                     iterations each model ran (params.instance_stop; else instances x
+                                     total_outer_iters) */
 } pdipc_stats;
 
 /* Launch configuration a context runs with, and how it was chosen (no

@@ -751,6 +751,39 @@ __global__ void k_toi_finalize(TC* __restrict__ toi_min, TC* __restrict__ toi, d
     *toi_min = TC(1);
 }
 
+// Per-instance stopping: each candidate whose time of impact is below 1
+// lowers the running minimum of every instance among its vertices (static
+// vertices belong to none); then each instance's clamp.
+template <typename TC>
+__global__ void k_inst_toi(int64_t n, const int4* __restrict__ cand, const TC* __restrict__ per,
+                           const int* __restrict__ VInst, TC* __restrict__ inst_min,
+                           const OuterGate* __restrict__ gate) {
+    if (outer_stopped(gate)) return;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const TC v = per[t];
+        if (!(v < TC(1))) continue;
+        const int4 c = cand[t];
+        const int k[4] = {VInst[c.x], VInst[c.y], VInst[c.z], VInst[c.w]};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            bool seen = k[j] < 0;
+#pragma unroll
+            for (int q = 0; q < j; ++q) seen = seen || k[q] == k[j];
+            if (!seen) atomic_min_nonneg(inst_min + k[j], v);
+        }
+    }
+}
+template <typename TC>
+__global__ void k_inst_toi_finalize(int ninst, TC* __restrict__ inst_min, TC* __restrict__ inst_toi, double scale,
+                                    const OuterGate* __restrict__ gate) {
+    if (outer_stopped(gate)) return;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ninst; k += gridDim.x * blockDim.x) {
+        const TC m = inst_min[k];
+        inst_toi[k] = (m < TC(1)) ? (TC)((double)m * scale) : TC(1);
+        inst_min[k] = TC(1);
+    }
+}
+
 // the contact pass's accumulators start from zero
 template <typename T>
 __global__ void k_contact_clear(int n, T* __restrict__ diag, V4<T>* __restrict__ rhs,
@@ -1057,6 +1090,18 @@ void launch_toi(const Dev<T, TC>& d, Pos<T, TC> X0, Pos<T, TC> X1, const SolverC
     }
 }
 template <typename T, typename TC>
+void launch_inst_toi(const Dev<T, TC>& d, const TC* per_pt, const TC* per_ee, const SolverConsts& c, cudaStream_t s) {
+    if (d.ninst == 0) return;
+    if (d.nPT > 0 && per_pt)
+        k_inst_toi<TC><<<grid_cap(d.nPT, kBlock, c.cand_grid), kBlock, 0, s>>>(d.nPT, d.PT, per_pt, d.VInst,
+                                                                             d.InstToiMin, d.Gate);
+    if (d.nEE > 0 && per_ee)
+        k_inst_toi<TC><<<grid_cap(d.nEE, kBlock, c.cand_grid), kBlock, 0, s>>>(d.nEE, d.EE, per_ee, d.VInst,
+                                                                             d.InstToiMin, d.Gate);
+    k_inst_toi_finalize<TC><<<blocks_for(d.ninst), kBlock, 0, s>>>(d.ninst, d.InstToiMin, d.InstToi, c.toi_scale,
+                                                                   d.Gate);
+}
+template <typename T, typename TC>
 void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s) {
     k_toi_finalize<TC><<<1, 1, 0, s>>>(d.ToiMin, d.Toi, c.toi_scale, d.Gate);
 }
@@ -1122,6 +1167,8 @@ cudaError_t toi_scratch(ToiScratch* out) {
     template void launch_toi<T, TC>(const Dev<T, TC>&, Pos<T, TC>, Pos<T, TC>, const SolverConsts&, TC*,      \
                                     TC*, cudaStream_t);                                                       \
     template void launch_toi_finalize<T, TC>(const Dev<T, TC>&, const SolverConsts&, cudaStream_t);           \
+    template void launch_inst_toi<T, TC>(const Dev<T, TC>&, const TC*, const TC*, const SolverConsts&,        \
+                                         cudaStream_t);                                                      \
     template void launch_contact<T, TC>(const Dev<T, TC>&, Pos<T, TC>, const SolverConsts&, cudaStream_t);
 
 PDIPC_INST_COLL(float, float)

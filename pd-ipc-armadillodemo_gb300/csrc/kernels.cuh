@@ -148,7 +148,32 @@ struct Dev {
     // CCD, clamp, contact, copy into Pold, persistent solve) return at entry
     // once Gate->stop is set; null everywhere else (stage entry points)
     OuterGate* Gate = nullptr;
+
+    // per-instance stopping (pdipc_params.instance_stop; null otherwise): the
+    // instance (simulated model) of every vertex (-1: static), the instances'
+    // vertex ranges, and per instance its stop flag (cleared outside steps),
+    // residual, running time-of-impact minimum, clamp and outer-iteration count
+    int ninst = 0;
+    int* VInst = nullptr;          // [ntot]
+    int* InstBeg = nullptr;        // [ninst + 1]
+    unsigned* InstStop = nullptr;  // [ninst]
+    double* InstResid = nullptr;   // [ninst]
+    TC* InstToiMin = nullptr;      // [ninst]
+    TC* InstToi = nullptr;         // [ninst]
+    int* InstIters = nullptr;      // [ninst]
 };
+
+// Rows the per-row PD kernels skip: those of instances that have stopped
+// (pdipc_params.instance_stop); stop is null when nothing is skipped.
+struct RowSkip {
+    const int* inst;
+    const unsigned* stop;
+    __device__ __forceinline__ bool operator()(int i) const { return stop && __ldg(stop + __ldg(inst + i)); }
+};
+template <typename T, typename TC>
+inline RowSkip skip_of(const Dev<T, TC>& d) {
+    return RowSkip{d.VInst, d.InstStop};
+}
 
 // The matrix N as the per-row kernels read it.
 template <typename T>
@@ -232,6 +257,14 @@ void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s);
 // outer iteration `outer`, stop when test && outer > 0 && Resid < tol
 template <typename T, typename TC>
 void launch_outer_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cudaStream_t s);
+// per-instance stopping: |dir|^2 of every instance into InstResid; after the
+// contact pass, each running instance's test (its iteration count, then
+// stop when test && outer > 0 && InstResid < tol), and the step's record in
+// d.Gate (stop once every instance has stopped; resid the sum)
+template <typename T, typename TC>
+void launch_inst_resid(const Dev<T, TC>& d, cudaStream_t s);
+template <typename T, typename TC>
+void launch_inst_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cudaStream_t s);
 // correction form: write the float-float mirror (hi, lo; lo may be null) of n
 // positions X, after a host write of X
 template <typename T, typename TC>
@@ -267,6 +300,11 @@ void launch_toi(const Dev<T, TC>& d, Pos<T, TC> X0, Pos<T, TC> X1, const SolverC
                 TC* per_ee, cudaStream_t s);
 template <typename T, typename TC>
 void launch_toi_finalize(const Dev<T, TC>& d, const SolverConsts& c, cudaStream_t s);
+// per-instance stopping: the per-candidate times of impact (per_pt, per_ee of
+// launch_toi) reduced into every instance a candidate's vertices belong to,
+// then each instance's clamp InstToi (scaled when below 1; minima reset)
+template <typename T, typename TC>
+void launch_inst_toi(const Dev<T, TC>& d, const TC* per_pt, const TC* per_ee, const SolverConsts& c, cudaStream_t s);
 template <typename T, typename TC>
 void launch_contact(const Dev<T, TC>& d, Pos<T, TC> X, const SolverConsts& c, cudaStream_t s);
 

@@ -99,10 +99,11 @@ __global__ void k_diag(int nsim, const T* __restrict__ De, const T* __restrict__
 template <typename T, typename S>
 __global__ void k_tet_project(int ntet, const int4* __restrict__ Tets, const T* __restrict__ Idm,
                               const T* __restrict__ W, const V4<S>* __restrict__ P, const V4<T>* __restrict__ Ph,
-                              const V4<T>* __restrict__ Pl, V4<T>* __restrict__ Out) {
+                              const V4<T>* __restrict__ Pl, V4<T>* __restrict__ Out, const RowSkip skip) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ntet) return;
     const int4 q = Tets[e];
+    if (skip(q.x)) return;  // an element's vertices belong to one model
     // a cloth triangle's strain element has no fourth vertex (-1): its first
     // vertex stands in, so the third edge is zero and unused
     const bool tri = q.w < 0;
@@ -153,9 +154,9 @@ template <typename T>
 __global__ void k_local_aq(int nsim, const V4<T>* __restrict__ P, const int* __restrict__ lPtr,
                            const int* __restrict__ tOff, const int* __restrict__ tNbr, const T* __restrict__ tLbo,
                            const T* __restrict__ tLbo0, const T* __restrict__ CurvNorm,
-                           V4<T>* __restrict__ Aq) {
+                           V4<T>* __restrict__ Aq, const RowSkip skip) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nsim) return;
+    if (i >= nsim || skip(i)) return;
     const int2 st = stencil_of(i, lPtr, tOff);
     const V4<T> x = ld4(P, i);
     const T l0 = __ldg(tLbo0 + i);
@@ -208,9 +209,9 @@ __global__ void __launch_bounds__(kBlock) k_local_rhs_sweep(
     const T* __restrict__ Strain, const V4<T>* __restrict__ Aq, const V4<T>* __restrict__ Rhs0,
     const V4<T>* __restrict__ CollRhs, const V4<T>* __restrict__ PinRhs, const T* __restrict__ InvD,
     const Sell<T> M, const int* __restrict__ vtPtr, const int* __restrict__ vtIdx,
-    const V4<T>* __restrict__ TetOut, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
+    const V4<T>* __restrict__ TetOut, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y, const RowSkip skip) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nsim) return;
+    if (i >= nsim || skip(i)) return;
     const int2 st = stencil_of(i, lPtr, tOff);
     const V4<T> x = ld4(P, i);
     const T strain = __ldg(Strain + i);
@@ -270,9 +271,9 @@ template <typename T, bool kCheby>
 __global__ void __launch_bounds__(kBlock) k_sweep(int nsim, T relax, T omega, const V4<T>* __restrict__ src,
                                                   const V4<T>* __restrict__ prev, V4<T>* __restrict__ out,
                                                   const V4<T>* __restrict__ Rhs, const T* __restrict__ InvD,
-                                                  const Sell<T> M) {
+                                                  const Sell<T> M, const RowSkip skip) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nsim) return;
+    if (i >= nsim || skip(i)) return;
     T s0, s1, s2;
     sell_row(i, M, src, s0, s1, s2);
     const V4<T> x = ld4(src, i);
@@ -315,9 +316,9 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
     const T* __restrict__ Strain,
     const V4<T>* __restrict__ Aq, const T* __restrict__ InvD,
     const Sell<T> M, const int* __restrict__ vtPtr, const int* __restrict__ vtIdx,
-    const V4<T>* __restrict__ TetOut, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y) {
+    const V4<T>* __restrict__ TetOut, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y, const RowSkip skip) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nsim) return;
+    if (i >= nsim || skip(i)) return;
     const V4<S> x = ld4(P, i);
     Sum2 r0, r1, r2;
     {   // inertia
@@ -414,9 +415,9 @@ __global__ void __launch_bounds__(kBlock) k_sweep_delta(int nsim, T relax, T ome
                                                         V4<S>* __restrict__ P, V4<T>* __restrict__ Ph,
                                                         V4<T>* __restrict__ Pl,
                                                         const V4<T>* __restrict__ Rhs, const T* __restrict__ InvD,
-                                                        const Sell<T> M) {
+                                                        const Sell<T> M, const RowSkip skip) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nsim) return;
+    if (i >= nsim || skip(i)) return;
     T s0, s1, s2;
     sell_row(i, M, src, s0, s1, s2);
     const V4<T> x = ld4(src, i);
@@ -455,10 +456,10 @@ __global__ void k_local_aq_rel(int nsim, const V4<float>* __restrict__ Ph, const
                                const int* __restrict__ lPtr, const int* __restrict__ tOff,
                                const int* __restrict__ tNbr, const float* __restrict__ tLbo,
                                const float* __restrict__ CurvNorm,
-                               V4<float>* __restrict__ Aq) {
+                               V4<float>* __restrict__ Aq, const RowSkip skip) {
     using T = float;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nsim) return;
+    if (i >= nsim || skip(i)) return;
     const int2 st = stencil_of(i, lPtr, tOff);
     const V4<T> h = ld4(Ph, i), l = ld4(Pl, i);
     T a0 = T(0), a1 = T(0), a2 = T(0);
@@ -508,10 +509,11 @@ __global__ void k_direction(int nsim, const V4<S>* __restrict__ P, const V4<S>* 
 template <typename T, typename S>  // S: the state scalar
 __global__ void k_clamp(int nsim, const V4<S>* __restrict__ Pold, const V4<S>* __restrict__ Dir,
                         const S* __restrict__ Toi, V4<S>* __restrict__ P, V4<T>* __restrict__ Ph,
-                        V4<T>* __restrict__ Pl, const OuterGate* __restrict__ gate) {
+                        V4<T>* __restrict__ Pl, const OuterGate* __restrict__ gate, const int* __restrict__ VInst,
+                        const S* __restrict__ InstToi) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsim || outer_stopped(gate)) return;
-    const S t = *Toi;
+    const S t = InstToi ? InstToi[VInst[i]] : *Toi;  // per-instance stopping: the instance's own clamp
     const V4<S> a = Pold[i], d = Dir[i];
     const S x = a.x + t * d.x, y = a.y + t * d.y, z = a.z + t * d.z;
     P[i] = V4<S>{x, y, z, S(0)};
@@ -558,6 +560,68 @@ __global__ void k_outer_gate(OuterGate* __restrict__ g, const double* __restrict
     if (test && outer > 0 && r < tol) g->stop = 1u;
 }
 
+// Per-instance stopping: |dir|^2 of every instance, one block per instance
+// over its vertex range, in a fixed order.
+template <typename S>
+__global__ void k_inst_resid(const int* __restrict__ beg, const V4<S>* __restrict__ Dir, double* __restrict__ resid,
+                             const OuterGate* __restrict__ gate) {
+    if (outer_stopped(gate)) return;
+    const int k = blockIdx.x;
+    double acc = 0.0;
+    for (int i = beg[k] + (int)threadIdx.x; i < beg[k + 1]; i += blockDim.x) {
+        const V4<S> d = Dir[i];
+        acc += (double)d.x * (double)d.x + (double)d.y * (double)d.y + (double)d.z * (double)d.z;
+    }
+    __shared__ double red[kBlock / 32];
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        resid[k] = t;
+    }
+}
+
+// Per-instance stopping test after outer iteration `outer` (PdIpcSimulator.cpp:
+// 1776 applied to each instance): a running instance counts the iteration and
+// stops when test && outer > 0 && its |dir|^2 < tol.  The step's record: the
+// loop stops once every instance has; resid the sum over the instances that ran.
+template <typename TC>
+__global__ void k_inst_gate(int ninst, unsigned* __restrict__ stop, int* __restrict__ iters,
+                            const double* __restrict__ resid, OuterGate* __restrict__ g, const TC* __restrict__ toi,
+                            const unsigned long long* __restrict__ active, int outer, double tol, int test) {
+    if (g->stop) return;
+    __shared__ double rsum[kBlock];
+    __shared__ int running[kBlock];
+    double r = 0.0;
+    int run = 0;
+    for (int k = threadIdx.x; k < ninst; k += blockDim.x) {
+        if (stop[k]) continue;
+        const double rk = resid[k];
+        r += rk;
+        iters[k] = outer + 1;
+        if (test && outer > 0 && rk < tol) stop[k] = 1u;
+        else ++run;
+    }
+    rsum[threadIdx.x] = r;
+    running[threadIdx.x] = run;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        int n = 0;
+        for (int w = 0; w < (int)blockDim.x; ++w) {
+            t += rsum[w];
+            n += running[w];
+        }
+        g->resid = t;
+        g->iters = outer + 1;
+        g->toi = (double)*toi;
+        g->active = *active;
+        if (n == 0) g->stop = 1u;
+    }
+}
+
 template <typename T>
 __global__ void k_velocity(int nsim, T invt, const V4<T>* __restrict__ P, const V4<T>* __restrict__ X0,
                            V4<T>* __restrict__ Vel, unsigned int* __restrict__ err) {
@@ -591,23 +655,24 @@ template <typename T, typename TC>
 void launch_tet_project(const Dev<T, TC>& d, cudaStream_t s) {
     if (d.ntet == 0) return;
     k_tet_project<T, TC><<<blocks_for(d.ntet, 128), 128, 0, s>>>(d.ntet, d.Tets, d.TetIdm, d.TetW, d.P, d.Ph, d.Pl,
-                                                                d.TetOut);
+                                                                d.TetOut, skip_of(d));
 }
 template <typename T, typename TC>
 void launch_local_aq(const Dev<T, TC>& d, cudaStream_t s) {
     if constexpr (correction_form<T, TC>())
         k_local_aq_rel<<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Ph, d.Pl, d.lPtr, d.tOff, d.tNbr, d.tLbo,
-                                                              d.CurvNorm, d.Aq);
+                                                              d.CurvNorm, d.Aq, skip_of(d));
     else
         k_local_aq<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.lPtr, d.tOff, d.tNbr, d.tLbo, d.tLbo0,
-                                                            d.CurvNorm, d.Aq);
+                                                            d.CurvNorm, d.Aq, skip_of(d));
 }
 template <typename T, typename TC>
 void launch_local_residual(const Dev<T, TC>& d, T relax, cudaStream_t s) {
     if constexpr (kMirror<T, TC>) {
         k_local_residual<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(
             d.nsim, relax, d.P, d.Ph, d.Pl, d.Pold, d.Xrest, d.Rhs0, d.Dinert, d.CollDiag, d.CollRhs, d.PinFlag,
-            d.PinK, d.lPtr, d.tOff, d.tNbr, d.tRest, d.tBend0, d.tBendT, d.Strain, d.Aq, d.InvD, sell_of(d), d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs, d.Y);
+            d.PinK, d.lPtr, d.tOff, d.tNbr, d.tRest, d.tBend0, d.tBendT, d.Strain, d.Aq, d.InvD, sell_of(d), d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs, d.Y,
+            skip_of(d));
     }
 }
 template <typename T, typename TC>
@@ -617,7 +682,7 @@ void launch_sweep_delta(const Dev<T, TC>& d, int mode, const V4<T>* src, const V
 #define PDIPC_SWEEP_DELTA(M)                                                                                   \
     case M:                                                                                                    \
         k_sweep_delta<T, TC, M><<<nb, kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.P, d.Ph, d.Pl,  \
-                                                      d.Rhs, d.InvD, sell_of(d));          \
+                                                      d.Rhs, d.InvD, sell_of(d), skip_of(d));          \
         break;
     switch (mode) {
         PDIPC_SWEEP_DELTA(0)
@@ -637,17 +702,17 @@ void launch_local_rhs_sweep(const Dev<T, TC>& d, T relax, cudaStream_t s) {
         k_local_rhs_sweep<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(
             d.nsim, relax, d.P, d.lPtr, d.tOff, d.tNbr, d.tRest, d.tBend0, d.tBendT, d.Strain, d.Aq, d.Rhs0, d.CollRhs,
             d.PinRhs, d.InvD, sell_of(d), d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs,
-            d.Y);
+            d.Y, skip_of(d));
 }
 template <typename T, typename TC>
 void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T>* out, T relax, T omega,
                   cudaStream_t s) {
     if (prev)
         k_sweep<T, true><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.Rhs, d.InvD,
-                                                              sell_of(d));
+                                                              sell_of(d), skip_of(d));
     else
         k_sweep<T, false><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, relax, omega, src, prev, out, d.Rhs,
-                                                               d.InvD, sell_of(d));
+                                                               d.InvD, sell_of(d), skip_of(d));
 }
 template <typename T, typename TC>
 void launch_direction(const Dev<T, TC>& d, cudaStream_t s) {
@@ -657,7 +722,8 @@ void launch_direction(const Dev<T, TC>& d, cudaStream_t s) {
 }
 template <typename T, typename TC>
 void launch_clamp(const Dev<T, TC>& d, cudaStream_t s) {
-    k_clamp<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Pold, d.Dir, d.Toi, d.P, d.Ph, d.Pl, d.Gate);
+    k_clamp<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.Pold, d.Dir, d.Toi, d.P, d.Ph, d.Pl, d.Gate,
+                                                          d.VInst, d.InstStop ? d.InstToi : nullptr);
 }
 template <typename T, typename TC>
 void launch_split(const Dev<T, TC>& d, const V4<TC>* X, V4<T>* hi, V4<T>* lo, int n, cudaStream_t s) {
@@ -672,6 +738,15 @@ void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s) {
 template <typename T, typename TC>
 void launch_outer_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cudaStream_t s) {
     k_outer_gate<TC><<<1, 1, 0, s>>>(d.Gate, d.Resid, d.Toi, d.ActiveCount, outer, tol, test ? 1 : 0);
+}
+template <typename T, typename TC>
+void launch_inst_resid(const Dev<T, TC>& d, cudaStream_t s) {
+    if (d.ninst > 0) k_inst_resid<TC><<<d.ninst, kBlock, 0, s>>>(d.InstBeg, d.Dir, d.InstResid, d.Gate);
+}
+template <typename T, typename TC>
+void launch_inst_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cudaStream_t s) {
+    k_inst_gate<TC><<<1, kBlock, 0, s>>>(d.ninst, d.InstStop, d.InstIters, d.InstResid, d.Gate, d.Toi,
+                                         d.ActiveCount, outer, tol, test ? 1 : 0);
 }
 template <typename T, typename TC>
 void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {
@@ -693,6 +768,8 @@ void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {
     template void launch_clamp<T, TC>(const Dev<T, TC>&, cudaStream_t);                                      \
     template void launch_copy_old<T, TC>(const Dev<T, TC>&, cudaStream_t);                                   \
     template void launch_outer_gate<T, TC>(const Dev<T, TC>&, int, double, bool, cudaStream_t);              \
+    template void launch_inst_resid<T, TC>(const Dev<T, TC>&, cudaStream_t);                                 \
+    template void launch_inst_gate<T, TC>(const Dev<T, TC>&, int, double, bool, cudaStream_t);               \
     template void launch_split<T, TC>(const Dev<T, TC>&, const V4<TC>*, V4<T>*, V4<T>*, int, cudaStream_t);  \
     template void launch_velocity<T, TC>(const Dev<T, TC>&, TC, cudaStream_t);
 

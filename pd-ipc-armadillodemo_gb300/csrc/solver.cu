@@ -122,6 +122,8 @@ public:
         Dev<T, TC>& d = d_;
         d.nsim = H.nsim;
         d.ntot = H.ntot;
+        num_sim_models_ = H.nsim > 0 ? 1 : 0;
+        for (int i = 1; i < H.nsim; ++i) num_sim_models_ += H.vertexModel[i] != H.vertexModel[i - 1];
         d.nface = (int)H.faces.size() / 3;
         d.nedge = (int)H.edges.size() / 2;
         d.npatch = H.npatch;
@@ -362,6 +364,25 @@ public:
         PD_CK(zeros(d.ErrFlags, 1));
         PD_CK(zeros(d.ActiveCount, 1));
         PD_CK(zeros(gate_, 1));
+        if (prm_.instance_stop) {
+            // the instances: simulated models, each a contiguous run of vertices
+            std::vector<int> vinst(nt, -1), beg(1, 0);
+            for (int i = 0; i < ns; ++i) {
+                if (i > 0 && H.vertexModel[i] != H.vertexModel[i - 1]) beg.push_back(i);
+                vinst[i] = (int)beg.size() - 1;
+            }
+            beg.push_back(ns);
+            d.ninst = ns > 0 ? (int)beg.size() - 1 : 0;
+            std::vector<TC> ones(std::max(d.ninst, 1), TC(1));
+            PD_CK(up(d.VInst, vinst));
+            PD_CK(up(d.InstBeg, beg));
+            PD_CK(zeros(d.InstStop, std::max(d.ninst, 1)));
+            PD_CK(zeros(d.InstResid, std::max(d.ninst, 1)));
+            PD_CK(up(d.InstToiMin, ones));
+            PD_CK(up(d.InstToi, ones));
+            PD_CK(zeros(d.InstIters, std::max(d.ninst, 1)));
+            instIters_.assign(std::max(d.ninst, 1), 0);
+        }
         PD_CK(cudaMallocHost(&pin_, sizeof(Pinned)));
         std::memset(pin_, 0, sizeof(Pinned));
         PD_CK(cudaMallocHost(&stage_, sizeof(V4<TC>) * (size_t)std::max(nt, 1)));
@@ -639,6 +660,7 @@ public:
         contact_ms_ = 0.0;
         st_.max_outer_iters = 0;
         st_.total_outer_iters = 0;
+        inst_outer_ = 0;
         for (int k = 0; k < n; ++k) {
             if (adj_every_ > 0) {
                 pdipc_status r = adjoint_checkpoint(err);
@@ -733,6 +755,8 @@ public:
         s->pd_solve_bytes = pd_bytes_;
         s->ccd_ms = ccd_ms_;
         s->contact_ms = contact_ms_;
+        s->instances = d_.ninst > 0 ? d_.ninst : num_sim_models_;
+        s->instance_outer_iters = prm_.instance_stop ? inst_outer_ : (int64_t)s->instances * st_.total_outer_iters;
     }
 
     // ---------------- stages ----------------
@@ -1040,6 +1064,10 @@ private:
         }
         adjoint_clear();
         if (every == 0) return PDIPC_OK;
+        if (prm_.instance_stop) {
+            err = "adjoint: not with per-instance stopping (params.instance_stop)";
+            return PDIPC_ERR_STATE;
+        }
         if (!kAdjoint) {
             err = "adjoint: the plain FP64 form only (precision PDIPC_PREC_FP64)";
             return PDIPC_ERR_STATE;
@@ -1360,8 +1388,9 @@ private:
         dfree(pSLen_);
         dfree(pSCol_);
         dfree(pSVal_);
-        // the persistent solve covers cloth stencils only: tet models take the per-sweep path
-        if (!std::is_same<T, float>::value || !prm_.persistent || c_.cheby >= kMaxCheby)
+        // the persistent solve covers cloth stencils only: tet models take the per-sweep path;
+        // per-instance stopping (rows skipped per instance) runs the per-sweep path too
+        if (!std::is_same<T, float>::value || !prm_.persistent || c_.cheby >= kMaxCheby || prm_.instance_stop)
             return PDIPC_OK;
         Dev<T, TC>& d = d_;
         const int ns = d.nsim;
@@ -1955,19 +1984,35 @@ private:
         PD_CK(cudaEventRecord(ev[kEvP1], s_));
         launch_direction(d, s_);
         launches_ += 2;
+        const bool inst = d.ninst > 0;
+        if (inst) {
+            launch_inst_resid(d, s_);
+            ++launches_;
+        }
         if (outer == 0) {
             r = broadphase(err);
             if (r != PDIPC_OK) return r;
+            if (inst) {  // per-candidate times of impact, reduced per instance
+                PD_CK(grow(instPT_, instPTCap_, std::max<int64_t>(d.nPT, 1)));
+                PD_CK(grow(instEE_, instEECap_, std::max<int64_t>(d.nEE, 1)));
+            }
         }
         PD_CK(cudaEventRecord(ev[kEvC0], s_));
-        launch_toi(d, pos_old(), pos(), c_, (TC*)nullptr, (TC*)nullptr, s_);
+        launch_toi(d, pos_old(), pos(), c_, inst ? instPT_ : (TC*)nullptr, inst ? instEE_ : (TC*)nullptr, s_);
         launch_toi_finalize(d, c_, s_);
+        if (inst) {
+            launch_inst_toi(d, instPT_, instEE_, c_, s_);
+            launches_ += 1 + (d.nPT > 0) + (d.nEE > 0);
+        }
         PD_CK(cudaEventRecord(ev[kEvC1], s_));
         launch_clamp(d, s_);
         PD_CK(cudaEventRecord(ev[kEvQ0], s_));
         launch_contact(d, pos(), c_, s_);
         PD_CK(cudaEventRecord(ev[kEvQ1], s_));
-        launch_outer_gate(d, outer, prm_.outer_tol, prm_.fixed_outer <= 0, s_);
+        if (inst)
+            launch_inst_gate(d, outer, prm_.outer_tol, prm_.fixed_outer <= 0, s_);
+        else
+            launch_outer_gate(d, outer, prm_.outer_tol, prm_.fixed_outer <= 0, s_);
         PD_CK(cudaMemcpyAsync(&pin_->gate[outer & 1], d.Gate, sizeof(OuterGate), cudaMemcpyDeviceToHost, s_));
         PD_CK(cudaEventRecord(ev[kEvGate], s_));
         launch_copy_old(d, s_);
@@ -1997,6 +2042,10 @@ private:
         const TC dt = (TC)c_.dt;
         GateScope scope(d_, gate_);
         PD_CK(cudaMemsetAsync(gate_, 0, sizeof(OuterGate), s_));
+        if (d.ninst > 0) {
+            PD_CK(cudaMemsetAsync(d.InstStop, 0, sizeof(unsigned) * d.ninst, s_));
+            PD_CK(cudaMemsetAsync(d.InstIters, 0, sizeof(int) * d.ninst, s_));
+        }
         launch_predict(d, dt, s_);
         ++launches_;
         const int max_outer = prm_.fixed_outer > 0 ? prm_.fixed_outer : prm_.max_outer;
@@ -2040,8 +2089,14 @@ private:
         PD_CK(cudaMemcpyAsync(&pin_->active, d.ActiveCount, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s_));
         TC toi;
         PD_CK(cudaMemcpyAsync(&toi, d.Toi, sizeof(TC), cudaMemcpyDeviceToHost, s_));
+        if (d.ninst > 0) {
+            // the instances' outer-iteration counts; outside a step no row is skipped
+            PD_CK(cudaMemcpyAsync(instIters_.data(), d.InstIters, sizeof(int) * d.ninst, cudaMemcpyDeviceToHost, s_));
+            PD_CK(cudaMemsetAsync(d.InstStop, 0, sizeof(unsigned) * d.ninst, s_));
+        }
         PD_CK(cudaStreamSynchronize(s_));
         PD_CK(cudaGetLastError());
+        for (int k = 0; k < d.ninst; ++k) inst_outer_ += instIters_[k];
         st_.last_toi = (double)toi;
         st_.active_contacts = (int64_t)pin_->active;
         st_.last_outer_iters = outer;
@@ -2145,6 +2200,13 @@ private:
     int graph_nodes_ = 0;
     bool inited_ = false;
     pdipc_stats st_{};
+    // per-instance stopping: per-candidate times of impact and the instances' counts
+    TC* instPT_ = nullptr;
+    TC* instEE_ = nullptr;
+    int64_t instPTCap_ = 0, instEECap_ = 0;
+    std::vector<int> instIters_;
+    int64_t inst_outer_ = 0;
+    int num_sim_models_ = 0;
 };
 
 std::unique_ptr<SolverBase> make_solver(int precision) {

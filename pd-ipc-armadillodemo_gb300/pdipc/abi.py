@@ -54,7 +54,8 @@ class Params(C.Structure):
         ("wait_limit_us", C.c_int),
         ("autotune", C.c_int),
         ("ccd_mode", C.c_int),
-        ("reserved", C.c_int * 3),
+        ("instance_stop", C.c_int),
+        ("reserved", C.c_int * 2),
     ]
 
 
@@ -153,6 +154,9 @@ class Stats(C.Structure):
         ("pd_solve_bytes", C.c_double),
         ("ccd_ms", C.c_double),
         ("contact_ms", C.c_double),
+        ("instances", C.c_int32),
+        ("reserved_i", C.c_int32),
+        ("instance_outer_iters", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
