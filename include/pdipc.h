@@ -498,14 +498,16 @@ pdipc_status pdipc_stage_penalty_dcd(pdipc_ctx* ctx, const double* x, const int*
  * simulated vertex's stretch stiffness (n_sim; the per-vertex strain weight
  * that the model's k_stretch sets, PdIpcClothModel.h:177-328).  It is the exact
  * derivative of the executed iteration: every local-global iteration, every
- * weighted-Jacobi sweep and Chebyshev step, the prediction and the velocity
- * update, for the outer-iteration counts the recorded steps ran (fix them with
- * pdipc_params.fixed_outer for a smooth rollout).  It replays the recorded
- * steps from the checkpoints (two replays per step) and leaves the context's
- * state and stats as they were.  PDIPC_ERR_STATE unless the context is in the
- * plain FP64 form (PDIPC_PREC_FP64) with cloth models only, steps were
- * recorded, and every replayed outer iteration ran a full, contact-free step
- * (time of impact 1, no active contact constraints). */
+ * weighted-Jacobi sweep and Chebyshev step, the strain-limit projections of
+ * tets and cloth triangles (through the derivative of their clamped SVD), the
+ * prediction and the velocity update, for the outer-iteration counts the
+ * recorded steps ran (fix them with pdipc_params.fixed_outer for a smooth
+ * rollout).  It replays the recorded steps from the checkpoints (two replays
+ * per step) and leaves the context's state and stats as they were.
+ * PDIPC_ERR_STATE unless the context is in the plain FP64 form
+ * (PDIPC_PREC_FP64) without per-instance stopping, steps were recorded, and
+ * every replayed outer iteration ran a full, contact-free step (time of impact
+ * 1, no active contact constraints). */
 pdipc_status pdipc_adjoint_record(pdipc_ctx* ctx, int checkpoint_every);
 pdipc_status pdipc_adjoint_backward(pdipc_ctx* ctx, const double* dl_dx, const double* dl_dv, double* dl_dx0,
                                     double* dl_dv0, double* dl_dstrain);

@@ -440,6 +440,143 @@ static void tri_project(const R* x0, const R* x1, const R* x2, const R* idm, R w
     out[3][0] = out[3][1] = out[3][2] = R(0);
 }
 
+// Adjoint of R(F) = U C V^T (F = U diag(s) V^T, row-major; c the clamped
+// singular values, dc = dc/ds): Fb = U Pb V^T from Rb, with Rb' = U^T Rb V,
+// Pb_kk = dc_k Rb'_kk and, for k < m, Pb_km = a Rb'_km + b Rb'_mk,
+// Pb_mk = b Rb'_km + a Rb'_mk, a = (c_m s_m - c_k s_k) / (s_m^2 - s_k^2),
+// b = (c_m s_k - c_k s_m) / (s_m^2 - s_k^2) (the SVD's differentials U^T dU,
+// V^T dV); unclamped pairs a = 1, b = 0; equal values clamped to one bound
+// a = -b = c / (s_k + s_m).  The library's k_adj_elem computes the same.
+template <typename R>
+static void clamp_svd_adjoint(const R* U, const R* s, const R* V, const R* c, const R* dc, const R* Rb, R* Fb) {
+    R Rp[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            R a = 0;
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) a += U[3 * k + i] * Rb[3 * k + l] * V[3 * l + j];
+            Rp[3 * i + j] = a;
+        }
+    R Pb[9];
+    for (int k = 0; k < 3; ++k) Pb[4 * k] = dc[k] * Rp[4 * k];
+    for (int k = 0; k < 3; ++k)
+        for (int m = k + 1; m < 3; ++m) {
+            R al, be;
+            if (c[k] == s[k] && c[m] == s[m]) {
+                al = 1;
+                be = 0;
+            } else {
+                const R den = s[m] * s[m] - s[k] * s[k];
+                const R q = s[k] * s[k] + s[m] * s[m];
+                if (den * den < R(1e-28) * q * q) {
+                    const R ss = s[k] + s[m];
+                    al = ss != R(0) ? c[k] / ss : R(0);
+                    be = -al;
+                } else {
+                    al = (c[m] * s[m] - c[k] * s[k]) / den;
+                    be = (c[m] * s[k] - c[k] * s[m]) / den;
+                }
+            }
+            Pb[3 * k + m] = al * Rp[3 * k + m] + be * Rp[3 * m + k];
+            Pb[3 * m + k] = be * Rp[3 * k + m] + al * Rp[3 * m + k];
+        }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            R a = 0;
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) a += U[3 * i + k] * Pb[3 * k + l] * V[3 * j + l];
+            Fb[3 * i + j] = a;
+        }
+}
+
+// Adjoint of one strain-limit element (tet_project / tri_project above) at
+// the positions the forward projected: out[c] went to vertex c's right-hand
+// side, so with rb the right-hand sides' adjoint (per vertex c) the vertices'
+// position adjoints land in eb[c] (4 x 3).
+template <typename R>
+static void elem_adjoint(const R* const* x, bool tri, const R* idm, R w, const R* const* rb, R eb[4][3]) {
+    R F[9], U[9], sv[3], V[9], c[3], dc[3], Rb[9] = {}, Fb[9];
+    auto clampv = [](R a, R& d) {
+        d = (a > R(0.999) && a < R(1.001)) ? R(1) : R(0);
+        return a < R(1.001) ? (a < R(0.999) ? R(0.999) : a) : R(1.001);
+    };
+    for (int c2 = 0; c2 < 4; ++c2)
+        for (int k = 0; k < 3; ++k) eb[c2][k] = 0;
+    if (tri) {
+        for (int k = 0; k < 3; ++k) {
+            const R a = x[1][k] - x[0][k], b = x[2][k] - x[0][k];
+            F[3 * k + 0] = a * idm[0] + b * idm[2];
+            F[3 * k + 1] = a * idm[1] + b * idm[3];
+        }
+        const R n[3] = {F[3] * F[7] - F[6] * F[4], F[6] * F[1] - F[0] * F[7], F[0] * F[4] - F[3] * F[1]};
+        const R nl = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int k = 0; k < 3; ++k) F[3 * k + 2] = nl > R(0) ? n[k] / nl : R(0);
+        svd3_onesided(F, U, sv, V);
+        for (int k = 0; k < 3; ++k) {
+            c[k] = clampv(sv[k] < R(0) ? -sv[k] : sv[k], dc[k]);
+            if (sv[k] < R(0)) c[k] = -c[k];
+        }
+        const R G[3][2] = {{-(idm[0] + idm[2]), -(idm[1] + idm[3])}, {idm[0], idm[1]}, {idm[2], idm[3]}};
+        for (int r = 0; r < 3; ++r)
+            for (int j = 0; j < 2; ++j) {
+                R a = 0;
+                for (int v = 0; v < 3; ++v) a += rb[v][r] * G[v][j];
+                Rb[3 * r + j] = w * a;
+            }
+        clamp_svd_adjoint(U, sv, V, c, dc, Rb, Fb);
+        if (nl > R(0)) {  // the unit-normal column, n = a x b
+            R nb[3] = {Fb[2], Fb[5], Fb[8]};
+            const R h[3] = {n[0] / nl, n[1] / nl, n[2] / nl};
+            const R pr = h[0] * nb[0] + h[1] * nb[1] + h[2] * nb[2];
+            for (int k = 0; k < 3; ++k) nb[k] = (nb[k] - h[k] * pr) / nl;
+            const R a[3] = {F[0], F[3], F[6]}, b[3] = {F[1], F[4], F[7]};
+            const R ab[3] = {b[1] * nb[2] - b[2] * nb[1], b[2] * nb[0] - b[0] * nb[2], b[0] * nb[1] - b[1] * nb[0]};
+            const R bb[3] = {nb[1] * a[2] - nb[2] * a[1], nb[2] * a[0] - nb[0] * a[2], nb[0] * a[1] - nb[1] * a[0]};
+            for (int k = 0; k < 3; ++k) {
+                Fb[3 * k] += ab[k];
+                Fb[3 * k + 1] += bb[k];
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            const R d0 = Fb[3 * k] * idm[0] + Fb[3 * k + 1] * idm[1];
+            const R d1 = Fb[3 * k] * idm[2] + Fb[3 * k + 1] * idm[3];
+            eb[1][k] = d0;
+            eb[2][k] = d1;
+            eb[0][k] = -(d0 + d1);
+        }
+        return;
+    }
+    for (int k = 0; k < 3; ++k) {
+        const R d[3] = {x[1][k] - x[0][k], x[2][k] - x[0][k], x[3][k] - x[0][k]};
+        for (int j = 0; j < 3; ++j) F[3 * k + j] = d[0] * idm[j] + d[1] * idm[3 + j] + d[2] * idm[6 + j];
+    }
+    svd3_onesided(F, U, sv, V);
+    for (int k = 0; k < 3; ++k) {  // c_k = clamp(|s_k|): a negative determinant's s_2 flipped
+        c[k] = clampv(sv[k] < R(0) ? -sv[k] : sv[k], dc[k]);
+        if (sv[k] < R(0)) dc[k] = -dc[k];
+    }
+    R G[3][4];
+    for (int i = 0; i < 3; ++i) {
+        G[i][1] = idm[i];
+        G[i][2] = idm[3 + i];
+        G[i][3] = idm[6 + i];
+        G[i][0] = -(G[i][1] + G[i][2] + G[i][3]);
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int j = 0; j < 3; ++j) {
+            R a = 0;
+            for (int v = 0; v < 4; ++v) a += rb[v][r] * G[j][v];
+            Rb[3 * r + j] = w * a;
+        }
+    clamp_svd_adjoint(U, sv, V, c, dc, Rb, Fb);
+    for (int k = 0; k < 3; ++k)
+        for (int v = 0; v < 3; ++v) {
+            const R d = Fb[3 * k] * idm[3 * v] + Fb[3 * k + 1] * idm[3 * v + 1] + Fb[3 * k + 2] * idm[3 * v + 2];
+            eb[1 + v][k] = d;
+            eb[0][k] -= d;
+        }
+}
+
 // FP64 coplanarity-cubic CCD of one candidate (pdipc_params.ccd_mode 1; no
 // reference kernel: the reference compiles Commom/PolynomialSolver.h:10-60 and
 // never calls it).  Four points moving linearly are coplanar where
@@ -1845,7 +1982,7 @@ struct Sim {
     // velocities) after the step on entry and before it on return; kb (nsim)
     // collects dL/d(strain weight).  X, V are left at the step's end.
     int adjoint_step(std::vector<T>& pb, std::vector<T>& vb, std::vector<T>& kb) {
-        if (global_form != 1 || ntet > 0) return PDIPC_ERR_STATE;
+        if (global_form != 1) return PDIPC_ERR_STATE;
         std::vector<std::vector<T>> tape;
         lgTape = &tape;
         contactSeen = false;
@@ -2019,6 +2156,30 @@ struct Sim {
                     kb[m] += rest * kr;
                 }
                 for (int k = 0; k < 3; ++k) pb[3 * (size_t)m + k] = acc[k];
+            }
+            // strain-limit elements: their adjoints per element, then each
+            // vertex adds its elements' in ascending element order
+            if (ntet > 0) {
+                std::vector<T> eb(12 * (size_t)ntet);
+#pragma omp parallel for schedule(static) num_threads(threads)
+                for (int e = 0; e < ntet; ++e) {
+                    const auto& q = tets[e];
+                    const bool tri = q[3] < 0;
+                    const T* xs[4];
+                    const T* rs[4];
+                    for (int c2 = 0; c2 < 4; ++c2) {
+                        const int v = (tri && c2 == 3) ? q[0] : q[c2];
+                        xs[c2] = &x[3 * (size_t)v];
+                        rs[c2] = &rb[3 * (size_t)v];
+                    }
+                    T out[4][3];
+                    elem_adjoint<T>(xs, tri, &tetIdm[9 * (size_t)e], tetW[e], rs, out);
+                    for (int c2 = 0; c2 < 4; ++c2)
+                        for (int k = 0; k < 3; ++k) eb[12 * (size_t)e + 3 * c2 + k] = out[c2][k];
+                }
+                for (int i = 0; i < nsim; ++i)
+                    for (int t = vtPtr[i]; t < vtPtr[i + 1]; ++t)
+                        for (int k = 0; k < 3; ++k) pb[3 * (size_t)i + k] += eb[3 * (size_t)vtIdx[t] + k];
             }
         }
         // through the prediction (pinned vertices start at x with v = 0)

@@ -22,6 +22,7 @@
 #include <type_traits>
 
 #include "kernels.cuh"
+#include "svd3.cuh"
 
 namespace pdipc {
 
@@ -225,6 +226,198 @@ __global__ void k_adj_local(int nsim, const V4<T>* __restrict__ x, const V4<T>* 
     kbar[m] += kb;
 }
 
+// Adjoint of the strain-limit projection R(F) = U C V^T (svd3.cuh: F = U
+// diag(s) V^T, C the clamped singular values) at F: given Rb = dL/dR, returns
+// Fb = dL/dF = U Pb V^T, where in the singular frame (Rb' = U^T Rb V) the
+// differential of R is dR'_kk = c'_k dP_kk and, for k != m,
+// dR'_km = alpha dP_km + beta dP_mk, dR'_mk = beta dP_km + alpha dP_mk with
+// alpha = (c_m s_m - c_k s_k) / (s_m^2 - s_k^2), beta = (c_m s_k - c_k s_m) /
+// (s_m^2 - s_k^2) (from U^T dU and V^T dV, the SVD's skew differentials).
+// Unclamped pairs give alpha = 1, beta = 0 (R = F there); two values clamped to
+// one bound give alpha = -beta = c / (s_k + s_m).  dc[k] = dc_k / ds_k.
+template <typename T>
+__device__ void clamp_svd_adjoint(const T (&U)[3][3], const T (&s)[3], const T (&V)[3][3], const T (&c)[3],
+                                  const T (&dc)[3], const T (&Rb)[3][3], T (&Fb)[3][3]) {
+    T A[3][3], Pb[3][3];  // A = Rb V, then Rb' = U^T A
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) A[i][j] = Rb[i][0] * V[0][j] + Rb[i][1] * V[1][j] + Rb[i][2] * V[2][j];
+    T Rp[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Rp[i][j] = U[0][i] * A[0][j] + U[1][i] * A[1][j] + U[2][i] * A[2][j];
+    for (int k = 0; k < 3; ++k) Pb[k][k] = dc[k] * Rp[k][k];
+    for (int k = 0; k < 3; ++k)
+        for (int m = k + 1; m < 3; ++m) {
+            T al, be;
+            const T sk = s[k], sm = s[m];
+            if (c[k] == sk && c[m] == sm) {
+                al = T(1);
+                be = T(0);
+            } else {
+                T den = sm * sm - sk * sk;
+                if (den * den < T(1e-28) * (sk * sk + sm * sm) * (sk * sk + sm * sm)) {
+                    // equal singular values: the limit for values clamped to one bound
+                    const T ss = sk + sm;
+                    al = (ss != T(0)) ? c[k] / ss : T(0);
+                    be = -al;
+                } else {
+                    al = (c[m] * sm - c[k] * sk) / den;
+                    be = (c[m] * sk - c[k] * sm) / den;
+                }
+            }
+            Pb[k][m] = al * Rp[k][m] + be * Rp[m][k];
+            Pb[m][k] = be * Rp[k][m] + al * Rp[m][k];
+        }
+    for (int i = 0; i < 3; ++i)  // Fb = U Pb V^T
+        for (int j = 0; j < 3; ++j) {
+            T a = T(0);
+            for (int k = 0; k < 3; ++k) {
+                const T w = U[i][k];
+                a += w * (Pb[k][0] * V[j][0] + Pb[k][1] * V[j][1] + Pb[k][2] * V[j][2]);
+            }
+            Fb[i][j] = a;
+        }
+}
+
+// Adjoint of the strain-limit projections (tets; cloth triangles, whose
+// fourth vertex is -1) at the positions x the forward projected: element e
+// added out[c] = w R G[:, c] to its vertex c's right-hand side (svd3.cuh:
+// tet_project, tri_project), so with rb the right-hand sides' adjoint,
+// Rb = w sum_c rb_c G[:, c]^T; through the SVD (and, for a triangle, its unit
+// normal column) to Fb, then Dsb = Fb Dm^-T and the vertices' adjoints into
+// Eb[4 e + c] (gathered per vertex in ascending element order).
+template <typename T>
+__global__ void k_adj_elem(int ntet, const int4* __restrict__ Tets, const T* __restrict__ Idm,
+                           const T* __restrict__ W, const V4<T>* __restrict__ x, const V4<T>* __restrict__ rb,
+                           V4<T>* __restrict__ Eb) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ntet) return;
+    const int4 q = Tets[e];
+    const bool tri = q.w < 0;
+    const int id[4] = {q.x, q.y, q.z, tri ? q.x : q.w};
+    const V4<T> x0 = x[id[0]];
+    T Ds[3][3];
+    for (int c = 0; c < 3; ++c) {
+        const V4<T> xc = x[id[c + 1]];
+        Ds[0][c] = xc.x - x0.x;
+        Ds[1][c] = xc.y - x0.y;
+        Ds[2][c] = xc.z - x0.z;
+    }
+    T idm[9];
+    for (int k = 0; k < 9; ++k) idm[k] = Idm[9 * (size_t)e + k];
+    const T w = W[e];
+    T F[3][3], U[3][3], sv[3], V[3][3], c[3], dc[3], Rb[3][3], Fb[3][3];
+    auto clamp_ = [](T a, T& d) {
+        d = (a > T(0.999) && a < T(1.001)) ? T(1) : T(0);
+        return a < T(1.001) ? (a < T(0.999) ? T(0.999) : a) : T(1.001);
+    };
+    auto rbv = [&](int c) -> V4<T> { return rb[id[c]]; };
+    if (tri) {
+        for (int i = 0; i < 3; ++i) {
+            F[i][0] = Ds[i][0] * idm[0] + Ds[i][1] * idm[2];
+            F[i][1] = Ds[i][0] * idm[1] + Ds[i][1] * idm[3];
+        }
+        const T n[3] = {F[1][0] * F[2][1] - F[2][0] * F[1][1], F[2][0] * F[0][1] - F[0][0] * F[2][1],
+                        F[0][0] * F[1][1] - F[1][0] * F[0][1]};
+        const T nn = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+        const T nl = nn > T(0) ? dsqrt(nn) : T(0);
+        const T inv = nl > T(0) ? T(1) / nl : T(0);
+        for (int i = 0; i < 3; ++i) F[i][2] = n[i] * inv;
+        svd::svd3(F, U, sv, V);
+        for (int k = 0; k < 3; ++k) {  // sc_k = sign(s_k) clamp(|s_k|): dc_k / ds_k = clamp'(|s_k|)
+            const T a = sv[k] < T(0) ? -sv[k] : sv[k];
+            c[k] = clamp_(a, dc[k]);
+            if (sv[k] < T(0)) c[k] = -c[k];
+        }
+        const T G[3][2] = {{-(idm[0] + idm[2]), -(idm[1] + idm[3])}, {idm[0], idm[1]}, {idm[2], idm[3]}};
+        for (int r = 0; r < 3; ++r) {
+            Rb[r][2] = T(0);
+            for (int j = 0; j < 2; ++j) {
+                T a = T(0);
+                for (int cc = 0; cc < 3; ++cc) {
+                    const V4<T> v = rbv(cc);
+                    a += (r == 0 ? v.x : r == 1 ? v.y : v.z) * G[cc][j];
+                }
+                Rb[r][j] = w * a;
+            }
+        }
+        clamp_svd_adjoint(U, sv, V, c, dc, Rb, Fb);
+        // the normal column: F[:, 2] = n / |n| with n = a x b (a, b the first two columns)
+        T nb[3] = {Fb[0][2], Fb[1][2], Fb[2][2]};
+        if (nl > T(0)) {
+            const T h[3] = {n[0] * inv, n[1] * inv, n[2] * inv};
+            const T pr = h[0] * nb[0] + h[1] * nb[1] + h[2] * nb[2];
+            for (int i = 0; i < 3; ++i) nb[i] = (nb[i] - h[i] * pr) * inv;
+            const T a[3] = {F[0][0], F[1][0], F[2][0]}, b[3] = {F[0][1], F[1][1], F[2][1]};
+            // d(a x b) = da x b + a x db: ab += b x nb, bb += nb x a
+            Fb[0][0] += b[1] * nb[2] - b[2] * nb[1];
+            Fb[1][0] += b[2] * nb[0] - b[0] * nb[2];
+            Fb[2][0] += b[0] * nb[1] - b[1] * nb[0];
+            Fb[0][1] += nb[1] * a[2] - nb[2] * a[1];
+            Fb[1][1] += nb[2] * a[0] - nb[0] * a[2];
+            Fb[2][1] += nb[0] * a[1] - nb[1] * a[0];
+        }
+        T d0[3], d1[3];
+        for (int i = 0; i < 3; ++i) {
+            d0[i] = Fb[i][0] * idm[0] + Fb[i][1] * idm[1];
+            d1[i] = Fb[i][0] * idm[2] + Fb[i][1] * idm[3];
+        }
+        Eb[4 * (size_t)e + 0] = V4<T>{-(d0[0] + d1[0]), -(d0[1] + d1[1]), -(d0[2] + d1[2]), T(0)};
+        Eb[4 * (size_t)e + 1] = V4<T>{d0[0], d0[1], d0[2], T(0)};
+        Eb[4 * (size_t)e + 2] = V4<T>{d1[0], d1[1], d1[2], T(0)};
+        Eb[4 * (size_t)e + 3] = V4<T>{T(0), T(0), T(0), T(0)};
+        return;
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) F[i][j] = Ds[i][0] * idm[j] + Ds[i][1] * idm[3 + j] + Ds[i][2] * idm[6 + j];
+    svd::svd3(F, U, sv, V);
+    // sc_k = clamp(|s_k|) (a negative determinant's s_2 flipped, |s| already
+    // descending): dc_k / ds_k = clamp'(|s_k|) sign(s_k)
+    for (int k = 0; k < 3; ++k) {
+        const T a = sv[k] < T(0) ? -sv[k] : sv[k];
+        c[k] = clamp_(a, dc[k]);
+        if (sv[k] < T(0)) dc[k] = -dc[k];
+    }
+    T G[3][4];
+    for (int i = 0; i < 3; ++i) {
+        G[i][1] = idm[i];
+        G[i][2] = idm[3 + i];
+        G[i][3] = idm[6 + i];
+        G[i][0] = -(G[i][1] + G[i][2] + G[i][3]);
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int j = 0; j < 3; ++j) {
+            T a = T(0);
+            for (int cc = 0; cc < 4; ++cc) {
+                const V4<T> v = rbv(cc);
+                a += (r == 0 ? v.x : r == 1 ? v.y : v.z) * G[j][cc];
+            }
+            Rb[r][j] = w * a;
+        }
+    clamp_svd_adjoint(U, sv, V, c, dc, Rb, Fb);
+    T db[3][3];  // Dsb = Fb Dm^-T
+    for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k) db[i][k] = Fb[i][0] * idm[3 * k] + Fb[i][1] * idm[3 * k + 1] + Fb[i][2] * idm[3 * k + 2];
+    Eb[4 * (size_t)e + 0] =
+        V4<T>{-(db[0][0] + db[0][1] + db[0][2]), -(db[1][0] + db[1][1] + db[1][2]), -(db[2][0] + db[2][1] + db[2][2]), T(0)};
+    for (int k = 0; k < 3; ++k) Eb[4 * (size_t)e + 1 + k] = V4<T>{db[0][k], db[1][k], db[2][k], T(0)};
+}
+
+// xb_i += the element adjoints of vertex i, in ascending element order
+template <typename T>
+__global__ void k_adj_elem_gather(int nsim, const int* __restrict__ vtPtr, const int* __restrict__ vtIdx,
+                                  const V4<T>* __restrict__ Eb, V4<T>* __restrict__ xb) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim) return;
+    V4<T> a = xb[i];
+    for (int q = vtPtr[i]; q < vtPtr[i + 1]; ++q) {
+        const V4<T> v = Eb[vtIdx[q]];
+        a.x += v.x;
+        a.y += v.y;
+        a.z += v.z;
+    }
+    xb[i] = a;
+}
+
 // step output adjoints (pb of P, vb of V = (P - X0) invt) -> pb of the solved
 // positions, vb := adjoint of X0; r0b := 0
 template <typename T>
@@ -277,12 +470,16 @@ void launch_adj_sweep(const Dev<T, TC>& d, const T* NTval, T relax, T scale, con
 }
 template <typename T, typename TC>
 void launch_adj_local(const Dev<T, TC>& d, const T* lLboT, T relax, const V4<T>* x, const V4<T>* rho, V4<T>* rb,
-                      V4<T>* qb, V4<T>* r0b, V4<T>* xb, T* kbar, cudaStream_t s) {
+                      V4<T>* qb, V4<T>* r0b, V4<T>* xb, T* kbar, V4<T>* eb, cudaStream_t s) {
     k_adj_rhs<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, relax, rho, d.InvD, rb, r0b);
     k_adj_curv<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, x, rb, d.lPtr, d.lNbr, d.lLbo, d.lBend, d.CurvNorm,
                                                         qb);
     k_adj_local<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, x, rb, qb, d.lPtr, d.lNbr, lLboT, d.lRest,
                                                          d.Strain, xb, kbar);
+    if (d.ntet > 0 && eb) {
+        k_adj_elem<T><<<blocks_for(d.ntet, 128), 128, 0, s>>>(d.ntet, d.Tets, d.TetIdm, d.TetW, x, rb, eb);
+        k_adj_elem_gather<T><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.vtPtr, d.vtIdx, eb, xb);
+    }
 }
 template <typename T, typename TC>
 void launch_adj_step_begin(const Dev<T, TC>& d, T invt, V4<T>* pb, V4<T>* vb, V4<T>* r0b, cudaStream_t s) {
@@ -299,7 +496,7 @@ template void launch_adj_sweep<double, double>(const Dev<double, double>&, const
                                                bool, V4<double>*, double*, cudaStream_t);
 template void launch_adj_local<double, double>(const Dev<double, double>&, const double*, double,
                                                const V4<double>*, const V4<double>*, V4<double>*, V4<double>*,
-                                               V4<double>*, V4<double>*, double*, cudaStream_t);
+                                               V4<double>*, V4<double>*, double*, V4<double>*, cudaStream_t);
 template void launch_adj_step_begin<double, double>(const Dev<double, double>&, double, V4<double>*, V4<double>*,
                                                     V4<double>*, cudaStream_t);
 template void launch_adj_step_end<double, double>(const Dev<double, double>&, double, V4<double>*, V4<double>*,

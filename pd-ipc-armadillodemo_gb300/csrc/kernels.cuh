@@ -334,10 +334,12 @@ template <typename T, typename TC>
 void launch_adj_sweep(const Dev<T, TC>& d, const T* NTval, T relax, T scale, const V4<T>* in, V4<T>* other,
                       const V4<T>* z, V4<T>* out, bool accumulate, V4<T>* rho, T* kbar, cudaStream_t s);
 // the local step's adjoint at x from rho (sum of the sweeps' output adjoints):
-// rb, qb scratch; r0b += w D^-1 rho; xb += d(rhs)/dx^T rb; kbar += d(rhs)/dk . rb
+// rb, qb scratch; r0b += w D^-1 rho; xb += d(rhs)/dx^T rb; kbar += d(rhs)/dk . rb;
+// with strain-limit elements (tets, cloth triangles) their SVD-derivative
+// adjoint through eb (4 per element, scratch)
 template <typename T, typename TC>
 void launch_adj_local(const Dev<T, TC>& d, const T* lLboT, T relax, const V4<T>* x, const V4<T>* rho, V4<T>* rb,
-                      V4<T>* qb, V4<T>* r0b, V4<T>* xb, T* kbar, cudaStream_t s);
+                      V4<T>* qb, V4<T>* r0b, V4<T>* xb, T* kbar, V4<T>* eb, cudaStream_t s);
 // step output adjoints -> adjoint of the solved positions (pb) and of X0 (vb); r0b = 0
 template <typename T, typename TC>
 void launch_adj_step_begin(const Dev<T, TC>& d, T invt, V4<T>* pb, V4<T>* vb, V4<T>* r0b, cudaStream_t s);

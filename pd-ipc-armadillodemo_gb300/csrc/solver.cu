@@ -1072,10 +1072,6 @@ private:
             err = "adjoint: the plain FP64 form only (precision PDIPC_PREC_FP64)";
             return PDIPC_ERR_STATE;
         }
-        if (d_.ntet > 0) {
-            err = "adjoint: cloth models only (the scene has tets)";
-            return PDIPC_ERR_STATE;
-        }
         adj_every_ = every;
         return PDIPC_OK;
     }
@@ -1114,6 +1110,7 @@ private:
         PD_CK(alloc(adj_ntval_, (size_t)sell_padded_));
         PD_CK(alloc(adj_final_, 2 * (size_t)ns));
         PD_CK(alloc(adj_kb_, (size_t)ns));
+        if (d_.ntet > 0) PD_CK(alloc(adj_eb_, 4 * (size_t)d_.ntet));
         for (V4<TC>** b : {&adj_pb_, &adj_vb_, &adj_r0b_, &adj_rb_, &adj_qb_, &adj_u_, &adj_rho_})
             PD_CK(alloc(*b, (size_t)ns));
         adj_xb_.assign(cb + 1, nullptr);
@@ -1177,7 +1174,8 @@ private:
                                  adj_rho_, adj_kb_, s_);
                 launch_adj_sweep(d, adj_ntval_, w, T(1), adj_u_, (V4<T>*)nullptr, adj_xs_[0], adj_xb_[0], true,
                                  adj_rho_, adj_kb_, s_);
-                launch_adj_local(d, adj_lboT_, w, x, adj_rho_, adj_rb_, adj_qb_, adj_r0b_, adj_xb_[0], adj_kb_, s_);
+                launch_adj_local(d, adj_lboT_, w, x, adj_rho_, adj_rb_, adj_qb_, adj_r0b_, adj_xb_[0], adj_kb_,
+                                 adj_eb_, s_);
                 std::swap(adj_xb_[0], adj_pb_);  // the adjoint of the previous iteration's result
             }
             launch_adj_step_end(d, (T)dt, adj_pb_, adj_vb_, adj_r0b_, s_);
@@ -2170,6 +2168,7 @@ private:
     T* adj_lboT_ = nullptr;
     T* adj_ntval_ = nullptr;
     T* adj_kb_ = nullptr;
+    V4<TC>* adj_eb_ = nullptr;  // strain-limit elements' adjoints (4 per element)
     V4<TC>* adj_final_ = nullptr;
     V4<TC>*adj_pb_ = nullptr, *adj_vb_ = nullptr, *adj_r0b_ = nullptr, *adj_rb_ = nullptr, *adj_qb_ = nullptr,
            *adj_u_ = nullptr, *adj_rho_ = nullptr;

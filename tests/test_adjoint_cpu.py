@@ -350,3 +350,44 @@ def test_oracle_adjoint_tangent_identity_128_cloth_50_steps():
     50 steps, 3 outer iterations of 10 local-global iterations per step."""
     for name, lhs, rhs, scale in _oracle_identity(128, 50, 10, 15, 3):
         assert abs(lhs - rhs) <= 1e-10 * scale, (name, lhs, rhs, scale)
+
+
+def test_oracle_adjoint_through_strain_limits_matches_its_central_differences():
+    """The oracle's adjoint of the strain-limit projections (the derivative of
+    the clamped 3x3 SVD, and for a cloth triangle of its unit-normal column)
+    against central differences of the oracle's own forward: an 8x8 cloth with
+    the triangle strain limit, and a 2x2x2 tet block, with initial velocities
+    that stretch most elements past the clamp."""
+    from oracle.oracle import FORM_JJ, Oracle
+    from pdipc import scenes
+
+    cloth = scenes.cloth_drop(8, 1, with_sphere=False, lg=3)
+    cloth.cloths[0].k_tri_strain = 2e3
+    X, Tt = scenes.tet_block(2, 2, 2, size=(0.1, 0.1, 0.1))
+    block = scenes.Scene("tet_adjoint", [], [], lg_iterations=3, steps=10, solids=[
+        scenes.SolidSpec(X, Tt, np.array([0], np.int32), density=500.0, k_strain=2e3, patch_dim=2)])
+    for sc, seed in ((cloth, 11), (block, 12)):
+        orc = Oracle(sc, "fp64", FORM_JJ, threads=2, cheby_iterations=5, fixed_outer=2)
+        r = np.random.default_rng(seed)
+        nv, T = sc.n_sim, 3
+        x0 = sc.initial_positions()
+        v0 = r.uniform(-0.3, 0.3, (nv, 3))
+        cx, cv = r.normal(size=(nv, 3)), r.normal(size=(nv, 3))
+
+        def run(x, v):
+            orc.set_state(x, v)
+            orc.step(T)
+            return orc.positions()[:nv].copy(), orc.velocities().copy()
+
+        def loss(x, v):
+            return float(np.sum(cx * x) + np.sum(cv * v))
+
+        gx0, gv0, _ = orc.adjoint_rollout(T, x0, v0, cx, cv)
+        for trial in range(3):
+            d = r.normal(size=(nv, 3))
+            fd = (loss(*run(x0, v0 + 1e-6 * d)) - loss(*run(x0, v0 - 1e-6 * d))) / 2e-6
+            ad = float(np.sum(gv0 * d))
+            assert abs(fd - ad) <= 1e-5 * abs(fd), ("v", sc.name, trial, fd, ad)
+            fd = (loss(*run(x0 + 1e-8 * d, v0)) - loss(*run(x0 - 1e-8 * d, v0))) / 2e-8
+            ad = float(np.sum(gx0 * d))
+            assert abs(fd - ad) <= 1e-5 * abs(fd), ("x", sc.name, trial, fd, ad)

@@ -230,3 +230,73 @@ def test_adjoint_matches_the_oracle_on_the_128_cloth_50_steps(built_lib):
     for name, a, b in zip(("x0", "v0", "k"), ours, ref):
         assert np.all(np.isfinite(a)) and np.linalg.norm(b) > 0
         assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b), (name, np.linalg.norm(a - b), np.linalg.norm(b))
+
+
+def strained_cloth(n=10):
+    """free_cloth with the triangle strain limit on every triangle."""
+    sc = free_cloth(n)
+    sc.cloths[0].k_tri_strain = 2e3
+    return sc
+
+
+def tet_scene():
+    """A 2x2x2 tet block, one corner vertex pinned, no obstacle."""
+    X, T = scenes.tet_block(2, 2, 2, size=(0.1, 0.1, 0.1))
+    solid = scenes.SolidSpec(X, T, np.array([0], np.int32), density=500.0, k_strain=2e3, patch_dim=2)
+    return scenes.Scene("tet_adjoint", [], [], solids=[solid], lg_iterations=4, steps=10)
+
+
+@pytest.mark.parametrize("which", ["triangle", "tet"])
+def test_adjoint_through_strain_limits_matches_central_differences(which, built_lib):
+    """The strain-limit projections (the clamped 3x3 SVD of every triangle's
+    or tet's deformation gradient) in the reverse pass: gradients with respect
+    to initial positions and velocities against central differences of the GPU
+    forward, with initial velocities large enough that most elements' singular
+    values leave [0.999, 1.001] and are clamped."""
+    sc = strained_cloth() if which == "triangle" else tet_scene()
+    kw = dict(cheby_iterations=5, fixed_outer=2)
+    sim = make(sc, **kw)
+    rng = np.random.default_rng(31 if which == "triangle" else 37)
+    n, T = sc.n_sim, 3
+    x0 = sc.initial_positions()
+    v0 = rng.uniform(-0.3, 0.3, (n, 3))
+    cx, cv = rng.normal(size=(n, 3)), rng.normal(size=(n, 3))
+
+    def loss(x, v):
+        return float(np.sum(cx * x) + np.sum(cv * v))
+
+    x, v = rollout(sim, x0, v0, T, every=2)
+    gx0, gv0, _ = sim.adjoint_backward(cx, cv)
+    assert np.all(np.isfinite(gx0)) and np.all(np.isfinite(gv0))
+    for trial in range(3):
+        d = rng.normal(size=(n, 3))
+        ev = 1e-6
+        fd = (loss(*rollout(sim, x0, v0 + ev * d, T)) - loss(*rollout(sim, x0, v0 - ev * d, T))) / (2 * ev)
+        assert rel(fd, np.sum(gv0 * d)) < 1e-4, ("v", trial, fd, np.sum(gv0 * d))
+        ex = 1e-8
+        fd = (loss(*rollout(sim, x0 + ex * d, v0, T)) - loss(*rollout(sim, x0 - ex * d, v0, T))) / (2 * ex)
+        assert rel(fd, np.sum(gx0 * d)) < 1e-4, ("x", trial, fd, np.sum(gx0 * d))
+
+
+@pytest.mark.parametrize("which", ["triangle", "tet"])
+def test_adjoint_through_strain_limits_matches_the_oracle(which, built_lib):
+    """The GPU's element adjoint (k_adj_elem: its own SVD, svd3.cuh) against the
+    oracle's restatement (one-sided Jacobi SVD; the clamped projection is a
+    spectral function of F, so both give the same derivative to round-off),
+    norm-relative within 1e-6."""
+    from oracle.oracle import FORM_JJ, Oracle
+
+    sc = strained_cloth() if which == "triangle" else tet_scene()
+    kw = dict(cheby_iterations=5, fixed_outer=2)
+    sim = make(sc, **kw)
+    orc = Oracle(sc, "fp64", FORM_JJ, threads=4, **kw)
+    rng = np.random.default_rng(41)
+    n, T = sc.n_sim, 3
+    x0 = sc.initial_positions()
+    v0 = rng.uniform(-0.3, 0.3, (n, 3))
+    gx, gv = rng.normal(size=(n, 3)), rng.normal(size=(n, 3))
+    rollout(sim, x0, v0, T, every=1)
+    ours = sim.adjoint_backward(gx, gv)
+    ref = orc.adjoint_rollout(T, x0, v0, gx, gv)
+    for name, a, b in zip(("x0", "v0"), ours[:2], ref[:2]):
+        assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b), (name, np.linalg.norm(a - b), np.linalg.norm(b))
