@@ -19,7 +19,9 @@ from pdipc.abi import PDIPC_ERR_STATE
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-10, "mixed": 1e-8}
+# mixed: FP32 sums and float atomics of the contact pass in another order; the
+# FP64 form pins the logic to round-off
+TOL = {"fp64": 1e-10, "mixed": 1e-5}
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
