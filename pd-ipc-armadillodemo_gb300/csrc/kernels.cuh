@@ -253,10 +253,12 @@ template <typename T, typename TC>
 void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s);
 template <typename T, typename TC>
 void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s);
-// the outer loop's stopping test on the device (d.Gate must be set): after
-// outer iteration `outer`, stop when test && outer > 0 && Resid < tol
+// the outer loop's stopping test on the device (d.Gate must be set, zeroed at
+// the step's start): after outer iteration k = Gate->iters, stop when
+// test && k > 0 && Resid < tol (the iteration index comes from the device, so
+// the launch is the same in every iteration and can sit in a CUDA graph)
 template <typename T, typename TC>
-void launch_outer_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cudaStream_t s);
+void launch_outer_gate(const Dev<T, TC>& d, double tol, bool test, cudaStream_t s);
 // per-instance stopping: |dir|^2 of every instance into InstResid; after the
 // contact pass, each running instance's test (its iteration count, then
 // stop when test && outer > 0 && InstResid < tol), and the step's record in
@@ -264,7 +266,7 @@ void launch_outer_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cu
 template <typename T, typename TC>
 void launch_inst_resid(const Dev<T, TC>& d, cudaStream_t s);
 template <typename T, typename TC>
-void launch_inst_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cudaStream_t s);
+void launch_inst_gate(const Dev<T, TC>& d, double tol, bool test, cudaStream_t s);
 // correction form: write the float-float mirror (hi, lo; lo may be null) of n
 // positions X, after a host write of X
 template <typename T, typename TC>

@@ -550,8 +550,9 @@ __global__ void k_copy_old(int nsim, const V4<S>* __restrict__ P, V4<S>* __restr
 // cpp:1683-1796: stop once |dir|^2 < tol after the first iteration)
 template <typename TC>
 __global__ void k_outer_gate(OuterGate* __restrict__ g, const double* __restrict__ resid, const TC* __restrict__ toi,
-                             const unsigned long long* __restrict__ active, int outer, double tol, int test) {
+                             const unsigned long long* __restrict__ active, double tol, int test) {
     if (g->stop) return;
+    const int outer = g->iters;  // iterations tested so far: this one's index (graph-invariant)
     const double r = *resid;
     g->resid = r;
     g->iters = outer + 1;
@@ -590,8 +591,9 @@ __global__ void k_inst_resid(const int* __restrict__ beg, const V4<S>* __restric
 template <typename TC>
 __global__ void k_inst_gate(int ninst, unsigned* __restrict__ stop, int* __restrict__ iters,
                             const double* __restrict__ resid, OuterGate* __restrict__ g, const TC* __restrict__ toi,
-                            const unsigned long long* __restrict__ active, int outer, double tol, int test) {
+                            const unsigned long long* __restrict__ active, double tol, int test) {
     if (g->stop) return;
+    const int outer = g->iters;  // read by every thread before thread 0 writes it below
     __shared__ double rsum[kBlock];
     __shared__ int running[kBlock];
     double r = 0.0;
@@ -736,17 +738,17 @@ void launch_copy_old(const Dev<T, TC>& d, cudaStream_t s) {
     k_copy_old<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(d.nsim, d.P, d.Pold, d.Ph, d.Pl, d.Poh, d.Pol, d.Gate);
 }
 template <typename T, typename TC>
-void launch_outer_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cudaStream_t s) {
-    k_outer_gate<TC><<<1, 1, 0, s>>>(d.Gate, d.Resid, d.Toi, d.ActiveCount, outer, tol, test ? 1 : 0);
+void launch_outer_gate(const Dev<T, TC>& d, double tol, bool test, cudaStream_t s) {
+    k_outer_gate<TC><<<1, 1, 0, s>>>(d.Gate, d.Resid, d.Toi, d.ActiveCount, tol, test ? 1 : 0);
 }
 template <typename T, typename TC>
 void launch_inst_resid(const Dev<T, TC>& d, cudaStream_t s) {
     if (d.ninst > 0) k_inst_resid<TC><<<d.ninst, kBlock, 0, s>>>(d.InstBeg, d.Dir, d.InstResid, d.Gate);
 }
 template <typename T, typename TC>
-void launch_inst_gate(const Dev<T, TC>& d, int outer, double tol, bool test, cudaStream_t s) {
+void launch_inst_gate(const Dev<T, TC>& d, double tol, bool test, cudaStream_t s) {
     k_inst_gate<TC><<<1, kBlock, 0, s>>>(d.ninst, d.InstStop, d.InstIters, d.InstResid, d.Gate, d.Toi,
-                                         d.ActiveCount, outer, tol, test ? 1 : 0);
+                                         d.ActiveCount, tol, test ? 1 : 0);
 }
 template <typename T, typename TC>
 void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {
@@ -767,9 +769,9 @@ void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {
     template void launch_direction<T, TC>(const Dev<T, TC>&, cudaStream_t);                                  \
     template void launch_clamp<T, TC>(const Dev<T, TC>&, cudaStream_t);                                      \
     template void launch_copy_old<T, TC>(const Dev<T, TC>&, cudaStream_t);                                   \
-    template void launch_outer_gate<T, TC>(const Dev<T, TC>&, int, double, bool, cudaStream_t);              \
+    template void launch_outer_gate<T, TC>(const Dev<T, TC>&, double, bool, cudaStream_t);                   \
     template void launch_inst_resid<T, TC>(const Dev<T, TC>&, cudaStream_t);                                 \
-    template void launch_inst_gate<T, TC>(const Dev<T, TC>&, int, double, bool, cudaStream_t);               \
+    template void launch_inst_gate<T, TC>(const Dev<T, TC>&, double, bool, cudaStream_t);                    \
     template void launch_split<T, TC>(const Dev<T, TC>&, const V4<TC>*, V4<T>*, V4<T>*, int, cudaStream_t);  \
     template void launch_velocity<T, TC>(const Dev<T, TC>&, TC, cudaStream_t);
 

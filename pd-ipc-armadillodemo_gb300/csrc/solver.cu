@@ -15,6 +15,7 @@
 #include <cstring>
 #include <vector>
 
+#include <array>
 #include <map>
 #include <mutex>
 #include <string>
@@ -1342,6 +1343,12 @@ private:
         return o;
     }
     void release() {
+        for (int p = 0; p < 2; ++p) {
+            if (coll_exec_[p]) cudaGraphExecDestroy(coll_exec_[p]);
+            if (coll_graph_[p]) cudaGraphDestroy(coll_graph_[p]);
+            coll_exec_[p] = nullptr;
+            coll_graph_[p] = nullptr;
+        }
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         if (graph_) cudaGraphDestroy(graph_);
         graph_exec_ = nullptr;
@@ -1980,42 +1987,100 @@ private:
         pdipc_status r = pd_solve(err);
         if (r != PDIPC_OK) return r;
         PD_CK(cudaEventRecord(ev[kEvP1], s_));
-        launch_direction(d, s_);
-        launches_ += 2;
-        const bool inst = d.ninst > 0;
-        if (inst) {
-            launch_inst_resid(d, s_);
-            ++launches_;
+        if (outer > 0 && prm_.use_graphs) {
+            // the collision pass as one graph launch (captured once per step,
+            // after the first iteration's broad phase fixed the candidate lists)
+            r = collision_graph(err);
+            if (r != PDIPC_OK) return r;
+            PD_CK(cudaGraphLaunch(coll_exec_[outer & 1], s_));
+            launches_ += coll_nodes_;
+            return PDIPC_OK;
         }
+        launches_ += coll_head();
         if (outer == 0) {
             r = broadphase(err);
             if (r != PDIPC_OK) return r;
-            if (inst) {  // per-candidate times of impact, reduced per instance
+            if (d.ninst > 0) {  // per-candidate times of impact, reduced per instance
                 PD_CK(grow(instPT_, instPTCap_, std::max<int64_t>(d.nPT, 1)));
                 PD_CK(grow(instEE_, instEECap_, std::max<int64_t>(d.nEE, 1)));
             }
         }
+        int n = 0;
+        r = coll_tail(outer & 1, n, err);
+        launches_ += n;
+        return r;
+    }
+
+    // The collision pass of an outer iteration after its PD solve, in two
+    // parts around the first iteration's broad phase.  Head: the direction
+    // and its residual (per instance too).  Tail: toi pass, clamp, contact
+    // pass, the stopping test on the device with its 16-byte record copied to
+    // pinned memory (slot `parity`), then the copy of the positions into Pold,
+    // which the test skips when it stops the loop.  Nothing in them depends on
+    // the iteration's index beyond its parity (the test reads the index from
+    // the device), so both can be captured in a graph.  Return the kernels
+    // they launch.
+    int coll_head() {
+        launch_direction(d_, s_);
+        if (d_.ninst > 0) launch_inst_resid(d_, s_);
+        return 2 + (d_.ninst > 0);
+    }
+    pdipc_status coll_tail(int parity, int& n, std::string& err) {
+        Dev<T, TC>& d = d_;
+        cudaEvent_t* ev = evo_[parity];
+        const bool inst = d.ninst > 0;
         PD_CK(cudaEventRecord(ev[kEvC0], s_));
         launch_toi(d, pos_old(), pos(), c_, inst ? instPT_ : (TC*)nullptr, inst ? instEE_ : (TC*)nullptr, s_);
         launch_toi_finalize(d, c_, s_);
-        if (inst) {
-            launch_inst_toi(d, instPT_, instEE_, c_, s_);
-            launches_ += 1 + (d.nPT > 0) + (d.nEE > 0);
-        }
+        if (inst) launch_inst_toi(d, instPT_, instEE_, c_, s_);
         PD_CK(cudaEventRecord(ev[kEvC1], s_));
         launch_clamp(d, s_);
         PD_CK(cudaEventRecord(ev[kEvQ0], s_));
         launch_contact(d, pos(), c_, s_);
         PD_CK(cudaEventRecord(ev[kEvQ1], s_));
         if (inst)
-            launch_inst_gate(d, outer, prm_.outer_tol, prm_.fixed_outer <= 0, s_);
+            launch_inst_gate(d, prm_.outer_tol, prm_.fixed_outer <= 0, s_);
         else
-            launch_outer_gate(d, outer, prm_.outer_tol, prm_.fixed_outer <= 0, s_);
-        PD_CK(cudaMemcpyAsync(&pin_->gate[outer & 1], d.Gate, sizeof(OuterGate), cudaMemcpyDeviceToHost, s_));
+            launch_outer_gate(d, prm_.outer_tol, prm_.fixed_outer <= 0, s_);
+        PD_CK(cudaMemcpyAsync(&pin_->gate[parity], d.Gate, sizeof(OuterGate), cudaMemcpyDeviceToHost, s_));
         PD_CK(cudaEventRecord(ev[kEvGate], s_));
         launch_copy_old(d, s_);
-        // toi x2, finalize, clamp, contact clear, contact x2, gate, copy into Pold
-        launches_ += 2 * ((d.nPT > 0) + (d.nEE > 0)) + 5;
+        // toi x2 (+ cubic), finalize, clamp, contact clear, contact x2, gate, copy into Pold
+        n = (1 + (c_.ccd_mode != 0)) * ((d.nPT > 0) + (d.nEE > 0)) + (d.nPT > 0) + (d.nEE > 0) + 5 +
+            (inst ? 1 + (d.nPT > 0) + (d.nEE > 0) : 0);
+        return PDIPC_OK;
+    }
+    // The collision pass (head and tail) captured as a graph per parity of the
+    // outer iteration (the events and the pinned record slot alternate), again
+    // whenever the candidate lists or the buffers they use changed since the
+    // last capture.
+    pdipc_status collision_graph(std::string& err) {
+        const Dev<T, TC>& d = d_;
+        const std::array<const void*, 6> sig{(const void*)d.PT, (const void*)d.EE, (const void*)instPT_,
+                                             (const void*)instEE_, (const void*)(intptr_t)d.nPT,
+                                             (const void*)(intptr_t)d.nEE};
+        if (coll_exec_[0] && sig == coll_sig_) return PDIPC_OK;
+        for (int p = 0; p < 2; ++p) {
+            if (coll_exec_[p]) cudaGraphExecDestroy(coll_exec_[p]);
+            if (coll_graph_[p]) cudaGraphDestroy(coll_graph_[p]);
+            coll_exec_[p] = nullptr;
+            coll_graph_[p] = nullptr;
+            PD_CK(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
+            int n = coll_head();
+            int m = 0;
+            pdipc_status r = coll_tail(p, m, err);
+            cudaGraph_t g = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(s_, &g);
+            if (r != PDIPC_OK) {
+                if (g) cudaGraphDestroy(g);
+                return r;
+            }
+            PD_CK(ce);
+            coll_graph_[p] = g;
+            PD_CK(cudaGraphInstantiate(&coll_exec_[p], g, 0));
+            coll_nodes_ = n + m;
+        }
+        coll_sig_ = sig;
         return PDIPC_OK;
     }
 
@@ -2197,6 +2262,11 @@ private:
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;
     int graph_nodes_ = 0;
+    // the collision pass of outer iterations 1, 2, ... as a graph per parity
+    cudaGraph_t coll_graph_[2] = {};
+    cudaGraphExec_t coll_exec_[2] = {};
+    std::array<const void*, 6> coll_sig_{};
+    int coll_nodes_ = 0;
     bool inited_ = false;
     pdipc_stats st_{};
     // per-instance stopping: per-candidate times of impact and the instances' counts
