@@ -2025,25 +2025,28 @@ private:
         if (d_.ninst > 0) launch_inst_resid(d_, s_);
         return 2 + (d_.ninst > 0);
     }
-    pdipc_status coll_tail(int parity, int& n, std::string& err) {
+    pdipc_status coll_tail(int parity, int& n, std::string& err, bool capturing = false) {
         Dev<T, TC>& d = d_;
         cudaEvent_t* ev = evo_[parity];
         const bool inst = d.ninst > 0;
-        PD_CK(cudaEventRecord(ev[kEvC0], s_));
+        // in a capture, an event record becomes a graph node only when external
+        // (the host synchronises on these events after each launch)
+        const unsigned rf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+        PD_CK(cudaEventRecordWithFlags(ev[kEvC0], s_, rf));
         launch_toi(d, pos_old(), pos(), c_, inst ? instPT_ : (TC*)nullptr, inst ? instEE_ : (TC*)nullptr, s_);
         launch_toi_finalize(d, c_, s_);
         if (inst) launch_inst_toi(d, instPT_, instEE_, c_, s_);
-        PD_CK(cudaEventRecord(ev[kEvC1], s_));
+        PD_CK(cudaEventRecordWithFlags(ev[kEvC1], s_, rf));
         launch_clamp(d, s_);
-        PD_CK(cudaEventRecord(ev[kEvQ0], s_));
+        PD_CK(cudaEventRecordWithFlags(ev[kEvQ0], s_, rf));
         launch_contact(d, pos(), c_, s_);
-        PD_CK(cudaEventRecord(ev[kEvQ1], s_));
+        PD_CK(cudaEventRecordWithFlags(ev[kEvQ1], s_, rf));
         if (inst)
             launch_inst_gate(d, prm_.outer_tol, prm_.fixed_outer <= 0, s_);
         else
             launch_outer_gate(d, prm_.outer_tol, prm_.fixed_outer <= 0, s_);
         PD_CK(cudaMemcpyAsync(&pin_->gate[parity], d.Gate, sizeof(OuterGate), cudaMemcpyDeviceToHost, s_));
-        PD_CK(cudaEventRecord(ev[kEvGate], s_));
+        PD_CK(cudaEventRecordWithFlags(ev[kEvGate], s_, rf));
         launch_copy_old(d, s_);
         // toi x2 (+ cubic), finalize, clamp, contact clear, contact x2, gate, copy into Pold
         n = (1 + (c_.ccd_mode != 0)) * ((d.nPT > 0) + (d.nEE > 0)) + (d.nPT > 0) + (d.nEE > 0) + 5 +
@@ -2068,7 +2071,7 @@ private:
             PD_CK(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
             int n = coll_head();
             int m = 0;
-            pdipc_status r = coll_tail(p, m, err);
+            pdipc_status r = coll_tail(p, m, err, true);
             cudaGraph_t g = nullptr;
             const cudaError_t ce = cudaStreamEndCapture(s_, &g);
             if (r != PDIPC_OK) {
