@@ -107,10 +107,7 @@ typedef struct {
                                 its step by its own time of impact, and the step ends when every model has
                                 stopped (or at max_outer).  A model that has stopped skips its sweeps.  Models
                                 that touch one another should keep 0.  Runs the per-sweep PD solve. */
-    int local_split;         /* mixed mode, per-sweep PD solve: the local residual with one thread per row (0)
-                                or two (1: the matrix sum on the second); -1 (default): the autotuner's
-                                choice, 0 without autotuning */
-    int reserved[1];
+    int reserved[2];
 } pdipc_params;
 
 /* Per-context statistics of the most recent pdipc_step call. */
@@ -170,7 +167,7 @@ typedef struct {
     int32_t traverse_block;     /* threads per block of the broad-phase traversal */
     int32_t expand_block;       /* threads per block of the candidate expansion */
     int32_t candidates_timed;   /* configurations the autotuner timed */
-    int32_t local_split;        /* mixed mode's per-sweep local residual: 1 two threads per row */
+    int32_t reserved0;
     double pd_solve_ms;         /* one outer iteration's PD solve, chosen configuration (0: not timed) */
     double pd_default_ms;       /* the same with the default configuration */
     double collision_ms;        /* broad phase + time of impact + contact, chosen shapes */

@@ -147,7 +147,6 @@ void pdipc_default_params(pdipc_params* p) {
     p->device = 0;
     p->rebuild_bvh = 0;
     p->persistent = 1;
-    p->local_split = -1;
 }
 
 const char* pdipc_status_string(pdipc_status s) {

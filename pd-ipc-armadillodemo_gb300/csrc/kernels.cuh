@@ -214,8 +214,6 @@ struct SolverConsts {
     int cand_grid = 152 * 16;
     int trav_block = 128;
     int expand_block = 256;
-    // the per-sweep path's local residual: 1 two threads per row (matrix sum apart)
-    int local_split = 0;
     // 1: after the additive CCD, the FP64 coplanarity-cubic pass (pdipc_params.ccd_mode)
     int ccd_mode = 0;
 };
@@ -241,7 +239,7 @@ void launch_sweep(const Dev<T, TC>& d, const V4<T>* src, const V4<T>* prev, V4<T
 // residual r0 = b - A x from relative coordinates (compensated FP32 sums) into Rhs
 // and the first sweep from delta = 0 into Y.
 template <typename T, typename TC>
-void launch_local_residual(const Dev<T, TC>& d, T relax, bool split, cudaStream_t s);
+void launch_local_residual(const Dev<T, TC>& d, T relax, cudaStream_t s);
 // sweep on the correction: mode bits 1 Chebyshev, 2 the previous iterate is
 // zero, 4 the result is added to the positions P instead of written to out.
 template <typename T, typename TC>

@@ -305,11 +305,7 @@ __global__ void __launch_bounds__(kBlock) k_sweep(int nsim, T relax, T omega, co
 // delta = 0: Y = w r0 / D.  Positions are FP64 (S): the vertex's own terms
 // subtract in FP64 once, the neighbour differences come from the float-float
 // mirror (Ph, Pl) in FP32; each enters the FP32 arithmetic as about one rounding.
-// kSplit: two threads per row (rows blockIdx.x * kBlock / 2 + threadIdx.x / 2):
-// the even thread takes every term but the matrix sum, the odd one the matrix
-// sum, so each row's two longest chains of dependent gathers run side by side;
-// the odd thread's compensated sums join the even thread's by shuffles.
-template <typename T, typename S, bool kSplit>
+template <typename T, typename S>
 __global__ void __launch_bounds__(kBlock) k_local_residual(
     int nsim, T relax, const V4<S>* __restrict__ P, const V4<T>* __restrict__ Ph, const V4<T>* __restrict__ Pl,
     const V4<S>* __restrict__ Pold, const V4<S>* __restrict__ Xrest,
@@ -321,14 +317,10 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
     const V4<T>* __restrict__ Aq, const T* __restrict__ InvD,
     const Sell<T> M, const int* __restrict__ vtPtr, const int* __restrict__ vtIdx,
     const V4<T>* __restrict__ TetOut, V4<T>* __restrict__ Rhs, V4<T>* __restrict__ Y, const RowSkip skip) {
-    const int i = kSplit ? blockIdx.x * (blockDim.x >> 1) + (threadIdx.x >> 1) : blockIdx.x * blockDim.x + threadIdx.x;
-    const bool part1 = kSplit && (threadIdx.x & 1);  // the matrix sum of a split row
-    const bool live = i < nsim && !skip(i);
-    if (!kSplit && !live) return;
-    Sum2 r0, r1, r2;
-    const V4<T> h = live ? ld4(Ph, i) : V4<T>{}, l = live ? ld4(Pl, i) : V4<T>{};
-    if (live && !part1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsim || skip(i)) return;
     const V4<S> x = ld4(P, i);
+    Sum2 r0, r1, r2;
     {   // inertia
         const V4<S> y = ld4(Ypred, i);
         const T di = __ldg(Dinert + i);
@@ -357,6 +349,7 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
     }
     const int2 st = stencil_of(i, lPtr, tOff);
     const T strain = __ldg(Strain + i);
+    const V4<T> h = ld4(Ph, i), l = ld4(Pl, i);
     for (int k = 0; k < st.y; ++k) {  // mass-spring projections
         const int s = st.x + kSlice * k;
         const int j = __ldg(tNbr + s);
@@ -391,8 +384,7 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
             r1.add(t.y);
             r2.add(t.z);
         }
-    }
-    if (live && (!kSplit || part1)) {   // sum_j N_ij (x_j - x_i)
+    {   // sum_j N_ij (x_j - x_i)
         const int sl = i >> 5, lane = i & 31;
         const int base = __ldg(M.off + sl) + lane;
         const int len = __ldg(M.len + sl);
@@ -406,19 +398,6 @@ __global__ void __launch_bounds__(kBlock) k_local_residual(
             r1.add(v * diff_ff(hj.y, lj.y, h.y, l.y));
             r2.add(v * diff_ff(hj.z, lj.z, h.z, l.z));
         }
-    }
-    if constexpr (kSplit) {  // the matrix sum joins the row's other terms
-        const float m[6] = {r0.s, r0.c, r1.s, r1.c, r2.s, r2.c};
-        float o[6];
-#pragma unroll
-        for (int q = 0; q < 6; ++q) o[q] = __shfl_down_sync(0xffffffffu, m[q], 1);
-        if (part1 || !live) return;
-        r0.add(o[0]);
-        r0.add(o[1]);
-        r1.add(o[2]);
-        r1.add(o[3]);
-        r2.add(o[4]);
-        r2.add(o[5]);
     }
     const T f0 = r0.value(), f1 = r1.value(), f2 = r2.value();
     Rhs[i] = V4<T>{f0, f1, f2, T(0)};
@@ -690,18 +669,12 @@ void launch_local_aq(const Dev<T, TC>& d, cudaStream_t s) {
                                                             d.CurvNorm, d.Aq, skip_of(d));
 }
 template <typename T, typename TC>
-void launch_local_residual(const Dev<T, TC>& d, T relax, bool split, cudaStream_t s) {
+void launch_local_residual(const Dev<T, TC>& d, T relax, cudaStream_t s) {
     if constexpr (kMirror<T, TC>) {
-        auto go = [&](auto kernel, int blocks) {
-            kernel<<<blocks, kBlock, 0, s>>>(d.nsim, relax, d.P, d.Ph, d.Pl, d.Pold, d.Xrest, d.Rhs0, d.Dinert,
-                                             d.CollDiag, d.CollRhs, d.PinFlag, d.PinK, d.lPtr, d.tOff, d.tNbr,
-                                             d.tRest, d.tBend0, d.tBendT, d.Strain, d.Aq, d.InvD, sell_of(d),
-                                             d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs, d.Y, skip_of(d));
-        };
-        if (split)
-            go(k_local_residual<T, TC, true>, blocks_for(d.nsim, kBlock / 2));
-        else
-            go(k_local_residual<T, TC, false>, blocks_for(d.nsim));
+        k_local_residual<T, TC><<<blocks_for(d.nsim), kBlock, 0, s>>>(
+            d.nsim, relax, d.P, d.Ph, d.Pl, d.Pold, d.Xrest, d.Rhs0, d.Dinert, d.CollDiag, d.CollRhs, d.PinFlag,
+            d.PinK, d.lPtr, d.tOff, d.tNbr, d.tRest, d.tBend0, d.tBendT, d.Strain, d.Aq, d.InvD, sell_of(d), d.ntet ? d.vtPtr : nullptr, d.vtIdx, d.TetOut, d.Rhs, d.Y,
+            skip_of(d));
     }
 }
 template <typename T, typename TC>
@@ -788,7 +761,7 @@ void launch_velocity(const Dev<T, TC>& d, TC invt, cudaStream_t s) {
     template void launch_tet_project<T, TC>(const Dev<T, TC>&, cudaStream_t);                                \
     template void launch_local_aq<T, TC>(const Dev<T, TC>&, cudaStream_t);                                   \
     template void launch_local_rhs_sweep<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                         \
-    template void launch_local_residual<T, TC>(const Dev<T, TC>&, T, bool, cudaStream_t);                    \
+    template void launch_local_residual<T, TC>(const Dev<T, TC>&, T, cudaStream_t);                          \
     template void launch_sweep_delta<T, TC>(const Dev<T, TC>&, int, const V4<T>*, const V4<T>*, V4<T>*, T, T, \
                                             cudaStream_t);                                                   \
     template void launch_sweep<T, TC>(const Dev<T, TC>&, const V4<T>*, const V4<T>*, V4<T>*, T, T,           \

@@ -109,11 +109,6 @@ public:
             return PDIPC_ERR_ARG;
         }
         c_.ccd_mode = p.ccd_mode;
-        if (p.local_split < -1 || p.local_split > 1) {
-            err = "local_split must be -1 (the autotuner's choice), 0 or 1";
-            return PDIPC_ERR_ARG;
-        }
-        c_.local_split = p.local_split < 0 ? 0 : p.local_split;
         {
             int khz = 0;
             PD_CK(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, p.device));
@@ -416,7 +411,7 @@ private:
     // ---------------- autotuner ----------------
     struct Tuned {
         PlanChoice pd;
-        int cand_grid, trav_block, expand_block, local_split;
+        int cand_grid, trav_block, expand_block;
     };
 
     void fill_tuning_record() {
@@ -428,7 +423,6 @@ private:
         tuning_.cand_grid = c_.cand_grid;
         tuning_.traverse_block = c_.trav_block;
         tuning_.expand_block = c_.expand_block;
-        tuning_.local_split = c_.local_split;
     }
 
     PlanChoice current_choice() const {
@@ -522,7 +516,7 @@ private:
                                 std::to_string(d_.npatch) + "/" + std::to_string(sell_entries_) + "/" +
                                 std::to_string(c_.lg) + "/" + std::to_string(c_.cheby) + "/" +
                                 std::to_string(prm_.persistent) + "/" + std::to_string(d_.ntet);
-        Tuned best{current_choice(), c_.cand_grid, c_.trav_block, c_.expand_block, c_.local_split};
+        Tuned best{current_choice(), c_.cand_grid, c_.trav_block, c_.expand_block};
         bool cached = false;
         {
             std::lock_guard<std::mutex> g(mu);
@@ -539,7 +533,6 @@ private:
             c_.cand_grid = best.cand_grid;
             c_.trav_block = best.trav_block;
             c_.expand_block = best.expand_block;
-            c_.local_split = best.local_split;
             fill_tuning_record();
             tuning_.autotuned = 1;
             tuning_.from_cache = 1;
@@ -627,22 +620,6 @@ private:
         c_.trav_block = best.trav_block;
         c_.expand_block = best.expand_block;
         tuning_.collision_ms = collBest;
-        // ---- the per-sweep path's local residual: one or two threads per row ----
-        if (kCorrection && prm_.local_split < 0) {
-            float lbest = -1.f;
-            for (int sp = 0; sp < 2; ++sp) {
-                c_.local_split = sp;
-                double ms = 0.0, bytes = 0.0;
-                r = local_timing(50, &ms, &bytes, err);
-                if (r != PDIPC_OK) return r;
-                ++tuning_.candidates_timed;
-                if (lbest < 0.f || ms < lbest) {
-                    lbest = (float)ms;
-                    best.local_split = sp;
-                }
-            }
-            c_.local_split = best.local_split;
-        }
         // ---- the state as it was ----
         PD_CK(cudaMemcpyAsync(d_.P, saveP, sizeof(V4<TC>) * ns, cudaMemcpyDeviceToDevice, s_));
         PD_CK(cudaMemcpyAsync(d_.Vel, saveV, sizeof(V4<TC>) * ns, cudaMemcpyDeviceToDevice, s_));
@@ -1031,7 +1008,7 @@ public:
         const T w = (T)c_.relax;
         auto once = [&]() {
             launch_local_aq(d_, s_);
-            if constexpr (kCorrection) launch_local_residual(d_, w, c_.local_split != 0, s_);
+            if constexpr (kCorrection) launch_local_residual(d_, w, s_);
             else launch_local_rhs_sweep(d_, w, s_);
         };
         launch_diag(d_, s_);
@@ -1920,7 +1897,7 @@ private:
             launch_local_aq(d, s_);
             launch_tet_project(d, s_);
             k += d.ntet > 0;
-            launch_local_residual(d, w, c_.local_split != 0, s_);
+            launch_local_residual(d, w, s_);
             launch_sweep_delta<T, TC>(d, c_.cheby == 1 ? 4 : 0, d.Y, nullptr, d.B, w, T(0), s_);
             k += 3;
             T om = omega_first(rho2);

@@ -55,8 +55,7 @@ class Params(C.Structure):
         ("autotune", C.c_int),
         ("ccd_mode", C.c_int),
         ("instance_stop", C.c_int),
-        ("local_split", C.c_int),
-        ("reserved", C.c_int * 1),
+        ("reserved", C.c_int * 2),
     ]
 
 
@@ -85,7 +84,6 @@ def default_params() -> Params:
     p.device = 0
     p.rebuild_bvh = 0
     p.persistent = 1
-    p.local_split = -1
     return p
 
 
@@ -179,7 +177,7 @@ class Tuning(C.Structure):
         ("traverse_block", C.c_int32),
         ("expand_block", C.c_int32),
         ("candidates_timed", C.c_int32),
-        ("local_split", C.c_int32),
+        ("reserved0", C.c_int32),
         ("pd_solve_ms", C.c_double),
         ("pd_default_ms", C.c_double),
         ("collision_ms", C.c_double),

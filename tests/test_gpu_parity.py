@@ -305,20 +305,3 @@ def test_animate_returns_positions_and_counts_launches(built_lib):
     assert out.shape == (sc.n_total, 3) and np.isfinite(out).all()
     st = sim.stats()
     assert st["kernel_launches"] > 10 and st["steps_done"] == 1
-
-
-@pytest.mark.parametrize("n", [37, 96])
-def test_local_residual_split_matches_one_thread_per_row(n, built_lib):
-    """The per-sweep path's local residual with two threads per row (the matrix
-    sum on the second, its compensated sums joined by shuffles) gives the PD
-    solve and the steps of the one-thread form to FP32 rounding of the
-    correction (the mixed mode)."""
-    sc = small_scene(n, 2)
-    a = pdipc.Simulator(sc, "mixed", persistent=0, local_split=0)
-    b = pdipc.Simulator(sc, "mixed", persistent=0, local_split=1)
-    X = np.concatenate([c.X for c in sc.cloths] + [s.X for s in sc.statics])
-    V = np.random.default_rng(9).uniform(-0.1, 0.1, (sc.n_sim, 3))
-    assert np.abs(a.stage_pd(X, V) - b.stage_pd(X, V)).max() < 1e-8
-    a.step(4)
-    b.step(4)
-    assert np.abs(a.positions() - b.positions()).max() < 1e-6
