@@ -447,10 +447,18 @@ def run_ours(args):
             g32.step(1)
             ms32 += g32.stats()["device_ms"]
             outers32.append(g32.stats()["last_outer_iters"])
+        # the local step of the per-sweep path in the reference's arithmetic (FP32
+        # state: the algorithmic bytes' sizes), timed alone like local_alone
+        lms32, lb32 = g32.local_timing(400)
+        pk, _ = measured_peak_hbm()
         fp32 = {"value": round(k32 / (ms32 * 1e-3), 4), "unit": UNIT, "steps": k32,
                 "ms_per_step": round(ms32 / k32, 3),
                 "outer_iterations_per_step": {"mean": float(np.mean(outers32)), "max": int(max(outers32))},
-                "ms_per_outer_iteration": round(ms32 / max(sum(outers32), 1), 4)}
+                "ms_per_outer_iteration": round(ms32 / max(sum(outers32), 1), 4),
+                "local_alone": {"kernel": "k_local_aq + k_local_rhs_sweep (FP32 state), 400 back to back",
+                                "bytes_per_launch": lb32, "ms_per_launch": round(lms32, 6),
+                                "achieved": round(lb32 / (lms32 * 1e-3) / 1e9, 1),
+                                "frac": round(lb32 / (lms32 * 1e-3) / 1e9 / pk, 4)}}
         g32.close()
         del g32
 
