@@ -309,11 +309,13 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     // consecutive; the band path's last warp has no rows ----
     // pk[r] packs the row's entry count (bits 0-9) and, on the band path, the
     // bounds of its entries on own rows (bits 10-19, 20-29).  slotof(r) is the
-    // row's slot (iterates, band), rowof(r) the row itself (state arrays).
+    // row's slot (its place in the matrix slices), rowof(r) the row itself
+    // (state arrays), itof(r) = swz(rowof(r)) its place in the iterates and the band.
     const int nrw = (int)(blockDim.x >> 5) - (band ? 1 : 0);
     const int slot0 = (a.ctaSlice[cta] + warp * R) * 32 + lane;
     auto slotof = [&](int r) { return slot0 + 32 * r; };
     auto rowof = [&](int r) { return row_of(slot0 + 32 * r); };
+    auto itof = [&](int r) { return swz(row_of(slot0 + 32 * r)); };
     int gb[R], pk[R], pid[R];
     bool val[R];
 #pragma unroll
@@ -359,7 +361,8 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     // thread writes its rows' new values there.  The halo, slots
     // [brange.x, own0) and [own1, brange.y), is copied from global memory in
     // two bulk copies once the neighbours have published it.  A CTA owns whole
-    // 64-row windows, so a row j is one of its own exactly when slot_of(j) is.
+    // 64-row windows (which swz maps onto themselves), so the own and halo
+    // ranges are the same in rows and in the iterates' swizzled order.
     const int own0 = a.ctaSlice[cta] * 32, own1 = min(a.ctaSlice[cta + 1] * 32, a.nslot);
     const int nlo = band ? own0 - brange.x : 0, nhi = band ? brange.y - own1 : 0;
     // The band path runs one extra warp, the last, with no rows: it publishes
@@ -470,14 +473,17 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
         }
         pk[r] |= (b << 10) | (e << 20);
     }
-    // entries [k0, k1) of owned row r against the band
+    // entries [k0, k1) of owned row r against the band (band path: values in
+    // shared memory, offsets from parameter space); brange.x is a multiple of
+    // 64, so swz(j) - brange.x = swz(j - brange.x)
     auto band_sum = [&](int r, int k0, int k1, T& s0, T& s1, T& s2) {
+        const int rb = rowof(r) - brange.x;
+        const T* vp = sval + (gb[r] - eb);
+        const int16_t* pp = a.patc + pid[r];
 #pragma unroll 8
         for (int k = k0; k < k1; ++k) {
-            T v;
-            int j;
-            entry(r, k, v, j);
-            const int q = slot_of(j) - brange.x;
+            const T v = vp[32 * k];
+            const int q = swz(rb + (int)pp[k]);
             s0 += v * bx[q];
             s1 += v * by[q];
             s2 += v * bz[q];
@@ -521,7 +527,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
             T v;
             int j;
             entry(r, k, v, j);
-            const V4<T> xj = ldv<kL1>(src, slots ? slot_of(j) : j);
+            const V4<T> xj = ldv<kL1>(src, slots ? swz(j) : j);
             s0 += v * xj.x;
             s1 += v * xj.y;
             s2 += v * xj.z;
@@ -728,7 +734,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
             y[0] = om1 * c[0] + w * ((s0 + rh[r][0]) * id[r]);
             y[1] = om1 * c[1] + w * ((s1 + rh[r][1]) * id[r]);
             y[2] = om1 * c[2] + w * ((s2 + rh[r][2]) * id[r]);
-            if (val[r]) st_it(a.GY, slotof(r), y[0], y[1], y[2]);
+            if (val[r]) st_it(a.GY, itof(r), y[0], y[1], y[2]);
         };
         // second sweep of step it: S(y), Chebyshev-combined with the previous
         // second-sweep iterate p except for the first step; the last one
@@ -760,7 +766,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     stcg4(a.P, rowof(r), n[0], n[1], n[2]);
                 }
             } else {
-                st_it(xout, slotof(r), n[0], n[1], n[2]);
+                st_it(xout, itof(r), n[0], n[1], n[2]);
             }
         };
         const int nsteps = a.cheby;
@@ -783,7 +789,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                 }
             };
             auto own_slot = [&](int r, T (&c)[3]) {
-                const int q = val[r] ? slotof(r) - brange.x : 0;
+                const int q = val[r] ? itof(r) - brange.x : 0;
                 c[0] = bx[q];
                 c[1] = by[q];
                 c[2] = bz[q];
@@ -792,7 +798,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
 #pragma unroll
                 for (int r = 0; r < R; ++r)
                     if (val[r]) {
-                        const int q = slotof(r) - brange.x;
+                        const int q = itof(r) - brange.x;
                         bx[q] = nv[r][0];
                         by[q] = nv[r][1];
                         bz[q] = nv[r][2];
@@ -833,7 +839,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                 const T zero[3] = {T(0), T(0), T(0)};
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    if (val[r]) st_it(a.GX2, slotof(r), T(0), T(0), T(0));
+                    if (val[r]) st_it(a.GX2, itof(r), T(0), T(0), T(0));
                     finish_y(r, T(0), T(0), T(0), zero, nv[r]);
                 }
             }
@@ -850,7 +856,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                     for (int r = 0; r < R; ++r) {
                         p[r][0] = p[r][1] = p[r][2] = T(0);
                         if (it > 0 && val[r]) {
-                            const V4<T> g = ld_it(xb, slotof(r));
+                            const V4<T> g = ld_it(xb, itof(r));
                             p[r][0] = g.x;
                             p[r][1] = g.y;
                             p[r][2] = g.z;

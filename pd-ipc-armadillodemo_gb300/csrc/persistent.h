@@ -19,16 +19,20 @@ constexpr int kParamPatterns = 4096;
 
 // Slot order of the persistent solve: in every window of 64 rows, its 32 even
 // rows, then its 32 odd rows (a fixed bijection of [0, 64 ceil(n / 64))).  The
-// iterates, the matrix slices and the band in shared memory are kept in slot
-// order; the state arrays stay in row (vertex) order.  A structured triangle
-// mesh whose quads alternate their diagonal has two stencil shapes that
-// alternate with the row parity: in slot order the 32 rows of a warp share one
-// shape, so a warp's k-th entries read 32 consecutive slots (no shared-memory
-// bank conflicts) and its column offsets are one constant-cache address.
+// matrix slices and the rows' assignment to threads follow slot order, so the
+// 32 rows of a warp are the even or the odd rows of one window.  A structured
+// triangle mesh whose quads alternate their diagonal has two stencil shapes
+// that alternate with the row parity: in slot order a warp's rows share one
+// shape, so its column offsets are one constant-cache address and its k-th
+// entries read rows two apart.  The iterates and the band in shared memory are
+// in row order with swz applied: bit 0 of every row in an odd 32-row block is
+// flipped, so 32 rows two apart (spanning two or three 32-row blocks) fall in
+// 32 distinct shared-memory banks.  swz maps every 64-row window onto itself.
 __host__ __device__ __forceinline__ int slot_of(int row) { return (row & ~63) | ((row & 1) << 5) | ((row >> 1) & 31); }
 __host__ __device__ __forceinline__ int row_of(int slot) {
     return (slot & ~63) | ((slot >> 5) & 1) | ((slot & 31) << 1);
 }
+__host__ __device__ __forceinline__ int swz(int row) { return row ^ ((row >> 5) & 1); }
 
 // One configuration of the persistent solve, as the autotuner names it.
 struct PlanChoice {
@@ -75,9 +79,9 @@ struct PersistArgs {
     const V4<T>* CollRhs;
     const V4<T>* PinRhs;
     V4<T>* Aq;
-    V4<T>* GX;   // second-sweep iterates (odd steps in GX2 on the band path), slot order [nslot]
+    V4<T>* GX;   // second-sweep iterates (odd steps in GX2 on the band path), at swz(row) [nslot]
     V4<T>* GX2;
-    V4<T>* GY;   // first-sweep iterates, slot order [nslot]
+    V4<T>* GY;   // first-sweep iterates, at swz(row) [nslot]
     const T* Delastic;
     const T* Dinert;
     const T* CollDiag;
@@ -133,7 +137,7 @@ struct PersistArgs {
     const int2* nbr;
     unsigned epoch0;
     // band of the iterate in shared memory (band != null, matrix in shared
-    // memory, neighbour synchronisation): CTA c's matrix rows read the slots
+    // memory, neighbour synchronisation): CTA c's matrix rows read the rows
     // [band[c].x, band[c].y) (whole 64-row windows).  Its own rows stay in three planar arrays of
     // ownMax floats that its threads update after every sweep; the halo (the
     // columns outside its own rows, at most haloMax vertices) is copied from
