@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PDIPC_ABI_VERSION 8
+#define PDIPC_ABI_VERSION 9
 
 typedef struct pdipc_ctx pdipc_ctx;
 
@@ -106,8 +106,13 @@ typedef struct {
                                 simulated model: each model stops on its own |dx|^2 < outer_tol and clamps
                                 its step by its own time of impact, and the step ends when every model has
                                 stopped (or at max_outer).  A model that has stopped skips its sweeps.  Models
-                                that touch one another should keep 0.  Runs the per-sweep PD solve. */
-    int reserved[2];
+                                that touch one another should keep 0.  A stopped model's rows leave the
+                                persistent PD solve (its CTAs return at entry when all their rows have
+                                stopped). */
+    int pd_group_ctas;       /* persistent PD solve: at most this many CTAs per launch (0: every CTA the
+                                device holds at once).  A plan with more CTAs runs as one launch per group
+                                of whole models (models share no matrix entry), in order. */
+    int reserved[1];
 } pdipc_params;
 
 /* Per-context statistics of the most recent pdipc_step call. */
@@ -167,7 +172,7 @@ typedef struct {
     int32_t traverse_block;     /* threads per block of the broad-phase traversal */
     int32_t expand_block;       /* threads per block of the candidate expansion */
     int32_t candidates_timed;   /* configurations the autotuner timed */
-    int32_t reserved0;
+    int32_t pd_launches;        /* launches of one persistent PD solve (groups of whole models) */
     double pd_solve_ms;         /* one outer iteration's PD solve, chosen configuration (0: not timed) */
     double pd_default_ms;       /* the same with the default configuration */
     double collision_ms;        /* broad phase + time of impact + contact, chosen shapes */

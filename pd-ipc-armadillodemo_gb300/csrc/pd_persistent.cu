@@ -258,6 +258,30 @@ __device__ __noinline__ void tet_project_one(int e, const int4* __restrict__ Tet
     for (int c = 0; c < 4; ++c) __stcg(reinterpret_cast<float4*>(Out) + 4 * (size_t)e + c, make_float4(out[c][0], out[c][1], out[c][2], 0.f));
 }
 
+// A CTA without rows to update in a launch (rows of other groups, or of
+// stopped instances; the rule of row_valid in k_pd_persistent) takes no part:
+// with neighbour synchronisation it publishes the launch's last phase at once
+// (its rows are read by no row that is updated) and returns.  Out of line, so
+// that the solve's register allocation does not carry it.
+template <typename T, typename S, int R>
+__device__ __noinline__ bool cta_idle(const PersistArgs<T, S>& a, int cta, int nrw) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    bool any = false;
+    for (int r = 0; r < R; ++r) {
+        const int s = a.ctaSlice[cta] + warp * R + r;
+        if (warp >= nrw || s >= a.ctaSlice[cta + 1]) continue;
+        const int row = row_of(s * 32 + lane);
+        any = any || (row >= a.row0 && row < a.row1 && row < a.nsim &&
+                      !(a.instStop && __ldg(a.instStop + __ldg(a.vInst + row))));
+    }
+    if (__syncthreads_or(any) || !a.nbr) return false;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        st_release_gpu(a.flags + cta, a.epoch0 + a.nphases);
+    }
+    return true;
+}
+
 // S is the state scalar: T in the direct form, double in the correction form,
 // where positions enter the FP32 arithmetic as differences formed from their
 // float-float mirror (Ph, Pl): no FP64 arithmetic in the per-neighbour loops.
@@ -276,8 +300,20 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     // its first phase; flags and barrier counters stay as they are (the next
     // launch's phase numbers lie above them all the same)
     if (outer_stopped(a.gate)) return;
-    const int cta = blockIdx.x;
+    const int cta = (int)blockIdx.x + a.ctaLo;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // Row r of this thread (slice ctaSlice[cta] + warp R + r, lane) is
+    // updated in this launch when it is simulated, in [row0, row1) and its
+    // instance has not stopped.
+    const int nrw = (int)(blockDim.x >> 5) - (band ? 1 : 0);
+    auto row_valid = [&](int r) -> bool {
+        const int s = a.ctaSlice[cta] + warp * R + r;
+        if (warp >= nrw || s >= a.ctaSlice[cta + 1]) return false;
+        const int row = row_of(s * 32 + lane);
+        return row >= a.row0 && row < a.row1 && row < a.nsim &&
+               !(a.instStop && __ldg(a.instStop + __ldg(a.vInst + row)));
+    };
+    if (cta_idle<T, S, R>(a, cta, nrw)) return;
     // ---- this CTA's matrix values and the offset patterns into shared memory ----
     const int eb = a.ctaEntry[cta], ee = a.ctaEntry[cta + 1];
     const int E = ee - eb;
@@ -311,7 +347,6 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     // bounds of its entries on own rows (bits 10-19, 20-29).  slotof(r) is the
     // row's slot (its place in the matrix slices), rowof(r) the row itself
     // (state arrays), itof(r) = swz(rowof(r)) its place in the iterates and the band.
-    const int nrw = (int)(blockDim.x >> 5) - (band ? 1 : 0);
     const int slot0 = (a.ctaSlice[cta] + warp * R) * 32 + lane;
     auto slotof = [&](int r) { return slot0 + 32 * r; };
     auto rowof = [&](int r) { return row_of(slot0 + 32 * r); };
@@ -322,7 +357,7 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     for (int r = 0; r < R; ++r) {
         const int s = a.ctaSlice[cta] + warp * R + r;
         const bool sv = warp < nrw && s < a.ctaSlice[cta + 1];
-        val[r] = sv && rowof(r) < a.nsim;
+        val[r] = row_valid(r);
         gb[r] = sv ? a.sliceEntry[s] + lane : 0;
         pk[r] = sv ? a.sliceLen[s] : 0;
         pid[r] = (kSmem && val[r]) ? a.rowPattern[rowof(r)] * a.patW : 0;
@@ -343,7 +378,11 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
     __syncthreads();
     unsigned my_gen = 0;
     if (threadIdx.x == 0) my_gen = ld_acquire_gpu(a.bar);
-    const int2 nrange = a.nbr ? a.nbr[cta] : make_int2(0, -1);
+    // the neighbours within this launch's group (the instances of its rows lie inside it)
+    const int2 nrange = [&]() {
+        const int2 n = a.nbr ? a.nbr[cta] : make_int2(0, -1);
+        return make_int2(max(n.x, a.ctaLo), min(n.y, a.ctaHi));
+    }();
     unsigned epoch = a.epoch0;
     // end of a phase: neighbour synchronisation or the grid barrier
     auto sync = [&]() -> bool {
@@ -985,7 +1024,9 @@ cudaError_t launch_args(const PersistPlan& plan, const PersistArgs<float, S>& ar
                                       plan.rows_per_thread, args.ntet > 0);
     if (!f) return cudaErrorInvalidConfiguration;
     void* params[] = {(void*)&args};
-    return cudaLaunchCooperativeKernel(f, dim3(plan.ctas), dim3(plan.threads), params, plan.smem_bytes, s);
+    const int grid = args.ctaHi - args.ctaLo + 1;
+    if (grid < 1 || args.ctaLo < 0 || args.ctaHi >= plan.ctas) return cudaErrorInvalidConfiguration;
+    return cudaLaunchCooperativeKernel(f, dim3(grid), dim3(plan.threads), params, plan.smem_bytes, s);
 }
 
 cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, float>& args, cudaStream_t s) {

@@ -42,6 +42,12 @@ struct PlanChoice {
     bool local_sync = true;
 };
 
+// A launch of the plan: CTAs [cta_lo, cta_hi], rows [row0, row1).
+struct PersistGroup {
+    int cta_lo = 0, cta_hi = -1;
+    int row0 = 0, row1 = 0;
+};
+
 struct PersistPlan {
     bool enabled = false;
     bool matrix_in_smem = false;  // values in shared memory, columns from the pattern table
@@ -145,12 +151,29 @@ struct PersistArgs {
     const int2* band;
     int ownMax;
     int haloMax;
+    // Launch groups: one plan covers every row and may hold more CTAs than
+    // are co-resident; a launch runs CTAs [ctaLo, ctaHi] (blockIdx.x + ctaLo)
+    // and updates rows [row0, row1) only, whole independent instances, so no
+    // CTA waits for one outside the group (a CTA shared by two groups runs in
+    // both launches, each time for its own rows).  nphases: the phase count the
+    // host reserves per launch (epoch0 + nphases lies above every phase).
+    int ctaLo;
+    int ctaHi;
+    int row0;
+    int row1;
+    unsigned nphases;
+    // per-instance stopping (instStop != null): rows of a stopped instance
+    // are not updated; a CTA without rows to update publishes its last phase
+    // and returns (neighbour synchronisation only)
+    const int* vInst;
+    const unsigned* instStop;
 };
 
 // nullptr: no such kernel (tets need L1 gathers and at most two rows per thread)
 const void* persistent_kernel(bool correction, bool matrix_in_smem, bool band, bool l1_gather, int rows_per_thread,
                               bool tets);
 // direct form (FP32 state) and correction form (FP64 state)
+// (args.ctaLo .. args.ctaHi: the CTAs of this launch)
 cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, float>& args, cudaStream_t s);
 cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, double>& args, cudaStream_t s);
 

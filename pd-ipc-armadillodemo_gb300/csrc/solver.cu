@@ -417,6 +417,7 @@ private:
     void fill_tuning_record() {
         tuning_.pd_rows_per_thread = plan_.enabled ? plan_.rows_per_thread : 0;
         tuning_.pd_ctas = plan_.enabled ? plan_.ctas : 0;
+        tuning_.pd_launches = plan_.enabled ? (int)groups_.size() : 0;
         tuning_.pd_band = plan_.enabled && plan_.own_max > 0;
         tuning_.pd_l1_gather = plan_.enabled && plan_.l1_gather;
         tuning_.pd_local_sync = plan_.enabled && plan_.local_sync;
@@ -1393,10 +1394,8 @@ private:
         dfree(pSLen_);
         dfree(pSCol_);
         dfree(pSVal_);
-        // the persistent solve covers cloth stencils only: tet models take the per-sweep path;
-        // per-instance stopping (rows skipped per instance) runs the per-sweep path too
-        if (!std::is_same<T, float>::value || !prm_.persistent || c_.cheby >= kMaxCheby || prm_.instance_stop)
-            return PDIPC_OK;
+        groups_.clear();
+        if (!std::is_same<T, float>::value || !prm_.persistent || c_.cheby >= kMaxCheby) return PDIPC_OK;
         Dev<T, TC>& d = d_;
         const int ns = d.nsim;
         int dev = 0, nsm = 0, smem_optin = 0, coop = 0;
@@ -1512,7 +1511,36 @@ private:
             size_t sm;
             int ownMax, haloMax;
             std::vector<int2> band;
+            std::vector<PersistGroup> groups;
         };
+        // Launch groups.  A plan whose CTAs are not all co-resident (or more
+        // than params.pd_group_ctas) runs as several launches, each over whole
+        // instances (runs of rows of one simulated model, which share no
+        // matrix entry or stencil with other models): group g holds the
+        // instances whose rows lie in at most maxc consecutive CTAs.  False
+        // when one instance needs more CTAs than a launch holds.
+        std::vector<int> instEnd;  // end row of every instance, ascending
+        for (int i = 1; i <= ns; ++i)
+            if (i == ns || H.vertexModel[i] != H.vertexModel[i - 1]) instEnd.push_back(i);
+        auto form_groups = [&](int spc, int ctas, int maxc, std::vector<PersistGroup>& out) -> bool {
+            out.clear();
+            if (ctas <= maxc) {
+                out.push_back(PersistGroup{0, ctas - 1, 0, ns});
+                return true;
+            }
+            if (H.ntet > 0) return false;  // tets: one launch (a CTA projects tets of its own rows only)
+            const int rpc = spc * kSlice;  // rows of a CTA
+            size_t k = 0;
+            for (int g0 = 0; g0 < ns;) {
+                int end = g0;
+                while (k < instEnd.size() && (instEnd[k] - 1) / rpc - g0 / rpc + 1 <= maxc) end = instEnd[k++];
+                if (end == g0) return false;
+                out.push_back(PersistGroup{g0 / rpc, (end - 1) / rpc, g0, end});
+                g0 = end;
+            }
+            return true;
+        };
+        const int group_cap = prm_.pd_group_ctas > 0 ? prm_.pd_group_ctas : INT_MAX;
         std::vector<Cand> cands;
         const bool dflt_l1 = prm_.persistent != 2, dflt_ls = prm_.persistent != 3;
         for (int pass = 0; pass < 2; ++pass) {
@@ -1522,7 +1550,13 @@ private:
             for (int R = 1; R <= 4; ++R) {
                 int W = std::max(1, (nsl + nsm * R - 1) / (nsm * R));
                 if ((W * R) & 1) ++W;  // CTAs own whole windows (pairs of slices)
-                if (W > kMaxPersistWarps) continue;
+                if (W > kMaxPersistWarps) {
+                    // more rows than one launch holds: the widest CTAs that
+                    // leave a warp for the band path, in launch groups
+                    if (H.ntet > 0 || instEnd.size() < 2) continue;
+                    W = kMaxPersistWarps - 1;
+                    if ((W * R) & 1) --W;
+                }
                 const int spc = W * R;
                 const int ctas = (nsl + spc - 1) / spc;
                 const size_t sm0 = cta_smem(spc, smem_mat, 0);
@@ -1550,7 +1584,7 @@ private:
                                                (int)std::max<size_t>(c.sm, 1)));
                     int per_sm = 0;
                     PD_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, c.threads, c.sm));
-                    if (per_sm < 1 || ctas > per_sm * nsm) continue;
+                    if (per_sm < 1 || !form_groups(c.spc, c.ctas, std::min(per_sm * nsm, group_cap), c.groups)) continue;
                     cands.push_back(std::move(c));
                 }
             }
@@ -1583,6 +1617,7 @@ private:
         plan_.pattern_width = patW;
         plan_.own_max = pick->ownMax;
         plan_.halo_max = pick->haloMax;
+        groups_ = pick->groups;
         const std::vector<int2> bandRange = pick->band;
         std::vector<int> ctaSlice(plan_.ctas + 1), ctaEntry(plan_.ctas + 1);
         for (int c = 0; c <= plan_.ctas; ++c) {
@@ -1733,6 +1768,18 @@ private:
             a.ownMax = plan_.own_max;
             a.haloMax = plan_.halo_max;
             a.epoch0 = 0;
+            a.nphases = (unsigned)(c_.lg * (2 * c_.cheby + 1) + 1);
+            a.ctaLo = 0;
+            a.ctaHi = plan_.ctas - 1;
+            a.row0 = 0;
+            a.row1 = ns;
+            a.vInst = prm_.instance_stop ? d.VInst : nullptr;
+            a.instStop = prm_.instance_stop ? d.InstStop : nullptr;
+            if (prm_.instance_stop && (!a.vInst || !a.instStop)) {
+                plan_.enabled = false;
+                err = "persistent solve: unallocated instance table";
+                return PDIPC_ERR_STATE;
+            }
             const void* ptrs[] = {a.P, a.Pold, a.Xrest, a.Rhs0, a.CollRhs, a.PinRhs, a.Aq, a.GX, a.GX2, a.GY, a.Delastic,
                                   a.Dinert, a.CollDiag, a.PinFlag, a.PinK, a.lPtr, a.tOff, a.tNbr, a.tRest,
                                   a.tLbo, a.tBendT, a.tBend0, a.tLbo0, a.Strain, a.CurvNorm, a.sliceEntry, a.sliceLen, a.sCol,
@@ -1757,13 +1804,23 @@ private:
         return PDIPC_OK;
     }
 
-    cudaError_t launch_persistent() {
+    // one PD solve: a launch per group, in order on the stream; returns the launches made
+    cudaError_t launch_persistent(int* launched = nullptr) {
         if constexpr (std::is_same<T, float>::value) {
-            // fresh phase numbers for this launch: every flag from earlier launches is below them
-            pargs_.epoch0 = epoch_;
-            epoch_ += (unsigned)(c_.lg * (2 * c_.cheby + 1) + 1);
             pargs_.gate = d_.Gate;
-            return launch_pd_persistent(plan_, pargs_, s_);
+            for (const PersistGroup& g : groups_) {
+                // fresh phase numbers for this launch: every flag from earlier launches is below them
+                pargs_.epoch0 = epoch_;
+                epoch_ += pargs_.nphases;
+                pargs_.ctaLo = g.cta_lo;
+                pargs_.ctaHi = g.cta_hi;
+                pargs_.row0 = g.row0;
+                pargs_.row1 = g.row1;
+                const cudaError_t e = launch_pd_persistent(plan_, pargs_, s_);
+                if (e != cudaSuccess) return e;
+                if (launched) ++*launched;
+            }
+            return cudaSuccess;
         }
         return cudaErrorNotSupported;
     }
@@ -1956,8 +2013,9 @@ private:
 
     pdipc_status pd_solve(std::string& err) {
         if (plan_.enabled) {
-            PD_CK(launch_persistent());
-            ++launches_;
+            int n = 0;
+            PD_CK(launch_persistent(&n));
+            launches_ += n;
             return PDIPC_OK;
         }
         if (!prm_.use_graphs || taping_) {
@@ -2245,6 +2303,7 @@ private:
     std::vector<PlanChoice> plan_choices_;  // every persistent configuration that fits (default planning)
     pdipc_tuning tuning_{};
     PersistArgs<float, TC> pargs_{};
+    std::vector<PersistGroup> groups_;  // launches of one persistent PD solve
     // the matrix in SELL-32 over slots (slot_of) for the persistent solve
     int* pSOff_ = nullptr;
     int* pSLen_ = nullptr;

@@ -42,7 +42,7 @@ EXPORTS = [
 ]
 
 
-ABI_VERSION = 8  # PDIPC_ABI_VERSION of include/pdipc.h
+ABI_VERSION = 9  # PDIPC_ABI_VERSION of include/pdipc.h
 
 
 class PdipcError(RuntimeError):

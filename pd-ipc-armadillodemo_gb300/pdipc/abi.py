@@ -55,7 +55,8 @@ class Params(C.Structure):
         ("autotune", C.c_int),
         ("ccd_mode", C.c_int),
         ("instance_stop", C.c_int),
-        ("reserved", C.c_int * 2),
+        ("pd_group_ctas", C.c_int),
+        ("reserved", C.c_int * 1),
     ]
 
 
@@ -177,7 +178,7 @@ class Tuning(C.Structure):
         ("traverse_block", C.c_int32),
         ("expand_block", C.c_int32),
         ("candidates_timed", C.c_int32),
-        ("reserved0", C.c_int32),
+        ("pd_launches", C.c_int32),
         ("pd_solve_ms", C.c_double),
         ("pd_default_ms", C.c_double),
         ("collision_ms", C.c_double),

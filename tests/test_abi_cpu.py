@@ -42,7 +42,7 @@ def test_default_params_match_reference_constants(built_lib):
         if name == "reserved":
             continue
         assert getattr(p, name) == getattr(q, name), name
-    assert L.pdipc_abi_version() == pdipc.ABI_VERSION == 8
+    assert L.pdipc_abi_version() == pdipc.ABI_VERSION == 9
     assert L.pdipc_status_string(3) == b"PDIPC_ERR_OVERFLOW"
 
 

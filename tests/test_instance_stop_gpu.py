@@ -28,7 +28,7 @@ TOL = {"fp64": 1e-10, "mixed": 1e-5}
 def test_batch_with_instance_stop_equals_each_instance_alone(prec, built_lib):
     sc = scenes.batched(6, 8, 20, seed=3, steps=60)
     steps = 60  # through first contact with the spheres
-    batch = pdipc.Simulator(sc, prec, instance_stop=1)
+    batch = pdipc.Simulator(sc, prec, instance_stop=1, persistent=0)
     assert batch.stats()["pd_path"] == 0 and batch.stats()["instances"] == 6
     alone = [pdipc.Simulator(scenes.instance_slice(sc, k, k + 1), prec, persistent=0) for k in range(6)]
     contact = False
