@@ -62,6 +62,7 @@ struct PersistPlan {
     int pattern_width = 0;
     int own_max = 0;              // > 0: the CTA's column band lives in shared memory (needs local_sync)
     int halo_max = 0;
+    bool band_param = true;       // band path: offset patterns in parameter space (else per CTA in shared memory)
 };
 
 // T: solver scalar; S: state scalar (T in the direct form, double in the
@@ -125,9 +126,11 @@ struct PersistArgs {
     const T* sVal;
     const int* ctaSlice;    // first slice of each CTA (ctas + 1; even: CTAs own whole 64-row windows)
     const int* ctaEntry;    // first SELL entry of each CTA (ctas + 1)
-    const int* rowPattern;  // pattern id of every row (matrix in shared memory)
-    const int16_t* patOff;  // [patterns x pattern_width] column offsets in row order
-    int16_t patc[kParamPatterns];  // band path: the same table (patterns x pattern_width <= kParamPatterns)
+    const int* rowPattern;  // pattern id of every row in the whole table (kMode 2)
+    const int* rowPatLocal; // pattern id of every row in its CTA's table (kModes 1 and 3)
+    const int* ctaPat;      // first pattern of every CTA's table in patLocal (ctas + 1)
+    const int16_t* patLocal;  // the CTAs' tables, [patterns x pattern_width] column offsets each
+    int16_t patc[kParamPatterns];  // kMode 2: the whole table (patterns x pattern_width <= kParamPatterns)
     int patterns;
     int patW;
     // grid barrier: [0] generation, [1] arrival counter
@@ -169,9 +172,13 @@ struct PersistArgs {
     const unsigned* instStop;
 };
 
-// nullptr: no such kernel (tets need L1 gathers and at most two rows per thread)
-const void* persistent_kernel(bool correction, bool matrix_in_smem, bool band, bool l1_gather, int rows_per_thread,
-                              bool tets);
+// nullptr: no such kernel (tets need L1 gathers and at most two rows per thread;
+// the band path runs the correction form).  band_param: the band path reads the
+// offset patterns from parameter space (else each CTA's own table in shared memory).
+const void* persistent_kernel(bool correction, bool matrix_in_smem, bool band, bool band_param, bool l1_gather,
+                              int rows_per_thread, bool tets);
+// the band variants (correction form), compiled in their own translation unit
+const void* persistent_band_kernel(bool param_patterns, bool l1_gather, int rows_per_thread, bool tets);
 // direct form (FP32 state) and correction form (FP64 state)
 // (args.ctaLo .. args.ctaHi: the CTAs of this launch)
 cudaError_t launch_pd_persistent(const PersistPlan& plan, const PersistArgs<float, float>& args, cudaStream_t s);

@@ -1388,7 +1388,9 @@ private:
         dfree(pCtaSlice_);
         dfree(pCtaEntry_);
         dfree(pRowPat_);
-        dfree(pPatOff_);
+        dfree(pRowPatLoc_);
+        dfree(pCtaPat_);
+        dfree(pPatLoc_);
         dfree(pBar_);
         dfree(pSOff_);
         dfree(pSLen_);
@@ -1455,19 +1457,50 @@ private:
             for (int k = len; k < patW && len > 0; ++k) o[k] = o[len - 1];
             auto it = pats.emplace(o, (int)pats.size()).first;
             rowPat[i] = it->second;
-            if (pats.size() > 4096) fits16 = false;
+            if (pats.size() > (size_t)1 << 20) fits16 = false;
         }
-        const size_t patBytes = fits16 ? pats.size() * (size_t)patW * sizeof(int16_t) : 0;
         auto a16 = [](size_t b) { return (b + 15) / 16 * 16; };
-        // matrix values (+ the pattern table, except on the band path, which reads
-        // it from parameter space) + the band
-        auto cta_smem = [&](int spc, bool smem_mat, size_t band_bytes) -> size_t {
+        // Each CTA's own pattern table (the patterns of its rows, in order of
+        // first use): ctaPat[c] .. ctaPat[c + 1] of the concatenated tables,
+        // and every row's id in its CTA's table.  A batch of many mesh sizes
+        // has thousands of patterns, a CTA's rows a few dozen.
+        auto local_pats = [&](int spc, std::vector<int>& ctaPat, std::vector<int16_t>* table,
+                              std::vector<int>* rowLoc) {
+            const int ctas = (nsl + spc - 1) / spc;
+            ctaPat.assign(ctas + 1, 0);
+            std::vector<int> stamp(pats.size(), -1), loc(pats.size(), 0);
+            std::vector<const std::vector<int16_t>*> byId(table ? pats.size() : 0, nullptr);
+            if (table) {
+                for (auto& kv : pats) byId[kv.second] = &kv.first;
+                table->clear();
+            }
+            if (rowLoc) rowLoc->assign(ns, 0);
+            for (int c = 0; c < ctas; ++c) {
+                int n = 0;
+                for (int r = c * spc * kSlice; r < std::min(ns, (c + 1) * spc * kSlice); ++r) {
+                    const int p = rowPat[r];
+                    if (stamp[p] != c) {
+                        stamp[p] = c;
+                        loc[p] = n++;
+                        if (table) table->insert(table->end(), byId[p]->begin(), byId[p]->end());
+                    }
+                    if (rowLoc) (*rowLoc)[r] = loc[p];
+                }
+                ctaPat[c + 1] = ctaPat[c] + n;
+            }
+        };
+        // matrix values + the CTA's pattern table (unless the band path reads
+        // the whole table from parameter space) + the band
+        auto cta_smem = [&](int spc, bool smem_mat, size_t band_bytes, bool param_pats) -> size_t {
             if (!smem_mat) return 0;
+            std::vector<int> cp;
+            if (!param_pats) local_pats(spc, cp, nullptr, nullptr);
             size_t mx = 0;
             for (int c = 0; c * spc < nsl; ++c) {
                 const int s0 = c * spc, s1 = std::min(nsl, s0 + spc);
                 const size_t E = (size_t)(soff[s1] - soff[s0]);
-                mx = std::max(mx, a16(E * sizeof(T)) + (band_bytes ? 0 : a16(patBytes)) + band_bytes);
+                const size_t pb = param_pats ? 0 : a16((size_t)(cp[c + 1] - cp[c]) * patW * sizeof(int16_t));
+                mx = std::max(mx, a16(E * sizeof(T)) + pb + band_bytes);
             }
             return mx;
         };
@@ -1512,6 +1545,7 @@ private:
             int ownMax, haloMax;
             std::vector<int2> band;
             std::vector<PersistGroup> groups;
+            bool band_param = true;  // band path: the whole pattern table in parameter space
         };
         // Launch groups.  A plan whose CTAs are not all co-resident (or more
         // than params.pd_group_ctas) runs as several launches, each over whole
@@ -1559,26 +1593,29 @@ private:
                 }
                 const int spc = W * R;
                 const int ctas = (nsl + spc - 1) / spc;
-                const size_t sm0 = cta_smem(spc, smem_mat, 0);
+                const size_t sm0 = cta_smem(spc, smem_mat, 0, false);
                 if (sm0 > limit) continue;
                 std::vector<Cand> vs;
-                if (kCorrection && smem_mat && prm_.persistent == 1 && W + 1 <= kMaxPersistWarps &&
-                    pats.size() * (size_t)patW <= (size_t)kParamPatterns) {
+                if (kCorrection && smem_mat && prm_.persistent == 1 && W + 1 <= kMaxPersistWarps) {
+                    // the whole pattern table in parameter space when it fits
+                    // (uniform offsets read through the constant cache), else
+                    // each CTA's own table in shared memory
+                    const bool param = pats.size() * (size_t)patW <= (size_t)kParamPatterns;
                     std::vector<int2> rg;
                     const int hx = col_ranges(spc, rg);
                     const int om = spc * kSlice;
-                    const size_t smb =
-                        cta_smem(spc, smem_mat, a16(3 * (size_t)(om + hx) * sizeof(T)) + 16);
+                    const size_t smb = cta_smem(spc, smem_mat, a16(3 * (size_t)(om + hx) * sizeof(T)) + 16, param);
                     if (smb <= limit)
                         vs.push_back(Cand{PlanChoice{R, true, true, true}, smem_mat, spc, ctas, (W + 1) * 32, smb, om,
-                                          hx, std::move(rg)});
+                                          hx, std::move(rg), {}, param});
                 }
                 for (int v = 0; v < 4 && (v == 0 || prm_.persistent == 1); ++v) {
                     const bool l1 = (v & 1) ? !dflt_l1 : dflt_l1, ls = (v & 2) ? !dflt_ls : dflt_ls;
                     vs.push_back(Cand{PlanChoice{R, false, l1, ls}, smem_mat, spc, ctas, W * 32, sm0, 0, 0, {}});
                 }
                 for (Cand& c : vs) {
-                    const void* f = persistent_kernel(kCorrection, smem_mat, c.ch.band, c.ch.l1_gather, R, H.ntet > 0);
+                    const void* f =
+                        persistent_kernel(kCorrection, smem_mat, c.ch.band, c.band_param, c.ch.l1_gather, R, H.ntet > 0);
                     if (!f) continue;
                     PD_CK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)std::max<size_t>(c.sm, 1)));
@@ -1618,6 +1655,7 @@ private:
         plan_.own_max = pick->ownMax;
         plan_.halo_max = pick->haloMax;
         groups_ = pick->groups;
+        plan_.band_param = pick->band_param;
         const std::vector<int2> bandRange = pick->band;
         std::vector<int> ctaSlice(plan_.ctas + 1), ctaEntry(plan_.ctas + 1);
         for (int c = 0; c <= plan_.ctas; ++c) {
@@ -1694,7 +1732,15 @@ private:
         PD_CK(up(pCtaSlice_, ctaSlice));
         PD_CK(up(pCtaEntry_, ctaEntry));
         PD_CK(up(pRowPat_, rowPat));
-        PD_CK(up(pPatOff_, patOff));
+        {
+            std::vector<int> ctaPat, rowLoc;
+            std::vector<int16_t> table;
+            local_pats(plan_.slices_per_cta, ctaPat, &table, &rowLoc);
+            if (table.empty()) table.push_back(0);
+            PD_CK(up(pRowPatLoc_, rowLoc));
+            PD_CK(up(pCtaPat_, ctaPat));
+            PD_CK(up(pPatLoc_, table));
+        }
         PD_CK(zeros(pBar_, 2));
         if constexpr (std::is_same<T, float>::value) {
             PersistArgs<float, TC>& a = pargs_;
@@ -1755,9 +1801,11 @@ private:
             a.ctaSlice = pCtaSlice_;
             a.ctaEntry = pCtaEntry_;
             a.rowPattern = pRowPat_;
-            a.patOff = pPatOff_;
+            a.rowPatLocal = pRowPatLoc_;
+            a.ctaPat = pCtaPat_;
+            a.patLocal = pPatLoc_;
             std::fill(a.patc, a.patc + kParamPatterns, (int16_t)0);
-            if (plan_.own_max > 0) std::copy(patOff.begin(), patOff.end(), a.patc);
+            if (plan_.own_max > 0 && plan_.band_param) std::copy(patOff.begin(), patOff.end(), a.patc);
             a.patterns = plan_.patterns;
             a.patW = patW;
             a.bar = pBar_;
@@ -1783,7 +1831,8 @@ private:
             const void* ptrs[] = {a.P, a.Pold, a.Xrest, a.Rhs0, a.CollRhs, a.PinRhs, a.Aq, a.GX, a.GX2, a.GY, a.Delastic,
                                   a.Dinert, a.CollDiag, a.PinFlag, a.PinK, a.lPtr, a.tOff, a.tNbr, a.tRest,
                                   a.tLbo, a.tBendT, a.tBend0, a.tLbo0, a.Strain, a.CurvNorm, a.sliceEntry, a.sliceLen, a.sCol,
-                                  a.sVal, a.ctaSlice, a.ctaEntry, a.rowPattern, a.patOff, a.bar, a.err};
+                                  a.sVal, a.ctaSlice, a.ctaEntry, a.rowPattern, a.rowPatLocal, a.ctaPat, a.patLocal,
+                                  a.bar, a.err};
             if (a.ntet > 0 && (!a.Tets || !a.TetIdm || !a.TetW || !a.TetOut || !a.vtPtr || !a.vtIdx)) {
                 plan_.enabled = false;
                 err = "persistent solve: unallocated tet table";
@@ -2312,7 +2361,9 @@ private:
     int* pCtaSlice_ = nullptr;
     int* pCtaEntry_ = nullptr;
     int* pRowPat_ = nullptr;
-    int16_t* pPatOff_ = nullptr;
+    int* pRowPatLoc_ = nullptr;  // persistent plan: every row's id in its CTA's pattern table
+    int* pCtaPat_ = nullptr;
+    int16_t* pPatLoc_ = nullptr;
     unsigned* pBar_ = nullptr;
     unsigned* pFlags_ = nullptr;  // per-CTA phase counts of the neighbour synchronisation
     int2* pNbr_ = nullptr;        // per-CTA range of CTAs to wait for

@@ -19,7 +19,7 @@ INC = os.path.join(ROOT, "include")
 OUT = os.path.join(PKG, "libpdipc.so")
 OBJ = os.path.join(PKG, "_build")
 
-SOURCES = ["pd_kernels.cu", "pd_persistent.cu", "collision_kernels.cu", "penalty_kernels.cu", "primitives.cu",
+SOURCES = ["pd_kernels.cu", "pd_persistent.cu", "pd_persistent_band.cu", "collision_kernels.cu", "penalty_kernels.cu", "primitives.cu",
            "adjoint_kernels.cu", "solver.cu",
            "host_tables.cpp", "capi.cpp", "scene_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

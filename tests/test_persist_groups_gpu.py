@@ -71,7 +71,8 @@ def test_config2_all_256_instances_in_launch_groups(built_lib):
     grp = pdipc.Simulator(sc, "mixed", autotune=0, instance_stop=1)
     per = pdipc.Simulator(sc, "mixed", autotune=0, instance_stop=1, persistent=0)
     t = grp.tuning()
-    assert t["pd_rows_per_thread"] > 0 and t["pd_launches"] > 1, t
+    # more offset patterns than parameter space holds: each CTA's own table in shared memory
+    assert t["pd_rows_per_thread"] > 0 and t["pd_launches"] > 1 and t["pd_band"] == 1, t
     worst = 0.0
     for k in range(3):
         grp.step(1)
