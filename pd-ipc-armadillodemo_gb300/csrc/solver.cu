@@ -12,6 +12,8 @@
 // (1 + lg x (2 + 2 cheby - 1) kernels) is captured once as a CUDA graph and
 // replayed.
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -579,6 +581,11 @@ private:
             r = time_pd_solve(start, startH, startL, 3, &ms, err);
             if (r != PDIPC_OK) return r;
             ++tuning_.candidates_timed;
+            if (std::getenv("PDIPC_AUTOTUNE_LOG"))  // every timed PD configuration, on stderr
+                std::fprintf(stderr, "pdipc autotune: PD rows/thread %d band %d l1 %d nbr-sync %d ctas %d launches %d: %.4f ms\n",
+                             plan_.enabled ? plan_.rows_per_thread : 0, plan_.enabled && plan_.own_max > 0,
+                             plan_.enabled && plan_.l1_gather, plan_.enabled && plan_.local_sync,
+                             plan_.enabled ? plan_.ctas : 0, plan_.enabled ? (int)groups_.size() : 0, ms);
             if (k == 0) tuning_.pd_default_ms = ms;
             if (ms > 0.f && (bestMs < 0.f || ms < bestMs)) {
                 bestMs = ms;
