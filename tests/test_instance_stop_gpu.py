@@ -19,9 +19,12 @@ from pdipc.abi import PDIPC_ERR_STATE
 
 pytestmark = pytest.mark.gpu
 
-# mixed: FP32 sums and float atomics of the contact pass in another order; the
-# FP64 form pins the logic to round-off
-TOL = {"fp64": 1e-10, "mixed": 1e-5}
+# mixed: FP32 sums and float atomics of the contact pass in another order (the
+# batch's candidates interleave the instances'), compounding over the steps
+# after first contact (2.5e-5 m seen after 60 steps, with equal outer counts
+# every step); the accuracy bar of the mixed form is 1e-4 m.  The FP64 form
+# pins the logic to round-off.
+TOL = {"fp64": 1e-10, "mixed": 1e-4}
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
