@@ -27,6 +27,7 @@ start after --ref-budget-s are not run and `steps` says how many ran.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -148,9 +149,15 @@ def barrier(dist, device=None):
 
 # ---------------------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """nvidia-smi clocks and throttle reasons during the timed region.
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    nvidia-smi starts (and its NVML session comes up, which can hold up the
+    process's CUDA calls for a while) before the timed region: __enter__
+    returns once the first sample has arrived.  Only samples stamped between
+    mark_start() and mark_end() count (the one right after the region too,
+    when the region is shorter than the sampling period)."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -158,6 +165,7 @@ class ClockSampler:
         self.gpu = gpu
         self.proc = None
         self.lines: list[str] = []
+        self.t_start = self.t_end = None
 
     def __enter__(self):
         try:
@@ -166,9 +174,18 @@ class ClockSampler:
                  "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            deadline = time.time() + 10.0
+            while not self.lines and time.time() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self
+
+    def mark_start(self):
+        self.t_start = datetime.datetime.now()
+
+    def mark_end(self):
+        self.t_end = datetime.datetime.now()
 
     def _read(self):
         for line in self.proc.stdout:
@@ -182,13 +199,29 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
 
+    def _in_region(self) -> list[list[str]]:
+        rows = []
+        for ln in list(self.lines):
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 10:
+                continue
+            try:
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+            except ValueError:
+                continue
+            rows.append((ts, parts[1:]))
+        if self.t_start is None or self.t_end is None:
+            return [p for _, p in rows]
+        inside = [p for ts, p in rows if self.t_start <= ts <= self.t_end]
+        if not inside:  # a region shorter than the period: the first sample after its start
+            after = [p for ts, p in rows if ts >= self.t_start]
+            inside = after[:1]
+        return inside
+
     def summary(self) -> dict:
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
-                continue
+        for parts in self._in_region():
             try:
                 sm.append(float(parts[1]))
                 mx.append(float(parts[2]))
@@ -332,6 +365,7 @@ def run_ours(args):
     e2e_wall = time.perf_counter() - t0
     range_pop = nvtx_push("timed")           # lets a profiler select the timed launches
     with ClockSampler(local) as clk:
+        clk.mark_start()
         for _ in range(args.steps):
             flush.zero_()                    # L2 flush between timed steps (256 MB write)
             torch.cuda.synchronize()
@@ -347,6 +381,7 @@ def run_ours(args):
             ccd_ms += st["ccd_ms"]
             contact_ms += st["contact_ms"]
         torch.cuda.synchronize()
+        clk.mark_end()
     range_pop()
     barrier(dist, dev)
     dev_ms_max = max_over_ranks(dist, dev_ms, dev)

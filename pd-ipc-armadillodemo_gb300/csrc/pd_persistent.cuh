@@ -134,12 +134,12 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
 // separate steps so that a CTA can work on its own rows in between.
 //
 // nbr_publish: the caller has passed a __syncthreads() after its writes of the
-// phase; thread 0 releases the phase count (cumulative over the CTA's writes).
+// phase; thread 0 releases the phase count.  No separate fence: the CTA
+// barrier synchronises every thread's writes with thread 0, and the release
+// store at GPU scope is cumulative over what precedes it in causality order,
+// so a neighbour whose acquire load reads the count sees all of them.
 __device__ __forceinline__ void nbr_publish(unsigned* flags, int cta, unsigned epoch) {
-    if (threadIdx.x == 0) {
-        __threadfence();
-        st_release_gpu(flags + cta, epoch);
-    }
+    if (threadIdx.x == 0) st_release_gpu(flags + cta, epoch);
 }
 
 // nbr_wait: lanes of warp 0 poll one neighbour flag each until it reaches
@@ -858,10 +858,9 @@ __global__ void __launch_bounds__(kMaxPersistWarps * 32, 1) k_pd_persistent(cons
                 __syncthreads();
                 ++epoch;
                 if (syncw) {
-                    if (lane == 0) {
-                        __threadfence();
-                        st_release_gpu(a.flags + cta, epoch);
-                    }
+                    // release after the CTA barrier: cumulative over every
+                    // thread's stores of the sweep (as in nbr_publish)
+                    if (lane == 0) st_release_gpu(a.flags + cta, epoch);
                 } else {
                     write_own();
                     comp_bar();
