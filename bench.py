@@ -192,6 +192,13 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        # a region shorter than the sampling period: wait (briefly) for the
+        # first sample stamped after its start
+        deadline = time.time() + 0.6
+        while self.proc and self.t_start is not None and time.time() < deadline and self.proc.poll() is None:
+            if any(self._stamp(ln) is not None and self._stamp(ln) >= self.t_start for ln in list(self.lines)):
+                break
+            time.sleep(0.01)
         if self.proc:
             self.proc.terminate()
             try:
@@ -199,15 +206,19 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
 
+    @staticmethod
+    def _stamp(ln: str):
+        try:
+            return datetime.datetime.strptime(ln.split(",")[0].strip(), "%Y/%m/%d %H:%M:%S.%f")
+        except ValueError:
+            return None
+
     def _in_region(self) -> list[list[str]]:
         rows = []
         for ln in list(self.lines):
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 10:
-                continue
-            try:
-                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
-            except ValueError:
+            ts = self._stamp(ln)
+            if len(parts) < 10 or ts is None:
                 continue
             rows.append((ts, parts[1:]))
         if self.t_start is None or self.t_end is None:
