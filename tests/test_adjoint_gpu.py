@@ -300,3 +300,56 @@ def test_adjoint_through_strain_limits_matches_the_oracle(which, built_lib):
     ref = orc.adjoint_rollout(T, x0, v0, gx, gv)
     for name, a, b in zip(("x0", "v0"), ours[:2], ref[:2]):
         assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b), (name, np.linalg.norm(a - b), np.linalg.norm(b))
+
+
+def test_config3_central_differences_converge_to_the_adjoint(built_lib):
+    """Config 3 as specified (128x128 cloth, 50 steps, checkpoints every 10,
+    per-triangle stretch stiffness log-uniform in [1e3, 1e5], initial velocity
+    uniform +/-0.1 m/s, loss = squared distance of the final positions to the
+    initial grid displaced by +/-0.05 m), with three outer iterations per step
+    so that the rollout is smooth.  Central differences along seeded
+    directions do not converge at the specified step of 1e-4 (measured on a
+    GB300: median relative difference 0.75 for velocity directions, 0.10 for
+    relative stiffness directions): the rollout is strongly curved.  They
+    approach the adjoint as the step shrinks (velocity 0.42 at 1e-5, 0.015 at
+    1e-6; stiffness 0.005 at 1e-5), which is what is checked here."""
+    rng = np.random.default_rng(2024)
+
+    def scene(kt):
+        sc = free_cloth(128)
+        sc.cloths[0].tri_stretch = kt.copy()
+        return sc
+
+    nf = free_cloth(128).cloths[0].F.shape[0]
+    kt = 10.0 ** (3.0 + 2.0 * rng.uniform(size=nf))
+    sc = scene(kt)
+    n, T = sc.n_sim, 50
+    x0 = sc.initial_positions()
+    v0 = rng.uniform(-0.1, 0.1, (n, 3))
+    target = x0 + rng.uniform(-0.05, 0.05, x0.shape)
+    sim = make(sc, fixed_outer=3)
+
+    def L(s, vv):
+        x, _ = rollout(s, x0, vv, T)
+        return float(np.sum((x - target) ** 2))
+
+    x, _ = rollout(sim, x0, v0, T, every=10)
+    _, gv0, gk = sim.adjoint_backward(2.0 * (x - target))
+    gkt = sim.stretch_gradient_per_triangle(gk)
+
+    def v_err(eps, t):
+        d = np.random.default_rng(100 + t).uniform(-1, 1, (n, 3))
+        fd = (L(sim, v0 + eps * d) - L(sim, v0 - eps * d)) / (2 * eps)
+        return rel(fd, float(np.sum(gv0 * d)))
+
+    def k_err(eps, t):
+        d = np.random.default_rng(200 + t).uniform(-1, 1, nf)
+        lp = L(make(scene(kt * (1 + eps * d)), fixed_outer=3, autotune=0), v0)
+        lm = L(make(scene(kt * (1 - eps * d)), fixed_outer=3, autotune=0), v0)
+        return rel((lp - lm) / (2 * eps), float(np.sum(gkt * kt * d)))
+
+    v_coarse = np.median([v_err(1e-4, t) for t in range(4)])
+    v_fine = np.median([v_err(1e-6, t) for t in range(4)])
+    assert v_fine < v_coarse and v_fine < 0.05, (v_coarse, v_fine)
+    k_fine = [k_err(1e-5, t) for t in range(4)]
+    assert np.median(k_fine) < 1e-2 and max(k_fine) < 3e-2, k_fine
