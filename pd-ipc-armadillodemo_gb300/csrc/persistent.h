@@ -131,7 +131,6 @@ struct PersistArgs {
     const int* ctaPat;      // first pattern of every CTA's table in patLocal (ctas + 1)
     const int16_t* patLocal;  // the CTAs' tables, [patterns x pattern_width] column offsets each
     int16_t patc[kParamPatterns];  // kMode 2: the whole table (patterns x pattern_width <= kParamPatterns)
-    int patterns;
     int patW;
     // grid barrier: [0] generation, [1] arrival counter
     unsigned* bar;

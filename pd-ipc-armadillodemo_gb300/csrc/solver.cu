@@ -1813,7 +1813,6 @@ private:
             a.patLocal = pPatLoc_;
             std::fill(a.patc, a.patc + kParamPatterns, (int16_t)0);
             if (plan_.own_max > 0 && plan_.band_param) std::copy(patOff.begin(), patOff.end(), a.patc);
-            a.patterns = plan_.patterns;
             a.patW = patW;
             a.bar = pBar_;
             a.err = d.ErrFlags;
