@@ -42,13 +42,14 @@ def test_groups_give_the_bits_of_one_launch(stop, built_lib):
         assert one.stats()["last_outer_iters"] == grp.stats()["last_outer_iters"], k
         assert one.stats()["instance_outer_iters"] == grp.stats()["instance_outer_iters"], k
         assert np.array_equal(one.positions(), grp.positions()), k
-    # through contact (the contact pass sums in float atomics): round-off
+    # through contact the contact pass sums in float atomics, whose order varies
+    # from run to run and compounds over the steps: the mixed form's 1e-4 m bar
     worst = 0.0
     for _ in range(30):
         one.step(1)
         grp.step(1)
         worst = max(worst, float(np.abs(one.positions() - grp.positions()).max()))
-    assert worst < 1e-5, worst
+    assert worst < 1e-4, worst
     assert grp.stats()["pd_solves"] > 0
 
 
@@ -63,7 +64,7 @@ def test_instance_stop_persistent_against_per_sweep(built_lib):
         grp.step(1)
         assert per.stats()["instance_outer_iters"] == grp.stats()["instance_outer_iters"], k
         worst = max(worst, float(np.abs(per.positions() - grp.positions()).max()))
-    assert worst < 1e-5, worst
+    assert worst < 1e-4, worst
 
 
 def test_config2_all_256_instances_in_launch_groups(built_lib):
